@@ -1,0 +1,1195 @@
+// The C ABI of libgainls.so: kernel-level drop-ins, the engine that owns device memory,
+// the plain FP64 and split-precision block-pair runs, line assembly and line text.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "gain_internal.h"
+#include "split.h"
+
+namespace gain {
+
+// ------------------------------------------------------------------ errors
+namespace {
+thread_local std::string g_last_error;
+}
+
+gain_status set_error(gain_status s, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+void clear_error() { g_last_error.clear(); }
+gain_status cuda_fail(cudaError_t e, const char* what) {
+    (void)cudaGetLastError();
+    return set_error(e == cudaErrorMemoryAllocation ? GAIN_ERR_OOM : GAIN_ERR_CUDA, "%s: %s", what,
+                     cudaGetErrorString(e));
+}
+
+namespace {
+
+template <class T>
+struct DevArray {
+    T* p = nullptr;
+    size_t n = 0;
+    DevArray() = default;
+    DevArray(const DevArray&) = delete;
+    DevArray& operator=(const DevArray&) = delete;
+    DevArray(DevArray&& o) noexcept : p(o.p), n(o.n) {
+        o.p = nullptr;
+        o.n = 0;
+    }
+    DevArray& operator=(DevArray&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevArray() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    gain_status alloc(size_t count) {
+        if (p && count <= n) return GAIN_OK;
+        release();
+        if (!count) return GAIN_OK;
+        cudaError_t e = cudaMalloc((void**)&p, sizeof(T) * count);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return cuda_fail(e, "cudaMalloc");
+        }
+        n = count;
+        return GAIN_OK;
+    }
+    gain_status upload(const T* h, size_t count) {
+        GAIN_TRY(alloc(count));
+        if (count) GAIN_CUDA(cudaMemcpy(p, h, sizeof(T) * count, cudaMemcpyHostToDevice));
+        return GAIN_OK;
+    }
+    gain_status upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
+    gain_status zero(cudaStream_t st, size_t count) {
+        if (count) GAIN_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * count, st));
+        return GAIN_OK;
+    }
+};
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+struct Basis {
+    bool present = false;
+    int J = 0, dimen = 0;
+    std::vector<int> K, tau, vib, kblock, kstart;
+    DevArray<int> dK, dtau, dvib, dkblock;
+};
+
+// Per symmetry of one J: derived structures of the expansion (ideg 0).
+struct GammaMaps {
+    bool built = false;
+    std::vector<int> support;        // primitive functions the expansion touches, ascending
+    std::vector<int> sup_start;      // [J+2] support grouped by K
+    std::vector<int> csr_ptr, csr_col;   // transpose expansion: sym index -> primitives
+    std::vector<double> csr_val;
+    bool selection = false;          // every sym index is one primitive times a coefficient
+    std::vector<int> sym_prim;
+    std::vector<double> sym_coef;
+    DevArray<int> d_support, d_sup_start, d_csr_ptr, d_csr_col;
+    DevArray<double> d_csr_val;
+};
+
+struct Inflation {
+    bool present = false;
+    int dimen = 0, maxcoeff = 0, matsize = 0;
+    std::vector<int> icontr, ijterms, Ntot, sdeg;
+    std::vector<std::vector<int>> N;
+    std::vector<std::vector<double>> repres;
+    DevArray<int> dicontr, dijterms;
+    std::vector<std::unique_ptr<DevArray<int>>> dN;
+    std::vector<std::unique_ptr<DevArray<double>>> drepres;
+    std::vector<std::unique_ptr<GammaMaps>> maps;
+};
+
+struct Eig {
+    int nlevels = 0, nsize = 0;
+    DevArray<double> d;
+};
+
+struct StatsDev {
+    DevArray<int> e, nnz;
+    DevArray<float> l1, dn, inerr;
+    gain_status alloc(size_t rows, int nch, bool with_inerr) {
+        GAIN_TRY(e.alloc(rows));
+        GAIN_TRY(nnz.alloc(rows));
+        GAIN_TRY(l1.alloc(rows));
+        GAIN_TRY(dn.alloc(rows * (size_t)nch));
+        if (with_inerr) GAIN_TRY(inerr.alloc(rows));
+        return GAIN_OK;
+    }
+    gain_status zero(cudaStream_t st, size_t rows, int nch, bool with_inerr) {
+        GAIN_TRY(e.zero(st, rows));
+        GAIN_TRY(nnz.zero(st, rows));
+        GAIN_TRY(l1.zero(st, rows));
+        GAIN_TRY(dn.zero(st, rows * (size_t)nch));
+        if (with_inerr) GAIN_TRY(inerr.zero(st, rows));
+        return GAIN_OK;
+    }
+    split::RowStats view(bool with_inerr) {
+        split::RowStats r;
+        r.e = e.p;
+        r.l1 = l1.p;
+        r.nnz = nnz.p;
+        r.dn = dn.p;
+        r.inerr = with_inerr ? inerr.p : nullptr;
+        return r;
+    }
+};
+
+// Split-path layout of one block pair (lower layout padded per K block to BK, upper layout
+// padded per K block to BN so that no output tile straddles two upper K blocks).
+struct PairLayout {
+    int key[4] = {-1, -1, -1, -1};
+    long dip_version = -1;
+    int nI = 0, kpadI = 0, nF = 0, fpad = 0, W = 0;
+    std::vector<int> kpad_startI;   // [J_I + 2]
+    std::vector<int> colposI, i_sym, i_prim;
+    std::vector<double> i_coef;
+    std::vector<int> colposF, f_sym, f_prim, band_k0, band_len;
+    std::vector<double> f_coef;
+    std::vector<std::pair<int, int>> fblocks;   // padded [start, end) of each upper K block
+    DevArray<int> d_colposI, d_i_sym, d_i_prim, d_colposF, d_f_prim, d_band_k0, d_band_len;
+    DevArray<double> d_i_coef, d_f_coef, band;
+    int beta1 = 0, s1 = 0;
+    DevArray<__nv_bfloat16> bandDig;
+    StatsDev bandStats;
+    CUtensorMap tmBand;
+};
+
+// Plain-path structures of one block pair.
+struct PlainLayout {
+    int key[4] = {-1, -1, -1, -1};
+    std::vector<HlsCta> ctas;
+    DevArray<HlsCta> d_ctas;
+    DevArray<int> d_flist;
+};
+
+}  // namespace
+}  // namespace gain
+
+struct gain_engine_s {
+    int device = 0;
+    int jmax = 0, nsym = 0, maxdeg = 0;
+    int num_sms = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6] = {};
+    gain::DevArray<double> d3j;
+    std::vector<gain::Basis> bases;
+    std::vector<gain::Inflation> infl;
+    gain::DevArray<double> dipole;
+    int dipN = 0, startF = 0, endF = 0, ncontrF = 0;
+    bool dip_present = false;
+    long dip_version = 0;
+    std::map<std::pair<int, int>, std::unique_ptr<gain::Eig>> eig;
+
+    // last run
+    gain::DevArray<double> amp;
+    int amp_rows = 0, amp_cols = 0;
+    long amp_ld = 0;
+    bool have_amp = false;
+
+    // work buffers
+    gain::DevArray<int> d_lower, d_upper;
+    gain::DevArray<double> primI, hprim, hsym;
+    gain::DevArray<__nv_bfloat16> Vdig, Hdig, Udig;
+    gain::StatsDev Vst, Hst, Ust;
+    gain::DevArray<double> H;
+    gain::DevArray<float> rowerr;
+    gain::DevArray<int2> flags1, flags2;
+    gain::DevArray<unsigned int> counters;      // [0] nflags1 [1] nflags2
+    gain::DevArray<unsigned long long> ull;     // [0] uncertified [1] nkeep
+    gain::DevArray<int> err;
+    gain::DevArray<gain::split::Tile> tiles1, tiles2;
+    gain::DevArray<gain::split::Prod> prods1, prods2;
+    gain::DevArray<double> lineS, lineA, lineI, eIdev, eFdev;
+    gain::DevArray<unsigned char> lineKeep;
+
+    gain::PairLayout layout;
+    gain::PlainLayout plain;
+};
+
+namespace gain {
+namespace {
+
+constexpr int kMaxFlags = 1 << 22;
+
+gain_status check_engine(gain_engine e) {
+    if (!e) return set_error(GAIN_ERR_INVALID_ARG, "engine is NULL");
+    GAIN_CUDA(cudaSetDevice(e->device));
+    return GAIN_OK;
+}
+
+GammaMaps* gamma_maps(gain_engine e, int jind, int g) {
+    Basis& b = e->bases[jind];
+    Inflation& inf = e->infl[jind];
+    GammaMaps& m = *inf.maps[g];
+    if (m.built) return &m;
+    const int d = inf.dimen;
+    const int Ntot = inf.Ntot[g], sdeg = inf.sdeg[g];
+    m.support.clear();
+    m.sup_start.assign(b.J + 2, 0);
+    std::vector<std::vector<std::pair<int, double>>> rows(Ntot);
+    bool sel = true;
+    for (int r = 0; r < d; ++r) {
+        const int irow = inf.icontr[r], ib = inf.icontr[r + d];
+        const int nel = inf.N[g][irow];
+        if (nel <= 0) continue;
+        m.support.push_back(r);
+        if (nel != 1) sel = false;
+        const int iterm = inf.ijterms[irow + g * inf.maxcoeff];
+        for (int i = 0; i < nel; ++i) {
+            const int s = iterm + i;
+            const double coef = inf.repres[g][(size_t)s + (size_t)ib * sdeg * Ntot];
+            rows[s].push_back({r, coef});
+        }
+    }
+    for (int r : m.support) m.sup_start[b.K[r] + 1]++;
+    for (int k = 0; k <= b.J; ++k) m.sup_start[k + 1] += m.sup_start[k];
+    m.csr_ptr.assign(Ntot + 1, 0);
+    m.csr_col.clear();
+    m.csr_val.clear();
+    m.sym_prim.assign(Ntot, -1);
+    m.sym_coef.assign(Ntot, 0.0);
+    for (int s = 0; s < Ntot; ++s) {
+        std::sort(rows[s].begin(), rows[s].end());
+        for (auto& pr : rows[s]) {
+            m.csr_col.push_back(pr.first);
+            m.csr_val.push_back(pr.second);
+        }
+        m.csr_ptr[s + 1] = (int)m.csr_col.size();
+        if (rows[s].size() == 1) {
+            m.sym_prim[s] = rows[s][0].first;
+            m.sym_coef[s] = rows[s][0].second;
+        } else {
+            sel = false;
+        }
+    }
+    m.selection = sel;
+    if (m.d_support.upload(m.support) || m.d_sup_start.upload(m.sup_start) ||
+        m.d_csr_ptr.upload(m.csr_ptr) || m.d_csr_col.upload(m.csr_col) || m.d_csr_val.upload(m.csr_val))
+        return nullptr;
+    m.built = true;
+    return &m;
+}
+
+gain_status validate_job(gain_engine e, const gain_pair_job* j) {
+    if (!j) return set_error(GAIN_ERR_INVALID_ARG, "job is NULL");
+    const int nj = (int)e->bases.size();
+    if (j->jindI < 0 || j->jindI >= nj || j->jindF < 0 || j->jindF >= nj)
+        return set_error(GAIN_ERR_INVALID_ARG, "jind out of range");
+    if (!e->bases[j->jindI].present || !e->bases[j->jindF].present)
+        return set_error(GAIN_ERR_NOT_READY, "basis set of jind %d/%d not uploaded", j->jindI, j->jindF);
+    if (!e->infl[j->jindI].present || !e->infl[j->jindF].present)
+        return set_error(GAIN_ERR_NOT_READY, "expansion tables not uploaded");
+    if (!e->dip_present) return set_error(GAIN_ERR_NOT_READY, "dipole not uploaded");
+    if (j->gammaI < 0 || j->gammaI >= e->nsym || j->gammaF < 0 || j->gammaF >= e->nsym)
+        return set_error(GAIN_ERR_INVALID_ARG, "gamma out of range");
+    const int JI = e->bases[j->jindI].J, JF = e->bases[j->jindF].J;
+    if (std::abs(JI - JF) > 1) return set_error(GAIN_ERR_INVALID_ARG, "|J' - J''| > 1");
+    if (JI > e->jmax || JF > e->jmax) return set_error(GAIN_ERR_INVALID_ARG, "J above jmax");
+    auto itI = e->eig.find({j->jindI, j->gammaI});
+    auto itF = e->eig.find({j->jindF, j->gammaF});
+    if (itI == e->eig.end() || itF == e->eig.end())
+        return set_error(GAIN_ERR_NOT_READY, "eigenvectors of the pair not uploaded");
+    if (j->nlower <= 0 || j->nupper <= 0 || !j->lower_levels || !j->upper_levels)
+        return set_error(GAIN_ERR_INVALID_ARG, "empty level lists");
+    for (int i = 0; i < j->nlower; ++i)
+        if (j->lower_levels[i] < 0 || j->lower_levels[i] >= itI->second->nlevels)
+            return set_error(GAIN_ERR_INVALID_ARG, "lower level %d out of range", j->lower_levels[i]);
+    for (int i = 0; i < j->nupper; ++i)
+        if (j->upper_levels[i] < 0 || j->upper_levels[i] >= itF->second->nlevels)
+            return set_error(GAIN_ERR_INVALID_ARG, "upper level %d out of range", j->upper_levels[i]);
+    if (itI->second->nsize != e->infl[j->jindI].Ntot[j->gammaI] ||
+        itF->second->nsize != e->infl[j->jindF].Ntot[j->gammaF])
+        return set_error(GAIN_ERR_INVALID_ARG, "eigenvector length differs from the symmetry block size");
+    return GAIN_OK;
+}
+
+// ------------------------------------------------------------------ plain FP64 path
+gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) {
+    Basis& bI = e->bases[j->jindI];
+    Basis& bF = e->bases[j->jindF];
+    Inflation& iI = e->infl[j->jindI];
+    Inflation& iF = e->infl[j->jindF];
+    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI);
+    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF);
+    if (!mI || !mF) return GAIN_ERR_OOM;
+    PlainLayout& L = e->plain;
+    const int key[4] = {j->jindI, j->gammaI, j->jindF, j->gammaF};
+    if (!std::equal(key, key + 4, L.key)) {
+        L.ctas.clear();
+        std::vector<int> flist;
+        for (int k = 0; k <= bF.J; ++k) {
+            const int s0 = mF->sup_start[k], s1 = mF->sup_start[k + 1];
+            for (int b = s0; b < s1; b += kHlsTile) {
+                HlsCta c;
+                c.kF = k;
+                c.f_begin = b;
+                c.f_count = std::min(kHlsTile, s1 - b);
+                c.pad = 0;
+                L.ctas.push_back(c);
+            }
+        }
+        GAIN_TRY(L.d_ctas.upload(L.ctas));
+        std::copy(key, key + 4, L.key);
+    }
+    const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+    const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+    GAIN_TRY(e->d_lower.upload(j->lower_levels, j->nlower));
+    GAIN_TRY(e->d_upper.upload(j->upper_levels, j->nupper));
+    GAIN_TRY(e->primI.alloc(bI.dimen));
+    GAIN_TRY(e->hprim.alloc(bF.dimen));
+    GAIN_TRY(e->hsym.alloc(iF.Ntot[j->gammaF]));
+    GAIN_TRY(e->amp.alloc((size_t)j->nlower * j->nupper));
+    cudaStream_t st = e->st;
+    GAIN_CUDA(cudaEventRecord(e->ev[0], st));
+    int launches = 0;
+    for (int l = 0; l < j->nlower; ++l) {
+        const double* vrow = EI.d.p + (size_t)j->lower_levels[l] * EI.nsize;
+        GAIN_CUDA(launch_expand(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
+                                iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
+                                vrow, e->primI.p, st));
+        GAIN_CUDA(launch_hls_needed(L.d_ctas.p, (int)L.ctas.size(), mF->d_support.p, bI.J, bF.J, bI.dtau.p,
+                                    bF.dtau.p, bI.dvib.p, bF.dvib.p, mI->d_support.p, mI->d_sup_start.p,
+                                    e->startF, e->endF, e->ncontrF, e->dipole.p, e->dipN, e->primI.p,
+                                    e->d3j.p, e->jmax, e->hprim.p, st));
+        GAIN_CUDA(launch_contract(iF.Ntot[j->gammaF], mF->d_csr_ptr.p, mF->d_csr_col.p, mF->d_csr_val.p,
+                                  e->hprim.p, e->hsym.p, st));
+        GAIN_CUDA(launch_gemv_rows(j->nupper, EF.nsize, EF.d.p, EF.nsize, e->d_upper.p, e->hsym.p,
+                                   e->amp.p + (size_t)l * j->nupper, st));
+        launches += 4;
+    }
+    GAIN_CUDA(cudaEventRecord(e->ev[1], st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    GAIN_CUDA(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
+    e->amp_rows = j->nlower;
+    e->amp_cols = j->nupper;
+    e->amp_ld = j->nupper;
+    e->have_amp = true;
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        stats->device_ms = ms;
+        stats->rows = j->nlower;
+        stats->cols = j->nupper;
+        stats->kernel_launches = launches;
+    }
+    return GAIN_OK;
+}
+
+// ------------------------------------------------------------------ split path
+struct SplitParams {
+    int beta, slices, chunks;
+};
+
+// Digits and chunking from the inner length K of the exact accumulations: the Cauchy-Schwarz
+// certificate needs ||d_i|| ||d_j|| < 2^24 over every chunk; balanced residual digits have
+// ||d||^2 ~ K 4^beta / 12, so K_chunk 4^beta / 12 <= 2^23 leaves a factor-two margin.
+SplitParams choose_params(int K, const gain_split_opts* o) {
+    SplitParams p;
+    p.beta = (o && o->beta) ? o->beta : 7;
+    p.slices = (o && o->slices) ? o->slices : (49 + p.beta - 1) / p.beta;
+    if (o && o->kchunks) {
+        p.chunks = o->kchunks;
+    } else {
+        const double limit = 8388608.0 * 12.0 / std::ldexp(1.0, 2 * p.beta);
+        p.chunks = std::max(1, (int)std::ceil((double)K / limit));
+    }
+    p.chunks = std::min(p.chunks, split::MAX_CHUNKS);
+    return p;
+}
+
+void bound_consts(const SplitParams& p, int nprods, float* c_l1, float* c_nnz, float* c_rec) {
+    const double rho = 1.0 / (1.0 - std::ldexp(1.0, -p.beta));
+    const double q = (double)p.slices * p.beta;
+    const double h = std::ldexp(1.0, -(int)q - 1);
+    *c_l1 = (float)(h * (1.0 + rho) * 1.001);
+    *c_nnz = (float)(h * (rho * (p.slices - 1) / 2.0 + 2.0 * rho * std::ldexp(1.0, -p.beta)) * 1.001);
+    *c_rec = (float)(((double)nprods * std::ldexp(1.0, -46) + std::ldexp(1.0, -52)) * rho * rho * 1.1);
+}
+
+std::vector<split::Prod> make_prods(const SplitParams& p) {
+    std::vector<split::Prod> v;
+    for (int t = 0; t < p.slices; ++t)
+        for (int i = 0; i <= t; ++i)
+            for (int c = 0; c < p.chunks; ++c) v.push_back({i, t - i, t, c});
+    return v;
+}
+
+gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, GammaMaps* mF) {
+    PairLayout& L = e->layout;
+    const int key[4] = {j->jindI, j->gammaI, j->jindF, j->gammaF};
+    if (std::equal(key, key + 4, L.key) && L.dip_version == e->dip_version) return GAIN_OK;
+    Basis& bI = e->bases[j->jindI];
+    Basis& bF = e->bases[j->jindF];
+    L.nI = (int)mI->sym_prim.size();
+    L.nF = (int)mF->sym_prim.size();
+    // lower layout: symmetry functions grouped by K, each group padded to BK
+    std::vector<std::vector<int>> byK(bI.J + 1);
+    for (int s = 0; s < L.nI; ++s) byK[bI.K[mI->sym_prim[s]]].push_back(s);
+    L.kpad_startI.assign(bI.J + 2, 0);
+    for (int k = 0; k <= bI.J; ++k) L.kpad_startI[k + 1] = L.kpad_startI[k] + round_up((int)byK[k].size(), split::BK);
+    L.kpadI = std::max(L.kpad_startI[bI.J + 1], split::BK);
+    L.colposI.assign(L.nI, 0);
+    L.i_sym.assign(L.kpadI, -1);
+    L.i_prim.assign(L.kpadI, -1);
+    L.i_coef.assign(L.kpadI, 0.0);
+    for (int k = 0; k <= bI.J; ++k)
+        for (size_t x = 0; x < byK[k].size(); ++x) {
+            const int s = byK[k][x], pos = L.kpad_startI[k] + (int)x;
+            L.colposI[s] = pos;
+            L.i_sym[pos] = s;
+            L.i_prim[pos] = mI->sym_prim[s];
+            L.i_coef[pos] = mI->sym_coef[s];
+        }
+    // upper layout: grouped by K, each group padded to BN
+    std::vector<std::vector<int>> byKF(bF.J + 1);
+    for (int s = 0; s < L.nF; ++s) byKF[bF.K[mF->sym_prim[s]]].push_back(s);
+    L.fblocks.clear();
+    int pos = 0;
+    L.colposF.assign(L.nF, 0);
+    std::vector<int> f_k;
+    for (int k = 0; k <= bF.J; ++k) {
+        const int n = (int)byKF[k].size();
+        if (!n) continue;
+        const int np = round_up(n, split::BN);
+        L.fblocks.push_back({pos, pos + np});
+        for (int x = 0; x < np; ++x) f_k.push_back(k);
+        pos += np;
+    }
+    L.fpad = std::max(pos, split::BN);
+    if (f_k.empty()) f_k.assign(L.fpad, 0);
+    L.f_sym.assign(L.fpad, -1);
+    L.f_prim.assign(L.fpad, -1);
+    L.f_coef.assign(L.fpad, 0.0);
+    L.band_k0.assign(L.fpad, 0);
+    L.band_len.assign(L.fpad, 0);
+    {
+        int p2 = 0;
+        for (int k = 0; k <= bF.J; ++k) {
+            const int n = (int)byKF[k].size();
+            if (!n) continue;
+            for (int x = 0; x < n; ++x) {
+                const int s = byKF[k][x];
+                L.colposF[s] = p2 + x;
+                L.f_sym[p2 + x] = s;
+                L.f_prim[p2 + x] = mF->sym_prim[s];
+                L.f_coef[p2 + x] = mF->sym_coef[s];
+            }
+            p2 += round_up(n, split::BN);
+        }
+    }
+    L.W = split::BK;
+    for (int r = 0; r < L.fpad; ++r) {
+        const int kF = f_k[r];
+        const int klo = std::max(kF - 1, 0), khi = std::min(kF + 1, bI.J);
+        if (klo > khi) continue;
+        L.band_k0[r] = L.kpad_startI[klo];
+        L.band_len[r] = L.kpad_startI[khi + 1] - L.kpad_startI[klo];
+        L.W = std::max(L.W, L.band_len[r]);
+    }
+    GAIN_TRY(L.d_colposI.upload(L.colposI));
+    GAIN_TRY(L.d_i_sym.upload(L.i_sym));
+    GAIN_TRY(L.d_i_prim.upload(L.i_prim));
+    GAIN_TRY(L.d_i_coef.upload(L.i_coef));
+    GAIN_TRY(L.d_colposF.upload(L.colposF));
+    GAIN_TRY(L.d_f_prim.upload(L.f_prim));
+    GAIN_TRY(L.d_f_coef.upload(L.f_coef));
+    GAIN_TRY(L.d_band_k0.upload(L.band_k0));
+    GAIN_TRY(L.d_band_len.upload(L.band_len));
+    GAIN_TRY(L.band.alloc((size_t)L.fpad * L.W));
+    split::BandArgs ba;
+    ba.fpad = L.fpad;
+    ba.W = L.W;
+    ba.f_prim = L.d_f_prim.p;
+    ba.f_coef = L.d_f_coef.p;
+    ba.band_k0 = L.d_band_k0.p;
+    ba.kpadI = L.kpadI;
+    ba.i_prim = L.d_i_prim.p;
+    ba.i_coef = L.d_i_coef.p;
+    ba.KI = bI.dK.p;
+    ba.tauI = bI.dtau.p;
+    ba.vibI = bI.dvib.p;
+    ba.KF = bF.dK.p;
+    ba.tauF = bF.dtau.p;
+    ba.vibF = bF.dvib.p;
+    ba.jI = bI.J;
+    ba.jF = bF.J;
+    ba.jmax = e->jmax;
+    ba.threej = e->d3j.p;
+    ba.dipole = e->dipole.p;
+    ba.dipN = e->dipN;
+    ba.startF = e->startF;
+    ba.endF = e->endF;
+    ba.ncontrF = e->ncontrF;
+    ba.band = L.band.p;
+    GAIN_CUDA(split::launch_band(ba, e->st));
+    L.beta1 = 0;
+    L.s1 = 0;
+    std::copy(key, key + 4, L.key);
+    L.dip_version = e->dip_version;
+    return GAIN_OK;
+}
+
+gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows, int nrows, int ncols,
+                  const int* col_map, int kpad, int rows_pad, __nv_bfloat16* dig, const SplitParams& p,
+                  int nkb_total, StatsDev& stv, bool with_inerr, const float* inerr_prev,
+                  const int* e_prev) {
+    split::SliceArgs a;
+    a.src = src;
+    a.ld_src = ld;
+    a.src_rows = src_rows;
+    a.nrows = nrows;
+    a.ncols = ncols;
+    a.col_map = col_map;
+    a.kpad = kpad;
+    a.slice_stride = (long)rows_pad * kpad;
+    a.digits = dig;
+    a.slices = p.slices;
+    a.beta = p.beta;
+    a.nchunks = p.chunks;
+    a.nkb_total = nkb_total;
+    a.st = stv.view(with_inerr);
+    a.inerr_prev = inerr_prev;
+    a.e_prev = e_prev;
+    GAIN_CUDA(split::launch_slice(a, e->st));
+    return GAIN_OK;
+}
+
+gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_opts* opts, gain_stats* stats) {
+    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI);
+    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF);
+    if (!mI || !mF) return GAIN_ERR_OOM;
+    if (!mI->selection || !mF->selection)
+        return set_error(GAIN_ERR_UNSUPPORTED,
+                         "split path needs symmetry blocks whose expansion selects one primitive per function");
+    if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "split path handles non-degenerate symmetries only");
+    const double tol = (opts && opts->tol > 0) ? opts->tol : 2e-9;
+    cudaStream_t st = e->st;
+    GAIN_CUDA(cudaEventRecord(e->ev[0], st));
+    GAIN_TRY(build_layout(e, j, mI, mF));
+    PairLayout& L = e->layout;
+    const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+    const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+
+    const SplitParams p1 = choose_params(L.W, opts);
+    SplitParams p1x = p1;
+    p1x.chunks = 1;   // band tiles have their own k ranges: one chunk, certified per row
+    if (p1.chunks > 1 && !(opts && opts->kchunks)) {
+        // shrink digits of the first GEMM until one chunk suffices
+        while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
+            --p1x.beta;
+            p1x.slices = (49 + p1x.beta - 1) / p1x.beta;
+        }
+    }
+    const SplitParams p2 = choose_params(L.fpad, opts);
+    if (p1x.slices * p1x.beta > 62 || p2.slices * p2.beta > 62 || p1x.slices > split::MAX_SLICES ||
+        p2.slices > split::MAX_SLICES || p1x.beta < 2 || p1x.beta > 8 || p2.beta < 2 || p2.beta > 8 ||
+        2 * (p2.slices - 1) * p2.beta > 126 || 2 * (p1x.slices - 1) * p1x.beta > 126)
+        return set_error(GAIN_ERR_INVALID_ARG, "unsupported digit configuration");
+
+    // band digits (cached per digit configuration)
+    if (L.beta1 != p1x.beta || L.s1 != p1x.slices) {
+        GAIN_TRY(L.bandDig.alloc((size_t)p1x.slices * L.fpad * L.W));
+        GAIN_TRY(L.bandDig.zero(st, (size_t)p1x.slices * L.fpad * L.W));
+        GAIN_TRY(L.bandStats.alloc(L.fpad, 1, false));
+        GAIN_TRY(L.bandStats.zero(st, L.fpad, 1, false));
+        GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, L.W, L.fpad, L.bandDig.p, p1x,
+                       L.W / split::BK, L.bandStats, false, nullptr, nullptr));
+        if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1x.slices))
+            return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed for the band digits");
+        L.beta1 = p1x.beta;
+        L.s1 = p1x.slices;
+    }
+
+    const int B = j->nlower, Bpad = round_up(B, split::BM);
+    const int Nu = j->nupper, Nupad = round_up(Nu, split::BN);
+    GAIN_TRY(e->d_lower.upload(j->lower_levels, B));
+    GAIN_TRY(e->d_upper.upload(j->upper_levels, Nu));
+    GAIN_TRY(e->counters.alloc(4));
+    GAIN_TRY(e->counters.zero(st, 4));
+    GAIN_TRY(e->ull.alloc(4));
+    GAIN_TRY(e->ull.zero(st, 4));
+    GAIN_TRY(e->err.alloc(1));
+    GAIN_TRY(e->err.zero(st, 1));
+    GAIN_TRY(e->flags1.alloc(kMaxFlags));
+    GAIN_TRY(e->flags2.alloc(kMaxFlags));
+
+    // ---- lower vectors -> digits in the padded lower layout
+    const size_t vdig = (size_t)p1x.slices * Bpad * L.kpadI;
+    GAIN_TRY(e->Vdig.alloc(vdig));
+    GAIN_TRY(e->Vdig.zero(st, vdig));
+    GAIN_TRY(e->Vst.alloc(Bpad, 1, false));
+    GAIN_TRY(e->Vst.zero(st, Bpad, 1, false));
+    GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, L.kpadI, Bpad, e->Vdig.p,
+                   p1x, L.kpadI / split::BK, e->Vst, false, nullptr, nullptr));
+    CUtensorMap tmV, tmH, tmU;
+    if (!split::make_digit_map(&tmV, e->Vdig.p, L.kpadI, Bpad, p1x.slices))
+        return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (lower digits)");
+
+    // ---- GEMM 1: H = V M
+    std::vector<split::Tile> t1;
+    for (auto& fb : L.fblocks)
+        for (int n0 = fb.first; n0 < fb.second; n0 += split::BN)
+            for (int m0 = 0; m0 < Bpad; m0 += split::BM) {
+                split::Tile t;
+                memset(&t, 0, sizeof t);
+                t.m0 = m0;
+                t.n0 = n0;
+                t.a_k0 = L.band_k0[n0];
+                t.b_k0 = 0;
+                t.nkb = L.band_len[n0] / split::BK;
+                t1.push_back(t);
+            }
+    const std::vector<split::Prod> pr1 = make_prods(p1x);
+    GAIN_TRY(e->tiles1.upload(t1));
+    GAIN_TRY(e->prods1.upload(pr1));
+    GAIN_TRY(e->H.alloc((size_t)Bpad * L.fpad));
+    GAIN_TRY(e->rowerr.alloc(Bpad));
+    GAIN_TRY(e->rowerr.zero(st, Bpad));
+    split::GemmArgs g1;
+    memset(&g1, 0, sizeof g1);
+    g1.tiles = e->tiles1.p;
+    g1.ntiles = (int)t1.size();
+    g1.prods = e->prods1.p;
+    g1.nprods = (int)pr1.size();
+    g1.nchunks = 1;
+    g1.beta = p1x.beta;
+    g1.slices = p1x.slices;
+    g1.out = e->H.p;
+    g1.ldo = L.fpad;
+    g1.A = e->Vst.view(false);
+    g1.B = L.bandStats.view(false);
+    bound_consts(p1x, (int)pr1.size(), &g1.c_l1, &g1.c_nnz, &g1.c_rec);
+    g1.rowerr_units = e->rowerr.p;
+    g1.flag_mode = 0;
+    g1.tol = (float)tol;
+    g1.flags = e->flags1.p;
+    g1.nflags = e->counters.p + 0;
+    g1.max_flags = kMaxFlags;
+    g1.rows_valid = B;
+    g1.cols_valid = L.fpad;
+    g1.err = e->err.p;
+    GAIN_CUDA(cudaEventRecord(e->ev[2], st));
+    GAIN_CUDA(split::launch_gemm(tmV, L.tmBand, g1, e->num_sms, st));
+    GAIN_CUDA(cudaEventRecord(e->ev[3], st));
+    // inexact first-GEMM entries recomputed in FP64
+    split::RefineHArgs rh;
+    rh.flags = e->flags1.p;
+    rh.nflags = e->counters.p + 0;
+    rh.max_flags = kMaxFlags;
+    rh.vecs = EI.d.p;
+    rh.nsize = EI.nsize;
+    rh.row_level = e->d_lower.p;
+    rh.i_sym = L.d_i_sym.p;
+    rh.band_k0 = L.d_band_k0.p;
+    rh.band_len = L.d_band_len.p;
+    rh.band = L.band.p;
+    rh.W = L.W;
+    rh.H = e->H.p;
+    rh.ldh = L.fpad;
+    rh.eA = e->Vst.e.p;
+    rh.rowerr_units = e->rowerr.p;
+    GAIN_CUDA(split::launch_refine_h(rh, 2 * e->num_sms, st));
+
+    // ---- H -> digits, upper vectors -> digits
+    const size_t hdig = (size_t)p2.slices * Bpad * L.fpad;
+    GAIN_TRY(e->Hdig.alloc(hdig));
+    GAIN_TRY(e->Hdig.zero(st, hdig));
+    GAIN_TRY(e->Hst.alloc(Bpad, p2.chunks, true));
+    GAIN_TRY(e->Hst.zero(st, Bpad, p2.chunks, true));
+    GAIN_TRY(slice(e, e->H.p, L.fpad, nullptr, B, L.fpad, nullptr, L.fpad, Bpad, e->Hdig.p, p2,
+                   L.fpad / split::BK, e->Hst, true, e->rowerr.p, e->Vst.e.p));
+    const size_t udig = (size_t)p2.slices * Nupad * L.fpad;
+    GAIN_TRY(e->Udig.alloc(udig));
+    GAIN_TRY(e->Udig.zero(st, udig));
+    GAIN_TRY(e->Ust.alloc(Nupad, p2.chunks, false));
+    GAIN_TRY(e->Ust.zero(st, Nupad, p2.chunks, false));
+    GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, L.fpad, Nupad, e->Udig.p,
+                   p2, L.fpad / split::BK, e->Ust, false, nullptr, nullptr));
+    if (!split::make_digit_map(&tmH, e->Hdig.p, L.fpad, Bpad, p2.slices) ||
+        !split::make_digit_map(&tmU, e->Udig.p, L.fpad, Nupad, p2.slices))
+        return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (second GEMM digits)");
+
+    // ---- GEMM 2: amp = H U^T
+    std::vector<split::Tile> t2;
+    for (int n0 = 0; n0 < Nupad; n0 += split::BN)
+        for (int m0 = 0; m0 < Bpad; m0 += split::BM) {
+            split::Tile t;
+            memset(&t, 0, sizeof t);
+            t.m0 = m0;
+            t.n0 = n0;
+            t.a_k0 = 0;
+            t.b_k0 = 0;
+            t.nkb = L.fpad / split::BK;
+            t2.push_back(t);
+        }
+    const std::vector<split::Prod> pr2 = make_prods(p2);
+    GAIN_TRY(e->tiles2.upload(t2));
+    GAIN_TRY(e->prods2.upload(pr2));
+    GAIN_TRY(e->amp.alloc((size_t)Bpad * Nupad));
+    split::GemmArgs g2;
+    memset(&g2, 0, sizeof g2);
+    g2.tiles = e->tiles2.p;
+    g2.ntiles = (int)t2.size();
+    g2.prods = e->prods2.p;
+    g2.nprods = (int)pr2.size();
+    g2.nchunks = p2.chunks;
+    g2.beta = p2.beta;
+    g2.slices = p2.slices;
+    g2.out = e->amp.p;
+    g2.ldo = Nupad;
+    g2.A = e->Hst.view(true);
+    g2.B = e->Ust.view(false);
+    bound_consts(p2, (int)pr2.size(), &g2.c_l1, &g2.c_nnz, &g2.c_rec);
+    g2.rowerr_units = nullptr;
+    g2.flag_mode = 1;
+    g2.tol = (float)tol;
+    g2.flags = e->flags2.p;
+    g2.nflags = e->counters.p + 1;
+    g2.max_flags = kMaxFlags;
+    g2.rows_valid = B;
+    g2.cols_valid = Nu;
+    g2.err = e->err.p;
+    GAIN_CUDA(cudaEventRecord(e->ev[4], st));
+    GAIN_CUDA(split::launch_gemm(tmH, tmU, g2, e->num_sms, st));
+    GAIN_CUDA(cudaEventRecord(e->ev[5], st));
+    split::RefineAmpArgs ra;
+    ra.flags = e->flags2.p;
+    ra.nflags = e->counters.p + 1;
+    ra.max_flags = kMaxFlags;
+    ra.U = EF.d.p;
+    ra.nsize = EF.nsize;
+    ra.col_level = e->d_upper.p;
+    ra.colpos = L.d_colposF.p;
+    ra.H = e->H.p;
+    ra.ldh = L.fpad;
+    ra.h_inerr = e->Hst.inerr.p;
+    ra.eH = e->Hst.e.p;
+    ra.amp = e->amp.p;
+    ra.lda = Nupad;
+    ra.tol = tol;
+    ra.uncertified = e->ull.p;
+    GAIN_CUDA(split::launch_refine_amp(ra, 4 * e->num_sms, st));
+    GAIN_CUDA(cudaEventRecord(e->ev[1], st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+
+    unsigned int cnt[4];
+    unsigned long long unc[4];
+    int errw = 0;
+    GAIN_CUDA(cudaMemcpy(cnt, e->counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
+    GAIN_CUDA(cudaMemcpy(unc, e->ull.p, sizeof unc, cudaMemcpyDeviceToHost));
+    GAIN_CUDA(cudaMemcpy(&errw, e->err.p, sizeof errw, cudaMemcpyDeviceToHost));
+    e->amp_rows = B;
+    e->amp_cols = Nu;
+    e->amp_ld = Nupad;
+    e->have_amp = errw == 0;
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        float ms = 0.f, g1ms = 0.f, g2ms = 0.f;
+        cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
+        cudaEventElapsedTime(&g1ms, e->ev[2], e->ev[3]);
+        cudaEventElapsedTime(&g2ms, e->ev[4], e->ev[5]);
+        stats->device_ms = ms;
+        stats->gemm1_ms = g1ms;
+        stats->gemm2_ms = g2ms;
+        stats->rows = B;
+        stats->cols = Nu;
+        stats->refined = (long long)std::min<unsigned>(cnt[1], kMaxFlags) + std::min<unsigned>(cnt[0], kMaxFlags);
+        stats->uncertified = (long long)unc[0];
+        stats->inexact = (long long)cnt[0];
+        stats->beta1 = p1x.beta;
+        stats->slices1 = p1x.slices;
+        stats->chunks1 = 1;
+        stats->beta2 = p2.beta;
+        stats->slices2 = p2.slices;
+        stats->chunks2 = p2.chunks;
+        stats->products1 = (int)pr1.size();
+        stats->products2 = (int)pr2.size();
+        stats->kernel_launches = 10;
+        double f = 0;
+        for (auto& t : t1) f += 2.0 * split::BM * split::BN * split::BK * (double)t.nkb * p1x.slices * (p1x.slices + 1) / 2;
+        for (auto& t : t2) f += 2.0 * split::BM * split::BN * split::BK * (double)t.nkb * p2.slices * (p2.slices + 1) / 2;
+        stats->tensor_flops = f;
+    }
+    if (errw != 0)
+        return set_error(GAIN_ERR_TIMEOUT, "a bounded device wait of the tensor-core GEMM gave up (code %d)", errw);
+    if (cnt[0] > (unsigned)kMaxFlags || cnt[1] > (unsigned)kMaxFlags)
+        return set_error(GAIN_ERR_TOL_NOT_MET, "more lines need FP64 refinement than the refinement list holds");
+    if (unc[0] > 0)
+        return set_error(GAIN_ERR_TOL_NOT_MET, "%llu refined lines still exceed the tolerance bound", unc[0]);
+    return GAIN_OK;
+}
+
+}  // namespace
+}  // namespace gain
+
+// ====================================================================== C ABI
+using namespace gain;
+
+extern "C" {
+
+const char* gain_last_error_string(void) { return gain::g_last_error.c_str(); }
+
+const char* gain_status_string(gain_status s) {
+    switch (s) {
+        case GAIN_OK: return "GAIN_OK";
+        case GAIN_ERR_INVALID_ARG: return "GAIN_ERR_INVALID_ARG";
+        case GAIN_ERR_OOM: return "GAIN_ERR_OOM";
+        case GAIN_ERR_CUDA: return "GAIN_ERR_CUDA";
+        case GAIN_ERR_TIMEOUT: return "GAIN_ERR_TIMEOUT";
+        case GAIN_ERR_TOL_NOT_MET: return "GAIN_ERR_TOL_NOT_MET";
+        case GAIN_ERR_NOT_READY: return "GAIN_ERR_NOT_READY";
+        case GAIN_ERR_UNSUPPORTED: return "GAIN_ERR_UNSUPPORTED";
+    }
+    return "GAIN_ERR_UNKNOWN";
+}
+
+int gain_abi_version(void) { return GAIN_ABI_VERSION; }
+
+gain_status gain_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF, const int* tauI, const int* tauF,
+                            const int* icorrI, const int* icorrF, int startF_idx, int startI_idx,
+                            int startFblock, int endFblock, int ncontrF, int kFBlocksize,
+                            const int* kblock_size, const double* dipole_me, const double* vector,
+                            const double* threej, double* half_ls, int jmax, int dip_stride, void* stream) {
+    clear_error();
+    (void)kFBlocksize;
+    if (dimenF < 0 || dimenI < 0 || jI < 0 || jF < 0 || kF < 0 || kF > jF || jI > jmax || jF > jmax ||
+        std::abs(jI - jF) > 1 || ncontrF <= 0 || dip_stride <= 0 || startF_idx < 0 || startI_idx < 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_hls_kblock: inconsistent sizes");
+    if (dimenF > 0 && (!tauI || !tauF || !icorrI || !icorrF || !kblock_size || !dipole_me || !vector ||
+                       !threej || !half_ls))
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_hls_kblock: NULL pointer");
+    GAIN_CUDA(launch_hls_kblock(dimenF, dimenI, jI, jF, kF, tauI, tauF, icorrI, icorrF, startF_idx,
+                                startI_idx, startFblock, endFblock, ncontrF, kblock_size, dipole_me,
+                                vector, threej, half_ls, jmax, dip_stride, (cudaStream_t)stream));
+    return GAIN_OK;
+}
+
+gain_status gain_expand(int dimenI, int igammaI, int maxcoeff, int idegI, int sdeg, int Ntot,
+                        const int* ijterms, const int* icontr, const int* N, const double* repres,
+                        const double* vecI, double* vec, void* stream) {
+    clear_error();
+    if (dimenI < 0 || igammaI < 0 || maxcoeff <= 0 || idegI < 0 || sdeg <= 0 || Ntot < 0 || idegI >= sdeg)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_expand: inconsistent sizes");
+    if (dimenI > 0 && (!ijterms || !icontr || !N || !repres || !vecI || !vec))
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_expand: NULL pointer");
+    GAIN_CUDA(launch_expand(dimenI, igammaI, maxcoeff, idegI, sdeg, Ntot, ijterms, icontr, N, repres, vecI,
+                            vec, (cudaStream_t)stream));
+    return GAIN_OK;
+}
+
+gain_status gain_dot(int n, const double* x, const double* y, double* result, void* stream) {
+    clear_error();
+    if (n < 0 || !result || (n > 0 && (!x || !y))) return set_error(GAIN_ERR_INVALID_ARG, "gain_dot: bad argument");
+    GAIN_CUDA(launch_dot(n, x, y, result, (cudaStream_t)stream));
+    return GAIN_OK;
+}
+
+gain_status gain_threej_table(int jmax, double* table) {
+    clear_error();
+    if (jmax < 0 || jmax > 200 || !table) return set_error(GAIN_ERR_INVALID_ARG, "gain_threej_table: bad argument");
+    threej_table_host(jmax, table);
+    return GAIN_OK;
+}
+
+gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_engine* out) {
+    clear_error();
+    if (!out || jmax < 0 || jmax > 200 || nsym <= 0 || maxdeg <= 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_engine_create: bad argument");
+    *out = nullptr;
+    int ndev = 0;
+    GAIN_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return set_error(GAIN_ERR_INVALID_ARG, "no CUDA device %d", device);
+    GAIN_CUDA(cudaSetDevice(device));
+    std::unique_ptr<gain_engine_s> e(new gain_engine_s());
+    e->device = device;
+    e->jmax = jmax;
+    e->nsym = nsym;
+    e->maxdeg = maxdeg;
+    GAIN_CUDA(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device));
+    GAIN_CUDA(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+    for (auto& ev : e->ev) GAIN_CUDA(cudaEventCreate(&ev));
+    std::vector<double> t((size_t)(jmax + 1) * (jmax + 1) * 9);
+    threej_table_host(jmax, t.data());
+    GAIN_TRY(e->d3j.upload(t));
+    *out = e.release();
+    return GAIN_OK;
+}
+
+gain_status gain_engine_destroy(gain_engine e) {
+    clear_error();
+    if (!e) return GAIN_OK;
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->st);
+    for (auto& ev : e->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->st) cudaStreamDestroy(e->st);
+    delete e;
+    return GAIN_OK;
+}
+
+gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const int* K, const int* tau,
+                              const int* vib, const int* kblock_size, const int* kstart) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (jind < 0 || jind > 1000 || J < 0 || J > e->jmax || dimen <= 0 || !K || !tau || !vib || !kblock_size || !kstart)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_basis: bad argument");
+    // K-sorted, K-blocks consistent with the per-function K (TroveBasisSet.cpp:659-681)
+    int pos = 0;
+    for (int k = 0; k <= J; ++k) {
+        if (kstart[k] != pos || kblock_size[k] < 0) return set_error(GAIN_ERR_INVALID_ARG, "inconsistent kstart at K=%d", k);
+        for (int i = 0; i < kblock_size[k]; ++i)
+            if (pos + i >= dimen || K[pos + i] != k)
+                return set_error(GAIN_ERR_INVALID_ARG, "function %d is not in K block %d", pos + i, k);
+        pos += kblock_size[k];
+    }
+    if (pos != dimen) return set_error(GAIN_ERR_INVALID_ARG, "K blocks cover %d of %d functions", pos, dimen);
+    for (int i = 0; i < dimen; ++i)
+        if (vib[i] < 0 || tau[i] < 0) return set_error(GAIN_ERR_INVALID_ARG, "negative tau or vibrational index");
+    if ((int)e->bases.size() <= jind) {
+        e->bases.resize(jind + 1);
+        e->infl.resize(jind + 1);
+    }
+    Basis& b = e->bases[jind];
+    b.J = J;
+    b.dimen = dimen;
+    b.K.assign(K, K + dimen);
+    b.tau.assign(tau, tau + dimen);
+    for (auto& t : b.tau) t &= 1;
+    b.vib.assign(vib, vib + dimen);
+    b.kblock.assign(kblock_size, kblock_size + J + 1);
+    b.kstart.assign(kstart, kstart + J + 1);
+    GAIN_TRY(b.dK.upload(b.K));
+    GAIN_TRY(b.dtau.upload(b.tau));
+    GAIN_TRY(b.dvib.upload(b.vib));
+    GAIN_TRY(b.dkblock.upload(b.kblock));
+    b.present = true;
+    e->layout.key[0] = -1;
+    e->plain.key[0] = -1;
+    if (e->infl[jind].present)
+        for (auto& m : e->infl[jind].maps) m->built = false;
+    return GAIN_OK;
+}
+
+gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, const int* ijterms, int dimen,
+                                  int maxcoeff, int matsize, const int* const* N, const double* const* repres,
+                                  const int* Ntot, const int* sdeg) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (jind < 0 || jind >= (int)e->bases.size() || !e->bases[jind].present)
+        return set_error(GAIN_ERR_NOT_READY, "upload the basis of jind %d first", jind);
+    if (dimen != e->bases[jind].dimen || maxcoeff <= 0 || matsize <= 0 || !icontr || !ijterms || !N || !repres ||
+        !Ntot || !sdeg)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_inflation: bad argument");
+    Inflation& inf = e->infl[jind];
+    inf.dimen = dimen;
+    inf.maxcoeff = maxcoeff;
+    inf.matsize = matsize;
+    inf.icontr.assign(icontr, icontr + 2 * (size_t)dimen);
+    inf.ijterms.assign(ijterms, ijterms + (size_t)maxcoeff * e->nsym);
+    inf.Ntot.assign(Ntot, Ntot + e->nsym);
+    inf.sdeg.assign(sdeg, sdeg + e->nsym);
+    inf.N.clear();
+    inf.repres.clear();
+    inf.dN.clear();
+    inf.drepres.clear();
+    inf.maps.clear();
+    for (int r = 0; r < dimen; ++r)
+        if (inf.icontr[r] < 0 || inf.icontr[r] >= maxcoeff || inf.icontr[r + dimen] < 0)
+            return set_error(GAIN_ERR_INVALID_ARG, "icontr entry %d out of range", r);
+    for (int g = 0; g < e->nsym; ++g) {
+        if (Ntot[g] < 0 || sdeg[g] <= 0 || !N[g] || (Ntot[g] > 0 && !repres[g]))
+            return set_error(GAIN_ERR_INVALID_ARG, "bad expansion table of Gamma %d", g);
+        inf.N.emplace_back(N[g], N[g] + maxcoeff);
+        const size_t nrep = (size_t)Ntot[g] * sdeg[g] * matsize;
+        inf.repres.emplace_back(repres[g], repres[g] + nrep);
+        for (int r = 0; r < dimen; ++r) {
+            const int irow = inf.icontr[r], ib = inf.icontr[r + dimen];
+            const int it = inf.ijterms[irow + g * maxcoeff], n = inf.N[g][irow];
+            if (n > 0 && (it < 0 || it + n > Ntot[g] || ib >= matsize))
+                return set_error(GAIN_ERR_INVALID_ARG, "expansion of function %d leaves Gamma %d's range", r, g);
+        }
+        inf.dN.emplace_back(new DevArray<int>());
+        inf.drepres.emplace_back(new DevArray<double>());
+        GAIN_TRY(inf.dN.back()->upload(inf.N.back()));
+        GAIN_TRY(inf.drepres.back()->upload(inf.repres.back()));
+        inf.maps.emplace_back(new GammaMaps());
+    }
+    GAIN_TRY(inf.dicontr.upload(inf.icontr));
+    GAIN_TRY(inf.dijterms.upload(inf.ijterms));
+    inf.present = true;
+    e->layout.key[0] = -1;
+    e->plain.key[0] = -1;
+    return GAIN_OK;
+}
+
+gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int startF, int endF, int ncontrF) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!piece || N <= 0 || startF < 0 || endF > N || endF - startF != ncontrF || ncontrF <= 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_dipole: bad block (N=%d, [%d,%d), ncontrF=%d)", N, startF,
+                         endF, ncontrF);
+    for (auto& b : e->bases)
+        if (b.present)
+            for (int v : b.vib)
+                if (v >= N) return set_error(GAIN_ERR_INVALID_ARG, "vibrational index %d >= dipole size %d", v, N);
+    GAIN_TRY(e->dipole.upload(piece, (size_t)3 * N * ncontrF));
+    e->dipN = N;
+    e->startF = startF;
+    e->endF = endF;
+    e->ncontrF = ncontrF;
+    e->dip_present = true;
+    ++e->dip_version;
+    return GAIN_OK;
+}
+
+gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize, const double* vecs) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (jind < 0 || gamma < 0 || gamma >= e->nsym || nlevels <= 0 || nsize <= 0 || !vecs)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs: bad argument");
+    auto& slot = e->eig[{jind, gamma}];
+    if (!slot) slot.reset(new Eig());
+    slot->nlevels = nlevels;
+    slot->nsize = nsize;
+    GAIN_TRY(slot->d.alloc((size_t)nlevels * nsize));
+    GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyHostToDevice,
+                              e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    return GAIN_OK;
+}
+
+gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path path, const gain_split_opts* opts,
+                          gain_stats* stats) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    GAIN_TRY(validate_job(e, job));
+    e->have_amp = false;
+    if (path == GAIN_PATH_PLAIN_FP64) return run_plain(e, job, stats);
+    if (path == GAIN_PATH_SPLIT) return run_split(e, job, opts, stats);
+    return set_error(GAIN_ERR_INVALID_ARG, "unknown path %d", (int)path);
+}
+
+gain_status gain_pair_amp_device(gain_engine e, const double** amp, int* ld) {
+    clear_error();
+    if (!e || !amp || !ld) return set_error(GAIN_ERR_INVALID_ARG, "NULL argument");
+    if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
+    *amp = e->amp.p;
+    *ld = (int)e->amp_ld;
+    return GAIN_OK;
+}
+
+gain_status gain_fetch_amp(gain_engine e, double* amp_host) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!amp_host) return set_error(GAIN_ERR_INVALID_ARG, "NULL output");
+    if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
+    GAIN_CUDA(cudaMemcpy2DAsync(amp_host, sizeof(double) * e->amp_cols, e->amp.p, sizeof(double) * e->amp_ld,
+                                sizeof(double) * e->amp_cols, e->amp_rows, cudaMemcpyDeviceToHost, e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    return GAIN_OK;
+}
+
+gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                            const double* energiesF, int jI, int jF, double* S, double* A, double* I,
+                            unsigned char* keep, long long* n_lines) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!prm || !energiesI || !energiesF || jI < 0 || jF < 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines: bad argument");
+    if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
+    if (prm->ndegI != 1 || prm->ndegF != 1)
+        return set_error(GAIN_ERR_UNSUPPORTED, "line assembly handles non-degenerate symmetries only");
+    if (prm->temperature <= 0 || prm->q_part <= 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "temperature and partition function must be positive");
+    const int rows = e->amp_rows, cols = e->amp_cols;
+    const size_t n = (size_t)rows * cols;
+    cudaStream_t st = e->st;
+    GAIN_TRY(e->eIdev.upload(energiesI, rows));
+    GAIN_TRY(e->eFdev.upload(energiesF, cols));
+    GAIN_TRY(e->lineS.alloc(n));
+    GAIN_TRY(e->lineA.alloc(n));
+    GAIN_TRY(e->lineI.alloc(n));
+    GAIN_TRY(e->lineKeep.alloc(n));
+    GAIN_TRY(e->ull.alloc(4));
+    GAIN_TRY(e->ull.zero(st, 4));
+    LineParams p;
+    p.acoef_2jI1 = 3.13618923e-7 * (double)(2 * jI + 1);
+    p.cmcoef = 1.327209365e-12;
+    p.gnsF = prm->gnsF;
+    p.two_jF1 = 2.0 * (double)jF + 1.0;
+    p.beta = 6.62606896e-27 * 2.99792458e+10 / (1.380658e-16 * prm->temperature);
+    p.zpe = prm->zpe;
+    p.q_part = prm->q_part;
+    p.thresh = prm->thresh;
+    p.freq_lo = prm->freq_lo;
+    p.freq_hi = prm->freq_hi;
+    p.with_intensity = I != nullptr;
+    GAIN_CUDA(launch_lines(rows, cols, e->amp.p, e->amp_ld, e->eIdev.p, e->eFdev.p, p, e->lineS.p, e->lineA.p,
+                           e->lineI.p, e->lineKeep.p, e->ull.p + 1, st));
+    unsigned long long nk = 0;
+    GAIN_CUDA(cudaMemcpyAsync(&nk, e->ull.p + 1, sizeof nk, cudaMemcpyDeviceToHost, st));
+    if (S) GAIN_CUDA(cudaMemcpyAsync(S, e->lineS.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (A) GAIN_CUDA(cudaMemcpyAsync(A, e->lineA.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (I) GAIN_CUDA(cudaMemcpyAsync(I, e->lineI.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (keep) GAIN_CUDA(cudaMemcpyAsync(keep, e->lineKeep.p, n, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    if (n_lines) *n_lines = (long long)nk;
+    return GAIN_OK;
+}
+
+int gain_format_line(char* buf, size_t cap, double nu, int indexF, int jF, int gammaF, int indexI, int jI,
+                     int gammaI, double A, int with_intensity, double intensity, const double* amps, int namp) {
+    if (!buf || cap == 0) return 0;
+    std::string s;
+    char tmp[256];
+    snprintf(tmp, sizeof tmp, "%12.6f %8d %4d %4d <- %8d %4d %4d %16.9E ", nu, indexF + 1, jF, gammaF + 1,
+             indexI + 1, jI, gammaI + 1, A);
+    s += tmp;
+    if (with_intensity) {
+        snprintf(tmp, sizeof tmp, "%16.9E ", intensity);
+        s += tmp;
+    }
+    if (amps && namp > 0) {
+        std::string l;
+        for (int i = 0; i < namp; ++i) {
+            snprintf(tmp, sizeof tmp, " %16.9E", amps[i]);
+            l += tmp;
+        }
+        s += "[ " + l + " ] ";
+    }
+    s += "|| \n";
+    const size_t n = std::min(cap - 1, s.size());
+    memcpy(buf, s.data(), n);
+    buf[n] = 0;
+    return (int)n;
+}
+
+}  // extern "C"

@@ -1,0 +1,363 @@
+// FP64 kernels of the line-strength path: the kernel-level drop-ins (K-block half line
+// strength, vector expansion, dot product), the plain-path kernels (half line strength of
+// the needed upper functions, transpose expansion, GEMV against resident upper vectors) and
+// the S / A / I line assembly.
+#include "gain_internal.h"
+
+namespace gain {
+namespace {
+
+__device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
+
+// 3j table index of GpuManager.cpp:179 / dipole_GPU.cu:445
+__device__ __forceinline__ int threej_index(int jI, int kI, int jF, int kF, int jmax) {
+    const int n = jmax + 1;
+    return jI + kI * n + (jF - jI + 1) * n * n + (kF - kI + 1) * n * n * 3;
+}
+
+// The rotational factor of one (lower, upper) primitive pair, as the reference kernel
+// evaluates it (GPU/dipole_GPU.cu:490-495): dipole component and integer coefficient.
+__device__ __forceinline__ void rot_factor(int kI, int kF, int tauI, int tauF, int* didx, int* c) {
+    const int eq = (kF == kI), neq = !eq;
+    const int tneq = (tauF != tauI);
+    *didx = 2 * eq + neq * (!tneq);
+    *c = (tauF - tauI) * eq + (tauF - tauI) * (kF - kI) * neq * tneq - neq * (!tneq);
+}
+
+// ---------------------------------------------------------------------------------------
+// Drop-in K-block kernel.  One thread per upper primitive of the K block; lower functions
+// of the three neighbouring K blocks are staged through shared memory 128 at a time.  Each
+// output is accumulated in ascending lower index with one fused multiply-add per term, the
+// same operation sequence as the reference kernel, so results agree bit for bit.
+constexpr int kDropTile = 128;
+
+__global__ void __launch_bounds__(kDropTile)
+k_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF, const int* __restrict__ tauI,
+             const int* __restrict__ tauF, const int* __restrict__ icorrI,
+             const int* __restrict__ icorrF, int startF_idx, int startI_idx, int startFblock,
+             int endFblock, int ncontrF, const int* __restrict__ kblock_size,
+             const double* __restrict__ dipole_me, const double* __restrict__ vector,
+             const double* __restrict__ threej, double* __restrict__ half_ls, int jmax,
+             int dip_stride) {
+    __shared__ double s_lsf[kDropTile];
+    __shared__ double s_sgn[kDropTile];
+    __shared__ int s_tau[kDropTile];
+    __shared__ long s_off[kDropTile];
+
+    const int f = blockIdx.x * kDropTile + threadIdx.x;
+    const int irootF = startF_idx + f;
+    const bool inF = f < dimenF;
+    int icF = 0, tF = 0;
+    if (inF) {
+        icF = icorrF[irootF];
+        tF = tauF[irootF] & 1;
+    }
+    const bool valid = inF && icF >= startFblock && icF < endFblock;
+    icF -= startFblock;
+    const long stride = (long)ncontrF * dip_stride;
+    double acc = 0.0;
+    int startI = startI_idx;
+    for (int kI = max(kF - 1, 0); kI < kF + 2 && kI < jI + 1; ++kI) {
+        const int kbs = kblock_size[kI];
+        const double sq = (kI * kF != 0) ? kSqrt2Ref : 1.0;
+        const double f3j = threej[threej_index(jI, kI, jF, kF, jmax)];
+        int didx_same, c_same, didx_flip, c_flip;   // tau_I == tau_F and tau_I != tau_F cases
+        rot_factor(kI, kF, tF, tF, &didx_same, &c_same);
+        rot_factor(kI, kF, tF ^ 1, tF, &didx_flip, &c_flip);
+        for (int base = 0; base < kbs; base += kDropTile) {
+            const int loc = base + threadIdx.x;
+            double lsf = 0.0, sg = 1.0;
+            int ti = 0;
+            long off = 0;
+            if (loc < kbs) {
+                const int ir = startI + loc;
+                ti = tauI[ir];
+                off = (long)icorrI[ir] * ncontrF;
+                sg = parity_sign((kI % 3) * ti + kI);
+                double ls = vector[ir];
+                if (kF != kI) ls = __dmul_rn(ls, sq);
+                lsf = __dmul_rn(ls, f3j);
+            }
+            __syncthreads();
+            s_lsf[threadIdx.x] = lsf;
+            s_sgn[threadIdx.x] = sg;
+            s_tau[threadIdx.x] = ti;
+            s_off[threadIdx.x] = off;
+            __syncthreads();
+            const int n = min(kDropTile, kbs - base);
+            if (valid) {
+                for (int i = 0; i < n; ++i) {
+                    const double l = s_lsf[i];
+                    if (l == 0.0) continue;
+                    const int t = s_tau[i];
+                    int didx, c;
+                    if (t == tF) { didx = didx_same; c = c_same; }
+                    else if (t == (tF ^ 1)) { didx = didx_flip; c = c_flip; }
+                    else rot_factor(kI, kF, t, tF, &didx, &c);
+                    const double ls = __dmul_rn(l, (double)c);
+                    acc = __fma_rn(__dmul_rn(ls, s_sgn[i]), dipole_me[icF + s_off[i] + didx * stride], acc);
+                }
+            }
+        }
+        startI += kbs;
+        if (startI >= dimenI) break;
+    }
+    if (valid) half_ls[irootF] = __dmul_rn(acc, parity_sign((kF % 3) * tF));
+}
+
+// ---------------------------------------------------------------------------------------
+// device_expand_vectors (GPU/dipole_GPU.cu:859-889): one thread per primitive function.
+__global__ void k_expand(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                         const int* __restrict__ ijterms, const int* __restrict__ icontr,
+                         const int* __restrict__ N, const double* __restrict__ repres,
+                         const double* __restrict__ vecI, double* __restrict__ vec) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= dimen) return;
+    const int irow = icontr[r];
+    const int ib = icontr[r + dimen];
+    const int iterm = ijterms[irow + igamma * maxcoeff];
+    const int nelem = N[irow];
+    const long base = (long)ideg * Ntot + (long)ib * sdeg * Ntot;
+    double acc = 0.0;
+    for (int i = 0; i < nelem; ++i) acc = __fma_rn(vecI[iterm + i], repres[iterm + i + base], acc);
+    vec[r] = acc;
+}
+
+// ---------------------------------------------------------------------------------------
+// dot product with a device result: one CTA, strided partial sums, tree reduction.
+__global__ void __launch_bounds__(1024) k_dot(int n, const double* __restrict__ x,
+                                              const double* __restrict__ y, double* result) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc = __fma_rn(x[i], y[i], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) *result = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Plain path: half line strength of the listed upper primitives.  Each CTA covers
+// functions of one upper K; the lower functions come from the per-K support lists of the
+// lower symmetry class, in ascending primitive order, so each output equals the
+// reference kernel's value bit for bit (entries outside the support are zero and the
+// reference skips them).
+__global__ void __launch_bounds__(kHlsTile)
+k_hls_needed(const HlsCta* __restrict__ ctas, const int* __restrict__ f_list, int jI, int jF,
+             const int* __restrict__ tauI, const int* __restrict__ tauF,
+             const int* __restrict__ icorrI, const int* __restrict__ icorrF,
+             const int* __restrict__ sup_list, const int* __restrict__ sup_start,
+             int startFblock, int endFblock, int ncontrF, const double* __restrict__ dipole_me,
+             int dip_stride, const double* __restrict__ prim_vec, const double* __restrict__ threej,
+             int jmax, double* __restrict__ half_ls) {
+    __shared__ double s_lsf[kHlsTile];
+    __shared__ double s_sgn[kHlsTile];
+    __shared__ int s_tau[kHlsTile];
+    __shared__ long s_off[kHlsTile];
+    const HlsCta cta = ctas[blockIdx.x];
+    const int kF = cta.kF;
+    const bool inF = (int)threadIdx.x < cta.f_count;
+    int irootF = 0, icF = 0, tF = 0;
+    if (inF) {
+        irootF = f_list[cta.f_begin + threadIdx.x];
+        icF = icorrF[irootF];
+        tF = tauF[irootF] & 1;
+    }
+    const bool valid = inF && icF >= startFblock && icF < endFblock;
+    icF -= startFblock;
+    const long stride = (long)ncontrF * dip_stride;
+    double acc = 0.0;
+    for (int kI = max(kF - 1, 0); kI < kF + 2 && kI < jI + 1; ++kI) {
+        const int s0 = sup_start[kI], ns = sup_start[kI + 1] - s0;
+        const double sq = (kI * kF != 0) ? kSqrt2Ref : 1.0;
+        const double f3j = threej[threej_index(jI, kI, jF, kF, jmax)];
+        for (int base = 0; base < ns; base += kHlsTile) {
+            const int loc = base + threadIdx.x;
+            double lsf = 0.0, sg = 1.0;
+            int ti = 0;
+            long off = 0;
+            if (loc < ns) {
+                const int ir = sup_list[s0 + loc];
+                ti = tauI[ir];
+                off = (long)icorrI[ir] * ncontrF;
+                sg = parity_sign((kI % 3) * ti + kI);
+                double ls = prim_vec[ir];
+                if (kF != kI) ls = __dmul_rn(ls, sq);
+                lsf = __dmul_rn(ls, f3j);
+            }
+            __syncthreads();
+            s_lsf[threadIdx.x] = lsf;
+            s_sgn[threadIdx.x] = sg;
+            s_tau[threadIdx.x] = ti;
+            s_off[threadIdx.x] = off;
+            __syncthreads();
+            const int n = min(kHlsTile, ns - base);
+            if (valid) {
+                for (int i = 0; i < n; ++i) {
+                    const double l = s_lsf[i];
+                    if (l == 0.0) continue;
+                    int didx, c;
+                    rot_factor(kI, kF, s_tau[i], tF, &didx, &c);
+                    const double ls = __dmul_rn(l, (double)c);
+                    acc = __fma_rn(__dmul_rn(ls, s_sgn[i]), dipole_me[icF + s_off[i] + didx * stride], acc);
+                }
+            }
+        }
+    }
+    if (valid) half_ls[irootF] = __dmul_rn(acc, parity_sign((kF % 3) * tF));
+    else if (inF) half_ls[irootF] = 0.0;
+}
+
+__global__ void k_contract(int nsym, const int* __restrict__ rowptr, const int* __restrict__ col,
+                           const double* __restrict__ val, const double* __restrict__ h,
+                           double* __restrict__ hsym) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsym) return;
+    double acc = 0.0;
+    for (int e = rowptr[s]; e < rowptr[s + 1]; ++e) acc = __fma_rn(h[col[e]], val[e], acc);
+    hsym[s] = acc;
+}
+
+// one warp per output row
+__global__ void __launch_bounds__(256)
+k_gemv_rows(int nrows, int n, const double* __restrict__ U, long ldu, const int* __restrict__ levels,
+            const double* __restrict__ x, double* __restrict__ out) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    const double* row = U + (long)levels[warp] * ldu;
+    double a0 = 0.0, a1 = 0.0;
+    int i = lane;
+    for (; i + 32 < n; i += 64) {
+        a0 = __fma_rn(__ldg(row + i), __ldg(x + i), a0);
+        a1 = __fma_rn(__ldg(row + i + 32), __ldg(x + i + 32), a1);
+    }
+    if (i < n) a0 = __fma_rn(__ldg(row + i), __ldg(x + i), a0);
+    double acc = a0 + a1;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[warp] = acc;
+}
+
+__global__ void k_scatter_select(int dimen, const int* __restrict__ sym_of,
+                                 const double* __restrict__ coef, const double* __restrict__ vec,
+                                 double* __restrict__ prim) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= dimen) return;
+    const int s = sym_of[r];
+    prim[r] = s >= 0 ? __dmul_rn(vec[s], coef[r]) : 0.0;
+}
+
+// S / A / I of every amplitude (non-degenerate symmetries), Output.cpp:52-112.
+__global__ void k_lines(int rows, int cols, const double* __restrict__ amp, long ld,
+                        const double* __restrict__ eI, const double* __restrict__ eF, LineParams p,
+                        double* __restrict__ S, double* __restrict__ A, double* __restrict__ I,
+                        unsigned char* __restrict__ keep, unsigned long long* nkeep) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long total = (long)rows * cols;
+    int k = 0;
+    if (idx < total) {
+        const int r = (int)(idx / cols), c = (int)(idx - (long)r * cols);
+        const double a = amp[(long)r * ld + c];
+        const double nu = eF[c] - eI[r];
+        double ls = __dmul_rn(a, a);                          // :83, ndegI = ndegF = 1
+        const double anu = fabs(nu);
+        const double Aein = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, ls), anu), anu), anu);  // :93
+        k = (nu >= p.freq_lo && nu <= p.freq_hi && nu >= 1e-40 && Aein >= p.thresh) ? 1 : 0;
+        double inten = 0.0;
+        if (p.with_intensity && nu >= 1e-40) {
+            // CMCOEF*A*gns*(2jF+1)*exp(-beta E'')*(1-exp(-beta nu))/(nu^2 Q), :101-102
+            inten = __dmul_rn(p.cmcoef, Aein);
+            inten = __dmul_rn(inten, p.gnsF);
+            inten = __dmul_rn(inten, p.two_jF1);
+            inten = __dmul_rn(inten, exp(-p.beta * (eI[r] - p.zpe)));
+            inten = __dmul_rn(inten, 1.0 - exp(-p.beta * nu));
+            inten = __ddiv_rn(inten, __dmul_rn(__dmul_rn(nu, nu), p.q_part));
+        }
+        if (S) S[idx] = ls;
+        if (A) A[idx] = Aein;
+        if (I) I[idx] = inten;
+        if (keep) keep[idx] = (unsigned char)k;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, k);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(nkeep, (unsigned long long)__popc(m));
+}
+
+}  // namespace
+
+cudaError_t launch_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF, const int* tauI,
+                              const int* tauF, const int* icorrI, const int* icorrF, int startF_idx,
+                              int startI_idx, int startFblock, int endFblock, int ncontrF,
+                              const int* kblock_size, const double* dipole_me,
+                              const double* vector, const double* threej, double* half_ls,
+                              int jmax, int dip_stride, cudaStream_t st) {
+    if (dimenF <= 0) return cudaSuccess;
+    k_hls_kblock<<<(dimenF + kDropTile - 1) / kDropTile, kDropTile, 0, st>>>(
+        dimenF, dimenI, jI, jF, kF, tauI, tauF, icorrI, icorrF, startF_idx, startI_idx,
+        startFblock, endFblock, ncontrF, kblock_size, dipole_me, vector, threej, half_ls, jmax,
+        dip_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expand(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                          const int* ijterms, const int* icontr, const int* N,
+                          const double* repres, const double* vecI, double* vec, cudaStream_t st) {
+    if (dimen <= 0) return cudaSuccess;
+    k_expand<<<(dimen + 255) / 256, 256, 0, st>>>(dimen, igamma, maxcoeff, ideg, sdeg, Ntot,
+                                                   ijterms, icontr, N, repres, vecI, vec);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dot(int n, const double* x, const double* y, double* result, cudaStream_t st) {
+    k_dot<<<1, 1024, 0, st>>>(n, x, y, result);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hls_needed(const HlsCta* ctas, int ncta, const int* f_list, int jI, int jF,
+                              const int* tauI, const int* tauF, const int* icorrI,
+                              const int* icorrF, const int* sup_list, const int* sup_start,
+                              int startFblock, int endFblock, int ncontrF,
+                              const double* dipole_me, int dip_stride, const double* prim_vec,
+                              const double* threej, int jmax, double* half_ls, cudaStream_t st) {
+    if (ncta <= 0) return cudaSuccess;
+    k_hls_needed<<<ncta, kHlsTile, 0, st>>>(ctas, f_list, jI, jF, tauI, tauF, icorrI, icorrF,
+                                            sup_list, sup_start, startFblock, endFblock, ncontrF,
+                                            dipole_me, dip_stride, prim_vec, threej, jmax, half_ls);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contract(int nsym, const int* rowptr, const int* col, const double* val,
+                            const double* h, double* hsym, cudaStream_t st) {
+    if (nsym <= 0) return cudaSuccess;
+    k_contract<<<(nsym + 255) / 256, 256, 0, st>>>(nsym, rowptr, col, val, h, hsym);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemv_rows(int nrows, int n, const double* U, long ldu, const int* levels,
+                             const double* x, double* amp_row, cudaStream_t st) {
+    if (nrows <= 0) return cudaSuccess;
+    k_gemv_rows<<<(nrows + 7) / 8, 256, 0, st>>>(nrows, n, U, ldu, levels, x, amp_row);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* coef,
+                                  const double* vec, double* prim, cudaStream_t st) {
+    if (dimen <= 0) return cudaSuccess;
+    k_scatter_select<<<(dimen + 255) / 256, 256, 0, st>>>(dimen, sym_of, coef, vec, prim);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lines(int rows, int cols, const double* amp, long ld, const double* eI,
+                         const double* eF, LineParams p, double* S, double* A, double* I,
+                         unsigned char* keep, unsigned long long* nkeep, cudaStream_t st) {
+    const long total = (long)rows * cols;
+    if (total <= 0) return cudaSuccess;
+    const long blocks = (total + 255) / 256;
+    k_lines<<<(unsigned)blocks, 256, 0, st>>>(rows, cols, amp, ld, eI, eF, p, S, A, I, keep, nkeep);
+    return cudaGetLastError();
+}
+
+}  // namespace gain

@@ -1,0 +1,88 @@
+// Internal declarations shared by the translation units of libgainls.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+
+#include "../../include/gain_ls.h"
+
+namespace gain {
+
+// ---------------------------------------------------------------- error reporting
+gain_status set_error(gain_status s, const char* fmt, ...);
+void clear_error();
+gain_status cuda_fail(cudaError_t e, const char* what);
+
+#define GAIN_CUDA(call)                                                   \
+    do {                                                                  \
+        cudaError_t e__ = (call);                                         \
+        if (e__ != cudaSuccess) return ::gain::cuda_fail(e__, #call);     \
+    } while (0)
+
+#define GAIN_TRY(call)                                                    \
+    do {                                                                  \
+        gain_status s__ = (call);                                         \
+        if (s__ != GAIN_OK) return s__;                                   \
+    } while (0)
+
+// the reference's truncated 1/sqrt(2), GPU/dipole_GPU.cu:24
+constexpr double kSqrt2Ref = 0.70710678118;
+
+// exact Wigner 3j table (threej.cpp)
+void threej_table_host(int jmax, double* table);
+
+// ---------------------------------------------------------------- FP64 kernels (fp64_kernels.cu)
+cudaError_t launch_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF, const int* tauI,
+                              const int* tauF, const int* icorrI, const int* icorrF, int startF_idx,
+                              int startI_idx, int startFblock, int endFblock, int ncontrF,
+                              const int* kblock_size, const double* dipole_me,
+                              const double* vector, const double* threej, double* half_ls,
+                              int jmax, int dip_stride, cudaStream_t st);
+cudaError_t launch_expand(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                          const int* ijterms, const int* icontr, const int* N,
+                          const double* repres, const double* vecI, double* vec, cudaStream_t st);
+cudaError_t launch_dot(int n, const double* x, const double* y, double* result, cudaStream_t st);
+
+// Plain FP64 path: one CTA table entry covers up to kHlsTile upper functions of one K block.
+struct HlsCta {
+    int kF;        // upper K of every function in this CTA
+    int f_begin;   // offset into the needed-F list
+    int f_count;   // <= kHlsTile
+    int pad;
+};
+constexpr int kHlsTile = 128;
+
+// half_ls restricted to the needed upper primitives (F list), summing over the lower
+// support lists per K block. Writes half_ls[F] (primitive index) for every listed F.
+cudaError_t launch_hls_needed(const HlsCta* ctas, int ncta, const int* f_list, int jI, int jF,
+                              const int* tauI, const int* tauF, const int* icorrI,
+                              const int* icorrF, const int* sup_list, const int* sup_start,
+                              int startFblock, int endFblock, int ncontrF,
+                              const double* dipole_me, int dip_stride, const double* prim_vec,
+                              const double* threej, int jmax, double* half_ls, cudaStream_t st);
+
+// hsym[s] = sum_{e in row s} h[col[e]] * val[e]  (transpose of the expansion)
+cudaError_t launch_contract(int nsym, const int* rowptr, const int* col, const double* val,
+                            const double* h, double* hsym, cudaStream_t st);
+
+// amp_row[u] = sum_f U[level[u]*ldu + f] * x[f], u < nrows
+cudaError_t launch_gemv_rows(int nrows, int n, const double* U, long ldu, const int* levels,
+                             const double* x, double* amp_row, cudaStream_t st);
+
+// gather-expand of a selection expansion: prim[r] = coef[r] * vec[sym_of[r]] (sym_of<0 -> 0)
+cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* coef,
+                                  const double* vec, double* prim, cudaStream_t st);
+
+// S, A, I of a [rows x cols] amplitude block (ndeg = 1), Output.cpp:52-112
+struct LineParams {
+    double acoef_2jI1;   // ACOEF * (2 jI + 1), the first product of Output.cpp:93
+    double cmcoef, gnsF, two_jF1;
+    double beta, zpe, q_part, thresh, freq_lo, freq_hi;
+    int with_intensity;
+};
+cudaError_t launch_lines(int rows, int cols, const double* amp, long ld, const double* eI,
+                         const double* eF, LineParams p, double* S, double* A, double* I,
+                         unsigned char* keep, unsigned long long* nkeep, cudaStream_t st);
+
+}  // namespace gain

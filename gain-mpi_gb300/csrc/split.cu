@@ -1,0 +1,726 @@
+// Split-precision tensor-core path: digit slicing, rotational-dipole band construction,
+// the persistent tcgen05 digit-product GEMM and the FP64 refinement kernels.
+#include "split.h"
+
+#include <cuda_bf16.h>
+
+#include "gain_internal.h"
+
+namespace gain {
+namespace split {
+namespace {
+
+constexpr uint32_t STAGE_A = BM * BK * 2;   // bytes per A stage (16 KB)
+constexpr uint32_t STAGE_B = BN * BK * 2;   // bytes per B stage (16 KB)
+constexpr int NTHREADS = 192;               // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr uint32_t TMEM_COLS = 512;         // acc0 [0,128) acc1 [128,256) hi [256,384) lo [384,512)
+constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s per wait before giving up
+
+// ------------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait on a barrier phase.  Gives up when another role raised the CTA abort flag
+// (unless ignore_abort) or after kWaitNs, raising the flag and the device error word.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
+                          int code, bool ignore_abort = false) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 127u) == 0) {
+            if (!ignore_abort && *abort_flag) return false;
+            if (globaltimer() - t0 > kWaitNs) {
+                *abort_flag = 1;
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
+                                            int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+        "l"((unsigned long long)map), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+#define GAIN_R8(b) "=r"(r[b + 0]), "=r"(r[b + 1]), "=r"(r[b + 2]), "=r"(r[b + 3]), \
+                   "=r"(r[b + 4]), "=r"(r[b + 5]), "=r"(r[b + 6]), "=r"(r[b + 7])
+#define GAIN_W8(b) "r"(r[b + 0]), "r"(r[b + 1]), "r"(r[b + 2]), "r"(r[b + 3]), \
+                   "r"(r[b + 4]), "r"(r[b + 5]), "r"(r[b + 6]), "r"(r[b + 7])
+
+// 32 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : GAIN_R8(0), GAIN_R8(8), GAIN_R8(16), GAIN_R8(24)
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+        "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+        GAIN_W8(0), GAIN_W8(8), GAIN_W8(16), GAIN_W8(24)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with 128-byte swizzle:
+// rows of 128 bytes, 8-row groups 1024 bytes apart (SBO), base 1024-byte aligned.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);       // start address
+    d |= (uint64_t)1 << 16;                        // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+    d |= (uint64_t)1 << 46;                        // descriptor version
+    d |= (uint64_t)2 << 61;                        // 128-byte swizzle
+    return d;
+}
+// Instruction descriptor: BF16 x BF16 -> F32, A and B K-major, M = BM, N = BN.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ float pow2f(int e) {   // exact 2^e for -126 <= e <= 127
+    return __int_as_float((e + 127) << 23);
+}
+__device__ __forceinline__ double pow2d(int e) {
+    if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
+    return ldexp(1.0, e);
+}
+__device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, int* hi) {
+    *lo = (int)(((long)c * nkb) / nch);
+    *hi = (int)(((long)(c + 1) * nkb) / nch);
+}
+
+// ------------------------------------------------------------------- the GEMM kernel
+__global__ void __launch_bounds__(NTHREADS, 1)
+k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+             const GemmArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + STAGES * STAGE_A;
+    uint64_t* bars = (uint64_t*)(sB + STAGES * STAGE_B);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + STAGES;
+    uint64_t* accfull = bars + 2 * STAGES;
+    uint64_t* accempty = bars + 2 * STAGES + 2;
+    uint64_t* drain = bars + 2 * STAGES + 4;
+    uint32_t* tmem_holder = (uint32_t*)(bars + 2 * STAGES + 5);
+    volatile int* abort_flag = (volatile int*)(tmem_holder + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&accfull[b]), 1);
+            mbar_init(smem_u32(&accempty[b]), 128);
+        }
+        mbar_init(smem_u32(drain), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0 && lane == 0) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
+    }
+    if (warp == 1) {
+        tmem_alloc(smem_u32(tmem_holder), TMEM_COLS);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    if (warp == 0) {
+        // ---------------- TMA producer
+        if (lane == 0) {
+            uint32_t stage = 0, phase = 0;
+            uint32_t issued_mask = 0, last_par = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+                const Tile tl = a.tiles[t];
+                for (int p = 0; p < a.nprods && ok; ++p) {
+                    const Prod pr = a.prods[p];
+                    int lo, hi;
+                    chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
+                    for (int kb = lo; kb < hi; ++kb) {
+                        if (!mbar_wait(smem_u32(&empty[stage]), phase ^ 1, abort_flag, a.err, 1)) {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t fb = smem_u32(&full[stage]);
+                        mbar_expect_tx(fb, STAGE_A + STAGE_B);
+                        tma_load_3d(smem_u32(sA + stage * STAGE_A), &tmA, fb, tl.a_k0 + kb * BK, tl.m0, pr.ia);
+                        tma_load_3d(smem_u32(sB + stage * STAGE_B), &tmB, fb, tl.b_k0 + kb * BK, tl.n0, pr.ib);
+                        issued_mask |= 1u << stage;
+                        last_par = (last_par & ~(1u << stage)) | (phase << stage);
+                        if (++stage == STAGES) { stage = 0; phase ^= 1; }
+                    }
+                }
+            }
+            if (!ok) {
+                // let the copies already issued land before the CTA leaves
+                for (int s = 0; s < STAGES; ++s)
+                    if (issued_mask & (1u << s))
+                        mbar_wait(smem_u32(&full[s]), (last_par >> s) & 1, abort_flag, a.err, 1, true);
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer (one thread)
+        if (lane == 0) {
+            uint32_t stage = 0, phase = 0, acc_cnt = 0;
+            bool ok = true, any = false;
+            for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+                const Tile tl = a.tiles[t];
+                for (int p = 0; p < a.nprods && ok; ++p) {
+                    const Prod pr = a.prods[p];
+                    int lo, hi;
+                    chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
+                    if (hi <= lo) continue;
+                    const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
+                    if (!mbar_wait(smem_u32(&accempty[b]), aphase ^ 1, abort_flag, a.err, 2)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tmem + b * BN;
+                    for (int kb = lo; kb < hi; ++kb) {
+                        if (!mbar_wait(smem_u32(&full[stage]), phase, abort_flag, a.err, 3)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint64_t ad = smem_desc(smem_u32(sA + stage * STAGE_A));
+                        const uint64_t bd = smem_desc(smem_u32(sB + stage * STAGE_B));
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; ++kk)
+                            mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (kb > lo || kk > 0) ? 1u : 0u);
+                        any = true;
+                        mma_commit(smem_u32(&empty[stage]));
+                        if (++stage == STAGES) { stage = 0; phase ^= 1; }
+                    }
+                    if (!ok) break;
+                    mma_commit(smem_u32(&accfull[b]));
+                    ++acc_cnt;
+                }
+            }
+            if (any) {
+                // all MMAs of this CTA complete before TMEM is released
+                mma_commit(smem_u32(drain));
+                mbar_wait(smem_u32(drain), 0, abort_flag, a.err, 4, true);
+            }
+        }
+    } else {
+        // ---------------- epilogue: warps 2..5, one TMEM lane (output row) per thread
+        const int q = warp & 3;
+        const int row_in_tile = q * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        const float c_l1 = a.c_l1, c_nnz = a.c_nnz, c_rec = a.c_rec;
+        const float two24 = 16777216.0f;
+        uint32_t acc_cnt = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+            const Tile tl = a.tiles[t];
+            bool first = true;
+            for (int p = 0; p < a.nprods && ok; ++p) {
+                const Prod pr = a.prods[p];
+                int lo, hi;
+                chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
+                if (hi <= lo) continue;
+                const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
+                if (!mbar_wait(smem_u32(&accfull[b]), aphase, abort_flag, a.err, 5)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const float w = pow2f(-pr.t * a.beta);
+#pragma unroll 1
+                for (int c = 0; c < BN / 32; ++c) {
+                    uint32_t acc[32], hi_r[32], lo_r[32];
+                    tmem_ld32(tmem + lane_off + b * BN + c * 32, acc);
+                    if (!first) {
+                        tmem_ld32(tmem + lane_off + 256 + c * 32, hi_r);
+                        tmem_ld32(tmem + lane_off + 384 + c * 32, lo_r);
+                    }
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const float x = __fmul_rn(__uint_as_float(acc[j]), w);
+                        if (first) {
+                            hi_r[j] = __float_as_uint(x);
+                            lo_r[j] = 0u;
+                        } else {
+                            const float h = __uint_as_float(hi_r[j]);
+                            const float s = __fadd_rn(h, x);
+                            const float bb = __fsub_rn(s, h);
+                            const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+                            // renormalise (hi, lo) so |lo| <= ulp(hi)/2 after every product
+                            const float tt = __fadd_rn(__uint_as_float(lo_r[j]), e);
+                            const float nh = __fadd_rn(s, tt);
+                            hi_r[j] = __float_as_uint(nh);
+                            lo_r[j] = __float_as_uint(__fsub_rn(tt, __fsub_rn(nh, s)));
+                        }
+                    }
+                    tmem_st32(tmem + lane_off + 256 + c * 32, hi_r);
+                    tmem_st32(tmem + lane_off + 384 + c * 32, lo_r);
+                }
+                tmem_wait_st();
+                tc_fence_before();
+                mbar_arrive(smem_u32(&accempty[b]));
+                ++acc_cnt;
+                first = false;
+            }
+            if (!ok) break;
+            // ---- finalize the tile: value, certified bound, flags
+            const int r = tl.m0 + row_in_tile;
+            const bool rvalid = r < a.rows_valid;
+            const int eA = a.A.e[r];
+            const float l1A = a.A.l1[r];
+            const int nnzA = a.A.nnz[r];
+            const float inA = a.A.inerr ? a.A.inerr[r] : 0.0f;
+            float dnA[MAX_CHUNKS];
+#pragma unroll
+            for (int c = 0; c < MAX_CHUNKS; ++c) dnA[c] = c < a.nchunks ? a.A.dn[(long)r * a.nchunks + c] : 0.0f;
+            float rowerr = 0.0f;
+            double* orow = a.out + (long)r * a.ldo;
+#pragma unroll 1
+            for (int c = 0; c < BN / 32; ++c) {
+                uint32_t hi_r[32], lo_r[32];
+                if (!first) {
+                    tmem_ld32(tmem + lane_off + 256 + c * 32, hi_r);
+                    tmem_ld32(tmem + lane_off + 384 + c * 32, lo_r);
+                    tmem_wait_ld();
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) { hi_r[j] = 0u; lo_r[j] = 0u; }
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int col = tl.n0 + c * 32 + j;
+                    const float hf = __uint_as_float(hi_r[j]);
+                    const double R = (double)hf + (double)__uint_as_float(lo_r[j]);
+                    const int eB = a.B.e[col];
+                    const double v = R * pow2d(eA + eB - 2 * a.beta);
+                    orow[col] = v;
+                    const int nnzB = a.B.nnz[col];
+                    if (nnzA == 0 || nnzB == 0) continue;
+                    const float l1B = a.B.l1[col];
+                    float bound = __fmaf_ru(c_l1, __fadd_ru(l1A, l1B), 0.0f);
+                    bound = __fmaf_ru(c_nnz, (float)min(nnzA, nnzB), bound);
+                    bound = __fmaf_ru(c_rec, fminf(l1A, l1B), bound);
+                    bound = __fmaf_ru(inA, l1B, bound);
+                    bool exact = true;
+#pragma unroll
+                    for (int cc = 0; cc < MAX_CHUNKS; ++cc)
+                        if (cc < a.nchunks && __fmul_ru(dnA[cc], a.B.dn[(long)col * a.nchunks + cc]) >= two24)
+                            exact = false;
+                    if (a.rowerr_units) rowerr = fmaxf(rowerr, __fmul_ru(bound, pow2f(max(-126, min(127, eB)))));
+                    bool flag = !exact;
+                    if (a.flag_mode == 1) flag = flag || (bound > a.tol * fabsf(hf) * pow2f(-2 * a.beta));
+                    if (flag && rvalid && col < a.cols_valid) {
+                        const unsigned int idx = atomicAdd(a.nflags, 1u);
+                        if ((int)idx < a.max_flags) a.flags[idx] = make_int2(r, col);
+                    }
+                }
+            }
+            if (a.rowerr_units && rvalid && rowerr > 0.0f)
+                atomicMax((int*)&a.rowerr_units[r], __float_as_int(rowerr));
+            // make sure TMEM reads finished before the next tile overwrites hi/lo
+            tc_fence_before();
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// ------------------------------------------------------------------- slicing
+__device__ __forceinline__ unsigned long long rne_shr(unsigned long long m, int k) {
+    if (k <= 0) return m;
+    if (k > 55) return 0ull;
+    const unsigned long long q = m >> k;
+    const unsigned long long rem = m & ((1ull << k) - 1ull);
+    const unsigned long long half = 1ull << (k - 1);
+    return (rem > half || (rem == half && (q & 1ull))) ? q + 1ull : q;
+}
+
+constexpr int SLICE_THREADS = 256;
+
+__global__ void __launch_bounds__(SLICE_THREADS)
+k_slice(const SliceArgs a) {
+    const int row = blockIdx.x;
+    const int tid = threadIdx.x;
+    const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
+    const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
+    __shared__ unsigned long long red_u[SLICE_THREADS / 32];
+    __shared__ float red_f[SLICE_THREADS / 32];
+    __shared__ int red_i[SLICE_THREADS / 32];
+    __shared__ unsigned int red_d[SLICE_THREADS / 32][MAX_SLICES * MAX_CHUNKS];
+
+    // pass 1: max |x| through the IEEE bit pattern (integer compares only)
+    unsigned long long mx = 0;
+    for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+        const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
+        mx = b > mx ? b : mx;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+    }
+    if ((tid & 31) == 0) red_u[tid >> 5] = mx;
+    __syncthreads();
+    mx = 0;
+    for (int w = 0; w < SLICE_THREADS / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
+    if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
+    const int Emax = (int)(mx >> 52);
+    const bool zero_row = (mx == 0);
+    const int e = zero_row ? 0 : (Emax > 0 ? Emax - 1022 : -1022);
+    const int s = a.slices, beta = a.beta;
+    const int q = s * beta;
+    const long sstride = a.slice_stride;
+    __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
+
+    float l1 = 0.0f;
+    int nnz = 0;
+    unsigned int dsq[MAX_SLICES * MAX_CHUNKS];
+#pragma unroll
+    for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i) dsq[i] = 0u;
+    const long mask = (1l << beta) - 1l, halfb = 1l << (beta - 1);
+    const float inv2q = pow2f(-q);
+    for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+        const unsigned long long bits = src[c];
+        const int dc = a.col_map ? a.col_map[c] : c;
+        const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
+        long long I = 0;
+        if (!zero_row && ab != 0 && ab < 0x7FF0000000000000ull) {
+            const int E = (int)(ab >> 52);
+            unsigned long long mant = ab & 0xFFFFFFFFFFFFFull;
+            int ex;
+            if (E > 0) { mant |= 1ull << 52; ex = E - 1075; }
+            else ex = -1074;
+            const int sh = ex + q - e;
+            const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
+            I = (bits >> 63) ? -(long long)m : (long long)m;
+        }
+        int chunk = 0;
+        for (int cc = 1; cc < a.nchunks; ++cc)
+            if (dc / BK >= (int)(((long)cc * a.nkb_total) / a.nchunks)) chunk = cc;
+        long long v = I;
+        int d[MAX_SLICES];
+#pragma unroll
+        for (int i = MAX_SLICES - 1; i >= 1; --i) {
+            if (i < s) {
+                long r = (long)(v & mask);
+                if (r > halfb) r -= (1l << beta);
+                d[i] = (int)r;
+                v = (v - r) >> beta;
+            } else {
+                d[i] = 0;
+            }
+        }
+        d[0] = (int)v;
+#pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i) {
+            if (i < s) {
+                drow[i * sstride + dc] = __float2bfloat16_rn((float)d[i]);
+#pragma unroll
+                for (int cc = 0; cc < MAX_CHUNKS; ++cc)
+                    if (cc == chunk) dsq[i * MAX_CHUNKS + cc] += (unsigned int)(d[i] * d[i]);
+            }
+        }
+        if (I != 0) {
+            ++nnz;
+            const unsigned long long aI = (unsigned long long)(I < 0 ? -I : I);
+            l1 = __fadd_ru(l1, __fmul_ru(__ull2float_ru(aI), inv2q));
+        }
+    }
+    // block reductions
+    for (int o = 16; o > 0; o >>= 1) {
+        l1 = __fadd_ru(l1, __shfl_xor_sync(0xffffffffu, l1, o));
+        nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
+    }
+#pragma unroll
+    for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i)
+        for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
+    if ((tid & 31) == 0) {
+        red_f[tid >> 5] = l1;
+        red_i[tid >> 5] = nnz;
+#pragma unroll
+        for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i) red_d[tid >> 5][i] = dsq[i];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float L = 0.0f;
+        int N = 0;
+        for (int w = 0; w < SLICE_THREADS / 32; ++w) { L = __fadd_ru(L, red_f[w]); N += red_i[w]; }
+        // the bound uses |x 2^-e|; digits represent it to within 2^{-q-1} per entry
+        L = __fadd_ru(L, __fmul_ru((float)N, pow2f(-q - 1)));
+        a.st.e[row] = e;
+        a.st.l1[row] = L;
+        a.st.nnz[row] = N;
+        for (int c = 0; c < a.nchunks; ++c) {
+            unsigned int m = 0;
+            for (int i = 0; i < s; ++i) {
+                unsigned int t = 0;
+                for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
+                m = t > m ? t : m;
+            }
+            a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__uint2float_ru(m));
+        }
+        if (a.st.inerr) {
+            float v = 0.0f;
+            if (a.inerr_prev && !zero_row) {
+                const int de = a.e_prev[row] - e;
+                v = __fmul_ru(a.inerr_prev[row], pow2f(max(-126, min(127, de))));
+                if (de > 127) v = __int_as_float(0x7f800000);   // cannot certify: infinite bound
+            }
+            a.st.inerr[row] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------- band builder
+__device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
+
+__global__ void k_band(const BandArgs a) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)a.fpad * a.W) return;
+    const int row = (int)(idx / a.W), w = (int)(idx - (long)row * a.W);
+    double val = 0.0;
+    const int rF = a.f_prim[row];
+    const int kc = a.band_k0[row] + w;
+    if (rF >= 0 && kc < a.kpadI) {
+        const int rI = a.i_prim[kc];
+        if (rI >= 0) {
+            const int kI = a.KI[rI], kF = a.KF[rF];
+            const int vF = a.vibF[rF];
+            if (abs(kI - kF) <= 1 && vF >= a.startF && vF < a.endF) {
+                const int tI = a.tauI[rI], tF = a.tauF[rF] & 1;
+                const int eq = (kF == kI), neq = !eq, tneq = (tF != tI);
+                const int didx = 2 * eq + neq * (!tneq);
+                const int c = (tF - tI) * eq + (tF - tI) * (kF - kI) * neq * tneq - neq * (!tneq);
+                if (c != 0) {
+                    const int n = a.jmax + 1;
+                    double m = a.threej[a.jI + kI * n + (a.jF - a.jI + 1) * n * n + (kF - kI + 1) * n * n * 3];
+                    if (kI != kF && kI * kF != 0) m = __dmul_rn(m, kSqrt2Ref);
+                    m = __dmul_rn(m, (double)c * parity_sign((kI % 3) * tI + kI) * parity_sign((kF % 3) * tF));
+                    const double mu = a.dipole[(long)(vF - a.startF) + (long)a.vibI[rI] * a.ncontrF +
+                                               (long)didx * a.dipN * a.ncontrF];
+                    m = __dmul_rn(m, mu);
+                    m = __dmul_rn(m, __dmul_rn(a.i_coef[kc], a.f_coef[row]));
+                    val = m;
+                }
+            }
+        }
+    }
+    a.band[idx] = val;
+}
+
+// ------------------------------------------------------------------- refinement
+__global__ void k_refine_h(const RefineHArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = min((int)*a.nflags, a.max_flags);
+    for (int f = gw; f < n; f += nw) {
+        const int2 rc = a.flags[f];
+        const int r = rc.x, c = rc.y;
+        const double* v = a.vecs + (long)a.row_level[r] * a.nsize;
+        const double* b = a.band + (long)c * a.W;
+        const int k0 = a.band_k0[c], len = a.band_len[c];
+        double acc = 0.0, aacc = 0.0;
+        for (int w = lane; w < len; w += 32) {
+            const int s = a.i_sym[k0 + w];
+            if (s < 0) continue;
+            const double p = v[s] * b[w];
+            acc = __fma_rn(v[s], b[w], acc);
+            aacc += fabs(p);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            aacc += __shfl_xor_sync(0xffffffffu, aacc, o);
+        }
+        if (lane == 0) {
+            a.H[(long)r * a.ldh + c] = acc;
+            // rounding error of this FP64 sum (gamma_n with n <= len + 32), in units of 2^{eA}
+            const double err = aacc * (double)(len + 64) * 1.1102230246251565e-16 * 1.01;
+            const float u = __double2float_ru(err * pow2d(-a.eA[r]));
+            atomicMax((int*)&a.rowerr_units[r], __float_as_int(u));
+        }
+    }
+}
+
+__global__ void k_refine_amp(const RefineAmpArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = min((int)*a.nflags, a.max_flags);
+    for (int f = gw; f < n; f += nw) {
+        const int2 rc = a.flags[f];
+        const int r = rc.x, c = rc.y;
+        const double* u = a.U + (long)a.col_level[c] * a.nsize;
+        const double* h = a.H + (long)r * a.ldh;
+        double acc = 0.0, aacc = 0.0, l1 = 0.0;
+        for (int s = lane; s < a.nsize; s += 32) {
+            const double uv = u[s], hv = h[a.colpos[s]];
+            acc = __fma_rn(uv, hv, acc);
+            aacc += fabs(uv * hv);
+            l1 += fabs(uv);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            aacc += __shfl_xor_sync(0xffffffffu, aacc, o);
+            l1 += __shfl_xor_sync(0xffffffffu, l1, o);
+        }
+        if (lane == 0) {
+            a.amp[(long)r * a.lda + c] = acc;
+            const double herr = (double)a.h_inerr[r] * pow2d(a.eH[r]);
+            const double bound = herr * l1 * 1.001 + aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
+            if (!(bound <= a.tol * fabs(acc))) atomicAdd(a.uncertified, 1ull);
+        }
+    }
+}
+
+}  // namespace
+
+size_t gemm_smem_bytes() {
+    return (size_t)STAGES * (STAGE_A + STAGE_B) + 1024 /* align slack */ + 256 /* barriers */;
+}
+
+cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a,
+                        int num_sms, cudaStream_t st) {
+    static bool attr_set = false;
+    const size_t smem = gemm_smem_bytes();
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_digit_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    if (a.ntiles <= 0) return cudaSuccess;
+    const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
+    k_digit_gemm<<<grid, NTHREADS, smem, st>>>(tmA, tmB, a);
+    return cudaGetLastError();
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &qr) !=
+                cudaSuccess || qr != cudaDriverEntryPointSuccess || !p)
+            return false;
+        fn = (EncodeTiledFn)p;
+    }
+    if (((uintptr_t)base & 15) || (kpad % BK) || (rows_pad % BM)) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)slices};
+    cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)kpad * 2 * (cuuint64_t)rows_pad};
+    cuuint32_t box[3] = {BK, BM, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st) {
+    if (a.nrows <= 0) return cudaSuccess;
+    k_slice<<<a.nrows, SLICE_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_band(const BandArgs& a, cudaStream_t st) {
+    const long total = (long)a.fpad * a.W;
+    if (total <= 0) return cudaSuccess;
+    k_band<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_h(const RefineHArgs& a, int max_blocks, cudaStream_t st) {
+    k_refine_h<<<max_blocks, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_amp(const RefineAmpArgs& a, int max_blocks, cudaStream_t st) {
+    k_refine_amp<<<max_blocks, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace split
+}  // namespace gain

@@ -1,0 +1,162 @@
+// Split-precision (Ozaki-style) tensor-core path: internal interface.
+//
+// Every FP64 operand row x is written as x = 2^e (sum_{i<s} d_i 2^{-(i+1) beta} + r),
+// |r| <= 2^{-s beta - 1}, with balanced integer digits d_i (|d_0| <= 2^beta,
+// |d_i| <= 2^{beta-1}) stored as BF16 (exact for beta <= 8).  A product of two rows is
+// sum over digit pairs (i, j), i + j < s, of an integer dot product computed exactly by
+// BF16 tcgen05 MMAs with FP32 accumulation (exact while every partial sum is an integer
+// below 2^24, certified per output by Cauchy-Schwarz on per-row digit norms), weighted
+// by 2^{-(i+j) beta} and summed in double-float in tensor memory.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace gain {
+namespace split {
+
+constexpr int BM = 128;     // output rows per tile (TMEM lanes)
+constexpr int BN = 128;     // output columns per tile
+constexpr int BK = 64;      // inner elements per stage (one 128-byte swizzle row of BF16)
+constexpr int STAGES = 6;
+constexpr int MAX_CHUNKS = 4;
+constexpr int MAX_SLICES = 10;
+
+struct Tile {
+    int m0, n0;     // first output row (A row) / column (B row)
+    int a_k0;       // A inner coordinate of k-block 0
+    int b_k0;       // B inner coordinate of k-block 0
+    int nkb;        // k-blocks of BK
+    int pad[3];
+};
+
+struct Prod {
+    int ia, ib;     // digit index of A and of B
+    int t;          // ia + ib (weight 2^{-t beta})
+    int chunk;      // inner-dimension chunk
+};
+
+// Per-row data of a sliced operand.
+struct RowStats {
+    int* e;          // scale exponent (row values < 2^e)
+    float* l1;       // sum |x| 2^{-e}, rounded up
+    int* nnz;        // non-zero count
+    float* dn;       // [rows * nchunks]: max_i ||d_i restricted to chunk||_2, rounded up
+    float* inerr;    // optional: input error of the row in units of 2^e (rounded up)
+};
+
+struct GemmArgs {
+    const Tile* tiles;
+    int ntiles;
+    const Prod* prods;
+    int nprods;
+    int nchunks;
+    int beta;
+    int slices;
+    double* out;
+    long ldo;
+    RowStats A, B;
+    // bound constants (units of 2^{eA+eB})
+    float c_l1, c_nnz, c_rec;
+    // GEMM1: per-row maximum bound in units of 2^{eA} (atomic max on float bits), may be null
+    float* rowerr_units;
+    // flags
+    int flag_mode;          // 0: inexact accumulation only; 1: also bound > tol |value|
+    float tol;
+    int2* flags;
+    unsigned int* nflags;
+    int max_flags;
+    int rows_valid, cols_valid;
+    int* err;               // device error word (0 ok, else timeout code)
+};
+
+size_t gemm_smem_bytes();
+cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a,
+                        int num_sms, cudaStream_t st);
+
+// Tensor map of a digit array [slices][rows_pad][kpad] BF16 (box 64 x 128 x 1, 128B swizzle).
+bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices);
+
+struct SliceArgs {
+    const double* src;      // source rows
+    long ld_src;
+    const int* src_rows;    // optional source row per output row
+    int nrows;              // output rows to produce
+    int ncols;              // source columns
+    const int* col_map;     // optional destination column per source column
+    int kpad;               // destination row length
+    long slice_stride;      // rows_pad * kpad
+    __nv_bfloat16* digits;
+    int slices, beta;
+    int nchunks;            // chunks of the destination inner dimension for dn
+    int nkb_total;          // k-blocks of BK the chunks split (chunk c: [c n/nch, (c+1) n/nch))
+    RowStats st;
+    const float* inerr_prev;   // optional: row error in units of 2^{e_prev}
+    const int* e_prev;         // exponent those units refer to
+};
+cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st);
+
+// Rotational-dipole band matrix of one block pair (rows: padded upper functions,
+// columns: W band positions starting at band_k0[row] of the padded lower layout).
+struct BandArgs {
+    int fpad, W;
+    const int* f_prim;      // primitive index of each padded upper row (-1: padding)
+    const double* f_coef;
+    const int* band_k0;
+    int kpadI;
+    const int* i_prim;      // primitive index of each padded lower column (-1: padding)
+    const double* i_coef;
+    const int *KI, *tauI, *vibI, *KF, *tauF, *vibF;
+    int jI, jF, jmax;
+    const double* threej;
+    const double* dipole;
+    int dipN, startF, endF, ncontrF;
+    double* band;
+};
+cudaError_t launch_band(const BandArgs& a, cudaStream_t st);
+
+// FP64 recomputation of flagged first-GEMM outputs (H entries).
+struct RefineHArgs {
+    const int2* flags;
+    const unsigned int* nflags;
+    int max_flags;
+    const double* vecs;     // lower eigenvectors [levels][nsize]
+    int nsize;
+    const int* row_level;   // level of each batch row
+    const int* i_sym;       // symmetry index of each padded lower column (-1: padding)
+    const int* band_k0;
+    const int* band_len;    // per padded upper row
+    const double* band;
+    int W;
+    double* H;
+    long ldh;
+    const int* eA;
+    float* rowerr_units;
+};
+cudaError_t launch_refine_h(const RefineHArgs& a, int max_blocks, cudaStream_t st);
+
+// FP64 recomputation of flagged amplitudes.
+struct RefineAmpArgs {
+    const int2* flags;
+    const unsigned int* nflags;
+    int max_flags;
+    const double* U;        // upper eigenvectors [levels][nsize]
+    int nsize;
+    const int* col_level;   // level of each output column
+    const int* colpos;      // padded position of each upper symmetry index
+    const double* H;
+    long ldh;
+    const float* h_inerr;   // first-GEMM error of each H row in units of 2^{eH}
+    const int* eH;
+    double* amp;
+    long lda;
+    double tol;
+    unsigned long long* uncertified;
+};
+cudaError_t launch_refine_amp(const RefineAmpArgs& a, int max_blocks, cudaStream_t st);
+
+}  // namespace split
+}  // namespace gain

@@ -1,0 +1,294 @@
+"""Python host binding of libgainls.so (the C ABI declared in include/gain_ls.h).
+
+The library is the product; this module only marshals arguments through ctypes.  It never
+falls back to a CPU implementation: if the shared library is missing, every call raises.
+
+    import gainls
+    eng = gainls.Engine(jmax=11, nsym=4, maxdeg=1)
+    gainls.upload_problem(eng, problem)          # a synth.Problem
+    stats = eng.run_pair(job, gainls.PATH_SPLIT)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgainls.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "gain_ls.h")
+
+PATH_PLAIN_FP64 = 0
+PATH_SPLIT = 1
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_TOL_NOT_MET, ERR_NOT_READY, ERR_UNSUPPORTED = range(8)
+
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+
+class GainError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_status_name(status)}: {message}")
+        self.status = status
+
+
+class PairJob(ctypes.Structure):
+    _fields_ = [("jindI", ctypes.c_int), ("gammaI", ctypes.c_int), ("jindF", ctypes.c_int),
+                ("gammaF", ctypes.c_int), ("nlower", ctypes.c_int), ("lower_levels", _ip),
+                ("nupper", ctypes.c_int), ("upper_levels", _ip)]
+
+
+class SplitOpts(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("slices", ctypes.c_int), ("beta", ctypes.c_int),
+                ("kchunks", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("rows", ctypes.c_longlong), ("cols", ctypes.c_longlong),
+                ("refined", ctypes.c_longlong), ("uncertified", ctypes.c_longlong),
+                ("inexact", ctypes.c_longlong),
+                ("beta1", ctypes.c_int), ("slices1", ctypes.c_int), ("chunks1", ctypes.c_int),
+                ("beta2", ctypes.c_int), ("slices2", ctypes.c_int), ("chunks2", ctypes.c_int),
+                ("products1", ctypes.c_int), ("products2", ctypes.c_int),
+                ("kernel_launches", ctypes.c_int),
+                ("gemm1_ms", ctypes.c_double), ("gemm2_ms", ctypes.c_double),
+                ("tensor_flops", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LineParams(ctypes.Structure):
+    _fields_ = [("temperature", ctypes.c_double), ("q_part", ctypes.c_double), ("zpe", ctypes.c_double),
+                ("thresh", ctypes.c_double), ("freq_lo", ctypes.c_double), ("freq_hi", ctypes.c_double),
+                ("gnsF", ctypes.c_double), ("ndegI", ctypes.c_int), ("ndegF", ctypes.c_int),
+                ("reduced", ctypes.c_int)]
+
+
+_lib = None
+
+
+def _status_name(s: int) -> str:
+    names = ["GAIN_OK", "GAIN_ERR_INVALID_ARG", "GAIN_ERR_OOM", "GAIN_ERR_CUDA", "GAIN_ERR_TIMEOUT",
+             "GAIN_ERR_TOL_NOT_MET", "GAIN_ERR_NOT_READY", "GAIN_ERR_UNSUPPORTED"]
+    return names[s] if 0 <= s < len(names) else f"status {s}"
+
+
+def lib():
+    """Load libgainls.so; raise if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with gain-mpi_gb300/build.py "
+                               "(or __graft_entry__.build()); there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _declare(L):
+    I, D, S = ctypes.c_int, ctypes.c_double, ctypes.c_int
+    L.gain_last_error_string.restype = ctypes.c_char_p
+    L.gain_status_string.restype = ctypes.c_char_p
+    L.gain_status_string.argtypes = [I]
+    L.gain_abi_version.restype = I
+    L.gain_hls_kblock.argtypes = [I, I, I, I, I, _vp, _vp, _vp, _vp, I, I, I, I, I, I, _vp, _vp, _vp,
+                                  _vp, _vp, I, I, _vp]
+    L.gain_expand.argtypes = [I, I, I, I, I, I, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.gain_dot.argtypes = [I, _vp, _vp, _vp, _vp]
+    L.gain_threej_table.argtypes = [I, _dp]
+    L.gain_engine_create.argtypes = [I, I, I, I, ctypes.POINTER(_vp)]
+    L.gain_engine_destroy.argtypes = [_vp]
+    L.gain_upload_basis.argtypes = [_vp, I, I, I, _ip, _ip, _ip, _ip, _ip]
+    L.gain_upload_inflation.argtypes = [_vp, I, _ip, _ip, I, I, I, ctypes.POINTER(_ip), ctypes.POINTER(_dp),
+                                        _ip, _ip]
+    L.gain_upload_dipole.argtypes = [_vp, _dp, I, I, I, I]
+    L.gain_upload_eigvecs.argtypes = [_vp, I, I, I, I, _dp]
+    L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
+    L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
+    L.gain_fetch_amp.argtypes = [_vp, _dp]
+    L.gain_pair_lines.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, _dp, _dp, _dp,
+                                  ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_longlong)]
+    L.gain_format_line.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
+    L.gain_format_line.restype = I
+    for name in ("gain_hls_kblock", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
+                 "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
+                 "gain_upload_eigvecs", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_pair_lines"):
+        getattr(L, name).restype = S
+
+
+def check(status: int):
+    if status != OK:
+        msg = lib().gain_last_error_string().decode(errors="replace")
+        raise GainError(status, msg)
+
+
+def declared_symbols() -> list[str]:
+    """Every function name include/gain_ls.h declares."""
+    import re
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(gain_[a-z0-9_]+)\s*\(", text)))
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+# --------------------------------------------------------------------------- layer 1
+def threej_table(jmax: int) -> np.ndarray:
+    t = np.zeros((jmax + 1) * (jmax + 1) * 9, np.float64)
+    check(lib().gain_threej_table(jmax, _p(t, _dp)))
+    return t
+
+
+def hls_kblock(dimenF, dimenI, jI, jF, kF, tauI, tauF, icorrI, icorrF, startF_idx, startI_idx,
+               startFblock, endFblock, ncontrF, kFBlocksize, kblock_size, dipole_me, vector, threej,
+               half_ls, jmax, dip_stride, stream=0):
+    """Drop-in K-block kernel; pointer arguments are device addresses (ints)."""
+    check(lib().gain_hls_kblock(dimenF, dimenI, jI, jF, kF, tauI, tauF, icorrI, icorrF, startF_idx,
+                                startI_idx, startFblock, endFblock, ncontrF, kFBlocksize, kblock_size,
+                                dipole_me, vector, threej, half_ls, jmax, dip_stride, stream))
+
+
+def expand(dimenI, igammaI, maxcoeff, idegI, sdeg, Ntot, ijterms, icontr, N, repres, vecI, vec, stream=0):
+    check(lib().gain_expand(dimenI, igammaI, maxcoeff, idegI, sdeg, Ntot, ijterms, icontr, N, repres,
+                            vecI, vec, stream))
+
+
+def dot(n, x, y, result, stream=0):
+    check(lib().gain_dot(n, x, y, result, stream))
+
+
+def format_line(nu, indexF, jF, gammaF, indexI, jI, gammaI, A, intensity=None, amps=None) -> str:
+    buf = ctypes.create_string_buffer(4096)
+    a = _f64(amps) if amps is not None else None
+    n = lib().gain_format_line(buf, 4096, nu, indexF, jF, gammaF, indexI, jI, gammaI, A,
+                               int(intensity is not None), 0.0 if intensity is None else intensity,
+                               _p(a, _dp) if a is not None else None, 0 if a is None else len(a))
+    return buf.raw[:n].decode()
+
+
+# --------------------------------------------------------------------------- layer 2
+class Engine:
+    def __init__(self, jmax: int, nsym: int, maxdeg: int = 1, device: int = 0):
+        h = _vp()
+        check(lib().gain_engine_create(device, jmax, nsym, maxdeg, ctypes.byref(h)))
+        self.h = h
+        self.nsym = nsym
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            lib().gain_engine_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_basis(self, jind, J, K, tau, vib, kblock, kstart):
+        K, tau, vib, kblock, kstart = map(_i32, (K, tau, vib, kblock, kstart))
+        check(lib().gain_upload_basis(self.h, jind, J, len(K), _p(K, _ip), _p(tau, _ip), _p(vib, _ip),
+                                      _p(kblock, _ip), _p(kstart, _ip)))
+
+    def upload_inflation(self, jind, icontr, ijterms, dimen, maxcoeff, matsize, N, repres, Ntot, sdeg):
+        icontr, ijterms, Ntot, sdeg = map(_i32, (icontr, ijterms, Ntot, sdeg))
+        Ns = [_i32(x) for x in N]
+        Rs = [_f64(x) for x in repres]
+        Np = (_ip * len(Ns))(*[_p(x, _ip) for x in Ns])
+        Rp = (_dp * len(Rs))(*[_p(x, _dp) for x in Rs])
+        check(lib().gain_upload_inflation(self.h, jind, _p(icontr, _ip), _p(ijterms, _ip), dimen, maxcoeff,
+                                          matsize, Np, Rp, _p(Ntot, _ip), _p(sdeg, _ip)))
+
+    def upload_dipole(self, piece, N, startF, endF, ncontrF):
+        piece = _f64(piece)
+        check(lib().gain_upload_dipole(self.h, _p(piece, _dp), N, startF, endF, ncontrF))
+
+    def upload_eigvecs(self, jind, gamma, vecs):
+        vecs = _f64(vecs)
+        check(lib().gain_upload_eigvecs(self.h, jind, gamma, vecs.shape[0], vecs.shape[1], _p(vecs, _dp)))
+
+    def run_pair(self, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
+                 upper_levels: Sequence[int], path: int = PATH_SPLIT, tol: float = 0.0,
+                 slices: int = 0, beta: int = 0, kchunks: int = 0, raise_on_error: bool = True) -> dict:
+        lo, up = _i32(lower_levels), _i32(upper_levels)
+        job = PairJob(jindI, gammaI, jindF, gammaF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
+        opts = SplitOpts(tol, slices, beta, kchunks)
+        st = Stats()
+        s = lib().gain_run_pair(self.h, ctypes.byref(job), path, ctypes.byref(opts), ctypes.byref(st))
+        self._shape = (len(lo), len(up))
+        out = st.as_dict()
+        out["status"] = s
+        if s != OK:
+            out["error"] = lib().gain_last_error_string().decode(errors="replace")
+            if raise_on_error:
+                check(s)
+        return out
+
+    def amp_device(self):
+        p, ld = ctypes.c_void_p(), ctypes.c_int()
+        check(lib().gain_pair_amp_device(self.h, ctypes.byref(p), ctypes.byref(ld)))
+        return p.value, ld.value
+
+    def fetch_amp(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self._shape, np.float64)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self._shape[0] * self._shape[1]
+        check(lib().gain_fetch_amp(self.h, _p(out, _dp)))
+        return out.reshape(self._shape)
+
+    def lines(self, eI, eF, jI, jF, temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0,
+              freq=(-1e9, 1e9), gnsF=1.0, intensity=True, want=("S", "A", "I", "keep")):
+        eI, eF = _f64(eI), _f64(eF)
+        n = self._shape[0] * self._shape[1]
+        prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
+        S = np.empty(n) if "S" in want else None
+        A = np.empty(n) if "A" in want else None
+        I = np.empty(n) if (intensity and "I" in want) else None
+        K = np.empty(n, np.uint8) if "keep" in want else None
+        nl = ctypes.c_longlong()
+        check(lib().gain_pair_lines(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF,
+                                    _p(S, _dp) if S is not None else None,
+                                    _p(A, _dp) if A is not None else None,
+                                    _p(I, _dp) if I is not None else None,
+                                    K.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)) if K is not None else None,
+                                    ctypes.byref(nl)))
+        shp = self._shape
+        return {"S": None if S is None else S.reshape(shp), "A": None if A is None else A.reshape(shp),
+                "I": None if I is None else I.reshape(shp), "keep": None if K is None else K.reshape(shp),
+                "n_lines": nl.value}
+
+
+def upload_problem(eng: Engine, p, dipole_block=None, blocks=None):
+    """Upload a synth.Problem: bases, expansion tables, dipole piece, eigenvectors."""
+    for jind, b in enumerate(p.bases):
+        eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
+        inf = p.infl[jind]
+        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, 1, inf.N, inf.repres,
+                             inf.Ntot, inf.sdeg)
+    nv = p.dipole.shape[-1]
+    if dipole_block is None:
+        eng.upload_dipole(p.dipole.reshape(-1), nv, 0, nv, nv)
+    else:
+        s, e = dipole_block
+        piece = np.ascontiguousarray(p.dipole[:, :, s:e])
+        eng.upload_dipole(piece.reshape(-1), nv, s, e, e - s)
+    for (jind, g), blk in p.blocks.items():
+        if blocks is None or (jind, g) in blocks:
+            eng.upload_eigvecs(jind, g, blk.vecs)

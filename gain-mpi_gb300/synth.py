@@ -1,0 +1,272 @@
+"""Seeded synthetic stand-in for the TROVE checkpoint inputs of the line-strength path.
+
+No TROVE checkpoint files (j0_extfield.chk, j0eigen_*.chk) exist for this work, so every
+input the reference reads from them is generated here with fixed seeds:
+
+* primitive rotational-vibrational basis per J, in the K-sorted order the reference's
+  K-block kernel assumes (TroveClasses/TroveBasisSet.cpp:659-681): K ascending; K = 0 holds
+  one tau (= J mod 2), K >= 1 hold tau = 0 then tau = 1; inside each (K, tau) the
+  vibrational index v = 0 .. N_v-1.  K-block sizes are therefore N_v (K = 0) and 2 N_v.
+* symmetry classes: either one class holding the whole basis ("full"), or four classes
+  Gamma = 2 (v mod 2) + ((K + tau) mod 2) ("c4").  The pairing Gamma <-> Gamma xor 1 is
+  what the reference derives from SELECTION 1 1 2 2 (TroveClasses/TroveInput.cpp:202-236).
+  The symmetry-adapted basis of a class is the set of its primitive functions in primitive
+  order, so the expansion tables (ijterms, icontr, N, repres) describe a selection with
+  coefficient 1.0 (the reference's general expansion, GPU/dipole_GPU.cu:859-889, still runs
+  on them unchanged).
+* vibrational dipole: three N_v x N_v components, entries N(0,1) 0.5 exp(-|i-j|/20),
+  symmetrised, seed 1234, stored in the reference's flipped layout
+  piece[f + i N + d N N] (TroveClasses/TroveDipole.cpp:107-110).
+* eigenvectors of each (J, Gamma) block: Q of a QR factorisation of a seeded N(0,1) square
+  matrix (seed 1000 + 100 J + Gamma); state k has coefficient vector Q[:, k].
+* energies of each (J, Gamma) block: sorted U[0, 8000] cm^-1 (seed 5000 + 100 J + Gamma);
+  state k of the block has the k-th energy.
+"""
+from __future__ import annotations
+
+import dataclasses
+import numpy as np
+
+DIPOLE_SEED = 1234
+
+
+def vec_seed(J: int, gamma: int) -> int:
+    return 1000 + 100 * J + gamma
+
+
+def energy_seed(J: int, gamma: int) -> int:
+    return 5000 + 100 * J + gamma
+
+
+@dataclasses.dataclass
+class Basis:
+    """Primitive basis of one J: per-function K, tau, vibrational index and K-blocks."""
+    J: int
+    nv: int
+    K: np.ndarray        # int32 [dimen]
+    tau: np.ndarray      # int32 [dimen], 0/1
+    vib: np.ndarray      # int32 [dimen], J=0 contracted (vibrational) index
+    kstart: np.ndarray   # int32 [J+1]
+    kblock: np.ndarray   # int32 [J+1]
+
+    @property
+    def dimen(self) -> int:
+        return int(self.K.shape[0])
+
+
+def make_basis(J: int, nv: int) -> Basis:
+    K, tau, vib = [], [], []
+    kstart = np.zeros(J + 1, np.int32)
+    kblock = np.zeros(J + 1, np.int32)
+    pos = 0
+    for k in range(J + 1):
+        taus = [J % 2] if k == 0 else [0, 1]
+        kstart[k] = pos
+        for t in taus:
+            K.append(np.full(nv, k, np.int32))
+            tau.append(np.full(nv, t, np.int32))
+            vib.append(np.arange(nv, dtype=np.int32))
+            pos += nv
+        kblock[k] = pos - kstart[k]
+    return Basis(J, nv, np.concatenate(K), np.concatenate(tau), np.concatenate(vib),
+                 kstart, kblock)
+
+
+def classes_of(basis: Basis, rule: str) -> np.ndarray:
+    if rule == "full":
+        return np.zeros(basis.dimen, np.int32)
+    if rule == "c4":
+        return (2 * (basis.vib % 2) + ((basis.K + basis.tau) % 2)).astype(np.int32)
+    raise ValueError(f"unknown symmetry rule {rule!r}")
+
+
+def nsym_of(rule: str) -> int:
+    return {"full": 1, "c4": 4}[rule]
+
+
+def selection_of(rule: str) -> np.ndarray:
+    """isym_pairs: classes with equal entries pair up (SELECTION keyword)."""
+    return {"full": np.array([1], np.int32), "c4": np.array([1, 1, 2, 2], np.int32)}[rule]
+
+
+def igamma_pair_of(isym_pairs: np.ndarray) -> np.ndarray:
+    """Gamma -> paired Gamma, the rule of TroveInput::ComputeIGammaPair (TroveInput.cpp:202-236)."""
+    n = len(isym_pairs)
+    pair = np.arange(n, dtype=np.int32)
+    for gi in range(n):
+        found = 0
+        for gf in range(n):
+            if gi != gf and isym_pairs[gi] == isym_pairs[gf]:
+                pair[gi] = gf
+                found += 1
+                if found > 1:
+                    raise ValueError("selection rules do not come in pairs")
+    return pair
+
+
+@dataclasses.dataclass
+class Inflation:
+    """Symmetry-adapted -> primitive expansion tables of one J (GpuManager::TransferInflation)."""
+    maxcoeff: int
+    icontr: np.ndarray          # int32 [2*dimen]: irow, then ib
+    ijterms: np.ndarray         # int32 [maxcoeff*nsym]
+    N: list                     # per Gamma int32 [maxcoeff]
+    repres: list                # per Gamma float64 [Ntot*sdeg*matsize]
+    Ntot: np.ndarray            # int32 [nsym]
+    sdeg: np.ndarray            # int32 [nsym]
+    members: list               # per Gamma: primitive indices of the class, ascending
+
+
+def make_inflation(basis: Basis, cls: np.ndarray, nsym: int) -> Inflation:
+    d = basis.dimen
+    icontr = np.concatenate([np.arange(d, dtype=np.int32), np.zeros(d, np.int32)])
+    ijterms = np.zeros(d * nsym, np.int32)
+    Ns, repres, members = [], [], []
+    Ntot = np.zeros(nsym, np.int32)
+    for g in range(nsym):
+        n_g = (cls == g).astype(np.int32)
+        ijterms[g * d:(g + 1) * d] = np.concatenate([[0], np.cumsum(n_g)[:-1]]).astype(np.int32)
+        Ns.append(n_g)
+        Ntot[g] = int(n_g.sum())
+        repres.append(np.ones(int(Ntot[g]), np.float64))
+        members.append(np.nonzero(cls == g)[0].astype(np.int32))
+    return Inflation(d, icontr, ijterms, Ns, repres, Ntot, np.ones(nsym, np.int32), members)
+
+
+def make_dipole(nv: int, seed: int = DIPOLE_SEED) -> np.ndarray:
+    """[3, N, N] array whose flat order is the flipped piece layout f + i N + d N N."""
+    rng = np.random.default_rng(seed)
+    idx = np.arange(nv)
+    decay = 0.5 * np.exp(-np.abs(idx[:, None] - idx[None, :]) / 20.0)
+    out = np.empty((3, nv, nv), np.float64)
+    for d in range(3):
+        a = rng.standard_normal((nv, nv)) * decay
+        out[d] = 0.5 * (a + a.T)
+    return out
+
+
+def make_energies(n: int, J: int, gamma: int) -> np.ndarray:
+    rng = np.random.default_rng(energy_seed(J, gamma))
+    return np.sort(rng.uniform(0.0, 8000.0, n))
+
+
+def make_eigvecs(n: int, J: int, gamma: int, device: str | None = None) -> np.ndarray:
+    """Rows are state coefficient vectors (Q[:, k] of QR of a seeded Gaussian matrix).
+
+    device=None uses numpy's QR; device="cuda" runs the same factorisation through torch on
+    the GPU (used only to make large inputs quickly, never on a timed path).
+    """
+    rng = np.random.default_rng(vec_seed(J, gamma))
+    g = rng.standard_normal((n, n))
+    if device is None:
+        q, r = np.linalg.qr(g)
+        s = np.sign(np.diag(r))
+        s[s == 0] = 1.0
+        q = q * s[None, :]
+        return np.ascontiguousarray(q.T)
+    import torch
+    t = torch.from_numpy(g).to(device)
+    q, r = torch.linalg.qr(t)
+    s = torch.sign(torch.diagonal(r))
+    s[s == 0] = 1.0
+    q = q * s[None, :]
+    return np.ascontiguousarray(q.T.cpu().numpy())
+
+
+@dataclasses.dataclass
+class Block:
+    J: int
+    jind: int
+    gamma: int
+    vecs: np.ndarray      # [nlevels, Ntot]
+    energies: np.ndarray  # [nlevels]
+
+
+@dataclasses.dataclass
+class Problem:
+    nv: int
+    jvals: list
+    rule: str
+    nsym: int
+    sym_degen: np.ndarray
+    isym_pairs: np.ndarray
+    igamma_pair: np.ndarray
+    bases: list
+    infl: list
+    classes: list
+    dipole: np.ndarray
+    blocks: dict          # (jind, gamma) -> Block
+    # state table in global energy order (TroveStates::ReadStates sorts by energy)
+    st_J: np.ndarray = None
+    st_jind: np.ndarray = None
+    st_gamma: np.ndarray = None
+    st_ndeg: np.ndarray = None
+    st_ilevel: np.ndarray = None
+    st_energy: np.ndarray = None
+
+    def block_states(self, jind: int, gamma: int) -> np.ndarray:
+        """Global state indices of a block, in the block's level order."""
+        sel = np.nonzero((self.st_jind == jind) & (self.st_gamma == gamma))[0]
+        return sel[np.argsort(self.st_ilevel[sel], kind="stable")]
+
+
+def make_problem(nv: int, jvals, rule: str = "c4", blocks=None, qr_device=None,
+                 max_levels=None) -> Problem:
+    """Build bases, expansion tables, dipole and the (J, Gamma) blocks.
+
+    blocks: iterable of (J, Gamma) to materialise (default: every class of every J).
+    max_levels: optional cap on how many (lowest) levels of a block are kept.
+    """
+    nsym = nsym_of(rule)
+    isym_pairs = selection_of(rule)
+    bases, infl, classes = [], [], []
+    for J in jvals:
+        b = make_basis(J, nv)
+        c = classes_of(b, rule)
+        bases.append(b)
+        classes.append(c)
+        infl.append(make_inflation(b, c, nsym))
+    if blocks is None:
+        blocks = [(J, g) for J in jvals for g in range(nsym)]
+    blk = {}
+    for (J, g) in blocks:
+        jind = list(jvals).index(J)
+        n = int(infl[jind].Ntot[g])
+        if n == 0:
+            continue
+        vecs = make_eigvecs(n, J, g, qr_device)
+        en = make_energies(n, J, g)
+        if max_levels is not None and max_levels < n:
+            vecs, en = vecs[:max_levels], en[:max_levels]
+        blk[(jind, g)] = Block(J, jind, g, np.ascontiguousarray(vecs), en)
+    p = Problem(nv, list(jvals), rule, nsym, np.ones(nsym, np.int32), isym_pairs,
+                igamma_pair_of(isym_pairs), bases, infl, classes, make_dipole(nv), blk)
+    J_, jind_, g_, lev_, e_ = [], [], [], [], []
+    for (jind, g), b in sorted(blk.items()):
+        n = b.energies.shape[0]
+        J_ += [b.J] * n
+        jind_ += [jind] * n
+        g_ += [g] * n
+        lev_ += list(range(n))
+        e_.append(b.energies)
+    e = np.concatenate(e_) if e_ else np.zeros(0)
+    order = np.argsort(e, kind="stable")
+    p.st_J = np.asarray(J_, np.int32)[order]
+    p.st_jind = np.asarray(jind_, np.int32)[order]
+    p.st_gamma = np.asarray(g_, np.int32)[order]
+    p.st_ndeg = p.sym_degen[p.st_gamma].astype(np.int32)
+    p.st_ilevel = np.asarray(lev_, np.int32)[order]
+    p.st_energy = e[order]
+    return p
+
+
+# Named workloads (sizes of the reference's headline configurations).
+CONFIGS = {
+    # J''=0 -> J'=1, whole basis, 50 lowest J=0 states against every J=1 state.
+    "cfg1": dict(nv=200, jvals=[0, 1], rule="full", lower=(0, 0), upper=(1, 0), n_lower=50,
+                 e_lower=(0.0, 8000.0), e_upper=(0.0, 8000.0)),
+    # J''=10 class 0 (11000 functions) -> J'=11 class 1 (12000 functions); the 2000 lowest
+    # lower states (all below 5000 cm^-1) against every upper state below 10000 cm^-1.
+    "cfg2": dict(nv=2000, jvals=[10, 11], rule="c4", lower=(10, 0), upper=(11, 1), n_lower=2000,
+                 e_lower=(0.0, 5000.0), e_upper=(0.0, 10000.0)),
+}

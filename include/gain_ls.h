@@ -1,0 +1,198 @@
+/* gain_ls.h -- C ABI of the GB300 line-strength library (libgainls.so).
+ *
+ * Drop-in replacement for GAIN-MPI's GPU line-strength path: the kernel wrappers of
+ * GPU/dipole_GPU.h and the device work GpuManager (BaseClasses/GpuManager.h) orchestrates.
+ * Plain pointers and sizes only; every entry point returns a gain_status and never aborts
+ * the process (the reference calls MPI_Abort through LogErrorAndAbort on any CUDA error,
+ * BaseClasses/GpuManager.cpp:80-93, common/BaseProcess.cpp:42-52).
+ *
+ * Two layers:
+ *   1. kernel-level entry points with the reference wrappers' arguments and semantics
+ *      (device pointers, asynchronous on the caller's stream);
+ *   2. an engine that owns device memory (basis sets, expansion tables, dipole,
+ *      eigenvectors) and computes whole (J'',Gamma'') -> (J',Gamma') block pairs, through
+ *      either the reference's plain FP64 method or the split-precision tensor-core method.
+ */
+#ifndef GAIN_LS_H
+#define GAIN_LS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GAIN_ABI_VERSION 1
+
+typedef enum gain_status {
+    GAIN_OK = 0,
+    GAIN_ERR_INVALID_ARG = 1,   /* rejected on the host before any launch */
+    GAIN_ERR_OOM = 2,           /* device or pinned allocation failed */
+    GAIN_ERR_CUDA = 3,          /* a CUDA runtime / driver call failed */
+    GAIN_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+    GAIN_ERR_TOL_NOT_MET = 5,   /* split path: some lines could not be certified */
+    GAIN_ERR_NOT_READY = 6,     /* a required upload has not happened */
+    GAIN_ERR_UNSUPPORTED = 7    /* valid input outside what this build implements */
+} gain_status;
+
+/* Message describing the most recent failure on the calling thread ("" if none). */
+const char* gain_last_error_string(void);
+const char* gain_status_string(gain_status s);
+int gain_abi_version(void);
+
+/* ======================= layer 1: kernel-level drop-ins ============================ */
+
+/* One upper K-block kF of the half line strength.
+ * Replaces compute_gpu_half_linestrength_ (GPU/dipole_GPU.h:23-26, GPU/dipole_GPU.cu:185-210)
+ * with the same arguments in the same order; the two __constant__ values the reference sets
+ * beforehand (c_jmax through copy_jmax_constant, GPU/dipole_GPU.h:14, and dip_stride_1
+ * through copy_dipole_constant, :15) are the trailing arguments jmax and dip_stride.
+ * Writes half_ls[startF_idx + f], 0 <= f < dimenF, for the F whose vibrational index lies
+ * in [startFblock, endFblock); other entries are untouched.  Device pointers; asynchronous
+ * on `stream` (a cudaStream_t, NULL = legacy default stream).  Results are bit-identical to
+ * the reference kernel (same operations in the same order per output element). */
+gain_status gain_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF,
+                            const int* tauI, const int* tauF, const int* icorrI, const int* icorrF,
+                            int startF_idx, int startI_idx, int startFblock, int endFblock,
+                            int ncontrF, int kFBlocksize, const int* kblock_size,
+                            const double* dipole_me, const double* vector, const double* threej,
+                            double* half_ls, int jmax, int dip_stride, void* stream);
+
+/* Symmetry-adapted -> primitive expansion of one vector.
+ * Replaces transform_vector_primitive (GPU/dipole_GPU.h:19, GPU/dipole_GPU.cu:137-156,
+ * kernel :859-889): vec[r] = sum_{i<N[irow]} vecI[iterm+i] * repres[iterm+i + idegI*Ntot + ib*sdeg*Ntot]
+ * with irow = icontr[r], ib = icontr[r+dimenI], iterm = ijterms[irow + igammaI*maxcoeff]. */
+gain_status gain_expand(int dimenI, int igammaI, int maxcoeff, int idegI, int sdeg, int Ntot,
+                        const int* ijterms, const int* icontr, const int* N, const double* repres,
+                        const double* vecI, double* vec, void* stream);
+
+/* result[0] = sum_i x[i]*y[i] (device pointers, device result).
+ * Replaces the cublasDdot of GpuManager::ExecuteDotProduct (BaseClasses/GpuManager.cpp:741),
+ * which runs in CUBLAS_POINTER_MODE_DEVICE (:202). */
+gain_status gain_dot(int n, const double* x, const double* y, double* result, void* stream);
+
+/* Host: the Wigner-3j table GpuManager::InitializeAndTransferConstants builds
+ * (BaseClasses/GpuManager.cpp:166-181, three_j -> TroveFortran/fort_func.f90:7-104):
+ *   table[jI + kI(jmax+1) + (jF-jI+1)(jmax+1)^2 + (kF-kI+1)3(jmax+1)^2] = 3j(jI 1 jF; kI, kF-kI, -kF)
+ * table holds 9 (jmax+1)^2 doubles.  Values are exact rationals rounded once, correctly. */
+gain_status gain_threej_table(int jmax, double* table);
+
+/* ======================= layer 2: the line-strength engine ========================= */
+
+typedef struct gain_engine_s* gain_engine;
+
+/* GpuManager ctor + InitializeAndTransferConstants (BaseClasses/GpuManager.cpp:69-213):
+ * binds `device`, builds the 3j table for jmax on the device. nsym = number of irreducible
+ * representations, maxdeg = largest degeneracy. */
+gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_engine* out);
+gain_status gain_engine_destroy(gain_engine e);
+
+/* GpuManager::TransferBasisSet (BaseClasses/GpuManager.cpp:215-265): the primitive basis
+ * of J (index jind): per function K, tau (ktau & 1), vibrational index; K-blocks.
+ * Functions must be K-sorted (TroveClasses/TroveBasisSet.cpp:659-681). Host arrays, copied. */
+gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const int* K,
+                              const int* tau, const int* vib, const int* kblock_size,
+                              const int* kstart);
+
+/* GpuManager::TransferInflation (BaseClasses/GpuManager.cpp:381-422): expansion tables of
+ * jind.  icontr[2*dimen], ijterms[maxcoeff*nsym]; per Gamma g: N[g][maxcoeff],
+ * repres[g][Ntot[g]*sdeg[g]*matsize].  Host arrays, copied. */
+gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, const int* ijterms,
+                                  int dimen, int maxcoeff, int matsize, const int* const* N,
+                                  const double* const* repres, const int* Ntot, const int* sdeg);
+
+/* GpuManager::TransferDipole (BaseClasses/GpuManager.cpp:499-526) for one DipolePiece
+ * (BaseClasses/Dipole.h:9-15): piece[f-startF + i*ncontrF + d*N*ncontrF], d = 0..2,
+ * N = Dipole::GetMaxContracts. Host array, copied. */
+gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int startF, int endF,
+                               int ncontrF);
+
+/* Eigenvectors of one (J, Gamma) block kept resident (the reference re-uploads one vector
+ * per transition, GpuManager::UpdateEigenVector, :537-545): vecs[level*nsize + c].  Host
+ * array (pinned memory transfers fastest), copied synchronously. */
+gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize,
+                                const double* vecs);
+
+typedef enum gain_path {
+    GAIN_PATH_PLAIN_FP64 = 0,   /* the reference's method: half_ls per lower state, GEMV */
+    GAIN_PATH_SPLIT = 1         /* Ozaki-sliced BF16 tcgen05 GEMMs + FP64 refinement */
+} gain_path;
+
+/* One block pair: rows = lower levels of (jindI, gammaI), columns = upper levels of
+ * (jindF, gammaF).  Level lists are host arrays of level indices. */
+typedef struct gain_pair_job {
+    int jindI, gammaI, jindF, gammaF;
+    int nlower;
+    const int* lower_levels;
+    int nupper;
+    const int* upper_levels;
+} gain_pair_job;
+
+typedef struct gain_split_opts {
+    double tol;       /* relative tolerance on each amplitude; lines whose certified bound
+                         exceeds tol*|amp| are recomputed in FP64 (0 -> 2e-9) */
+    int slices;       /* digits per operand (0 -> chosen from beta for ~49 bits) */
+    int beta;         /* bits per digit, 4..8 (0 -> chosen from the inner dimension) */
+    int kchunks;      /* inner-dimension chunks for exact FP32 accumulation (0 -> auto) */
+} gain_split_opts;
+
+typedef struct gain_stats {
+    double device_ms;           /* device time of the last run (CUDA events) */
+    long long rows, cols;       /* lower x upper amplitudes computed */
+    long long refined;          /* split path: amplitudes recomputed in FP64 */
+    long long uncertified;      /* split path: refined lines whose bound still exceeds tol */
+    long long inexact;          /* split path: pairs outside the exact-accumulation guarantee */
+    int beta1, slices1, chunks1;  /* first GEMM (lower vectors x rotational-dipole matrix) */
+    int beta2, slices2, chunks2;  /* second GEMM (half line strengths x upper vectors) */
+    int products1, products2;   /* BF16 digit products per GEMM */
+    int kernel_launches;        /* kernels launched by the last run */
+    double gemm1_ms, gemm2_ms;  /* device time of the two tensor-core GEMMs */
+    double tensor_flops;        /* BF16 MMA flops issued by the two GEMMs (no padding) */
+} gain_stats;
+
+/* Compute amplitudes amp[l][u] = <upper u | mu . rot | lower l> for one block pair into an
+ * engine-owned device matrix (row-major; its pointer and leading dimension come from
+ * gain_pair_amp_device).  Blocks on completion.  opts may be NULL (defaults).  stats may be
+ * NULL. */
+gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path path,
+                          const gain_split_opts* opts, gain_stats* stats);
+
+/* Device pointer / leading dimension of the last run's amplitude matrix. */
+gain_status gain_pair_amp_device(gain_engine e, const double** amp, int* ld);
+
+/* Copy the last run's amplitudes to a host array amp[nlower*nupper] (row-major). */
+gain_status gain_fetch_amp(gain_engine e, double* amp_host);
+
+/* Intensity-block parameters (TroveClasses/TroveInput.cpp:239-326) the line assembly uses. */
+typedef struct gain_line_params {
+    double temperature;       /* TEMPERATURE */
+    double q_part;            /* QSTAT */
+    double zpe;               /* ZPE */
+    double thresh;            /* THRESH_LINE */
+    double freq_lo, freq_hi;  /* FREQ-WINDOW */
+    double gnsF;              /* GNS of the upper Gamma */
+    int ndegI, ndegF;         /* degeneracies (1 in this build's batched path) */
+    int reduced;              /* SYMMETRY REDUCED */
+} gain_line_params;
+
+/* Line strength S, Einstein A and intensity I of every amplitude of the last run
+ * (Output::OutputLinestrength, BaseClasses/Output.cpp:52-112), on the device.
+ * energiesI/F are host arrays of the rows' / columns' energies.  keep[l*nupper+u] = 1 when
+ * the reference would write the line (nu inside FREQ-WINDOW, nu >= 1e-40, A >= THRESH_LINE).
+ * Host outputs (any may be NULL): S, A, I [nlower*nupper] doubles, keep [nlower*nupper]
+ * bytes; n_lines = number kept. */
+gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                            const double* energiesF, int jI, int jF, double* S, double* A,
+                            double* I, unsigned char* keep, long long* n_lines);
+
+/* Text of one line exactly as Output.cpp:99-111 prints it (without the amplitude list
+ * unless namp > 0).  Returns the number of characters written (excluding the NUL). */
+int gain_format_line(char* buf, size_t cap, double nu, int indexF, int jF, int gammaF,
+                     int indexI, int jI, int gammaI, double A, int with_intensity,
+                     double intensity, const double* amps, int namp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAIN_LS_H */

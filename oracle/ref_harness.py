@@ -1,0 +1,119 @@
+"""ORACLE (test infrastructure only): Python side of ref_harness.cu.
+
+Runs the reference's own unmodified kernels (oracle/_ref/dipole_GPU.cubin, compiled from
+the reference tree by oracle/build_ref.sh) on the GPU, driven like GpuManager drives them.
+Used to make golden fixtures and to pin the oracle; never part of the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import platform
+import shutil
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build", platform.machine())
+LIB = os.path.join(BUILD, "libgainrefh.so")
+SRC = os.path.join(HERE, "ref_harness.cu")
+CUBIN = os.path.join(HERE, "_ref", "dipole_GPU.cubin")
+
+_lib = None
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class RefhPair(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("jI", "jF", "jmax", "dimenI", "dimenF")] + \
+        [(n, _ip) for n in ("tauI", "tauF", "icorrI", "icorrF", "kstartI", "kblockI", "kstartF", "kblockF")] + \
+        [(n, ctypes.c_int) for n in ("gammaI", "gammaF", "maxcoeffI", "maxcoeffF", "NtotI", "NtotF",
+                                     "nsymI", "nsymF")] + \
+        [("ijtermsI", _ip), ("icontrI", _ip), ("NI", _ip), ("represI", _dp),
+         ("ijtermsF", _ip), ("icontrF", _ip), ("NF", _ip), ("represF", _dp), ("dipole_me", _dp)] + \
+        [(n, ctypes.c_int) for n in ("dip_stride", "startFblock", "endFblock", "ncontrF")] + \
+        [("threej", _dp), ("nlower", ctypes.c_int), ("nupper", ctypes.c_int), ("vec_lower", _dp),
+         ("vec_upper", _dp)]
+
+
+def available() -> bool:
+    return os.path.exists(CUBIN)
+
+
+def build() -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+        cmd = [nvcc, "-O2", "-shared", "-Xcompiler", "-fPIC", SRC, "-o", LIB + ".tmp", "-lcublas", "-lcuda"]
+        stub = "/usr/local/cuda/lib64/stubs"
+        if os.path.isdir(stub):
+            cmd += ["-L", stub]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.refh_init.argtypes = [ctypes.c_char_p]
+        L.refh_init.restype = ctypes.c_int
+        L.refh_error.restype = ctypes.c_char_p
+        L.refh_run_pair.argtypes = [ctypes.POINTER(RefhPair), _dp, _dp, _dp]
+        L.refh_run_pair.restype = ctypes.c_int
+        if L.refh_init(CUBIN.encode()) != 0:
+            raise RuntimeError("reference harness: " + L.refh_error().decode())
+        _lib = L
+    return _lib
+
+
+def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, threej, jmax,
+             dipole_block=None, vec_lower=None, vec_upper=None):
+    """(amp [nl, nu], half_ls [nl, dimenF], seconds of the per-transition loop)."""
+    p = problem
+    bI, bF = p.bases[jindI], p.bases[jindF]
+    iI, iF = p.infl[jindI], p.infl[jindF]
+    vl = vec_lower if vec_lower is not None else p.blocks[(jindI, gammaI)].vecs[np.asarray(lower_levels, int)]
+    vu = vec_upper if vec_upper is not None else p.blocks[(jindF, gammaF)].vecs[np.asarray(upper_levels, int)]
+    vl = np.ascontiguousarray(vl, np.float64)
+    vu = np.ascontiguousarray(vu, np.float64)
+    nv = p.dipole.shape[-1]
+    if dipole_block is None:
+        startF, endF = 0, nv
+        piece = np.ascontiguousarray(p.dipole)
+    else:
+        startF, endF = dipole_block
+        piece = np.ascontiguousarray(p.dipole[:, :, startF:endF])
+    keep = []
+
+    def I(a):
+        a = np.ascontiguousarray(a, np.int32); keep.append(a); return a.ctypes.data_as(_ip)
+
+    def D(a):
+        a = np.ascontiguousarray(a, np.float64); keep.append(a); return a.ctypes.data_as(_dp)
+
+    s = RefhPair()
+    s.jI, s.jF, s.jmax, s.dimenI, s.dimenF = bI.J, bF.J, jmax, bI.dimen, bF.dimen
+    s.tauI, s.tauF, s.icorrI, s.icorrF = I(bI.tau), I(bF.tau), I(bI.vib), I(bF.vib)
+    s.kstartI, s.kblockI, s.kstartF, s.kblockF = I(bI.kstart), I(bI.kblock), I(bF.kstart), I(bF.kblock)
+    s.gammaI, s.gammaF = gammaI, gammaF
+    s.maxcoeffI, s.maxcoeffF = iI.maxcoeff, iF.maxcoeff
+    s.NtotI, s.NtotF = int(iI.Ntot[gammaI]), int(iF.Ntot[gammaF])
+    s.nsymI, s.nsymF = len(iI.N), len(iF.N)
+    s.ijtermsI, s.icontrI, s.NI, s.represI = I(iI.ijterms), I(iI.icontr), I(iI.N[gammaI]), D(iI.repres[gammaI])
+    s.ijtermsF, s.icontrF, s.NF, s.represF = I(iF.ijterms), I(iF.icontr), I(iF.N[gammaF]), D(iF.repres[gammaF])
+    s.dipole_me = D(piece.reshape(-1))
+    s.dip_stride, s.startFblock, s.endFblock, s.ncontrF = nv, startF, endF, endF - startF
+    s.threej = D(threej)
+    s.nlower, s.nupper = vl.shape[0], vu.shape[0]
+    s.vec_lower, s.vec_upper = D(vl), D(vu)
+    amp = np.zeros((vl.shape[0], vu.shape[0]), np.float64)
+    hls = np.zeros((vl.shape[0], bF.dimen), np.float64)
+    secs = ctypes.c_double()
+    if lib().refh_run_pair(ctypes.byref(s), amp.ctypes.data_as(_dp), hls.ctypes.data_as(_dp),
+                           ctypes.byref(secs)) != 0:
+        raise RuntimeError("reference harness: " + lib().refh_error().decode())
+    return amp, hls, secs.value

@@ -1,0 +1,70 @@
+"""Generate the golden fixtures of the line-strength path by running the reference's own
+kernels on a GPU.
+
+The reference (GAIN-MPI) ships no tests, sample inputs or expected outputs.  These fixtures
+are outputs of its unmodified GPU/dipole_GPU.cu (compiled for sm_103a into
+oracle/_ref/dipole_GPU.cubin by oracle/build_ref.sh), driven by oracle/ref_harness.cu the
+way BaseClasses/GpuManager.cpp drives it: per lower state the expansion kernel and one
+K-block launch per K', then per upper state the expansion kernel and cublasDdot.
+
+Each fixture stores the exact inputs that are not pure integer tables (eigenvectors,
+dipole piece, 3j table) next to the reference outputs (half_ls per lower state and the
+amplitudes), so the CPU tests can replay them anywhere.
+
+    python tests/golden/make_golden.py OUTDIR      # needs a GPU and the reference cubin
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "gain-mpi_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import synth  # noqa: E402
+import threej  # noqa: E402
+import ref_harness  # noqa: E402
+
+# name: nv, J values, symmetry rule, (J'', Gamma''), (J', Gamma'), lower levels, upper levels, dipole block
+CASES = {
+    "cfg1_small": (200, [0, 1], "full", (0, 0), (1, 0), list(range(8)), list(range(64)), None),
+    "c4_dJp1": (16, [2, 3], "c4", (2, 0), (3, 1), None, None, None),
+    "c4_dJm1": (16, [2, 3], "c4", (3, 1), (2, 0), None, None, None),
+    "c4_dJ0": (16, [2, 3], "c4", (3, 2), (3, 3), None, None, None),
+    "c4_highJ": (6, [10, 11], "c4", (10, 0), (11, 1), list(range(12)), list(range(20)), None),
+    "full_blocked": (16, [2, 3], "full", (2, 0), (3, 0), list(range(6)), list(range(30)), (5, 11)),
+}
+
+
+def make_case(name, jmax=11):
+    nv, jvals, rule, (JI, gI), (JF, gF), lo, up, blk = CASES[name]
+    p = synth.make_problem(nv, jvals, rule, blocks=[(JI, gI), (JF, gF)])
+    jI, jF = jvals.index(JI), jvals.index(JF)
+    nI = p.blocks[(jI, gI)].vecs.shape[0]
+    nF = p.blocks[(jF, gF)].vecs.shape[0]
+    lo = list(range(nI)) if lo is None else lo
+    up = list(range(nF)) if up is None else up
+    tj = threej.threej_table(jmax)
+    vl = p.blocks[(jI, gI)].vecs[lo]
+    vu = p.blocks[(jF, gF)].vecs[up]
+    amp, hls, _ = ref_harness.run_pair(p, jI, gI, jF, gF, lo, up, tj, jmax, dipole_block=blk,
+                                       vec_lower=vl, vec_upper=vu)
+    return dict(nv=nv, jvals=np.array(jvals), rule=rule, JI=JI, gI=gI, JF=JF, gF=gF,
+                lower=np.array(lo), upper=np.array(up), block=np.array(blk if blk else (0, nv)),
+                jmax=jmax, threej=tj, dipole=p.dipole, vec_lower=vl, vec_upper=vu,
+                ref_hls=hls, ref_amp=amp)
+
+
+def main(outdir):
+    os.makedirs(outdir, exist_ok=True)
+    for name in CASES:
+        d = make_case(name)
+        np.savez_compressed(os.path.join(outdir, name + ".npz"), **d)
+        print(name, d["ref_hls"].shape, d["ref_amp"].shape, float(np.abs(d["ref_amp"]).max()))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__)))

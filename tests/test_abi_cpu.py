@@ -1,0 +1,75 @@
+"""The C ABI without a GPU: the library loads, exports every declared entry point, rejects
+bad arguments on the host with a status (never aborting), and prints lines exactly as the
+reference's Output::OutputLinestrength does."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import has_gpu
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    import gainls
+    L = gainls.lib()
+    names = gainls.declared_symbols()
+    assert "gain_hls_kblock" in names and "gain_run_pair" in names
+    for n in names:
+        assert hasattr(L, n), n
+    assert L.gain_abi_version() == 1
+
+
+def test_status_strings(built_lib):
+    import gainls
+    L = gainls.lib()
+    for s in range(8):
+        assert L.gain_status_string(s).decode().startswith("GAIN_")
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-GPU error path")
+def test_engine_without_gpu_reports_status(built_lib):
+    import gainls
+    with pytest.raises(gainls.GainError) as e:
+        gainls.Engine(11, 4, 1)
+    assert e.value.status in (gainls.ERR_CUDA, gainls.ERR_INVALID_ARG)
+
+
+def test_engine_rejects_bad_arguments(built_lib):
+    import gainls
+    h = ctypes.c_void_p()
+    assert gainls.lib().gain_engine_create(0, -1, 4, 1, ctypes.byref(h)) == gainls.ERR_INVALID_ARG
+    assert gainls.lib().gain_engine_create(0, 11, 0, 1, ctypes.byref(h)) == gainls.ERR_INVALID_ARG
+    assert "bad argument" in gainls.lib().gain_last_error_string().decode()
+    assert gainls.lib().gain_run_pair(None, None, 0, None, None) == gainls.ERR_INVALID_ARG
+
+
+def test_dropin_validation_is_host_side(built_lib):
+    import gainls
+    # |jI - jF| > 1, negative sizes, kF > jF: all rejected before touching any pointer
+    bad = [
+        dict(jI=1, jF=3, kF=0, dimenF=4),
+        dict(jI=2, jF=2, kF=3, dimenF=4),
+        dict(jI=2, jF=2, kF=0, dimenF=-1),
+    ]
+    for b in bad:
+        with pytest.raises(gainls.GainError) as e:
+            gainls.hls_kblock(b["dimenF"], 4, b["jI"], b["jF"], b["kF"], 1, 1, 1, 1, 0, 0, 0, 4, 4, 4, 1, 1,
+                              1, 1, 1, 11, 4)
+        assert e.value.status == gainls.ERR_INVALID_ARG
+    with pytest.raises(gainls.GainError):
+        gainls.expand(4, 0, 0, 0, 1, 4, 1, 1, 1, 1, 1, 1)
+
+
+@pytest.mark.parametrize("args", [
+    (1234.5678901, 3, 1, 0, 0, 0, 0, 1.23456789e-5, None, None),
+    (0.000001, 11999, 11, 1, 1999, 10, 0, 3.5e-300, 1.0e-30, None),
+    (8000.0, 0, 31, 3, 5, 30, 2, 0.0, 0.0, [0.1, -0.25, 3.0e-9]),
+    (-12.5, 7, 2, 1, 7, 2, 0, 1e10, None, [1.0]),
+])
+def test_line_text_matches_reference_format(built_lib, args):
+    import gainls
+    import oracle
+    nu, iF, jF, gF, iI, jI, gI, A, inten, amps = args
+    a = gainls.format_line(nu, iF, jF, gF, iI, jI, gI, A, intensity=inten, amps=amps)
+    b = oracle.line_text(nu, iF, jF, gF, iI, jI, gI, A, intens=inten, amps=amps)
+    assert a == b

@@ -1,0 +1,153 @@
+"""GPU parity of the engine's two block-pair paths against the CPU oracle.
+
+plain FP64 path: the reference's method (half line strength per lower state, then dot
+products with the upper vectors); must match the oracle to FP64 rounding (relative 1e-12
+of the largest amplitude, far below the 1e-10 required on S).
+split path: Ozaki-sliced BF16 tensor-core GEMMs with certified bounds and FP64 refinement;
+line strengths S = amp^2 must match within 1e-8 relative for every line with
+S > 1e-10 S_max (the tolerance of the headline metric).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+JMAX = 11
+S_REL_TOL = 1e-8
+
+
+def _oracle_amp(p, jI, gI, jF, gF, lo, up, mode, nthreads=8):
+    import oracle
+    import threej
+    return oracle.run_pair(p, jI, gI, jF, gF, lo, up, threej.threej_table(JMAX), JMAX, mode, nthreads)
+
+
+def _s_rel_err(amp, ref):
+    S, Sr = amp ** 2, ref ** 2
+    m = Sr > 1e-10 * Sr.max()
+    return float(np.max(np.abs(S[m] - Sr[m]) / Sr[m]))
+
+
+@pytest.fixture(scope="module")
+def c4_small(built_lib):
+    import gainls
+    import synth
+    p = synth.make_problem(16, [2, 3], "c4")
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    return p, eng
+
+
+PAIRS = [(0, 0, 1, 1), (1, 1, 0, 0), (1, 2, 1, 3), (0, 3, 1, 2)]
+
+
+@pytest.mark.parametrize("pair", PAIRS)
+def test_plain_fp64_matches_oracle(c4_small, pair):
+    import gainls
+    import oracle
+    p, eng = c4_small
+    jI, gI, jF, gF = pair
+    lo = list(range(p.blocks[(jI, gI)].vecs.shape[0]))
+    up = list(range(p.blocks[(jF, gF)].vecs.shape[0]))
+    eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_PLAIN_FP64)
+    amp = eng.fetch_amp()
+    ref = _oracle_amp(p, jI, gI, jF, gF, lo, up, oracle.DD)
+    assert np.max(np.abs(amp - ref)) <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("pair", PAIRS)
+def test_split_matches_oracle(c4_small, pair):
+    import gainls
+    import oracle
+    p, eng = c4_small
+    jI, gI, jF, gF = pair
+    lo = list(range(p.blocks[(jI, gI)].vecs.shape[0]))
+    up = list(range(p.blocks[(jF, gF)].vecs.shape[0]))
+    st = eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_SPLIT)
+    amp = eng.fetch_amp()
+    ref = _oracle_amp(p, jI, gI, jF, gF, lo, up, oracle.DD)
+    assert st["status"] == gainls.OK
+    assert _s_rel_err(amp, ref) <= S_REL_TOL
+    assert np.max(np.abs(amp - ref)) <= 1e-11 * np.abs(ref).max()
+
+
+def test_split_level_subsets_and_order(c4_small):
+    """Arbitrary (unsorted, partial) level lists on both sides."""
+    import gainls
+    import oracle
+    p, eng = c4_small
+    rng = np.random.default_rng(5)
+    nI = p.blocks[(0, 0)].vecs.shape[0]
+    nF = p.blocks[(1, 1)].vecs.shape[0]
+    lo = list(rng.permutation(nI)[: nI - 3])
+    up = list(rng.permutation(nF)[: nF - 5])
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    amp = eng.fetch_amp()
+    ref = _oracle_amp(p, 0, 0, 1, 1, lo, up, oracle.DD)
+    assert _s_rel_err(amp, ref) <= S_REL_TOL
+
+
+@pytest.fixture(scope="module")
+def c4_medium(built_lib):
+    import gainls
+    import synth
+    p = synth.make_problem(120, [5, 6], "c4", blocks=[(5, 0), (6, 1)])
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    return p, eng
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(beta=6), dict(kchunks=2), dict(beta=8, slices=6, kchunks=3)])
+def test_split_matches_plain_medium(c4_medium, opts):
+    """Several tiles per GEMM, digit widths 6-8 and 1-3 exact-accumulation chunks."""
+    import gainls
+    p, eng = c4_medium
+    nI = p.blocks[(0, 0)].vecs.shape[0]
+    nF = p.blocks[(1, 1)].vecs.shape[0]
+    lo, up = list(range(nI)), list(range(nF))
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+    ref = eng.fetch_amp().copy()
+    st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT, **opts)
+    amp = eng.fetch_amp()
+    assert st["status"] == gainls.OK, st
+    assert _s_rel_err(amp, ref) <= S_REL_TOL
+    if opts.get("kchunks"):
+        assert st["chunks2"] == opts["kchunks"]
+
+
+def test_plain_medium_matches_oracle_ref_order(c4_medium):
+    import gainls
+    import oracle
+    p, eng = c4_medium
+    lo = list(range(0, p.blocks[(0, 0)].vecs.shape[0], 37))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+    amp = eng.fetch_amp()
+    ref = _oracle_amp(p, 0, 0, 1, 1, lo, up, oracle.REF)
+    assert np.max(np.abs(amp - ref)) <= 1e-12 * np.abs(ref).max()
+
+
+def test_full_rule_pair_and_dipole_block(built_lib):
+    """One symmetry class (the whole basis) and a dipole piece covering part of the
+    vibrational range: only upper functions whose vibrational index lies in the piece
+    get contributions (BaseClasses/Dipole.h:9-15, GPU/dipole_GPU.cu:429)."""
+    import gainls
+    import oracle
+    import synth
+    p = synth.make_problem(16, [1, 2], "full")
+    eng = gainls.Engine(JMAX, 1, 1)
+    gainls.upload_problem(eng, p, dipole_block=(5, 11))
+    lo = list(range(10))
+    up = list(range(p.blocks[(1, 0)].vecs.shape[0]))
+    ref = _oracle_amp_block(p, lo, up)
+    for path in (gainls.PATH_PLAIN_FP64, gainls.PATH_SPLIT):
+        eng.run_pair(0, 0, 1, 0, lo, up, path)
+        amp = eng.fetch_amp()
+        assert np.max(np.abs(amp - ref)) <= 1e-11 * np.abs(ref).max()
+
+
+def _oracle_amp_block(p, lo, up):
+    import oracle
+    import threej
+    return oracle.run_pair(p, 0, 0, 1, 0, lo, up, threej.threej_table(JMAX), JMAX, oracle.DD, 8,
+                           dipole_block=(5, 11))
