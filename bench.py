@@ -1,0 +1,346 @@
+"""Benchmark of the line-strength hot path (one JSON line on rank 0).
+
+Workload (the headline configuration): N_v = 2000, J''=10 symmetry class 0 (11000 basis
+functions) -> J'=11 class 1 (12000 functions); the 2000 lowest lower states (all below
+5000 cm^-1) against all 12000 upper states (all below 10000 cm^-1): 2.4e7 line strengths
+per step.  Synthetic, seeded inputs stand in for the TROVE checkpoints.
+
+One step = the split-precision tensor-core path over the whole block pair starting from
+FP64 inputs resident in HBM: digit slicing of both eigenvector sets, the rotational-dipole
+band GEMM, the amplitude GEMM, FP64 refinement of uncertified lines.  `e2e` runs the same
+step through the C ABI from pinned host buffers: upload of both eigenvector sets, the run,
+and the device-to-host read of S and A.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gain-mpi_gb300"))
+
+METRIC = "transitions/s: split-prec TC vs FP64 plain @ S rel-err≤1e-8; % of roofline"
+UNIT = "transitions/s"
+NV, JI, JF, GI, GF = 2000, 10, 11, 0, 1
+N_LOWER = 2000
+WORKLOAD = ("N_v=2000, J''=10 Gamma 0 (11000 functions) -> J'=11 Gamma 1 (12000 functions), "
+            "2000 lowest lower states x 12000 upper states")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--small", action="store_true", help="reduced sizes (development only)")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------------- inputs
+def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = True):
+    """orthonormal=False replaces the QR eigenvectors by normalised Gaussian rows of the same
+    shape (used only where the values do not matter: timing the CPU reference formula)."""
+    import synth
+    nv, n_lower = (200, 64) if small else (NV, N_LOWER)
+    bI, bF = synth.make_basis(JI, nv), synth.make_basis(JF, nv)
+    cI, cF = synth.classes_of(bI, "c4"), synth.classes_of(bF, "c4")
+    iI, iF = synth.make_inflation(bI, cI, 4), synth.make_inflation(bF, cF, 4)
+    nI, nF = int(iI.Ntot[GI]), int(iF.Ntot[GF])
+    # each rank takes its own batch of lower states (weak scaling, no data exchange)
+    first = (rank * n_lower) % max(nI - n_lower + 1, 1)
+    if orthonormal:
+        vl = synth.make_eigvecs(nI, JI, GI, device=device, nstates=first + n_lower)[first:first + n_lower]
+        vu = synth.make_eigvecs(nF, JF, GF, device=device)
+    else:
+        rng = np.random.default_rng(synth.vec_seed(JI, GI))
+        vl = rng.standard_normal((n_lower, nI)) / np.sqrt(nI)
+        vu = np.random.default_rng(synth.vec_seed(JF, GF)).standard_normal((nF, nF)) / np.sqrt(nF)
+    eI = synth.make_energies(nI, JI, GI)[first:first + n_lower]
+    eF = synth.make_energies(nF, JF, GF)
+    return dict(nv=nv, bases=[bI, bF], infl=[iI, iF], dipole=synth.make_dipole(nv), vl=np.ascontiguousarray(vl),
+                vu=np.ascontiguousarray(vu), eI=eI, eF=eF, first=first)
+
+
+def pinned(a: np.ndarray) -> np.ndarray:
+    import torch
+    t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+    out = t.numpy()
+    out[...] = a
+    out._keep = t  # noqa: SLF001  (keep the pinned buffer alive)
+    return out
+
+
+def setup_engine(inp, device_index: int):
+    import gainls
+    eng = gainls.Engine(11, 4, 1, device=device_index)
+    for jind, (b, inf) in enumerate(zip(inp["bases"], inp["infl"])):
+        eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
+        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, 1, inf.N, inf.repres,
+                             inf.Ntot, inf.sdeg)
+    nv = inp["nv"]
+    eng.upload_dipole(inp["dipole"].reshape(-1), nv, 0, nv, nv)
+    eng.upload_eigvecs(0, GI, inp["vl"])
+    eng.upload_eigvecs(1, GF, inp["vu"])
+    return eng
+
+
+# ------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(inp, n_sample: int):
+    """The reference's FP64 formula restated in C (oracle), OpenMP over upper states as in
+    main.cpp:292, on all host cores; a bounded sample of lower states of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import threej
+    import synth
+    oracle.build()
+    nv = inp["nv"]
+    p = synth.Problem(nv, [JI, JF], "c4", 4, np.ones(4, np.int32), synth.selection_of("c4"),
+                      synth.igamma_pair_of(synth.selection_of("c4")), inp["bases"], inp["infl"],
+                      [synth.classes_of(b, "c4") for b in inp["bases"]], inp["dipole"],
+                      {(0, GI): synth.Block(JI, 0, GI, inp["vl"][:n_sample], inp["eI"][:n_sample]),
+                       (1, GF): synth.Block(JF, 1, GF, inp["vu"], inp["eF"])})
+    cores = os.cpu_count() or 1
+    tj = threej.threej_table(11)
+    t0 = time.perf_counter()
+    oracle.run_pair(p, 0, GI, 1, GF, list(range(n_sample)), list(range(inp["vu"].shape[0])), tj, 11,
+                    oracle.REF, cores)
+    secs = time.perf_counter() - t0
+    n = n_sample * inp["vu"].shape[0]
+    return {"value": n / secs, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n_sample} lower states x {inp['vu'].shape[0]} upper states of the workload "
+                      f"({n} transitions, {secs:.1f} s)"}
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    inp = make_inputs(args.small, 0, None, orthonormal=False)
+    sample = 2 if not args.small else 4
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(inp, sample)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.median(vals))
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * sample * inp["vu"].shape[0] / v,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "impl": "reference",
+           "config": {"workload": WORKLOAD, "sample": f"{sample} lower states per step"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port",
+                            "sample": r["sample"]},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------------- our arm
+def main():
+    args = parse()
+    ws, rank, local = dist_info()
+    if args.impl == "reference":
+        if ws > 1 and rank != 0:
+            return
+        return reference_arm(args, ws, rank)
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import gainls
+    inp = make_inputs(args.small, rank, "cuda")
+    eng = setup_engine(inp, local)
+    B, NU = inp["vl"].shape[0], inp["vu"].shape[0]
+    lo, up = list(range(B)), list(range(NU))
+    transitions = B * NU
+
+    def step():
+        return eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT)
+
+    for _ in range(args.warmup):
+        st = step()
+    # timed region: device time of each step from CUDA events on the engine's stream
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms_list, g1, g2 = [], [], []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st = step()
+            ms_list.append(st["device_ms"])
+            g1.append(st["gemm1_ms"])
+            g2.append(st["gemm2_ms"])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    total_ms = float(np.sum(ms_list))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ms_step = total_ms / args.steps
+    value = ws * transitions / (ms_step * 1e-3)
+
+    # accuracy of this run against the plain FP64 path (the reference's own method)
+    split_amp = eng.fetch_amp().copy()
+    extra = {}
+    if not args.no_plain:
+        sp = eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_PLAIN_FP64)
+        plain_amp = eng.fetch_amp()
+        S, Sr = split_amp ** 2, plain_amp ** 2
+        m = Sr > 1e-10 * Sr.max()
+        rel = np.abs(S[m] - Sr[m]) / Sr[m]
+        extra["plain_fp64"] = {"value": transitions / (sp["device_ms"] * 1e-3), "unit": UNIT,
+                               "ms_per_step": sp["device_ms"], "kernel_launches": sp["kernel_launches"]}
+        extra["speedup_vs_plain_fp64"] = extra["plain_fp64"]["ms_per_step"] / ms_step
+        extra["accuracy"] = {"reference": "plain FP64 GPU path", "lines_checked": int(m.sum()),
+                             "max_rel_err_S": float(rel.max()), "p99_rel_err_S": float(np.quantile(rel, 0.99)),
+                             "domain": "S > 1e-10 S_max", "refined_lines": st["refined"],
+                             "uncertified": st["uncertified"], "uncertified_weak": st["uncertified_weak"]}
+        eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT)   # leave the split result resident
+
+    # e2e: host buffers through the C ABI (inputs up, S and A down), every step
+    vl_h, vu_h = pinned(inp["vl"]), pinned(inp["vu"])
+    S_h, A_h = pinned(np.zeros((B, NU))), pinned(np.zeros((B, NU)))
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.upload_eigvecs(0, GI, vl_h)
+        eng.upload_eigvecs(1, GF, vu_h)
+        eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT)
+        eng.lines(inp["eI"], inp["eF"], JI, JF, intensity=False, want=("S", "A"), out_S=S_h, out_A=A_h)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_step = float(np.median(e2e_ms))
+    h2d = inp["vl"].nbytes + inp["vu"].nbytes
+    d2h = 2 * B * NU * 8
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    # algorithmic tensor work of the amplitude GEMM: digit products x 2 B N_up N_F
+    NF = int(inp["infl"][1].Ntot[GF])
+    prods2 = st["slices2"] * (st["slices2"] + 1) // 2
+    alg2 = prods2 * 2.0 * B * NU * NF
+    g2ms = float(np.median(g2))
+    achieved = alg2 / (g2ms * 1e-3) / 1e12
+    traffic = None
+    try:
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))["gemm2_bytes_per_launch"]
+    except Exception:
+        pass
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(inp, 4 if args.small else 8)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+               "config": {"workload": WORKLOAD, "lower_states": B, "upper_states": NU, "N_v": inp["nv"],
+                          "lower_dim": int(inp["infl"][0].Ntot[GI]), "upper_dim": NF,
+                          "l2": "inputs larger than L2 (BF16 digits of the upper vectors ~2 GB per step)",
+                          "parallelism": f"replicas by lower-state range x{ws}",
+                          "precision": f"Ozaki digits: GEMM1 beta={st['beta1']} x{st['slices1']}, "
+                                       f"GEMM2 beta={st['beta2']} x{st['slices2']} chunks={st['chunks2']}; "
+                                       "exact FP32 accumulation, FP64 recombination + refinement"},
+               "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                            "frac": achieved / peak, "traffic": traffic,
+                            "kernel": "k_digit_gemm (amplitude GEMM)", "kernel_ms": g2ms,
+                            "algorithmic_flops": alg2, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
+               "cpu_baseline": cpu,
+               "e2e": {"value": ws * transitions / (e2e_step * 1e-3), "unit": UNIT, "ms_per_step": e2e_step,
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+               "clocks": clk.summary(),
+               "gpu_launches": int(st["kernel_launches"]) * args.steps,
+               "gemm1_ms": float(np.median(g1)), "gemm2_ms": g2ms, "wall_ms_per_step": wall * 1e3 / args.steps,
+               "tensor_flops_executed_per_step": st["tensor_flops"]}
+        out.update(extra)
+        print(json.dumps(out), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -134,29 +134,35 @@ struct Eig {
 
 struct StatsDev {
     DevArray<int> e, nnz;
-    DevArray<float> l1, dn, inerr;
+    DevArray<float> l2, dn, dnv, rnv, inerr;
     gain_status alloc(size_t rows, int nch, bool with_inerr) {
         GAIN_TRY(e.alloc(rows));
         GAIN_TRY(nnz.alloc(rows));
-        GAIN_TRY(l1.alloc(rows));
+        GAIN_TRY(l2.alloc(rows));
         GAIN_TRY(dn.alloc(rows * (size_t)nch));
+        GAIN_TRY(dnv.alloc(rows * (size_t)split::MAX_SLICES));
+        GAIN_TRY(rnv.alloc(rows * (size_t)split::MAX_SLICES));
         if (with_inerr) GAIN_TRY(inerr.alloc(rows));
         return GAIN_OK;
     }
     gain_status zero(cudaStream_t st, size_t rows, int nch, bool with_inerr) {
         GAIN_TRY(e.zero(st, rows));
         GAIN_TRY(nnz.zero(st, rows));
-        GAIN_TRY(l1.zero(st, rows));
+        GAIN_TRY(l2.zero(st, rows));
         GAIN_TRY(dn.zero(st, rows * (size_t)nch));
+        GAIN_TRY(dnv.zero(st, rows * (size_t)split::MAX_SLICES));
+        GAIN_TRY(rnv.zero(st, rows * (size_t)split::MAX_SLICES));
         if (with_inerr) GAIN_TRY(inerr.zero(st, rows));
         return GAIN_OK;
     }
     split::RowStats view(bool with_inerr) {
         split::RowStats r;
         r.e = e.p;
-        r.l1 = l1.p;
         r.nnz = nnz.p;
+        r.l2 = l2.p;
         r.dn = dn.p;
+        r.dnv = dnv.p;
+        r.rnv = rnv.p;
         r.inerr = with_inerr ? inerr.p : nullptr;
         return r;
     }
@@ -411,10 +417,10 @@ struct SplitParams {
 // Digits and chunking from the inner length K of the exact accumulations: the Cauchy-Schwarz
 // certificate needs ||d_i|| ||d_j|| < 2^24 over every chunk; balanced residual digits have
 // ||d||^2 ~ K 4^beta / 12, so K_chunk 4^beta / 12 <= 2^23 leaves a factor-two margin.
-SplitParams choose_params(int K, const gain_split_opts* o) {
+SplitParams choose_params(int K, const gain_split_opts* o, int bits) {
     SplitParams p;
     p.beta = (o && o->beta) ? o->beta : 7;
-    p.slices = (o && o->slices) ? o->slices : (49 + p.beta - 1) / p.beta;
+    p.slices = (o && o->slices) ? o->slices : (bits + p.beta - 1) / p.beta;
     if (o && o->kchunks) {
         p.chunks = o->kchunks;
     } else {
@@ -425,13 +431,11 @@ SplitParams choose_params(int K, const gain_split_opts* o) {
     return p;
 }
 
-void bound_consts(const SplitParams& p, int nprods, float* c_l1, float* c_nnz, float* c_rec) {
-    const double rho = 1.0 / (1.0 - std::ldexp(1.0, -p.beta));
-    const double q = (double)p.slices * p.beta;
-    const double h = std::ldexp(1.0, -(int)q - 1);
-    *c_l1 = (float)(h * (1.0 + rho) * 1.001);
-    *c_nnz = (float)(h * (rho * (p.slices - 1) / 2.0 + 2.0 * rho * std::ldexp(1.0, -p.beta)) * 1.001);
-    *c_rec = (float)(((double)nprods * std::ldexp(1.0, -46) + std::ldexp(1.0, -52)) * rho * rho * 1.1);
+// Bound of the int64 fixed-point recombination, units of 2^{eA+eB}: each digit product adds
+// at most one truncated unit of 2^{-kFix} (in digit units 2^{-2 beta}); the final int64 ->
+// double conversion adds a relative 2^-53, negligible against tol, absorbed by the 1.01.
+float fix_const(const SplitParams& p, int nprods) {
+    return (float)((double)nprods * std::ldexp(1.0, -split::kFix - 2 * p.beta) * 1.01);
 }
 
 std::vector<split::Prod> make_prods(const SplitParams& p) {
@@ -576,7 +580,7 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     a.nchunks = p.chunks;
     a.nkb_total = nkb_total;
     a.st = stv.view(with_inerr);
-    a.inerr_prev = inerr_prev;
+    a.inerr2_prev = inerr_prev;
     a.e_prev = e_prev;
     GAIN_CUDA(split::launch_slice(a, e->st));
     return GAIN_OK;
@@ -590,7 +594,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         return set_error(GAIN_ERR_UNSUPPORTED,
                          "split path needs symmetry blocks whose expansion selects one primitive per function");
     if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "split path handles non-degenerate symmetries only");
-    const double tol = (opts && opts->tol > 0) ? opts->tol : 2e-9;
+    const double tol = (opts && opts->tol > 0) ? opts->tol : 4.5e-9;
     cudaStream_t st = e->st;
     GAIN_CUDA(cudaEventRecord(e->ev[0], st));
     GAIN_TRY(build_layout(e, j, mI, mF));
@@ -598,17 +602,19 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
 
-    const SplitParams p1 = choose_params(L.W, opts);
+    // First GEMM: 56 bits (its error reaches every amplitude through ||dH||_2 ||u||_2), one
+    // inner chunk per band tile, digits narrowed until that single chunk stays exact.
+    // Second GEMM: 49 bits; options (beta, slices, kchunks) apply to it.
+    gain_split_opts o1{};
+    if (opts) o1.beta = opts->beta;
+    const SplitParams p1 = choose_params(L.W, &o1, 56);
     SplitParams p1x = p1;
-    p1x.chunks = 1;   // band tiles have their own k ranges: one chunk, certified per row
-    if (p1.chunks > 1 && !(opts && opts->kchunks)) {
-        // shrink digits of the first GEMM until one chunk suffices
-        while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
-            --p1x.beta;
-            p1x.slices = (49 + p1x.beta - 1) / p1x.beta;
-        }
+    p1x.chunks = 1;
+    while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
+        --p1x.beta;
+        p1x.slices = (56 + p1x.beta - 1) / p1x.beta;
     }
-    const SplitParams p2 = choose_params(L.fpad, opts);
+    const SplitParams p2 = choose_params(L.fpad, opts, 49);
     if (p1x.slices * p1x.beta > 62 || p2.slices * p2.beta > 62 || p1x.slices > split::MAX_SLICES ||
         p2.slices > split::MAX_SLICES || p1x.beta < 2 || p1x.beta > 8 || p2.beta < 2 || p2.beta > 8 ||
         2 * (p2.slices - 1) * p2.beta > 126 || 2 * (p1x.slices - 1) * p1x.beta > 126)
@@ -686,8 +692,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g1.ldo = L.fpad;
     g1.A = e->Vst.view(false);
     g1.B = L.bandStats.view(false);
-    bound_consts(p1x, (int)pr1.size(), &g1.c_l1, &g1.c_nnz, &g1.c_rec);
-    g1.rowerr_units = e->rowerr.p;
+    g1.c_fix = fix_const(p1x, (int)pr1.size());
+    g1.rowerr2 = e->rowerr.p;
     g1.flag_mode = 0;
     g1.tol = (float)tol;
     g1.flags = e->flags1.p;
@@ -715,7 +721,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     rh.H = e->H.p;
     rh.ldh = L.fpad;
     rh.eA = e->Vst.e.p;
-    rh.rowerr_units = e->rowerr.p;
+    rh.rowerr2 = e->rowerr.p;
     GAIN_CUDA(split::launch_refine_h(rh, 2 * e->num_sms, st));
 
     // ---- H -> digits, upper vectors -> digits
@@ -767,8 +773,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.ldo = Nupad;
     g2.A = e->Hst.view(true);
     g2.B = e->Ust.view(false);
-    bound_consts(p2, (int)pr2.size(), &g2.c_l1, &g2.c_nnz, &g2.c_rec);
-    g2.rowerr_units = nullptr;
+    g2.c_fix = fix_const(p2, (int)pr2.size());
+    g2.rowerr2 = nullptr;
+    g2.absmax = e->ull.p + 2;
     g2.flag_mode = 1;
     g2.tol = (float)tol;
     g2.flags = e->flags2.p;
@@ -795,7 +802,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     ra.amp = e->amp.p;
     ra.lda = Nupad;
     ra.tol = tol;
+    ra.absmax = e->ull.p + 2;
+    ra.amp_floor = std::sqrt((opts && opts->s_floor > 0) ? opts->s_floor : 1e-10);
     ra.uncertified = e->ull.p;
+    ra.uncertified_weak = e->ull.p + 3;
     GAIN_CUDA(split::launch_refine_amp(ra, 4 * e->num_sms, st));
     GAIN_CUDA(cudaEventRecord(e->ev[1], st));
     GAIN_CUDA(cudaStreamSynchronize(st));
@@ -823,6 +833,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         stats->cols = Nu;
         stats->refined = (long long)std::min<unsigned>(cnt[1], kMaxFlags) + std::min<unsigned>(cnt[0], kMaxFlags);
         stats->uncertified = (long long)unc[0];
+        stats->uncertified_weak = (long long)unc[3];
+        stats->amp_max = __builtin_bit_cast(double, unc[2]);
         stats->inexact = (long long)cnt[0];
         stats->beta1 = p1x.beta;
         stats->slices1 = p1x.slices;

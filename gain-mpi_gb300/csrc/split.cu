@@ -281,11 +281,18 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         }
     } else {
         // ---------------- epilogue: warps 2..5, one TMEM lane (output row) per thread
+        // Each digit product arrives as an FP32 accumulator holding an exact integer (|acc| <
+        // 2^24 where certified).  It is added, shifted to its weight, into an int64 fixed-point
+        // running sum (TMEM columns 256..383 low words, 384..511 high words); only the
+        // weights below 2^{-kFix} are truncated (floor), at most one unit per product.
         const int q = warp & 3;
         const int row_in_tile = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        const float c_l1 = a.c_l1, c_nnz = a.c_nnz, c_rec = a.c_rec;
         const float two24 = 16777216.0f;
+        const int s = a.slices;
+        float wdig[MAX_SLICES];   // 2^{-(i+1) beta}
+#pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i) wdig[i] = pow2f(-(i + 1) * a.beta);
         uint32_t acc_cnt = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
@@ -302,36 +309,28 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     break;
                 }
                 tc_fence_after();
-                const float w = pow2f(-pr.t * a.beta);
+                const int sh = kFix - pr.t * a.beta;
 #pragma unroll 1
                 for (int c = 0; c < BN / 32; ++c) {
-                    uint32_t acc[32], hi_r[32], lo_r[32];
+                    uint32_t acc[32], lo_r[32], hi_r[32];
                     tmem_ld32(tmem + lane_off + b * BN + c * 32, acc);
                     if (!first) {
-                        tmem_ld32(tmem + lane_off + 256 + c * 32, hi_r);
-                        tmem_ld32(tmem + lane_off + 384 + c * 32, lo_r);
+                        tmem_ld32(tmem + lane_off + 256 + c * 32, lo_r);
+                        tmem_ld32(tmem + lane_off + 384 + c * 32, hi_r);
                     }
                     tmem_wait_ld();
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
-                        const float x = __fmul_rn(__uint_as_float(acc[j]), w);
-                        if (first) {
-                            hi_r[j] = __float_as_uint(x);
-                            lo_r[j] = 0u;
-                        } else {
-                            const float h = __uint_as_float(hi_r[j]);
-                            const float s = __fadd_rn(h, x);
-                            const float bb = __fsub_rn(s, h);
-                            const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(x, bb));
-                            // renormalise (hi, lo) so |lo| <= ulp(hi)/2 after every product
-                            const float tt = __fadd_rn(__uint_as_float(lo_r[j]), e);
-                            const float nh = __fadd_rn(s, tt);
-                            hi_r[j] = __float_as_uint(nh);
-                            lo_r[j] = __float_as_uint(__fsub_rn(tt, __fsub_rn(nh, s)));
-                        }
+                        const long long ai = (long long)__float2int_rz(__uint_as_float(acc[j]));
+                        const long long v = sh >= 0 ? (ai << sh) : (ai >> (-sh));
+                        long long run = first ? 0ll
+                                              : (long long)(((unsigned long long)hi_r[j] << 32) | lo_r[j]);
+                        run += v;
+                        lo_r[j] = (uint32_t)(unsigned long long)run;
+                        hi_r[j] = (uint32_t)((unsigned long long)run >> 32);
                     }
-                    tmem_st32(tmem + lane_off + 256 + c * 32, hi_r);
-                    tmem_st32(tmem + lane_off + 384 + c * 32, lo_r);
+                    tmem_st32(tmem + lane_off + 256 + c * 32, lo_r);
+                    tmem_st32(tmem + lane_off + 384 + c * 32, hi_r);
                 }
                 tmem_wait_st();
                 tc_fence_before();
@@ -340,61 +339,89 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 first = false;
             }
             if (!ok) break;
-            // ---- finalize the tile: value, certified bound, flags
+            // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags
             const int r = tl.m0 + row_in_tile;
             const bool rvalid = r < a.rows_valid;
             const int eA = a.A.e[r];
-            const float l1A = a.A.l1[r];
             const int nnzA = a.A.nnz[r];
+            const float l2A = a.A.l2[r];
             const float inA = a.A.inerr ? a.A.inerr[r] : 0.0f;
-            float dnA[MAX_CHUNKS];
+            float dnA[MAX_CHUNKS], dvA[MAX_SLICES], rvA[MAX_SLICES];
 #pragma unroll
             for (int c = 0; c < MAX_CHUNKS; ++c) dnA[c] = c < a.nchunks ? a.A.dn[(long)r * a.nchunks + c] : 0.0f;
-            float rowerr = 0.0f;
+#pragma unroll
+            for (int i = 0; i < MAX_SLICES; ++i) {
+                dvA[i] = i < s ? a.A.dnv[(long)r * MAX_SLICES + i] : 0.0f;
+                rvA[i] = i < s ? a.A.rnv[(long)r * MAX_SLICES + i] : 0.0f;
+            }
+            float rowerr2 = 0.0f;
+            unsigned long long vmax = 0ull;
             double* orow = a.out + (long)r * a.ldo;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
-                uint32_t hi_r[32], lo_r[32];
+                uint32_t lo_r[32], hi_r[32];
                 if (!first) {
-                    tmem_ld32(tmem + lane_off + 256 + c * 32, hi_r);
-                    tmem_ld32(tmem + lane_off + 384 + c * 32, lo_r);
+                    tmem_ld32(tmem + lane_off + 256 + c * 32, lo_r);
+                    tmem_ld32(tmem + lane_off + 384 + c * 32, hi_r);
                     tmem_wait_ld();
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) { hi_r[j] = 0u; lo_r[j] = 0u; }
+                    for (int j = 0; j < 32; ++j) { lo_r[j] = 0u; hi_r[j] = 0u; }
                 }
-#pragma unroll
+#pragma unroll 2
                 for (int j = 0; j < 32; ++j) {
                     const int col = tl.n0 + c * 32 + j;
-                    const float hf = __uint_as_float(hi_r[j]);
-                    const double R = (double)hf + (double)__uint_as_float(lo_r[j]);
-                    const int eB = a.B.e[col];
-                    const double v = R * pow2d(eA + eB - 2 * a.beta);
+                    const long long run = (long long)(((unsigned long long)hi_r[j] << 32) | lo_r[j]);
+                    const int eB = __ldg(&a.B.e[col]);
+                    const double v = (double)run * pow2d(eA + eB - 2 * a.beta - kFix);
                     orow[col] = v;
-                    const int nnzB = a.B.nnz[col];
+                    const int nnzB = __ldg(&a.B.nnz[col]);
                     if (nnzA == 0 || nnzB == 0) continue;
-                    const float l1B = a.B.l1[col];
-                    float bound = __fmaf_ru(c_l1, __fadd_ru(l1A, l1B), 0.0f);
-                    bound = __fmaf_ru(c_nnz, (float)min(nnzA, nnzB), bound);
-                    bound = __fmaf_ru(c_rec, fminf(l1A, l1B), bound);
-                    bound = __fmaf_ru(inA, l1B, bound);
                     bool exact = true;
 #pragma unroll
                     for (int cc = 0; cc < MAX_CHUNKS; ++cc)
-                        if (cc < a.nchunks && __fmul_ru(dnA[cc], a.B.dn[(long)col * a.nchunks + cc]) >= two24)
+                        if (cc < a.nchunks &&
+                            __fmul_ru(dnA[cc], __ldg(&a.B.dn[(long)col * a.nchunks + cc])) >= two24)
                             exact = false;
-                    if (a.rowerr_units) rowerr = fmaxf(rowerr, __fmul_ru(bound, pow2f(max(-126, min(127, eB)))));
+                    // |x^ y^ - C| <= ||x^ - X|| ||y^|| + sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)||
+                    // and the same with x and y exchanged; the smaller of the two holds.
+                    const float l2B = __ldg(&a.B.l2[col]);
+                    const float* dvB = a.B.dnv + (long)col * MAX_SLICES;
+                    const float* rvB = a.B.rnv + (long)col * MAX_SLICES;
+                    float bA = __fmul_ru(rvA[s - 1], l2B);
+                    float bB = __fmul_ru(__ldg(&rvB[s - 1]), l2A);
+#pragma unroll
+                    for (int i = 0; i < MAX_SLICES; ++i) {
+                        if (i < s) {
+                            bA = __fmaf_ru(__fmul_ru(wdig[i], dvA[i]), __ldg(&rvB[s - 1 - i]), bA);
+                            bB = __fmaf_ru(__fmul_ru(wdig[i], __ldg(&dvB[i])), rvA[s - 1 - i], bB);
+                        }
+                    }
+                    float bound = __fadd_ru(fminf(bA, bB), a.c_fix);
+                    bound = __fmaf_ru(inA, l2B, bound);
+                    if (exact && rvalid && col < a.cols_valid) {
+                        const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+                        vmax = vb > vmax ? vb : vmax;
+                    }
+                    if (a.rowerr2) {
+                        const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
+                        rowerr2 = __fmaf_ru(bb, bb, rowerr2);
+                    }
                     bool flag = !exact;
-                    if (a.flag_mode == 1) flag = flag || (bound > a.tol * fabsf(hf) * pow2f(-2 * a.beta));
+                    if (a.flag_mode == 1) {
+                        // |value| in units of 2^{eA+eB}: run 2^{-2 beta - kFix}
+                        const float av = fabsf((float)run) * pow2f(-2 * a.beta - kFix);
+                        flag = flag || (bound > a.tol * av);
+                    }
                     if (flag && rvalid && col < a.cols_valid) {
                         const unsigned int idx = atomicAdd(a.nflags, 1u);
                         if ((int)idx < a.max_flags) a.flags[idx] = make_int2(r, col);
                     }
                 }
             }
-            if (a.rowerr_units && rvalid && rowerr > 0.0f)
-                atomicMax((int*)&a.rowerr_units[r], __float_as_int(rowerr));
-            // make sure TMEM reads finished before the next tile overwrites hi/lo
+            if (a.absmax && vmax) atomicMax(a.absmax, vmax);
+            if (a.rowerr2 && rvalid && rowerr2 > 0.0f) atomicAdd(&a.rowerr2[r], rowerr2);
+            // make sure TMEM reads finished before the next tile overwrites the running sums
             tc_fence_before();
         }
     }
@@ -427,6 +454,7 @@ k_slice(const SliceArgs a) {
     __shared__ unsigned long long red_u[SLICE_THREADS / 32];
     __shared__ float red_f[SLICE_THREADS / 32];
     __shared__ int red_i[SLICE_THREADS / 32];
+    __shared__ float red_t[SLICE_THREADS / 32][MAX_SLICES];
     __shared__ unsigned int red_d[SLICE_THREADS / 32][MAX_SLICES * MAX_CHUNKS];
 
     // pass 1: max |x| through the IEEE bit pattern (integer compares only)
@@ -452,9 +480,12 @@ k_slice(const SliceArgs a) {
     const long sstride = a.slice_stride;
     __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
 
-    float l1 = 0.0f;
     int nnz = 0;
+    float l2sq = 0.0f;
+    float tsq[MAX_SLICES];
     unsigned int dsq[MAX_SLICES * MAX_CHUNKS];
+#pragma unroll
+    for (int i = 0; i < MAX_SLICES; ++i) tsq[i] = 0.0f;
 #pragma unroll
     for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i) dsq[i] = 0u;
     const long mask = (1l << beta) - 1l, halfb = 1l << (beta - 1);
@@ -491,6 +522,15 @@ k_slice(const SliceArgs a) {
             }
         }
         d[0] = (int)v;
+        // tails x^(rounded) - X^(n) = sum_{i>n} d_i 2^{-(i+1) beta}, squared into tsq[n]
+        float tail = 0.0f;
+#pragma unroll
+        for (int i = MAX_SLICES - 1; i >= 1; --i) {
+            if (i < s) {
+                tail = __fadd_rn(tail, (float)d[i] * pow2f(-(i + 1) * beta));
+                tsq[i - 1] = __fmaf_ru(tail, tail, tsq[i - 1]);
+            }
+        }
 #pragma unroll
         for (int i = 0; i < MAX_SLICES; ++i) {
             if (i < s) {
@@ -503,33 +543,53 @@ k_slice(const SliceArgs a) {
         if (I != 0) {
             ++nnz;
             const unsigned long long aI = (unsigned long long)(I < 0 ? -I : I);
-            l1 = __fadd_ru(l1, __fmul_ru(__ull2float_ru(aI), inv2q));
+            const float xv = __fmul_ru(__ull2float_ru(aI), inv2q);
+            l2sq = __fmaf_ru(xv, xv, l2sq);
         }
     }
     // block reductions
     for (int o = 16; o > 0; o >>= 1) {
-        l1 = __fadd_ru(l1, __shfl_xor_sync(0xffffffffu, l1, o));
+        l2sq = __fadd_ru(l2sq, __shfl_xor_sync(0xffffffffu, l2sq, o));
         nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
     }
+#pragma unroll
+    for (int i = 0; i < MAX_SLICES; ++i)
+        for (int o = 16; o > 0; o >>= 1) tsq[i] = __fadd_ru(tsq[i], __shfl_xor_sync(0xffffffffu, tsq[i], o));
 #pragma unroll
     for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i)
         for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
     if ((tid & 31) == 0) {
-        red_f[tid >> 5] = l1;
+        red_f[tid >> 5] = l2sq;
         red_i[tid >> 5] = nnz;
+#pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i) red_t[tid >> 5][i] = tsq[i];
 #pragma unroll
         for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i) red_d[tid >> 5][i] = dsq[i];
     }
     __syncthreads();
     if (tid == 0) {
-        float L = 0.0f;
+        float L2 = 0.0f;
         int N = 0;
-        for (int w = 0; w < SLICE_THREADS / 32; ++w) { L = __fadd_ru(L, red_f[w]); N += red_i[w]; }
-        // the bound uses |x 2^-e|; digits represent it to within 2^{-q-1} per entry
-        L = __fadd_ru(L, __fmul_ru((float)N, pow2f(-q - 1)));
+        for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
+        // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
+        const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
+        const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
         a.st.e[row] = e;
-        a.st.l1[row] = L;
         a.st.nnz[row] = N;
+        a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(L2), slack), dq);
+        for (int i = 0; i < MAX_SLICES; ++i) {
+            float tq = 0.0f;
+            unsigned int dd = 0;
+            if (i < s) {
+                for (int w = 0; w < SLICE_THREADS / 32; ++w) {
+                    tq = __fadd_ru(tq, red_t[w][i]);
+                    for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
+                }
+            }
+            a.st.dnv[(long)row * MAX_SLICES + i] = i < s ? __fsqrt_ru(__uint2float_ru(dd)) : 0.0f;
+            a.st.rnv[(long)row * MAX_SLICES + i] =
+                i < s ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
+        }
         for (int c = 0; c < a.nchunks; ++c) {
             unsigned int m = 0;
             for (int i = 0; i < s; ++i) {
@@ -541,9 +601,9 @@ k_slice(const SliceArgs a) {
         }
         if (a.st.inerr) {
             float v = 0.0f;
-            if (a.inerr_prev && !zero_row) {
+            if (a.inerr2_prev && !zero_row) {
                 const int de = a.e_prev[row] - e;
-                v = __fmul_ru(a.inerr_prev[row], pow2f(max(-126, min(127, de))));
+                v = __fmul_ru(__fmul_ru(__fsqrt_ru(a.inerr2_prev[row]), 1.0001f), pow2f(max(-126, min(127, de))));
                 if (de > 127) v = __int_as_float(0x7f800000);   // cannot certify: infinite bound
             }
             a.st.inerr[row] = v;
@@ -614,10 +674,11 @@ __global__ void k_refine_h(const RefineHArgs a) {
         }
         if (lane == 0) {
             a.H[(long)r * a.ldh + c] = acc;
-            // rounding error of this FP64 sum (gamma_n with n <= len + 32), in units of 2^{eA}
+            // rounding error of this FP64 sum (gamma_n with n <= len + 32), in units of 2^{eA},
+            // added to the row's sum of squared element bounds
             const double err = aacc * (double)(len + 64) * 1.1102230246251565e-16 * 1.01;
             const float u = __double2float_ru(err * pow2d(-a.eA[r]));
-            atomicMax((int*)&a.rowerr_units[r], __float_as_int(u));
+            atomicAdd(&a.rowerr2[r], __fmul_ru(u, u));
         }
     }
 }
@@ -632,23 +693,27 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
         const int r = rc.x, c = rc.y;
         const double* u = a.U + (long)a.col_level[c] * a.nsize;
         const double* h = a.H + (long)r * a.ldh;
-        double acc = 0.0, aacc = 0.0, l1 = 0.0;
+        double acc = 0.0, aacc = 0.0, l2 = 0.0;
         for (int s = lane; s < a.nsize; s += 32) {
             const double uv = u[s], hv = h[a.colpos[s]];
             acc = __fma_rn(uv, hv, acc);
             aacc += fabs(uv * hv);
-            l1 += fabs(uv);
+            l2 = __fma_rn(uv, uv, l2);
         }
         for (int o = 16; o > 0; o >>= 1) {
             acc += __shfl_xor_sync(0xffffffffu, acc, o);
             aacc += __shfl_xor_sync(0xffffffffu, aacc, o);
-            l1 += __shfl_xor_sync(0xffffffffu, l1, o);
+            l2 += __shfl_xor_sync(0xffffffffu, l2, o);
         }
         if (lane == 0) {
             a.amp[(long)r * a.lda + c] = acc;
+            // |<dH, u>| <= ||dH||_2 ||u||_2, plus the rounding of this FP64 dot product
             const double herr = (double)a.h_inerr[r] * pow2d(a.eH[r]);
-            const double bound = herr * l1 * 1.001 + aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
-            if (!(bound <= a.tol * fabs(acc))) atomicAdd(a.uncertified, 1ull);
+            const double bound = herr * sqrt(l2) * 1.001 + aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
+            if (!(bound <= a.tol * fabs(acc))) {
+                const double amax = __longlong_as_double((long long)*a.absmax);
+                atomicAdd(fabs(acc) >= a.amp_floor * amax ? a.uncertified : a.uncertified_weak, 1ull);
+            }
         }
     }
 }

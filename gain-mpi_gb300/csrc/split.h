@@ -39,13 +39,19 @@ struct Prod {
     int chunk;      // inner-dimension chunk
 };
 
-// Per-row data of a sliced operand.
+// Fixed-point position of the exact recombination: the running sum of the digit products
+// of one output is an int64 in units of 2^{-kFix} (of the product's digit units 2^{-2 beta}).
+constexpr int kFix = 36;
+
+// Per-row data of a sliced operand (x^ = x 2^{-e}; all norms rounded up).
 struct RowStats {
     int* e;          // scale exponent (row values < 2^e)
-    float* l1;       // sum |x| 2^{-e}, rounded up
     int* nnz;        // non-zero count
-    float* dn;       // [rows * nchunks]: max_i ||d_i restricted to chunk||_2, rounded up
-    float* inerr;    // optional: input error of the row in units of 2^e (rounded up)
+    float* l2;       // ||x^||_2
+    float* dn;       // [rows * nchunks]: max_i ||d_i restricted to chunk||_2 (exactness certificate)
+    float* dnv;      // [rows * MAX_SLICES]: ||d_i||_2 over the whole row
+    float* rnv;      // [rows * MAX_SLICES]: ||x^ - X^(n)||_2, X^(n) = sum_{i<=n} d_i 2^{-(i+1) beta}
+    float* inerr;    // optional: ||input error of the row||_2 in units of 2^e
 };
 
 struct GemmArgs {
@@ -59,10 +65,12 @@ struct GemmArgs {
     double* out;
     long ldo;
     RowStats A, B;
-    // bound constants (units of 2^{eA+eB})
-    float c_l1, c_nnz, c_rec;
-    // GEMM1: per-row maximum bound in units of 2^{eA} (atomic max on float bits), may be null
-    float* rowerr_units;
+    // bound of the fixed-point recombination (units of 2^{eA+eB}): nprods 2^{-kFix - 2 beta}
+    float c_fix;
+    // GEMM1: per row, sum over columns of (bound in units of 2^{eA})^2 (atomic add), may be null
+    float* rowerr2;
+    // optional: largest |value| over valid outputs (atomic max on the IEEE bits)
+    unsigned long long* absmax;
     // flags
     int flag_mode;          // 0: inexact accumulation only; 1: also bound > tol |value|
     float tol;
@@ -94,7 +102,7 @@ struct SliceArgs {
     int nchunks;            // chunks of the destination inner dimension for dn
     int nkb_total;          // k-blocks of BK the chunks split (chunk c: [c n/nch, (c+1) n/nch))
     RowStats st;
-    const float* inerr_prev;   // optional: row error in units of 2^{e_prev}
+    const float* inerr2_prev;  // optional: squared row error in units of 2^{2 e_prev}
     const int* e_prev;         // exponent those units refer to
 };
 cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st);
@@ -134,7 +142,7 @@ struct RefineHArgs {
     double* H;
     long ldh;
     const int* eA;
-    float* rowerr_units;
+    float* rowerr2;
 };
 cudaError_t launch_refine_h(const RefineHArgs& a, int max_blocks, cudaStream_t st);
 
@@ -149,12 +157,15 @@ struct RefineAmpArgs {
     const int* colpos;      // padded position of each upper symmetry index
     const double* H;
     long ldh;
-    const float* h_inerr;   // first-GEMM error of each H row in units of 2^{eH}
+    const float* h_inerr;   // ||first-GEMM error of the H row||_2 in units of 2^{eH}
     const int* eH;
     double* amp;
     long lda;
     double tol;
-    unsigned long long* uncertified;
+    const unsigned long long* absmax;    // largest |amp| of the run (IEEE bits)
+    double amp_floor;                    // sqrt(s_floor): certification domain |amp| >= floor*max
+    unsigned long long* uncertified;     // in the domain
+    unsigned long long* uncertified_weak;  // below it
 };
 cudaError_t launch_refine_amp(const RefineAmpArgs& a, int max_blocks, cudaStream_t st);
 

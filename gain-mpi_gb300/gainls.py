@@ -44,13 +44,14 @@ class PairJob(ctypes.Structure):
 
 class SplitOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("slices", ctypes.c_int), ("beta", ctypes.c_int),
-                ("kchunks", ctypes.c_int)]
+                ("kchunks", ctypes.c_int), ("s_floor", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("device_ms", ctypes.c_double), ("rows", ctypes.c_longlong), ("cols", ctypes.c_longlong),
                 ("refined", ctypes.c_longlong), ("uncertified", ctypes.c_longlong),
-                ("inexact", ctypes.c_longlong),
+                ("uncertified_weak", ctypes.c_longlong), ("inexact", ctypes.c_longlong),
+                ("amp_max", ctypes.c_double),
                 ("beta1", ctypes.c_int), ("slices1", ctypes.c_int), ("chunks1", ctypes.c_int),
                 ("beta2", ctypes.c_int), ("slices2", ctypes.c_int), ("chunks2", ctypes.c_int),
                 ("products1", ctypes.c_int), ("products2", ctypes.c_int),
@@ -226,10 +227,11 @@ class Engine:
 
     def run_pair(self, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
                  upper_levels: Sequence[int], path: int = PATH_SPLIT, tol: float = 0.0,
-                 slices: int = 0, beta: int = 0, kchunks: int = 0, raise_on_error: bool = True) -> dict:
+                 slices: int = 0, beta: int = 0, kchunks: int = 0, s_floor: float = 0.0,
+                 raise_on_error: bool = True) -> dict:
         lo, up = _i32(lower_levels), _i32(upper_levels)
         job = PairJob(jindI, gammaI, jindF, gammaF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
-        opts = SplitOpts(tol, slices, beta, kchunks)
+        opts = SplitOpts(tol, slices, beta, kchunks, s_floor)
         st = Stats()
         s = lib().gain_run_pair(self.h, ctypes.byref(job), path, ctypes.byref(opts), ctypes.byref(st))
         self._shape = (len(lo), len(up))
@@ -254,12 +256,15 @@ class Engine:
         return out.reshape(self._shape)
 
     def lines(self, eI, eF, jI, jF, temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0,
-              freq=(-1e9, 1e9), gnsF=1.0, intensity=True, want=("S", "A", "I", "keep")):
+              freq=(-1e9, 1e9), gnsF=1.0, intensity=True, want=("S", "A", "I", "keep"),
+              out_S=None, out_A=None):
+        """S, A (and I, keep) of the last run; out_S / out_A may be preallocated (e.g. pinned)
+        contiguous float64 arrays of nlower*nupper elements."""
         eI, eF = _f64(eI), _f64(eF)
         n = self._shape[0] * self._shape[1]
         prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
-        S = np.empty(n) if "S" in want else None
-        A = np.empty(n) if "A" in want else None
+        S = (out_S.reshape(-1) if out_S is not None else np.empty(n)) if "S" in want else None
+        A = (out_A.reshape(-1) if out_A is not None else np.empty(n)) if "A" in want else None
         I = np.empty(n) if (intensity and "I" in want) else None
         K = np.empty(n, np.uint8) if "keep" in want else None
         nl = ctypes.c_longlong()

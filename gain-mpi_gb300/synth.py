@@ -137,7 +137,13 @@ def make_dipole(nv: int, seed: int = DIPOLE_SEED) -> np.ndarray:
     """[3, N, N] array whose flat order is the flipped piece layout f + i N + d N N."""
     rng = np.random.default_rng(seed)
     idx = np.arange(nv)
-    decay = 0.5 * np.exp(-np.abs(idx[:, None] - idx[None, :]) / 20.0)
+    # exp(-k/20) as successive powers of the double nearest e^{-1/20}: IEEE products give the
+    # same bits on every machine, unlike libm's exp
+    pw = np.empty(max(nv, 1))
+    pw[0] = 1.0
+    for k in range(1, nv):
+        pw[k] = pw[k - 1] * 0.951229424500714
+    decay = 0.5 * pw[np.abs(idx[:, None] - idx[None, :])]
     out = np.empty((3, nv, nv), np.float64)
     for d in range(3):
         a = rng.standard_normal((nv, nv)) * decay
@@ -150,14 +156,19 @@ def make_energies(n: int, J: int, gamma: int) -> np.ndarray:
     return np.sort(rng.uniform(0.0, 8000.0, n))
 
 
-def make_eigvecs(n: int, J: int, gamma: int, device: str | None = None) -> np.ndarray:
+def make_eigvecs(n: int, J: int, gamma: int, device: str | None = None,
+                 nstates: int | None = None) -> np.ndarray:
     """Rows are state coefficient vectors (Q[:, k] of QR of a seeded Gaussian matrix).
 
+    nstates < n keeps the first nstates states only; the first k columns of Q depend only
+    on the first k columns of the Gaussian matrix, so they equal the full factorisation's.
     device=None uses numpy's QR; device="cuda" runs the same factorisation through torch on
     the GPU (used only to make large inputs quickly, never on a timed path).
     """
     rng = np.random.default_rng(vec_seed(J, gamma))
     g = rng.standard_normal((n, n))
+    if nstates is not None and nstates < n:
+        g = np.ascontiguousarray(g[:, :nstates])
     if device is None:
         q, r = np.linalg.qr(g)
         s = np.sign(np.diag(r))

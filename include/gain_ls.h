@@ -131,18 +131,25 @@ typedef struct gain_pair_job {
 
 typedef struct gain_split_opts {
     double tol;       /* relative tolerance on each amplitude; lines whose certified bound
-                         exceeds tol*|amp| are recomputed in FP64 (0 -> 2e-9) */
-    int slices;       /* digits per operand (0 -> chosen from beta for ~49 bits) */
-    int beta;         /* bits per digit, 4..8 (0 -> chosen from the inner dimension) */
+                         exceeds tol*|amp| are recomputed in FP64 (0 -> 4.5e-9, so that
+                         S = amp^2 meets 1e-8) */
+    int slices;       /* digits per operand of the amplitude GEMM (0 -> 49 bits; the
+                         rotational-dipole GEMM always keeps 56 bits) */
+    int beta;         /* bits per digit, 2..8 (0 -> 7) */
     int kchunks;      /* inner-dimension chunks for exact FP32 accumulation (0 -> auto) */
+    double s_floor;   /* certification domain: lines with S >= s_floor * S_max must meet tol
+                         (0 -> 1e-10, the domain of the headline accuracy requirement) */
 } gain_split_opts;
 
 typedef struct gain_stats {
     double device_ms;           /* device time of the last run (CUDA events) */
     long long rows, cols;       /* lower x upper amplitudes computed */
     long long refined;          /* split path: amplitudes recomputed in FP64 */
-    long long uncertified;      /* split path: refined lines whose bound still exceeds tol */
+    long long uncertified;      /* split path: refined lines with S >= s_floor S_max whose
+                                   bound still exceeds tol (non-zero -> GAIN_ERR_TOL_NOT_MET) */
+    long long uncertified_weak; /* the same below s_floor S_max (outside the accuracy domain) */
     long long inexact;          /* split path: pairs outside the exact-accumulation guarantee */
+    double amp_max;             /* split path: largest |amplitude| of the run */
     int beta1, slices1, chunks1;  /* first GEMM (lower vectors x rotational-dipole matrix) */
     int beta2, slices2, chunks2;  /* second GEMM (half line strengths x upper vectors) */
     int products1, products2;   /* BF16 digit products per GEMM */

@@ -1,0 +1,92 @@
+// Drives gain::GpuManager (include/gain_gpu_manager.hpp) the way GAIN-MPI's main.cpp drives
+// its GpuManager (main.cpp:172-336), on one block pair read from a flat binary file, and
+// writes the amplitude of every (lower, upper) pair.  Built and run by tests/test_gpu_manager.py.
+//
+// input (little-endian int32 / float64 records, written by the test):
+//   ints:  nv jmax nsym JI JF gI gF nlower nupper startF endF
+//   per J (I then F): dimen, K[dimen], ktau[dimen], vib[dimen], kblock[J+1], kstart[J+1],
+//                     icontr[2 dimen], ijterms[dimen nsym], N[nsym][dimen], Ntot[nsym]
+//   doubles: dipole piece [3 nv (endF-startF)], lower vectors [nlower NtotI],
+//            upper vectors [nupper NtotF]
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "gain_gpu_manager.hpp"
+
+namespace {
+FILE* fin;
+int geti() { int v; if (fread(&v, 4, 1, fin) != 1) { fprintf(stderr, "short read\n"); exit(2); } return v; }
+std::vector<int> getiv(size_t n) { std::vector<int> v(n); if (n && fread(v.data(), 4, n, fin) != n) exit(2); return v; }
+std::vector<double> getdv(size_t n) { std::vector<double> v(n); if (n && fread(v.data(), 8, n, fin) != n) exit(2); return v; }
+struct J { int J, dimen; std::vector<int> K, ktau, vib, kblock, kstart, icontr, ijterms, Ntot; std::vector<std::vector<int>> N; };
+}
+
+int main(int argc, char** argv) {
+    if (argc < 3) { fprintf(stderr, "usage: %s input output\n", argv[0]); return 1; }
+    fin = fopen(argv[1], "rb");
+    if (!fin) return 1;
+    const int nv = geti(), jmax = geti(), nsym = geti(), JI = geti(), JF = geti(), gI = geti(), gF = geti();
+    const int nlower = geti(), nupper = geti(), startF = geti(), endF = geti();
+    J js[2];
+    for (int t = 0; t < 2; ++t) {
+        J& j = js[t];
+        j.J = t == 0 ? JI : JF;
+        j.dimen = geti();
+        j.K = getiv(j.dimen); j.ktau = getiv(j.dimen); j.vib = getiv(j.dimen);
+        j.kblock = getiv(j.J + 1); j.kstart = getiv(j.J + 1);
+        j.icontr = getiv(2 * (size_t)j.dimen); j.ijterms = getiv((size_t)j.dimen * nsym);
+        for (int g = 0; g < nsym; ++g) j.N.push_back(getiv(j.dimen));
+        j.Ntot = getiv(nsym);
+    }
+    std::vector<double> piece = getdv((size_t)3 * nv * (endF - startF));
+    std::vector<double> vl = getdv((size_t)nlower * js[0].Ntot[gI]);
+    std::vector<double> vu = getdv((size_t)nupper * js[1].Ntot[gF]);
+    fclose(fin);
+    try {
+        gain::GpuManager gpu(0, 1);
+        gpu.InitializeAndTransferConstants(jmax, nsym, 1);
+        gpu.TransferDipole(piece.data(), nv, startF, endF, endF - startF);
+        int dimen_max = 0, nsize_max = 0;
+        for (int t = 0; t < 2; ++t) {
+            J& j = js[t];
+            gpu.TransferBasisSet(j.J, j.dimen, j.K.data(), j.ktau.data(), j.vib.data(), j.kblock.data(), j.kstart.data());
+            std::vector<double*> repres;
+            std::vector<std::vector<double>> ones;
+            std::vector<int*> N;
+            for (int g = 0; g < nsym; ++g) {
+                ones.emplace_back(std::max(1, j.Ntot[g]), 1.0);
+                N.push_back(j.N[g].data());
+                nsize_max = std::max(nsize_max, j.Ntot[g]);
+            }
+            for (auto& o : ones) repres.push_back(o.data());
+            gpu.TransferInflation(j.icontr.data(), j.ijterms.data(), j.dimen, j.dimen, 1, repres, N, j.Ntot,
+                                  std::vector<int>(nsym, 1));
+            dimen_max = std::max(dimen_max, j.dimen);
+        }
+        gpu.AllocateVectors(2, nsize_max, dimen_max);
+        std::vector<double> amp((size_t)nlower * nupper);
+        for (int l = 0; l < nlower; ++l) {                  // main.cpp:238 lower-state loop
+            std::copy(vl.begin() + (size_t)l * js[0].Ntot[gI], vl.begin() + (size_t)(l + 1) * js[0].Ntot[gI],
+                      gpu.GetInitialVector());
+            gpu.UpdateEigenVector();
+            gpu.ResetHalfLinestrength(1, 0);
+            gpu.ExecuteHalfLs(0, 1, 0, gI);                 // MultiGpuManager::ExecuteHalfLs
+            for (int u = 0; u < nupper; ++u) {              // main.cpp:293 upper-state loop
+                std::copy(vu.begin() + (size_t)u * js[1].Ntot[gF], vu.begin() + (size_t)(u + 1) * js[1].Ntot[gF],
+                          gpu.GetFinalVector(0));
+                gpu.UpdateEigenVector(0);
+                gpu.ExecuteDotProduct(1, 0, 0, gF, 0);
+                gpu.WaitForLineStrengthResult(0);
+                amp[(size_t)l * nupper + u] = gpu.GetLinestrength(0)[0];
+            }
+        }
+        FILE* fo = fopen(argv[2], "wb");
+        fwrite(amp.data(), 8, amp.size(), fo);
+        fclose(fo);
+    } catch (const gain::Error& e) {
+        fprintf(stderr, "gain error: %s\n", e.what());
+        return 3;
+    }
+    return 0;
+}

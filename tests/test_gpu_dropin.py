@@ -76,7 +76,8 @@ def test_dot_matches_oracle(built_lib):
     for n in (1, 31, 1000, 12345):
         x, y = rng.standard_normal(n), rng.standard_normal(n)
         res = torch.zeros(1, dtype=torch.float64, device="cuda")
-        gainls.dot(n, _dev(x).data_ptr(), _dev(y).data_ptr(), res.data_ptr())
+        dx, dy = _dev(x), _dev(y)          # keep both alive while the kernel reads them
+        gainls.dot(n, dx.data_ptr(), dy.data_ptr(), res.data_ptr())
         torch.cuda.synchronize()
         ref = oracle.dot(x, y, oracle.DD)
         assert abs(res.item() - ref) <= 4 * n * 1.2e-16 * np.sum(np.abs(x * y))
