@@ -55,6 +55,24 @@ def dist_info():
     return ws, rank, local
 
 
+# ------------------------------------------------------------------------- sharding
+def lower_first(rank: int, n_lower: int, n_block: int) -> int:
+    """First lower level of rank's batch: consecutive, disjoint batches of n_lower levels
+    while they fit in the block, wrapping around (replicas) beyond that."""
+    nb = max(n_block // n_lower, 1)
+    return (rank % nb) * n_lower if n_block >= n_lower else 0
+
+
+def max_over_ranks(value: float, dist=None, device=None) -> float:
+    """The step time the bench reports: the slowest rank's."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------------------- inputs
 def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = True):
     """orthonormal=False replaces the QR eigenvectors by normalised Gaussian rows of the same
@@ -66,7 +84,7 @@ def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = 
     iI, iF = synth.make_inflation(bI, cI, 4), synth.make_inflation(bF, cF, 4)
     nI, nF = int(iI.Ntot[GI]), int(iF.Ntot[GF])
     # each rank takes its own batch of lower states (weak scaling, no data exchange)
-    first = (rank * n_lower) % max(nI - n_lower + 1, 1)
+    first = lower_first(rank, n_lower, nI)
     if orthonormal:
         vl = synth.make_eigvecs(nI, JI, GI, device=device, nstates=first + n_lower)[first:first + n_lower]
         vu = synth.make_eigvecs(nF, JF, GF, device=device)
@@ -246,11 +264,8 @@ def main():
             g2.append(st["gemm2_ms"])
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    total_ms = float(np.sum(ms_list))
+    total_ms = max_over_ranks(float(np.sum(ms_list)), dist, "cuda")
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     ms_step = total_ms / args.steps
     value = ws * transitions / (ms_step * 1e-3)

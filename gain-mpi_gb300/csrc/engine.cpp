@@ -693,6 +693,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g1.A = e->Vst.view(false);
     g1.B = L.bandStats.view(false);
     g1.c_fix = fix_const(p1x, (int)pr1.size());
+    g1.c_f64 = (float)((double)(L.W + 64) * std::ldexp(1.0, -53) * 1.01);
     g1.rowerr2 = e->rowerr.p;
     g1.flag_mode = 0;
     g1.tol = (float)tol;
@@ -774,6 +775,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.A = e->Hst.view(true);
     g2.B = e->Ust.view(false);
     g2.c_fix = fix_const(p2, (int)pr2.size());
+    g2.c_f64 = (float)((double)(L.nF + 64) * std::ldexp(1.0, -53) * 1.01);
     g2.rowerr2 = nullptr;
     g2.absmax = e->ull.p + 2;
     g2.flag_mode = 1;

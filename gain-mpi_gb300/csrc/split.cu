@@ -411,7 +411,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     if (a.flag_mode == 1) {
                         // |value| in units of 2^{eA+eB}: run 2^{-2 beta - kFix}
                         const float av = fabsf((float)run) * pow2f(-2 * a.beta - kFix);
-                        flag = flag || (bound > a.tol * av);
+                        const float f64b = a.c_f64 * l2A * l2B;
+                        flag = flag || (bound > fmaxf(a.tol * av, f64b));
                     }
                     if (flag && rvalid && col < a.cols_valid) {
                         const unsigned int idx = atomicAdd(a.nflags, 1u);
@@ -707,10 +708,13 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
         }
         if (lane == 0) {
             a.amp[(long)r * a.lda + c] = acc;
-            // |<dH, u>| <= ||dH||_2 ||u||_2, plus the rounding of this FP64 dot product
+            // |<dH, u>| <= ||dH||_2 ||u||_2 (first-GEMM error carried into this line); the
+            // rounding of this FP64 dot product itself is the FP64 method's own bound.  The line
+            // is certified when the carried error stays within max(tol |amp|, that bound).
             const double herr = (double)a.h_inerr[r] * pow2d(a.eH[r]);
-            const double bound = herr * sqrt(l2) * 1.001 + aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
-            if (!(bound <= a.tol * fabs(acc))) {
+            const double carried = herr * sqrt(l2) * 1.001;
+            const double f64b = aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
+            if (!(carried <= fmax(a.tol * fabs(acc), f64b))) {
                 const double amax = __longlong_as_double((long long)*a.absmax);
                 atomicAdd(fabs(acc) >= a.amp_floor * amax ? a.uncertified : a.uncertified_weak, 1ull);
             }

@@ -67,6 +67,10 @@ struct GemmArgs {
     RowStats A, B;
     // bound of the fixed-point recombination (units of 2^{eA+eB}): nprods 2^{-kFix - 2 beta}
     float c_fix;
+    // worst-case rounding bound of an FP64 dot product of the same two rows, per unit of
+    // ||x^||_2 ||y^||_2: (K + 64) 2^-53; a line is certified when its bound is within
+    // max(tol |value|, that FP64 bound)
+    float c_f64;
     // GEMM1: per row, sum over columns of (bound in units of 2^{eA})^2 (atomic add), may be null
     float* rowerr2;
     // optional: largest |value| over valid outputs (atomic max on the IEEE bits)

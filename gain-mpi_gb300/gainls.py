@@ -70,6 +70,75 @@ class LineParams(ctypes.Structure):
                 ("reduced", ctypes.c_int)]
 
 
+class State(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("J", ctypes.c_int), ("jind", ctypes.c_int),
+                ("gamma", ctypes.c_int), ("ndeg", ctypes.c_int), ("ilevel", ctypes.c_int)]
+
+
+class Filters(ctypes.Structure):
+    _fields_ = [("nsym", ctypes.c_int), ("gns", _dp), ("isym_pairs", _ip), ("igamma_pair", _ip),
+                ("sym_degen", _ip), ("erange_lower", ctypes.c_double * 2), ("erange_upper", ctypes.c_double * 2),
+                ("freq_window", ctypes.c_double * 2), ("zpe", ctypes.c_double), ("maxJ", ctypes.c_int),
+                ("reduced", ctypes.c_int), ("symmetry_type", ctypes.c_int)]
+
+
+def make_filters(gns, isym_pairs, igamma_pair, sym_degen, erange_lower, erange_upper,
+                 freq_window=(-1e9, 1e9), zpe=0.0, maxJ=0, reduced=False, symmetry_type=1):
+    """A Filters struct plus the arrays it points to (kept alive on the struct)."""
+    arrs = [np.ascontiguousarray(gns, np.float64), np.ascontiguousarray(isym_pairs, np.int32),
+            np.ascontiguousarray(igamma_pair, np.int32), np.ascontiguousarray(sym_degen, np.int32)]
+    f = Filters(len(arrs[0]), arrs[0].ctypes.data_as(_dp), arrs[1].ctypes.data_as(_ip),
+                arrs[2].ctypes.data_as(_ip), arrs[3].ctypes.data_as(_ip),
+                (ctypes.c_double * 2)(*erange_lower), (ctypes.c_double * 2)(*erange_upper),
+                (ctypes.c_double * 2)(*freq_window), zpe, maxJ, int(reduced), symmetry_type)
+    f._keep = arrs
+    return f
+
+
+def state_table(energy, J, jind, gamma, ndeg, ilevel):
+    n = len(energy)
+    arr = (State * n)()
+    for i in range(n):
+        arr[i] = State(float(energy[i]), int(J[i]), int(jind[i]), int(gamma[i]), int(ndeg[i]), int(ilevel[i]))
+    return arr
+
+
+def filter_intensity(f: Filters, I: State, F: State) -> bool:
+    return bool(lib().gain_filter_intensity(ctypes.byref(f), ctypes.byref(I), ctypes.byref(F)))
+
+
+def filter_lower(f: Filters, I: State) -> bool:
+    return bool(lib().gain_filter_lower(ctypes.byref(f), ctypes.byref(I)))
+
+
+def degeneracy_filter(f: Filters, gI, gF, idegI, idegF) -> bool:
+    return bool(lib().gain_degeneracy_filter(ctypes.byref(f), gI, gF, idegI, idegF))
+
+
+def transition_details(f: Filters, table):
+    a, b, c = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int()
+    check(lib().gain_transition_details(ctypes.byref(f), table, len(table), ctypes.byref(a), ctypes.byref(b),
+                                        ctypes.byref(c)))
+    return a.value, b.value, c.value
+
+
+def plan_pairs(f: Filters, table):
+    """[(jindI, gammaI, jindF, gammaF, lower_levels, upper_levels), ...]"""
+    npairs, nlev = ctypes.c_int(), ctypes.c_longlong()
+    check(lib().gain_plan_pairs(ctypes.byref(f), table, len(table), ctypes.byref(npairs), None, None,
+                                ctypes.byref(nlev), None))
+    pairs = np.zeros(4 * npairs.value, np.int32)
+    offs = np.zeros(2 * npairs.value + 1, np.int32)
+    levels = np.zeros(max(nlev.value, 1), np.int32)
+    check(lib().gain_plan_pairs(ctypes.byref(f), table, len(table), ctypes.byref(npairs), _p(pairs, _ip),
+                                _p(offs, _ip), ctypes.byref(nlev), _p(levels, _ip)))
+    out = []
+    for p in range(npairs.value):
+        out.append((*[int(x) for x in pairs[4 * p:4 * p + 4]], levels[offs[2 * p]:offs[2 * p + 1]].tolist(),
+                    levels[offs[2 * p + 1]:offs[2 * p + 2]].tolist()))
+    return out
+
+
 _lib = None
 
 
@@ -117,6 +186,17 @@ def _declare(L):
                                   ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_longlong)]
     L.gain_format_line.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
     L.gain_format_line.restype = I
+    FP, SP = ctypes.POINTER(Filters), ctypes.POINTER(State)
+    L.gain_filter_lower.argtypes = [FP, SP]
+    L.gain_filter_lower.restype = I
+    L.gain_filter_intensity.argtypes = [FP, SP, SP]
+    L.gain_filter_intensity.restype = I
+    L.gain_degeneracy_filter.argtypes = [FP, I, I, I, I]
+    L.gain_degeneracy_filter.restype = I
+    L.gain_transition_details.argtypes = [FP, SP, I, _ip, ctypes.POINTER(ctypes.c_longlong), _ip]
+    L.gain_transition_details.restype = S
+    L.gain_plan_pairs.argtypes = [FP, SP, I, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong), _ip]
+    L.gain_plan_pairs.restype = S
     for name in ("gain_hls_kblock", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",

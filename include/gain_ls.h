@@ -129,9 +129,14 @@ typedef struct gain_pair_job {
     const int* upper_levels;
 } gain_pair_job;
 
+/* Certification of the split path: every amplitude carries a rigorous error bound computed
+ * from per-row norms.  A line is certified when its bound is within
+ *   max(tol |amp|, the worst-case rounding bound of an FP64 dot product of the same rows),
+ * i.e. it is either within tol or at least as trustworthy as the reference's own FP64
+ * method.  Uncertified lines (and any whose exact-accumulation certificate fails) are
+ * recomputed in FP64. */
 typedef struct gain_split_opts {
-    double tol;       /* relative tolerance on each amplitude; lines whose certified bound
-                         exceeds tol*|amp| are recomputed in FP64 (0 -> 4.5e-9, so that
+    double tol;       /* relative tolerance on each amplitude (0 -> 4.5e-9, so that
                          S = amp^2 meets 1e-8) */
     int slices;       /* digits per operand of the amplitude GEMM (0 -> 49 bits; the
                          rotational-dipole GEMM always keeps 56 bits) */
@@ -146,7 +151,8 @@ typedef struct gain_stats {
     long long rows, cols;       /* lower x upper amplitudes computed */
     long long refined;          /* split path: amplitudes recomputed in FP64 */
     long long uncertified;      /* split path: refined lines with S >= s_floor S_max whose
-                                   bound still exceeds tol (non-zero -> GAIN_ERR_TOL_NOT_MET) */
+                                   carried first-GEMM error still exceeds max(tol |amp|, FP64
+                                   bound) (non-zero -> GAIN_ERR_TOL_NOT_MET) */
     long long uncertified_weak; /* the same below s_floor S_max (outside the accuracy domain) */
     long long inexact;          /* split path: pairs outside the exact-accumulation guarantee */
     double amp_max;             /* split path: largest |amplitude| of the run */
@@ -192,6 +198,54 @@ typedef struct gain_line_params {
 gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI,
                             const double* energiesF, int jI, int jF, double* S, double* A,
                             double* I, unsigned char* keep, long long* n_lines);
+
+/* ======================= host: state selection (BaseClasses/States.*) ============== */
+
+/* One eigenstate (BaseClasses/States.h:327-346): J, index of J in the J list, symmetry,
+ * degeneracy, level index inside its (J, Gamma) block, energy (cm^-1). */
+typedef struct gain_state {
+    double energy;
+    int J, jind, gamma, ndeg, ilevel;
+} gain_state;
+
+/* The selection parameters of the INTENSITY block (TroveClasses/TroveInput.cpp:239-326).
+ * isym_do[g] is derived as gns[g] >= 1e-15 (TroveInput.cpp:300-304). */
+typedef struct gain_filters {
+    int nsym;
+    const double* gns;          /* [nsym] GNS */
+    const int* isym_pairs;      /* [nsym] SELECTION */
+    const int* igamma_pair;     /* [nsym] TroveInput::ComputeIGammaPair */
+    const int* sym_degen;       /* [nsym] degeneracies */
+    double erange_lower[2];     /* ENERGY LOW  lo hi */
+    double erange_upper[2];     /* ENERGY UPPER lo hi */
+    double freq_window[2];      /* FREQ-WINDOW lo hi */
+    double zpe;                 /* ZPE */
+    int maxJ;                   /* largest J of the run */
+    int reduced;                /* SYMMETRY REDUCED */
+    int symmetry_type;          /* 1 generic, 2 C3v/D3h, 3 Td (TroveInput.cpp:104-107) */
+} gain_filters;
+
+/* States::filter_lower / FilterLowerState (BaseClasses/States.cpp:46-49, States.h:61) */
+int gain_filter_lower(const gain_filters* f, const gain_state* I);
+/* States::FilterIntensity (BaseClasses/States.cpp:54-76) */
+int gain_filter_intensity(const gain_filters* f, const gain_state* I, const gain_state* F);
+/* States::DegeneracyFilter (BaseClasses/States.cpp:95-116) */
+int gain_degeneracy_filter(const gain_filters* f, int gammaI, int gammaF, int idegI, int idegF);
+/* States::GetTransitionDetails (BaseClasses/States.cpp:126-157) over a state table. */
+gain_status gain_transition_details(const gain_filters* f, const gain_state* st, int n,
+                                    int* num_initial, long long* num_trans, int* max_trans);
+
+/* Block-pair plan of a state table: every (J'',Gamma'') -> (J',Gamma') pair that has at
+ * least one transition, with the lower levels passing filter_lower and the upper levels
+ * passing filter_upper (the separable part of FilterIntensity; the frequency window and
+ * nu are applied per line by gain_pair_lines).  Pair p is
+ *   pairs[4p .. 4p+3] = jindI, gammaI, jindF, gammaF,
+ *   its lower levels  levels[offs[2p]   .. offs[2p+1]),
+ *   its upper levels  levels[offs[2p+1] .. offs[2p+2]).
+ * Call with pairs = NULL to get the sizes (n_pairs, n_levels); then with arrays of
+ * 4 n_pairs, 2 n_pairs + 1 and n_levels ints. */
+gain_status gain_plan_pairs(const gain_filters* f, const gain_state* st, int n, int* n_pairs,
+                            int* pairs, int* offs, long long* n_levels, int* levels);
 
 /* Text of one line exactly as Output.cpp:99-111 prints it (without the amplitude list
  * unless namp > 0).  Returns the number of characters written (excluding the NUL). */
