@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--small", action="store_true", help="reduced sizes (development only)")
+    ap.add_argument("--lower", type=int, default=0,
+                    help="number of lower states (profiling captures; default: the workload's 2000)")
     return ap.parse_args()
 
 
@@ -74,11 +76,13 @@ def max_over_ranks(value: float, dist=None, device=None) -> float:
 
 
 # ------------------------------------------------------------------------- inputs
-def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = True):
+def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = True, n_lower_override: int = 0):
     """orthonormal=False replaces the QR eigenvectors by normalised Gaussian rows of the same
     shape (used only where the values do not matter: timing the CPU reference formula)."""
     import synth
     nv, n_lower = (200, 64) if small else (NV, N_LOWER)
+    if n_lower_override > 0:
+        n_lower = n_lower_override
     bI, bF = synth.make_basis(JI, nv), synth.make_basis(JF, nv)
     cI, cF = synth.classes_of(bI, "c4"), synth.classes_of(bF, "c4")
     iI, iF = synth.make_inflation(bI, cI, 4), synth.make_inflation(bF, cF, 4)
@@ -98,12 +102,16 @@ def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = 
                 vu=np.ascontiguousarray(vu), eI=eI, eF=eF, first=first)
 
 
+_PINNED = []   # pinned host tensors backing the arrays handed out by pinned()
+
+
 def pinned(a: np.ndarray) -> np.ndarray:
+    """A page-locked copy of a (the torch tensor that owns it is kept alive)."""
     import torch
     t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+    _PINNED.append(t)
     out = t.numpy()
     out[...] = a
-    out._keep = t  # noqa: SLF001  (keep the pinned buffer alive)
     return out
 
 
@@ -239,7 +247,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import gainls
-    inp = make_inputs(args.small, rank, "cuda")
+    inp = make_inputs(args.small, rank, "cuda", n_lower_override=args.lower)
     eng = setup_engine(inp, local)
     B, NU = inp["vl"].shape[0], inp["vu"].shape[0]
     lo, up = list(range(B)), list(range(NU))

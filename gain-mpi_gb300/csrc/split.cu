@@ -407,12 +407,16 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
                         rowerr2 = __fmaf_ru(bb, bb, rowerr2);
                     }
+                    // certification: flag_mode 1 -> within max(tol |value|, FP64 bound of the
+                    // same dot product); flag_mode 2 -> within the FP64 bound (FP64-grade)
                     bool flag = !exact;
+                    const float f64b = __fmul_ru(__fmul_ru(a.c_f64, l2A), l2B);
                     if (a.flag_mode == 1) {
                         // |value| in units of 2^{eA+eB}: run 2^{-2 beta - kFix}
                         const float av = fabsf((float)run) * pow2f(-2 * a.beta - kFix);
-                        const float f64b = a.c_f64 * l2A * l2B;
                         flag = flag || (bound > fmaxf(a.tol * av, f64b));
+                    } else if (a.flag_mode == 2) {
+                        flag = flag || (bound > f64b);
                     }
                     if (flag && rvalid && col < a.cols_valid) {
                         const unsigned int idx = atomicAdd(a.nflags, 1u);
@@ -708,13 +712,12 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
         }
         if (lane == 0) {
             a.amp[(long)r * a.lda + c] = acc;
-            // |<dH, u>| <= ||dH||_2 ||u||_2 (first-GEMM error carried into this line); the
-            // rounding of this FP64 dot product itself is the FP64 method's own bound.  The line
-            // is certified when the carried error stays within max(tol |amp|, that bound).
-            const double herr = (double)a.h_inerr[r] * pow2d(a.eH[r]);
-            const double carried = herr * sqrt(l2) * 1.001;
+            // The recomputed amplitude now carries the FP64 method's own bound: the rounding
+            // of this dot product plus the H error, which the first GEMM certified FP64-grade.
+            // Lines where even that bound exceeds tol |amp| are counted (information only).
             const double f64b = aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
-            if (!(carried <= fmax(a.tol * fabs(acc), f64b))) {
+            (void)l2;
+            if (!(f64b <= a.tol * fabs(acc))) {
                 const double amax = __longlong_as_double((long long)*a.absmax);
                 atomicAdd(fabs(acc) >= a.amp_floor * amax ? a.uncertified : a.uncertified_weak, 1ull);
             }

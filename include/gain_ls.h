@@ -129,12 +129,12 @@ typedef struct gain_pair_job {
     const int* upper_levels;
 } gain_pair_job;
 
-/* Certification of the split path: every amplitude carries a rigorous error bound computed
- * from per-row norms.  A line is certified when its bound is within
- *   max(tol |amp|, the worst-case rounding bound of an FP64 dot product of the same rows),
- * i.e. it is either within tol or at least as trustworthy as the reference's own FP64
- * method.  Uncertified lines (and any whose exact-accumulation certificate fails) are
- * recomputed in FP64. */
+/* Certification of the split path: every output carries a rigorous error bound computed
+ * from per-row norms.  Each half-line-strength entry (first GEMM) must be within the
+ * worst-case rounding bound of an FP64 dot product of the same rows ("FP64-grade"); each
+ * amplitude (second GEMM) within max(tol |amp|, that FP64 bound).  Outputs that fail (or
+ * whose exact-accumulation certificate fails) are recomputed in FP64.  Every amplitude is
+ * therefore within tol or within the reference FP64 method's own worst-case bound. */
 typedef struct gain_split_opts {
     double tol;       /* relative tolerance on each amplitude (0 -> 4.5e-9, so that
                          S = amp^2 meets 1e-8) */
@@ -150,11 +150,12 @@ typedef struct gain_stats {
     double device_ms;           /* device time of the last run (CUDA events) */
     long long rows, cols;       /* lower x upper amplitudes computed */
     long long refined;          /* split path: amplitudes recomputed in FP64 */
-    long long uncertified;      /* split path: refined lines with S >= s_floor S_max whose
-                                   carried first-GEMM error still exceeds max(tol |amp|, FP64
-                                   bound) (non-zero -> GAIN_ERR_TOL_NOT_MET) */
+    long long uncertified;      /* split path, information: refined lines with S >= s_floor S_max
+                                   whose FP64 bound itself exceeds tol |amp| (the reference's
+                                   FP64 method cannot certify them either) */
     long long uncertified_weak; /* the same below s_floor S_max (outside the accuracy domain) */
-    long long inexact;          /* split path: pairs outside the exact-accumulation guarantee */
+    long long inexact;          /* split path: first-GEMM entries recomputed in FP64 (exactness
+                                   certificate failed or bound above the FP64 bound) */
     double amp_max;             /* split path: largest |amplitude| of the run */
     int beta1, slices1, chunks1;  /* first GEMM (lower vectors x rotational-dipole matrix) */
     int beta2, slices2, chunks2;  /* second GEMM (half line strengths x upper vectors) */
