@@ -90,8 +90,23 @@ def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = 
     # each rank takes its own batch of lower states (weak scaling, no data exchange)
     first = lower_first(rank, n_lower, nI)
     if orthonormal:
-        vl = synth.make_eigvecs(nI, JI, GI, device=device, nstates=first + n_lower)[first:first + n_lower]
-        vu = synth.make_eigvecs(nF, JF, GF, device=device)
+        # QR eigenvectors are cached between runs of the same workload (profilers cannot
+        # always load torch's linear-algebra library inside their injected process)
+        import tempfile
+        cdir = os.environ.get("GAIN_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "gain_bench_inputs"))
+        cfile = os.path.join(cdir, f"eig_nv{nv}_J{JI}g{GI}_{first}_{n_lower}_J{JF}g{GF}.npz")
+        if os.path.exists(cfile):
+            z = np.load(cfile)
+            vl, vu = z["vl"], z["vu"]
+        else:
+            vl = synth.make_eigvecs(nI, JI, GI, device=device, nstates=first + n_lower)[first:first + n_lower]
+            vu = synth.make_eigvecs(nF, JF, GF, device=device)
+            try:
+                os.makedirs(cdir, exist_ok=True)
+                np.savez(cfile + ".tmp.npz", vl=vl, vu=vu)
+                os.replace(cfile + ".tmp.npz", cfile)
+            except OSError:
+                pass
     else:
         rng = np.random.default_rng(synth.vec_seed(JI, GI))
         vl = rng.standard_normal((n_lower, nI)) / np.sqrt(nI)

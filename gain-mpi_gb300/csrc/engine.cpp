@@ -369,26 +369,31 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) 
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
     GAIN_TRY(e->d_lower.upload(j->lower_levels, j->nlower));
     GAIN_TRY(e->d_upper.upload(j->upper_levels, j->nupper));
-    GAIN_TRY(e->primI.alloc(bI.dimen));
-    GAIN_TRY(e->hprim.alloc(bF.dimen));
-    GAIN_TRY(e->hsym.alloc(iF.Ntot[j->gammaF]));
+    // The reference's method, one half line strength per lower state followed by its dot
+    // products with every upper vector; kPlainBatch lower states share each launch (and each
+    // read of an upper vector), every amplitude keeps its own FP64 summation.
+    const int G = kPlainBatch;
+    const int NtF = iF.Ntot[j->gammaF];
+    GAIN_TRY(e->primI.alloc((size_t)G * bI.dimen));
+    GAIN_TRY(e->hprim.alloc((size_t)G * bF.dimen));
+    GAIN_TRY(e->hsym.alloc((size_t)G * NtF));
     GAIN_TRY(e->amp.alloc((size_t)j->nlower * j->nupper));
     cudaStream_t st = e->st;
     GAIN_CUDA(cudaEventRecord(e->ev[0], st));
     int launches = 0;
-    for (int l = 0; l < j->nlower; ++l) {
-        const double* vrow = EI.d.p + (size_t)j->lower_levels[l] * EI.nsize;
-        GAIN_CUDA(launch_expand(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
-                                iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
-                                vrow, e->primI.p, st));
+    for (int l0 = 0; l0 < j->nlower; l0 += G) {
+        const int nb = std::min(G, j->nlower - l0);
+        GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
+                                       iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
+                                       EI.d.p, EI.nsize, e->d_lower.p + l0, e->primI.p, bI.dimen, nb, st));
         GAIN_CUDA(launch_hls_needed(L.d_ctas.p, (int)L.ctas.size(), mF->d_support.p, bI.J, bF.J, bI.dtau.p,
                                     bF.dtau.p, bI.dvib.p, bF.dvib.p, mI->d_support.p, mI->d_sup_start.p,
-                                    e->startF, e->endF, e->ncontrF, e->dipole.p, e->dipN, e->primI.p,
-                                    e->d3j.p, e->jmax, e->hprim.p, st));
-        GAIN_CUDA(launch_contract(iF.Ntot[j->gammaF], mF->d_csr_ptr.p, mF->d_csr_col.p, mF->d_csr_val.p,
-                                  e->hprim.p, e->hsym.p, st));
-        GAIN_CUDA(launch_gemv_rows(j->nupper, EF.nsize, EF.d.p, EF.nsize, e->d_upper.p, e->hsym.p,
-                                   e->amp.p + (size_t)l * j->nupper, st));
+                                    e->startF, e->endF, e->ncontrF, e->dipole.p, e->dipN, e->primI.p, bI.dimen,
+                                    e->d3j.p, e->jmax, e->hprim.p, bF.dimen, nb, st));
+        GAIN_CUDA(launch_contract(NtF, mF->d_csr_ptr.p, mF->d_csr_col.p, mF->d_csr_val.p, e->hprim.p, bF.dimen,
+                                  e->hsym.p, NtF, nb, st));
+        GAIN_CUDA(launch_gemv_batch(j->nupper, EF.nsize, EF.d.p, EF.nsize, e->d_upper.p, e->hsym.p, NtF, nb,
+                                    e->amp.p + (size_t)l0 * j->nupper, j->nupper, st));
         launches += 4;
     }
     GAIN_CUDA(cudaEventRecord(e->ev[1], st));

@@ -152,12 +152,15 @@ k_hls_needed(const HlsCta* __restrict__ ctas, const int* __restrict__ f_list, in
              const int* __restrict__ icorrI, const int* __restrict__ icorrF,
              const int* __restrict__ sup_list, const int* __restrict__ sup_start,
              int startFblock, int endFblock, int ncontrF, const double* __restrict__ dipole_me,
-             int dip_stride, const double* __restrict__ prim_vec, const double* __restrict__ threej,
-             int jmax, double* __restrict__ half_ls) {
+             int dip_stride, const double* __restrict__ prim_vec, long ld_prim,
+             const double* __restrict__ threej, int jmax, double* __restrict__ half_ls, long ld_h) {
     __shared__ double s_lsf[kHlsTile];
     __shared__ double s_sgn[kHlsTile];
     __shared__ int s_tau[kHlsTile];
     __shared__ long s_off[kHlsTile];
+    // blockIdx.y: lower state of the batch
+    prim_vec += (long)blockIdx.y * ld_prim;
+    half_ls += (long)blockIdx.y * ld_h;
     const HlsCta cta = ctas[blockIdx.x];
     const int kF = cta.kF;
     const bool inF = (int)threadIdx.x < cta.f_count;
@@ -213,33 +216,61 @@ k_hls_needed(const HlsCta* __restrict__ ctas, const int* __restrict__ f_list, in
 }
 
 __global__ void k_contract(int nsym, const int* __restrict__ rowptr, const int* __restrict__ col,
-                           const double* __restrict__ val, const double* __restrict__ h,
-                           double* __restrict__ hsym) {
+                           const double* __restrict__ val, const double* __restrict__ h, long ld_h,
+                           double* __restrict__ hsym, long ld_hs) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsym) return;
+    h += (long)blockIdx.y * ld_h;
+    hsym += (long)blockIdx.y * ld_hs;
     double acc = 0.0;
     for (int e = rowptr[s]; e < rowptr[s + 1]; ++e) acc = __fma_rn(h[col[e]], val[e], acc);
     hsym[s] = acc;
 }
 
-// one warp per output row
+// expansion of a batch of stored vectors: blockIdx.y picks the level
+__global__ void k_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                const int* __restrict__ ijterms, const int* __restrict__ icontr,
+                                const int* __restrict__ N, const double* __restrict__ repres,
+                                const double* __restrict__ vecs, long ldv, const int* __restrict__ levels,
+                                double* __restrict__ prim, long ldp) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= dimen) return;
+    const double* vecI = vecs + (long)levels[blockIdx.y] * ldv;
+    const int irow = icontr[r];
+    const int ib = icontr[r + dimen];
+    const int iterm = ijterms[irow + igamma * maxcoeff];
+    const int nelem = N[irow];
+    const long base = (long)ideg * Ntot + (long)ib * sdeg * Ntot;
+    double acc = 0.0;
+    for (int i = 0; i < nelem; ++i) acc = __fma_rn(vecI[iterm + i], repres[iterm + i + base], acc);
+    prim[(long)blockIdx.y * ldp + r] = acc;
+}
+
+// One warp per upper state: its vector is read once and dotted with the half line
+// strengths of up to kGemvBatch lower states (each dot: lane-strided FMA, tree reduction).
+constexpr int kGemvBatch = 8;
 __global__ void __launch_bounds__(256)
-k_gemv_rows(int nrows, int n, const double* __restrict__ U, long ldu, const int* __restrict__ levels,
-            const double* __restrict__ x, double* __restrict__ out) {
+k_gemv_batch(int nrows, int n, const double* __restrict__ U, long ldu, const int* __restrict__ levels,
+             const double* __restrict__ x, long ldx, int nb, double* __restrict__ out, long ldo) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nrows) return;
     const double* row = U + (long)levels[warp] * ldu;
-    double a0 = 0.0, a1 = 0.0;
-    int i = lane;
-    for (; i + 32 < n; i += 64) {
-        a0 = __fma_rn(__ldg(row + i), __ldg(x + i), a0);
-        a1 = __fma_rn(__ldg(row + i + 32), __ldg(x + i + 32), a1);
+    double acc[kGemvBatch];
+#pragma unroll
+    for (int g = 0; g < kGemvBatch; ++g) acc[g] = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        const double u = __ldg(row + i);
+#pragma unroll
+        for (int g = 0; g < kGemvBatch; ++g)
+            if (g < nb) acc[g] = __fma_rn(u, __ldg(x + (long)g * ldx + i), acc[g]);
     }
-    if (i < n) a0 = __fma_rn(__ldg(row + i), __ldg(x + i), a0);
-    double acc = a0 + a1;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) out[warp] = acc;
+#pragma unroll
+    for (int g = 0; g < kGemvBatch; ++g) {
+        double a = acc[g];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0 && g < nb) out[(long)g * ldo + warp] = a;
+    }
 }
 
 __global__ void k_scatter_select(int dimen, const int* __restrict__ sym_of,
@@ -321,25 +352,38 @@ cudaError_t launch_hls_needed(const HlsCta* ctas, int ncta, const int* f_list, i
                               const int* icorrF, const int* sup_list, const int* sup_start,
                               int startFblock, int endFblock, int ncontrF,
                               const double* dipole_me, int dip_stride, const double* prim_vec,
-                              const double* threej, int jmax, double* half_ls, cudaStream_t st) {
-    if (ncta <= 0) return cudaSuccess;
-    k_hls_needed<<<ncta, kHlsTile, 0, st>>>(ctas, f_list, jI, jF, tauI, tauF, icorrI, icorrF,
-                                            sup_list, sup_start, startFblock, endFblock, ncontrF,
-                                            dipole_me, dip_stride, prim_vec, threej, jmax, half_ls);
+                              long ld_prim, const double* threej, int jmax, double* half_ls,
+                              long ld_h, int nbatch, cudaStream_t st) {
+    if (ncta <= 0 || nbatch <= 0) return cudaSuccess;
+    k_hls_needed<<<dim3(ncta, nbatch), kHlsTile, 0, st>>>(
+        ctas, f_list, jI, jF, tauI, tauF, icorrI, icorrF, sup_list, sup_start, startFblock, endFblock,
+        ncontrF, dipole_me, dip_stride, prim_vec, ld_prim, threej, jmax, half_ls, ld_h);
     return cudaGetLastError();
 }
 
 cudaError_t launch_contract(int nsym, const int* rowptr, const int* col, const double* val,
-                            const double* h, double* hsym, cudaStream_t st) {
-    if (nsym <= 0) return cudaSuccess;
-    k_contract<<<(nsym + 255) / 256, 256, 0, st>>>(nsym, rowptr, col, val, h, hsym);
+                            const double* h, long ld_h, double* hsym, long ld_hs, int nbatch,
+                            cudaStream_t st) {
+    if (nsym <= 0 || nbatch <= 0) return cudaSuccess;
+    k_contract<<<dim3((nsym + 255) / 256, nbatch), 256, 0, st>>>(nsym, rowptr, col, val, h, ld_h, hsym, ld_hs);
     return cudaGetLastError();
 }
 
-cudaError_t launch_gemv_rows(int nrows, int n, const double* U, long ldu, const int* levels,
-                             const double* x, double* amp_row, cudaStream_t st) {
-    if (nrows <= 0) return cudaSuccess;
-    k_gemv_rows<<<(nrows + 7) / 8, 256, 0, st>>>(nrows, n, U, ldu, levels, x, amp_row);
+cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                 const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                 const double* vecs, long ldv, const int* levels, double* prim, long ldp,
+                                 int nbatch, cudaStream_t st) {
+    if (dimen <= 0 || nbatch <= 0) return cudaSuccess;
+    k_expand_levels<<<dim3((dimen + 255) / 256, nbatch), 256, 0, st>>>(
+        dimen, igamma, maxcoeff, ideg, sdeg, Ntot, ijterms, icontr, N, repres, vecs, ldv, levels, prim, ldp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemv_batch(int nrows, int n, const double* U, long ldu, const int* levels, const double* x,
+                              long ldx, int nbatch, double* out, long ldo, cudaStream_t st) {
+    if (nrows <= 0 || nbatch <= 0) return cudaSuccess;
+    if (nbatch > kGemvBatch) return cudaErrorInvalidValue;
+    k_gemv_batch<<<(nrows + 7) / 8, 256, 0, st>>>(nrows, n, U, ldu, levels, x, ldx, nbatch, out, ldo);
     return cudaGetLastError();
 }
 

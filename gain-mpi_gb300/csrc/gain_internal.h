@@ -60,15 +60,24 @@ cudaError_t launch_hls_needed(const HlsCta* ctas, int ncta, const int* f_list, i
                               const int* icorrF, const int* sup_list, const int* sup_start,
                               int startFblock, int endFblock, int ncontrF,
                               const double* dipole_me, int dip_stride, const double* prim_vec,
-                              const double* threej, int jmax, double* half_ls, cudaStream_t st);
+                              long ld_prim, const double* threej, int jmax, double* half_ls,
+                              long ld_h, int nbatch, cudaStream_t st);
 
-// hsym[s] = sum_{e in row s} h[col[e]] * val[e]  (transpose of the expansion)
+// hsym[s] = sum_{e in row s} h[col[e]] * val[e]  (transpose of the expansion), per batch row
 cudaError_t launch_contract(int nsym, const int* rowptr, const int* col, const double* val,
-                            const double* h, double* hsym, cudaStream_t st);
+                            const double* h, long ld_h, double* hsym, long ld_hs, int nbatch,
+                            cudaStream_t st);
 
-// amp_row[u] = sum_f U[level[u]*ldu + f] * x[f], u < nrows
-cudaError_t launch_gemv_rows(int nrows, int n, const double* U, long ldu, const int* levels,
-                             const double* x, double* amp_row, cudaStream_t st);
+// expansion of the stored vectors vecs[levels[b]] into prim[b] (b < nbatch)
+cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                 const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                 const double* vecs, long ldv, const int* levels, double* prim, long ldp,
+                                 int nbatch, cudaStream_t st);
+
+// out[b*ldo + u] = sum_f U[level[u]*ldu + f] * x[b*ldx + f], u < nrows, b < nbatch <= 8
+constexpr int kPlainBatch = 8;
+cudaError_t launch_gemv_batch(int nrows, int n, const double* U, long ldu, const int* levels, const double* x,
+                              long ldx, int nbatch, double* out, long ldo, cudaStream_t st);
 
 // gather-expand of a selection expansion: prim[r] = coef[r] * vec[sym_of[r]] (sym_of<0 -> 0)
 cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* coef,
