@@ -204,7 +204,9 @@ struct gain_engine_s {
     int jmax = 0, nsym = 0, maxdeg = 0;
     int num_sms = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev[6] = {};
+    cudaStream_t st2 = nullptr;   // overlaps the upper-vector slicing with the first GEMM
+    cudaEvent_t ev[8] = {};
+    std::vector<long> zkey_V, zkey_H, zkey_U;   // shape/layout the digit buffers were cleared for
     gain::DevArray<double> d3j;
     std::vector<gain::Basis> bases;
     std::vector<gain::Inflation> infl;
@@ -566,11 +568,22 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     return GAIN_OK;
 }
 
+// Digits of nrows source rows into dig [slices][rows_pad][kpad].  host_map (the host copy of
+// col_map, increasing; NULL for the identity) locates each GEMM chunk's source columns.
 gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows, int nrows, int ncols,
-                  const int* col_map, int kpad, int rows_pad, __nv_bfloat16* dig, const SplitParams& p,
-                  int nkb_total, StatsDev& stv, bool with_inerr, const float* inerr_prev,
-                  const int* e_prev) {
+                  const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
+                  __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
+                  const float* inerr_prev, const int* e_prev, cudaStream_t st) {
     split::SliceArgs a;
+    const int nkb = kpad / split::BK;
+    for (int c = 0; c <= p.chunks; ++c) {
+        const int dest0 = c == p.chunks ? kpad : (int)(((long)c * nkb) / p.chunks) * split::BK;
+        int s0;
+        if (c == p.chunks) s0 = ncols;
+        else if (!host_map) s0 = std::min(dest0, ncols);
+        else s0 = (int)(std::lower_bound(host_map->begin(), host_map->begin() + ncols, dest0) - host_map->begin());
+        a.src_chunk[c] = s0;
+    }
     a.src = src;
     a.ld_src = ld;
     a.src_rows = src_rows;
@@ -583,11 +596,10 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     a.slices = p.slices;
     a.beta = p.beta;
     a.nchunks = p.chunks;
-    a.nkb_total = nkb_total;
     a.st = stv.view(with_inerr);
     a.inerr2_prev = inerr_prev;
     a.e_prev = e_prev;
-    GAIN_CUDA(split::launch_slice(a, e->st));
+    GAIN_CUDA(split::launch_slice(a, st));
     return GAIN_OK;
 }
 
@@ -631,8 +643,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         GAIN_TRY(L.bandDig.zero(st, (size_t)p1x.slices * L.fpad * L.W));
         GAIN_TRY(L.bandStats.alloc(L.fpad, 1, false));
         GAIN_TRY(L.bandStats.zero(st, L.fpad, 1, false));
-        GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, L.W, L.fpad, L.bandDig.p, p1x,
-                       L.W / split::BK, L.bandStats, false, nullptr, nullptr));
+        GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, nullptr, L.W, L.fpad, L.bandDig.p, p1x,
+                       L.bandStats, false, nullptr, nullptr, st));
         if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1x.slices))
             return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed for the band digits");
         L.beta1 = p1x.beta;
@@ -652,14 +664,47 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     GAIN_TRY(e->flags1.alloc(kMaxFlags));
     GAIN_TRY(e->flags2.alloc(kMaxFlags));
 
-    // ---- lower vectors -> digits in the padded lower layout
+    // Digit buffers and their row statistics are cleared only when their shape or layout
+    // changes: padding rows and columns are never written, every other entry is.
+    const long lkey = (long)L.key[0] * 1000003L + L.key[1] * 1009L + L.key[2] * 31L + L.key[3];
     const size_t vdig = (size_t)p1x.slices * Bpad * L.kpadI;
+    const size_t hdig = (size_t)p2.slices * Bpad * L.fpad;
+    const size_t udig = (size_t)p2.slices * Nupad * L.fpad;
     GAIN_TRY(e->Vdig.alloc(vdig));
-    GAIN_TRY(e->Vdig.zero(st, vdig));
     GAIN_TRY(e->Vst.alloc(Bpad, 1, false));
-    GAIN_TRY(e->Vst.zero(st, Bpad, 1, false));
-    GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, L.kpadI, Bpad, e->Vdig.p,
-                   p1x, L.kpadI / split::BK, e->Vst, false, nullptr, nullptr));
+    GAIN_TRY(e->Hdig.alloc(hdig));
+    GAIN_TRY(e->Hst.alloc(Bpad, p2.chunks, true));
+    GAIN_TRY(e->Udig.alloc(udig));
+    GAIN_TRY(e->Ust.alloc(Nupad, p2.chunks, false));
+    const std::vector<long> kV = {lkey, p1x.slices, p1x.beta, B, Bpad, (long)(uintptr_t)e->Vdig.p};
+    const std::vector<long> kH = {lkey, p2.slices, p2.chunks, B, Bpad, (long)(uintptr_t)e->Hdig.p};
+    const std::vector<long> kU = {lkey, p2.slices, p2.chunks, Nu, Nupad, (long)(uintptr_t)e->Udig.p};
+    if (e->zkey_V != kV) {
+        GAIN_TRY(e->Vdig.zero(st, vdig));
+        GAIN_TRY(e->Vst.zero(st, Bpad, 1, false));
+        e->zkey_V = kV;
+    }
+    if (e->zkey_H != kH) {
+        GAIN_TRY(e->Hdig.zero(st, hdig));
+        GAIN_TRY(e->Hst.zero(st, Bpad, p2.chunks, true));
+        e->zkey_H = kH;
+    }
+    if (e->zkey_U != kU) {
+        GAIN_TRY(e->Udig.zero(st, udig));
+        GAIN_TRY(e->Ust.zero(st, Nupad, p2.chunks, false));
+        e->zkey_U = kU;
+    }
+
+    // ---- upper vectors -> digits, on the second stream, overlapping the first GEMM
+    GAIN_CUDA(cudaEventRecord(e->ev[6], st));
+    GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
+    GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
+                   e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2));
+    GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
+
+    // ---- lower vectors -> digits in the padded lower layout
+    GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI, Bpad,
+                   e->Vdig.p, p1x, e->Vst, false, nullptr, nullptr, st));
     CUtensorMap tmV, tmH, tmU;
     if (!split::make_digit_map(&tmV, e->Vdig.p, L.kpadI, Bpad, p1x.slices))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (lower digits)");
@@ -730,21 +775,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     rh.rowerr2 = e->rowerr.p;
     GAIN_CUDA(split::launch_refine_h(rh, 2 * e->num_sms, st));
 
-    // ---- H -> digits, upper vectors -> digits
-    const size_t hdig = (size_t)p2.slices * Bpad * L.fpad;
-    GAIN_TRY(e->Hdig.alloc(hdig));
-    GAIN_TRY(e->Hdig.zero(st, hdig));
-    GAIN_TRY(e->Hst.alloc(Bpad, p2.chunks, true));
-    GAIN_TRY(e->Hst.zero(st, Bpad, p2.chunks, true));
-    GAIN_TRY(slice(e, e->H.p, L.fpad, nullptr, B, L.fpad, nullptr, L.fpad, Bpad, e->Hdig.p, p2,
-                   L.fpad / split::BK, e->Hst, true, e->rowerr.p, e->Vst.e.p));
-    const size_t udig = (size_t)p2.slices * Nupad * L.fpad;
-    GAIN_TRY(e->Udig.alloc(udig));
-    GAIN_TRY(e->Udig.zero(st, udig));
-    GAIN_TRY(e->Ust.alloc(Nupad, p2.chunks, false));
-    GAIN_TRY(e->Ust.zero(st, Nupad, p2.chunks, false));
-    GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, L.fpad, Nupad, e->Udig.p,
-                   p2, L.fpad / split::BK, e->Ust, false, nullptr, nullptr));
+    // ---- H -> digits; the upper digits (second stream) must be ready before the second GEMM
+    GAIN_TRY(slice(e, e->H.p, L.fpad, nullptr, B, L.fpad, nullptr, nullptr, L.fpad, Bpad, e->Hdig.p, p2,
+                   e->Hst, true, e->rowerr.p, e->Vst.e.p, st));
+    GAIN_CUDA(cudaStreamWaitEvent(st, e->ev[7], 0));
     if (!split::make_digit_map(&tmH, e->Hdig.p, L.fpad, Bpad, p2.slices) ||
         !split::make_digit_map(&tmU, e->Udig.p, L.fpad, Nupad, p2.slices))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (second GEMM digits)");
@@ -952,6 +986,7 @@ gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_
     e->maxdeg = maxdeg;
     GAIN_CUDA(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device));
     GAIN_CUDA(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+    GAIN_CUDA(cudaStreamCreateWithFlags(&e->st2, cudaStreamNonBlocking));
     for (auto& ev : e->ev) GAIN_CUDA(cudaEventCreate(&ev));
     std::vector<double> t((size_t)(jmax + 1) * (jmax + 1) * 9);
     threej_table_host(jmax, t.data());
@@ -967,6 +1002,7 @@ gain_status gain_engine_destroy(gain_engine e) {
     cudaStreamSynchronize(e->st);
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
+    if (e->st2) cudaStreamDestroy(e->st2);
     if (e->st) cudaStreamDestroy(e->st);
     delete e;
     return GAIN_OK;

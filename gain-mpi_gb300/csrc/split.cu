@@ -488,14 +488,18 @@ k_slice(const SliceArgs a) {
     int nnz = 0;
     float l2sq = 0.0f;
     float tsq[MAX_SLICES];
-    unsigned int dsq[MAX_SLICES * MAX_CHUNKS];
 #pragma unroll
     for (int i = 0; i < MAX_SLICES; ++i) tsq[i] = 0.0f;
-#pragma unroll
-    for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i) dsq[i] = 0u;
     const long mask = (1l << beta) - 1l, halfb = 1l << (beta - 1);
     const float inv2q = pow2f(-q);
-    for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+    // source columns come in chunk order (the column map is increasing): chunk ch covers
+    // src_chunk[ch] .. src_chunk[ch+1]
+    for (int ch = 0; ch < a.nchunks; ++ch) {
+    unsigned int dsq[MAX_SLICES];
+#pragma unroll
+    for (int i = 0; i < MAX_SLICES; ++i) dsq[i] = 0u;
+    const int cend = a.src_chunk[ch + 1];
+    for (int c = a.src_chunk[ch] + tid; c < cend; c += SLICE_THREADS) {
         const unsigned long long bits = src[c];
         const int dc = a.col_map ? a.col_map[c] : c;
         const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
@@ -510,9 +514,6 @@ k_slice(const SliceArgs a) {
             const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
             I = (bits >> 63) ? -(long long)m : (long long)m;
         }
-        int chunk = 0;
-        for (int cc = 1; cc < a.nchunks; ++cc)
-            if (dc / BK >= (int)(((long)cc * a.nkb_total) / a.nchunks)) chunk = cc;
         long long v = I;
         int d[MAX_SLICES];
 #pragma unroll
@@ -540,9 +541,7 @@ k_slice(const SliceArgs a) {
         for (int i = 0; i < MAX_SLICES; ++i) {
             if (i < s) {
                 drow[i * sstride + dc] = __float2bfloat16_rn((float)d[i]);
-#pragma unroll
-                for (int cc = 0; cc < MAX_CHUNKS; ++cc)
-                    if (cc == chunk) dsq[i * MAX_CHUNKS + cc] += (unsigned int)(d[i] * d[i]);
+                dsq[i] += (unsigned int)(d[i] * d[i]);
             }
         }
         if (I != 0) {
@@ -552,6 +551,13 @@ k_slice(const SliceArgs a) {
             l2sq = __fmaf_ru(xv, xv, l2sq);
         }
     }
+    // this chunk's digit sums of squares: warp partials into shared memory
+#pragma unroll
+    for (int i = 0; i < MAX_SLICES; ++i) {
+        for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
+        if ((tid & 31) == 0) red_d[tid >> 5][i * MAX_CHUNKS + ch] = dsq[i];
+    }
+    }
     // block reductions
     for (int o = 16; o > 0; o >>= 1) {
         l2sq = __fadd_ru(l2sq, __shfl_xor_sync(0xffffffffu, l2sq, o));
@@ -560,16 +566,11 @@ k_slice(const SliceArgs a) {
 #pragma unroll
     for (int i = 0; i < MAX_SLICES; ++i)
         for (int o = 16; o > 0; o >>= 1) tsq[i] = __fadd_ru(tsq[i], __shfl_xor_sync(0xffffffffu, tsq[i], o));
-#pragma unroll
-    for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i)
-        for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
     if ((tid & 31) == 0) {
         red_f[tid >> 5] = l2sq;
         red_i[tid >> 5] = nnz;
 #pragma unroll
         for (int i = 0; i < MAX_SLICES; ++i) red_t[tid >> 5][i] = tsq[i];
-#pragma unroll
-        for (int i = 0; i < MAX_SLICES * MAX_CHUNKS; ++i) red_d[tid >> 5][i] = dsq[i];
     }
     __syncthreads();
     if (tid == 0) {

@@ -104,7 +104,9 @@ struct SliceArgs {
     __nv_bfloat16* digits;
     int slices, beta;
     int nchunks;            // chunks of the destination inner dimension for dn
-    int nkb_total;          // k-blocks of BK the chunks split (chunk c: [c n/nch, (c+1) n/nch))
+    // source-column range of each chunk (the column map is increasing): chunk c covers the
+    // sources mapped into destination k-blocks [c n/nch, (c+1) n/nch) of the GEMM
+    int src_chunk[MAX_CHUNKS + 1];
     RowStats st;
     const float* inerr2_prev;  // optional: squared row error in units of 2^{2 e_prev}
     const int* e_prev;         // exponent those units refer to
