@@ -1000,6 +1000,7 @@ gain_status gain_engine_destroy(gain_engine e) {
     if (!e) return GAIN_OK;
     cudaSetDevice(e->device);
     cudaStreamSynchronize(e->st);
+    if (e->st2) cudaStreamSynchronize(e->st2);
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
     if (e->st2) cudaStreamDestroy(e->st2);
