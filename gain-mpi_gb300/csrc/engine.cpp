@@ -424,25 +424,28 @@ struct SplitParams {
 // Digits and chunking from the inner length K of the exact accumulations: the Cauchy-Schwarz
 // certificate needs ||d_i|| ||d_j|| < 2^24 over every chunk; balanced residual digits have
 // ||d||^2 ~ K 4^beta / 12, so K_chunk 4^beta / 12 <= 2^23 leaves a factor-two margin.
-SplitParams choose_params(int K, const gain_split_opts* o, int bits) {
+// Without an explicit digit width the widest one (from beta_default down) whose chunks fit
+// MAX_CHUNKS is taken: wider digits mean fewer digit products for the same bits.
+SplitParams choose_params(int K, const gain_split_opts* o, int bits, int beta_default) {
+    auto chunks_for = [K](int beta) {
+        const double limit = 8388608.0 * 12.0 / std::ldexp(1.0, 2 * beta);
+        return std::max(1, (int)std::ceil((double)K / limit));
+    };
     SplitParams p;
-    p.beta = (o && o->beta) ? o->beta : 7;
+    p.beta = (o && o->beta) ? o->beta : beta_default;
+    if (!(o && (o->beta || o->kchunks)))
+        while (p.beta > 4 && chunks_for(p.beta) > split::MAX_CHUNKS) --p.beta;
     p.slices = (o && o->slices) ? o->slices : (bits + p.beta - 1) / p.beta;
-    if (o && o->kchunks) {
-        p.chunks = o->kchunks;
-    } else {
-        const double limit = 8388608.0 * 12.0 / std::ldexp(1.0, 2 * p.beta);
-        p.chunks = std::max(1, (int)std::ceil((double)K / limit));
-    }
+    p.chunks = (o && o->kchunks) ? o->kchunks : chunks_for(p.beta);
     p.chunks = std::min(p.chunks, split::MAX_CHUNKS);
     return p;
 }
 
 // Bound of the int64 fixed-point recombination, units of 2^{eA+eB}: each digit product adds
-// at most one truncated unit of 2^{-kFix} (in digit units 2^{-2 beta}); the final int64 ->
-// double conversion adds a relative 2^-53, negligible against tol, absorbed by the 1.01.
-float fix_const(const SplitParams& p, int nprods) {
-    return (float)((double)nprods * std::ldexp(1.0, -split::kFix - 2 * p.beta) * 1.01);
+// at most one truncated unit of 2^{-kFixTotal}; the final int64 -> double conversion adds a
+// relative 2^-53, negligible against tol, absorbed by the 1.01.
+float fix_const(int nprods) {
+    return (float)((double)nprods * std::ldexp(1.0, -split::kFixTotal) * 1.01);
 }
 
 std::vector<split::Prod> make_prods(const SplitParams& p) {
@@ -621,17 +624,18 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
 
     // First GEMM: 56 bits (its error reaches every amplitude through ||dH||_2 ||u||_2), one
     // inner chunk per band tile, digits narrowed until that single chunk stays exact.
-    // Second GEMM: 49 bits; options (beta, slices, kchunks) apply to it.
+    // Second GEMM: 48 bits (8-bit digits in up to MAX_CHUNKS chunks, else 7 x 7 bits);
+    // options (beta, slices, kchunks) apply to it.
     gain_split_opts o1{};
     if (opts) o1.beta = opts->beta;
-    const SplitParams p1 = choose_params(L.W, &o1, 56);
+    const SplitParams p1 = choose_params(L.W, &o1, 56, 7);
     SplitParams p1x = p1;
     p1x.chunks = 1;
     while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
         --p1x.beta;
         p1x.slices = (56 + p1x.beta - 1) / p1x.beta;
     }
-    const SplitParams p2 = choose_params(L.fpad, opts, 49);
+    const SplitParams p2 = choose_params(L.fpad, opts, 48, 8);
     if (p1x.slices * p1x.beta > 62 || p2.slices * p2.beta > 62 || p1x.slices > split::MAX_SLICES ||
         p2.slices > split::MAX_SLICES || p1x.beta < 2 || p1x.beta > 8 || p2.beta < 2 || p2.beta > 8 ||
         2 * (p2.slices - 1) * p2.beta > 126 || 2 * (p1x.slices - 1) * p1x.beta > 126)
@@ -695,12 +699,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         e->zkey_U = kU;
     }
 
-    // ---- upper vectors -> digits, on the second stream, overlapping the first GEMM
-    GAIN_CUDA(cudaEventRecord(e->ev[6], st));
-    GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
-    GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
-                   e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2));
-    GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
+    GAIN_CUDA(cudaEventRecord(e->ev[6], st));   // buffers cleared: the upper slicing may start
 
     // ---- lower vectors -> digits in the padded lower layout
     GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI, Bpad,
@@ -742,7 +741,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g1.ldo = L.fpad;
     g1.A = e->Vst.view(false);
     g1.B = L.bandStats.view(false);
-    g1.c_fix = fix_const(p1x, (int)pr1.size());
+    g1.c_fix = fix_const((int)pr1.size());
     g1.c_f64 = (float)((double)(L.W + 64) * std::ldexp(1.0, -53) * 1.01);
     g1.rowerr2 = e->rowerr.p;
     g1.flag_mode = 2;   // every H entry FP64-grade, else recomputed in FP64
@@ -756,6 +755,12 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     GAIN_CUDA(cudaEventRecord(e->ev[2], st));
     GAIN_CUDA(split::launch_gemm(tmV, L.tmBand, g1, e->num_sms, st));
     GAIN_CUDA(cudaEventRecord(e->ev[3], st));
+    // ---- upper vectors -> digits on the low-priority second stream, submitted after the
+    // first GEMM so its CTAs fill the room the GEMM leaves on each SM
+    GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
+    GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
+                   e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2));
+    GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
     // inexact first-GEMM entries recomputed in FP64
     split::RefineHArgs rh;
     rh.flags = e->flags1.p;
@@ -813,7 +818,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.ldo = Nupad;
     g2.A = e->Hst.view(false);   // H is FP64-grade: its error is the FP64 method's own
     g2.B = e->Ust.view(false);
-    g2.c_fix = fix_const(p2, (int)pr2.size());
+    g2.c_fix = fix_const((int)pr2.size());
     g2.c_f64 = (float)((double)(L.nF + 64) * std::ldexp(1.0, -53) * 1.01);
     g2.rowerr2 = nullptr;
     g2.absmax = e->ull.p + 2;
@@ -986,7 +991,11 @@ gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_
     e->maxdeg = maxdeg;
     GAIN_CUDA(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device));
     GAIN_CUDA(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
-    GAIN_CUDA(cudaStreamCreateWithFlags(&e->st2, cudaStreamNonBlocking));
+    {
+        int lo = 0, hi = 0;   // numerically larger = lower priority
+        GAIN_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        GAIN_CUDA(cudaStreamCreateWithPriority(&e->st2, cudaStreamNonBlocking, lo));
+    }
     for (auto& ev : e->ev) GAIN_CUDA(cudaEventCreate(&ev));
     std::vector<double> t((size_t)(jmax + 1) * (jmax + 1) * 9);
     threej_table_host(jmax, t.data());

@@ -2,6 +2,8 @@
 // the persistent tcgen05 digit-product GEMM and the FP64 refinement kernels.
 #include "split.h"
 
+#include <atomic>
+
 #include <cuda_bf16.h>
 
 #include "gain_internal.h"
@@ -120,6 +122,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         : GAIN_R8(0), GAIN_R8(8), GAIN_R8(16), GAIN_R8(24)
         : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : GAIN_R8(0), GAIN_R8(8)
+        : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
@@ -151,12 +160,45 @@ __device__ __forceinline__ double pow2d(int e) {
     if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
     return ldexp(1.0, e);
 }
+// Bits of the double nearest (ties to even) to run 2^E, by integer operations only (the FP64
+// units are slow on this part); *mag = |run| 2^-kFixTotal as a float, truncated.  Results
+// outside the normal range take the FP64 route.
+__device__ __forceinline__ unsigned long long scaled_bits(long long run, int E, float* mag) {
+    if (run == 0) {
+        *mag = 0.0f;
+        return 0ull;
+    }
+    const unsigned long long sign = run < 0 ? (1ull << 63) : 0ull;
+    unsigned long long m = run < 0 ? 0ull - (unsigned long long)run : (unsigned long long)run;
+    int msb = 63 - __clzll((long long)m);
+    if (msb > 52) {
+        const int k = msb - 52;
+        const unsigned long long q = m >> k;
+        const unsigned long long rem = m & ((1ull << k) - 1ull);
+        const unsigned long long half = 1ull << (k - 1);
+        m = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+        if (m >> 53) {   // rounded up to 2^53
+            m >>= 1;
+            ++msb;
+        }
+    } else {
+        m <<= (52 - msb);
+    }
+    *mag = __uint_as_float(((unsigned)(msb - kFixTotal + 127) << 23) | (unsigned)((m >> 29) & 0x7FFFFFull));
+    const int be = msb + E + 1023;
+    if (be <= 0 || be >= 2047) return (unsigned long long)__double_as_longlong((double)run * pow2d(E));
+    return sign | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull);
+}
+
 __device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, int* hi) {
     *lo = (int)(((long)c * nkb) / nch);
     *hi = (int)(((long)(c + 1) * nkb) / nch);
 }
 
 // ------------------------------------------------------------------- the GEMM kernel
+// SMAX / CMAX: compile-time bounds of the slices and chunks a launch may use (register arrays
+// of the epilogue are sized by them).
+template <int SMAX, int CMAX>
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
              const GemmArgs a) {
@@ -284,15 +326,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         // Each digit product arrives as an FP32 accumulator holding an exact integer (|acc| <
         // 2^24 where certified).  It is added, shifted to its weight, into an int64 fixed-point
         // running sum (TMEM columns 256..383 low words, 384..511 high words); only the
-        // weights below 2^{-kFix} are truncated (floor), at most one unit per product.
+        // weights below 2^{-kFixTotal} are truncated (floor), at most one unit per product.
         const int q = warp & 3;
         const int row_in_tile = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         const float two24 = 16777216.0f;
         const int s = a.slices;
-        float wdig[MAX_SLICES];   // 2^{-(i+1) beta}
-#pragma unroll
-        for (int i = 0; i < MAX_SLICES; ++i) wdig[i] = pow2f(-(i + 1) * a.beta);
         uint32_t acc_cnt = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
@@ -309,7 +348,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     break;
                 }
                 tc_fence_after();
-                const int sh = kFix - pr.t * a.beta;
+                const int sh = fix_bits(a.beta) - pr.t * a.beta;
 #pragma unroll 1
                 for (int c = 0; c < BN / 32; ++c) {
                     uint32_t acc[32], lo_r[32], hi_r[32];
@@ -339,88 +378,127 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 first = false;
             }
             if (!ok) break;
-            // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags
+            // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags.
+            // Row terms live in registers; the statistics of 32 columns at a time are read one
+            // column per lane and broadcast with shuffles (no shared memory, no cross-warp sync).
             const int r = tl.m0 + row_in_tile;
             const bool rvalid = r < a.rows_valid;
             const int eA = a.A.e[r];
             const int nnzA = a.A.nnz[r];
             const float l2A = a.A.l2[r];
             const float inA = a.A.inerr ? a.A.inerr[r] : 0.0f;
-            float dnA[MAX_CHUNKS], dvA[MAX_SLICES], rvA[MAX_SLICES];
+            const float* dvA = a.A.dnv + (long)r * MAX_SLICES;
+            const float* rvA = a.A.rnv + (long)r * MAX_SLICES;
+            const float rlastA = rvA[s - 1];
+            float dnA[CMAX], wA[SMAX], rA[SMAX];
 #pragma unroll
-            for (int c = 0; c < MAX_CHUNKS; ++c) dnA[c] = c < a.nchunks ? a.A.dn[(long)r * a.nchunks + c] : 0.0f;
+            for (int c = 0; c < CMAX; ++c) dnA[c] = c < a.nchunks ? a.A.dn[(long)r * a.nchunks + c] : 0.0f;
+            // |running sum| <= 2^kFixTotal SA SB with S = sum_i 2^{-(i+1) beta} ||d_i||: below
+            // 2^62 (SA SB < 2^12) the int64 recombination cannot overflow
+            float sA = 0.0f;
 #pragma unroll
-            for (int i = 0; i < MAX_SLICES; ++i) {
-                dvA[i] = i < s ? a.A.dnv[(long)r * MAX_SLICES + i] : 0.0f;
-                rvA[i] = i < s ? a.A.rnv[(long)r * MAX_SLICES + i] : 0.0f;
+            for (int i = 0; i < SMAX; ++i) {
+                wA[i] = 0.0f;
+                rA[i] = 0.0f;
+                if (i < s) {
+                    const float dv = dvA[i];
+                    wA[i] = __fmul_ru(pow2f(-(i + 1) * a.beta), dv);
+                    rA[i] = rvA[s - 1 - i];
+                    sA = __fmaf_ru(pow2f(-(i + 1) * a.beta), dv, sA);
+                }
             }
+            const float cf64A = __fmul_ru(a.c_f64, l2A);
             float rowerr2 = 0.0f;
             unsigned long long vmax = 0ull;
             double* orow = a.out + (long)r * a.ldo;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
-                uint32_t lo_r[32], hi_r[32];
-                if (!first) {
-                    tmem_ld32(tmem + lane_off + 256 + c * 32, lo_r);
-                    tmem_ld32(tmem + lane_off + 384 + c * 32, hi_r);
-                    tmem_wait_ld();
-                } else {
+                // this lane's column of the group of 32
+                const int mycol = tl.n0 + c * 32 + lane;
+                const int ceB = __ldg(&a.B.e[mycol]);
+                const int cnz = __ldg(&a.B.nnz[mycol]);
+                const float cl2 = __ldg(&a.B.l2[mycol]);
+                const float* dvB = a.B.dnv + (long)mycol * MAX_SLICES;
+                const float* rvB = a.B.rnv + (long)mycol * MAX_SLICES;
+                const float crl = __ldg(&rvB[s - 1]);
+                float cA[SMAX], cB[SMAX], cdn[CMAX];
+                float csB = 0.0f;
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) { lo_r[j] = 0u; hi_r[j] = 0u; }
+                for (int i = 0; i < SMAX; ++i) {
+                    cA[i] = 0.0f;
+                    cB[i] = 0.0f;
+                    if (i < s) {
+                        cA[i] = __ldg(&rvB[s - 1 - i]);
+                        cB[i] = __fmul_ru(pow2f(-(i + 1) * a.beta), __ldg(&dvB[i]));
+                        csB = __fadd_ru(csB, cB[i]);
+                    }
                 }
-#pragma unroll 2
-                for (int j = 0; j < 32; ++j) {
-                    const int col = tl.n0 + c * 32 + j;
-                    const long long run = (long long)(((unsigned long long)hi_r[j] << 32) | lo_r[j]);
-                    const int eB = __ldg(&a.B.e[col]);
-                    const double v = (double)run * pow2d(eA + eB - 2 * a.beta - kFix);
-                    orow[col] = v;
-                    const int nnzB = __ldg(&a.B.nnz[col]);
-                    if (nnzA == 0 || nnzB == 0) continue;
-                    bool exact = true;
 #pragma unroll
-                    for (int cc = 0; cc < MAX_CHUNKS; ++cc)
-                        if (cc < a.nchunks &&
-                            __fmul_ru(dnA[cc], __ldg(&a.B.dn[(long)col * a.nchunks + cc])) >= two24)
-                            exact = false;
-                    // |x^ y^ - C| <= ||x^ - X|| ||y^|| + sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)||
-                    // and the same with x and y exchanged; the smaller of the two holds.
-                    const float l2B = __ldg(&a.B.l2[col]);
-                    const float* dvB = a.B.dnv + (long)col * MAX_SLICES;
-                    const float* rvB = a.B.rnv + (long)col * MAX_SLICES;
-                    float bA = __fmul_ru(rvA[s - 1], l2B);
-                    float bB = __fmul_ru(__ldg(&rvB[s - 1]), l2A);
+                for (int cc = 0; cc < CMAX; ++cc)
+                    cdn[cc] = cc < a.nchunks ? __ldg(&a.B.dn[(long)mycol * a.nchunks + cc]) : 0.0f;
+#pragma unroll 1
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t lo_r[16], hi_r[16];
+                    if (!first) {
+                        tmem_ld16(tmem + lane_off + 256 + c * 32 + h * 16, lo_r);
+                        tmem_ld16(tmem + lane_off + 384 + c * 32 + h * 16, hi_r);
+                        tmem_wait_ld();
+                    } else {
 #pragma unroll
-                    for (int i = 0; i < MAX_SLICES; ++i) {
-                        if (i < s) {
-                            bA = __fmaf_ru(__fmul_ru(wdig[i], dvA[i]), __ldg(&rvB[s - 1 - i]), bA);
-                            bB = __fmaf_ru(__fmul_ru(wdig[i], __ldg(&dvB[i])), rvA[s - 1 - i], bB);
+                        for (int j = 0; j < 16; ++j) { lo_r[j] = 0u; hi_r[j] = 0u; }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int src = h * 16 + j;   // lane holding this column's statistics
+                        const int col = tl.n0 + c * 32 + src;
+                        const long long run = (long long)(((unsigned long long)hi_r[j] << 32) | lo_r[j]);
+                        const int eB = __shfl_sync(0xffffffffu, ceB, src);
+                        float av;
+                        const unsigned long long vbits = scaled_bits(run, eA + eB - kFixTotal, &av);
+                        orow[col] = __longlong_as_double((long long)vbits);
+                        const int nnzB = __shfl_sync(0xffffffffu, cnz, src);
+                        const float l2B = __shfl_sync(0xffffffffu, cl2, src);
+                        bool exact = true;
+#pragma unroll
+                        for (int cc = 0; cc < CMAX; ++cc) {
+                            const float dB = __shfl_sync(0xffffffffu, cdn[cc], src);
+                            if (cc < a.nchunks && __fmul_ru(dnA[cc], dB) >= two24) exact = false;
                         }
-                    }
-                    float bound = __fadd_ru(fminf(bA, bB), a.c_fix);
-                    bound = __fmaf_ru(inA, l2B, bound);
-                    if (exact && rvalid && col < a.cols_valid) {
-                        const unsigned long long vb = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-                        vmax = vb > vmax ? vb : vmax;
-                    }
-                    if (a.rowerr2) {
-                        const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
-                        rowerr2 = __fmaf_ru(bb, bb, rowerr2);
-                    }
-                    // certification: flag_mode 1 -> within max(tol |value|, FP64 bound of the
-                    // same dot product); flag_mode 2 -> within the FP64 bound (FP64-grade)
-                    bool flag = !exact;
-                    const float f64b = __fmul_ru(__fmul_ru(a.c_f64, l2A), l2B);
-                    if (a.flag_mode == 1) {
-                        // |value| in units of 2^{eA+eB}: run 2^{-2 beta - kFix}
-                        const float av = fabsf((float)run) * pow2f(-2 * a.beta - kFix);
-                        flag = flag || (bound > fmaxf(a.tol * av, f64b));
-                    } else if (a.flag_mode == 2) {
-                        flag = flag || (bound > f64b);
-                    }
-                    if (flag && rvalid && col < a.cols_valid) {
-                        const unsigned int idx = atomicAdd(a.nflags, 1u);
-                        if ((int)idx < a.max_flags) a.flags[idx] = make_int2(r, col);
+                        // |x^ y^ - C| <= ||x^ - X|| ||y^|| + sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)||
+                        // and the same with x and y exchanged; the smaller of the two holds.
+                        float bA = __fmul_ru(rlastA, l2B);
+                        float bB = __fmul_ru(__shfl_sync(0xffffffffu, crl, src), l2A);
+#pragma unroll
+                        for (int i = 0; i < SMAX; ++i) {
+                            const float ca = __shfl_sync(0xffffffffu, cA[i], src);
+                            const float cb = __shfl_sync(0xffffffffu, cB[i], src);
+                            if (i < s) {
+                                bA = __fmaf_ru(wA[i], ca, bA);
+                                bB = __fmaf_ru(cb, rA[i], bB);
+                            }
+                        }
+                        if (__fmul_ru(sA, __shfl_sync(0xffffffffu, csB, src)) >= 4096.0f) exact = false;
+                        if (nnzA == 0 || nnzB == 0) continue;
+                        float bound = __fadd_ru(fminf(bA, bB), a.c_fix);
+                        bound = __fmaf_ru(inA, l2B, bound);
+                        if (exact && rvalid && col < a.cols_valid) {
+                            const unsigned long long vb = vbits & 0x7FFFFFFFFFFFFFFFull;
+                            vmax = vb > vmax ? vb : vmax;
+                        }
+                        if (a.rowerr2) {
+                            const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
+                            rowerr2 = __fmaf_ru(bb, bb, rowerr2);
+                        }
+                        // certification: flag_mode 1 -> within max(tol |value|, FP64 bound of the
+                        // same dot product); flag_mode 2 -> within the FP64 bound (FP64-grade)
+                        bool flag = !exact;
+                        const float f64b = __fmul_ru(cf64A, l2B);
+                        if (a.flag_mode == 1) flag = flag || (bound > fmaxf(a.tol * av, f64b));
+                        else if (a.flag_mode == 2) flag = flag || (bound > f64b);
+                        if (flag && rvalid && col < a.cols_valid) {
+                            const unsigned int idx = atomicAdd(a.nflags, 1u);
+                            if ((int)idx < a.max_flags) a.flags[idx] = make_int2(r, col);
+                        }
                     }
                 }
             }
@@ -585,25 +663,25 @@ k_slice(const SliceArgs a) {
         a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(L2), slack), dq);
         for (int i = 0; i < MAX_SLICES; ++i) {
             float tq = 0.0f;
-            unsigned int dd = 0;
+            unsigned long long dd = 0;
             if (i < s) {
                 for (int w = 0; w < SLICE_THREADS / 32; ++w) {
                     tq = __fadd_ru(tq, red_t[w][i]);
                     for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
                 }
             }
-            a.st.dnv[(long)row * MAX_SLICES + i] = i < s ? __fsqrt_ru(__uint2float_ru(dd)) : 0.0f;
+            a.st.dnv[(long)row * MAX_SLICES + i] = i < s ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
             a.st.rnv[(long)row * MAX_SLICES + i] =
                 i < s ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
         }
         for (int c = 0; c < a.nchunks; ++c) {
-            unsigned int m = 0;
+            unsigned long long m = 0;
             for (int i = 0; i < s; ++i) {
-                unsigned int t = 0;
+                unsigned long long t = 0;
                 for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
                 m = t > m ? t : m;
             }
-            a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__uint2float_ru(m));
+            a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
         }
         if (a.st.inerr) {
             float v = 0.0f;
@@ -732,18 +810,48 @@ size_t gemm_smem_bytes() {
     return (size_t)STAGES * (STAGE_A + STAGE_B) + 1024 /* align slack */ + 256 /* barriers */;
 }
 
+// Kernel instances by (max slices, max chunks): the two common configurations (first GEMM:
+// up to 8 slices in one chunk; second GEMM: up to 6 slices in up to 8 chunks) and a general one.
+typedef void (*GemmKernel)(const CUtensorMap, const CUtensorMap, const GemmArgs);
+static GemmKernel gemm_kernel_for(int slices, int chunks) {
+    if (slices <= 8 && chunks <= 1) return k_digit_gemm<8, 1>;
+    if (slices <= 6 && chunks <= MAX_CHUNKS) return k_digit_gemm<6, MAX_CHUNKS>;
+    return k_digit_gemm<MAX_SLICES, MAX_CHUNKS>;
+}
+
+// Function attributes are per device: set them once on each device that launches.
+// All kernels ask for the largest shared-memory carveout, so that slicing CTAs can share
+// an SM with a resident GEMM CTA (an SM runs one L1/shared split at a time).
+static cudaError_t set_attributes_once() {
+    static std::atomic<unsigned long long> done{0};   // bit per device ordinal (< 64)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return cudaSuccess;
+    const GemmKernel ks[3] = {k_digit_gemm<8, 1>, k_digit_gemm<6, MAX_CHUNKS>, k_digit_gemm<MAX_SLICES, MAX_CHUNKS>};
+    for (GemmKernel k : ks) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    }
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_slice, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    done.fetch_or(bit);
+    return cudaSuccess;
+}
+
 cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a,
                         int num_sms, cudaStream_t st) {
-    static bool attr_set = false;
     const size_t smem = gemm_smem_bytes();
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_digit_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    cudaError_t e = set_attributes_once();
+    if (e != cudaSuccess) return e;
     if (a.ntiles <= 0) return cudaSuccess;
+    if (a.slices < 1 || a.slices > MAX_SLICES || a.nchunks < 1 || a.nchunks > MAX_CHUNKS)
+        return cudaErrorInvalidValue;
     const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
-    k_digit_gemm<<<grid, NTHREADS, smem, st>>>(tmA, tmB, a);
+    gemm_kernel_for(a.slices, a.nchunks)<<<grid, NTHREADS, smem, st>>>(tmA, tmB, a);
     return cudaGetLastError();
 }
 
@@ -774,6 +882,8 @@ bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int sl
 
 cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st) {
     if (a.nrows <= 0) return cudaSuccess;
+    cudaError_t e = set_attributes_once();
+    if (e != cudaSuccess) return e;
     k_slice<<<a.nrows, SLICE_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }

@@ -22,7 +22,7 @@ constexpr int BM = 128;     // output rows per tile (TMEM lanes)
 constexpr int BN = 128;     // output columns per tile
 constexpr int BK = 64;      // inner elements per stage (one 128-byte swizzle row of BF16)
 constexpr int STAGES = 6;
-constexpr int MAX_CHUNKS = 4;
+constexpr int MAX_CHUNKS = 8;
 constexpr int MAX_SLICES = 10;
 
 struct Tile {
@@ -40,8 +40,10 @@ struct Prod {
 };
 
 // Fixed-point position of the exact recombination: the running sum of the digit products
-// of one output is an int64 in units of 2^{-kFix} (of the product's digit units 2^{-2 beta}).
-constexpr int kFix = 36;
+// of one output is an int64 in units of 2^{-kFixTotal} of 2^{eA+eB}, i.e. 2^{-fix_bits(beta)}
+// of the digit-product units 2^{-2 beta}.
+constexpr int kFixTotal = 50;
+__host__ __device__ constexpr int fix_bits(int beta) { return kFixTotal - 2 * beta; }
 
 // Per-row data of a sliced operand (x^ = x 2^{-e}; all norms rounded up).
 struct RowStats {
@@ -65,7 +67,7 @@ struct GemmArgs {
     double* out;
     long ldo;
     RowStats A, B;
-    // bound of the fixed-point recombination (units of 2^{eA+eB}): nprods 2^{-kFix - 2 beta}
+    // bound of the fixed-point recombination (units of 2^{eA+eB}): nprods 2^{-kFixTotal}
     float c_fix;
     // worst-case rounding bound of an FP64 dot product of the same two rows, per unit of
     // ||x^||_2 ||y^||_2: (K + 64) 2^-53; a line is certified when its bound is within

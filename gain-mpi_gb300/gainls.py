@@ -17,7 +17,8 @@ from typing import Optional, Sequence
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libgainls.so")
+# GAINLS_LIBRARY selects another build of the same C ABI (e.g. an instrumented one)
+LIB_PATH = os.environ.get("GAINLS_LIBRARY") or os.path.join(HERE, "lib", "libgainls.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "gain_ls.h")
 
 PATH_PLAIN_FP64 = 0
