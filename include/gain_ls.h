@@ -72,6 +72,19 @@ gain_status gain_expand(int dimenI, int igammaI, int maxcoeff, int idegI, int sd
  * which runs in CUBLAS_POINTER_MODE_DEVICE (:202). */
 gain_status gain_dot(int n, const double* x, const double* y, double* result, void* stream);
 
+/* Same result as gain_dot (summed in another order: blocks of GAIN_DOT_NOALLOC_CHUNK
+ * elements, then the block sums in block order) for callers that cannot allocate device
+ * memory: it calls no cudaMalloc/cudaFree and no allocating library.  Its scratch is a
+ * fixed device array (GAIN_DOT_NOALLOC_MAX_N / GAIN_DOT_NOALLOC_CHUNK partial sums plus a
+ * completion ticket, about 128 KB per device); n above GAIN_DOT_NOALLOC_MAX_N is rejected
+ * with GAIN_ERR_INVALID_ARG.  The first call on each device looks up that array's address
+ * (set-up); make that first call before any stream capture.  The scratch is shared by all
+ * calls on a device: calls whose kernels overlap on the GPU race on it.
+ * No counterpart in the reference (its dot product is the cuBLAS call gain_dot replaces). */
+#define GAIN_DOT_NOALLOC_CHUNK 4096
+#define GAIN_DOT_NOALLOC_MAX_N (16384LL * GAIN_DOT_NOALLOC_CHUNK)
+gain_status gain_dot_noalloc(int n, const double* x, const double* y, double* result, void* stream);
+
 /* Host: the Wigner-3j table GpuManager::InitializeAndTransferConstants builds
  * (BaseClasses/GpuManager.cpp:166-181, three_j -> TroveFortran/fort_func.f90:7-104):
  *   table[jI + kI(jmax+1) + (jF-jI+1)(jmax+1)^2 + (kF-kI+1)3(jmax+1)^2] = 3j(jI 1 jF; kI, kF-kI, -kF)
