@@ -12,8 +12,10 @@ namespace gain {
 namespace split {
 namespace {
 
-constexpr uint32_t STAGE_A = BM * BK * 2;   // bytes per A stage (16 KB)
-constexpr uint32_t STAGE_B = BN * BK * 2;   // bytes per B stage (16 KB)
+constexpr uint32_t BOX_A = BM * BK * 2;     // bytes of one A k-block box (16 KB)
+constexpr uint32_t BOX_B = BN * BK * 2;     // bytes of one B k-block box (16 KB)
+constexpr uint32_t STAGE_A = KSTEP * BOX_A; // bytes per A stage
+constexpr uint32_t STAGE_B = KSTEP * BOX_B; // bytes per B stage
 constexpr int NTHREADS = 192;               // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr uint32_t TMEM_COLS = 512;         // acc0 [0,128) acc1 [128,256) hi [256,384) lo [384,512)
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s per wait before giving up
@@ -32,14 +34,16 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
+// Probe with a zero suspend-time hint: the caller loops (with its own time limit), and a
+// probe that does not offer to suspend costs the MMA-issuing thread less time per stage.
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(0)
         : "memory");
     return ok != 0;
 }
@@ -254,15 +258,21 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     const Prod pr = a.prods[p];
                     int lo, hi;
                     chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
-                    for (int kb = lo; kb < hi; ++kb) {
+                    // one stage holds up to KSTEP consecutive k-blocks of the pass
+                    for (int kb = lo; kb < hi; kb += KSTEP) {
+                        const int nk = hi - kb < KSTEP ? hi - kb : KSTEP;
                         if (!mbar_wait(smem_u32(&empty[stage]), phase ^ 1, abort_flag, a.err, 1)) {
                             ok = false;
                             break;
                         }
                         const uint32_t fb = smem_u32(&full[stage]);
-                        mbar_expect_tx(fb, STAGE_A + STAGE_B);
-                        tma_load_3d(smem_u32(sA + stage * STAGE_A), &tmA, fb, tl.a_k0 + kb * BK, tl.m0, pr.ia);
-                        tma_load_3d(smem_u32(sB + stage * STAGE_B), &tmB, fb, tl.b_k0 + kb * BK, tl.n0, pr.ib);
+                        mbar_expect_tx(fb, (uint32_t)nk * (BOX_A + BOX_B));
+                        for (int h = 0; h < nk; ++h) {
+                            tma_load_3d(smem_u32(sA + stage * STAGE_A + h * BOX_A), &tmA, fb,
+                                        tl.a_k0 + (kb + h) * BK, tl.m0, pr.ia);
+                            tma_load_3d(smem_u32(sB + stage * STAGE_B + h * BOX_B), &tmB, fb,
+                                        tl.b_k0 + (kb + h) * BK, tl.n0, pr.ib);
+                        }
                         issued_mask |= 1u << stage;
                         last_par = (last_par & ~(1u << stage)) | (phase << stage);
                         if (++stage == STAGES) { stage = 0; phase ^= 1; }
@@ -295,7 +305,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
                     tc_fence_after();
                     const uint32_t d = tmem + b * BN;
-                    for (int kb = lo; kb < hi; ++kb) {
+                    for (int kb = lo; kb < hi; kb += KSTEP) {
+                        const int nk = hi - kb < KSTEP ? hi - kb : KSTEP;
                         if (!mbar_wait(smem_u32(&full[stage]), phase, abort_flag, a.err, 3)) {
                             ok = false;
                             break;
@@ -306,6 +317,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
 #pragma unroll
                         for (int kk = 0; kk < BK / 16; ++kk)
                             mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (kb > lo || kk > 0) ? 1u : 0u);
+                        if (nk > 1) {
+                            // second k-block of the stage: boxes 16 KB further (descriptor units of 16 B)
+#pragma unroll
+                            for (int kk = 0; kk < BK / 16; ++kk)
+                                mma_bf16(d, ad + (BOX_A >> 4) + 2 * kk, bd + (BOX_B >> 4) + 2 * kk, kIdesc, 1u);
+                        }
                         any = true;
                         mma_commit(smem_u32(&empty[stage]));
                         if (++stage == STAGES) { stage = 0; phase ^= 1; }

@@ -21,7 +21,8 @@ namespace split {
 constexpr int BM = 128;     // output rows per tile (TMEM lanes)
 constexpr int BN = 128;     // output columns per tile
 constexpr int BK = 64;      // inner elements per stage (one 128-byte swizzle row of BF16)
-constexpr int STAGES = 6;
+constexpr int KSTEP = 2;    // k-blocks per pipeline stage (one barrier wait per 8 MMAs)
+constexpr int STAGES = 3;   // stages of KSTEP k-blocks (64 KB each)
 constexpr int MAX_CHUNKS = 8;
 constexpr int MAX_SLICES = 10;
 
