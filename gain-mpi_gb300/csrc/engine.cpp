@@ -448,11 +448,16 @@ float fix_const(int nprods) {
     return (float)((double)nprods * std::ldexp(1.0, -split::kFixTotal) * 1.01);
 }
 
+// Digit products of a tile in chunk-major order, then by A digit plane: while the persistent
+// CTAs work through one inner chunk, that chunk's digit tiles for all their rows and columns
+// (tens of MB) stay in L2 and are read from HBM once, and consecutive passes reuse the same
+// A plane (product-major order re-streamed every plane of every chunk from HBM).  The int64
+// recombination does not depend on the order.
 std::vector<split::Prod> make_prods(const SplitParams& p) {
     std::vector<split::Prod> v;
-    for (int t = 0; t < p.slices; ++t)
-        for (int i = 0; i <= t; ++i)
-            for (int c = 0; c < p.chunks; ++c) v.push_back({i, t - i, t, c});
+    for (int c = 0; c < p.chunks; ++c)
+        for (int i = 0; i < p.slices; ++i)
+            for (int j = 0; i + j < p.slices; ++j) v.push_back({i, j, i + j, c});
     return v;
 }
 
