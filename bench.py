@@ -318,8 +318,9 @@ def main():
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng.upload_eigvecs(0, GI, vl_h)
-        eng.upload_eigvecs(1, GF, vu_h)
+        # queued copies: the upper vectors stream in while the lower side is computed
+        eng.upload_eigvecs_async(0, GI, vl_h)
+        eng.upload_eigvecs_async(1, GF, vu_h)
         eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT)
         eng.lines(inp["eI"], inp["eF"], JI, JF, intensity=False, want=("S", "A"), out_S=S_h, out_A=A_h)
         torch.cuda.synchronize()

@@ -130,6 +130,15 @@ struct Inflation {
 struct Eig {
     int nlevels = 0, nsize = 0;
     DevArray<double> d;
+    // recorded on the copy stream after an asynchronous upload; every consumer's stream waits
+    // on it before reading d (NULL until the first asynchronous upload)
+    cudaEvent_t ready = nullptr;
+    Eig() = default;
+    Eig(const Eig&) = delete;
+    Eig& operator=(const Eig&) = delete;
+    ~Eig() {
+        if (ready) cudaEventDestroy(ready);
+    }
 };
 
 struct StatsDev {
@@ -204,8 +213,10 @@ struct gain_engine_s {
     int jmax = 0, nsym = 0, maxdeg = 0;
     int num_sms = 0;
     cudaStream_t st = nullptr;
-    cudaStream_t st2 = nullptr;   // overlaps the upper-vector slicing with the first GEMM
+    cudaStream_t st2 = nullptr;   // upper-vector slicing, concurrent with the lower side
+    cudaStream_t stc = nullptr;   // asynchronous eigenvector uploads
     cudaEvent_t ev[8] = {};
+    cudaEvent_t ev_up = nullptr;  // orders an asynchronous upload after queued engine work
     std::vector<long> zkey_V, zkey_H, zkey_U;   // shape/layout the digit buffers were cleared for
     gain::DevArray<double> d3j;
     std::vector<gain::Basis> bases;
@@ -369,6 +380,8 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) 
     }
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+    if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st, EI.ready, 0));
+    if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st, EF.ready, 0));
     GAIN_TRY(e->d_lower.upload(j->lower_levels, j->nlower));
     GAIN_TRY(e->d_upper.upload(j->upper_levels, j->nupper));
     // The reference's method, one half line strength per lower state followed by its dot
@@ -581,8 +594,9 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
 gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows, int nrows, int ncols,
                   const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
                   __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
-                  const float* inerr_prev, const int* e_prev, cudaStream_t st) {
+                  const float* inerr_prev, const int* e_prev, cudaStream_t st, int grid_limit = 0) {
     split::SliceArgs a;
+    a.grid_limit = grid_limit;
     const int nkb = kpad / split::BK;
     for (int c = 0; c <= p.chunks; ++c) {
         const int dest0 = c == p.chunks ? kpad : (int)(((long)c * nkb) / p.chunks) * split::BK;
@@ -626,6 +640,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     PairLayout& L = e->layout;
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+    // an asynchronous upload of the lower vectors must land before the lower slicing; the upper
+    // vectors are awaited on the second stream only, so their copy overlaps the lower side
+    if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EI.ready, 0));
 
     // First GEMM: 56 bits (its error reaches every amplitude through ||dH||_2 ||u||_2), one
     // inner chunk per band tile, digits narrowed until that single chunk stays exact.
@@ -704,7 +721,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         e->zkey_U = kU;
     }
 
-    GAIN_CUDA(cudaEventRecord(e->ev[6], st));   // buffers cleared: the upper slicing may start
+    // The upper slicing runs on the second stream from here on.  It cannot share SMs with the
+    // first GEMM (the GEMM's 256-register warps fill two SM sub-partitions' register files),
+    // so it overlaps the lower slicing and precedes the GEMM.
+    GAIN_CUDA(cudaEventRecord(e->ev[6], st));
 
     // ---- lower vectors -> digits in the padded lower layout
     GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI, Bpad,
@@ -760,9 +780,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     GAIN_CUDA(cudaEventRecord(e->ev[2], st));
     GAIN_CUDA(split::launch_gemm(tmV, L.tmBand, g1, e->num_sms, st));
     GAIN_CUDA(cudaEventRecord(e->ev[3], st));
-    // ---- upper vectors -> digits on the low-priority second stream, submitted after the
-    // first GEMM so its CTAs fill the room the GEMM leaves on each SM
+    // ---- upper vectors -> digits on the low-priority second stream
     GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
+    if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready, 0));
     GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
                    e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2));
     GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
@@ -1001,7 +1021,9 @@ gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_
         GAIN_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
         GAIN_CUDA(cudaStreamCreateWithPriority(&e->st2, cudaStreamNonBlocking, lo));
     }
+    GAIN_CUDA(cudaStreamCreateWithFlags(&e->stc, cudaStreamNonBlocking));
     for (auto& ev : e->ev) GAIN_CUDA(cudaEventCreate(&ev));
+    GAIN_CUDA(cudaEventCreateWithFlags(&e->ev_up, cudaEventDisableTiming));
     std::vector<double> t((size_t)(jmax + 1) * (jmax + 1) * 9);
     threej_table_host(jmax, t.data());
     GAIN_TRY(e->d3j.upload(t));
@@ -1015,8 +1037,11 @@ gain_status gain_engine_destroy(gain_engine e) {
     cudaSetDevice(e->device);
     cudaStreamSynchronize(e->st);
     if (e->st2) cudaStreamSynchronize(e->st2);
+    if (e->stc) cudaStreamSynchronize(e->stc);
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
+    if (e->ev_up) cudaEventDestroy(e->ev_up);
+    if (e->stc) cudaStreamDestroy(e->stc);
     if (e->st2) cudaStreamDestroy(e->st2);
     if (e->st) cudaStreamDestroy(e->st);
     delete e;
@@ -1145,12 +1170,43 @@ gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels,
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs: bad argument");
     auto& slot = e->eig[{jind, gamma}];
     if (!slot) slot.reset(new Eig());
+    if (slot->ready) GAIN_CUDA(cudaEventSynchronize(slot->ready));   // an asynchronous copy into it
     slot->nlevels = nlevels;
     slot->nsize = nsize;
     GAIN_TRY(slot->d.alloc((size_t)nlevels * nsize));
     GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyHostToDevice,
                               e->st));
     GAIN_CUDA(cudaStreamSynchronize(e->st));
+    return GAIN_OK;
+}
+
+gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nlevels, int nsize,
+                                      const double* vecs) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (jind < 0 || gamma < 0 || gamma >= e->nsym || nlevels <= 0 || nsize <= 0 || !vecs)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs_async: bad argument");
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, vecs) != cudaSuccess) {
+        (void)cudaGetLastError();
+        pa.type = cudaMemoryTypeUnregistered;
+    }
+    // pageable memory cannot be copied asynchronously: the synchronous upload
+    if (pa.type != cudaMemoryTypeHost) return gain_upload_eigvecs(e, jind, gamma, nlevels, nsize, vecs);
+    auto& slot = e->eig[{jind, gamma}];
+    if (!slot) slot.reset(new Eig());
+    if (!slot->ready) GAIN_CUDA(cudaEventCreateWithFlags(&slot->ready, cudaEventDisableTiming));
+    GAIN_CUDA(cudaEventSynchronize(slot->ready));   // a previous asynchronous copy into it
+    slot->nlevels = nlevels;
+    slot->nsize = nsize;
+    GAIN_TRY(slot->d.alloc((size_t)nlevels * nsize));
+    // after everything already queued on the engine's streams (the second stream's work is
+    // joined to the first before each run ends)
+    GAIN_CUDA(cudaEventRecord(e->ev_up, e->st));
+    GAIN_CUDA(cudaStreamWaitEvent(e->stc, e->ev_up, 0));
+    GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyHostToDevice,
+                              e->stc));
+    GAIN_CUDA(cudaEventRecord(slot->ready, e->stc));
     return GAIN_OK;
 }
 

@@ -547,168 +547,172 @@ constexpr int SLICE_THREADS = 256;
 
 __global__ void __launch_bounds__(SLICE_THREADS)
 k_slice(const SliceArgs a) {
-    const int row = blockIdx.x;
     const int tid = threadIdx.x;
-    const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
-    const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
-    __shared__ unsigned long long red_u[SLICE_THREADS / 32];
-    __shared__ float red_f[SLICE_THREADS / 32];
-    __shared__ int red_i[SLICE_THREADS / 32];
-    __shared__ float red_t[SLICE_THREADS / 32][MAX_SLICES];
-    __shared__ unsigned int red_d[SLICE_THREADS / 32][MAX_SLICES * MAX_CHUNKS];
+    // one row per iteration; the grid may be smaller than the row count (a capped grid
+    // leaves room on every SM for a concurrent kernel)
+    for (int row = blockIdx.x; row < a.nrows; row += gridDim.x) {
+        const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
+        const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
+        __shared__ unsigned long long red_u[SLICE_THREADS / 32];
+        __shared__ float red_f[SLICE_THREADS / 32];
+        __shared__ int red_i[SLICE_THREADS / 32];
+        __shared__ float red_t[SLICE_THREADS / 32][MAX_SLICES];
+        __shared__ unsigned int red_d[SLICE_THREADS / 32][MAX_SLICES * MAX_CHUNKS];
 
-    // pass 1: max |x| through the IEEE bit pattern (integer compares only)
-    unsigned long long mx = 0;
-    for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
-        const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
-        mx = b > mx ? b : mx;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
-        mx = y > mx ? y : mx;
-    }
-    if ((tid & 31) == 0) red_u[tid >> 5] = mx;
-    __syncthreads();
-    mx = 0;
-    for (int w = 0; w < SLICE_THREADS / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
-    if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
-    const int Emax = (int)(mx >> 52);
-    const bool zero_row = (mx == 0);
-    const int e = zero_row ? 0 : (Emax > 0 ? Emax - 1022 : -1022);
-    const int s = a.slices, beta = a.beta;
-    const int q = s * beta;
-    const long sstride = a.slice_stride;
-    __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
+        // pass 1: max |x| through the IEEE bit pattern (integer compares only)
+        unsigned long long mx = 0;
+        for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+            const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+            mx = y > mx ? y : mx;
+        }
+        if ((tid & 31) == 0) red_u[tid >> 5] = mx;
+        __syncthreads();
+        mx = 0;
+        for (int w = 0; w < SLICE_THREADS / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
+        if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
+        const int Emax = (int)(mx >> 52);
+        const bool zero_row = (mx == 0);
+        const int e = zero_row ? 0 : (Emax > 0 ? Emax - 1022 : -1022);
+        const int s = a.slices, beta = a.beta;
+        const int q = s * beta;
+        const long sstride = a.slice_stride;
+        __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
 
-    int nnz = 0;
-    float l2sq = 0.0f;
-    float tsq[MAX_SLICES];
-#pragma unroll
-    for (int i = 0; i < MAX_SLICES; ++i) tsq[i] = 0.0f;
-    const long mask = (1l << beta) - 1l, halfb = 1l << (beta - 1);
-    const float inv2q = pow2f(-q);
-    // source columns come in chunk order (the column map is increasing): chunk ch covers
-    // src_chunk[ch] .. src_chunk[ch+1]
-    for (int ch = 0; ch < a.nchunks; ++ch) {
-    unsigned int dsq[MAX_SLICES];
-#pragma unroll
-    for (int i = 0; i < MAX_SLICES; ++i) dsq[i] = 0u;
-    const int cend = a.src_chunk[ch + 1];
-    for (int c = a.src_chunk[ch] + tid; c < cend; c += SLICE_THREADS) {
-        const unsigned long long bits = src[c];
-        const int dc = a.col_map ? a.col_map[c] : c;
-        const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
-        long long I = 0;
-        if (!zero_row && ab != 0 && ab < 0x7FF0000000000000ull) {
-            const int E = (int)(ab >> 52);
-            unsigned long long mant = ab & 0xFFFFFFFFFFFFFull;
-            int ex;
-            if (E > 0) { mant |= 1ull << 52; ex = E - 1075; }
-            else ex = -1074;
-            const int sh = ex + q - e;
-            const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
-            I = (bits >> 63) ? -(long long)m : (long long)m;
-        }
-        long long v = I;
-        int d[MAX_SLICES];
-#pragma unroll
-        for (int i = MAX_SLICES - 1; i >= 1; --i) {
-            if (i < s) {
-                long r = (long)(v & mask);
-                if (r > halfb) r -= (1l << beta);
-                d[i] = (int)r;
-                v = (v - r) >> beta;
-            } else {
-                d[i] = 0;
+        int nnz = 0;
+        float l2sq = 0.0f;
+        float tsq[MAX_SLICES];
+    #pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i) tsq[i] = 0.0f;
+        const long mask = (1l << beta) - 1l, halfb = 1l << (beta - 1);
+        const float inv2q = pow2f(-q);
+        // source columns come in chunk order (the column map is increasing): chunk ch covers
+        // src_chunk[ch] .. src_chunk[ch+1]
+        for (int ch = 0; ch < a.nchunks; ++ch) {
+        unsigned int dsq[MAX_SLICES];
+    #pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i) dsq[i] = 0u;
+        const int cend = a.src_chunk[ch + 1];
+        for (int c = a.src_chunk[ch] + tid; c < cend; c += SLICE_THREADS) {
+            const unsigned long long bits = src[c];
+            const int dc = a.col_map ? a.col_map[c] : c;
+            const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
+            long long I = 0;
+            if (!zero_row && ab != 0 && ab < 0x7FF0000000000000ull) {
+                const int E = (int)(ab >> 52);
+                unsigned long long mant = ab & 0xFFFFFFFFFFFFFull;
+                int ex;
+                if (E > 0) { mant |= 1ull << 52; ex = E - 1075; }
+                else ex = -1074;
+                const int sh = ex + q - e;
+                const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
+                I = (bits >> 63) ? -(long long)m : (long long)m;
             }
-        }
-        d[0] = (int)v;
-        // tails x^(rounded) - X^(n) = sum_{i>n} d_i 2^{-(i+1) beta}, squared into tsq[n]
-        float tail = 0.0f;
-#pragma unroll
-        for (int i = MAX_SLICES - 1; i >= 1; --i) {
-            if (i < s) {
-                tail = __fadd_rn(tail, (float)d[i] * pow2f(-(i + 1) * beta));
-                tsq[i - 1] = __fmaf_ru(tail, tail, tsq[i - 1]);
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < MAX_SLICES; ++i) {
-            if (i < s) {
-                drow[i * sstride + dc] = __float2bfloat16_rn((float)d[i]);
-                dsq[i] += (unsigned int)(d[i] * d[i]);
-            }
-        }
-        if (I != 0) {
-            ++nnz;
-            const unsigned long long aI = (unsigned long long)(I < 0 ? -I : I);
-            const float xv = __fmul_ru(__ull2float_ru(aI), inv2q);
-            l2sq = __fmaf_ru(xv, xv, l2sq);
-        }
-    }
-    // this chunk's digit sums of squares: warp partials into shared memory
-#pragma unroll
-    for (int i = 0; i < MAX_SLICES; ++i) {
-        for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
-        if ((tid & 31) == 0) red_d[tid >> 5][i * MAX_CHUNKS + ch] = dsq[i];
-    }
-    }
-    // block reductions
-    for (int o = 16; o > 0; o >>= 1) {
-        l2sq = __fadd_ru(l2sq, __shfl_xor_sync(0xffffffffu, l2sq, o));
-        nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
-    }
-#pragma unroll
-    for (int i = 0; i < MAX_SLICES; ++i)
-        for (int o = 16; o > 0; o >>= 1) tsq[i] = __fadd_ru(tsq[i], __shfl_xor_sync(0xffffffffu, tsq[i], o));
-    if ((tid & 31) == 0) {
-        red_f[tid >> 5] = l2sq;
-        red_i[tid >> 5] = nnz;
-#pragma unroll
-        for (int i = 0; i < MAX_SLICES; ++i) red_t[tid >> 5][i] = tsq[i];
-    }
-    __syncthreads();
-    if (tid == 0) {
-        float L2 = 0.0f;
-        int N = 0;
-        for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
-        // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
-        const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
-        const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
-        a.st.e[row] = e;
-        a.st.nnz[row] = N;
-        a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(L2), slack), dq);
-        for (int i = 0; i < MAX_SLICES; ++i) {
-            float tq = 0.0f;
-            unsigned long long dd = 0;
-            if (i < s) {
-                for (int w = 0; w < SLICE_THREADS / 32; ++w) {
-                    tq = __fadd_ru(tq, red_t[w][i]);
-                    for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
+            long long v = I;
+            int d[MAX_SLICES];
+    #pragma unroll
+            for (int i = MAX_SLICES - 1; i >= 1; --i) {
+                if (i < s) {
+                    long r = (long)(v & mask);
+                    if (r > halfb) r -= (1l << beta);
+                    d[i] = (int)r;
+                    v = (v - r) >> beta;
+                } else {
+                    d[i] = 0;
                 }
             }
-            a.st.dnv[(long)row * MAX_SLICES + i] = i < s ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
-            a.st.rnv[(long)row * MAX_SLICES + i] =
-                i < s ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
-        }
-        for (int c = 0; c < a.nchunks; ++c) {
-            unsigned long long m = 0;
-            for (int i = 0; i < s; ++i) {
-                unsigned long long t = 0;
-                for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
-                m = t > m ? t : m;
+            d[0] = (int)v;
+            // tails x^(rounded) - X^(n) = sum_{i>n} d_i 2^{-(i+1) beta}, squared into tsq[n]
+            float tail = 0.0f;
+    #pragma unroll
+            for (int i = MAX_SLICES - 1; i >= 1; --i) {
+                if (i < s) {
+                    tail = __fadd_rn(tail, (float)d[i] * pow2f(-(i + 1) * beta));
+                    tsq[i - 1] = __fmaf_ru(tail, tail, tsq[i - 1]);
+                }
             }
-            a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
-        }
-        if (a.st.inerr) {
-            float v = 0.0f;
-            if (a.inerr2_prev && !zero_row) {
-                const int de = a.e_prev[row] - e;
-                v = __fmul_ru(__fmul_ru(__fsqrt_ru(a.inerr2_prev[row]), 1.0001f), pow2f(max(-126, min(127, de))));
-                if (de > 127) v = __int_as_float(0x7f800000);   // cannot certify: infinite bound
+    #pragma unroll
+            for (int i = 0; i < MAX_SLICES; ++i) {
+                if (i < s) {
+                    drow[i * sstride + dc] = __float2bfloat16_rn((float)d[i]);
+                    dsq[i] += (unsigned int)(d[i] * d[i]);
+                }
             }
-            a.st.inerr[row] = v;
+            if (I != 0) {
+                ++nnz;
+                const unsigned long long aI = (unsigned long long)(I < 0 ? -I : I);
+                const float xv = __fmul_ru(__ull2float_ru(aI), inv2q);
+                l2sq = __fmaf_ru(xv, xv, l2sq);
+            }
         }
+        // this chunk's digit sums of squares: warp partials into shared memory
+    #pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i) {
+            for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
+            if ((tid & 31) == 0) red_d[tid >> 5][i * MAX_CHUNKS + ch] = dsq[i];
+        }
+        }
+        // block reductions
+        for (int o = 16; o > 0; o >>= 1) {
+            l2sq = __fadd_ru(l2sq, __shfl_xor_sync(0xffffffffu, l2sq, o));
+            nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
+        }
+    #pragma unroll
+        for (int i = 0; i < MAX_SLICES; ++i)
+            for (int o = 16; o > 0; o >>= 1) tsq[i] = __fadd_ru(tsq[i], __shfl_xor_sync(0xffffffffu, tsq[i], o));
+        if ((tid & 31) == 0) {
+            red_f[tid >> 5] = l2sq;
+            red_i[tid >> 5] = nnz;
+    #pragma unroll
+            for (int i = 0; i < MAX_SLICES; ++i) red_t[tid >> 5][i] = tsq[i];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            float L2 = 0.0f;
+            int N = 0;
+            for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
+            // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
+            const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
+            const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
+            a.st.e[row] = e;
+            a.st.nnz[row] = N;
+            a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(L2), slack), dq);
+            for (int i = 0; i < MAX_SLICES; ++i) {
+                float tq = 0.0f;
+                unsigned long long dd = 0;
+                if (i < s) {
+                    for (int w = 0; w < SLICE_THREADS / 32; ++w) {
+                        tq = __fadd_ru(tq, red_t[w][i]);
+                        for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
+                    }
+                }
+                a.st.dnv[(long)row * MAX_SLICES + i] = i < s ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
+                a.st.rnv[(long)row * MAX_SLICES + i] =
+                    i < s ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
+            }
+            for (int c = 0; c < a.nchunks; ++c) {
+                unsigned long long m = 0;
+                for (int i = 0; i < s; ++i) {
+                    unsigned long long t = 0;
+                    for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
+                    m = t > m ? t : m;
+                }
+                a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
+            }
+            if (a.st.inerr) {
+                float v = 0.0f;
+                if (a.inerr2_prev && !zero_row) {
+                    const int de = a.e_prev[row] - e;
+                    v = __fmul_ru(__fmul_ru(__fsqrt_ru(a.inerr2_prev[row]), 1.0001f), pow2f(max(-126, min(127, de))));
+                    if (de > 127) v = __int_as_float(0x7f800000);   // cannot certify: infinite bound
+                }
+                a.st.inerr[row] = v;
+            }
+        }
+        __syncthreads();   // the shared reduction buffers are reused by the next row
     }
 }
 
@@ -901,7 +905,8 @@ cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st) {
     if (a.nrows <= 0) return cudaSuccess;
     cudaError_t e = set_attributes_once();
     if (e != cudaSuccess) return e;
-    k_slice<<<a.nrows, SLICE_THREADS, 0, st>>>(a);
+    const int grid = (a.grid_limit > 0 && a.grid_limit < a.nrows) ? a.grid_limit : a.nrows;
+    k_slice<<<grid, SLICE_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -113,6 +113,7 @@ struct SliceArgs {
     RowStats st;
     const float* inerr2_prev;  // optional: squared row error in units of 2^{2 e_prev}
     const int* e_prev;         // exponent those units refer to
+    int grid_limit;            // CTAs at most (0: one per row)
 };
 cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st);
 

@@ -180,6 +180,7 @@ def _declare(L):
                                         _ip, _ip]
     L.gain_upload_dipole.argtypes = [_vp, _dp, I, I, I, I]
     L.gain_upload_eigvecs.argtypes = [_vp, I, I, I, I, _dp]
+    L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
     L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
     L.gain_fetch_amp.argtypes = [_vp, _dp]
@@ -200,7 +201,7 @@ def _declare(L):
     L.gain_plan_pairs.restype = S
     for name in ("gain_hls_kblock", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
-                 "gain_upload_eigvecs", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines"):
         getattr(L, name).restype = S
 
@@ -305,6 +306,12 @@ class Engine:
     def upload_eigvecs(self, jind, gamma, vecs):
         vecs = _f64(vecs)
         check(lib().gain_upload_eigvecs(self.h, jind, gamma, vecs.shape[0], vecs.shape[1], _p(vecs, _dp)))
+
+    def upload_eigvecs_async(self, jind, gamma, vecs):
+        """Queue the copy of page-locked vecs (C-contiguous float64, kept unchanged until the
+        next run_pair returns); pageable arrays are copied synchronously."""
+        assert vecs.dtype == np.float64 and vecs.flags.c_contiguous and vecs.ndim == 2
+        check(lib().gain_upload_eigvecs_async(self.h, jind, gamma, vecs.shape[0], vecs.shape[1], _p(vecs, _dp)))
 
     def run_pair(self, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
                  upper_levels: Sequence[int], path: int = PATH_SPLIT, tol: float = 0.0,

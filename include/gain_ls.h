@@ -127,6 +127,14 @@ gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int st
 gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize,
                                 const double* vecs);
 
+/* As gain_upload_eigvecs, but from page-locked host memory the copy is only queued (on the
+ * engine's copy stream) and the call returns at once; the next gain_run_pair orders every
+ * read of these vectors after the copy, so the upper vectors of a pair stream in while the
+ * lower side is computed.  vecs must stay unchanged until that gain_run_pair returns.  From
+ * pageable memory it is the synchronous upload.  No counterpart in the reference. */
+gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nlevels, int nsize,
+                                      const double* vecs);
+
 typedef enum gain_path {
     GAIN_PATH_PLAIN_FP64 = 0,   /* the reference's method: half_ls per lower state, GEMV */
     GAIN_PATH_SPLIT = 1         /* Ozaki-sliced BF16 tcgen05 GEMMs + FP64 refinement */

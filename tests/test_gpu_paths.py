@@ -151,3 +151,37 @@ def _oracle_amp_block(p, lo, up):
     import threej
     return oracle.run_pair(p, 0, 0, 1, 0, lo, up, threej.threej_table(JMAX), JMAX, oracle.DD, 8,
                            dipole_block=(5, 11))
+
+
+def test_async_eigvec_upload_orders_reads_after_the_copy(built_lib):
+    """Queued uploads from page-locked memory give the synchronous upload's amplitudes on both
+    paths, and a second queued upload (lower vectors doubled) is the one the next run reads."""
+    import torch
+    import gainls
+    import synth
+    p = synth.make_problem(120, [5, 6], "c4", blocks=[(5, 0), (6, 1)])
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    vI, vF = p.blocks[(0, 0)].vecs, p.blocks[(1, 1)].vecs
+    lo, up = list(range(vI.shape[0])), list(range(vF.shape[0]))
+    ref = {}
+    for path in (gainls.PATH_SPLIT, gainls.PATH_PLAIN_FP64):
+        eng.run_pair(0, 0, 1, 1, lo, up, path)
+        ref[path] = eng.fetch_amp().copy()
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = a
+        return t
+
+    hI, hF = pinned(vI), pinned(vF)
+    for path in (gainls.PATH_SPLIT, gainls.PATH_PLAIN_FP64):
+        eng.upload_eigvecs_async(0, 0, hI.numpy())
+        eng.upload_eigvecs_async(1, 1, hF.numpy())
+        eng.run_pair(0, 0, 1, 1, lo, up, path)
+        assert np.array_equal(eng.fetch_amp(), ref[path])
+    hI2 = pinned(2.0 * vI)   # exact scaling: amplitudes double exactly
+    eng.upload_eigvecs_async(0, 0, hI2.numpy())
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    assert np.array_equal(eng.fetch_amp(), 2.0 * ref[gainls.PATH_SPLIT])
+    del eng
