@@ -189,7 +189,7 @@ struct PairLayout {
     std::vector<int> colposF, f_sym, f_prim, band_k0, band_len;
     std::vector<double> f_coef;
     std::vector<std::pair<int, int>> fblocks;   // padded [start, end) of each upper K block
-    DevArray<int> d_colposI, d_i_sym, d_i_prim, d_colposF, d_f_prim, d_band_k0, d_band_len;
+    DevArray<int> d_colposI, d_i_sym, d_i_prim, d_colposF, d_f_sym, d_f_prim, d_band_k0, d_band_len;
     DevArray<double> d_i_coef, d_f_coef, band;
     int beta1 = 0, s1 = 0;
     DevArray<__nv_bfloat16> bandDig;
@@ -551,6 +551,7 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     GAIN_TRY(L.d_i_prim.upload(L.i_prim));
     GAIN_TRY(L.d_i_coef.upload(L.i_coef));
     GAIN_TRY(L.d_colposF.upload(L.colposF));
+    GAIN_TRY(L.d_f_sym.upload(L.f_sym));
     GAIN_TRY(L.d_f_prim.upload(L.f_prim));
     GAIN_TRY(L.d_f_coef.upload(L.f_coef));
     GAIN_TRY(L.d_band_k0.upload(L.band_k0));
@@ -594,9 +595,11 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
 gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows, int nrows, int ncols,
                   const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
                   __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
-                  const float* inerr_prev, const int* e_prev, cudaStream_t st, int grid_limit = 0) {
+                  const float* inerr_prev, const int* e_prev, cudaStream_t st, const int* col_inv = nullptr,
+                  int grid_limit = 0) {
     split::SliceArgs a;
     a.grid_limit = grid_limit;
+    a.col_inv = col_inv;
     const int nkb = kpad / split::BK;
     for (int c = 0; c <= p.chunks; ++c) {
         const int dest0 = c == p.chunks ? kpad : (int)(((long)c * nkb) / p.chunks) * split::BK;
@@ -728,7 +731,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
 
     // ---- lower vectors -> digits in the padded lower layout
     GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI, Bpad,
-                   e->Vdig.p, p1x, e->Vst, false, nullptr, nullptr, st));
+                   e->Vdig.p, p1x, e->Vst, false, nullptr, nullptr, st, L.d_i_sym.p));
     CUtensorMap tmV, tmH, tmU;
     if (!split::make_digit_map(&tmV, e->Vdig.p, L.kpadI, Bpad, p1x.slices))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (lower digits)");
@@ -784,7 +787,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
     if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready, 0));
     GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
-                   e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2));
+                   e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p));
     GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
     // inexact first-GEMM entries recomputed in FP64
     split::RefineHArgs rh;

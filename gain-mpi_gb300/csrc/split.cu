@@ -407,52 +407,43 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             const float* dvA = a.A.dnv + (long)r * MAX_SLICES;
             const float* rvA = a.A.rnv + (long)r * MAX_SLICES;
             const float rlastA = rvA[s - 1];
-            float dnA[CMAX], wA[SMAX], rA[SMAX];
-#pragma unroll
-            for (int c = 0; c < CMAX; ++c) dnA[c] = c < a.nchunks ? a.A.dn[(long)r * a.nchunks + c] : 0.0f;
-            // |running sum| <= 2^kFixTotal SA SB with S = sum_i 2^{-(i+1) beta} ||d_i||: below
-            // 2^62 (SA SB < 2^12) the int64 recombination cannot overflow
-            float sA = 0.0f;
-#pragma unroll
-            for (int i = 0; i < SMAX; ++i) {
-                wA[i] = 0.0f;
-                rA[i] = 0.0f;
-                if (i < s) {
-                    const float dv = dvA[i];
-                    wA[i] = __fmul_ru(pow2f(-(i + 1) * a.beta), dv);
-                    rA[i] = rvA[s - 1 - i];
-                    sA = __fmaf_ru(pow2f(-(i + 1) * a.beta), dv, sA);
-                }
+            // Row terms of the certificates.  The cheap forms need one value per column (all
+            // rounded up):
+            //   exactness   max_c ||d_c(x)|| max_c ||d_c(y)|| < 2^24 implies every chunk's test;
+            //   error       sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)|| <= sigA rhoB with
+            //               sigA = 2^{-(s+1)b} sum_i ||d_i(x)||, rhoB = max_k ||y^ - Y^(k)|| 2^{(k+1)b},
+            // so rlastA l2B + sigA rhoB bounds the first of the two operand orders.  Outputs
+            // that fail a cheap test are checked again with the exact per-chunk and two-order
+            // forms, which read the column's statistics directly.
+            float dnAmax = 0.0f, sA = 0.0f, sumdA = 0.0f;
+            for (int c = 0; c < a.nchunks; ++c) dnAmax = fmaxf(dnAmax, a.A.dn[(long)r * a.nchunks + c]);
+            for (int i = 0; i < s; ++i) {
+                const float dv = dvA[i];
+                // |running sum| <= 2^kFixTotal SA SB, S = sum_i 2^{-(i+1) beta} ||d_i||: below 2^62
+                // (SA SB < 2^12) the int64 recombination cannot overflow
+                sA = __fmaf_ru(pow2f(-(i + 1) * a.beta), dv, sA);
+                sumdA = __fadd_ru(sumdA, dv);
             }
+            const float sigA = __fmul_ru(sumdA, pow2f(-(s + 1) * a.beta));
             const float cf64A = __fmul_ru(a.c_f64, l2A);
             float rowerr2 = 0.0f;
             unsigned long long vmax = 0ull;
             double* orow = a.out + (long)r * a.ldo;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
-                // this lane's column of the group of 32
+                // this lane's column of the group of 32: its five summary values
                 const int mycol = tl.n0 + c * 32 + lane;
                 const int ceB = __ldg(&a.B.e[mycol]);
-                const int cnz = __ldg(&a.B.nnz[mycol]);
-                const float cl2 = __ldg(&a.B.l2[mycol]);
+                const float cl2 = __ldg(&a.B.l2[mycol]);   // 0 exactly for an all-zero column
                 const float* dvB = a.B.dnv + (long)mycol * MAX_SLICES;
                 const float* rvB = a.B.rnv + (long)mycol * MAX_SLICES;
-                const float crl = __ldg(&rvB[s - 1]);
-                float cA[SMAX], cB[SMAX], cdn[CMAX];
-                float csB = 0.0f;
-#pragma unroll
-                for (int i = 0; i < SMAX; ++i) {
-                    cA[i] = 0.0f;
-                    cB[i] = 0.0f;
-                    if (i < s) {
-                        cA[i] = __ldg(&rvB[s - 1 - i]);
-                        cB[i] = __fmul_ru(pow2f(-(i + 1) * a.beta), __ldg(&dvB[i]));
-                        csB = __fadd_ru(csB, cB[i]);
-                    }
+                float crho = 0.0f, csB = 0.0f, cdnmax = 0.0f;
+                for (int k = 0; k < s; ++k) {
+                    crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * a.beta)));
+                    csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * a.beta), __ldg(&dvB[k])));
                 }
-#pragma unroll
-                for (int cc = 0; cc < CMAX; ++cc)
-                    cdn[cc] = cc < a.nchunks ? __ldg(&a.B.dn[(long)mycol * a.nchunks + cc]) : 0.0f;
+                for (int cc = 0; cc < a.nchunks; ++cc)
+                    cdnmax = fmaxf(cdnmax, __ldg(&a.B.dn[(long)mycol * a.nchunks + cc]));
 #pragma unroll 1
                 for (int h = 0; h < 2; ++h) {
                     uint32_t lo_r[16], hi_r[16];
@@ -466,38 +457,43 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int src = h * 16 + j;   // lane holding this column's statistics
+                        const int src = h * 16 + j;   // lane holding this column's values
                         const int col = tl.n0 + c * 32 + src;
                         const long long run = (long long)(((unsigned long long)hi_r[j] << 32) | lo_r[j]);
                         const int eB = __shfl_sync(0xffffffffu, ceB, src);
+                        const float l2B = __shfl_sync(0xffffffffu, cl2, src);
+                        const float rhoB = __shfl_sync(0xffffffffu, crho, src);
+                        const float sB = __shfl_sync(0xffffffffu, csB, src);
+                        const float dnBmax = __shfl_sync(0xffffffffu, cdnmax, src);
                         float av;
                         const unsigned long long vbits = scaled_bits(run, eA + eB - kFixTotal, &av);
                         orow[col] = __longlong_as_double((long long)vbits);
-                        const int nnzB = __shfl_sync(0xffffffffu, cnz, src);
-                        const float l2B = __shfl_sync(0xffffffffu, cl2, src);
-                        bool exact = true;
-#pragma unroll
-                        for (int cc = 0; cc < CMAX; ++cc) {
-                            const float dB = __shfl_sync(0xffffffffu, cdn[cc], src);
-                            if (cc < a.nchunks && __fmul_ru(dnA[cc], dB) >= two24) exact = false;
+                        if (nnzA == 0 || l2B == 0.0f) continue;   // an exact zero
+                        bool exact = __fmul_ru(sA, sB) < 4096.0f;
+                        if (exact && __fmul_ru(dnAmax, dnBmax) >= two24) {
+                            for (int cc = 0; cc < a.nchunks; ++cc)
+                                if (__fmul_ru(a.A.dn[(long)r * a.nchunks + cc],
+                                              __ldg(&a.B.dn[(long)col * a.nchunks + cc])) >= two24)
+                                    exact = false;
                         }
-                        // |x^ y^ - C| <= ||x^ - X|| ||y^|| + sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)||
-                        // and the same with x and y exchanged; the smaller of the two holds.
-                        float bA = __fmul_ru(rlastA, l2B);
-                        float bB = __fmul_ru(__shfl_sync(0xffffffffu, crl, src), l2A);
-#pragma unroll
-                        for (int i = 0; i < SMAX; ++i) {
-                            const float ca = __shfl_sync(0xffffffffu, cA[i], src);
-                            const float cb = __shfl_sync(0xffffffffu, cB[i], src);
-                            if (i < s) {
-                                bA = __fmaf_ru(wA[i], ca, bA);
-                                bB = __fmaf_ru(cb, rA[i], bB);
-                            }
-                        }
-                        if (__fmul_ru(sA, __shfl_sync(0xffffffffu, csB, src)) >= 4096.0f) exact = false;
-                        if (nnzA == 0 || nnzB == 0) continue;
-                        float bound = __fadd_ru(fminf(bA, bB), a.c_fix);
+                        const float f64b = __fmul_ru(cf64A, l2B);
+                        const float limit = a.flag_mode == 1 ? fmaxf(a.tol * av, f64b) : f64b;
+                        float bound = __fadd_ru(__fmaf_ru(rlastA, l2B, __fmul_ru(sigA, rhoB)), a.c_fix);
                         bound = __fmaf_ru(inA, l2B, bound);
+                        if (a.flag_mode != 0 && bound > limit) {
+                            // |x^ y^ - C| <= ||x^ - X|| ||y^|| + sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)||
+                            // and the same with x and y exchanged; the smaller of the two holds
+                            const float* cdv = a.B.dnv + (long)col * MAX_SLICES;
+                            const float* crv = a.B.rnv + (long)col * MAX_SLICES;
+                            float bA = __fmul_ru(rlastA, l2B);
+                            float bB = __fmul_ru(__ldg(&crv[s - 1]), l2A);
+                            for (int i = 0; i < s; ++i) {
+                                const float w = pow2f(-(i + 1) * a.beta);
+                                bA = __fmaf_ru(__fmul_ru(w, dvA[i]), __ldg(&crv[s - 1 - i]), bA);
+                                bB = __fmaf_ru(__fmul_ru(w, __ldg(&cdv[i])), rvA[s - 1 - i], bB);
+                            }
+                            bound = __fmaf_ru(inA, l2B, __fadd_ru(fminf(bA, bB), a.c_fix));
+                        }
                         if (exact && rvalid && col < a.cols_valid) {
                             const unsigned long long vb = vbits & 0x7FFFFFFFFFFFFFFFull;
                             vmax = vb > vmax ? vb : vmax;
@@ -508,10 +504,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         }
                         // certification: flag_mode 1 -> within max(tol |value|, FP64 bound of the
                         // same dot product); flag_mode 2 -> within the FP64 bound (FP64-grade)
-                        bool flag = !exact;
-                        const float f64b = __fmul_ru(cf64A, l2B);
-                        if (a.flag_mode == 1) flag = flag || (bound > fmaxf(a.tol * av, f64b));
-                        else if (a.flag_mode == 2) flag = flag || (bound > f64b);
+                        const bool flag = !exact || (a.flag_mode != 0 && bound > limit);
                         if (flag && rvalid && col < a.cols_valid) {
                             const unsigned int idx = atomicAdd(a.nflags, 1u);
                             if ((int)idx < a.max_flags) a.flags[idx] = make_int2(r, col);
@@ -716,6 +709,183 @@ k_slice(const SliceArgs a) {
     }
 }
 
+// The same digits and row statistics as k_slice for a compile-time slice count S, walking
+// the destination columns four at a time: col_inv gives each destination column's source
+// column (-1: padding, stored as zero digits), each slice's four digits leave as one 8-byte
+// store, and a chunk is a plain range of destination columns (the GEMM's k-block split).
+template <int S>
+__global__ void __launch_bounds__(SLICE_THREADS)
+k_slice4(const SliceArgs a) {
+    const int tid = threadIdx.x;
+    const int nkb = a.kpad / BK;
+    for (int row = blockIdx.x; row < a.nrows; row += gridDim.x) {
+        const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
+        const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
+        __shared__ unsigned long long red_u[SLICE_THREADS / 32];
+        __shared__ float red_f[SLICE_THREADS / 32];
+        __shared__ int red_i[SLICE_THREADS / 32];
+        __shared__ float red_t[SLICE_THREADS / 32][S];
+        __shared__ unsigned int red_d[SLICE_THREADS / 32][S * MAX_CHUNKS];
+
+        // pass 1: max |x| through the IEEE bit pattern (integer compares only)
+        unsigned long long mx = 0;
+#pragma unroll 4
+        for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+            const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
+            mx = b > mx ? b : mx;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+            mx = y > mx ? y : mx;
+        }
+        if ((tid & 31) == 0) red_u[tid >> 5] = mx;
+        __syncthreads();
+        mx = 0;
+        for (int w = 0; w < SLICE_THREADS / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
+        if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
+        const int Emax = (int)(mx >> 52);
+        const bool zero_row = (mx == 0);
+        const int e = zero_row ? 0 : (Emax > 0 ? Emax - 1022 : -1022);
+        const int beta = a.beta;
+        const int q = S * beta;
+        const long sstride = a.slice_stride;
+        __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
+
+        int nnz = 0;
+        float l2sq = 0.0f;
+        float tsq[S];
+#pragma unroll
+        for (int i = 0; i < S; ++i) tsq[i] = 0.0f;
+        const long long mask = (1ll << beta) - 1ll, halfb = 1ll << (beta - 1);
+        const float inv2q = pow2f(-q);
+        for (int ch = 0; ch < a.nchunks; ++ch) {
+            unsigned int dsq[S];
+#pragma unroll
+            for (int i = 0; i < S; ++i) dsq[i] = 0u;
+            const int d0 = (int)(((long)ch * nkb) / a.nchunks) * BK;
+            const int d1 = (int)(((long)(ch + 1) * nkb) / a.nchunks) * BK;
+            for (int dc = d0 + 4 * tid; dc < d1; dc += 4 * SLICE_THREADS) {
+                uint32_t pk[S][2];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int col = dc + u;
+                    const int sc = a.col_inv ? a.col_inv[col] : (col < a.ncols ? col : -1);
+                    const unsigned long long bits = sc >= 0 ? src[sc] : 0ull;
+                    const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
+                    long long I = 0;
+                    if (!zero_row && ab != 0 && ab < 0x7FF0000000000000ull) {
+                        const int E = (int)(ab >> 52);
+                        unsigned long long mant = ab & 0xFFFFFFFFFFFFFull;
+                        int ex;
+                        if (E > 0) { mant |= 1ull << 52; ex = E - 1075; }
+                        else ex = -1074;
+                        const int sh = ex + q - e;
+                        const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
+                        I = (bits >> 63) ? -(long long)m : (long long)m;
+                    }
+                    long long v = I;
+                    int d[S];
+#pragma unroll
+                    for (int i = S - 1; i >= 1; --i) {
+                        long long r = v & mask;
+                        if (r > halfb) r -= (1ll << beta);
+                        d[i] = (int)r;
+                        v = (v - r) >> beta;
+                    }
+                    d[0] = (int)v;
+                    // tails x^(rounded) - X^(n) = sum_{i>n} d_i 2^{-(i+1) beta}, squared into tsq[n]
+                    float tail = 0.0f;
+#pragma unroll
+                    for (int i = S - 1; i >= 1; --i) {
+                        tail = __fadd_rn(tail, (float)d[i] * pow2f(-(i + 1) * beta));
+                        tsq[i - 1] = __fmaf_ru(tail, tail, tsq[i - 1]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < S; ++i) {
+                        dsq[i] += (unsigned int)(d[i] * d[i]);
+                        const uint32_t h16 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)d[i]));
+                        if (u & 1) pk[i][u >> 1] |= h16 << 16;
+                        else pk[i][u >> 1] = h16;
+                    }
+                    if (I != 0) {
+                        ++nnz;
+                        const unsigned long long aI = (unsigned long long)(I < 0 ? -I : I);
+                        const float xv = __fmul_ru(__ull2float_ru(aI), inv2q);
+                        l2sq = __fmaf_ru(xv, xv, l2sq);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < S; ++i)
+                    *reinterpret_cast<uint2*>(drow + i * sstride + dc) = make_uint2(pk[i][0], pk[i][1]);
+            }
+            // this chunk's digit sums of squares: warp partials into shared memory
+#pragma unroll
+            for (int i = 0; i < S; ++i) {
+                for (int o = 16; o > 0; o >>= 1) dsq[i] += __shfl_xor_sync(0xffffffffu, dsq[i], o);
+                if ((tid & 31) == 0) red_d[tid >> 5][i * MAX_CHUNKS + ch] = dsq[i];
+            }
+        }
+        // block reductions
+        for (int o = 16; o > 0; o >>= 1) {
+            l2sq = __fadd_ru(l2sq, __shfl_xor_sync(0xffffffffu, l2sq, o));
+            nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
+        }
+#pragma unroll
+        for (int i = 0; i < S; ++i)
+            for (int o = 16; o > 0; o >>= 1) tsq[i] = __fadd_ru(tsq[i], __shfl_xor_sync(0xffffffffu, tsq[i], o));
+        if ((tid & 31) == 0) {
+            red_f[tid >> 5] = l2sq;
+            red_i[tid >> 5] = nnz;
+#pragma unroll
+            for (int i = 0; i < S; ++i) red_t[tid >> 5][i] = tsq[i];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            float L2 = 0.0f;
+            int N = 0;
+            for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
+            // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
+            const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
+            const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
+            a.st.e[row] = e;
+            a.st.nnz[row] = N;
+            a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(L2), slack), dq);
+            for (int i = 0; i < MAX_SLICES; ++i) {
+                float tq = 0.0f;
+                unsigned long long dd = 0;
+                if (i < S) {
+                    for (int w = 0; w < SLICE_THREADS / 32; ++w) {
+                        tq = __fadd_ru(tq, red_t[w][i]);
+                        for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
+                    }
+                }
+                a.st.dnv[(long)row * MAX_SLICES + i] = i < S ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
+                a.st.rnv[(long)row * MAX_SLICES + i] =
+                    i < S ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
+            }
+            for (int c = 0; c < a.nchunks; ++c) {
+                unsigned long long m = 0;
+                for (int i = 0; i < S; ++i) {
+                    unsigned long long t = 0;
+                    for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
+                    m = t > m ? t : m;
+                }
+                a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
+            }
+            if (a.st.inerr) {
+                float v = 0.0f;
+                if (a.inerr2_prev && !zero_row) {
+                    const int de = a.e_prev[row] - e;
+                    v = __fmul_ru(__fmul_ru(__fsqrt_ru(a.inerr2_prev[row]), 1.0001f), pow2f(max(-126, min(127, de))));
+                    if (de > 127) v = __int_as_float(0x7f800000);   // cannot certify: infinite bound
+                }
+                a.st.inerr[row] = v;
+            }
+        }
+        __syncthreads();   // the shared reduction buffers are reused by the next row
+    }
+}
+
 // ------------------------------------------------------------------- band builder
 __device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
 
@@ -858,6 +1028,9 @@ static cudaError_t set_attributes_once() {
     }
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_slice, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_slice4<6>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_slice4<7>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_slice4<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     done.fetch_or(bit);
     return cudaSuccess;
@@ -906,7 +1079,12 @@ cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st) {
     cudaError_t e = set_attributes_once();
     if (e != cudaSuccess) return e;
     const int grid = (a.grid_limit > 0 && a.grid_limit < a.nrows) ? a.grid_limit : a.nrows;
-    k_slice<<<grid, SLICE_THREADS, 0, st>>>(a);
+    // the four-column kernel needs the destination map (or the identity) and whole k-blocks
+    const bool four = (a.col_inv || !a.col_map) && (a.kpad % BK) == 0;
+    if (four && a.slices == 6) k_slice4<6><<<grid, SLICE_THREADS, 0, st>>>(a);
+    else if (four && a.slices == 7) k_slice4<7><<<grid, SLICE_THREADS, 0, st>>>(a);
+    else if (four && a.slices == 8) k_slice4<8><<<grid, SLICE_THREADS, 0, st>>>(a);
+    else k_slice<<<grid, SLICE_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

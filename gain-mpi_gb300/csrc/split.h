@@ -102,6 +102,8 @@ struct SliceArgs {
     int nrows;              // output rows to produce
     int ncols;              // source columns
     const int* col_map;     // optional destination column per source column
+    const int* col_inv;     // optional source column per destination column (-1: padding);
+                            // with it (or with no map at all) the four-column kernel runs
     int kpad;               // destination row length
     long slice_stride;      // rows_pad * kpad
     __nv_bfloat16* digits;
