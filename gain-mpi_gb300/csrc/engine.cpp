@@ -13,6 +13,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cstdlib>
+
 #include "gain_internal.h"
 #include "split.h"
 
@@ -194,7 +196,7 @@ struct PairLayout {
     int beta1 = 0, s1 = 0;
     DevArray<__nv_bfloat16> bandDig;
     StatsDev bandStats;
-    CUtensorMap tmBand;
+    CUtensorMap tmBand, tmBandPair;   // 128-row boxes; 64-row boxes for a CTA pair
 };
 
 // Plain-path structures of one block pair.
@@ -674,13 +676,20 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         GAIN_TRY(L.bandStats.zero(st, L.fpad, 1, false));
         GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, nullptr, L.W, L.fpad, L.bandDig.p, p1x,
                        L.bandStats, false, nullptr, nullptr, st));
-        if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1x.slices))
+        if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1x.slices) ||
+            !split::make_digit_map(&L.tmBandPair, L.bandDig.p, L.W, L.fpad, p1x.slices, split::BN / 2))
             return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed for the band digits");
         L.beta1 = p1x.beta;
         L.s1 = p1x.slices;
     }
 
-    const int B = j->nlower, Bpad = round_up(B, split::BM);
+    // CTA pairs (256 x 128 tiles) whenever the lower states fill more than one 128-row block;
+    // GAINLS_GEMM_PAIR=0 keeps single-CTA tiles
+    const int B = j->nlower;
+    const char* pair_env = getenv("GAINLS_GEMM_PAIR");
+    const bool pair = B > split::BM && !(pair_env && pair_env[0] == '0');
+    const int mstep = pair ? 2 * split::BM : split::BM;
+    const int Bpad = round_up(B, mstep);
     const int Nu = j->nupper, Nupad = round_up(Nu, split::BN);
     GAIN_TRY(e->d_lower.upload(j->lower_levels, B));
     GAIN_TRY(e->d_upper.upload(j->upper_levels, Nu));
@@ -740,7 +749,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     std::vector<split::Tile> t1;
     for (auto& fb : L.fblocks)
         for (int n0 = fb.first; n0 < fb.second; n0 += split::BN)
-            for (int m0 = 0; m0 < Bpad; m0 += split::BM) {
+            for (int m0 = 0; m0 < Bpad; m0 += mstep) {
                 split::Tile t;
                 memset(&t, 0, sizeof t);
                 t.m0 = m0;
@@ -781,7 +790,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g1.cols_valid = L.fpad;
     g1.err = e->err.p;
     GAIN_CUDA(cudaEventRecord(e->ev[2], st));
-    GAIN_CUDA(split::launch_gemm(tmV, L.tmBand, g1, e->num_sms, st));
+    GAIN_CUDA(split::launch_gemm(tmV, pair ? L.tmBandPair : L.tmBand, g1, e->num_sms, st, pair));
     GAIN_CUDA(cudaEventRecord(e->ev[3], st));
     // ---- upper vectors -> digits on the low-priority second stream
     GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
@@ -813,13 +822,13 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
                    e->Hst, true, e->rowerr.p, e->Vst.e.p, st));
     GAIN_CUDA(cudaStreamWaitEvent(st, e->ev[7], 0));
     if (!split::make_digit_map(&tmH, e->Hdig.p, L.fpad, Bpad, p2.slices) ||
-        !split::make_digit_map(&tmU, e->Udig.p, L.fpad, Nupad, p2.slices))
+        !split::make_digit_map(&tmU, e->Udig.p, L.fpad, Nupad, p2.slices, pair ? split::BN / 2 : split::BM))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (second GEMM digits)");
 
     // ---- GEMM 2: amp = H U^T
     std::vector<split::Tile> t2;
     for (int n0 = 0; n0 < Nupad; n0 += split::BN)
-        for (int m0 = 0; m0 < Bpad; m0 += split::BM) {
+        for (int m0 = 0; m0 < Bpad; m0 += mstep) {
             split::Tile t;
             memset(&t, 0, sizeof t);
             t.m0 = m0;
@@ -859,7 +868,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.cols_valid = Nu;
     g2.err = e->err.p;
     GAIN_CUDA(cudaEventRecord(e->ev[4], st));
-    GAIN_CUDA(split::launch_gemm(tmH, tmU, g2, e->num_sms, st));
+    GAIN_CUDA(split::launch_gemm(tmH, tmU, g2, e->num_sms, st, pair));
     GAIN_CUDA(cudaEventRecord(e->ev[5], st));
     split::RefineAmpArgs ra;
     ra.flags = e->flags2.p;

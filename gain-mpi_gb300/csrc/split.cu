@@ -78,6 +78,55 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         "l"((unsigned long long)map), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
         : "memory");
 }
+// ---- CTA-pair (cta_group::2) forms: the two CTAs of a cluster share each MMA (M = 256)
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_map(uint32_t addr, uint32_t rank) {   // peer's address
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap* map, uint32_t bar_cluster, int c0,
+                                                 int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+        "l"((unsigned long long)map), "r"(bar_cluster), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// arrive on the barrier at this offset in each CTA of mask (bit r = cluster rank r)
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t mask) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(bar), "h"(mask)
+                 : "memory");
+}
 __device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
                  "r"(ncols)
@@ -156,6 +205,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
 // Instruction descriptor: BF16 x BF16 -> F32, A and B K-major, M = BM, N = BN.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                             ((uint32_t)(BM >> 4) << 24);
+// the same for a CTA pair: M = 2 BM rows, each CTA holding BM rows of A and BN/2 rows of B
+constexpr uint32_t kIdescPair = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                ((uint32_t)((2 * BM) >> 4) << 24);
 
 __device__ __forceinline__ float pow2f(int e) {   // exact 2^e for -126 <= e <= 127
     return __int_as_float((e + 127) << 23);
@@ -201,33 +253,45 @@ __device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, in
 
 // ------------------------------------------------------------------- the GEMM kernel
 // SMAX / CMAX: compile-time bounds of the slices and chunks a launch may use (register arrays
-// of the epilogue are sized by them).
-template <int SMAX, int CMAX>
+// of the epilogue are sized by them).  PAIR: the two CTAs of a cluster compute one 256 x 128
+// tile together -- each loads its 128 rows of A and 64 of the 128 rows of B, the first CTA
+// (rank 0) issues the M = 256 MMAs for both, and each CTA's epilogue reads its own TMEM rows.
+// Every shared-memory operand byte then serves twice the MMA work of the single-CTA form.
+template <int SMAX, int CMAX, bool PAIR>
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
              const GemmArgs a) {
+    // stages: single CTA 3 x (32 KB A + 32 KB B); pair 4 x (32 KB A + 16 KB B)
+    constexpr int NST = PAIR ? 4 : STAGES;
+    constexpr uint32_t BOXB = PAIR ? BOX_B / 2 : BOX_B;
+    constexpr uint32_t STB = KSTEP * BOXB;
+    static_assert(NST * (STAGE_A + STB) <= STAGES * (STAGE_A + STAGE_B), "stage ring");
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
-    uint8_t* sB = smem + STAGES * STAGE_A;
-    uint64_t* bars = (uint64_t*)(sB + STAGES * STAGE_B);
+    uint8_t* sB = smem + NST * STAGE_A;
+    uint64_t* bars = (uint64_t*)(sB + NST * STB);
     uint64_t* full = bars;
-    uint64_t* empty = bars + STAGES;
-    uint64_t* accfull = bars + 2 * STAGES;
-    uint64_t* accempty = bars + 2 * STAGES + 2;
-    uint64_t* drain = bars + 2 * STAGES + 4;
-    uint32_t* tmem_holder = (uint32_t*)(bars + 2 * STAGES + 5);
+    uint64_t* empty = bars + NST;
+    uint64_t* accfull = bars + 2 * NST;
+    uint64_t* accempty = bars + 2 * NST + 2;
+    uint64_t* drain = bars + 2 * NST + 4;
+    uint32_t* tmem_holder = (uint32_t*)(bars + 2 * NST + 5);
     volatile int* abort_flag = (volatile int*)(tmem_holder + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = PAIR ? cluster_rank() : 0u;
+    // work unit: a CTA, or a CTA pair (consecutive blocks of a cluster)
+    const int unit = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int nunits = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < NST; ++s) {
             mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_u32(&accfull[b]), 1);
-            mbar_init(smem_u32(&accempty[b]), 128);
+            mbar_init(smem_u32(&accempty[b]), PAIR ? 256 : 128);   // both CTAs' epilogues drain
         }
         mbar_init(smem_u32(drain), 1);
         *abort_flag = 0;
@@ -238,11 +302,16 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
     }
     if (warp == 1) {
-        tmem_alloc(smem_u32(tmem_holder), TMEM_COLS);
-        tmem_relinquish();
+        if (PAIR) {
+            tmem_alloc_pair(smem_u32(tmem_holder), TMEM_COLS);   // both CTAs, same columns
+        } else {
+            tmem_alloc(smem_u32(tmem_holder), TMEM_COLS);
+            tmem_relinquish();
+        }
     }
     tc_fence_before();
-    __syncthreads();
+    if (PAIR) cluster_sync_all();   // the peer's barriers are initialised before any remote use
+    else __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_holder;
 
@@ -252,7 +321,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             uint32_t stage = 0, phase = 0;
             uint32_t issued_mask = 0, last_par = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+            for (int t = unit; t < a.ntiles && ok; t += nunits) {
                 const Tile tl = a.tiles[t];
                 for (int p = 0; p < a.nprods && ok; ++p) {
                     const Prod pr = a.prods[p];
@@ -265,33 +334,53 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             ok = false;
                             break;
                         }
-                        const uint32_t fb = smem_u32(&full[stage]);
-                        mbar_expect_tx(fb, (uint32_t)nk * (BOX_A + BOX_B));
-                        for (int h = 0; h < nk; ++h) {
-                            tma_load_3d(smem_u32(sA + stage * STAGE_A + h * BOX_A), &tmA, fb,
-                                        tl.a_k0 + (kb + h) * BK, tl.m0, pr.ia);
-                            tma_load_3d(smem_u32(sB + stage * STAGE_B + h * BOX_B), &tmB, fb,
-                                        tl.b_k0 + (kb + h) * BK, tl.n0, pr.ib);
+                        if (PAIR) {
+                            // both CTAs' copies complete on the first CTA's barrier, which expects
+                            // the bytes of both
+                            const uint32_t fb = cluster_map(smem_u32(&full[stage]), 0);
+                            if (rank == 0) mbar_expect_tx(smem_u32(&full[stage]), 2u * (uint32_t)nk * (BOX_A + BOXB));
+                            for (int h = 0; h < nk; ++h) {
+                                tma_load_3d_pair(smem_u32(sA + stage * STAGE_A + h * BOX_A), &tmA, fb,
+                                                 tl.a_k0 + (kb + h) * BK, tl.m0 + (int)rank * BM, pr.ia);
+                                tma_load_3d_pair(smem_u32(sB + stage * STB + h * BOXB), &tmB, fb,
+                                                 tl.b_k0 + (kb + h) * BK, tl.n0 + (int)rank * (BN / 2), pr.ib);
+                            }
+                        } else {
+                            const uint32_t fb = smem_u32(&full[stage]);
+                            mbar_expect_tx(fb, (uint32_t)nk * (BOX_A + BOX_B));
+                            for (int h = 0; h < nk; ++h) {
+                                tma_load_3d(smem_u32(sA + stage * STAGE_A + h * BOX_A), &tmA, fb,
+                                            tl.a_k0 + (kb + h) * BK, tl.m0, pr.ia);
+                                tma_load_3d(smem_u32(sB + stage * STB + h * BOXB), &tmB, fb,
+                                            tl.b_k0 + (kb + h) * BK, tl.n0, pr.ib);
+                            }
                         }
                         issued_mask |= 1u << stage;
                         last_par = (last_par & ~(1u << stage)) | (phase << stage);
-                        if (++stage == STAGES) { stage = 0; phase ^= 1; }
+                        if (++stage == NST) { stage = 0; phase ^= 1; }
                     }
                 }
             }
             if (!ok) {
-                // let the copies already issued land before the CTA leaves
-                for (int s = 0; s < STAGES; ++s)
-                    if (issued_mask & (1u << s))
-                        mbar_wait(smem_u32(&full[s]), (last_par >> s) & 1, abort_flag, a.err, 1, true);
+                // let the copies already issued land before the CTA leaves (the second CTA of a
+                // pair cannot observe the first's barrier: it allows them 100 us)
+                if (!PAIR || rank == 0) {
+                    for (int s = 0; s < NST; ++s)
+                        if (issued_mask & (1u << s))
+                            mbar_wait(smem_u32(&full[s]), (last_par >> s) & 1, abort_flag, a.err, 1, true);
+                } else {
+                    const unsigned long long t0 = globaltimer();
+                    while (globaltimer() - t0 < 100000ull) {
+                    }
+                }
             }
         }
     } else if (warp == 1) {
-        // ---------------- MMA issuer (one thread)
-        if (lane == 0) {
+        // ---------------- MMA issuer (one thread; of the first CTA of a pair)
+        if (lane == 0 && rank == 0) {
             uint32_t stage = 0, phase = 0, acc_cnt = 0;
             bool ok = true, any = false;
-            for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+            for (int t = unit; t < a.ntiles && ok; t += nunits) {
                 const Tile tl = a.tiles[t];
                 for (int p = 0; p < a.nprods && ok; ++p) {
                     const Prod pr = a.prods[p];
@@ -313,28 +402,37 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         }
                         tc_fence_after();
                         const uint64_t ad = smem_desc(smem_u32(sA + stage * STAGE_A));
-                        const uint64_t bd = smem_desc(smem_u32(sB + stage * STAGE_B));
+                        const uint64_t bd = smem_desc(smem_u32(sB + stage * STB));
+                        // second k-block of a stage: its boxes start BOX_A / BOXB bytes further
+                        // (descriptor address units of 16 B)
 #pragma unroll
-                        for (int kk = 0; kk < BK / 16; ++kk)
-                            mma_bf16(d, ad + 2 * kk, bd + 2 * kk, kIdesc, (kb > lo || kk > 0) ? 1u : 0u);
-                        if (nk > 1) {
-                            // second k-block of the stage: boxes 16 KB further (descriptor units of 16 B)
+                        for (int h = 0; h < KSTEP; ++h) {
+                            if (h < nk) {
 #pragma unroll
-                            for (int kk = 0; kk < BK / 16; ++kk)
-                                mma_bf16(d, ad + (BOX_A >> 4) + 2 * kk, bd + (BOX_B >> 4) + 2 * kk, kIdesc, 1u);
+                                for (int kk = 0; kk < BK / 16; ++kk) {
+                                    const uint32_t acc = (kb > lo || h > 0 || kk > 0) ? 1u : 0u;
+                                    const uint64_t a2 = ad + h * (BOX_A >> 4) + 2 * kk;
+                                    const uint64_t b2 = bd + h * (BOXB >> 4) + 2 * kk;
+                                    if (PAIR) mma_bf16_pair(d, a2, b2, kIdescPair, acc);
+                                    else mma_bf16(d, a2, b2, kIdesc, acc);
+                                }
+                            }
                         }
                         any = true;
-                        mma_commit(smem_u32(&empty[stage]));
-                        if (++stage == STAGES) { stage = 0; phase ^= 1; }
+                        if (PAIR) mma_commit_pair(smem_u32(&empty[stage]), (uint16_t)3);
+                        else mma_commit(smem_u32(&empty[stage]));
+                        if (++stage == NST) { stage = 0; phase ^= 1; }
                     }
                     if (!ok) break;
-                    mma_commit(smem_u32(&accfull[b]));
+                    if (PAIR) mma_commit_pair(smem_u32(&accfull[b]), (uint16_t)3);
+                    else mma_commit(smem_u32(&accfull[b]));
                     ++acc_cnt;
                 }
             }
             if (any) {
-                // all MMAs of this CTA complete before TMEM is released
-                mma_commit(smem_u32(drain));
+                // all MMAs of this CTA (pair) complete before TMEM is released
+                if (PAIR) mma_commit_pair(smem_u32(drain), (uint16_t)1);
+                else mma_commit(smem_u32(drain));
                 mbar_wait(smem_u32(drain), 0, abort_flag, a.err, 4, true);
             }
         }
@@ -351,7 +449,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const int s = a.slices;
         uint32_t acc_cnt = 0;
         bool ok = true;
-        for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+        for (int t = unit; t < a.ntiles && ok; t += nunits) {
             const Tile tl = a.tiles[t];
             bool first = true;
             for (int p = 0; p < a.nprods && ok; ++p) {
@@ -390,7 +488,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 }
                 tmem_wait_st();
                 tc_fence_before();
-                mbar_arrive(smem_u32(&accempty[b]));
+                if (PAIR && rank != 0) mbar_arrive_cluster(cluster_map(smem_u32(&accempty[b]), 0));
+                else mbar_arrive(smem_u32(&accempty[b]));
                 ++acc_cnt;
                 first = false;
             }
@@ -398,7 +497,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags.
             // Row terms live in registers; the statistics of 32 columns at a time are read one
             // column per lane and broadcast with shuffles (no shared memory, no cross-warp sync).
-            const int r = tl.m0 + row_in_tile;
+            const int r = tl.m0 + (int)rank * BM + row_in_tile;
             const bool rvalid = r < a.rows_valid;
             const int eA = a.A.e[r];
             const int nnzA = a.A.nnz[r];
@@ -519,10 +618,14 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         }
     }
     tc_fence_before();
-    __syncthreads();
+    // a pair stays together until the first CTA's MMAs (which read the second's shared memory
+    // and write its TMEM) have drained
+    if (PAIR) cluster_sync_all();
+    else __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem, TMEM_COLS);
+        if (PAIR) tmem_dealloc_pair(tmem, TMEM_COLS);
+        else tmem_dealloc(tmem, TMEM_COLS);
     }
 }
 
@@ -1001,18 +1104,19 @@ size_t gemm_smem_bytes() {
     return (size_t)STAGES * (STAGE_A + STAGE_B) + 1024 /* align slack */ + 256 /* barriers */;
 }
 
-// Kernel instances by (max slices, max chunks): the two common configurations (first GEMM:
-// up to 8 slices in one chunk; second GEMM: up to 6 slices in up to 8 chunks) and a general one.
+// Kernel instances by (max slices, max chunks, pair): the two common configurations (first
+// GEMM: up to 8 slices in one chunk; second GEMM: up to 6 slices in up to 8 chunks) and a
+// general one, each as a single CTA and as a CTA pair.
 typedef void (*GemmKernel)(const CUtensorMap, const CUtensorMap, const GemmArgs);
-static GemmKernel gemm_kernel_for(int slices, int chunks) {
-    if (slices <= 8 && chunks <= 1) return k_digit_gemm<8, 1>;
-    if (slices <= 6 && chunks <= MAX_CHUNKS) return k_digit_gemm<6, MAX_CHUNKS>;
-    return k_digit_gemm<MAX_SLICES, MAX_CHUNKS>;
+static GemmKernel gemm_kernel_for(int slices, int chunks, bool pair) {
+    if (slices <= 8 && chunks <= 1) return pair ? k_digit_gemm<8, 1, true> : k_digit_gemm<8, 1, false>;
+    if (slices <= 6 && chunks <= MAX_CHUNKS)
+        return pair ? k_digit_gemm<6, MAX_CHUNKS, true> : k_digit_gemm<6, MAX_CHUNKS, false>;
+    return pair ? k_digit_gemm<MAX_SLICES, MAX_CHUNKS, true> : k_digit_gemm<MAX_SLICES, MAX_CHUNKS, false>;
 }
 
 // Function attributes are per device: set them once on each device that launches.
-// All kernels ask for the largest shared-memory carveout, so that slicing CTAs can share
-// an SM with a resident GEMM CTA (an SM runs one L1/shared split at a time).
+// All kernels ask for the largest shared-memory carveout.
 static cudaError_t set_attributes_once() {
     static std::atomic<unsigned long long> done{0};   // bit per device ordinal (< 64)
     int dev = 0;
@@ -1020,7 +1124,9 @@ static cudaError_t set_attributes_once() {
     if (e != cudaSuccess) return e;
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load() & bit) return cudaSuccess;
-    const GemmKernel ks[3] = {k_digit_gemm<8, 1>, k_digit_gemm<6, MAX_CHUNKS>, k_digit_gemm<MAX_SLICES, MAX_CHUNKS>};
+    const GemmKernel ks[6] = {k_digit_gemm<8, 1, false>,          k_digit_gemm<6, MAX_CHUNKS, false>,
+                              k_digit_gemm<MAX_SLICES, MAX_CHUNKS, false>, k_digit_gemm<8, 1, true>,
+                              k_digit_gemm<6, MAX_CHUNKS, true>,   k_digit_gemm<MAX_SLICES, MAX_CHUNKS, true>};
     for (GemmKernel k : ks) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
@@ -1036,17 +1142,35 @@ static cudaError_t set_attributes_once() {
     return cudaSuccess;
 }
 
-cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a,
-                        int num_sms, cudaStream_t st) {
+cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a, int num_sms,
+                        cudaStream_t st, bool pair) {
     const size_t smem = gemm_smem_bytes();
     cudaError_t e = set_attributes_once();
     if (e != cudaSuccess) return e;
     if (a.ntiles <= 0) return cudaSuccess;
     if (a.slices < 1 || a.slices > MAX_SLICES || a.nchunks < 1 || a.nchunks > MAX_CHUNKS)
         return cudaErrorInvalidValue;
-    const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
-    gemm_kernel_for(a.slices, a.nchunks)<<<grid, NTHREADS, smem, st>>>(tmA, tmB, a);
-    return cudaGetLastError();
+    GemmKernel k = gemm_kernel_for(a.slices, a.nchunks, pair);
+    if (!pair) {
+        const int grid = a.ntiles < num_sms ? a.ntiles : num_sms;
+        k<<<grid, NTHREADS, smem, st>>>(tmA, tmB, a);
+        return cudaGetLastError();
+    }
+    // pairs of CTAs (clusters of two), one pair per tile at most
+    const int pairs = a.ntiles < num_sms / 2 ? a.ntiles : num_sms / 2;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(2 * pairs));
+    cfg.blockDim = dim3(NTHREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, tmA, tmB, a);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -1054,7 +1178,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices) {
+bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices, int box_rows) {
     static EncodeTiledFn fn = nullptr;
     if (!fn) {
         void* p = nullptr;
@@ -1067,7 +1191,8 @@ bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int sl
     if (((uintptr_t)base & 15) || (kpad % BK) || (rows_pad % BM)) return false;
     cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)slices};
     cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)kpad * 2 * (cuuint64_t)rows_pad};
-    cuuint32_t box[3] = {BK, BM, 1};
+    if (box_rows != BM && box_rows != BN / 2) return false;
+    cuuint32_t box[3] = {BK, (cuuint32_t)box_rows, 1};
     cuuint32_t es[3] = {1, 1, 1};
     return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,

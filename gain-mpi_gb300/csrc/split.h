@@ -89,11 +89,14 @@ struct GemmArgs {
 };
 
 size_t gemm_smem_bytes();
+// pair: CTA pairs computing 256 x 128 tiles (tile m0 multiples of 256, rows padded to 256;
+// the B operand's map with 64-row boxes)
 cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a,
-                        int num_sms, cudaStream_t st);
+                        int num_sms, cudaStream_t st, bool pair);
 
-// Tensor map of a digit array [slices][rows_pad][kpad] BF16 (box 64 x 128 x 1, 128B swizzle).
-bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices);
+// Tensor map of a digit array [slices][rows_pad][kpad] BF16 (box 64 x box_rows x 1, 128B
+// swizzle; box_rows 128, or 64 for the B operand of a CTA pair).
+bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices, int box_rows = BM);
 
 struct SliceArgs {
     const double* src;      // source rows
