@@ -261,15 +261,18 @@ template <int SMAX, int CMAX, bool PAIR>
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
              const GemmArgs a) {
-    // stages: single CTA 3 x (32 KB A + 32 KB B); pair 4 x (32 KB A + 16 KB B)
-    constexpr int NST = PAIR ? 4 : STAGES;
+    // stages: single CTA 3 x 2 k-blocks (32 KB A + 32 KB B); pair 3 x 3 k-blocks (48 KB A +
+    // 24 KB B), i.e. one barrier wait per 8 (single) or 12 (pair) MMAs
+    constexpr int KS = PAIR ? 3 : KSTEP;
+    constexpr int NST = STAGES;
     constexpr uint32_t BOXB = PAIR ? BOX_B / 2 : BOX_B;
-    constexpr uint32_t STB = KSTEP * BOXB;
-    static_assert(NST * (STAGE_A + STB) <= STAGES * (STAGE_A + STAGE_B), "stage ring");
+    constexpr uint32_t STA = KS * BOX_A;
+    constexpr uint32_t STB = KS * BOXB;
+    static_assert(NST * (STA + STB) + 1024 + 256 <= 227 * 1024, "stage ring");
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
-    uint8_t* sB = smem + NST * STAGE_A;
+    uint8_t* sB = smem + NST * STA;
     uint64_t* bars = (uint64_t*)(sB + NST * STB);
     uint64_t* full = bars;
     uint64_t* empty = bars + NST;
@@ -327,9 +330,9 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     const Prod pr = a.prods[p];
                     int lo, hi;
                     chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
-                    // one stage holds up to KSTEP consecutive k-blocks of the pass
-                    for (int kb = lo; kb < hi; kb += KSTEP) {
-                        const int nk = hi - kb < KSTEP ? hi - kb : KSTEP;
+                    // one stage holds up to KS consecutive k-blocks of the pass
+                    for (int kb = lo; kb < hi; kb += KS) {
+                        const int nk = hi - kb < KS ? hi - kb : KS;
                         if (!mbar_wait(smem_u32(&empty[stage]), phase ^ 1, abort_flag, a.err, 1)) {
                             ok = false;
                             break;
@@ -340,7 +343,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const uint32_t fb = cluster_map(smem_u32(&full[stage]), 0);
                             if (rank == 0) mbar_expect_tx(smem_u32(&full[stage]), 2u * (uint32_t)nk * (BOX_A + BOXB));
                             for (int h = 0; h < nk; ++h) {
-                                tma_load_3d_pair(smem_u32(sA + stage * STAGE_A + h * BOX_A), &tmA, fb,
+                                tma_load_3d_pair(smem_u32(sA + stage * STA + h * BOX_A), &tmA, fb,
                                                  tl.a_k0 + (kb + h) * BK, tl.m0 + (int)rank * BM, pr.ia);
                                 tma_load_3d_pair(smem_u32(sB + stage * STB + h * BOXB), &tmB, fb,
                                                  tl.b_k0 + (kb + h) * BK, tl.n0 + (int)rank * (BN / 2), pr.ib);
@@ -349,7 +352,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const uint32_t fb = smem_u32(&full[stage]);
                             mbar_expect_tx(fb, (uint32_t)nk * (BOX_A + BOX_B));
                             for (int h = 0; h < nk; ++h) {
-                                tma_load_3d(smem_u32(sA + stage * STAGE_A + h * BOX_A), &tmA, fb,
+                                tma_load_3d(smem_u32(sA + stage * STA + h * BOX_A), &tmA, fb,
                                             tl.a_k0 + (kb + h) * BK, tl.m0, pr.ia);
                                 tma_load_3d(smem_u32(sB + stage * STB + h * BOXB), &tmB, fb,
                                             tl.b_k0 + (kb + h) * BK, tl.n0, pr.ib);
@@ -394,19 +397,19 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
                     tc_fence_after();
                     const uint32_t d = tmem + b * BN;
-                    for (int kb = lo; kb < hi; kb += KSTEP) {
-                        const int nk = hi - kb < KSTEP ? hi - kb : KSTEP;
+                    for (int kb = lo; kb < hi; kb += KS) {
+                        const int nk = hi - kb < KS ? hi - kb : KS;
                         if (!mbar_wait(smem_u32(&full[stage]), phase, abort_flag, a.err, 3)) {
                             ok = false;
                             break;
                         }
                         tc_fence_after();
-                        const uint64_t ad = smem_desc(smem_u32(sA + stage * STAGE_A));
+                        const uint64_t ad = smem_desc(smem_u32(sA + stage * STA));
                         const uint64_t bd = smem_desc(smem_u32(sB + stage * STB));
                         // second k-block of a stage: its boxes start BOX_A / BOXB bytes further
                         // (descriptor address units of 16 B)
 #pragma unroll
-                        for (int h = 0; h < KSTEP; ++h) {
+                        for (int h = 0; h < KS; ++h) {
                             if (h < nk) {
 #pragma unroll
                                 for (int kk = 0; kk < BK / 16; ++kk) {
@@ -1100,8 +1103,8 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
 
 }  // namespace
 
-size_t gemm_smem_bytes() {
-    return (size_t)STAGES * (STAGE_A + STAGE_B) + 1024 /* align slack */ + 256 /* barriers */;
+size_t gemm_smem_bytes() {   // the larger of the two stage rings (the pair's three 72 KB stages)
+    return (size_t)STAGES * 3 * (BOX_A + BOX_B / 2) + 1024 /* align slack */ + 256 /* barriers */;
 }
 
 // Kernel instances by (max slices, max chunks, pair): the two common configurations (first
