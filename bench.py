@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--small", action="store_true", help="reduced sizes (development only)")
     ap.add_argument("--lower", type=int, default=0,
                     help="number of lower states (profiling captures; default: the workload's 2000)")
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="accuracy of each digit configuration of the amplitude GEMM against the "
+                         "double-double oracle (one JSON line per configuration)")
     return ap.parse_args()
 
 
@@ -225,6 +228,73 @@ def cpu_baseline(inp, n_sample: int):
                       f"({n} transitions, {secs:.1f} s)"}
 
 
+def precision_sweep(args):
+    """Digit configurations of the amplitude GEMM (8-bit digits x 3..7 slices, 7-bit x 5..7) on
+    the workload: time, refinement counts, and the relative error of S = amp^2 for lines with
+    S > 1e-10 S_max against (a) the double-double oracle on a sample of lower states and (b) the
+    plain FP64 path on all transitions.  One JSON line per configuration, then a summary."""
+    import torch
+    torch.cuda.set_device(0)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gainls
+    import oracle
+    import synth
+    import threej
+    oracle.build()
+    inp = make_inputs(args.small, 0, "cuda", n_lower_override=args.lower)
+    eng = setup_engine(inp, 0)
+    B, NU = inp["vl"].shape[0], inp["vu"].shape[0]
+    lo, up = list(range(B)), list(range(NU))
+    sample = list(range(0, B, max(1, B // 8)))[:8]
+    p = synth.Problem(inp["nv"], [JI, JF], "c4", 4, np.ones(4, np.int32), synth.selection_of("c4"),
+                      synth.igamma_pair_of(synth.selection_of("c4")), inp["bases"], inp["infl"],
+                      [synth.classes_of(b, "c4") for b in inp["bases"]], inp["dipole"],
+                      {(0, GI): synth.Block(JI, 0, GI, inp["vl"][sample], inp["eI"][sample]),
+                       (1, GF): synth.Block(JF, 1, GF, inp["vu"], inp["eF"])})
+    t0 = time.perf_counter()
+    dd = oracle.run_pair(p, 0, GI, 1, GF, list(range(len(sample))), up, threej.threej_table(11), 11, oracle.DD,
+                         os.cpu_count() or 1)
+    dd_secs = time.perf_counter() - t0
+    Sdd = dd ** 2
+    mdd = Sdd > 1e-10 * Sdd.max()
+
+    def err(S, Sr, m):
+        r = np.abs(S[m] - Sr[m]) / Sr[m]
+        return float(r.max()), float(np.quantile(r, 0.99))
+
+    sp = eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_PLAIN_FP64)
+    plain = eng.fetch_amp().copy()
+    Sp = plain ** 2
+    mp = Sp > 1e-10 * Sp.max()
+    e_plain = err(Sp[sample], Sdd, mdd)
+    print(json.dumps({"config": "plain FP64 path", "ms": sp["device_ms"],
+                      "max_rel_err_S_vs_dd": e_plain[0], "p99_rel_err_S_vs_dd": e_plain[1]}), flush=True)
+    best = None
+    for beta, slices in [(8, 3), (8, 4), (8, 5), (8, 6), (8, 7), (7, 5), (7, 6), (7, 7)]:
+        eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT, beta=beta, slices=slices, raise_on_error=False)
+        st = eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT, beta=beta, slices=slices, raise_on_error=False)
+        amp = eng.fetch_amp()
+        S = amp ** 2
+        e_dd = err(S[sample], Sdd, mdd)
+        e_fp = err(S, Sp, mp)
+        nprod = st["slices2"] * (st["slices2"] + 1) // 2
+        row = {"config": f"beta={st['beta2']} x{st['slices2']} ({st['slices2'] * beta} bits), "
+                         f"{nprod} digit products x {st['chunks2']} chunks",
+               "status": ["OK", "INVALID_ARG", "OOM", "CUDA", "TIMEOUT", "TOL_NOT_MET", "NOT_READY",
+                          "UNSUPPORTED"][st["status"]],
+               "ms": st["device_ms"], "gemm2_ms": st["gemm2_ms"], "refined": st["refined"],
+               "uncertified": st["uncertified"], "max_rel_err_S_vs_dd": e_dd[0], "p99_rel_err_S_vs_dd": e_dd[1],
+               "max_rel_err_S_vs_fp64": e_fp[0], "p99_rel_err_S_vs_fp64": e_fp[1]}
+        print(json.dumps(row), flush=True)
+        if beta == 8 and st["status"] == gainls.OK and e_dd[0] <= 1e-8 and best is None:
+            best = slices
+    print(json.dumps({"summary": "smallest 8-bit slice count meeting S rel-err <= 1e-8 against the "
+                                 "double-double oracle (sampled lower states), with certification",
+                      "slices": best, "oracle_sample": f"{len(sample)} lower x {NU} upper states "
+                      f"({dd_secs:.1f} s on {os.cpu_count()} cores)",
+                      "domain": "S > 1e-10 S_max"}), flush=True)
+
+
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
@@ -251,6 +321,8 @@ def reference_arm(args, ws, rank):
 def main():
     args = parse()
     ws, rank, local = dist_info()
+    if args.precision_sweep:
+        return precision_sweep(args)
     if args.impl == "reference":
         if ws > 1 and rank != 0:
             return
