@@ -985,6 +985,23 @@ gain_status gain_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF, cons
     return GAIN_OK;
 }
 
+gain_status gain_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int sym_max_degen, const int* kI,
+                            const int* kF, const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF,
+                            int startFblock, int endFblock, int ncontrF, const double* dipole_me, const double* wigner,
+                            const double* vector, double* half_ls, int dip_stride, void* stream) {
+    clear_error();
+    if (dimenF < 0 || dimenI < 0 || nlevelI <= 0 || nlevelF <= 0 || sym_max_degen <= 0 || ncontrF <= 0 ||
+        dip_stride <= 0 || startFblock < 0 || endFblock < startFblock)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_hls_rotsym: inconsistent sizes");
+    if (dimenF > 0 && (!kI || !kF || !ktauI || !ktauF || !icorrI || !icorrF || !dipole_me || !wigner ||
+                       !vector || !half_ls))
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_hls_rotsym: NULL pointer");
+    GAIN_CUDA(launch_hls_rotsym(dimenF, dimenI, nlevelI, nlevelF, sym_max_degen, kI, kF, ktauI, ktauF, icorrI,
+                                icorrF, startFblock, endFblock, ncontrF, dipole_me, dip_stride, wigner, vector,
+                                half_ls, (cudaStream_t)stream));
+    return GAIN_OK;
+}
+
 gain_status gain_expand(int dimenI, int igammaI, int maxcoeff, int idegI, int sdeg, int Ntot,
                         const int* ijterms, const int* icontr, const int* N, const double* repres,
                         const double* vecI, double* vec, void* stream) {

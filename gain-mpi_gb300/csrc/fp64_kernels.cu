@@ -342,6 +342,72 @@ cudaError_t launch_expand(int dimen, int igamma, int maxcoeff, int ideg, int sde
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------
+// Rotational-symmetry (Euler) half line strength, the drop-in for
+// device_compute_1st_half_ls_flipped_dipole_shared_rotsym_nontrove (GPU/dipole_GPU.cu:641-723):
+// one thread per upper primitive F in the dipole block, summing over every lower primitive
+// I in ascending order; per I the three components enter as fma(w0, mu0, w1 mu1), then
+// fma(w2, mu2, .), accumulated with one fused multiply-add -- the reference's own order,
+// so the values are bit-identical.  In this form K holds the degeneracy index and ktau the
+// rotational level index of each primitive.
+constexpr int kRotTile = 128;
+
+__global__ void __launch_bounds__(kRotTile)
+k_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* __restrict__ kI,
+             const int* __restrict__ kF, const int* __restrict__ ktauI, const int* __restrict__ ktauF,
+             const int* __restrict__ icorrI, const int* __restrict__ icorrF, int startFblock, int endFblock,
+             int ncontrF, const double* __restrict__ dipole_me, long dstride, const double* __restrict__ wigner,
+             const double* __restrict__ vector, double* __restrict__ half_ls) {
+    __shared__ double s_v[kRotTile];
+    __shared__ long s_ic[kRotTile];
+    __shared__ int s_lv[kRotTile], s_dg[kRotTile];
+    const int t = threadIdx.x;
+    const int f = blockIdx.x * kRotTile + t;
+    bool valid = f < dimenF;
+    long icF = 0, wF = 0;
+    if (valid) {
+        const int c = icorrF[f];
+        valid = c >= startFblock && c < endFblock;
+        icF = c - startFblock;
+        wF = (long)ktauF[f] * nlevelI * 3 + (long)kF[f] * maxdeg * nlevelI * nlevelF * 3;
+    }
+    const long wdeg = (long)nlevelI * nlevelF * 3;
+    double acc = 0.0;
+    for (int b = 0; b < dimenI; b += kRotTile) {
+        const int i = b + t;
+        if (i < dimenI) {
+            s_ic[t] = (long)icorrI[i] * ncontrF;
+            s_lv[t] = ktauI[i];
+            s_dg[t] = kI[i];
+            s_v[t] = vector[i];
+        }
+        __syncthreads();
+        const int n = min(kRotTile, dimenI - b);
+        if (valid) {
+            for (int j = 0; j < n; ++j) {
+                const long d = icF + s_ic[j];
+                const double mu0 = dipole_me[d], mu1 = dipole_me[d + dstride], mu2 = dipole_me[d + 2 * dstride];
+                const long w = (long)s_lv[j] * 3 + wF + (long)s_dg[j] * wdeg;
+                const double tt = __fma_rn(wigner[w + 2], mu2, __fma_rn(wigner[w], mu0, __dmul_rn(wigner[w + 1], mu1)));
+                acc = __fma_rn(s_v[j], tt, acc);
+            }
+        }
+        __syncthreads();
+    }
+    if (valid) half_ls[f] = acc;
+}
+
+cudaError_t launch_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI,
+                              const int* kF, const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF,
+                              int startFblock, int endFblock, int ncontrF, const double* dipole_me, int dip_stride,
+                              const double* wigner, const double* vector, double* half_ls, cudaStream_t st) {
+    if (dimenF <= 0) return cudaSuccess;
+    k_hls_rotsym<<<(dimenF + kRotTile - 1) / kRotTile, kRotTile, 0, st>>>(
+        dimenF, dimenI, nlevelI, nlevelF, maxdeg, kI, kF, ktauI, ktauF, icorrI, icorrF, startFblock, endFblock,
+        ncontrF, dipole_me, (long)ncontrF * dip_stride, wigner, vector, half_ls);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_dot(int n, const double* x, const double* y, double* result, cudaStream_t st) {
     k_dot<<<1, 1024, 0, st>>>(n, x, y, result);
     return cudaGetLastError();

@@ -43,6 +43,10 @@ cudaError_t launch_expand(int dimen, int igamma, int maxcoeff, int ideg, int sde
                           const int* ijterms, const int* icontr, const int* N,
                           const double* repres, const double* vecI, double* vec, cudaStream_t st);
 cudaError_t launch_dot(int n, const double* x, const double* y, double* result, cudaStream_t st);
+cudaError_t launch_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI,
+                              const int* kF, const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF,
+                              int startFblock, int endFblock, int ncontrF, const double* dipole_me, int dip_stride,
+                              const double* wigner, const double* vector, double* half_ls, cudaStream_t st);
 
 // Plain FP64 path: one CTA table entry covers up to kHlsTile upper functions of one K block.
 struct HlsCta {

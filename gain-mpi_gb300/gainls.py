@@ -171,6 +171,7 @@ def _declare(L):
     L.gain_hls_kblock.argtypes = [I, I, I, I, I, _vp, _vp, _vp, _vp, I, I, I, I, I, I, _vp, _vp, _vp,
                                   _vp, _vp, I, I, _vp]
     L.gain_expand.argtypes = [I, I, I, I, I, I, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
+    L.gain_hls_rotsym.argtypes = [I, I, I, I, I, _vp, _vp, _vp, _vp, _vp, _vp, I, I, I, _vp, _vp, _vp, _vp, I, _vp]
     L.gain_dot.argtypes = [I, _vp, _vp, _vp, _vp]
     L.gain_threej_table.argtypes = [I, _dp]
     L.gain_engine_create.argtypes = [I, I, I, I, ctypes.POINTER(_vp)]
@@ -199,7 +200,7 @@ def _declare(L):
     L.gain_transition_details.restype = S
     L.gain_plan_pairs.argtypes = [FP, SP, I, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong), _ip]
     L.gain_plan_pairs.restype = S
-    for name in ("gain_hls_kblock", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
+    for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines"):
@@ -250,6 +251,14 @@ def hls_kblock(dimenF, dimenI, jI, jF, kF, tauI, tauF, icorrI, icorrF, startF_id
 def expand(dimenI, igammaI, maxcoeff, idegI, sdeg, Ntot, ijterms, icontr, N, repres, vecI, vec, stream=0):
     check(lib().gain_expand(dimenI, igammaI, maxcoeff, idegI, sdeg, Ntot, ijterms, icontr, N, repres,
                             vecI, vec, stream))
+
+
+def hls_rotsym(dimenF, dimenI, nlevelI, nlevelF, sym_max_degen, kI, kF, ktauI, ktauF, icorrI, icorrF,
+               startFblock, endFblock, ncontrF, dipole_me, wigner, vector, half_ls, dip_stride, stream=0):
+    """gain_hls_rotsym on device pointers (ints)."""
+    check(lib().gain_hls_rotsym(dimenF, dimenI, nlevelI, nlevelF, sym_max_degen, kI, kF, ktauI, ktauF, icorrI,
+                                icorrF, startFblock, endFblock, ncontrF, dipole_me, wigner, vector, half_ls,
+                                dip_stride, stream))
 
 
 def dot(n, x, y, result, stream=0):

@@ -72,21 +72,52 @@ def make_basis(J: int, nv: int) -> Basis:
                  kstart, kblock)
 
 
+def make_rotsym_basis(J: int, nv: int, maxdeg: int = 1) -> Basis:
+    """Primitive basis of the rotational-symmetry (Euler) form: each function is a symmetrised
+    rotational level (2J+1 levels, each with maxdeg degenerate components) times a vibrational
+    function.  The fields follow the reference's rotsym use of the basis arrays
+    (TroveClasses/TroveBasisSet.cpp:480-483): K holds the degeneracy index, tau the level
+    index.  Order: vibrational index slowest, so the functions are not K-sorted."""
+    nlev = 2 * J + 1
+    v, lev, deg = np.meshgrid(np.arange(nv), np.arange(nlev), np.arange(maxdeg), indexing="ij")
+    K = deg.reshape(-1).astype(np.int32)
+    tau = lev.reshape(-1).astype(np.int32)
+    vib = v.reshape(-1).astype(np.int32)
+    return Basis(J, nv, K, tau, vib, np.zeros(J + 1, np.int32), np.zeros(J + 1, np.int32))
+
+
+def rotsym_levels(J: int) -> int:
+    return 2 * J + 1
+
+
+def make_wigner(JI: int, JF: int, maxdeg: int = 1) -> np.ndarray:
+    """Rotational matrix elements of the three dipole components between the symmetrised
+    levels of J'' and J' (synthetic, seeded): rot[d + 3 (lI + nI (lF + nF (dI + maxdeg dF)))],
+    the layout of GpuManager::TransferWigner (BaseClasses/GpuManager.cpp:457) and of the
+    rotsym kernel's index (GPU/dipole_GPU.cu:692)."""
+    nI, nF = rotsym_levels(JI), rotsym_levels(JF)
+    rng = np.random.default_rng(7000 + 100 * JI + JF)
+    return (0.5 * rng.uniform(-1.0, 1.0, 3 * nI * nF * maxdeg * maxdeg)).astype(np.float64)
+
+
 def classes_of(basis: Basis, rule: str) -> np.ndarray:
     if rule == "full":
         return np.zeros(basis.dimen, np.int32)
     if rule == "c4":
         return (2 * (basis.vib % 2) + ((basis.K + basis.tau) % 2)).astype(np.int32)
+    if rule == "c4r":   # rotsym basis: level index in place of K + tau
+        return (2 * (basis.vib % 2) + (basis.tau % 2)).astype(np.int32)
     raise ValueError(f"unknown symmetry rule {rule!r}")
 
 
 def nsym_of(rule: str) -> int:
-    return {"full": 1, "c4": 4}[rule]
+    return {"full": 1, "c4": 4, "c4r": 4}[rule]
 
 
 def selection_of(rule: str) -> np.ndarray:
     """isym_pairs: classes with equal entries pair up (SELECTION keyword)."""
-    return {"full": np.array([1], np.int32), "c4": np.array([1, 1, 2, 2], np.int32)}[rule]
+    return {"full": np.array([1], np.int32), "c4": np.array([1, 1, 2, 2], np.int32),
+            "c4r": np.array([1, 1, 2, 2], np.int32)}[rule]
 
 
 def igamma_pair_of(isym_pairs: np.ndarray) -> np.ndarray:

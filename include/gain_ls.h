@@ -59,6 +59,22 @@ gain_status gain_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF,
                             const double* dipole_me, const double* vector, const double* threej,
                             double* half_ls, int jmax, int dip_stride, void* stream);
 
+/* Rotational-symmetry (Euler) half line strength of one lower vector.
+ * Replaces compute_gpu_half_linestrength_rotsym_ (GPU/dipole_GPU.h:38-41, GPU/dipole_GPU.cu:238-262,
+ * kernel :641-723) with the same arguments in the same order; the __constant__ dip_stride_1
+ * becomes the trailing dip_stride.  For every F (0 <= F < dimenF) whose vibrational index
+ * icorrF[F] lies in [startFblock, endFblock):
+ *   half_ls[F] = sum_I vector[I] sum_d wigner[d + 3 (ktauI[I] + nlevelI (ktauF[F] + nlevelF (kI[I] + sym_max_degen kF[F])))]
+ *                * dipole_me[(icorrF[F] - startFblock) + icorrI[I] ncontrF + d ncontrF dip_stride],
+ * where k holds the degeneracy index and ktau the rotational level index of each primitive
+ * (TroveClasses/TroveBasisSet.cpp:480-483); other entries are untouched.  Device pointers;
+ * asynchronous on `stream`.  Results are bit-identical to the reference kernel. */
+gain_status gain_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int sym_max_degen,
+                            const int* kI, const int* kF, const int* ktauI, const int* ktauF,
+                            const int* icorrI, const int* icorrF, int startFblock, int endFblock,
+                            int ncontrF, const double* dipole_me, const double* wigner,
+                            const double* vector, double* half_ls, int dip_stride, void* stream);
+
 /* Symmetry-adapted -> primitive expansion of one vector.
  * Replaces transform_vector_primitive (GPU/dipole_GPU.h:19, GPU/dipole_GPU.cu:137-156,
  * kernel :859-889): vec[r] = sum_{i<N[irow]} vecI[iterm+i] * repres[iterm+i + idegI*Ntot + ib*sdeg*Ntot]

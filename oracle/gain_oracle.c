@@ -118,6 +118,54 @@ void orc_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF,
     }
 }
 
+/* The reference sums f_1 + f_2 + f_3 (f_d = w_d mu_d, GPU/dipole_GPU.cu:698-702) and adds
+ * s_vector[i] times that sum to the accumulator.  The reference cubin evaluates it as
+ *   t = fma(w0, mu0, w1 mu1); t = fma(w2, mu2, t); acc = fma(v, t, acc)
+ * (identified bit for bit against that cubin's outputs on the rotsym golden vectors). */
+static double rotsym_one(int irootF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI,
+                         const int* kF, const int* ktauI, const int* ktauF, const int* icorrI,
+                         const int* icorrF, int startFblock, int ncontrF, const double* dipole_me,
+                         int dip_stride, const double* wigner, const double* vector, int mode) {
+    const size_t dstride = (size_t)ncontrF * (size_t)dip_stride;          /* :660 */
+    const int icontrF = icorrF[irootF] - startFblock;                       /* :668,675 */
+    const int lvlF = ktauF[irootF], degF = kF[irootF];
+    double acc = 0.0;
+    dd acc_dd = dd_from(0.0);
+    for (int irootI = 0; irootI < dimenI; irootI++) {
+        const size_t ic = (size_t)icorrI[irootI] * (size_t)ncontrF;         /* :679 */
+        const double mu0 = dipole_me[icontrF + ic];                           /* :689-691 */
+        const double mu1 = dipole_me[icontrF + ic + dstride];
+        const double mu2 = dipole_me[icontrF + ic + 2 * dstride];
+        const size_t w = (size_t)ktauI[irootI] * 3 + (size_t)lvlF * (size_t)nlevelI * 3 +
+                         (size_t)kI[irootI] * (size_t)nlevelI * (size_t)nlevelF * 3 +
+                         (size_t)degF * (size_t)maxdeg * (size_t)nlevelI * (size_t)nlevelF * 3;   /* :692 */
+        const double w0 = wigner[w], w1 = wigner[w + 1], w2 = wigner[w + 2];
+        const double v = vector[irootI];
+        if (mode == ORC_DD) {
+            dd sm = dd_add(dd_add(dd_mul_d(dd_from(w0), mu0), dd_mul_d(dd_from(w1), mu1)), dd_mul_d(dd_from(w2), mu2));
+            acc_dd = dd_add(acc_dd, dd_mul_d(sm, v));
+        } else {
+            const double t = fma(w2, mu2, fma(w0, mu0, w1 * mu1));
+            acc = fma(v, t, acc);
+        }
+    }
+    return mode == ORC_DD ? dd_round(acc_dd) : acc;
+}
+
+void orc_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg,
+                    const int* kI, const int* kF, const int* ktauI, const int* ktauF,
+                    const int* icorrI, const int* icorrF, int startFblock, int endFblock, int ncontrF,
+                    const double* dipole_me, int dip_stride, const double* wigner,
+                    const double* vector, double* half_ls, int mode) {
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < dimenF; f++) {
+        const int icontrF = icorrF[f];
+        if (icontrF < startFblock || icontrF >= endFblock) continue;        /* :674 */
+        half_ls[f] = rotsym_one(f, dimenI, nlevelI, nlevelF, maxdeg, kI, kF, ktauI, ktauF, icorrI, icorrF,
+                                startFblock, ncontrF, dipole_me, dip_stride, wigner, vector, mode);   /* :719 */
+    }
+}
+
 void orc_half_ls(int jI, int jF, int dimenI, int dimenF,
                  const int* tauI, const int* tauF, const int* icorrI, const int* icorrF,
                  const int* kstartI, const int* kblockI, const int* kstartF, const int* kblockF,

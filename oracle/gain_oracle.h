@@ -51,6 +51,24 @@ void orc_half_ls(int jI, int jF, int dimenI, int dimenF,
                  const double* prim_vector, const double* threej, int jmax,
                  double* half_ls, int mode);
 
+/* Rotational-symmetry (Euler) half line strength of one lower vector:
+ * device_compute_1st_half_ls_flipped_dipole_shared_rotsym_nontrove, GPU/dipole_GPU.cu:641-723,
+ * launched by compute_gpu_half_linestrength_rotsym_ (:238-262) from
+ * GpuManager::ExecuteRotSymHalfLs (BaseClasses/GpuManager.cpp:547-610).  For every upper
+ * primitive F whose vibrational index lies in [startFblock, endFblock):
+ *   half_ls[F] = sum_I v[I] (w0 mu0 + w1 mu1 + w2 mu2),
+ *   w_d = wigner[d + 3 (ktauI[I] + nlevelI (ktauF[F] + nlevelF (kI[I] + maxdeg kF[F])))],
+ *   mu_d = dipole_me[(icorrF[F] - startFblock) + icorrI[I] ncontrF + d ncontrF dip_stride];
+ * in rotsym mode ktau holds the rotational level index and k the degeneracy index
+ * (TroveClasses/TroveBasisSet.cpp:480-483).  Other entries are untouched.  ORC_REF mode
+ * forms the three-term sum as fma(w0, mu0, w1 mu1), then fma(w2, mu2, .), and accumulates it
+ * with one fused multiply-add: the order of the reference cubin, bit for bit. */
+void orc_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg,
+                    const int* kI, const int* kF, const int* ktauI, const int* ktauF,
+                    const int* icorrI, const int* icorrF, int startFblock, int endFblock, int ncontrF,
+                    const double* dipole_me, int dip_stride, const double* wigner,
+                    const double* vector, double* half_ls, int mode);
+
 /* Symmetry-adapted -> primitive expansion: device_expand_vectors, GPU/dipole_GPU.cu:859-889. */
 void orc_expand(int dimenI, int igammaI, int maxcoeff, int idegI, int sdeg, int Ntot,
                 const int* ijterms, const int* icontr, const int* N, const double* repres,

@@ -73,6 +73,9 @@ def _declare(L):
     L.orc_half_ls.argtypes = [I, I, I, I, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, I, I, I, _dp, I,
                               _dp, _dp, I, _dp, I]
     L.orc_half_ls.restype = None
+    L.orc_hls_rotsym.argtypes = [I, I, I, I, I, _ip, _ip, _ip, _ip, _ip, _ip, I, I, I, _dp, I, _dp, _dp,
+                                 _dp, I]
+    L.orc_hls_rotsym.restype = None
     L.orc_expand.argtypes = [I, I, I, I, I, I, _ip, _ip, _ip, _dp, _dp, _dp, I]
     L.orc_expand.restype = None
     L.orc_dot.argtypes = [I, _dp, _dp, I]
@@ -111,6 +114,26 @@ def hls_kblock(dimenF, dimenI, jI, jF, kF, tauI, tauF, icorrI, icorrF, startF_id
     lib().orc_hls_kblock(dimenF, dimenI, jI, jF, kF, *args, startF_idx, startI_idx, startFblock,
                          endFblock, ncontrF, kbp, dmp, dip_stride, vecp, tjp, jmax,
                          half_ls.ctypes.data_as(_dp), mode)
+    return half_ls
+
+
+def hls_rotsym(bI, bF, nlevelI, nlevelF, maxdeg, dipole_piece, dip_stride, block, wigner, vector,
+               half_ls, mode=REF):
+    """Rotsym half_ls of one primitive lower vector (synth.Basis inputs, rotsym field meaning:
+    K = degeneracy index, tau = level index); entries outside the dipole block untouched."""
+    startF, endF, ncontrF = block
+    keep = []
+
+    def I(a):
+        arr, p = _i(a); keep.append(arr); return p
+
+    def D(a):
+        arr, p = _d(a); keep.append(arr); return p
+
+    assert half_ls.dtype == np.float64 and half_ls.flags.c_contiguous and half_ls.size >= bF.dimen
+    lib().orc_hls_rotsym(bF.dimen, bI.dimen, nlevelI, nlevelF, maxdeg, I(bI.K), I(bF.K), I(bI.tau), I(bF.tau),
+                         I(bI.vib), I(bF.vib), startF, endF, ncontrF, D(dipole_piece), dip_stride, D(wigner),
+                         D(vector), half_ls.ctypes.data_as(_dp), mode)
     return half_ls
 
 

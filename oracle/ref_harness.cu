@@ -27,9 +27,11 @@ namespace {
 const char* kHlsName =
     "_Z63device_compute_1st_half_ls_flipped_dipole_shared_block_nontroveiiiiiPKiS0_S0_S0_iiiiiS0_PKdS2_S2_Pd";
 const char* kExpandName = "_Z21device_expand_vectorsiiiiiiPKiS0_S0_PKdS2_Pd";
+const char* kRotsymName =
+    "_Z64device_compute_1st_half_ls_flipped_dipole_shared_rotsym_nontroveiiiiiPKiS0_S0_S0_S0_S0_iiiPKdS2_S2_Pd";
 
 CUmodule g_mod = nullptr;
-CUfunction g_hls = nullptr, g_expand = nullptr;
+CUfunction g_hls = nullptr, g_expand = nullptr, g_rotsym = nullptr;
 CUdeviceptr g_dip_stride = 0, g_jmax = 0;
 char g_err[512];
 
@@ -90,6 +92,7 @@ int refh_init(const char* cubin_path) {
     DRV(cuModuleLoad(&g_mod, cubin_path));
     DRV(cuModuleGetFunction(&g_hls, g_mod, kHlsName));
     DRV(cuModuleGetFunction(&g_expand, g_mod, kExpandName));
+    DRV(cuModuleGetFunction(&g_rotsym, g_mod, kRotsymName));
     size_t sz = 0;
     DRV(cuModuleGetGlobal(&g_dip_stride, &sz, g_mod, "dip_stride_1"));
     DRV(cuModuleGetGlobal(&g_jmax, &sz, g_mod, "c_jmax"));
@@ -191,6 +194,44 @@ int refh_run_pair(const refh_pair* p, double* amp, double* hls, double* seconds)
     cudaFreeHost(h_res);
     void* ptrs[] = {d_tauI, d_tauF, d_icI, d_icF, d_kbI, d_ijI, d_ctI, d_NI, d_ijF, d_ctF, d_NF,
                     d_rpI, d_rpF, d_dip, d_3j, d_vecI, d_vecF, d_primI, d_primF, d_hls, d_res};
+    for (void* q : ptrs) cudaFree(q);
+    RT(cudaGetLastError());
+    return 0;
+}
+
+// The rotational-symmetry half line strength of one primitive lower vector, as
+// GpuManager::ExecuteRotSymHalfLs launches it (BaseClasses/GpuManager.cpp:564-592) through
+// compute_gpu_half_linestrength_rotsym_ (GPU/dipole_GPU.cu:238-262: grid ceil(dimenF/128) x
+// 128), after the reset to zero of the half line strength (:761-766).  dipole: 3 x
+// dip_stride x ncontrF doubles; wigner: 3 nlevelI nlevelF maxdeg^2 doubles.
+int refh_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI, const int* kF,
+                    const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF, int startFblock,
+                    int endFblock, int ncontrF, const double* dipole, int dip_stride, const double* wigner,
+                    const double* vector, double* half_ls) {
+    if (!g_mod) {
+        snprintf(g_err, sizeof g_err, "refh_init not called");
+        return -1;
+    }
+    int stride = dip_stride;
+    DRV(cuMemcpyHtoD(g_dip_stride, &stride, sizeof(int)));
+    int *d_kI, *d_kF, *d_tI, *d_tF, *d_cI, *d_cF;
+    double *d_dip, *d_w, *d_v, *d_h;
+    const size_t wn = (size_t)3 * nlevelI * nlevelF * maxdeg * maxdeg;
+    if (upload(&d_kI, kI, dimenI) || upload(&d_kF, kF, dimenF) || upload(&d_tI, ktauI, dimenI) ||
+        upload(&d_tF, ktauF, dimenF) || upload(&d_cI, icorrI, dimenI) || upload(&d_cF, icorrF, dimenF) ||
+        upload(&d_dip, dipole, (size_t)3 * dip_stride * ncontrF) || upload(&d_w, wigner, wn) ||
+        upload(&d_v, vector, dimenI))
+        return -1;
+    RT(cudaMalloc(&d_h, sizeof(double) * dimenF));
+    RT(cudaMemset(d_h, 0, sizeof(double) * dimenF));
+    int a0 = dimenF, a1 = dimenI, a2 = nlevelI, a3 = nlevelF, a4 = maxdeg, a5 = startFblock, a6 = endFblock,
+        a7 = ncontrF;
+    void* args[] = {&a0, &a1, &a2, &a3, &a4, &d_kI, &d_kF, &d_tI, &d_tF, &d_cI, &d_cF,
+                    &a5, &a6, &a7, &d_dip, &d_w, &d_v, &d_h};
+    DRV(cuLaunchKernel(g_rotsym, (dimenF + 127) / 128, 1, 1, 128, 1, 1, 0, nullptr, args, nullptr));
+    RT(cudaDeviceSynchronize());
+    RT(cudaMemcpy(half_ls, d_h, sizeof(double) * dimenF, cudaMemcpyDeviceToHost));
+    void* ptrs[] = {d_kI, d_kF, d_tI, d_tF, d_cI, d_cF, d_dip, d_w, d_v, d_h};
     for (void* q : ptrs) cudaFree(q);
     RT(cudaGetLastError());
     return 0;

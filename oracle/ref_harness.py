@@ -64,6 +64,9 @@ def lib():
         L.refh_error.restype = ctypes.c_char_p
         L.refh_run_pair.argtypes = [ctypes.POINTER(RefhPair), _dp, _dp, _dp]
         L.refh_run_pair.restype = ctypes.c_int
+        I = ctypes.c_int
+        L.refh_hls_rotsym.argtypes = [I, I, I, I, I, _ip, _ip, _ip, _ip, _ip, _ip, I, I, I, _dp, I, _dp, _dp, _dp]
+        L.refh_hls_rotsym.restype = ctypes.c_int
         if L.refh_init(CUBIN.encode()) != 0:
             raise RuntimeError("reference harness: " + L.refh_error().decode())
         _lib = L
@@ -117,3 +120,25 @@ def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, 
                            ctypes.byref(secs)) != 0:
         raise RuntimeError("reference harness: " + lib().refh_error().decode())
     return amp, hls, secs.value
+
+
+def hls_rotsym(bI, bF, nlevelI, nlevelF, maxdeg, dipole, block, wigner, vector):
+    """The reference's rotsym half line strength of one primitive lower vector (dimen of J'),
+    zeros outside the dipole block; dipole is the full [3][N][N] flipped array."""
+    nv = dipole.shape[-1]
+    startF, endF = block
+    piece = np.ascontiguousarray(dipole[:, :, startF:endF])
+    keep = []
+
+    def I(a):
+        a = np.ascontiguousarray(a, np.int32); keep.append(a); return a.ctypes.data_as(_ip)
+
+    def D(a):
+        a = np.ascontiguousarray(a, np.float64); keep.append(a); return a.ctypes.data_as(_dp)
+
+    out = np.zeros(bF.dimen, np.float64)
+    if lib().refh_hls_rotsym(bF.dimen, bI.dimen, nlevelI, nlevelF, maxdeg, I(bI.K), I(bF.K), I(bI.tau), I(bF.tau),
+                             I(bI.vib), I(bF.vib), startF, endF, endF - startF, D(piece.reshape(-1)), nv,
+                             D(wigner), D(vector), out.ctypes.data_as(_dp)) != 0:
+        raise RuntimeError("reference harness: " + lib().refh_error().decode())
+    return out

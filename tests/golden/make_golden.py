@@ -11,7 +11,7 @@ Each fixture stores the exact inputs that are not pure integer tables (eigenvect
 dipole piece, 3j table) next to the reference outputs (half_ls per lower state and the
 amplitudes), so the CPU tests can replay them anywhere.
 
-    python tests/golden/make_golden.py OUTDIR      # needs a GPU and the reference cubin
+    python tests/golden/make_golden.py OUTDIR [rotsym]   # needs a GPU and the reference cubin
 """
 from __future__ import annotations
 
@@ -58,13 +58,49 @@ def make_case(name, jmax=11):
                 ref_hls=hls, ref_amp=amp)
 
 
+# rotational-symmetry (Euler) half line strength: nv, J'', J', degeneracy, lower vectors, dipole block
+ROTSYM_CASES = {
+    "rotsym_dJp1": (12, 2, 3, 2, 6, None),
+    "rotsym_dJ0": (12, 3, 3, 1, 6, None),
+    "rotsym_dJm1_blocked": (12, 3, 2, 2, 4, (3, 9)),
+}
+
+
+def make_rotsym_case(name):
+    """The reference's rotsym kernel (device_compute_1st_half_ls_flipped_dipole_shared_rotsym_
+    nontrove) on seeded primitive lower vectors of the synthetic rotsym basis."""
+    nv, JI, JF, maxdeg, nvec, blk = ROTSYM_CASES[name]
+    bI, bF = synth.make_rotsym_basis(JI, nv, maxdeg), synth.make_rotsym_basis(JF, nv, maxdeg)
+    nI, nF = synth.rotsym_levels(JI), synth.rotsym_levels(JF)
+    wig = synth.make_wigner(JI, JF, maxdeg)
+    dip = synth.make_dipole(nv)
+    rng = np.random.default_rng(4242 + 10 * JI + JF)
+    vecs = rng.standard_normal((nvec, bI.dimen)) / np.sqrt(bI.dimen)
+    block = blk if blk else (0, nv)
+    hls = np.stack([ref_harness.hls_rotsym(bI, bF, nI, nF, maxdeg, dip, block, wig, v) for v in vecs])
+    return dict(nv=nv, JI=JI, JF=JF, maxdeg=maxdeg, block=np.array(block), nlevelI=nI, nlevelF=nF,
+                wigner=wig, dipole=dip, vectors=vecs, ref_hls=hls)
+
+
 def main(outdir):
     os.makedirs(outdir, exist_ok=True)
     for name in CASES:
         d = make_case(name)
         np.savez_compressed(os.path.join(outdir, name + ".npz"), **d)
         print(name, d["ref_hls"].shape, d["ref_amp"].shape, float(np.abs(d["ref_amp"]).max()))
+    for name in ROTSYM_CASES:
+        d = make_rotsym_case(name)
+        np.savez_compressed(os.path.join(outdir, name + ".npz"), **d)
+        print(name, d["ref_hls"].shape, float(np.abs(d["ref_hls"]).max()))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__)))
+    out = sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__))
+    if len(sys.argv) > 2 and sys.argv[2] == "rotsym":   # only the rotsym fixtures
+        os.makedirs(out, exist_ok=True)
+        for name in ROTSYM_CASES:
+            d = make_rotsym_case(name)
+            np.savez_compressed(os.path.join(out, name + ".npz"), **d)
+            print(name, d["ref_hls"].shape, float(np.abs(d["ref_hls"]).max()))
+    else:
+        main(out)

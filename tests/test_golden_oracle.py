@@ -14,7 +14,8 @@ import pytest
 
 from conftest import GOLDEN
 
-FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+FIXTURES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz")) if not os.path.basename(f).startswith("rotsym_"))
+ROT_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "rotsym_*.npz")))
 
 
 def _problem(d):
@@ -78,3 +79,54 @@ def test_oracle_amplitudes_within_dot_bound(oracle_lib, path):
             a = oracle.dot(prim, h, oracle.DD)
             bound = 2 * len(h) * 1.12e-16 * float(np.sum(np.abs(prim * h))) + 1e-300
             assert abs(a - d["ref_amp"][l, u]) <= bound
+
+
+# ------------------------------------------------------------ rotational-symmetry (Euler) form
+
+def _rot_inputs(d):
+    import synth
+    nv, JI, JF, md = int(d["nv"]), int(d["JI"]), int(d["JF"]), int(d["maxdeg"])
+    bI, bF = synth.make_rotsym_basis(JI, nv, md), synth.make_rotsym_basis(JF, nv, md)
+    s, e = (int(x) for x in d["block"])
+    piece = np.ascontiguousarray(d["dipole"][:, :, s:e]).reshape(-1)
+    return nv, md, bI, bF, s, e, piece
+
+
+def test_rotsym_fixtures_present():
+    names = {os.path.basename(f)[:-4] for f in ROT_FIXTURES}
+    assert {"rotsym_dJp1", "rotsym_dJ0", "rotsym_dJm1_blocked"} <= names
+
+
+@pytest.mark.parametrize("path", ROT_FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+def test_rotsym_inputs_are_reproducible(path):
+    """The Wigner table regenerates exactly from its seed, the dipole to rounding."""
+    import synth
+    d = np.load(path)
+    assert np.array_equal(d["wigner"], synth.make_wigner(int(d["JI"]), int(d["JF"]), int(d["maxdeg"])))
+    assert np.allclose(d["dipole"], synth.make_dipole(int(d["nv"])), rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("path", ROT_FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+def test_rotsym_oracle_bit_exact_vs_reference_kernel(path):
+    """The oracle's restatement of the rotsym kernel (GPU/dipole_GPU.cu:641-723) equals the
+    reference kernel's half_ls bit for bit, including the untouched entries outside the
+    dipole block and degenerate levels (maxdeg 2)."""
+    import oracle
+    d = np.load(path)
+    nv, md, bI, bF, s, e, piece = _rot_inputs(d)
+    for v, ref in zip(d["vectors"], d["ref_hls"]):
+        h = np.zeros(bF.dimen)
+        oracle.hls_rotsym(bI, bF, int(d["nlevelI"]), int(d["nlevelF"]), md, piece, nv, (s, e, e - s), d["wigner"], v, h)
+        assert np.array_equal(h, ref)
+
+
+@pytest.mark.parametrize("path", ROT_FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+def test_rotsym_reference_within_rounding_of_double_double(path):
+    import oracle
+    d = np.load(path)
+    nv, md, bI, bF, s, e, piece = _rot_inputs(d)
+    for v, ref in zip(d["vectors"], d["ref_hls"]):
+        h = np.zeros(bF.dimen)
+        oracle.hls_rotsym(bI, bF, int(d["nlevelI"]), int(d["nlevelF"]), md, piece, nv, (s, e, e - s), d["wigner"], v, h,
+                          oracle.DD)
+        assert np.max(np.abs(h - ref)) <= 64 * 2.0 ** -53 * bI.dimen * np.abs(ref).max()

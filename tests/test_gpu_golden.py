@@ -9,7 +9,8 @@ import pytest
 from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
-FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+FIXTURES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz")) if not os.path.basename(f).startswith("rotsym_"))
+ROT_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "rotsym_*.npz")))
 
 
 def _problem(d):
@@ -83,3 +84,33 @@ def test_engine_paths_vs_reference_amplitudes(built_lib, path):
     assert np.max(np.abs(S[m] - Sr[m]) / Sr[m]) <= 1e-8
     assert np.max(np.abs(split - ref)) <= 1e-11 * np.abs(ref).max()
     eng.close()
+
+
+@pytest.mark.parametrize("path", ROT_FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
+def test_dropin_rotsym_bit_exact_vs_reference_kernel(built_lib, path):
+    """gain_hls_rotsym equals the reference's rotsym kernel bit for bit, and leaves the
+    entries outside the dipole block untouched."""
+    import torch
+    import gainls
+    import synth
+    d = np.load(path)
+    nv, JI, JF, md = int(d["nv"]), int(d["JI"]), int(d["JF"]), int(d["maxdeg"])
+    bI, bF = synth.make_rotsym_basis(JI, nv, md), synth.make_rotsym_basis(JF, nv, md)
+    s, e = (int(x) for x in d["block"])
+    piece = np.ascontiguousarray(d["dipole"][:, :, s:e]).reshape(-1)
+
+    def dev(a, dt):
+        return torch.from_numpy(np.ascontiguousarray(a, dt)).cuda()
+
+    keep = [dev(bI.K, np.int32), dev(bF.K, np.int32), dev(bI.tau, np.int32), dev(bF.tau, np.int32),
+            dev(bI.vib, np.int32), dev(bF.vib, np.int32), dev(piece, np.float64), dev(d["wigner"], np.float64)]
+    for v, ref in zip(d["vectors"], d["ref_hls"]):
+        dv = dev(v, np.float64)
+        out = torch.full((bF.dimen,), 7.0, dtype=torch.float64, device="cuda")
+        gainls.hls_rotsym(bF.dimen, bI.dimen, int(d["nlevelI"]), int(d["nlevelF"]), md, *[t.data_ptr() for t in keep[:6]],
+                          s, e, e - s, keep[6].data_ptr(), keep[7].data_ptr(), dv.data_ptr(), out.data_ptr(), nv)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        inside = (bF.vib >= s) & (bF.vib < e)
+        assert np.array_equal(got[inside], ref[inside])
+        assert np.all(got[~inside] == 7.0)
