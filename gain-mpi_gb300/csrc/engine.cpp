@@ -100,7 +100,8 @@ struct Basis {
     bool present = false;
     int J = 0, dimen = 0;
     std::vector<int> K, tau, vib, kblock, kstart;
-    DevArray<int> dK, dtau, dvib, dkblock;
+    std::vector<int> lev;   // tau as uploaded (the rotational level index of the rotsym form)
+    DevArray<int> dK, dtau, dvib, dkblock, dlev;
 };
 
 // Per symmetry of one J: derived structures of the expansion (ideg 0).
@@ -143,6 +144,14 @@ struct Eig {
     }
 };
 
+// Rotational matrix elements of one (J'', J') pair (the rotational-symmetry form):
+// rot[d + 3 (lI + nI (lF + nF (dI + maxdeg dF)))], as GpuManager::TransferWigner stores them.
+struct WignerTab {
+    int nI = 0, nF = 0, maxdeg = 0;
+    long version = 0;
+    DevArray<double> rot;
+};
+
 struct StatsDev {
     DevArray<int> e, nnz;
     DevArray<float> l2, dn, dnv, rnv, inerr;
@@ -183,8 +192,9 @@ struct StatsDev {
 // padded per K block to BN so that no output tile straddles two upper K blocks).
 struct PairLayout {
     int key[4] = {-1, -1, -1, -1};
-    long dip_version = -1;
+    long dip_version = -1, wig_version = -1;
     int nI = 0, kpadI = 0, nF = 0, fpad = 0, W = 0;
+    bool rotsym = false;
     std::vector<int> kpad_startI;   // [J_I + 2]
     std::vector<int> colposI, i_sym, i_prim;
     std::vector<double> i_coef;
@@ -193,7 +203,7 @@ struct PairLayout {
     std::vector<std::pair<int, int>> fblocks;   // padded [start, end) of each upper K block
     DevArray<int> d_colposI, d_i_sym, d_i_prim, d_colposF, d_f_sym, d_f_prim, d_band_k0, d_band_len;
     DevArray<double> d_i_coef, d_f_coef, band;
-    int beta1 = 0, s1 = 0;
+    int beta1 = 0, s1 = 0, c1 = 0;
     DevArray<__nv_bfloat16> bandDig;
     StatsDev bandStats;
     CUtensorMap tmBand, tmBandPair;   // 128-row boxes; 64-row boxes for a CTA pair
@@ -227,6 +237,8 @@ struct gain_engine_s {
     int dipN = 0, startF = 0, endF = 0, ncontrF = 0;
     bool dip_present = false;
     long dip_version = 0;
+    std::map<std::pair<int, int>, std::unique_ptr<gain::WignerTab>> wigner;   // by (jindI, jindF)
+    long wig_version = 0;
     std::map<std::pair<int, int>, std::unique_ptr<gain::Eig>> eig;
 
     // last run
@@ -353,6 +365,12 @@ gain_status validate_job(gain_engine e, const gain_pair_job* j) {
 }
 
 // ------------------------------------------------------------------ plain FP64 path
+// The pair's rotational-symmetry table, or NULL (the K-block form).
+const WignerTab* wigner_of(gain_engine e, int jindI, int jindF) {
+    auto it = e->wigner.find({jindI, jindF});
+    return it == e->wigner.end() ? nullptr : it->second.get();
+}
+
 gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) {
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
@@ -403,10 +421,22 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) 
         GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
                                        iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
                                        EI.d.p, EI.nsize, e->d_lower.p + l0, e->primI.p, bI.dimen, nb, st));
-        GAIN_CUDA(launch_hls_needed(L.d_ctas.p, (int)L.ctas.size(), mF->d_support.p, bI.J, bF.J, bI.dtau.p,
-                                    bF.dtau.p, bI.dvib.p, bF.dvib.p, mI->d_support.p, mI->d_sup_start.p,
-                                    e->startF, e->endF, e->ncontrF, e->dipole.p, e->dipN, e->primI.p, bI.dimen,
-                                    e->d3j.p, e->jmax, e->hprim.p, bF.dimen, nb, st));
+        if (const WignerTab* wt = wigner_of(e, j->jindI, j->jindF)) {
+            // rotational-symmetry form (GpuManager::ExecuteRotSymHalfLs): reset, then the dense
+            // half line strength of each lower state
+            GAIN_CUDA(cudaMemsetAsync(e->hprim.p, 0, sizeof(double) * (size_t)nb * bF.dimen, st));
+            for (int b = 0; b < nb; ++b)
+                GAIN_CUDA(launch_hls_rotsym(bF.dimen, bI.dimen, wt->nI, wt->nF, wt->maxdeg, bI.dK.p, bF.dK.p, bI.dlev.p,
+                                            bF.dlev.p, bI.dvib.p, bF.dvib.p, e->startF, e->endF, e->ncontrF,
+                                            e->dipole.p, e->dipN, wt->rot.p, e->primI.p + (size_t)b * bI.dimen,
+                                            e->hprim.p + (size_t)b * bF.dimen, st));
+            launches += nb;
+        } else {
+            GAIN_CUDA(launch_hls_needed(L.d_ctas.p, (int)L.ctas.size(), mF->d_support.p, bI.J, bF.J, bI.dtau.p,
+                                        bF.dtau.p, bI.dvib.p, bF.dvib.p, mI->d_support.p, mI->d_sup_start.p,
+                                        e->startF, e->endF, e->ncontrF, e->dipole.p, e->dipN, e->primI.p, bI.dimen,
+                                        e->d3j.p, e->jmax, e->hprim.p, bF.dimen, nb, st));
+        }
         GAIN_CUDA(launch_contract(NtF, mF->d_csr_ptr.p, mF->d_csr_col.p, mF->d_csr_val.p, e->hprim.p, bF.dimen,
                                   e->hsym.p, NtF, nb, st));
         GAIN_CUDA(launch_gemv_batch(j->nupper, EF.nsize, EF.d.p, EF.nsize, e->d_upper.p, e->hsym.p, NtF, nb,
@@ -479,7 +509,10 @@ std::vector<split::Prod> make_prods(const SplitParams& p) {
 gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, GammaMaps* mF) {
     PairLayout& L = e->layout;
     const int key[4] = {j->jindI, j->gammaI, j->jindF, j->gammaF};
-    if (std::equal(key, key + 4, L.key) && L.dip_version == e->dip_version) return GAIN_OK;
+    const WignerTab* wt = wigner_of(e, j->jindI, j->jindF);
+    const long wv = wt ? wt->version : 0;
+    if (std::equal(key, key + 4, L.key) && L.dip_version == e->dip_version && L.wig_version == wv) return GAIN_OK;
+    L.rotsym = wt != nullptr;
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
     L.nI = (int)mI->sym_prim.size();
@@ -541,6 +574,12 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     }
     L.W = split::BK;
     for (int r = 0; r < L.fpad; ++r) {
+        if (L.rotsym) {   // no K sparsity: every upper row spans the whole lower layout
+            L.band_k0[r] = 0;
+            L.band_len[r] = L.kpadI;
+            L.W = L.kpadI;
+            continue;
+        }
         const int kF = f_k[r];
         const int klo = std::max(kF - 1, 0), khi = std::min(kF + 1, bI.J);
         if (klo > khi) continue;
@@ -584,11 +623,21 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     ba.endF = e->endF;
     ba.ncontrF = e->ncontrF;
     ba.band = L.band.p;
+    ba.wigner = wt ? wt->rot.p : nullptr;
+    if (wt) {   // the rotsym form reads level indices where the K-block form reads tau parities
+        ba.tauI = bI.dlev.p;
+        ba.tauF = bF.dlev.p;
+    }
+    ba.nlevelI = wt ? wt->nI : 0;
+    ba.nlevelF = wt ? wt->nF : 0;
+    ba.maxdeg = wt ? wt->maxdeg : 0;
     GAIN_CUDA(split::launch_band(ba, e->st));
     L.beta1 = 0;
     L.s1 = 0;
+    L.c1 = 0;
     std::copy(key, key + 4, L.key);
     L.dip_version = e->dip_version;
+    L.wig_version = wv;
     return GAIN_OK;
 }
 
@@ -655,12 +704,18 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     // options (beta, slices, kchunks) apply to it.
     gain_split_opts o1{};
     if (opts) o1.beta = opts->beta;
-    const SplitParams p1 = choose_params(L.W, &o1, 56, 7);
-    SplitParams p1x = p1;
-    p1x.chunks = 1;
-    while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
-        --p1x.beta;
-        p1x.slices = (56 + p1x.beta - 1) / p1x.beta;
+    SplitParams p1x;
+    if (L.rotsym) {
+        // rotational-symmetry form: every tile spans the whole lower layout, so the inner
+        // dimension splits into chunks as in the second GEMM (per-chunk norms of both operands)
+        p1x = choose_params(L.W, &o1, 56, 8);
+    } else {
+        p1x = choose_params(L.W, &o1, 56, 7);
+        p1x.chunks = 1;
+        while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
+            --p1x.beta;
+            p1x.slices = (56 + p1x.beta - 1) / p1x.beta;
+        }
     }
     const SplitParams p2 = choose_params(L.fpad, opts, 48, 8);
     if (p1x.slices * p1x.beta > 62 || p2.slices * p2.beta > 62 || p1x.slices > split::MAX_SLICES ||
@@ -669,11 +724,11 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         return set_error(GAIN_ERR_INVALID_ARG, "unsupported digit configuration");
 
     // band digits (cached per digit configuration)
-    if (L.beta1 != p1x.beta || L.s1 != p1x.slices) {
+    if (L.beta1 != p1x.beta || L.s1 != p1x.slices || L.c1 != p1x.chunks) {
         GAIN_TRY(L.bandDig.alloc((size_t)p1x.slices * L.fpad * L.W));
         GAIN_TRY(L.bandDig.zero(st, (size_t)p1x.slices * L.fpad * L.W));
-        GAIN_TRY(L.bandStats.alloc(L.fpad, 1, false));
-        GAIN_TRY(L.bandStats.zero(st, L.fpad, 1, false));
+        GAIN_TRY(L.bandStats.alloc(L.fpad, p1x.chunks, false));
+        GAIN_TRY(L.bandStats.zero(st, L.fpad, p1x.chunks, false));
         GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, nullptr, L.W, L.fpad, L.bandDig.p, p1x,
                        L.bandStats, false, nullptr, nullptr, st));
         if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1x.slices) ||
@@ -681,6 +736,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
             return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed for the band digits");
         L.beta1 = p1x.beta;
         L.s1 = p1x.slices;
+        L.c1 = p1x.chunks;
     }
 
     // CTA pairs (256 x 128 tiles) whenever the lower states fill more than one 128-row block;
@@ -709,17 +765,17 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     const size_t hdig = (size_t)p2.slices * Bpad * L.fpad;
     const size_t udig = (size_t)p2.slices * Nupad * L.fpad;
     GAIN_TRY(e->Vdig.alloc(vdig));
-    GAIN_TRY(e->Vst.alloc(Bpad, 1, false));
+    GAIN_TRY(e->Vst.alloc(Bpad, p1x.chunks, false));
     GAIN_TRY(e->Hdig.alloc(hdig));
     GAIN_TRY(e->Hst.alloc(Bpad, p2.chunks, true));
     GAIN_TRY(e->Udig.alloc(udig));
     GAIN_TRY(e->Ust.alloc(Nupad, p2.chunks, false));
-    const std::vector<long> kV = {lkey, p1x.slices, p1x.beta, B, Bpad, (long)(uintptr_t)e->Vdig.p};
+    const std::vector<long> kV = {lkey, p1x.slices, p1x.beta, p1x.chunks, B, Bpad, (long)(uintptr_t)e->Vdig.p};
     const std::vector<long> kH = {lkey, p2.slices, p2.chunks, B, Bpad, (long)(uintptr_t)e->Hdig.p};
     const std::vector<long> kU = {lkey, p2.slices, p2.chunks, Nu, Nupad, (long)(uintptr_t)e->Udig.p};
     if (e->zkey_V != kV) {
         GAIN_TRY(e->Vdig.zero(st, vdig));
-        GAIN_TRY(e->Vst.zero(st, Bpad, 1, false));
+        GAIN_TRY(e->Vst.zero(st, Bpad, p1x.chunks, false));
         e->zkey_V = kV;
     }
     if (e->zkey_H != kH) {
@@ -771,7 +827,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g1.ntiles = (int)t1.size();
     g1.prods = e->prods1.p;
     g1.nprods = (int)pr1.size();
-    g1.nchunks = 1;
+    g1.nchunks = p1x.chunks;
     g1.beta = p1x.beta;
     g1.slices = p1x.slices;
     g1.out = e->H.p;
@@ -921,7 +977,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         stats->inexact = (long long)cnt[0];
         stats->beta1 = p1x.beta;
         stats->slices1 = p1x.slices;
-        stats->chunks1 = 1;
+        stats->chunks1 = p1x.chunks;
         stats->beta2 = p2.beta;
         stats->slices2 = p2.slices;
         stats->chunks2 = p2.chunks;
@@ -1104,12 +1160,14 @@ gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const i
     b.dimen = dimen;
     b.K.assign(K, K + dimen);
     b.tau.assign(tau, tau + dimen);
+    b.lev = b.tau;
     for (auto& t : b.tau) t &= 1;
     b.vib.assign(vib, vib + dimen);
     b.kblock.assign(kblock_size, kblock_size + J + 1);
     b.kstart.assign(kstart, kstart + J + 1);
     GAIN_TRY(b.dK.upload(b.K));
     GAIN_TRY(b.dtau.upload(b.tau));
+    GAIN_TRY(b.dlev.upload(b.lev));
     GAIN_TRY(b.dvib.upload(b.vib));
     GAIN_TRY(b.dkblock.upload(b.kblock));
     b.present = true;
@@ -1189,6 +1247,36 @@ gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int st
     e->ncontrF = ncontrF;
     e->dip_present = true;
     ++e->dip_version;
+    return GAIN_OK;
+}
+
+gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI, int nlevelsF, int maxdeg,
+                               const double* rot) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (jindI < 0 || jindF < 0 || jindI >= (int)e->bases.size() || jindF >= (int)e->bases.size() || nlevelsI <= 0 ||
+        nlevelsF <= 0 || maxdeg <= 0 || !rot)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_wigner: bad argument");
+    const Basis& bI = e->bases[jindI];
+    const Basis& bF = e->bases[jindF];
+    if (!bI.present || !bF.present) return set_error(GAIN_ERR_NOT_READY, "gain_upload_wigner: basis not uploaded");
+    if (std::abs(bF.J - bI.J) > 1) return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_wigner: |J' - J''| > 1");
+    // in the rotational-symmetry form tau holds the level index and K the degeneracy index
+    for (int x = 0; x < bI.dimen; ++x)
+        if (bI.lev[x] < 0 || bI.lev[x] >= nlevelsI || bI.K[x] < 0 || bI.K[x] >= maxdeg)
+            return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_wigner: lower function %d has level %d / index %d "
+                             "outside %d levels x %d", x, bI.lev[x], bI.K[x], nlevelsI, maxdeg);
+    for (int x = 0; x < bF.dimen; ++x)
+        if (bF.lev[x] < 0 || bF.lev[x] >= nlevelsF || bF.K[x] < 0 || bF.K[x] >= maxdeg)
+            return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_wigner: upper function %d has level %d / index %d "
+                             "outside %d levels x %d", x, bF.lev[x], bF.K[x], nlevelsF, maxdeg);
+    auto& slot = e->wigner[{jindI, jindF}];
+    if (!slot) slot.reset(new WignerTab());
+    slot->nI = nlevelsI;
+    slot->nF = nlevelsF;
+    slot->maxdeg = maxdeg;
+    GAIN_TRY(slot->rot.upload(rot, (size_t)3 * nlevelsI * nlevelsF * maxdeg * maxdeg));
+    slot->version = ++e->wig_version;
     return GAIN_OK;
 }
 

@@ -1002,7 +1002,18 @@ __global__ void k_band(const BandArgs a) {
     double val = 0.0;
     const int rF = a.f_prim[row];
     const int kc = a.band_k0[row] + w;
-    if (rF >= 0 && kc < a.kpadI) {
+    if (a.wigner && rF >= 0 && kc < a.kpadI) {
+        const int rI = a.i_prim[kc];
+        const int vF = a.vibF[rF];
+        if (rI >= 0 && vF >= a.startF && vF < a.endF) {
+            const long d = (long)(vF - a.startF) + (long)a.vibI[rI] * a.ncontrF, ds = (long)a.dipN * a.ncontrF;
+            const long wi = 3 * ((long)a.tauI[rI] + (long)a.nlevelI *
+                                 ((long)a.tauF[rF] + (long)a.nlevelF * ((long)a.KI[rI] + (long)a.maxdeg * a.KF[rF])));
+            const double t = __fma_rn(a.wigner[wi + 2], a.dipole[d + 2 * ds],
+                                      __fma_rn(a.wigner[wi], a.dipole[d], __dmul_rn(a.wigner[wi + 1], a.dipole[d + ds])));
+            val = __dmul_rn(t, __dmul_rn(a.i_coef[kc], a.f_coef[row]));
+        }
+    } else if (rF >= 0 && kc < a.kpadI) {
         const int rI = a.i_prim[kc];
         if (rI >= 0) {
             const int kI = a.KI[rI], kF = a.KF[rF];

@@ -138,6 +138,11 @@ struct BandArgs {
     const double* dipole;
     int dipN, startF, endF, ncontrF;
     double* band;
+    // rotational-symmetry form (GPU/dipole_GPU.cu:641-723) when non-null: dense in K, the entry
+    // of (F, I) is sum_d wigner[d + 3 (tauI + nlevelI (tauF + nlevelF (KI + maxdeg KF)))] mu_d,
+    // with tau = level index and K = degeneracy index
+    const double* wigner;
+    int nlevelI, nlevelF, maxdeg;
 };
 cudaError_t launch_band(const BandArgs& a, cudaStream_t st);
 

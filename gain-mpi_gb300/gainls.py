@@ -181,6 +181,7 @@ def _declare(L):
                                         _ip, _ip]
     L.gain_upload_dipole.argtypes = [_vp, _dp, I, I, I, I]
     L.gain_upload_eigvecs.argtypes = [_vp, I, I, I, I, _dp]
+    L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
     L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
     L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
@@ -202,7 +203,7 @@ def _declare(L):
     L.gain_plan_pairs.restype = S
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
-                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines"):
         getattr(L, name).restype = S
 
@@ -316,6 +317,11 @@ class Engine:
         vecs = _f64(vecs)
         check(lib().gain_upload_eigvecs(self.h, jind, gamma, vecs.shape[0], vecs.shape[1], _p(vecs, _dp)))
 
+    def upload_wigner(self, jindI, jindF, nlevelsI, nlevelsF, maxdeg, rot):
+        rot = _f64(rot)
+        assert rot.size == 3 * nlevelsI * nlevelsF * maxdeg * maxdeg
+        check(lib().gain_upload_wigner(self.h, jindI, jindF, nlevelsI, nlevelsF, maxdeg, _p(rot, _dp)))
+
     def upload_eigvecs_async(self, jind, gamma, vecs):
         """Queue the copy of page-locked vecs (C-contiguous float64, kept unchanged until the
         next run_pair returns); pageable arrays are copied synchronously."""
@@ -394,3 +400,10 @@ def upload_problem(eng: Engine, p, dipole_block=None, blocks=None):
     for (jind, g), blk in p.blocks.items():
         if blocks is None or (jind, g) in blocks:
             eng.upload_eigvecs(jind, g, blk.vecs)
+    if p.rule == "c4r":   # rotational-symmetry form: the Wigner table of every |dJ| <= 1 pair
+        import synth
+        for jI, bI in enumerate(p.bases):
+            for jF, bF in enumerate(p.bases):
+                if abs(bF.J - bI.J) <= 1:
+                    eng.upload_wigner(jI, jF, synth.rotsym_levels(bI.J), synth.rotsym_levels(bF.J), 1,
+                                      synth.make_wigner(bI.J, bF.J, 1))

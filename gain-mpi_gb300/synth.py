@@ -83,7 +83,12 @@ def make_rotsym_basis(J: int, nv: int, maxdeg: int = 1) -> Basis:
     K = deg.reshape(-1).astype(np.int32)
     tau = lev.reshape(-1).astype(np.int32)
     vib = v.reshape(-1).astype(np.int32)
-    return Basis(J, nv, K, tau, vib, np.zeros(J + 1, np.int32), np.zeros(J + 1, np.int32))
+    kblock = np.zeros(J + 1, np.int32)
+    kstart = np.zeros(J + 1, np.int32)
+    if maxdeg == 1:   # every K (degeneracy index) is 0: one K-block holding all functions
+        kblock[0] = K.shape[0]
+        kstart[1:] = K.shape[0]
+    return Basis(J, nv, K, tau, vib, kstart, kblock)
 
 
 def rotsym_levels(J: int) -> int:
@@ -263,7 +268,7 @@ def make_problem(nv: int, jvals, rule: str = "c4", blocks=None, qr_device=None,
     isym_pairs = selection_of(rule)
     bases, infl, classes = [], [], []
     for J in jvals:
-        b = make_basis(J, nv)
+        b = make_rotsym_basis(J, nv) if rule == "c4r" else make_basis(J, nv)
         c = classes_of(b, rule)
         bases.append(b)
         classes.append(c)

@@ -137,6 +137,16 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
 gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int startF, int endF,
                                int ncontrF);
 
+/* GpuManager::TransferWigner (BaseClasses/GpuManager.cpp:440-478): the rotational matrix
+ * elements of the pair (J of jindI) -> (J of jindF), rot[d + 3 (lI + nlevelsI (lF + nlevelsF
+ * (dI + maxdeg dF)))], d = 0..2 (the Wigner::rot layout the rotsym kernel reads,
+ * GPU/dipole_GPU.cu:692).  Block pairs of these two J then run in the rotational-symmetry
+ * form (GpuManager::ExecuteRotSymHalfLs, :547-610): M is dense in K, and each function's tau
+ * is its rotational level index and K its degeneracy index (TroveBasisSet.cpp:480-483).
+ * Host array, copied.  The batched engine handles non-degenerate levels (maxdeg 1). */
+gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI, int nlevelsF,
+                               int maxdeg, const double* rot);
+
 /* Eigenvectors of one (J, Gamma) block kept resident (the reference re-uploads one vector
  * per transition, GpuManager::UpdateEigenVector, :537-545): vecs[level*nsize + c].  Host
  * array (pinned memory transfers fastest), copied synchronously. */
