@@ -40,9 +40,7 @@ inline void check_cuda(cudaError_t e, const char* what) {
 class GpuManager {
    public:
     // GpuManager(int pgpu_id, int nprocs, bool rotsym), BaseClasses/GpuManager.cpp:69
-    GpuManager(int gpu_id, int nprocs, bool rotsym = false) : gpu_id_(gpu_id), nprocs_(nprocs) {
-        if (rotsym) throw Error(GAIN_ERR_UNSUPPORTED, "ROTSYM EULER half line strength is not built");
-    }
+    GpuManager(int gpu_id, int nprocs, bool rotsym = false) : gpu_id_(gpu_id), nprocs_(nprocs), rotsym_(rotsym) {}
     ~GpuManager() { release(); }
     GpuManager(const GpuManager&) = delete;
     GpuManager& operator=(const GpuManager&) = delete;
@@ -80,6 +78,8 @@ class GpuManager {
         std::vector<int> tau(ktau, ktau + dimen);
         for (auto& t : tau) t &= 1;
         b.tau = upload(tau.data(), tau.size());
+        b.K = upload(K, dimen);          // rotsym form: degeneracy index
+        b.lev = upload(ktau, dimen);     // rotsym form: rotational level index
         b.vib = upload(vib, dimen);
         b.kblock = upload(kblock, J + 1);
         b.host_kblock.assign(kblock, kblock + J + 1);
@@ -124,6 +124,25 @@ class GpuManager {
         cudaFree(dipole_);
         dipole_ = upload(piece, (size_t)3 * N * ncontrF);
         doing_half_ls_ = true;
+    }
+
+    // BaseClasses/GpuManager.cpp:440-478: the Wigner tables of the last basis set, indexed by
+    // dJ = J' - J'' + 1 (entries with rot == NULL are absent); WignerT has the reference
+    // Wigner fields rot, nlevelsI, nlevelsF (common/Wigner.h)
+    template <class WignerT>
+    void TransferWigner(const std::vector<WignerT>& w) {
+        if (!rotsym_) return;
+        std::vector<Wigner> row(3);
+        for (size_t dj = 0; dj < w.size() && dj < 3; ++dj) {
+            if (!w[dj].rot) continue;
+            Wigner& x = row[dj];
+            x.nI = w[dj].nlevelsI;
+            x.nF = w[dj].nlevelsF;
+            const size_t n = (size_t)3 * x.nI * x.nF * maxdeg_ * maxdeg_;
+            x.host.assign(w[dj].rot, w[dj].rot + n);
+            x.rot = upload(w[dj].rot, n);
+        }
+        wigner_.push_back(row);
     }
 
     // BaseClasses/GpuManager.cpp:267-378
@@ -180,6 +199,14 @@ class GpuManager {
         check(gain_expand(bI.dimen, igammaI, fI.maxcoeff, idegI, fI.sdeg[igammaI], fI.Ntot[igammaI], fI.ijterms,
                           fI.icontr, fI.N[igammaI], fI.repres[igammaI], vectorI_, prim_half_ls_[indF][idegI],
                           nullptr));
+        if (rotsym_) {   // ExecuteRotSymHalfLs, :547-610
+            const Wigner& w = wigner_at(indI, bF.J - bI.J + 1);
+            check(gain_hls_rotsym(bF.dimen, bI.dimen, w.nI, w.nF, maxdeg_, bI.K, bF.K, bI.lev, bF.lev, bI.vib, bF.vib,
+                                  startF_, endF_, ncontrF_, dipole_, w.rot, prim_half_ls_[indF][idegI],
+                                  half_ls_[indF][idegI], dipN_, nullptr));
+            check_cuda(cudaDeviceSynchronize(), "ExecuteHalfLs");
+            return;
+        }
         for (int kF = 0; kF < bF.J + 1; ++kF)
             check(gain_hls_kblock(bF.host_kblock[kF], bI.dimen, bI.J, bF.J, kF, bI.tau, bF.tau, bI.vib, bF.vib,
                                   bF.kstart[kF], bI.kstart[std::max(kF - 1, 0)], startF_, endF_, ncontrF_,
@@ -222,6 +249,14 @@ class GpuManager {
         check(gain_upload_eigvecs(engine_, jind, gamma, nlevels, nsize, vecs));
     }
     gain_stats ExecuteBlockPair(const gain_pair_job& job, gain_path path, const gain_split_opts* opts = nullptr) {
+        if (rotsym_) {   // the pair's rotational matrix elements, once per (J'', J') pair
+            const int key = job.jindI * 100000 + job.jindF;
+            if (std::find(wigner_sent_.begin(), wigner_sent_.end(), key) == wigner_sent_.end()) {
+                const Wigner& w = wigner_at(job.jindI, bases_.at(job.jindF).J - bases_.at(job.jindI).J + 1);
+                check(gain_upload_wigner(engine_, job.jindI, job.jindF, w.nI, w.nF, maxdeg_, w.host.data()));
+                wigner_sent_.push_back(key);
+            }
+        }
         gain_stats st{};
         check(gain_run_pair(engine_, &job, path, opts, &st));
         return st;
@@ -231,9 +266,19 @@ class GpuManager {
    private:
     struct Basis {
         int J = 0, dimen = 0;
-        int *tau = nullptr, *vib = nullptr, *kblock = nullptr;
+        int *tau = nullptr, *vib = nullptr, *kblock = nullptr, *K = nullptr, *lev = nullptr;
         std::vector<int> host_kblock, kstart;
     };
+    struct Wigner {
+        int nI = 0, nF = 0;
+        double* rot = nullptr;
+        std::vector<double> host;
+    };
+    const Wigner& wigner_at(int indI, int dj) const {
+        if (indI < 0 || indI >= (int)wigner_.size() || dj < 0 || dj > 2 || !wigner_[indI][dj].rot)
+            throw Error(GAIN_ERR_NOT_READY, "no Wigner table for this basis pair (TransferWigner)");
+        return wigner_[indI][dj];
+    }
     struct Inflation {
         int maxcoeff = 0;
         int *ijterms = nullptr, *icontr = nullptr;
@@ -275,6 +320,9 @@ class GpuManager {
     }
 
     int gpu_id_, nprocs_;
+    bool rotsym_ = false;
+    std::vector<std::vector<Wigner>> wigner_;
+    std::vector<int> wigner_sent_;
     int jmax_ = 0, nsym_ = 0, maxdeg_ = 1;
     gain_engine engine_ = nullptr;
     double* threej_ = nullptr;

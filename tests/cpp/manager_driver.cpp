@@ -8,6 +8,8 @@
 //                     icontr[2 dimen], ijterms[dimen nsym], N[nsym][dimen], Ntot[nsym]
 //   doubles: dipole piece [3 nv (endF-startF)], lower vectors [nlower NtotI],
 //            upper vectors [nupper NtotF]
+//   optional: int rotsym (1), ints nlevelsI nlevelsF, doubles rot[3 nlevelsI nlevelsF] -- the
+//             rotational-symmetry form, with the Wigner table of the pair JI -> JF
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -19,6 +21,7 @@ FILE* fin;
 int geti() { int v; if (fread(&v, 4, 1, fin) != 1) { fprintf(stderr, "short read\n"); exit(2); } return v; }
 std::vector<int> getiv(size_t n) { std::vector<int> v(n); if (n && fread(v.data(), 4, n, fin) != n) exit(2); return v; }
 std::vector<double> getdv(size_t n) { std::vector<double> v(n); if (n && fread(v.data(), 8, n, fin) != n) exit(2); return v; }
+struct Wig { double* rot; int nlevelsI, nlevelsF; };   // the fields of the reference's Wigner
 struct J { int J, dimen; std::vector<int> K, ktau, vib, kblock, kstart, icontr, ijterms, Ntot; std::vector<std::vector<int>> N; };
 }
 
@@ -42,15 +45,27 @@ int main(int argc, char** argv) {
     std::vector<double> piece = getdv((size_t)3 * nv * (endF - startF));
     std::vector<double> vl = getdv((size_t)nlower * js[0].Ntot[gI]);
     std::vector<double> vu = getdv((size_t)nupper * js[1].Ntot[gF]);
+    int rotsym = 0, nlevI = 0, nlevF = 0;
+    std::vector<double> rot;
+    if (fread(&rotsym, 4, 1, fin) == 1 && rotsym) {
+        nlevI = geti();
+        nlevF = geti();
+        rot = getdv((size_t)3 * nlevI * nlevF);
+    }
     fclose(fin);
     try {
-        gain::GpuManager gpu(0, 1);
+        gain::GpuManager gpu(0, 1, rotsym != 0);
         gpu.InitializeAndTransferConstants(jmax, nsym, 1);
         gpu.TransferDipole(piece.data(), nv, startF, endF, endF - startF);
         int dimen_max = 0, nsize_max = 0;
         for (int t = 0; t < 2; ++t) {
             J& j = js[t];
             gpu.TransferBasisSet(j.J, j.dimen, j.K.data(), j.ktau.data(), j.vib.data(), j.kblock.data(), j.kstart.data());
+            if (rotsym) {   // main.cpp:193, after each basis set: its tables by dJ = J' - J + 1
+                std::vector<Wig> w(3, Wig{nullptr, 0, 0});
+                if (t == 0) w[JF - JI + 1] = Wig{rot.data(), nlevI, nlevF};
+                gpu.TransferWigner(w);
+            }
             std::vector<double*> repres;
             std::vector<std::vector<double>> ones;
             std::vector<int*> N;

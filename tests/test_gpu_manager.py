@@ -47,6 +47,59 @@ def driver(built_lib, tmp_path_factory):
     return out
 
 
+def _write_rotsym_input(path, p, jI, gI, jF, gF, nlower, nupper, block):
+    """A rotsym block pair of a synth problem (rule c4r), with the Wigner table record."""
+    import synth
+    bI, bF = p.bases[jI], p.bases[jF]
+    s, e = block
+    nv = p.dipole.shape[-1]
+    ints = [nv, 11, p.nsym, bI.J, bF.J, gI, gF, nlower, nupper, s, e]
+    with open(path, "wb") as f:
+        f.write(np.asarray(ints, np.int32).tobytes())
+        for jind in (jI, jF):
+            b, inf = p.bases[jind], p.infl[jind]
+            f.write(np.asarray([b.dimen], np.int32).tobytes())
+            for a in (b.K, b.tau, b.vib, b.kblock, b.kstart, inf.icontr, inf.ijterms):
+                f.write(np.ascontiguousarray(a, np.int32).tobytes())
+            for g in range(p.nsym):
+                f.write(np.ascontiguousarray(inf.N[g], np.int32).tobytes())
+            f.write(np.ascontiguousarray(inf.Ntot, np.int32).tobytes())
+        f.write(np.ascontiguousarray(p.dipole[:, :, s:e]).tobytes())
+        f.write(np.ascontiguousarray(p.blocks[(jI, gI)].vecs[:nlower]).tobytes())
+        f.write(np.ascontiguousarray(p.blocks[(jF, gF)].vecs[:nupper]).tobytes())
+        nI, nF = synth.rotsym_levels(bI.J), synth.rotsym_levels(bF.J)
+        f.write(np.asarray([1, nI, nF], np.int32).tobytes())
+        f.write(np.ascontiguousarray(synth.make_wigner(bI.J, bF.J, 1)).tobytes())
+
+
+@pytest.mark.parametrize("block", [None, (3, 10)])
+def test_manager_rotsym_loop_matches_oracle(driver, tmp_path, block):
+    """GpuManager(rotsym=true): TransferWigner after each basis set, ExecuteHalfLs through the
+    rotsym drop-in, against the oracle's reference-order restatement of the same loop."""
+    import oracle
+    import synth
+    p = synth.make_problem(12, [2, 3], "c4r", blocks=[(2, 0), (3, 1)])
+    blk = block or (0, 12)
+    nlower, nupper = 6, 12
+    inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_rotsym_input(inp, p, 0, 0, 1, 1, nlower, nupper, blk)
+    subprocess.run([driver, inp, outp], check=True, timeout=120)
+    amp = np.fromfile(outp, np.float64).reshape(nlower, nupper)
+    bI, bF, iI, iF = p.bases[0], p.bases[1], p.infl[0], p.infl[1]
+    s, e = blk
+    piece = np.ascontiguousarray(p.dipole[:, :, s:e]).reshape(-1)
+    wig = synth.make_wigner(bI.J, bF.J, 1)
+    ref = np.zeros_like(amp)
+    for l in range(nlower):
+        prim = oracle.expand(iI, 0, p.blocks[(0, 0)].vecs[l])
+        h = np.zeros(bF.dimen)
+        oracle.hls_rotsym(bI, bF, synth.rotsym_levels(bI.J), synth.rotsym_levels(bF.J), 1, piece, 12, (s, e, e - s),
+                          wig, prim, h)
+        for u in range(nupper):
+            ref[l, u] = oracle.dot(oracle.expand(iF, 1, p.blocks[(1, 1)].vecs[u]), h)
+    assert np.max(np.abs(amp - ref)) <= 1e-14 * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("name", ["c4_dJp1", "c4_dJm1", "full_blocked", "c4_highJ"])
 def test_manager_loop_matches_reference(driver, tmp_path, name):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
