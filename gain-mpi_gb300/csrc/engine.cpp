@@ -250,6 +250,8 @@ struct gain_engine_s {
     // work buffers
     gain::DevArray<int> d_lower, d_upper;
     gain::DevArray<double> primI, hprim, hsym;
+    gain::DevArray<double> adj_dLdS, adj_G, adj_dH, adj_dh, adj_vp, adj_dmu;   // adjoint work space
+    gain::DevArray<int> adj_iota;
     gain::DevArray<__nv_bfloat16> Vdig, Hdig, Udig;
     gain::StatsDev Vst, Hst, Ust;
     gain::DevArray<double> H;
@@ -1324,6 +1326,96 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
     GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyHostToDevice,
                               e->stc));
     GAIN_CUDA(cudaEventRecord(slot->ready, e->stc));
+    return GAIN_OK;
+}
+
+gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
+                              gain_stats* stats) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    GAIN_TRY(validate_job(e, job));
+    if (!dL_dS || !dL_dmu) return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair: NULL argument");
+    if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: non-degenerate symmetries only");
+    e->have_amp = false;
+    // forward amplitudes of the pair in FP64 (the reference's method)
+    GAIN_TRY(run_plain(e, job, nullptr));
+    const Basis& bI = e->bases[job->jindI];
+    const Basis& bF = e->bases[job->jindF];
+    Inflation& iI = e->infl[job->jindI];
+    Inflation& iF = e->infl[job->jindF];
+    const Eig& EI = *e->eig[{job->jindI, job->gammaI}];
+    const Eig& EF = *e->eig[{job->jindF, job->gammaF}];
+    const int B = job->nlower, Nu = job->nupper, NtF = iF.Ntot[job->gammaF];
+    const size_t nS = (size_t)B * Nu, nmu = (size_t)3 * e->dipN * e->ncontrF;
+    cudaStream_t st = e->st;
+    GAIN_TRY(e->adj_dLdS.upload(dL_dS, nS));
+    GAIN_TRY(e->adj_G.alloc(nS));
+    GAIN_TRY(e->adj_dH.alloc((size_t)B * NtF));
+    GAIN_TRY(e->adj_dh.alloc((size_t)B * bF.dimen));
+    GAIN_TRY(e->adj_vp.alloc((size_t)B * bI.dimen));
+    GAIN_TRY(e->adj_dmu.alloc(nmu));
+    GAIN_TRY(e->adj_dmu.zero(st, nmu));
+    std::vector<int> iota(B);
+    for (int b = 0; b < B; ++b) iota[b] = b;
+    GAIN_TRY(e->adj_iota.upload(iota));
+    GAIN_CUDA(cudaEventRecord(e->ev[0], st));
+    // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dL/dH
+    GAIN_CUDA(launch_adj_scale((long)nS, e->adj_dLdS.p, e->amp.p, e->adj_G.p, st));
+    GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, e->adj_G.p, Nu, EF.d.p, EF.nsize, e->d_upper.p, e->adj_dH.p, NtF, st));
+    GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF, iF.dijterms.p,
+                                   iF.dicontr.p, iF.dN[job->gammaF]->p, iF.drepres[job->gammaF]->p, e->adj_dH.p, NtF,
+                                   e->adj_iota.p, e->adj_dh.p, bF.dimen, B, st));
+    // lower vectors in primitive space, then dL/dmu from the band (or dense) products
+    GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, 0, iI.sdeg[job->gammaI], iI.Ntot[job->gammaI],
+                                   iI.dijterms.p, iI.dicontr.p, iI.dN[job->gammaI]->p, iI.drepres[job->gammaI]->p,
+                                   EI.d.p, EI.nsize, e->d_lower.p, e->adj_vp.p, bI.dimen, B, st));
+    AdjArgs a;
+    memset(&a, 0, sizeof a);
+    a.dimF = bF.dimen;
+    a.dimI = bI.dimen;
+    a.nb = B;
+    a.vibF = bF.dvib.p;
+    a.vibI = bI.dvib.p;
+    a.KF = bF.dK.p;
+    a.KI = bI.dK.p;
+    a.tauF = bF.dtau.p;
+    a.tauI = bI.dtau.p;
+    a.levF = bF.dlev.p;
+    a.levI = bI.dlev.p;
+    a.jI = bI.J;
+    a.jF = bF.J;
+    a.jmax = e->jmax;
+    a.threej = e->d3j.p;
+    if (const WignerTab* wt = wigner_of(e, job->jindI, job->jindF)) {
+        a.wigner = wt->rot.p;
+        a.nlevelI = wt->nI;
+        a.nlevelF = wt->nF;
+        a.maxdeg = wt->maxdeg;
+    }
+    a.startF = e->startF;
+    a.endF = e->endF;
+    a.ncontrF = e->ncontrF;
+    a.dipN = e->dipN;
+    a.dh = e->adj_dh.p;
+    a.ld_dh = bF.dimen;
+    a.vp = e->adj_vp.p;
+    a.ld_vp = bI.dimen;
+    a.dmu = e->adj_dmu.p;
+    GAIN_CUDA(launch_adj_dmu(a, st));
+    GAIN_CUDA(cudaEventRecord(e->ev[1], st));
+    std::vector<double> h(nmu);
+    GAIN_CUDA(cudaMemcpyAsync(h.data(), e->adj_dmu.p, sizeof(double) * nmu, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < nmu; ++i) dL_dmu[i] += h[i];
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
+        stats->device_ms = ms;
+        stats->rows = B;
+        stats->cols = Nu;
+        stats->kernel_launches = 5;
+    }
     return GAIN_OK;
 }
 

@@ -43,6 +43,26 @@ cudaError_t launch_expand(int dimen, int igamma, int maxcoeff, int ideg, int sde
                           const int* ijterms, const int* icontr, const int* N,
                           const double* repres, const double* vecI, double* vec, cudaStream_t st);
 cudaError_t launch_dot(int n, const double* x, const double* y, double* result, cudaStream_t st);
+// ---------------------------------------------------------------- adjoint (adjoint.cu)
+struct AdjArgs {
+    int dimF, dimI, nb;                        // primitive dimensions, lower states
+    const int *vibF, *vibI, *KF, *KI, *tauF, *tauI, *levF, *levI;
+    int jI, jF, jmax;
+    const double* threej;
+    const double* wigner;                      // non-null: rotational-symmetry form
+    int nlevelI, nlevelF, maxdeg;
+    int startF, endF, ncontrF, dipN;
+    const double* dh;                          // [nb][ld_dh] dL/dh, primitive upper index
+    long ld_dh;
+    const double* vp;                          // [nb][ld_vp] lower vectors, primitive index
+    long ld_vp;
+    double* dmu;                               // [3][dipN][ncontrF] accumulated
+};
+cudaError_t launch_adj_scale(long n, const double* dLdS, const double* amp, double* G, cudaStream_t st);
+cudaError_t launch_adj_gemm(int M, int N, int K, const double* A, long lda, const double* B, long ldb,
+                            const int* levels, double* C, long ldc, cudaStream_t st);
+cudaError_t launch_adj_dmu(const AdjArgs& a, cudaStream_t st);
+
 cudaError_t launch_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI,
                               const int* kF, const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF,
                               int startFblock, int endFblock, int ncontrF, const double* dipole_me, int dip_stride,

@@ -182,6 +182,7 @@ def _declare(L):
     L.gain_upload_dipole.argtypes = [_vp, _dp, I, I, I, I]
     L.gain_upload_eigvecs.argtypes = [_vp, I, I, I, I, _dp]
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
+    L.gain_adjoint_pair.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.POINTER(Stats)]
     L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
     L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
@@ -203,7 +204,7 @@ def _declare(L):
     L.gain_plan_pairs.restype = S
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
-                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines"):
         getattr(L, name).restype = S
 
@@ -345,6 +346,21 @@ class Engine:
             if raise_on_error:
                 check(s)
         return out
+
+    def adjoint(self, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, dL_dS, dL_dmu=None):
+        """dL/dmu (the dipole piece's layout [3][N][ncontrF], accumulated into dL_dmu if given)
+        of a loss with gradient dL_dS [nlower, nupper] over the pair's line strengths."""
+        lo, up = _i32(lower_levels), _i32(upper_levels)
+        g = _f64(dL_dS)
+        assert g.size == len(lo) * len(up)
+        if dL_dmu is None:
+            raise ValueError("dL_dmu: a float64 array of the uploaded dipole piece's size")
+        assert dL_dmu.dtype == np.float64 and dL_dmu.flags.c_contiguous
+        job = PairJob(jindI, gammaI, jindF, gammaF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
+        st = Stats()
+        check(lib().gain_adjoint_pair(self.h, ctypes.byref(job), _p(g, _dp), _p(dL_dmu, _dp), ctypes.byref(st)))
+        self._shape = (len(lo), len(up))
+        return dL_dmu
 
     def amp_device(self):
         p, ld = ctypes.c_void_p(), ctypes.c_int()

@@ -212,6 +212,17 @@ typedef struct gain_stats {
     double tensor_flops;        /* BF16 MMA flops issued by the two GEMMs (no padding) */
 } gain_stats;
 
+/* Adjoint of one block pair (no counterpart in the reference): for a loss L over the line
+ * strengths S = amp^2 of the pair, given dL_dS[l*nupper + u] (host, job order), ADD dL/dmu to
+ * dL_dmu (host, the uploaded dipole piece's layout: [d][vibI][vibF - startF], 3 N ncontrF
+ * doubles).  It runs the pair's FP64 forward (the plain path, so gain_fetch_amp returns its
+ * amplitudes) and the adjoint chain in FP64: dL/damp = 2 amp dL/dS, dL/dH = dL/damp U,
+ * dL/dh = T_F dL/dH, dL/dM = dL/dh^T v and the scatter of dL/dM into mu through the half line
+ * strength's per-element factors (K-block or rotational-symmetry form).  Non-degenerate
+ * symmetries (maxdeg 1). */
+gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const double* dL_dS,
+                              double* dL_dmu, gain_stats* stats);
+
 /* Compute amplitudes amp[l][u] = <upper u | mu . rot | lower l> for one block pair into an
  * engine-owned device matrix (row-major; its pointer and leading dimension come from
  * gain_pair_amp_device).  Blocks on completion.  opts may be NULL (defaults).  stats may be
