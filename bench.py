@@ -50,6 +50,15 @@ def parse():
     ap.add_argument("--precision-sweep", action="store_true",
                     help="accuracy of each digit configuration of the amplitude GEMM against the "
                          "double-double oracle (one JSON line per configuration)")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="gradient of a line-strength loss over all block pairs of J=0..5, checked "
+                         "against central differences (one JSON line)")
+    ap.add_argument("--adj-nv", type=int, default=1000, help="vibrational basis size of --adjoint")
+    ap.add_argument("--adj-fd", type=int, default=200, help="entries checked by central differences")
+    ap.add_argument("--batch", action="store_true",
+                    help="every allowed block pair of J=0..--batch-jmax through the split path (one JSON line)")
+    ap.add_argument("--batch-nv", type=int, default=200, help="vibrational basis size of --batch")
+    ap.add_argument("--batch-jmax", type=int, default=30, help="largest J of --batch")
     return ap.parse_args()
 
 
@@ -201,6 +210,42 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def line_text_bench(eng, inp, steps: int) -> dict:
+    """The line list of the last run as text (Output.cpp:99-111 format, intensity column on),
+    built on the device and copied into page-locked host memory; wall time per call."""
+    import torch
+    text, nl = eng.lines_text(inp["eI"], inp["eF"], JI, JF, GI, GF)
+    host = torch.empty(max(1, len(text)), dtype=torch.uint8, pin_memory=True)
+    _PINNED.append(host)
+    buf = host.numpy()
+    ms = []
+    for i in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, nl = eng.lines_text(inp["eI"], inp["eF"], JI, JF, GI, GF, out=buf)
+        if i:
+            ms.append((time.perf_counter() - t0) * 1e3)
+    m = float(np.median(ms))
+    return {"lines": int(nl), "bytes": len(text), "ms": m, "lines_per_s": nl / (m * 1e-3),
+            "GB_per_s": len(text) / (m * 1e-3) / 1e9, "includes": "S/A/I, text on the device, copy to pinned host"}
+
+
+def cpu_text_baseline(eng, inp, rows: int) -> dict:
+    """The reference's sprintf/fprintf text (Output.cpp:52-112, restated in the oracle) of
+    the first rows lower states of the last run's amplitudes, one host thread."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    amp = eng.fetch_amp()[:rows].copy()
+    NU = amp.shape[1]
+    t0 = time.perf_counter()
+    text, nl = oracle.line_list(amp, inp["eI"][:rows], inp["eF"], list(range(rows)), list(range(NU)), JI, JF,
+                                GI, GF)
+    secs = time.perf_counter() - t0
+    return {"lines_per_s": nl / secs, "cores": 1, "kind": "port",
+            "sample": f"{rows} lower states x {NU} upper states ({nl} lines, {len(text)} bytes)"}
+
+
 # ------------------------------------------------------------------------- CPU baseline
 def cpu_baseline(inp, n_sample: int):
     """The reference's FP64 formula restated in C (oracle), OpenMP over upper states as in
@@ -295,6 +340,228 @@ def precision_sweep(args):
                       "domain": "S > 1e-10 S_max"}), flush=True)
 
 
+class _DeviceMatrix:
+    """A read view of an engine's device amplitude matrix for torch (no copy)."""
+
+    def __init__(self, ptr: int, rows: int, cols: int, ld: int):
+        self.__cuda_array_interface__ = {"shape": (rows, cols), "strides": (8 * ld, 8), "typestr": "<f8",
+                                         "data": (ptr, False), "version": 3, "stream": None}
+
+
+def adjoint_check(args):
+    """Gradient of a line-strength loss with respect to the dipole matrix elements.
+
+    All allowed block pairs of J = 0..5 (the reference's intensity filter with open energy and
+    frequency windows, J = J_max pairs excluded).  L = sum w (log S - log S_t)^2, S_t the line
+    strengths of a dipole perturbed elementwise by mu (1 + 0.01 N(0,1)) (seed 77); w = 1 on the
+    lines with S_t > 1e-10 max S_t and S > 1e-10 max S (a fixed mask: a line whose strength is
+    near zero has an unbounded log derivative).  dL/dmu comes from gain_adjoint_pair summed
+    over the pairs (FP64) and is checked on random entries with a non-zero gradient (seed 78)
+    and along random directions against (a) central differences of L (plain FP64 forwards,
+    h = 1e-6) and (b) the exact directional derivative: amp is linear in mu, so
+    dL/dmu . d = sum dL/dS 2 amp amp(d) with amp(d) the forward pass of the dipole d (one
+    plain FP64 forward per entry or direction, no step-size error).  One JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    import gainls
+    import synth
+    nv = args.adj_nv
+    t0 = time.perf_counter()
+    p = synth.make_problem(nv, list(range(6)), "c4", qr_device="cuda")
+    eng = gainls.Engine(5, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    filt = gainls.make_filters([1.0] * p.nsym, p.isym_pairs, p.igamma_pair, p.sym_degen, (-1e9, 1e9),
+                               (-1e9, 1e9), (-1e9, 1e9), 0.0, 5)
+    table = gainls.state_table(p.st_energy, p.st_J, p.st_jind, p.st_gamma, p.st_ndeg, p.st_ilevel)
+    pairs = gainls.plan_pairs(filt, table)
+    setup_s = time.perf_counter() - t0
+    mu0 = np.ascontiguousarray(p.dipole)
+    n_lines = sum(len(lo) * len(up) for *_, lo, up in pairs)
+
+    def amp_now(lo, up):
+        ptr, ld = eng.amp_device()
+        return torch.as_tensor(_DeviceMatrix(ptr, len(lo), len(up), ld), device="cuda")
+
+    def forward(mu, path=gainls.PATH_PLAIN_FP64, keep=False):
+        eng.upload_dipole(mu.reshape(-1), nv, 0, nv, nv)
+        out = []
+        for jI, gI, jF, gF, lo, up in pairs:
+            eng.run_pair(jI, gI, jF, gF, lo, up, path)
+            if keep:
+                out.append(amp_now(lo, up).clone())
+        torch.cuda.synchronize()
+        return out
+
+    # the target and the reference point
+    mu_t = mu0 * (1.0 + 0.01 * np.random.default_rng(77).standard_normal(mu0.shape))
+    S_t = [a * a for a in forward(mu_t, keep=True)]
+    S_0 = [a * a for a in forward(mu0, keep=True)]
+    smax_t = max(float(s.max()) for s in S_t)
+    smax_0 = max(float(s.max()) for s in S_0)
+    masks = [(st > 1e-10 * smax_t) & (s0 > 1e-10 * smax_0) for st, s0 in zip(S_t, S_0)]
+    logS_t = [torch.log(torch.where(m, st, torch.ones_like(st))) for st, m in zip(S_t, masks)]
+    del S_t
+
+    def loss(mu):
+        eng.upload_dipole(mu.reshape(-1), nv, 0, nv, nv)
+        total = torch.zeros((), dtype=torch.float64, device="cuda")
+        for (jI, gI, jF, gF, lo, up), m, lt in zip(pairs, masks, logS_t):
+            eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_PLAIN_FP64)
+            a = amp_now(lo, up)
+            d = torch.where(m, torch.log(a * a) - lt, torch.zeros_like(lt))
+            total += torch.sum(d * d)
+            torch.cuda.synchronize()   # the next run overwrites the amplitudes
+        return float(total)
+
+    # forward times over all pairs: plain FP64 and split paths
+    times = {}
+    for name, path in (("plain_fp64", gainls.PATH_PLAIN_FP64), ("split", gainls.PATH_SPLIT)):
+        forward(mu0, path)
+        t1 = time.perf_counter()
+        forward(mu0, path)
+        times[f"forward_{name}_s"] = time.perf_counter() - t1
+    # dL/dS at mu0, then the adjoint of every pair
+    amp0 = forward(mu0, keep=True)
+    dLdS_dev = []
+    for s0, m, lt in zip(S_0, masks, logS_t):
+        dLdS_dev.append(torch.where(m, 2.0 * (torch.log(s0) - lt) / s0, torch.zeros_like(s0)))
+    dLdS = [g.cpu().numpy() for g in dLdS_dev]
+    del S_0
+
+    def jvp(d):
+        """Exact dL/dmu . d from the forward pass of the dipole d (amp is linear in mu)."""
+        eng.upload_dipole(np.ascontiguousarray(d).reshape(-1), nv, 0, nv, nv)
+        total = torch.zeros((), dtype=torch.float64, device="cuda")
+        for (jI, gI, jF, gF, lo, up), g, a0 in zip(pairs, dLdS_dev, amp0):
+            eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_PLAIN_FP64)
+            total += torch.sum(g * 2.0 * a0 * amp_now(lo, up))
+            torch.cuda.synchronize()
+        return float(total)
+    L0 = loss(mu0)
+    grad = np.zeros(mu0.size)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for (jI, gI, jF, gF, lo, up), g in zip(pairs, dLdS):
+        eng.adjoint(jI, gI, jF, gF, lo, up, g, grad)
+    times["adjoint_s"] = time.perf_counter() - t1
+    grad = grad.reshape(mu0.shape)
+
+    # central differences
+    h = 1e-6
+    rng = np.random.default_rng(78)
+    gflat = grad.reshape(-1)
+    gmax = float(np.abs(gflat).max())
+    cand = np.flatnonzero(np.abs(gflat) > 0)
+    picks = rng.choice(cand, size=min(args.adj_fd, cand.size), replace=False)
+    rel, absn, jrel = [], [], []
+    t1 = time.perf_counter()
+    for k in picks:
+        mp, mm = mu0.copy(), mu0.copy()
+        mp.reshape(-1)[k] += h
+        mm.reshape(-1)[k] -= h
+        fd = (loss(mp) - loss(mm)) / (2 * h)
+        rel.append(abs(fd - gflat[k]) / abs(gflat[k]))
+        absn.append(abs(fd - gflat[k]) / gmax)
+    times["fd_s"] = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    for k in picks:
+        e = np.zeros(mu0.size)
+        e[k] = 1.0
+        jrel.append(abs(jvp(e) - gflat[k]) / abs(gflat[k]))
+    times["jvp_s"] = time.perf_counter() - t1
+    dirs, jdirs = [], []
+    for _ in range(3):
+        d = rng.standard_normal(mu0.shape)
+        gd = float(np.sum(grad * d))
+        fd = (loss(mu0 + h * d) - loss(mu0 - h * d)) / (2 * h)
+        dirs.append(abs(fd - gd) / abs(gd))
+        jdirs.append(abs(jvp(d) - gd) / abs(gd))
+    rel, jrel = np.asarray(rel), np.asarray(jrel)
+    out = {"mode": "adjoint", "workload": f"N_v={nv}, J=0..5, all allowed block pairs",
+           "pairs": len(pairs), "lines": n_lines, "lines_in_loss": int(sum(int(m.sum()) for m in masks)),
+           "loss": L0, "gradient_dtype": "f64", "fd_step": h, "fd_entries": int(len(picks)),
+           "fd_max_rel_err": float(rel.max()), "fd_median_rel_err": float(np.median(rel)),
+           "fd_p99_rel_err": float(np.quantile(rel, 0.99)),
+           "fd_max_err_over_max_grad": float(max(absn)), "fd_direction_rel_err": [float(x) for x in dirs],
+           "exact_partials_max_rel_err": float(jrel.max()), "exact_partials_median_rel_err": float(np.median(jrel)),
+           "exact_direction_rel_err": [float(x) for x in jdirs],
+           "nonzero_gradient_entries": int(cand.size), "gradient_entries": int(mu0.size),
+           "setup_s": setup_s}
+    out.update(times)
+    print(json.dumps(out), flush=True)
+    eng.close()
+
+
+def batch_plan(args):
+    """Many block pairs: every allowed (J'', Gamma'') -> (J', Gamma') pair of J = 0..jmax, four
+    symmetries, lower states below 4000 cm^-1 against every upper state (the reference's
+    intensity filter; J = J_max pairs excluded), run one after another through the split
+    path and once through the plain FP64 path.  One JSON line: transitions per second over
+    the whole plan (device time and wall time), the time of the largest pairs, and the
+    accuracy of S against the plain path."""
+    import torch
+    torch.cuda.set_device(0)
+    import gainls
+    import synth
+    nv, jmax = args.batch_nv, args.batch_jmax
+    t0 = time.perf_counter()
+    p = synth.make_problem(nv, list(range(jmax + 1)), "c4", qr_device="cuda")
+    eng = gainls.Engine(jmax, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    filt = gainls.make_filters([1.0] * p.nsym, p.isym_pairs, p.igamma_pair, p.sym_degen, (0.0, 4000.0),
+                               (-1e9, 1e9), (-1e9, 1e9), 0.0, jmax)
+    table = gainls.state_table(p.st_energy, p.st_J, p.st_jind, p.st_gamma, p.st_ndeg, p.st_ilevel)
+    pairs = gainls.plan_pairs(filt, table)
+    setup_s = time.perf_counter() - t0
+    trans = [len(lo) * len(up) for *_, lo, up in pairs]
+    total = int(sum(trans))
+
+    def sweep(path):
+        dev, amps = [], []
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for jI, gI, jF, gF, lo, up in pairs:
+            st = eng.run_pair(jI, gI, jF, gF, lo, up, path)
+            dev.append(st["device_ms"])
+        torch.cuda.synchronize()
+        return dev, (time.perf_counter() - w0) * 1e3
+
+    for _ in range(max(1, args.warmup)):
+        sweep(gainls.PATH_SPLIT)
+    runs = [sweep(gainls.PATH_SPLIT) for _ in range(max(1, args.steps))]
+    dev_ms = [float(np.sum(d)) for d, _ in runs]
+    wall_ms = [w for _, w in runs]
+    per_pair = np.median(np.array([d for d, _ in runs]), axis=0)
+    # accuracy and time of the plain FP64 path, pair by pair
+    worst, plain_ms, nchk = 0.0, 0.0, 0
+    for (jI, gI, jF, gF, lo, up) in pairs:
+        eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_SPLIT)
+        a = eng.fetch_amp().copy()
+        st = eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_PLAIN_FP64)
+        plain_ms += st["device_ms"]
+        r = eng.fetch_amp()
+        S, Sr = a * a, r * r
+        m = Sr > 1e-10 * Sr.max()
+        if m.any():
+            worst = max(worst, float(np.max(np.abs(S[m] - Sr[m]) / Sr[m])))
+            nchk += int(m.sum())
+    order = np.argsort(-per_pair)[:5]
+    out = {"mode": "batch", "workload": f"N_v={nv}, J=0..{jmax}, 4 symmetries, all allowed block pairs, "
+                                        "lower states E < 4000 cm^-1 x all upper states",
+           "pairs": len(pairs), "transitions": total, "setup_s": setup_s,
+           "split_device_ms": float(np.median(dev_ms)), "split_wall_ms": float(np.median(wall_ms)),
+           "transitions_per_s_device": total / (np.median(dev_ms) * 1e-3),
+           "transitions_per_s_wall": total / (np.median(wall_ms) * 1e-3),
+           "plain_fp64_device_ms": plain_ms, "speedup_vs_plain_fp64": plain_ms / float(np.median(dev_ms)),
+           "max_rel_err_S_vs_plain": worst, "lines_checked": nchk, "domain": "S > 1e-10 S_max of each pair",
+           "largest_pairs": [{"pair": list(pairs[i][:4]), "lower": len(pairs[i][4]), "upper": len(pairs[i][5]),
+                              "ms": float(per_pair[i])} for i in order],
+           "pairs_under_1M_transitions_ms": float(np.sum([per_pair[i] for i in range(len(pairs))
+                                                          if trans[i] < 1_000_000]))}
+    print(json.dumps(out), flush=True)
+    eng.close()
+
+
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
@@ -323,6 +590,10 @@ def main():
     ws, rank, local = dist_info()
     if args.precision_sweep:
         return precision_sweep(args)
+    if args.adjoint:
+        return adjoint_check(args)
+    if args.batch:
+        return batch_plan(args)
     if args.impl == "reference":
         if ws > 1 and rank != 0:
             return
@@ -401,6 +672,7 @@ def main():
     e2e_step = float(np.median(e2e_ms))
     h2d = inp["vl"].nbytes + inp["vu"].nbytes
     d2h = 2 * B * NU * 8
+    text = line_text_bench(eng, inp, max(2, min(args.steps, 5)))
 
     peaks = {}
     try:
@@ -446,6 +718,9 @@ def main():
                "gpu_launches": int(st["kernel_launches"]) * args.steps,
                "gemm1_ms": float(np.median(g1)), "gemm2_ms": g2ms, "wall_ms_per_step": wall * 1e3 / args.steps,
                "tensor_flops_executed_per_step": st["tensor_flops"]}
+        if rank == 0 and not args.no_cpu:
+            text["cpu_snprintf"] = cpu_text_baseline(eng, inp, 16)
+        out["line_list_text"] = text
         out.update(extra)
         print(json.dumps(out), flush=True)
     eng.close()

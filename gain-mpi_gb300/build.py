@@ -18,8 +18,8 @@ OBJ = os.path.join(HERE, "_build", platform.machine())
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libgainls.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cpp", "threej.cpp", "states.cpp", "fp64_kernels.cu", "split.cu", "noalloc.cu", "adjoint.cu"]
-HEADERS = ["gain_internal.h", "split.h"]
+SOURCES = ["engine.cpp", "threej.cpp", "states.cpp", "fp64_kernels.cu", "split.cu", "noalloc.cu", "adjoint.cu", "linetext.cu"]
+HEADERS = ["gain_internal.h", "split.h", "linefmt.h", "linemath.cuh"]
 
 
 def nvcc() -> str:

@@ -264,6 +264,11 @@ struct gain_engine_s {
     gain::DevArray<gain::split::Prod> prods1, prods2;
     gain::DevArray<double> lineS, lineA, lineI, eIdev, eFdev;
     gain::DevArray<unsigned char> lineKeep;
+    gain::DevArray<uint32_t> textLens;
+    gain::DevArray<unsigned long long> textBlocks;   // block offsets, then [nblocks] total, [nblocks+1] lines
+    gain::DevArray<char> text;
+    unsigned long long text_bytes = 0;
+    bool have_text = false;
 
     gain::PairLayout layout;
     gain::PlainLayout plain;
@@ -998,6 +1003,24 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     return GAIN_OK;
 }
 
+// Output.cpp constants (ACOEF, CMCOEF, the radiation constant of beta) and the INTENSITY
+// block's parameters for one (J'', J') pair.
+LineParams line_params(const gain_line_params* prm, int jI, int jF, bool with_intensity) {
+    LineParams p;
+    p.acoef_2jI1 = 3.13618923e-7 * (double)(2 * jI + 1);
+    p.cmcoef = 1.327209365e-12;
+    p.gnsF = prm->gnsF;
+    p.two_jF1 = 2.0 * (double)jF + 1.0;
+    p.beta = 6.62606896e-27 * 2.99792458e+10 / (1.380658e-16 * prm->temperature);
+    p.zpe = prm->zpe;
+    p.q_part = prm->q_part;
+    p.thresh = prm->thresh;
+    p.freq_lo = prm->freq_lo;
+    p.freq_hi = prm->freq_hi;
+    p.with_intensity = with_intensity;
+    return p;
+}
+
 }  // namespace
 }  // namespace gain
 
@@ -1473,18 +1496,7 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     GAIN_TRY(e->lineKeep.alloc(n));
     GAIN_TRY(e->ull.alloc(4));
     GAIN_TRY(e->ull.zero(st, 4));
-    LineParams p;
-    p.acoef_2jI1 = 3.13618923e-7 * (double)(2 * jI + 1);
-    p.cmcoef = 1.327209365e-12;
-    p.gnsF = prm->gnsF;
-    p.two_jF1 = 2.0 * (double)jF + 1.0;
-    p.beta = 6.62606896e-27 * 2.99792458e+10 / (1.380658e-16 * prm->temperature);
-    p.zpe = prm->zpe;
-    p.q_part = prm->q_part;
-    p.thresh = prm->thresh;
-    p.freq_lo = prm->freq_lo;
-    p.freq_hi = prm->freq_hi;
-    p.with_intensity = I != nullptr;
+    const LineParams p = line_params(prm, jI, jF, I != nullptr);
     GAIN_CUDA(launch_lines(rows, cols, e->amp.p, e->amp_ld, e->eIdev.p, e->eFdev.p, p, e->lineS.p, e->lineA.p,
                            e->lineI.p, e->lineKeep.p, e->ull.p + 1, st));
     unsigned long long nk = 0;
@@ -1495,6 +1507,106 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     if (keep) GAIN_CUDA(cudaMemcpyAsync(keep, e->lineKeep.p, n, cudaMemcpyDeviceToHost, st));
     GAIN_CUDA(cudaStreamSynchronize(st));
     if (n_lines) *n_lines = (long long)nk;
+    return GAIN_OK;
+}
+
+gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                 const double* energiesF, int jI, int jF, int gammaI, int gammaF, int flags,
+                                 unsigned long long* text_bytes, long long* n_lines) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!prm || !energiesI || !energiesF || jI < 0 || jF < 0 || gammaI < 0 || gammaF < 0 ||
+        (flags & ~(GAIN_TEXT_INTENSITY | GAIN_TEXT_AMPLITUDES)))
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines_text: bad argument");
+    if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
+    if (prm->ndegI != 1 || prm->ndegF != 1)
+        return set_error(GAIN_ERR_UNSUPPORTED, "line assembly handles non-degenerate symmetries only");
+    if (prm->temperature <= 0 || prm->q_part <= 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "temperature and partition function must be positive");
+    e->have_text = false;
+    const int rows = e->amp_rows, cols = e->amp_cols;
+    const size_t n = (size_t)rows * cols;
+    const long nb = text_blocks((long)n);
+    cudaStream_t st = e->st;
+    GAIN_TRY(e->eIdev.upload(energiesI, rows));
+    GAIN_TRY(e->eFdev.upload(energiesF, cols));
+    GAIN_TRY(e->textLens.alloc(n));
+    GAIN_TRY(e->textBlocks.alloc(nb + 2));
+    GAIN_TRY(e->textBlocks.zero(st, nb + 2));
+    TextArgs t;
+    t.rows = rows;
+    t.cols = cols;
+    t.amp = e->amp.p;
+    t.ld = e->amp_ld;
+    t.eI = e->eIdev.p;
+    t.eF = e->eFdev.p;
+    t.p = line_params(prm, jI, jF, (flags & GAIN_TEXT_INTENSITY) != 0);
+    t.levI = e->d_lower.p;
+    t.levF = e->d_upper.p;
+    t.jI = jI;
+    t.jF = jF;
+    t.gammaI = gammaI;
+    t.gammaF = gammaF;
+    t.with_amps = (flags & GAIN_TEXT_AMPLITUDES) != 0;
+    t.lens = e->textLens.p;
+    t.block_bytes = e->textBlocks.p;
+    t.nkeep = e->textBlocks.p + nb + 1;
+    t.text = nullptr;
+    t.text_size = 0;
+    GAIN_CUDA(launch_text_len(t, st));
+    unsigned long long tot[2] = {0, 0};
+    GAIN_CUDA(cudaMemcpyAsync(tot, e->textBlocks.p + nb, sizeof tot, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    GAIN_TRY(e->text.alloc(tot[0] ? tot[0] : 1));
+    t.text = e->text.p;
+    t.text_size = tot[0];
+    GAIN_CUDA(launch_text_write(t, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    e->text_bytes = tot[0];
+    e->have_text = true;
+    if (text_bytes) *text_bytes = tot[0];
+    if (n_lines) *n_lines = (long long)tot[1];
+    return GAIN_OK;
+}
+
+gain_status gain_fetch_lines_text(gain_engine e, char* out, unsigned long long cap) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!e->have_text) return set_error(GAIN_ERR_NOT_READY, "no line-list text has been built");
+    if (!out || cap < e->text_bytes)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_fetch_lines_text: buffer of %llu bytes, text of %llu",
+                         cap, e->text_bytes);
+    if (e->text_bytes)
+        GAIN_CUDA(cudaMemcpyAsync(out, e->text.p, e->text_bytes, cudaMemcpyDeviceToHost, e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    return GAIN_OK;
+}
+
+gain_status gain_lines_text_device(gain_engine e, const char** text, unsigned long long* bytes) {
+    clear_error();
+    if (!e || !text || !bytes) return set_error(GAIN_ERR_INVALID_ARG, "NULL argument");
+    if (!e->have_text) return set_error(GAIN_ERR_NOT_READY, "no line-list text has been built");
+    *text = e->text.p;
+    *bytes = e->text_bytes;
+    return GAIN_OK;
+}
+
+gain_status gain_format_values_device(const double* values, long long n, int conv, int width, int prec,
+                                      char* out, int stride, int* lens) {
+    clear_error();
+    if (n < 0 || (n > 0 && (!values || !out || !lens)) || (conv != 'E' && conv != 'f') || prec < 0 ||
+        prec > (conv == 'E' ? 17 : 9) || width < 0 || width > 64 || stride <= 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_format_values_device: bad argument");
+    if (n == 0) return GAIN_OK;
+    DevArray<double> v;
+    DevArray<char> o;
+    DevArray<int> l;
+    GAIN_TRY(v.upload(values, (size_t)n));
+    GAIN_TRY(o.alloc((size_t)n * stride));
+    GAIN_TRY(l.alloc((size_t)n));
+    GAIN_CUDA(launch_format_values(n, v.p, conv, width, prec, o.p, stride, l.p, nullptr));
+    GAIN_CUDA(cudaMemcpy(out, o.p, (size_t)n * stride, cudaMemcpyDeviceToHost));
+    GAIN_CUDA(cudaMemcpy(lens, l.p, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
     return GAIN_OK;
 }
 
@@ -1518,7 +1630,7 @@ int gain_format_line(char* buf, size_t cap, double nu, int indexF, int jF, int g
         }
         s += "[ " + l + " ] ";
     }
-    s += "|| \n";
+    s += " || \n";   // fprintf(output, "%s || \n", buffer), Output.cpp:111
     const size_t n = std::min(cap - 1, s.size());
     memcpy(buf, s.data(), n);
     buf[n] = 0;

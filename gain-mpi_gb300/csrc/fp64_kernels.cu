@@ -3,6 +3,7 @@
 // the needed upper functions, transpose expansion, GEMV against resident upper vectors) and
 // the S / A / I line assembly.
 #include "gain_internal.h"
+#include "linemath.cuh"
 
 namespace gain {
 namespace {
@@ -292,25 +293,11 @@ __global__ void k_lines(int rows, int cols, const double* __restrict__ amp, long
     int k = 0;
     if (idx < total) {
         const int r = (int)(idx / cols), c = (int)(idx - (long)r * cols);
-        const double a = amp[(long)r * ld + c];
-        const double nu = eF[c] - eI[r];
-        double ls = __dmul_rn(a, a);                          // :83, ndegI = ndegF = 1
-        const double anu = fabs(nu);
-        const double Aein = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, ls), anu), anu), anu);  // :93
-        k = (nu >= p.freq_lo && nu <= p.freq_hi && nu >= 1e-40 && Aein >= p.thresh) ? 1 : 0;
-        double inten = 0.0;
-        if (p.with_intensity && nu >= 1e-40) {
-            // CMCOEF*A*gns*(2jF+1)*exp(-beta E'')*(1-exp(-beta nu))/(nu^2 Q), :101-102
-            inten = __dmul_rn(p.cmcoef, Aein);
-            inten = __dmul_rn(inten, p.gnsF);
-            inten = __dmul_rn(inten, p.two_jF1);
-            inten = __dmul_rn(inten, exp(-p.beta * (eI[r] - p.zpe)));
-            inten = __dmul_rn(inten, 1.0 - exp(-p.beta * nu));
-            inten = __ddiv_rn(inten, __dmul_rn(__dmul_rn(nu, nu), p.q_part));
-        }
-        if (S) S[idx] = ls;
-        if (A) A[idx] = Aein;
-        if (I) I[idx] = inten;
+        const LineVals v = line_eval(amp[(long)r * ld + c], eI[r], eF[c], p);
+        k = v.keep;
+        if (S) S[idx] = v.ls;
+        if (A) A[idx] = v.A;
+        if (I) I[idx] = v.I;
         if (keep) keep[idx] = (unsigned char)k;
     }
     const unsigned m = __ballot_sync(0xffffffffu, k);

@@ -118,4 +118,25 @@ cudaError_t launch_lines(int rows, int cols, const double* amp, long ld, const d
                          const double* eF, LineParams p, double* S, double* A, double* I,
                          unsigned char* keep, unsigned long long* nkeep, cudaStream_t st);
 
+// ---------------------------------------------------------------- line-list text (linetext.cu)
+struct TextArgs {
+    int rows, cols;
+    const double* amp;
+    long ld;
+    const double *eI, *eF;
+    LineParams p;
+    const int *levI, *levF;                // printed level indices (0-based) of rows / columns
+    int jI, jF, gammaI, gammaF, with_amps;
+    uint32_t* lens;                        // [rows*cols] text length of each line (0: not written)
+    unsigned long long* block_bytes;       // [text_blocks + 1]: block offsets, then the total
+    unsigned long long* nkeep;             // lines written
+    char* text;
+    unsigned long long text_size;          // bytes of text (the write pass stays inside)
+};
+long text_blocks(long lines);
+cudaError_t launch_text_len(const TextArgs& t, cudaStream_t st);     // lens, offsets, total, nkeep
+cudaError_t launch_text_write(const TextArgs& t, cudaStream_t st);   // the text itself
+cudaError_t launch_format_values(long n, const double* vals, int conv, int width, int prec, char* out,
+                                 int stride, int* lens, cudaStream_t st);
+
 }  // namespace gain

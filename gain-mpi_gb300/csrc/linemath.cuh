@@ -1,0 +1,33 @@
+// S, A and I of one non-degenerate line (BaseClasses/Output.cpp:52-112), shared by the line
+// assembly (k_lines) and the line-list text kernels so both see the same doubles.
+#pragma once
+#include "gain_internal.h"
+
+namespace gain {
+
+struct LineVals {
+    double nu, ls, A, I;
+    int keep;   // the reference writes the line: nu in FREQ-WINDOW, nu >= 1e-40, A >= THRESH_LINE
+};
+
+__device__ __forceinline__ LineVals line_eval(double a, double eIr, double eFc, const LineParams& p) {
+    LineVals v;
+    v.nu = eFc - eIr;
+    v.ls = __dmul_rn(a, a);                                   // :83, ndegI = ndegF = 1
+    const double anu = fabs(v.nu);
+    v.A = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, v.ls), anu), anu), anu);   // :93
+    v.keep = (v.nu >= p.freq_lo && v.nu <= p.freq_hi && v.nu >= 1e-40 && v.A >= p.thresh) ? 1 : 0;
+    v.I = 0.0;
+    if (p.with_intensity && v.nu >= 1e-40) {
+        // CMCOEF*A*gns*(2jF+1)*exp(-beta E'')*(1-exp(-beta nu))/(nu^2 Q), :101-102
+        double t = __dmul_rn(p.cmcoef, v.A);
+        t = __dmul_rn(t, p.gnsF);
+        t = __dmul_rn(t, p.two_jF1);
+        t = __dmul_rn(t, exp(-p.beta * (eIr - p.zpe)));
+        t = __dmul_rn(t, 1.0 - exp(-p.beta * v.nu));
+        v.I = __ddiv_rn(t, __dmul_rn(__dmul_rn(v.nu, v.nu), p.q_part));
+    }
+    return v;
+}
+
+}  // namespace gain

@@ -191,6 +191,16 @@ def _declare(L):
                                   ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_longlong)]
     L.gain_format_line.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
     L.gain_format_line.restype = I
+    L.gain_format_line_native.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
+    L.gain_format_line_native.restype = I
+    L.gain_format_value.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I]
+    L.gain_format_value.restype = I
+    U64 = ctypes.c_ulonglong
+    L.gain_pair_lines_text.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, I, I, I,
+                                       ctypes.POINTER(U64), ctypes.POINTER(ctypes.c_longlong)]
+    L.gain_fetch_lines_text.argtypes = [_vp, ctypes.c_void_p, U64]
+    L.gain_lines_text_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(U64)]
+    L.gain_format_values_device.argtypes = [_dp, ctypes.c_longlong, I, I, I, ctypes.c_char_p, I, _ip]
     FP, SP = ctypes.POINTER(Filters), ctypes.POINTER(State)
     L.gain_filter_lower.argtypes = [FP, SP]
     L.gain_filter_lower.restype = I
@@ -205,7 +215,8 @@ def _declare(L):
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
-                 "gain_pair_lines"):
+                 "gain_pair_lines", "gain_pair_lines_text", "gain_fetch_lines_text", "gain_lines_text_device",
+                 "gain_format_values_device"):
         getattr(L, name).restype = S
 
 
@@ -265,6 +276,35 @@ def hls_rotsym(dimenF, dimenI, nlevelI, nlevelF, sym_max_degen, kI, kF, ktauI, k
 
 def dot(n, x, y, result, stream=0):
     check(lib().gain_dot(n, x, y, result, stream))
+
+
+def format_line_native(nu, indexF, jF, gammaF, indexI, jI, gammaI, A, intensity=None, amps=None) -> str:
+    """The same line through the library's own conversions (the device kernels' code)."""
+    buf = ctypes.create_string_buffer(4096)
+    a = _f64(amps) if amps is not None else None
+    n = lib().gain_format_line_native(buf, 4096, nu, indexF, jF, gammaF, indexI, jI, gammaI, A,
+                                      int(intensity is not None), 0.0 if intensity is None else intensity,
+                                      _p(a, _dp) if a is not None else None, 0 if a is None else len(a))
+    assert n > 0
+    return buf.raw[:n].decode()
+
+
+def format_value(x: float, conv: str, width: int, prec: int) -> str:
+    """x through the library's "%<width>.<prec>E" / "%<width>.<prec>f" conversion (host build)."""
+    buf = ctypes.create_string_buffer(512)
+    n = lib().gain_format_value(buf, 512, x, ord(conv), width, prec)
+    assert n > 0, n
+    return buf.raw[:n].decode()
+
+
+def format_values_device(values, conv: str, width: int, prec: int, stride: int = 400) -> list:
+    """values through the device conversion kernel (one GPU launch)."""
+    v = _f64(values)
+    out = ctypes.create_string_buffer(max(1, v.size * stride))
+    lens = np.zeros(v.size, np.int32)
+    check(lib().gain_format_values_device(_p(v, _dp), v.size, ord(conv), width, prec, out, stride, _p(lens, _ip)))
+    raw = out.raw
+    return [raw[i * stride:i * stride + int(n)].decode() for i, n in enumerate(lens)]
 
 
 def format_line(nu, indexF, jF, gammaF, indexI, jI, gammaI, A, intensity=None, amps=None) -> str:
@@ -397,6 +437,30 @@ class Engine:
         return {"S": None if S is None else S.reshape(shp), "A": None if A is None else A.reshape(shp),
                 "I": None if I is None else I.reshape(shp), "keep": None if K is None else K.reshape(shp),
                 "n_lines": nl.value}
+
+
+def _lines_text(self, eI, eF, jI, jF, gammaI, gammaF, temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0,
+                freq=(-1e9, 1e9), gnsF=1.0, intensity=True, amplitudes=False, out=None):
+    """The line-list text of the last run, built on the device (gain_pair_lines_text) and
+    copied into out (a uint8 array of at least the text's size, e.g. pinned) or a new bytes
+    object.  Returns (text, n_lines)."""
+    eI, eF = _f64(eI), _f64(eF)
+    prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
+    nb, nl = ctypes.c_ulonglong(), ctypes.c_longlong()
+    flags = (TEXT_INTENSITY if intensity else 0) | (TEXT_AMPLITUDES if amplitudes else 0)
+    check(lib().gain_pair_lines_text(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF, gammaI, gammaF,
+                                     flags, ctypes.byref(nb), ctypes.byref(nl)))
+    if out is None:
+        buf = np.empty(max(1, nb.value), np.uint8)
+        check(lib().gain_fetch_lines_text(self.h, buf.ctypes.data, buf.size))
+        return buf[:nb.value].tobytes(), nl.value
+    assert out.dtype == np.uint8 and out.flags.c_contiguous and out.size >= nb.value
+    check(lib().gain_fetch_lines_text(self.h, out.ctypes.data, out.size))
+    return memoryview(out)[:nb.value], nl.value
+
+
+Engine.lines_text = _lines_text
+TEXT_INTENSITY, TEXT_AMPLITUDES = 1, 2
 
 
 def upload_problem(eng: Engine, p, dipole_block=None, blocks=None):

@@ -258,6 +258,32 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
                             const double* energiesF, int jI, int jF, double* S, double* A,
                             double* I, unsigned char* keep, long long* n_lines);
 
+/* Line-list text of the last run, built on the device: every line gain_pair_lines keeps,
+ * written exactly as Output::OutputLinestrength prints it (BaseClasses/Output.cpp:99-111:
+ * "%12.6f %8d %4d %4d <- %8d %4d %4d %16.9E " [intensity "%16.9E "] [ "[ " " %16.9E" " ] " ]
+ * then " || \n"), in row-major order (lower state, then upper state).  Levels come from the
+ * run's level lists and are printed + 1, gammaI/gammaF likewise; jI/jF are J values.  The
+ * reference writes one line per Output call from an OpenMP loop over upper states
+ * (main.cpp:286-339), so its order across upper states is that of its threads; each line's
+ * bytes are what its sprintf/fprintf produce for the same doubles.  *text_bytes = size of the
+ * text, *n_lines = lines written.  The text stays on the device until the next call. */
+#define GAIN_TEXT_INTENSITY 1   /* compute_intensities: the intensity column */
+#define GAIN_TEXT_AMPLITUDES 2  /* output_linestrengths: the "[ ... ]" amplitude list */
+gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                 const double* energiesF, int jI, int jF, int gammaI, int gammaF,
+                                 int flags, unsigned long long* text_bytes, long long* n_lines);
+/* Copy the text of the last gain_pair_lines_text call into out (cap >= text_bytes). */
+gain_status gain_fetch_lines_text(gain_engine e, char* out, unsigned long long cap);
+/* Device address and size of that text (valid until the next gain_pair_lines_text). */
+gain_status gain_lines_text_device(gain_engine e, const char** text, unsigned long long* bytes);
+
+/* The line-list conversions on their own, on the current device: values[i] printed with
+ * "%<width>.<prec>E" (conv 'E', prec <= 17) or "%<width>.<prec>f" (conv 'f', prec <= 9) into
+ * out + i*stride (no NUL), lens[i] = its length (the text is written only when it fits in
+ * stride).  For checking the device conversion against the C library's printf. */
+gain_status gain_format_values_device(const double* values, long long n, int conv, int width, int prec,
+                                      char* out, int stride, int* lens);
+
 /* ======================= host: state selection (BaseClasses/States.*) ============== */
 
 /* One eigenstate (BaseClasses/States.h:327-346): J, index of J in the J list, symmetry,
@@ -306,11 +332,22 @@ gain_status gain_transition_details(const gain_filters* f, const gain_state* st,
 gain_status gain_plan_pairs(const gain_filters* f, const gain_state* st, int n, int* n_pairs,
                             int* pairs, int* offs, long long* n_levels, int* levels);
 
-/* Text of one line exactly as Output.cpp:99-111 prints it (without the amplitude list
- * unless namp > 0).  Returns the number of characters written (excluding the NUL). */
+/* Text of one line exactly as Output.cpp:99-111 prints it, " || \n" included (without the
+ * amplitude list unless namp > 0), through the C library's snprintf.  Returns the number of
+ * characters written (excluding the NUL). */
 int gain_format_line(char* buf, size_t cap, double nu, int indexF, int jF, int gammaF,
                      int indexI, int jI, int gammaI, double A, int with_intensity,
                      double intensity, const double* amps, int namp);
+/* The same text through this library's own conversions (the code the device kernels run),
+ * compiled for the host.  Returns the length, or minus the length needed when cap is too
+ * small. */
+int gain_format_line_native(char* buf, size_t cap, double nu, int indexF, int jF, int gammaF,
+                            int indexI, int jI, int gammaI, double A, int with_intensity,
+                            double intensity, const double* amps, int namp);
+/* One value through those conversions: conv 'E' ("%<width>.<prec>E", prec <= 17) or 'f'
+ * ("%<width>.<prec>f", prec <= 9); returns the length (minus the length needed when cap is
+ * too small, 0 for a bad argument). */
+int gain_format_value(char* buf, size_t cap, double x, int conv, int width, int prec);
 
 #ifdef __cplusplus
 }

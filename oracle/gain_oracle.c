@@ -281,3 +281,41 @@ int orc_line(const double* amp, const unsigned char* degmask, int maxdeg, int nd
     *I_out = I;
     return 1;
 }
+
+/* The line list of one block pair as the reference writes it: for every (lower r, upper c)
+ * in row-major order, FilterIntensity's frequency window (BaseClasses/States.cpp:54-76),
+ * then OutputLinestrength (BaseClasses/Output.cpp:52-112) with sprintf into a buffer and
+ * fprintf "%s || \n".  amp[r*ld + c] is the line's amplitude (ndeg = 1).  Writes at most
+ * cap bytes into out (out may be NULL to size); returns the text size, *n_lines the lines. */
+long long orc_line_list(int rows, int cols, const double* amp, long ld, const double* eI, const double* eF,
+                        const int* levI, const int* levF, int jI, int jF, int gammaI, int gammaF, double gnsF,
+                        double temperature, double q_part, double zpe, double threshold, double freq_lo,
+                        double freq_hi, int with_intensity, int with_amps, char* out, long long cap,
+                        long long* n_lines) {
+    const unsigned char one = 1;
+    long long pos = 0, nl = 0;
+    char buffer[1024], lsbuf[300];
+    for (int r = 0; r < rows; ++r)
+        for (int c = 0; c < cols; ++c) {
+            const double nu = eF[c] - eI[r];
+            if (!(nu >= freq_lo && nu <= freq_hi)) continue;
+            const double a = amp[(long)r * ld + c];
+            double S, A, I;
+            if (!orc_line(&a, &one, 1, 1, 1, 0, eI[r], eF[c], zpe, jI, jF, gnsF, temperature, q_part, threshold,
+                          &S, &A, &I))
+                continue;
+            lsbuf[0] = '\0';
+            if (with_amps) sprintf(lsbuf + strlen(lsbuf), " %16.9E", a);
+            sprintf(buffer, "%12.6f %8d %4d %4d <- %8d %4d %4d %16.9E ", nu, levF[c] + 1, jF, gammaF + 1,
+                    levI[r] + 1, jI, gammaI + 1, A);
+            if (with_intensity) sprintf(buffer + strlen(buffer), "%16.9E ", I);
+            if (with_amps) sprintf(buffer + strlen(buffer), "[ %s ] ", lsbuf);
+            char line[1100];
+            const int n = snprintf(line, sizeof line, "%s || \n", buffer);
+            if (out && pos + n <= cap) memcpy(out + pos, line, (size_t)n);
+            pos += n;
+            ++nl;
+        }
+    if (n_lines) *n_lines = nl;
+    return pos;
+}

@@ -115,6 +115,15 @@ int orc_line(const double* amp, const unsigned char* degmask, int maxdeg, int nd
              double gnsF, double temperature, double q_part, double threshold,
              double* S_out, double* A_out, double* I_out);
 
+/* The text the reference writes for one block pair's lines (row-major, ndeg = 1):
+ * States.cpp:54-76 frequency window, Output.cpp:52-112 values and sprintf/fprintf.  out may
+ * be NULL (sizing); returns the text size in bytes. */
+long long orc_line_list(int rows, int cols, const double* amp, long ld, const double* eI, const double* eF,
+                        const int* levI, const int* levF, int jI, int jF, int gammaI, int gammaF, double gnsF,
+                        double temperature, double q_part, double zpe, double threshold, double freq_lo,
+                        double freq_hi, int with_intensity, int with_amps, char* out, long long cap,
+                        long long* n_lines);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,9 @@ def _declare(L):
     L.orc_line.argtypes = [_dp, ctypes.POINTER(ctypes.c_ubyte), I, I, I, I, D, D, D, I, I, D, D, D,
                            D, _dp, _dp, _dp]
     L.orc_line.restype = I
+    L.orc_line_list.argtypes = [I, I, _dp, ctypes.c_long, _dp, _dp, _ip, _ip, I, I, I, I, D, D, D, D, D, D, D, I,
+                                I, ctypes.c_char_p, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
+    L.orc_line_list.restype = ctypes.c_longlong
 
 
 def _i(a):
@@ -305,6 +308,24 @@ def line(amp_slots, degmask, maxdeg, ndegI, ndegF, flt: Filters, eI, eF, jI, jF,
     return (S.value, A.value, Iv.value) if ok else None
 
 
+def line_list(amp, eI, eF, levI, levF, jI, jF, gI, gF, gnsF=1.0, temperature=296.0, q_part=1.0, zpe=0.0,
+              thresh=0.0, freq=(-1e9, 1e9), intensity=True, amplitudes=False):
+    """(text bytes, n_lines) of one block pair as the reference writes it (orc_line_list)."""
+    a, ap = _d(amp)
+    rows, cols = a.shape
+    ei, eip = _d(eI)
+    ef, efp = _d(eF)
+    li, lip = _i(levI)
+    lf, lfp = _i(levF)
+    nl = ctypes.c_longlong()
+    args = (rows, cols, ap, cols, eip, efp, lip, lfp, jI, jF, gI, gF, gnsF, temperature, q_part, zpe, thresh,
+            freq[0], freq[1], int(intensity), int(amplitudes))
+    n = lib().orc_line_list(*args, None, 0, ctypes.byref(nl))
+    buf = ctypes.create_string_buffer(max(1, n))
+    lib().orc_line_list(*args, buf, n, ctypes.byref(nl))
+    return buf.raw[:n], nl.value
+
+
 def line_text(nu, indexF, jF, gF, indexI, jI, gI, A, intens=None, amps=None):
     """Output.cpp:99-111 text of one line."""
     s = "%12.6f %8d %4d %4d <- %8d %4d %4d %16.9E " % (nu, indexF + 1, jF, gF + 1, indexI + 1,
@@ -313,4 +334,4 @@ def line_text(nu, indexF, jF, gF, indexI, jI, gI, A, intens=None, amps=None):
         s += "%16.9E " % intens
     if amps is not None:
         s += "[ %s ] " % "".join(" %16.9E" % x for x in amps)
-    return s + "|| \n"
+    return s + " || \n"   # fprintf(output, "%s || \n", buffer), Output.cpp:111

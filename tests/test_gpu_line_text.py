@@ -1,0 +1,99 @@
+"""Line-list text built on the device (gain_pair_lines_text, gain_format_values_device)
+against the C library's printf and the oracle's restatement of Output::OutputLinestrength
+(BaseClasses/Output.cpp:52-112): byte-identical text for the same doubles."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+JMAX = 11
+_libc = ctypes.CDLL(None)
+
+
+def c_printf(fmt: str, x: float) -> str:
+    buf = ctypes.create_string_buffer(512)
+    _libc.snprintf(buf, 512, fmt.encode(), ctypes.c_double(x))
+    return buf.value.decode()
+
+
+@pytest.mark.parametrize("conv,width,prec", [("E", 16, 9), ("f", 12, 6), ("E", 25, 17), ("f", 20, 9)])
+def test_device_conversion_matches_printf(built_lib, conv, width, prec):
+    import gainls
+    from test_line_text_cpu import _random_values, _special_values
+    vals = _special_values() + _random_values(20000, 77 + prec)
+    got = gainls.format_values_device(vals, conv, width, prec)
+    fmt = f"%{width}.{prec}{conv}"
+    bad = [(x, a, b) for x, a, b in zip(vals, got, (c_printf(fmt, x) for x in vals)) if a != b]
+    assert not bad, bad[:10]
+
+
+@pytest.fixture(scope="module")
+def pair_run(built_lib):
+    import gainls
+    import synth
+    p = synth.make_problem(40, [2, 3], "c4", blocks=[(2, 0), (3, 1)])
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    bI, bF = p.blocks[(0, 0)], p.blocks[(1, 1)]
+    lo = list(range(0, bI.vecs.shape[0], 2))
+    up = list(range(bF.vecs.shape[0]))
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    eI = bI.energies[lo] + 0.0
+    eF = bF.energies[up] + 0.0
+    return p, eng, lo, up, eI, eF
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(intensity=False), dict(amplitudes=True),
+                                dict(thresh=1e-3, freq=(50.0, 4000.0), zpe=120.0, temperature=1000.0,
+                                     gnsF=3.0, q_part=7.5, amplitudes=True)])
+def test_pair_text_matches_oracle(pair_run, kw):
+    """The device text equals the oracle's sprintf/fprintf text of the same amplitudes; with
+    the intensity column it is compared line by line against the C library's formatting of
+    the device's own S, A, I (the device and host exp may differ in the last bit)."""
+    import gainls
+    import oracle
+    p, eng, lo, up, eI, eF = pair_run
+    amp = eng.fetch_amp().copy()
+    args = dict(temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0, freq=(-1e9, 1e9), gnsF=1.0, intensity=True,
+                amplitudes=False)
+    args.update(kw)
+    text, n = eng.lines_text(eI, eF, 2, 3, 0, 1, **args)
+    assert n > 0 and len(text) > 0
+    ref, nref = oracle.line_list(amp, eI, eF, lo, up, 2, 3, 0, 1, gnsF=args["gnsF"],
+                                 temperature=args["temperature"], q_part=args["q_part"], zpe=args["zpe"],
+                                 thresh=args["thresh"], freq=args["freq"], intensity=args["intensity"],
+                                 amplitudes=args["amplitudes"])
+    assert n == nref
+    if not args["intensity"]:
+        assert bytes(text) == ref
+        return
+    lines = eng.lines(eI, eF, 2, 3, temperature=args["temperature"], q_part=args["q_part"], zpe=args["zpe"],
+                      thresh=args["thresh"], freq=args["freq"], gnsF=args["gnsF"])
+    want = []
+    for r, c in zip(*np.nonzero(lines["keep"])):
+        want.append(gainls.format_line(eF[c] - eI[r], up[c], 3, 1, lo[r], 2, 0, lines["A"][r, c],
+                                       intensity=lines["I"][r, c],
+                                       amps=[amp[r, c]] if args["amplitudes"] else None))
+    assert bytes(text).decode() == "".join(want)
+    # and line by line against the oracle: identical except possibly the intensity digits
+    got_l, ref_l = bytes(text).decode().splitlines(), ref.decode().splitlines()
+    assert len(got_l) == len(ref_l)
+    diff = [(a.split(), b.split()) for a, b in zip(got_l, ref_l) if a != b]
+    for a, b in diff:   # token 9 is the intensity
+        assert a[:9] + a[10:] == b[:9] + b[10:], (a, b)
+        assert abs(float(a[9]) - float(b[9])) <= 2e-9 * abs(float(b[9]))
+    assert len(diff) <= max(1, len(got_l) // 1000)
+
+
+def test_text_device_pointer_and_small_buffer(pair_run):
+    import gainls
+    p, eng, lo, up, eI, eF = pair_run
+    text, n = eng.lines_text(eI, eF, 2, 3, 0, 1)
+    ptr, nb = ctypes.c_void_p(), ctypes.c_ulonglong()
+    gainls.check(gainls.lib().gain_lines_text_device(eng.h, ctypes.byref(ptr), ctypes.byref(nb)))
+    assert nb.value == len(text) and ptr.value
+    small = np.empty(len(text) - 1, np.uint8)
+    with pytest.raises(gainls.GainError):
+        gainls.check(gainls.lib().gain_fetch_lines_text(eng.h, small.ctypes.data, small.size))
