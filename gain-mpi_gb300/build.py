@@ -18,7 +18,7 @@ OBJ = os.path.join(HERE, "_build", platform.machine())
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libgainls.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cpp", "threej.cpp", "states.cpp", "fp64_kernels.cu", "split.cu", "noalloc.cu", "adjoint.cu", "linetext.cu"]
+SOURCES = ["engine.cpp", "threej.cpp", "states.cpp", "fp64_kernels.cu", "split.cu", "noalloc.cu", "adjoint.cu", "linetext.cu", "trove.cpp"]
 HEADERS = ["gain_internal.h", "split.h", "linefmt.h", "linemath.cuh"]
 
 
@@ -39,7 +39,8 @@ def _stale(target: str, deps) -> bool:
 def _compile(src: str) -> str:
     path = os.path.join(CSRC, src)
     obj = os.path.join(OBJ, src + ".o")
-    deps = [path, os.path.join(ROOT, "include", "gain_ls.h")] + [os.path.join(CSRC, h) for h in HEADERS]
+    deps = [path, os.path.join(ROOT, "include", "gain_ls.h"), os.path.join(ROOT, "include", "gain_trove.h")]
+    deps += [os.path.join(CSRC, h) for h in HEADERS]
     if not _stale(obj, deps):
         return obj
     cmd = [nvcc(), "-c", "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",

@@ -83,6 +83,11 @@ class Filters(ctypes.Structure):
                 ("reduced", ctypes.c_int), ("symmetry_type", ctypes.c_int)]
 
 
+class TroveState(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("irec", ctypes.c_int), ("ilevel", ctypes.c_int),
+                ("krot", ctypes.c_int), ("taurot", ctypes.c_int), ("rec_len", ctypes.c_int)]
+
+
 def make_filters(gns, isym_pairs, igamma_pair, sym_degen, erange_lower, erange_upper,
                  freq_window=(-1e9, 1e9), zpe=0.0, maxJ=0, reduced=False, symmetry_type=1):
     """A Filters struct plus the arrays it points to (kept alive on the struct)."""
@@ -212,6 +217,26 @@ def _declare(L):
     L.gain_transition_details.restype = S
     L.gain_plan_pairs.argtypes = [FP, SP, I, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_longlong), _ip]
     L.gain_plan_pairs.restype = S
+    L.gain_trove_basis_read.argtypes = [ctypes.c_char_p, I, I, _ip, I, ctypes.POINTER(_vp)]
+    L.gain_trove_basis_free.argtypes = [_vp]
+    L.gain_trove_basis_free.restype = None
+    L.gain_trove_basis_info.argtypes = [_vp, _ip, _ip, _ip, _ip, _ip]
+    L.gain_trove_basis_arrays.argtypes = [_vp, _ip, _ip, _ip, _ip, _ip, _ip, _ip]
+    L.gain_trove_basis_repres.argtypes = [_vp, I, _ip, _dp]
+    L.gain_trove_basis_upload.argtypes = [_vp, I, _vp]
+    L.gain_trove_dipole_read.argtypes = [ctypes.c_char_p, ctypes.c_ulonglong, ctypes.POINTER(_vp)]
+    L.gain_trove_dipole_free.argtypes = [_vp]
+    L.gain_trove_dipole_free.restype = None
+    L.gain_trove_dipole_info.argtypes = [_vp, _ip, _ip]
+    L.gain_trove_dipole_block.argtypes = [_vp, I, _ip, _ip, _ip, ctypes.POINTER(_dp)]
+    L.gain_trove_states_read.argtypes = [ctypes.c_char_p, I, I, ctypes.POINTER(Filters), _ip,
+                                         ctypes.POINTER(TroveState), _ip]
+    L.gain_trove_vectors_read.argtypes = [ctypes.c_char_p, I, _ip, I, _dp]
+    for name in ("gain_trove_basis_read", "gain_trove_basis_info", "gain_trove_basis_arrays",
+                 "gain_trove_basis_repres", "gain_trove_basis_upload", "gain_trove_dipole_read",
+                 "gain_trove_dipole_info", "gain_trove_dipole_block", "gain_trove_states_read",
+                 "gain_trove_vectors_read"):
+        getattr(L, name).restype = S
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
@@ -227,9 +252,9 @@ def check(status: int):
 
 
 def declared_symbols() -> list[str]:
-    """Every function name include/gain_ls.h declares."""
+    """Every function name the C headers include/gain_ls.h and include/gain_trove.h declare."""
     import re
-    text = open(HEADER).read()
+    text = open(HEADER).read() + open(os.path.join(os.path.dirname(HEADER), "gain_trove.h")).read()
     return sorted(set(re.findall(r"\b(gain_[a-z0-9_]+)\s*\(", text)))
 
 
@@ -487,3 +512,84 @@ def upload_problem(eng: Engine, p, dipole_block=None, blocks=None):
                 if abs(bF.J - bI.J) <= 1:
                     eng.upload_wigner(jI, jF, synth.rotsym_levels(bI.J), synth.rotsym_levels(bF.J), 1,
                                       synth.make_wigner(bI.J, bF.J, 1))
+
+
+# ----------------------------------------------------------------------------- TROVE files
+def trove_basis(dirpath: str, J: int, nsym: int, sym_degen, rotsym: bool = False) -> dict:
+    """The basis of J read from j0eigen_quanta<J>.chk (with the J=0 file) in dirpath."""
+    h = _vp()
+    sd = _i32(sym_degen)
+    check(lib().gain_trove_basis_read(dirpath.encode(), J, nsym, _p(sd, _ip), int(rotsym), ctypes.byref(h)))
+    try:
+        j, d, mc, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        Ntot = np.zeros(nsym, np.int32)
+        check(lib().gain_trove_basis_info(h, ctypes.byref(j), ctypes.byref(d), ctypes.byref(mc), ctypes.byref(ms),
+                                          _p(Ntot, _ip)))
+        d, mc = d.value, mc.value
+        out = {k: np.zeros(n, np.int32) for k, n in (("K", d), ("tau", d), ("vib", d), ("kblock", J + 1),
+                                                      ("kstart", J + 1), ("icontr", 2 * d), ("ijterms", mc * nsym))}
+        check(lib().gain_trove_basis_arrays(h, *[_p(out[k], _ip) for k in
+                                                 ("K", "tau", "vib", "kblock", "kstart", "icontr", "ijterms")]))
+        out["N"], out["repres"] = [], []
+        for g in range(nsym):
+            N = np.zeros(mc, np.int32)
+            R = np.zeros(int(Ntot[g]) * int(sd[g]) * ms.value, np.float64)
+            check(lib().gain_trove_basis_repres(h, g, _p(N, _ip), _p(R, _dp)))
+            out["N"].append(N)
+            out["repres"].append(R)
+        out.update(J=j.value, dimen=d, maxcoeff=mc, matsize=ms.value, Ntot=Ntot, sdeg=sd)
+        return out
+    finally:
+        lib().gain_trove_basis_free(h)
+
+
+def trove_upload_basis(eng: "Engine", jind: int, dirpath: str, J: int, nsym: int, sym_degen, rotsym=False):
+    h = _vp()
+    sd = _i32(sym_degen)
+    check(lib().gain_trove_basis_read(dirpath.encode(), J, nsym, _p(sd, _ip), int(rotsym), ctypes.byref(h)))
+    try:
+        check(lib().gain_trove_basis_upload(eng.h, jind, h))
+    finally:
+        lib().gain_trove_basis_free(h)
+
+
+def trove_dipole(path: str, max_bytes: int = 1 << 62):
+    """(ncontr, [(startF, endF, ncontrF, piece[3*ncontr*ncontrF]), ...]) of j0_extfield.chk."""
+    h = _vp()
+    check(lib().gain_trove_dipole_read(path.encode(), max_bytes, ctypes.byref(h)))
+    try:
+        n, nb = ctypes.c_int(), ctypes.c_int()
+        check(lib().gain_trove_dipole_info(h, ctypes.byref(n), ctypes.byref(nb)))
+        pieces = []
+        for b in range(nb.value):
+            s, e, c, ptr = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), _dp()
+            check(lib().gain_trove_dipole_block(h, b, ctypes.byref(s), ctypes.byref(e), ctypes.byref(c),
+                                                ctypes.byref(ptr)))
+            size = 3 * n.value * c.value
+            arr = np.ctypeslib.as_array(ptr, shape=(size,)).copy() if size else np.zeros(0)
+            pieces.append((s.value, e.value, c.value, arr))
+        return n.value, pieces
+    finally:
+        lib().gain_trove_dipole_free(h)
+
+
+def trove_states(dirpath: str, J: int, gamma: int, f: Filters):
+    """States of j0eigen_descr<J>_<gamma+1>.chk passing the filters: (structured array, dim_basis)."""
+    n, dim = ctypes.c_int(), ctypes.c_int()
+    check(lib().gain_trove_states_read(dirpath.encode(), J, gamma, ctypes.byref(f), ctypes.byref(n), None,
+                                       ctypes.byref(dim)))
+    arr = (TroveState * max(1, n.value))()
+    check(lib().gain_trove_states_read(dirpath.encode(), J, gamma, ctypes.byref(f), ctypes.byref(n), arr,
+                                       ctypes.byref(dim)))
+    dt = np.dtype([("energy", np.float64), ("irec", np.int32), ("ilevel", np.int32), ("krot", np.int32),
+                   ("taurot", np.int32), ("rec_len", np.int32)], align=True)
+    assert dt.itemsize == ctypes.sizeof(TroveState)
+    out = np.frombuffer(bytes(arr), dtype=dt, count=n.value).copy()
+    return out, dim.value
+
+
+def trove_vectors(path: str, rec_len: int, records) -> np.ndarray:
+    r = _i32(records)
+    out = np.zeros((len(r), rec_len), np.float64)
+    check(lib().gain_trove_vectors_read(path.encode(), rec_len, _p(r, _ip), len(r), _p(out, _dp)))
+    return out

@@ -1,0 +1,62 @@
+"""A block pair run from ingested TROVE checkpoint files (gain_trove_basis_upload, the
+dipole pieces of j0_extfield.chk, eigenvector records) gives the amplitudes of the same
+problem uploaded directly; with the dipole split into pieces, the amplitudes summed over
+the pieces (one run per piece, MultiGpuManager::ExecuteHalfLs's block loop) agree too."""
+import os
+
+import numpy as np
+import pytest
+
+import trove_files
+
+pytestmark = pytest.mark.gpu
+
+JMAX = 11
+
+
+def test_pair_from_trove_files_matches_direct_upload(tmp_path, built_lib):
+    import gainls
+    import synth
+    p = synth.make_problem(20, [2, 3], "c4", blocks=[(2, 0), (3, 1)])
+    trove_files.write_problem(str(tmp_path), p)
+    d = str(tmp_path)
+    direct = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(direct, p)
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    for jind, J in enumerate(p.jvals):
+        gainls.trove_upload_basis(eng, jind, d, J, p.nsym, p.sym_degen)
+    n, pieces = gainls.trove_dipole(os.path.join(d, "j0_extfield.chk"))
+    (s, e, c, piece), = pieces
+    eng.upload_dipole(piece, n, s, e, c)
+    f = gainls.make_filters([1.0] * 4, p.isym_pairs, p.igamma_pair, p.sym_degen, (0.0, 1e9), (0.0, 1e9))
+    for jind, J, g in ((0, 2, 0), (1, 3, 1)):
+        st, dim = gainls.trove_states(d, J, g, f)
+        vecs = gainls.trove_vectors(os.path.join(d, f"j0eigen_vectors{J}_{g + 1}.chk"), dim, st["irec"])
+        eng.upload_eigvecs(jind, g, vecs)
+    lo = list(range(p.blocks[(0, 0)].vecs.shape[0]))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+    for path in (gainls.PATH_PLAIN_FP64, gainls.PATH_SPLIT):
+        direct.run_pair(0, 0, 1, 1, lo, up, path)
+        eng.run_pair(0, 0, 1, 1, lo, up, path)
+        np.testing.assert_array_equal(eng.fetch_amp(), direct.fetch_amp())
+
+
+def test_dipole_pieces_sum_to_the_whole(tmp_path, built_lib):
+    import gainls
+    import synth
+    p = synth.make_problem(20, [2, 3], "c4", blocks=[(2, 0), (3, 1)])
+    trove_files.write_problem(str(tmp_path), p)
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    lo = list(range(p.blocks[(0, 0)].vecs.shape[0]))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+    whole = eng.fetch_amp().copy()
+    n, pieces = gainls.trove_dipole(os.path.join(str(tmp_path), "j0_extfield.chk"), 3 * 20 * 20 * 8 // 3)
+    assert len(pieces) == 4
+    total = np.zeros_like(whole)
+    for s, e, c, piece in pieces:
+        eng.upload_dipole(piece, n, s, e, c)
+        eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+        total += eng.fetch_amp()
+    assert np.max(np.abs(total - whole)) <= 1e-13 * np.abs(whole).max()
