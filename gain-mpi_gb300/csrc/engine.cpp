@@ -237,6 +237,14 @@ struct gain_engine_s {
     int dipN = 0, startF = 0, endF = 0, ncontrF = 0;
     bool dip_present = false;
     long dip_version = 0;
+    // dipole pieces kept in host memory (gain_upload_dipole_pieces); runs loop over them
+    struct HostPiece {
+        const double* host;
+        int startF, endF;
+    };
+    std::vector<HostPiece> pieces;
+    int piece_loaded = -1;
+    gain::DevArray<double> acc;   // amplitude / H accumulator of a multi-piece run
     std::map<std::pair<int, int>, std::unique_ptr<gain::WignerTab>> wigner;   // by (jindI, jindF)
     long wig_version = 0;
     std::map<std::pair<int, int>, std::unique_ptr<gain::Eig>> eig;
@@ -468,6 +476,39 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) 
     return GAIN_OK;
 }
 
+gain_status load_piece(gain_engine e, int p);
+
+// The plain path over dipole pieces: one run per piece, amplitudes summed (each piece
+// contributes the upper functions of its vibrational range, MultiGpuManager.cpp:240-288).
+gain_status run_plain_pieces(gain_engine e, const gain_pair_job* j, gain_stats* stats) {
+    const size_t n = (size_t)j->nlower * j->nupper;
+    double ms = 0;
+    long long launches = 0;
+    for (int p = 0; p < (int)e->pieces.size(); ++p) {
+        GAIN_TRY(load_piece(e, p));
+        gain_stats sp;
+        GAIN_TRY(run_plain(e, j, &sp));
+        ms += sp.device_ms;
+        launches += sp.kernel_launches + 1;
+        if (p == 0) {
+            GAIN_TRY(e->acc.alloc(n));
+            GAIN_CUDA(cudaMemcpyAsync(e->acc.p, e->amp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, e->st));
+        } else {
+            GAIN_CUDA(launch_add(e->acc.p, e->amp.p, (long)n, e->st));
+        }
+    }
+    GAIN_CUDA(cudaMemcpyAsync(e->amp.p, e->acc.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        stats->device_ms = ms;
+        stats->rows = j->nlower;
+        stats->cols = j->nupper;
+        stats->kernel_launches = launches;
+    }
+    return GAIN_OK;
+}
+
 // ------------------------------------------------------------------ split path
 struct SplitParams {
     int beta, slices, chunks;
@@ -512,6 +553,8 @@ std::vector<split::Prod> make_prods(const SplitParams& p) {
             for (int j = 0; i + j < p.slices; ++j) v.push_back({i, j, i + j, c});
     return v;
 }
+
+gain_status launch_layout_band(gain_engine e, const gain_pair_job* j);
 
 gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, GammaMaps* mF) {
     PairLayout& L = e->layout;
@@ -605,6 +648,23 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     GAIN_TRY(L.d_band_k0.upload(L.band_k0));
     GAIN_TRY(L.d_band_len.upload(L.band_len));
     GAIN_TRY(L.band.alloc((size_t)L.fpad * L.W));
+    GAIN_TRY(launch_layout_band(e, j));
+    L.beta1 = 0;
+    L.s1 = 0;
+    L.c1 = 0;
+    std::copy(key, key + 4, L.key);
+    L.dip_version = e->dip_version;
+    L.wig_version = wv;
+    return GAIN_OK;
+}
+
+// The rotational-dipole band of the current layout from the dipole piece now on the device
+// (rows whose upper vibrational index lies outside the piece are zero).
+gain_status launch_layout_band(gain_engine e, const gain_pair_job* j) {
+    PairLayout& L = e->layout;
+    const WignerTab* wt = wigner_of(e, j->jindI, j->jindF);
+    Basis& bI = e->bases[j->jindI];
+    Basis& bF = e->bases[j->jindF];
     split::BandArgs ba;
     ba.fpad = L.fpad;
     ba.W = L.W;
@@ -639,12 +699,24 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     ba.nlevelF = wt ? wt->nF : 0;
     ba.maxdeg = wt ? wt->maxdeg : 0;
     GAIN_CUDA(split::launch_band(ba, e->st));
-    L.beta1 = 0;
-    L.s1 = 0;
-    L.c1 = 0;
-    std::copy(key, key + 4, L.key);
-    L.dip_version = e->dip_version;
-    L.wig_version = wv;
+    return GAIN_OK;
+}
+
+// Copy dipole piece p of the host list into the device buffer (after the work queued on the
+// engine's stream that reads the previous piece).
+gain_status load_piece(gain_engine e, int p) {
+    if (e->piece_loaded == p) return GAIN_OK;
+    const auto& hp = e->pieces[p];
+    const size_t n = (size_t)3 * e->dipN * (hp.endF - hp.startF);
+    size_t mx = 0;
+    for (auto& q : e->pieces) mx = std::max(mx, (size_t)3 * e->dipN * (q.endF - q.startF));
+    GAIN_TRY(e->dipole.alloc(mx));
+    GAIN_CUDA(cudaMemcpyAsync(e->dipole.p, hp.host, sizeof(double) * n, cudaMemcpyHostToDevice, e->st));
+    e->startF = hp.startF;
+    e->endF = hp.endF;
+    e->ncontrF = hp.endF - hp.startF;
+    e->piece_loaded = p;
+    ++e->dip_version;
     return GAIN_OK;
 }
 
@@ -697,6 +769,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     const double tol = (opts && opts->tol > 0) ? opts->tol : 4.5e-9;
     cudaStream_t st = e->st;
     GAIN_CUDA(cudaEventRecord(e->ev[0], st));
+    // dipole pieces (MultiGpuManager::ExecuteHalfLs's block loop): H accumulates the first
+    // GEMM of every piece, the second GEMM runs once
+    const int npieces = e->pieces.size() > 1 ? (int)e->pieces.size() : 1;
+    if (npieces > 1) GAIN_TRY(load_piece(e, 0));
     GAIN_TRY(build_layout(e, j, mI, mF));
     PairLayout& L = e->layout;
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
@@ -731,6 +807,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         return set_error(GAIN_ERR_INVALID_ARG, "unsupported digit configuration");
 
     // band digits (cached per digit configuration)
+    auto band_digits = [&]() -> gain_status {
     if (L.beta1 != p1x.beta || L.s1 != p1x.slices || L.c1 != p1x.chunks) {
         GAIN_TRY(L.bandDig.alloc((size_t)p1x.slices * L.fpad * L.W));
         GAIN_TRY(L.bandDig.zero(st, (size_t)p1x.slices * L.fpad * L.W));
@@ -745,6 +822,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         L.s1 = p1x.slices;
         L.c1 = p1x.chunks;
     }
+    return GAIN_OK;
+    };
+    GAIN_TRY(band_digits());
 
     // CTA pairs (256 x 128 tiles) whenever the lower states fill more than one 128-row block;
     // GAINLS_GEMM_PAIR=0 keeps single-CTA tiles
@@ -808,77 +888,109 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     if (!split::make_digit_map(&tmV, e->Vdig.p, L.kpadI, Bpad, p1x.slices))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (lower digits)");
 
-    // ---- GEMM 1: H = V M
-    std::vector<split::Tile> t1;
-    for (auto& fb : L.fblocks)
-        for (int n0 = fb.first; n0 < fb.second; n0 += split::BN)
-            for (int m0 = 0; m0 < Bpad; m0 += mstep) {
-                split::Tile t;
-                memset(&t, 0, sizeof t);
-                t.m0 = m0;
-                t.n0 = n0;
-                t.a_k0 = L.band_k0[n0];
-                t.b_k0 = 0;
-                t.nkb = L.band_len[n0] / split::BK;
-                t1.push_back(t);
-            }
+    // ---- GEMM 1: H = V M (one pass per dipole piece)
     const std::vector<split::Prod> pr1 = make_prods(p1x);
-    GAIN_TRY(e->tiles1.upload(t1));
     GAIN_TRY(e->prods1.upload(pr1));
     GAIN_TRY(e->H.alloc((size_t)Bpad * L.fpad));
     GAIN_TRY(e->rowerr.alloc(Bpad));
     GAIN_TRY(e->rowerr.zero(st, Bpad));
-    split::GemmArgs g1;
-    memset(&g1, 0, sizeof g1);
-    g1.tiles = e->tiles1.p;
-    g1.ntiles = (int)t1.size();
-    g1.prods = e->prods1.p;
-    g1.nprods = (int)pr1.size();
-    g1.nchunks = p1x.chunks;
-    g1.beta = p1x.beta;
-    g1.slices = p1x.slices;
-    g1.out = e->H.p;
-    g1.ldo = L.fpad;
-    g1.A = e->Vst.view(false);
-    g1.B = L.bandStats.view(false);
-    g1.c_fix = fix_const((int)pr1.size());
-    g1.c_f64 = (float)((double)(L.W + 64) * std::ldexp(1.0, -53) * 1.01);
-    g1.rowerr2 = e->rowerr.p;
-    g1.flag_mode = 2;   // every H entry FP64-grade, else recomputed in FP64
-    g1.tol = (float)tol;
-    g1.flags = e->flags1.p;
-    g1.nflags = e->counters.p + 0;
-    g1.max_flags = kMaxFlags;
-    g1.rows_valid = B;
-    g1.cols_valid = L.fpad;
-    g1.err = e->err.p;
-    GAIN_CUDA(cudaEventRecord(e->ev[2], st));
-    GAIN_CUDA(split::launch_gemm(tmV, pair ? L.tmBandPair : L.tmBand, g1, e->num_sms, st, pair));
-    GAIN_CUDA(cudaEventRecord(e->ev[3], st));
-    // ---- upper vectors -> digits on the low-priority second stream
-    GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
-    if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready, 0));
-    GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
-                   e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p));
-    GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
-    // inexact first-GEMM entries recomputed in FP64
-    split::RefineHArgs rh;
-    rh.flags = e->flags1.p;
-    rh.nflags = e->counters.p + 0;
-    rh.max_flags = kMaxFlags;
-    rh.vecs = EI.d.p;
-    rh.nsize = EI.nsize;
-    rh.row_level = e->d_lower.p;
-    rh.i_sym = L.d_i_sym.p;
-    rh.band_k0 = L.d_band_k0.p;
-    rh.band_len = L.d_band_len.p;
-    rh.band = L.band.p;
-    rh.W = L.W;
-    rh.H = e->H.p;
-    rh.ldh = L.fpad;
-    rh.eA = e->Vst.e.p;
-    rh.rowerr2 = e->rowerr.p;
-    GAIN_CUDA(split::launch_refine_h(rh, 2 * e->num_sms, st));
+    if (npieces > 1) {
+        GAIN_TRY(e->acc.alloc((size_t)Bpad * L.fpad));
+        GAIN_TRY(e->acc.zero(st, (size_t)Bpad * L.fpad));
+    }
+    const Basis& bFs = e->bases[j->jindF];
+    std::vector<split::Tile> t1;
+    for (int piece = 0; piece < npieces; ++piece) {
+        if (piece > 0) {   // the next piece's band (the previous GEMM and refinement read theirs)
+            GAIN_CUDA(cudaStreamSynchronize(st));
+            GAIN_TRY(load_piece(e, piece));
+            GAIN_TRY(launch_layout_band(e, j));
+            L.dip_version = e->dip_version;
+            L.beta1 = 0;
+            GAIN_TRY(band_digits());
+            GAIN_CUDA(cudaMemsetAsync(e->counters.p, 0, sizeof(unsigned int), st));
+        }
+        if (npieces > 1) GAIN_CUDA(cudaMemsetAsync(e->H.p, 0, sizeof(double) * (size_t)Bpad * L.fpad, st));
+        t1.clear();
+        for (auto& fb : L.fblocks)
+            for (int n0 = fb.first; n0 < fb.second; n0 += split::BN) {
+                if (npieces > 1) {   // only column tiles holding an upper function of this piece
+                    bool any = false;
+                    for (int r = n0; r < n0 + split::BN && r < L.fpad && !any; ++r) {
+                        const int fp = L.f_prim[r];
+                        any = fp >= 0 && bFs.vib[fp] >= e->startF && bFs.vib[fp] < e->endF;
+                    }
+                    if (!any) continue;
+                }
+                for (int m0 = 0; m0 < Bpad; m0 += mstep) {
+                    split::Tile t;
+                    memset(&t, 0, sizeof t);
+                    t.m0 = m0;
+                    t.n0 = n0;
+                    t.a_k0 = L.band_k0[n0];
+                    t.b_k0 = 0;
+                    t.nkb = L.band_len[n0] / split::BK;
+                    t1.push_back(t);
+                }
+            }
+        GAIN_TRY(e->tiles1.upload(t1));
+        split::GemmArgs g1;
+        memset(&g1, 0, sizeof g1);
+        g1.tiles = e->tiles1.p;
+        g1.ntiles = (int)t1.size();
+        g1.prods = e->prods1.p;
+        g1.nprods = (int)pr1.size();
+        g1.nchunks = p1x.chunks;
+        g1.beta = p1x.beta;
+        g1.slices = p1x.slices;
+        g1.out = e->H.p;
+        g1.ldo = L.fpad;
+        g1.A = e->Vst.view(false);
+        g1.B = L.bandStats.view(false);
+        g1.c_fix = fix_const((int)pr1.size());
+        g1.c_f64 = (float)((double)(L.W + 64) * std::ldexp(1.0, -53) * 1.01);
+        g1.rowerr2 = e->rowerr.p;
+        g1.flag_mode = 2;   // every H entry FP64-grade, else recomputed in FP64
+        g1.tol = (float)tol;
+        g1.flags = e->flags1.p;
+        g1.nflags = e->counters.p + 0;
+        g1.max_flags = kMaxFlags;
+        g1.rows_valid = B;
+        g1.cols_valid = L.fpad;
+        g1.err = e->err.p;
+        if (piece == 0) GAIN_CUDA(cudaEventRecord(e->ev[2], st));
+        if (!t1.empty()) GAIN_CUDA(split::launch_gemm(tmV, pair ? L.tmBandPair : L.tmBand, g1, e->num_sms, st, pair));
+        if (piece == npieces - 1) GAIN_CUDA(cudaEventRecord(e->ev[3], st));
+        if (piece == 0) {
+            // ---- upper vectors -> digits on the low-priority second stream
+            GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
+            if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready, 0));
+            GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
+                           e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p));
+            GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
+        }
+        // inexact first-GEMM entries recomputed in FP64
+        split::RefineHArgs rh;
+        rh.flags = e->flags1.p;
+        rh.nflags = e->counters.p + 0;
+        rh.max_flags = kMaxFlags;
+        rh.vecs = EI.d.p;
+        rh.nsize = EI.nsize;
+        rh.row_level = e->d_lower.p;
+        rh.i_sym = L.d_i_sym.p;
+        rh.band_k0 = L.d_band_k0.p;
+        rh.band_len = L.d_band_len.p;
+        rh.band = L.band.p;
+        rh.W = L.W;
+        rh.H = e->H.p;
+        rh.ldh = L.fpad;
+        rh.eA = e->Vst.e.p;
+        rh.rowerr2 = e->rowerr.p;
+        GAIN_CUDA(split::launch_refine_h(rh, 2 * e->num_sms, st));
+        if (npieces > 1) GAIN_CUDA(launch_add(e->acc.p, e->H.p, (long)Bpad * L.fpad, st));
+    }
+    if (npieces > 1)
+        GAIN_CUDA(cudaMemcpyAsync(e->H.p, e->acc.p, sizeof(double) * (size_t)Bpad * L.fpad, cudaMemcpyDeviceToDevice, st));
 
     // ---- H -> digits; the upper digits (second stream) must be ready before the second GEMM
     GAIN_TRY(slice(e, e->H.p, L.fpad, nullptr, B, L.fpad, nullptr, nullptr, L.fpad, Bpad, e->Hdig.p, p2,
@@ -1266,12 +1378,40 @@ gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int st
             for (int v : b.vib)
                 if (v >= N) return set_error(GAIN_ERR_INVALID_ARG, "vibrational index %d >= dipole size %d", v, N);
     GAIN_TRY(e->dipole.upload(piece, (size_t)3 * N * ncontrF));
+    e->pieces.clear();
+    e->piece_loaded = -1;
     e->dipN = N;
     e->startF = startF;
     e->endF = endF;
     e->ncontrF = ncontrF;
     e->dip_present = true;
     ++e->dip_version;
+    return GAIN_OK;
+}
+
+gain_status gain_upload_dipole_pieces(gain_engine e, int npieces, const double* const* pieces, int N,
+                                      const int* startF, const int* endF) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (npieces <= 0 || !pieces || !startF || !endF || N <= 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_dipole_pieces: bad argument");
+    for (int p = 0; p < npieces; ++p)
+        if (!pieces[p] || startF[p] < 0 || endF[p] > N || endF[p] <= startF[p] || (p > 0 && startF[p] < endF[p - 1]))
+            return set_error(GAIN_ERR_INVALID_ARG,
+                             "gain_upload_dipole_pieces: piece %d [%d,%d) is empty, outside [0,%d) or overlaps", p,
+                             startF[p], endF[p], N);
+    if (npieces == 1) return gain_upload_dipole(e, pieces[0], N, startF[0], endF[0], endF[0] - startF[0]);
+    for (auto& b : e->bases)
+        if (b.present)
+            for (int v : b.vib)
+                if (v >= N) return set_error(GAIN_ERR_INVALID_ARG, "vibrational index %d >= dipole size %d", v, N);
+    e->pieces.clear();
+    for (int p = 0; p < npieces; ++p) e->pieces.push_back({pieces[p], startF[p], endF[p]});
+    e->dipN = N;
+    e->dip_present = true;
+    e->piece_loaded = -1;
+    GAIN_TRY(load_piece(e, 0));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
     return GAIN_OK;
 }
 
@@ -1358,6 +1498,8 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     GAIN_TRY(check_engine(e));
     GAIN_TRY(validate_job(e, job));
     if (!dL_dS || !dL_dmu) return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair: NULL argument");
+    if (e && e->pieces.size() > 1)
+        return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: upload the dipole as one piece");
     if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: non-degenerate symmetries only");
     e->have_amp = false;
     // forward amplitudes of the pair in FP64 (the reference's method)
@@ -1448,7 +1590,7 @@ gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path pat
     GAIN_TRY(check_engine(e));
     GAIN_TRY(validate_job(e, job));
     e->have_amp = false;
-    if (path == GAIN_PATH_PLAIN_FP64) return run_plain(e, job, stats);
+    if (path == GAIN_PATH_PLAIN_FP64) return e->pieces.size() > 1 ? run_plain_pieces(e, job, stats) : run_plain(e, job, stats);
     if (path == GAIN_PATH_SPLIT) return run_split(e, job, opts, stats);
     return set_error(GAIN_ERR_INVALID_ARG, "unknown path %d", (int)path);
 }

@@ -2,6 +2,8 @@
 // strength, vector expansion, dot product), the plain-path kernels (half line strength of
 // the needed upper functions, transpose expansion, GEMV against resident upper vectors) and
 // the S / A / I line assembly.
+#include <algorithm>
+
 #include "gain_internal.h"
 #include "linemath.cuh"
 
@@ -283,6 +285,11 @@ __global__ void k_scatter_select(int dimen, const int* __restrict__ sym_of,
     prim[r] = s >= 0 ? __dmul_rn(vec[s], coef[r]) : 0.0;
 }
 
+__global__ void k_add(double* __restrict__ acc, const double* __restrict__ x, long n) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        acc[i] += x[i];
+}
+
 // S / A / I of every amplitude (non-degenerate symmetries), Output.cpp:52-112.
 __global__ void k_lines(int rows, int cols, const double* __restrict__ amp, long ld,
                         const double* __restrict__ eI, const double* __restrict__ eF, LineParams p,
@@ -444,6 +451,13 @@ cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* co
                                   const double* vec, double* prim, cudaStream_t st) {
     if (dimen <= 0) return cudaSuccess;
     k_scatter_select<<<(dimen + 255) / 256, 256, 0, st>>>(dimen, sym_of, coef, vec, prim);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add(double* acc, const double* x, long n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const long blocks = std::min<long>((n + 255) / 256, 4096);
+    k_add<<<(unsigned)blocks, 256, 0, st>>>(acc, x, n);
     return cudaGetLastError();
 }
 

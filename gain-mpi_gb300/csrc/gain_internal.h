@@ -107,6 +107,9 @@ cudaError_t launch_gemv_batch(int nrows, int n, const double* U, long ldu, const
 cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* coef,
                                   const double* vec, double* prim, cudaStream_t st);
 
+// acc[i] += x[i], i < n
+cudaError_t launch_add(double* acc, const double* x, long n, cudaStream_t st);
+
 // S, A, I of a [rows x cols] amplitude block (ndeg = 1), Output.cpp:52-112
 struct LineParams {
     double acoef_2jI1;   // ACOEF * (2 jI + 1), the first product of Output.cpp:93

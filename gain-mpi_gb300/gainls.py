@@ -186,6 +186,8 @@ def _declare(L):
                                         _ip, _ip]
     L.gain_upload_dipole.argtypes = [_vp, _dp, I, I, I, I]
     L.gain_upload_eigvecs.argtypes = [_vp, I, I, I, I, _dp]
+    L.gain_upload_dipole_pieces.argtypes = [_vp, I, ctypes.POINTER(_dp), I, _ip, _ip]
+    L.gain_upload_dipole_pieces.restype = S
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
     L.gain_adjoint_pair.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.POINTER(Stats)]
     L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
@@ -378,6 +380,15 @@ class Engine:
     def upload_dipole(self, piece, N, startF, endF, ncontrF):
         piece = _f64(piece)
         check(lib().gain_upload_dipole(self.h, _p(piece, _dp), N, startF, endF, ncontrF))
+
+    def upload_dipole_pieces(self, pieces, N):
+        """pieces: [(startF, endF, piece[3*N*(endF-startF)]), ...] kept in host memory (the
+        arrays stay referenced by the engine); runs loop over them."""
+        arrs = [_f64(a) for (_, _, a) in pieces]
+        self._keep["dipole_pieces"] = arrs
+        ptrs = (_dp * len(arrs))(*[_p(a, _dp) for a in arrs])
+        s, e = _i32([x[0] for x in pieces]), _i32([x[1] for x in pieces])
+        check(lib().gain_upload_dipole_pieces(self.h, len(arrs), ptrs, N, _p(s, _ip), _p(e, _ip)))
 
     def upload_eigvecs(self, jind, gamma, vecs):
         vecs = _f64(vecs)

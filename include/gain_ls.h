@@ -137,6 +137,18 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
 gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int startF, int endF,
                                int ncontrF);
 
+/* The dipole as pieces of the upper vibrational index kept in HOST memory (TroveDipole's
+ * blocks, TroveClasses/TroveDipole.cpp:85-112; each piece in the gain_upload_dipole layout
+ * [3][N][endF-startF]), for N_v whose dipole does not fit the device.  Pieces are disjoint
+ * and ascending.  Runs then loop over them as MultiGpuManager::ExecuteHalfLs loops over
+ * dipole blocks (BaseClasses/MultiGpuManager.cpp:240-262, GpuManager::SwitchDipoleBlock
+ * :481-496): one device buffer holds the piece in use; the split path accumulates the first
+ * GEMM of every piece and runs the second GEMM once; the plain path sums the amplitudes of
+ * one run per piece.  The host arrays must stay valid until the dipole is replaced or the
+ * engine destroyed.  gain_adjoint_pair needs a single piece. */
+gain_status gain_upload_dipole_pieces(gain_engine e, int npieces, const double* const* pieces, int N,
+                                      const int* startF, const int* endF);
+
 /* GpuManager::TransferWigner (BaseClasses/GpuManager.cpp:440-478): the rotational matrix
  * elements of the pair (J of jindI) -> (J of jindF), rot[d + 3 (lI + nlevelsI (lF + nlevelsF
  * (dI + maxdeg dF)))], d = 0..2 (the Wigner::rot layout the rotsym kernel reads,
