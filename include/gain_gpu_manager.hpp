@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -114,6 +115,37 @@ class GpuManager {
     void TransferDipole(DipoleT* d, int block) {
         TransferDipole(d->GetDipolePiece(block), (int)d->GetMaxContracts(), d->GetDipoleStart(block),
                        d->GetDipoleEnd(block), d->GetDipoleNcontr(block));
+        current_block_ = block;
+        switch_piece_ = [d](int b, const double** piece, int* N, int* s, int* e, int* n) {
+            *piece = d->GetDipolePiece(b);
+            *N = (int)d->GetMaxContracts();
+            *s = d->GetDipoleStart(b);
+            *e = d->GetDipoleEnd(b);
+            *n = d->GetDipoleNcontr(b);
+        };
+    }
+    // :481-496: the device takes another block of the dipole given to TransferDipole
+    void SwitchDipoleBlock(int block) {
+        if (!switch_piece_) throw std::runtime_error("SwitchDipoleBlock before TransferDipole(Dipole*, block)");
+        const double* piece;
+        int N, s, e, n;
+        switch_piece_(block, &piece, &N, &s, &e, &n);
+        TransferDipole(piece, N, s, e, n);
+        current_block_ = block;
+    }
+    // For ExecuteBlockPair: every block of the dipole at once, kept in host memory; the engine
+    // loops over them per run (gain_upload_dipole_pieces).  The pieces must outlive the runs.
+    template <class DipoleT>
+    void TransferDipolePieces(DipoleT* d) {
+        std::vector<const double*> p;
+        std::vector<int> s, e;
+        for (int b = 0; b < d->GetNumBlocks(); ++b) {
+            p.push_back(d->GetDipolePiece(b));
+            s.push_back(d->GetDipoleStart(b));
+            e.push_back(d->GetDipoleEnd(b));
+        }
+        check(gain_upload_dipole_pieces(engine_, (int)p.size(), p.data(), (int)d->GetMaxContracts(), s.data(),
+                                        e.data()));
     }
     void TransferDipole(const double* piece, int N, int startF, int endF, int ncontrF) {
         check(gain_upload_dipole(engine_, piece, N, startF, endF, ncontrF));
@@ -175,7 +207,7 @@ class GpuManager {
     double* GetFinalVector(int proc) { return host_vectorF_.at(proc); }
     double* GetLinestrength(int proc) { return host_ls_.at(proc); }
     bool WillDoHalfLs() const { return doing_half_ls_; }
-    int GetCurrentBlock() const { return 0; }
+    int GetCurrentBlock() const { return current_block_; }
 
     // :537-545
     void UpdateEigenVector() {
@@ -329,6 +361,8 @@ class GpuManager {
     double* dipole_ = nullptr;
     int dipN_ = 0, startF_ = 0, endF_ = 0, ncontrF_ = 0;
     bool doing_half_ls_ = false;
+    int current_block_ = 0;
+    std::function<void(int, const double**, int*, int*, int*, int*)> switch_piece_;
     int nsize_max_ = 0, dimen_max_ = 0;
     std::vector<Basis> bases_;
     std::vector<Inflation> infl_;

@@ -10,8 +10,10 @@
 //            upper vectors [nupper NtotF]
 //   optional: int rotsym (1), ints nlevelsI nlevelsF, doubles rot[3 nlevelsI nlevelsF] -- the
 //             rotational-symmetry form, with the Wigner table of the pair JI -> JF
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <vector>
 
 #include "gain_gpu_manager.hpp"
@@ -22,11 +24,39 @@ int geti() { int v; if (fread(&v, 4, 1, fin) != 1) { fprintf(stderr, "short read
 std::vector<int> getiv(size_t n) { std::vector<int> v(n); if (n && fread(v.data(), 4, n, fin) != n) exit(2); return v; }
 std::vector<double> getdv(size_t n) { std::vector<double> v(n); if (n && fread(v.data(), 8, n, fin) != n) exit(2); return v; }
 struct Wig { double* rot; int nlevelsI, nlevelsF; };   // the fields of the reference's Wigner
+// The reference Dipole's getters over a dipole split into nblocks pieces of the upper index
+// (TroveDipole.cpp:85-112: ceil(ncontr / nblocks) functions per piece, flipped layout).
+struct BlockedDipole {
+    int n;
+    std::vector<int> s, e;
+    std::vector<std::vector<double>> pieces;
+    BlockedDipole(const std::vector<double>& full, int nv, int nblocks) : n(nv) {
+        const int per = (int)ceilf((float)nv / (float)nblocks);
+        for (int b = 0; b < nblocks; ++b) {
+            const int s0 = b * per, e0 = std::min((b + 1) * per, nv), c = e0 - s0;
+            s.push_back(s0);
+            e.push_back(e0);
+            std::vector<double> p((size_t)3 * nv * c);
+            for (int k = 0; k < 3; ++k)
+                for (int i = 0; i < nv; ++i)
+                    for (int f = s0; f < e0; ++f)
+                        p[(f - s0) + (size_t)i * c + (size_t)k * nv * c] = full[f + (size_t)i * nv + (size_t)k * nv * nv];
+            pieces.push_back(std::move(p));
+        }
+    }
+    const double* GetDipolePiece(int b) { return pieces[b].data(); }
+    size_t GetMaxContracts() { return (size_t)n; }
+    int GetDipoleStart(int b) { return s[b]; }
+    int GetDipoleEnd(int b) { return e[b]; }
+    int GetDipoleNcontr(int b) { return e[b] - s[b]; }
+    int GetNumBlocks() { return (int)pieces.size(); }
+};
 struct J { int J, dimen; std::vector<int> K, ktau, vib, kblock, kstart, icontr, ijterms, Ntot; std::vector<std::vector<int>> N; };
 }
 
 int main(int argc, char** argv) {
-    if (argc < 3) { fprintf(stderr, "usage: %s input output\n", argv[0]); return 1; }
+    if (argc < 3) { fprintf(stderr, "usage: %s input output [dipole_blocks]\n", argv[0]); return 1; }
+    const int nblocks = argc > 3 ? atoi(argv[3]) : 1;
     fin = fopen(argv[1], "rb");
     if (!fin) return 1;
     const int nv = geti(), jmax = geti(), nsym = geti(), JI = geti(), JF = geti(), gI = geti(), gF = geti();
@@ -56,7 +86,14 @@ int main(int argc, char** argv) {
     try {
         gain::GpuManager gpu(0, 1, rotsym != 0);
         gpu.InitializeAndTransferConstants(jmax, nsym, 1);
-        gpu.TransferDipole(piece.data(), nv, startF, endF, endF - startF);
+        std::unique_ptr<BlockedDipole> blocked;
+        if (nblocks > 1) {   // MultiGpuManager::TransferDipole: the device starts with block 0
+            if (startF != 0 || endF != nv) { fprintf(stderr, "blocks need the whole dipole\n"); return 1; }
+            blocked.reset(new BlockedDipole(piece, nv, nblocks));
+            gpu.TransferDipole(blocked.get(), 0);
+        } else {
+            gpu.TransferDipole(piece.data(), nv, startF, endF, endF - startF);
+        }
         int dimen_max = 0, nsize_max = 0;
         for (int t = 0; t < 2; ++t) {
             J& j = js[t];
@@ -86,7 +123,10 @@ int main(int argc, char** argv) {
                       gpu.GetInitialVector());
             gpu.UpdateEigenVector();
             gpu.ResetHalfLinestrength(1, 0);
-            gpu.ExecuteHalfLs(0, 1, 0, gI);                 // MultiGpuManager::ExecuteHalfLs
+            for (int b = 0; b < nblocks; ++b) {             // MultiGpuManager::ExecuteHalfLs block loop
+                if (nblocks > 1 && gpu.GetCurrentBlock() != b) gpu.SwitchDipoleBlock(b);
+                gpu.ExecuteHalfLs(0, 1, 0, gI);
+            }
             for (int u = 0; u < nupper; ++u) {              // main.cpp:293 upper-state loop
                 std::copy(vu.begin() + (size_t)u * js[1].Ntot[gF], vu.begin() + (size_t)(u + 1) * js[1].Ntot[gF],
                           gpu.GetFinalVector(0));

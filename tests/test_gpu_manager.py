@@ -110,3 +110,19 @@ def test_manager_loop_matches_reference(driver, tmp_path, name):
     ref = d["ref_amp"]
     # same half_ls bits as the reference; the dot's summation order differs from cublasDdot
     assert np.max(np.abs(amp - ref)) <= 1e-14 * np.abs(ref).max() + 1e-300
+
+
+@pytest.mark.parametrize("nblocks", [2, 3])
+def test_manager_dipole_blocks_match_reference(driver, tmp_path, nblocks):
+    """The dipole split into blocks (TroveDipole's pieces), SwitchDipoleBlock between the
+    half line strength calls of each lower state (MultiGpuManager.cpp:240-262): the same
+    golden amplitudes as the whole dipole (each block writes its own upper functions)."""
+    d = np.load(os.path.join(GOLDEN, "c4_dJp1.npz"))
+    nv = int(d["nv"])
+    assert tuple(int(x) for x in d["block"]) == (0, nv)
+    inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    _write_input(inp, d)
+    subprocess.run([driver, inp, outp, str(nblocks)], check=True, timeout=120)
+    amp = np.fromfile(outp, np.float64).reshape(d["ref_amp"].shape)
+    ref = d["ref_amp"]
+    assert np.max(np.abs(amp - ref)) <= 1e-14 * np.abs(ref).max() + 1e-300
