@@ -445,6 +445,18 @@ def adjoint_check(args):
         eng.adjoint(jI, gI, jF, gF, lo, up, g, grad)
     times["adjoint_s"] = time.perf_counter() - t1
     grad = grad.reshape(mu0.shape)
+    # the same gradient from the split path's amplitudes: per pair the tensor-core forward,
+    # dL/dS on the device, then the adjoint (which takes the run's amplitudes)
+    grad_split = np.zeros(mu0.size)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for (jI, gI, jF, gF, lo, up), m, lt in zip(pairs, masks, logS_t):
+        eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_SPLIT)
+        s0 = amp_now(lo, up) ** 2
+        g = torch.where(m, 2.0 * (torch.log(s0) - lt) / s0, torch.zeros_like(s0)).cpu().numpy()
+        eng.adjoint(jI, gI, jF, gF, lo, up, g, grad_split)
+    times["gradient_split_forward_s"] = time.perf_counter() - t1
+    split_vs_fp64 = float(np.max(np.abs(grad_split - grad.reshape(-1))) / np.abs(grad).max())
 
     # central differences
     h = 1e-6
@@ -485,6 +497,7 @@ def adjoint_check(args):
            "fd_max_err_over_max_grad": float(max(absn)), "fd_direction_rel_err": [float(x) for x in dirs],
            "exact_partials_max_rel_err": float(jrel.max()), "exact_partials_median_rel_err": float(np.median(jrel)),
            "exact_direction_rel_err": [float(x) for x in jdirs],
+           "split_forward_gradient_max_err_over_max_grad": split_vs_fp64,
            "nonzero_gradient_entries": int(cand.size), "gradient_entries": int(mu0.size),
            "setup_s": setup_s}
     out.update(times)

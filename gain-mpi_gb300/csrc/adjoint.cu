@@ -16,10 +16,12 @@ namespace {
 
 __device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
 
-__global__ void k_adj_scale(long n, const double* __restrict__ dLdS, const double* __restrict__ amp,
-                            double* __restrict__ G) {
+__global__ void k_adj_scale(int rows, int cols, const double* __restrict__ dLdS, const double* __restrict__ amp,
+                            long ld_amp, double* __restrict__ G) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) G[i] = 2.0 * dLdS[i] * amp[i];
+    if (i >= (long)rows * cols) return;
+    const long r = i / cols, c = i - r * cols;
+    G[i] = 2.0 * dLdS[i] * amp[r * ld_amp + c];
 }
 
 // C[m][n] = sum_k A[m][k] B[levels[k]][n]: 64 x 64 tiles, 16 x 16 threads, 4 x 4 outputs each.
@@ -110,9 +112,11 @@ k_adj_dmu(AdjArgs a) {
 
 }  // namespace
 
-cudaError_t launch_adj_scale(long n, const double* dLdS, const double* amp, double* G, cudaStream_t st) {
+cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, double* G,
+                             cudaStream_t st) {
+    const long n = (long)rows * cols;
     if (n <= 0) return cudaSuccess;
-    k_adj_scale<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, dLdS, amp, G);
+    k_adj_scale<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, G);
     return cudaGetLastError();
 }
 

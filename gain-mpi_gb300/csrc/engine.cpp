@@ -254,6 +254,7 @@ struct gain_engine_s {
     int amp_rows = 0, amp_cols = 0;
     long amp_ld = 0;
     bool have_amp = false;
+    std::vector<int> amp_job;   // jindI, gammaI, jindF, gammaF, lower levels, upper levels of amp
 
     // work buffers
     gain::DevArray<int> d_lower, d_upper;
@@ -1115,6 +1116,14 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     return GAIN_OK;
 }
 
+// The identity of a block-pair job (its blocks and level lists).
+std::vector<int> job_key(const gain_pair_job* j) {
+    std::vector<int> k = {j->jindI, j->gammaI, j->jindF, j->gammaF, j->nlower, j->nupper};
+    k.insert(k.end(), j->lower_levels, j->lower_levels + j->nlower);
+    k.insert(k.end(), j->upper_levels, j->upper_levels + j->nupper);
+    return k;
+}
+
 // Output.cpp constants (ACOEF, CMCOEF, the radiation constant of beta) and the INTENSITY
 // block's parameters for one (J'', J') pair.
 LineParams line_params(const gain_line_params* prm, int jI, int jF, bool with_intensity) {
@@ -1274,6 +1283,7 @@ gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const i
                               const int* vib, const int* kblock_size, const int* kstart) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (jind < 0 || jind > 1000 || J < 0 || J > e->jmax || dimen <= 0 || !K || !tau || !vib || !kblock_size || !kstart)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_basis: bad argument");
     // K-sorted, K-blocks consistent with the per-function K (TroveBasisSet.cpp:659-681)
@@ -1320,6 +1330,7 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
                                   const int* Ntot, const int* sdeg) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (jind < 0 || jind >= (int)e->bases.size() || !e->bases[jind].present)
         return set_error(GAIN_ERR_NOT_READY, "upload the basis of jind %d first", jind);
     if (dimen != e->bases[jind].dimen || maxcoeff <= 0 || matsize <= 0 || !icontr || !ijterms || !N || !repres ||
@@ -1370,6 +1381,7 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
 gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int startF, int endF, int ncontrF) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (!piece || N <= 0 || startF < 0 || endF > N || endF - startF != ncontrF || ncontrF <= 0)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_dipole: bad block (N=%d, [%d,%d), ncontrF=%d)", N, startF,
                          endF, ncontrF);
@@ -1393,6 +1405,7 @@ gain_status gain_upload_dipole_pieces(gain_engine e, int npieces, const double* 
                                       const int* startF, const int* endF) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (npieces <= 0 || !pieces || !startF || !endF || N <= 0)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_dipole_pieces: bad argument");
     for (int p = 0; p < npieces; ++p)
@@ -1419,6 +1432,7 @@ gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI
                                const double* rot) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (jindI < 0 || jindF < 0 || jindI >= (int)e->bases.size() || jindF >= (int)e->bases.size() || nlevelsI <= 0 ||
         nlevelsF <= 0 || maxdeg <= 0 || !rot)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_wigner: bad argument");
@@ -1448,6 +1462,7 @@ gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI
 gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize, const double* vecs) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (jind < 0 || gamma < 0 || gamma >= e->nsym || nlevels <= 0 || nsize <= 0 || !vecs)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs: bad argument");
     auto& slot = e->eig[{jind, gamma}];
@@ -1466,6 +1481,7 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
                                       const double* vecs) {
     clear_error();
     GAIN_TRY(check_engine(e));
+    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
     if (jind < 0 || gamma < 0 || gamma >= e->nsym || nlevels <= 0 || nsize <= 0 || !vecs)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs_async: bad argument");
     cudaPointerAttributes pa{};
@@ -1501,9 +1517,14 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     if (e && e->pieces.size() > 1)
         return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: upload the dipole as one piece");
     if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: non-degenerate symmetries only");
-    e->have_amp = false;
-    // forward amplitudes of the pair in FP64 (the reference's method)
-    GAIN_TRY(run_plain(e, job, nullptr));
+    // forward amplitudes: those of the last run when it computed this job (either path),
+    // else the plain FP64 path (the reference's method)
+    if (!(e->have_amp && e->amp_job == job_key(job))) {
+        e->have_amp = false;
+        e->amp_job.clear();
+        GAIN_TRY(run_plain(e, job, nullptr));
+        e->amp_job = job_key(job);
+    }
     const Basis& bI = e->bases[job->jindI];
     const Basis& bF = e->bases[job->jindF];
     Inflation& iI = e->infl[job->jindI];
@@ -1525,7 +1546,7 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     GAIN_TRY(e->adj_iota.upload(iota));
     GAIN_CUDA(cudaEventRecord(e->ev[0], st));
     // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dL/dH
-    GAIN_CUDA(launch_adj_scale((long)nS, e->adj_dLdS.p, e->amp.p, e->adj_G.p, st));
+    GAIN_CUDA(launch_adj_scale(B, Nu, e->adj_dLdS.p, e->amp.p, e->amp_ld, e->adj_G.p, st));
     GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, e->adj_G.p, Nu, EF.d.p, EF.nsize, e->d_upper.p, e->adj_dH.p, NtF, st));
     GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF, iF.dijterms.p,
                                    iF.dicontr.p, iF.dN[job->gammaF]->p, iF.drepres[job->gammaF]->p, e->adj_dH.p, NtF,
@@ -1590,9 +1611,15 @@ gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path pat
     GAIN_TRY(check_engine(e));
     GAIN_TRY(validate_job(e, job));
     e->have_amp = false;
-    if (path == GAIN_PATH_PLAIN_FP64) return e->pieces.size() > 1 ? run_plain_pieces(e, job, stats) : run_plain(e, job, stats);
-    if (path == GAIN_PATH_SPLIT) return run_split(e, job, opts, stats);
-    return set_error(GAIN_ERR_INVALID_ARG, "unknown path %d", (int)path);
+    gain_status r;
+    if (path == GAIN_PATH_PLAIN_FP64)
+        r = e->pieces.size() > 1 ? run_plain_pieces(e, job, stats) : run_plain(e, job, stats);
+    else if (path == GAIN_PATH_SPLIT)
+        r = run_split(e, job, opts, stats);
+    else
+        return set_error(GAIN_ERR_INVALID_ARG, "unknown path %d", (int)path);
+    e->amp_job = r == GAIN_OK ? job_key(job) : std::vector<int>();
+    return r;
 }
 
 gain_status gain_pair_amp_device(gain_engine e, const double** amp, int* ld) {

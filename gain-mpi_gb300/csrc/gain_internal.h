@@ -58,7 +58,8 @@ struct AdjArgs {
     long ld_vp;
     double* dmu;                               // [3][dipN][ncontrF] accumulated
 };
-cudaError_t launch_adj_scale(long n, const double* dLdS, const double* amp, double* G, cudaStream_t st);
+cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, double* G,
+                             cudaStream_t st);
 cudaError_t launch_adj_gemm(int M, int N, int K, const double* A, long lda, const double* B, long ldb,
                             const int* levels, double* C, long ldc, cudaStream_t st);
 cudaError_t launch_adj_dmu(const AdjArgs& a, cudaStream_t st);

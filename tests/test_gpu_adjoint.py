@@ -51,3 +51,27 @@ def test_adjoint_matches_central_differences(built_lib, rule, block):
         d = d.reshape(piece0.shape)
         fd = (_phi(eng, p, piece0 + h * d, blk, lo, up, w) - _phi(eng, p, piece0 - h * d, blk, lo, up, w)) / (2 * h)
         assert abs(fd - grad.reshape(-1)[k]) <= 1e-8 * scale
+
+
+def test_adjoint_reuses_the_last_run_of_the_same_job(built_lib):
+    """After a run of the same pair (either path) the adjoint takes its amplitudes; after an
+    upload it runs its own FP64 forward.  The split path's amplitudes move the gradient by
+    their certified error only."""
+    import gainls
+    import synth
+    p = synth.make_problem(16, [2, 3], "c4", blocks=[(2, 0), (3, 1)])
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    lo = list(range(p.blocks[(0, 0)].vecs.shape[0]))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+    w = np.random.default_rng(3).standard_normal((len(lo), len(up)))
+    g_plain = eng.adjoint(0, 0, 1, 1, lo, up, w, np.zeros(p.dipole.size))
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    g_split = eng.adjoint(0, 0, 1, 1, lo, up, w, np.zeros(p.dipole.size))
+    assert np.max(np.abs(g_split - g_plain)) <= 1e-8 * np.abs(g_plain).max()
+    # a different dipole: the stored amplitudes no longer apply
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+    nv = p.dipole.shape[-1]
+    eng.upload_dipole((2.0 * p.dipole).reshape(-1), nv, 0, nv, nv)
+    g2 = eng.adjoint(0, 0, 1, 1, lo, up, w, np.zeros(p.dipole.size))
+    assert np.max(np.abs(g2 - 2.0 * g_plain)) <= 1e-12 * np.abs(g2).max()   # S = amp^2: dS/dmu doubles
