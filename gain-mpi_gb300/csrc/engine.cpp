@@ -1700,8 +1700,8 @@ gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, con
     GAIN_TRY(e->eIdev.upload(energiesI, rows));
     GAIN_TRY(e->eFdev.upload(energiesF, cols));
     GAIN_TRY(e->textLens.alloc(n));
-    GAIN_TRY(e->textBlocks.alloc(nb + 2));
-    GAIN_TRY(e->textBlocks.zero(st, nb + 2));
+    GAIN_TRY(e->textBlocks.alloc(nb + 3));
+    GAIN_TRY(e->textBlocks.zero(st, nb + 3));
     TextArgs t;
     t.rows = rows;
     t.cols = cols;
@@ -1723,13 +1723,13 @@ gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, con
     t.text = nullptr;
     t.text_size = 0;
     GAIN_CUDA(launch_text_len(t, st));
-    unsigned long long tot[2] = {0, 0};
+    unsigned long long tot[3] = {0, 0, 0};   // text size, lines, largest block
     GAIN_CUDA(cudaMemcpyAsync(tot, e->textBlocks.p + nb, sizeof tot, cudaMemcpyDeviceToHost, st));
     GAIN_CUDA(cudaStreamSynchronize(st));
     GAIN_TRY(e->text.alloc(tot[0] ? tot[0] : 1));
     t.text = e->text.p;
     t.text_size = tot[0];
-    GAIN_CUDA(launch_text_write(t, st));
+    GAIN_CUDA(launch_text_write(t, tot[2], st));
     GAIN_CUDA(cudaStreamSynchronize(st));
     e->text_bytes = tot[0];
     e->have_text = true;

@@ -132,14 +132,15 @@ struct TextArgs {
     const int *levI, *levF;                // printed level indices (0-based) of rows / columns
     int jI, jF, gammaI, gammaF, with_amps;
     uint32_t* lens;                        // [rows*cols] text length of each line (0: not written)
-    unsigned long long* block_bytes;       // [text_blocks + 1]: block offsets, then the total
+    unsigned long long* block_bytes;       // [text_blocks + 3]: block offsets, the total, -, the largest block
     unsigned long long* nkeep;             // lines written
     char* text;
     unsigned long long text_size;          // bytes of text (the write pass stays inside)
 };
 long text_blocks(long lines);
 cudaError_t launch_text_len(const TextArgs& t, cudaStream_t st);     // lens, offsets, total, nkeep
-cudaError_t launch_text_write(const TextArgs& t, cudaStream_t st);   // the text itself
+// the text itself; max_block_bytes = the largest block total (block_bytes[text_blocks + 2])
+cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_bytes, cudaStream_t st);
 cudaError_t launch_format_values(long n, const double* vals, int conv, int width, int prec, char* out,
                                  int stride, int* lens, cudaStream_t st);
 

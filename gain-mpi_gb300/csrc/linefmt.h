@@ -307,6 +307,57 @@ GAIN_HD void put_F(Sink& s, double x, int width, int prec) {
     }
 }
 
+// Text lengths without converting, where the value range makes them certain; anything else
+// is counted by the conversion itself, so the result always equals the converted length.
+GAIN_HD int len_d(int v, int width) {
+    const int n = ndigits(v < 0 ? (uint64_t)(-(int64_t)v) : (uint64_t)v) + (v < 0 ? 1 : 0);
+    return n > width ? n : width;
+}
+
+// "%<width>.<prec>E": the printed exponent X lies in [floor(e2 log10 2), floor((e2+1) log10 2) + 1]
+// with e2 = floor(log2 |x|), so for -325 <= e2 <= 321 it has two digits.
+GAIN_HD int len_E(double x, int width, int prec) {
+    const Parts p = decompose(x);
+    int body = -1;
+    if (p.nan || p.inf) {
+        body = 3 + (p.neg ? 1 : 0);
+    } else if (p.m == 0) {
+        body = (p.neg ? 1 : 0) + 1 + (prec ? 1 + prec : 0) + 4;
+    } else {
+        const int e2 = p.e + 63 - clz64(p.m);
+        if (e2 >= -325 && e2 <= 321) body = (p.neg ? 1 : 0) + 1 + (prec ? 1 + prec : 0) + 4;
+    }
+    if (body < 0) {
+        Sink c{nullptr, 0, 0};
+        put_E(c, x, 0, prec);
+        body = (int)c.n;
+    }
+    return body > width ? body : width;
+}
+
+// "%<width>.<prec>f": rounding moves the integer part from floor(|x|) to at most one more, so
+// when both have the same number of digits (and |x| < 2^53) that is the width of the text.
+GAIN_HD int len_F(double x, int width, int prec) {
+    const Parts p = decompose(x);
+    int body = -1;
+    if (p.nan || p.inf) {
+        body = 3 + (p.neg ? 1 : 0);
+    } else {
+        const double a = x < 0 ? -x : x;
+        if (a < 9007199254740992.0) {
+            const uint64_t ip = (uint64_t)a;
+            const int nd = ndigits(ip);
+            if (ndigits(ip + 1) == nd) body = (p.neg ? 1 : 0) + nd + (prec ? 1 + prec : 0);
+        }
+    }
+    if (body < 0) {
+        Sink c{nullptr, 0, 0};
+        put_F(c, x, 0, prec);
+        body = (int)c.n;
+    }
+    return body > width ? body : width;
+}
+
 // One line of the list exactly as Output.cpp:99-111 writes it (sprintf into the buffer,
 // then fprintf "%s || \n"); levels are 0-based and printed + 1, symmetries likewise.
 struct LineFields {
@@ -347,6 +398,18 @@ GAIN_HD void put_line(Sink& s, const LineFields& f) {
         s.puts(" ] ");
     }
     s.puts(" || \n");
+}
+
+// The length put_line writes for f.
+GAIN_HD long line_len(const LineFields& f) {
+    long n = len_F(f.nu, 12, 6) + 1 + len_d(f.indexF + 1, 8) + 1 + len_d(f.jF, 4) + 1 + len_d(f.gammaF + 1, 4) + 4 +
+             len_d(f.indexI + 1, 8) + 1 + len_d(f.jI, 4) + 1 + len_d(f.gammaI + 1, 4) + 1 + len_E(f.A, 16, 9) + 1;
+    if (f.with_intensity) n += len_E(f.intensity, 16, 9) + 1;
+    if (f.amps && f.namp > 0) {
+        n += 2 + 3;
+        for (int i = 0; i < f.namp; ++i) n += 1 + len_E(f.amps[i], 16, 9);
+    }
+    return n + 5;
 }
 
 }  // namespace fmt

@@ -2,13 +2,16 @@
 // as Output::OutputLinestrength prints it (BaseClasses/Output.cpp:99-111), compacted into one
 // contiguous buffer in row-major (lower state, then upper state) order.
 //
-// Three launches over the rows x cols lines, 2048 lines per block (256 threads x 8 lines):
+// Three launches over the rows x cols lines, 1024 lines per block (256 threads x 4 lines):
 //   k_text_len    S/A/I of each line (line_eval), its text length (0 when not written) and
-//                 the block's byte total;
-//   k_text_offs   exclusive scan of the block totals (one block);
-//   k_text_write  the block-local scan of the lengths, then each thread writes its lines.
-// The length pass runs the same conversion as the write pass with a counting sink, so the
-// offsets hold for any value (wide %f fields, three-digit exponents, NaN).
+//                 the block's byte total; the lengths come from the value ranges where those
+//                 fix them and from the conversion itself elsewhere (wide %f fields,
+//                 three-digit exponents), so they equal what the write pass writes;
+//   k_text_offs   exclusive scan of the block totals, the total and the largest block;
+//   k_text_write  the block-local scan of the lengths; each thread formats its lines into
+//                 shared memory, placed at the block's output offset modulo 16, and the block
+//                 copies its text out in aligned 16-byte stores (whole L2 sectors, no partial
+//                 writes).  A block whose text does not fit shared memory writes directly.
 #include "gain_internal.h"
 #include "linemath.cuh"
 #include "linefmt.h"
@@ -16,14 +19,16 @@
 namespace gain {
 namespace {
 
-constexpr int kTextThreads = 256, kTextItems = 8, kTextSpan = kTextThreads * kTextItems;
+constexpr int kTextThreads = 256, kTextItems = 4, kTextSpan = kTextThreads * kTextItems;
+constexpr int kStageMax = 200 * 1024;   // shared-memory staging of one block's text
 
-__device__ __forceinline__ long line_text(const TextArgs& t, long idx, fmt::Sink& s) {
+// The fields of line idx; false when the line is not written.
+__device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double* a_out, fmt::LineFields& f) {
     const int r = (int)(idx / t.cols), c = (int)(idx - (long)r * t.cols);
     const double a = t.amp[(long)r * t.ld + c];
+    *a_out = a;
     const LineVals v = line_eval(a, t.eI[r], t.eF[c], t.p);
-    if (!v.keep) return 0;
-    fmt::LineFields f;
+    if (!v.keep) return false;
     f.nu = v.nu;
     f.A = v.A;
     f.intensity = v.I;
@@ -34,11 +39,25 @@ __device__ __forceinline__ long line_text(const TextArgs& t, long idx, fmt::Sink
     f.jI = t.jI;
     f.gammaI = t.gammaI;
     f.with_intensity = t.p.with_intensity;
-    f.amps = t.with_amps ? &a : nullptr;
+    f.amps = t.with_amps ? a_out : nullptr;
     f.namp = 1;
+    return true;
+}
+
+__device__ __forceinline__ long line_text(const TextArgs& t, long idx, fmt::Sink& s) {
+    double a;
+    fmt::LineFields f;
+    if (!line_fields(t, idx, &a, f)) return 0;
     const long n0 = s.n;
     fmt::put_line(s, f);
     return s.n - n0;
+}
+
+__device__ __forceinline__ long line_length(const TextArgs& t, long idx) {
+    double a;
+    fmt::LineFields f;
+    if (!line_fields(t, idx, &a, f)) return 0;
+    return fmt::line_len(f);
 }
 
 // Block-wide exclusive scan of one value per thread (256 threads); returns the prefix and
@@ -73,8 +92,7 @@ __global__ void __launch_bounds__(kTextThreads) k_text_len(TextArgs t) {
     for (int i = 0; i < kTextItems; ++i) {
         const long idx = base + i;
         if (idx >= total) break;
-        fmt::Sink s{nullptr, 0, 0};
-        const long n = line_text(t, idx, s);
+        const long n = line_length(t, idx);
         t.lens[idx] = (uint32_t)n;
         sum += (unsigned long long)n;
         kept += n > 0;
@@ -88,18 +106,58 @@ __global__ void __launch_bounds__(kTextThreads) k_text_len(TextArgs t) {
     }
 }
 
-// Exclusive scan of nblocks block totals in place; block_bytes[nblocks] = the text size.
+// Exclusive scan of nblocks block totals in place; block_bytes[nblocks] = the text size,
+// block_bytes[nblocks + 2] = the largest block total.
 __global__ void __launch_bounds__(kTextThreads) k_text_offs(unsigned long long* block_bytes, long nblocks) {
-    unsigned long long carry = 0;
+    unsigned long long carry = 0, mx = 0;
     for (long b0 = 0; b0 < nblocks; b0 += kTextThreads) {
         const long b = b0 + threadIdx.x;
         const unsigned long long v = b < nblocks ? block_bytes[b] : 0ull;
+        mx = v > mx ? v : mx;
         unsigned long long all;
         const unsigned long long pre = block_exclusive_scan(v, &all);
         if (b < nblocks) block_bytes[b] = carry + pre;
         carry += all;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&block_bytes[nblocks + 2], mx);
     if (threadIdx.x == 0) block_bytes[nblocks] = carry;
+}
+
+// The staged write: dynamic shared memory of at least the largest block's text + 16 bytes.
+__global__ void __launch_bounds__(kTextThreads) k_text_write_staged(TextArgs t) {
+    extern __shared__ __align__(16) char stage[];
+    const long total = (long)t.rows * t.cols;
+    const long base = (long)blockIdx.x * kTextSpan + (long)threadIdx.x * kTextItems;
+    unsigned long long mine = 0;
+    for (int i = 0; i < kTextItems; ++i)
+        if (base + i < total) mine += t.lens[base + i];
+    unsigned long long all;
+    const unsigned long long pre = block_exclusive_scan(mine, &all);
+    const unsigned long long D = t.block_bytes[blockIdx.x];
+    const int pad = (int)(D & 15u);
+    fmt::Sink s{stage + pad + pre, 0, (long)(all - pre)};
+    for (int i = 0; i < kTextItems; ++i) {
+        const long idx = base + i;
+        if (idx >= total) break;
+        if (t.lens[idx]) line_text(t, idx, s);
+    }
+    __syncthreads();
+    // stage[pad + j] -> text[D + j], j < all, both 16-byte aligned from j = head on
+    const unsigned long long lim = t.text_size > D ? t.text_size - D : 0ull;
+    const long n = (long)(all < lim ? all : lim);
+    char* dst = t.text + D;
+    const long h0 = (16 - pad) & 15;
+    const long head = h0 < n ? h0 : n;
+    for (long j = threadIdx.x; j < head; j += kTextThreads) dst[j] = stage[pad + j];
+    const long nbody = (n - head) / 16;
+    const uint4* src4 = reinterpret_cast<const uint4*>(stage + pad + head);
+    uint4* dst4 = reinterpret_cast<uint4*>(dst + head);
+    for (long j = threadIdx.x; j < nbody; j += kTextThreads) dst4[j] = src4[j];
+    for (long j = head + nbody * 16 + threadIdx.x; j < n; j += kTextThreads) dst[j] = stage[pad + j];
 }
 
 __global__ void __launch_bounds__(kTextThreads) k_text_write(TextArgs t) {
@@ -146,10 +204,22 @@ cudaError_t launch_text_len(const TextArgs& t, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_text_write(const TextArgs& t, cudaStream_t st) {
+cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_bytes, cudaStream_t st) {
     const long nb = text_blocks((long)t.rows * t.cols);
     if (nb <= 0) return cudaSuccess;
-    k_text_write<<<(unsigned)nb, kTextThreads, 0, st>>>(t);
+    if (max_block_bytes + 16 <= (unsigned long long)kStageMax) {
+        static bool attr = false;
+        if (!attr) {
+            const cudaError_t e = cudaFuncSetAttribute(k_text_write_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       kStageMax);
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        const size_t smem = (size_t)((max_block_bytes + 16 + 15) & ~15ull);
+        k_text_write_staged<<<(unsigned)nb, kTextThreads, smem, st>>>(t);
+    } else {
+        k_text_write<<<(unsigned)nb, kTextThreads, 0, st>>>(t);
+    }
     return cudaGetLastError();
 }
 
@@ -188,6 +258,24 @@ int gain_format_line_native(char* buf, size_t cap, double nu, int indexF, int jF
     gain::fmt::put_line(s, f);
     buf[s.n] = 0;
     return (int)s.n;
+}
+
+long gain_line_length_native(double nu, int indexF, int jF, int gammaF, int indexI, int jI, int gammaI, double A,
+                             int with_intensity, double intensity, const double* amps, int namp) {
+    gain::fmt::LineFields f;
+    f.nu = nu;
+    f.A = A;
+    f.intensity = intensity;
+    f.indexF = indexF;
+    f.jF = jF;
+    f.gammaF = gammaF;
+    f.indexI = indexI;
+    f.jI = jI;
+    f.gammaI = gammaI;
+    f.with_intensity = with_intensity;
+    f.amps = amps;
+    f.namp = namp;
+    return gain::fmt::line_len(f);
 }
 
 int gain_format_value(char* buf, size_t cap, double x, int conv, int width, int prec) {

@@ -200,6 +200,8 @@ def _declare(L):
     L.gain_format_line.restype = I
     L.gain_format_line_native.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
     L.gain_format_line_native.restype = I
+    L.gain_line_length_native.argtypes = [D, I, I, I, I, I, I, D, I, D, _dp, I]
+    L.gain_line_length_native.restype = ctypes.c_long
     L.gain_format_value.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I]
     L.gain_format_value.restype = I
     U64 = ctypes.c_ulonglong
@@ -314,6 +316,13 @@ def format_line_native(nu, indexF, jF, gammaF, indexI, jI, gammaI, A, intensity=
                                       _p(a, _dp) if a is not None else None, 0 if a is None else len(a))
     assert n > 0
     return buf.raw[:n].decode()
+
+
+def line_length_native(nu, indexF, jF, gammaF, indexI, jI, gammaI, A, intensity=None, amps=None) -> int:
+    a = _f64(amps) if amps is not None else None
+    return int(lib().gain_line_length_native(nu, indexF, jF, gammaF, indexI, jI, gammaI, A,
+                                             int(intensity is not None), 0.0 if intensity is None else intensity,
+                                             _p(a, _dp) if a is not None else None, 0 if a is None else len(a)))
 
 
 def format_value(x: float, conv: str, width: int, prec: int) -> str:

@@ -356,6 +356,10 @@ int gain_format_line(char* buf, size_t cap, double nu, int indexF, int jF, int g
 int gain_format_line_native(char* buf, size_t cap, double nu, int indexF, int jF, int gammaF,
                             int indexI, int jI, int gammaI, double A, int with_intensity,
                             double intensity, const double* amps, int namp);
+/* The length of that text from the value ranges alone where they fix it (the device's
+ * length pass); equal to the length gain_format_line_native returns. */
+long gain_line_length_native(double nu, int indexF, int jF, int gammaF, int indexI, int jI, int gammaI,
+                             double A, int with_intensity, double intensity, const double* amps, int namp);
 /* One value through those conversions: conv 'E' ("%<width>.<prec>E", prec <= 17) or 'f'
  * ("%<width>.<prec>f", prec <= 9); returns the length (minus the length needed when cap is
  * too small, 0 for a bad argument). */

@@ -107,3 +107,20 @@ def test_oracle_line_list_matches_per_line_text(built_lib):
             lines.append(oracle.line_text(nu, levF[c], 5, 0, levI[r], 4, 1, v[1], intens=v[2], amps=[amp[r, c]]))
     assert n == kept > 0
     assert text.decode() == "".join(lines)
+
+
+def test_length_pass_equals_the_converted_length(built_lib):
+    """The device's length pass (value ranges, conversion only outside them) gives the
+    converted text's length for ordinary and extreme fields alike."""
+    import gainls
+    vals = _special_values() + _random_values(2000, 31)
+    rng = np.random.default_rng(12)
+    for i, x in enumerate(vals):
+        y = vals[(7 * i + 3) % len(vals)]
+        z = vals[(11 * i + 5) % len(vals)]
+        idx = int(rng.integers(-5, 10 ** 9))
+        for args in ((x, idx, 3, 1, 4, 2, 0, y), (abs(y), 9, -1, 7, idx, 1, 2, x)):
+            for inten, amps in ((None, None), (z, None), (z, [x, y]), (None, [z])):
+                n = gainls.line_length_native(*args, intensity=inten, amps=amps)
+                t = gainls.format_line_native(*args, intensity=inten, amps=amps)
+                assert n == len(t), (args, inten, amps, t)
