@@ -227,7 +227,7 @@ struct gain_engine_s {
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;   // upper-vector slicing, concurrent with the lower side
     cudaStream_t stc = nullptr;   // asynchronous eigenvector uploads
-    cudaEvent_t ev[8] = {};
+    cudaEvent_t ev[9] = {};
     cudaEvent_t ev_up = nullptr;  // orders an asynchronous upload after queued engine work
     std::vector<long> zkey_V, zkey_H, zkey_U;   // shape/layout the digit buffers were cleared for
     gain::DevArray<double> d3j;
@@ -1679,10 +1679,13 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     return GAIN_OK;
 }
 
-gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, const double* energiesI,
-                                 const double* energiesF, int jI, int jF, int gammaI, int gammaF, int flags,
-                                 unsigned long long* text_bytes, long long* n_lines) {
-    clear_error();
+namespace {
+// The text of the last run's lines: lengths, offsets and (into out, when given and large
+// enough) the text itself, its device-to-host copy in parts that overlap the formatting of
+// the following parts.
+gain_status lines_text(gain_engine e, const gain_line_params* prm, const double* energiesI, const double* energiesF,
+                       int jI, int jF, int gammaI, int gammaF, int flags, char* out, unsigned long long cap,
+                       unsigned long long* text_bytes, long long* n_lines) {
     GAIN_TRY(check_engine(e));
     if (!prm || !energiesI || !energiesF || jI < 0 || jF < 0 || gammaI < 0 || gammaF < 0 ||
         (flags & ~(GAIN_TEXT_INTENSITY | GAIN_TEXT_AMPLITUDES)))
@@ -1723,19 +1726,54 @@ gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, con
     t.text = nullptr;
     t.text_size = 0;
     GAIN_CUDA(launch_text_len(t, st));
-    unsigned long long tot[3] = {0, 0, 0};   // text size, lines, largest block
-    GAIN_CUDA(cudaMemcpyAsync(tot, e->textBlocks.p + nb, sizeof tot, cudaMemcpyDeviceToHost, st));
+    std::vector<unsigned long long> offs(nb + 3);   // block offsets, text size, lines, largest block
+    GAIN_CUDA(cudaMemcpyAsync(offs.data(), e->textBlocks.p, sizeof(unsigned long long) * (nb + 3),
+                              cudaMemcpyDeviceToHost, st));
     GAIN_CUDA(cudaStreamSynchronize(st));
-    GAIN_TRY(e->text.alloc(tot[0] ? tot[0] : 1));
+    const unsigned long long total = offs[nb], lines = offs[nb + 1], largest = offs[nb + 2];
+    if (text_bytes) *text_bytes = total;
+    if (n_lines) *n_lines = (long long)lines;
+    GAIN_TRY(e->text.alloc(total ? total : 1));
     t.text = e->text.p;
-    t.text_size = tot[0];
-    GAIN_CUDA(launch_text_write(t, tot[2], st));
+    t.text_size = total;
+    const bool copy = out && cap >= total;
+    // parts of at least 2048 blocks (about 200 MB of text) each, at most 8
+    const long nparts = copy ? std::max(1L, std::min(8L, nb / 2048)) : 1;
+    for (long part = 0; part < nparts; ++part) {
+        const long b0 = nb * part / nparts, b1 = nb * (part + 1) / nparts;
+        GAIN_CUDA(launch_text_write(t, largest, b0, b1, st));
+        if (copy) {
+            const unsigned long long o0 = offs[b0], o1 = b1 < nb ? offs[b1] : total;
+            GAIN_CUDA(cudaEventRecord(e->ev[8], st));
+            GAIN_CUDA(cudaStreamWaitEvent(e->stc, e->ev[8], 0));
+            if (o1 > o0) GAIN_CUDA(cudaMemcpyAsync(out + o0, e->text.p + o0, o1 - o0, cudaMemcpyDeviceToHost, e->stc));
+        }
+    }
     GAIN_CUDA(cudaStreamSynchronize(st));
-    e->text_bytes = tot[0];
+    if (copy) GAIN_CUDA(cudaStreamSynchronize(e->stc));
+    e->text_bytes = total;
     e->have_text = true;
-    if (text_bytes) *text_bytes = tot[0];
-    if (n_lines) *n_lines = (long long)tot[1];
+    if (out && !copy)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines_text_host: buffer of %llu bytes, text of %llu", cap,
+                         total);
     return GAIN_OK;
+}
+}  // namespace
+
+gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                 const double* energiesF, int jI, int jF, int gammaI, int gammaF, int flags,
+                                 unsigned long long* text_bytes, long long* n_lines) {
+    clear_error();
+    return lines_text(e, prm, energiesI, energiesF, jI, jF, gammaI, gammaF, flags, nullptr, 0, text_bytes, n_lines);
+}
+
+gain_status gain_pair_lines_text_host(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                      const double* energiesF, int jI, int jF, int gammaI, int gammaF, int flags,
+                                      char* out, unsigned long long cap, unsigned long long* text_bytes,
+                                      long long* n_lines) {
+    clear_error();
+    if (!out) return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines_text_host: NULL output");
+    return lines_text(e, prm, energiesI, energiesF, jI, jF, gammaI, gammaF, flags, out, cap, text_bytes, n_lines);
 }
 
 gain_status gain_fetch_lines_text(gain_engine e, char* out, unsigned long long cap) {

@@ -140,7 +140,9 @@ struct TextArgs {
 long text_blocks(long lines);
 cudaError_t launch_text_len(const TextArgs& t, cudaStream_t st);     // lens, offsets, total, nkeep
 // the text itself; max_block_bytes = the largest block total (block_bytes[text_blocks + 2])
-cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_bytes, cudaStream_t st);
+// blocks [b0, b1) of the text
+cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_bytes, long b0, long b1,
+                              cudaStream_t st);
 cudaError_t launch_format_values(long n, const double* vals, int conv, int width, int prec, char* out,
                                  int stride, int* lens, cudaStream_t st);
 

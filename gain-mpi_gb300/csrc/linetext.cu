@@ -128,16 +128,17 @@ __global__ void __launch_bounds__(kTextThreads) k_text_offs(unsigned long long* 
 }
 
 // The staged write: dynamic shared memory of at least the largest block's text + 16 bytes.
-__global__ void __launch_bounds__(kTextThreads) k_text_write_staged(TextArgs t) {
+__global__ void __launch_bounds__(kTextThreads) k_text_write_staged(TextArgs t, long block0) {
     extern __shared__ __align__(16) char stage[];
+    const long blk = block0 + blockIdx.x;
     const long total = (long)t.rows * t.cols;
-    const long base = (long)blockIdx.x * kTextSpan + (long)threadIdx.x * kTextItems;
+    const long base = blk * kTextSpan + (long)threadIdx.x * kTextItems;
     unsigned long long mine = 0;
     for (int i = 0; i < kTextItems; ++i)
         if (base + i < total) mine += t.lens[base + i];
     unsigned long long all;
     const unsigned long long pre = block_exclusive_scan(mine, &all);
-    const unsigned long long D = t.block_bytes[blockIdx.x];
+    const unsigned long long D = t.block_bytes[blk];
     const int pad = (int)(D & 15u);
     fmt::Sink s{stage + pad + pre, 0, (long)(all - pre)};
     for (int i = 0; i < kTextItems; ++i) {
@@ -160,15 +161,16 @@ __global__ void __launch_bounds__(kTextThreads) k_text_write_staged(TextArgs t) 
     for (long j = head + nbody * 16 + threadIdx.x; j < n; j += kTextThreads) dst[j] = stage[pad + j];
 }
 
-__global__ void __launch_bounds__(kTextThreads) k_text_write(TextArgs t) {
+__global__ void __launch_bounds__(kTextThreads) k_text_write(TextArgs t, long block0) {
+    const long blk = block0 + blockIdx.x;
     const long total = (long)t.rows * t.cols;
-    const long base = (long)blockIdx.x * kTextSpan + (long)threadIdx.x * kTextItems;
+    const long base = blk * kTextSpan + (long)threadIdx.x * kTextItems;
     unsigned long long mine = 0;
     for (int i = 0; i < kTextItems; ++i)
         if (base + i < total) mine += t.lens[base + i];
     unsigned long long all;
     const unsigned long long pre = block_exclusive_scan(mine, &all);
-    const unsigned long long off = t.block_bytes[blockIdx.x] + pre;   // bounded by the text size
+    const unsigned long long off = t.block_bytes[blk] + pre;   // bounded by the text size
     fmt::Sink s{t.text + off, 0, (long)(t.text_size > off ? t.text_size - off : 0)};
     for (int i = 0; i < kTextItems; ++i) {
         const long idx = base + i;
@@ -204,9 +206,11 @@ cudaError_t launch_text_len(const TextArgs& t, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_bytes, cudaStream_t st) {
+cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_bytes, long b0, long b1,
+                              cudaStream_t st) {
     const long nb = text_blocks((long)t.rows * t.cols);
-    if (nb <= 0) return cudaSuccess;
+    if (b1 > nb) b1 = nb;
+    if (b0 < 0 || b1 <= b0) return cudaSuccess;
     if (max_block_bytes + 16 <= (unsigned long long)kStageMax) {
         static bool attr = false;
         if (!attr) {
@@ -216,9 +220,9 @@ cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_by
             attr = true;
         }
         const size_t smem = (size_t)((max_block_bytes + 16 + 15) & ~15ull);
-        k_text_write_staged<<<(unsigned)nb, kTextThreads, smem, st>>>(t);
+        k_text_write_staged<<<(unsigned)(b1 - b0), kTextThreads, smem, st>>>(t, b0);
     } else {
-        k_text_write<<<(unsigned)nb, kTextThreads, 0, st>>>(t);
+        k_text_write<<<(unsigned)(b1 - b0), kTextThreads, 0, st>>>(t, b0);
     }
     return cudaGetLastError();
 }

@@ -208,6 +208,8 @@ def _declare(L):
     L.gain_pair_lines_text.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, I, I, I,
                                        ctypes.POINTER(U64), ctypes.POINTER(ctypes.c_longlong)]
     L.gain_fetch_lines_text.argtypes = [_vp, ctypes.c_void_p, U64]
+    L.gain_pair_lines_text_host.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, I, I, I,
+                                            ctypes.c_void_p, U64, ctypes.POINTER(U64), ctypes.POINTER(ctypes.c_longlong)]
     L.gain_lines_text_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(U64)]
     L.gain_format_values_device.argtypes = [_dp, ctypes.c_longlong, I, I, I, ctypes.c_char_p, I, _ip]
     FP, SP = ctypes.POINTER(Filters), ctypes.POINTER(State)
@@ -244,7 +246,8 @@ def _declare(L):
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
-                 "gain_pair_lines", "gain_pair_lines_text", "gain_fetch_lines_text", "gain_lines_text_device",
+                 "gain_pair_lines", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
+                 "gain_lines_text_device",
                  "gain_format_values_device"):
         getattr(L, name).restype = S
 
@@ -504,7 +507,23 @@ def _lines_text(self, eI, eF, jI, jF, gammaI, gammaF, temperature=296.0, q_part=
     return memoryview(out)[:nb.value], nl.value
 
 
+def _lines_text_host(self, eI, eF, jI, jF, gammaI, gammaF, out, temperature=296.0, q_part=1.0, zpe=0.0,
+                     thresh=0.0, freq=(-1e9, 1e9), gnsF=1.0, intensity=True, amplitudes=False):
+    """gain_pair_lines_text_host: the text formed on the device and copied into out (a uint8
+    array, page-locked for the overlap) part by part.  Returns (text view, n_lines)."""
+    eI, eF = _f64(eI), _f64(eF)
+    assert out.dtype == np.uint8 and out.flags.c_contiguous
+    prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
+    nb, nl = ctypes.c_ulonglong(), ctypes.c_longlong()
+    flags = (TEXT_INTENSITY if intensity else 0) | (TEXT_AMPLITUDES if amplitudes else 0)
+    check(lib().gain_pair_lines_text_host(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF, gammaI,
+                                          gammaF, flags, out.ctypes.data, out.size, ctypes.byref(nb),
+                                          ctypes.byref(nl)))
+    return memoryview(out)[:nb.value], nl.value
+
+
 Engine.lines_text = _lines_text
+Engine.lines_text_host = _lines_text_host
 TEXT_INTENSITY, TEXT_AMPLITUDES = 1, 2
 
 

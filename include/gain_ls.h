@@ -284,6 +284,14 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
 gain_status gain_pair_lines_text(gain_engine e, const gain_line_params* prm, const double* energiesI,
                                  const double* energiesF, int jI, int jF, int gammaI, int gammaF,
                                  int flags, unsigned long long* text_bytes, long long* n_lines);
+/* gain_pair_lines_text with the text copied into out as it is formed: the copy of each
+ * part overlaps the formatting of the next (page-locked out for that overlap).  cap must
+ * hold the whole text; otherwise nothing is copied, *text_bytes holds its size and the call
+ * returns GAIN_ERR_INVALID_ARG (the text stays on the device for gain_fetch_lines_text). */
+gain_status gain_pair_lines_text_host(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                      const double* energiesF, int jI, int jF, int gammaI, int gammaF,
+                                      int flags, char* out, unsigned long long cap,
+                                      unsigned long long* text_bytes, long long* n_lines);
 /* Copy the text of the last gain_pair_lines_text call into out (cap >= text_bytes). */
 gain_status gain_fetch_lines_text(gain_engine e, char* out, unsigned long long cap);
 /* Device address and size of that text (valid until the next gain_pair_lines_text). */

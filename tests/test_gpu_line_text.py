@@ -97,3 +97,16 @@ def test_text_device_pointer_and_small_buffer(pair_run):
     small = np.empty(len(text) - 1, np.uint8)
     with pytest.raises(gainls.GainError):
         gainls.check(gainls.lib().gain_fetch_lines_text(eng.h, small.ctypes.data, small.size))
+
+
+def test_text_into_host_buffer_part_by_part(pair_run):
+    """gain_pair_lines_text_host gives the text gain_pair_lines_text builds; a buffer that is
+    too small is refused with the size reported."""
+    import gainls
+    p, eng, lo, up, eI, eF = pair_run
+    ref, n = eng.lines_text(eI, eF, 2, 3, 0, 1, amplitudes=True)
+    out = np.zeros(len(ref) + 7, np.uint8)
+    got, n2 = eng.lines_text_host(eI, eF, 2, 3, 0, 1, out, amplitudes=True)
+    assert n2 == n and bytes(got) == bytes(ref)
+    with pytest.raises(gainls.GainError, match="buffer"):
+        eng.lines_text_host(eI, eF, 2, 3, 0, 1, np.zeros(len(ref) - 1, np.uint8), amplitudes=True)
