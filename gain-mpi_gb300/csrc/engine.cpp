@@ -1737,8 +1737,8 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
     t.text = e->text.p;
     t.text_size = total;
     const bool copy = out && cap >= total;
-    // parts of at least 2048 blocks (about 200 MB of text) each, at most 8
-    const long nparts = copy ? std::max(1L, std::min(8L, nb / 2048)) : 1;
+    // parts of at least 64 blocks (about 6 MB of text) each, at most 8
+    const long nparts = copy ? std::max(1L, std::min(8L, nb / 64)) : 1;
     for (long part = 0; part < nparts; ++part) {
         const long b0 = nb * part / nparts, b1 = nb * (part + 1) / nparts;
         GAIN_CUDA(launch_text_write(t, largest, b0, b1, st));

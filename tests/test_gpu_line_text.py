@@ -110,3 +110,20 @@ def test_text_into_host_buffer_part_by_part(pair_run):
     assert n2 == n and bytes(got) == bytes(ref)
     with pytest.raises(gainls.GainError, match="buffer"):
         eng.lines_text_host(eI, eF, 2, 3, 0, 1, np.zeros(len(ref) - 1, np.uint8), amplitudes=True)
+
+
+def test_text_into_host_buffer_in_several_parts(built_lib):
+    """A pair large enough for the copy to run in several parts (230 k lines)."""
+    import gainls
+    import synth
+    p = synth.make_problem(120, [7, 8], "c4", blocks=[(7, 0), (8, 1)])
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    bI, bF = p.blocks[(0, 0)], p.blocks[(1, 1)]
+    lo, up = list(range(bI.vecs.shape[0])), list(range(bF.vecs.shape[0]))
+    assert len(lo) * len(up) > 200_000
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    ref, n = eng.lines_text(bI.energies, bF.energies, 7, 8, 0, 1)
+    out = np.zeros(len(ref), np.uint8)
+    got, n2 = eng.lines_text_host(bI.energies, bF.energies, 7, 8, 0, 1, out)
+    assert n2 == n and bytes(got) == bytes(ref)
