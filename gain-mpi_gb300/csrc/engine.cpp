@@ -1659,15 +1659,17 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     cudaStream_t st = e->st;
     GAIN_TRY(e->eIdev.upload(energiesI, rows));
     GAIN_TRY(e->eFdev.upload(energiesF, cols));
-    GAIN_TRY(e->lineS.alloc(n));
-    GAIN_TRY(e->lineA.alloc(n));
-    GAIN_TRY(e->lineI.alloc(n));
-    GAIN_TRY(e->lineKeep.alloc(n));
+    if (S) GAIN_TRY(e->lineS.alloc(n));
+    if (A) GAIN_TRY(e->lineA.alloc(n));
+    if (I) GAIN_TRY(e->lineI.alloc(n));
+    if (keep) GAIN_TRY(e->lineKeep.alloc(n));
     GAIN_TRY(e->ull.alloc(4));
     GAIN_TRY(e->ull.zero(st, 4));
     const LineParams p = line_params(prm, jI, jF, I != nullptr);
-    GAIN_CUDA(launch_lines(rows, cols, e->amp.p, e->amp_ld, e->eIdev.p, e->eFdev.p, p, e->lineS.p, e->lineA.p,
-                           e->lineI.p, e->lineKeep.p, e->ull.p + 1, st));
+    // only the requested outputs are written
+    GAIN_CUDA(launch_lines(rows, cols, e->amp.p, e->amp_ld, e->eIdev.p, e->eFdev.p, p, S ? e->lineS.p : nullptr,
+                           A ? e->lineA.p : nullptr, I ? e->lineI.p : nullptr, keep ? e->lineKeep.p : nullptr,
+                           e->ull.p + 1, st));
     unsigned long long nk = 0;
     GAIN_CUDA(cudaMemcpyAsync(&nk, e->ull.p + 1, sizeof nk, cudaMemcpyDeviceToHost, st));
     if (S) GAIN_CUDA(cudaMemcpyAsync(S, e->lineS.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
