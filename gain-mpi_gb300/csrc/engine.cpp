@@ -255,6 +255,7 @@ struct gain_engine_s {
     long amp_ld = 0;
     bool have_amp = false;
     std::vector<int> amp_job;   // jindI, gammaI, jindF, gammaF, lower levels, upper levels of amp
+    long launches = 0;          // kernels this engine has launched (split path and band builds)
 
     // work buffers
     gain::DevArray<int> d_lower, d_upper;
@@ -700,6 +701,7 @@ gain_status launch_layout_band(gain_engine e, const gain_pair_job* j) {
     ba.nlevelF = wt ? wt->nF : 0;
     ba.maxdeg = wt ? wt->maxdeg : 0;
     GAIN_CUDA(split::launch_band(ba, e->st));
+    ++e->launches;
     return GAIN_OK;
 }
 
@@ -756,6 +758,7 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     a.inerr2_prev = inerr_prev;
     a.e_prev = e_prev;
     GAIN_CUDA(split::launch_slice(a, st));
+    ++e->launches;
     return GAIN_OK;
 }
 
@@ -769,6 +772,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "split path handles non-degenerate symmetries only");
     const double tol = (opts && opts->tol > 0) ? opts->tol : 4.5e-9;
     cudaStream_t st = e->st;
+    const long launches0 = e->launches;
     GAIN_CUDA(cudaEventRecord(e->ev[0], st));
     // dipole pieces (MultiGpuManager::ExecuteHalfLs's block loop): H accumulates the first
     // GEMM of every piece, the second GEMM runs once
@@ -960,7 +964,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         g1.cols_valid = L.fpad;
         g1.err = e->err.p;
         if (piece == 0) GAIN_CUDA(cudaEventRecord(e->ev[2], st));
-        if (!t1.empty()) GAIN_CUDA(split::launch_gemm(tmV, pair ? L.tmBandPair : L.tmBand, g1, e->num_sms, st, pair));
+        if (!t1.empty()) {
+            GAIN_CUDA(split::launch_gemm(tmV, pair ? L.tmBandPair : L.tmBand, g1, e->num_sms, st, pair));
+            ++e->launches;
+        }
         if (piece == npieces - 1) GAIN_CUDA(cudaEventRecord(e->ev[3], st));
         if (piece == 0) {
             // ---- upper vectors -> digits on the low-priority second stream
@@ -988,7 +995,11 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         rh.eA = e->Vst.e.p;
         rh.rowerr2 = e->rowerr.p;
         GAIN_CUDA(split::launch_refine_h(rh, 2 * e->num_sms, st));
-        if (npieces > 1) GAIN_CUDA(launch_add(e->acc.p, e->H.p, (long)Bpad * L.fpad, st));
+        ++e->launches;
+        if (npieces > 1) {
+            GAIN_CUDA(launch_add(e->acc.p, e->H.p, (long)Bpad * L.fpad, st));
+            ++e->launches;
+        }
     }
     if (npieces > 1)
         GAIN_CUDA(cudaMemcpyAsync(e->H.p, e->acc.p, sizeof(double) * (size_t)Bpad * L.fpad, cudaMemcpyDeviceToDevice, st));
@@ -1045,6 +1056,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.err = e->err.p;
     GAIN_CUDA(cudaEventRecord(e->ev[4], st));
     GAIN_CUDA(split::launch_gemm(tmH, tmU, g2, e->num_sms, st, pair));
+    ++e->launches;
     GAIN_CUDA(cudaEventRecord(e->ev[5], st));
     split::RefineAmpArgs ra;
     ra.flags = e->flags2.p;
@@ -1066,6 +1078,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     ra.uncertified = e->ull.p;
     ra.uncertified_weak = e->ull.p + 3;
     GAIN_CUDA(split::launch_refine_amp(ra, 4 * e->num_sms, st));
+    ++e->launches;
     GAIN_CUDA(cudaEventRecord(e->ev[1], st));
     GAIN_CUDA(cudaStreamSynchronize(st));
 
@@ -1103,7 +1116,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         stats->chunks2 = p2.chunks;
         stats->products1 = (int)pr1.size();
         stats->products2 = (int)pr2.size();
-        stats->kernel_launches = 10;
+        stats->kernel_launches = e->launches - launches0;
         double f = 0;
         for (auto& t : t1) f += 2.0 * split::BM * split::BN * split::BK * (double)t.nkb * p1x.slices * (p1x.slices + 1) / 2;
         for (auto& t : t2) f += 2.0 * split::BM * split::BN * split::BK * (double)t.nkb * p2.slices * (p2.slices + 1) / 2;
