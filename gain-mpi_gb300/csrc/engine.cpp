@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -209,6 +210,10 @@ struct PairLayout {
     CUtensorMap tmBand, tmBandPair;   // 128-row boxes; 64-row boxes for a CTA pair
 };
 
+size_t layout_bytes(const PairLayout& L) {
+    return L.band.n * sizeof(double) + L.bandDig.n * sizeof(__nv_bfloat16);
+}
+
 // Plain-path structures of one block pair.
 struct PlainLayout {
     int key[4] = {-1, -1, -1, -1};
@@ -280,7 +285,9 @@ struct gain_engine_s {
     unsigned long long text_bytes = 0;
     bool have_text = false;
 
-    gain::PairLayout layout;
+    // split-path layouts (band, its digits, padded index maps) per block pair, kept across runs
+    std::map<std::array<int, 4>, std::unique_ptr<gain::PairLayout>> layouts;
+    gain::PairLayout* cur = nullptr;   // the layout of the current run
     gain::PlainLayout plain;
 };
 
@@ -559,8 +566,23 @@ std::vector<split::Prod> make_prods(const SplitParams& p) {
 gain_status launch_layout_band(gain_engine e, const gain_pair_job* j);
 
 gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, GammaMaps* mF) {
-    PairLayout& L = e->layout;
     const int key[4] = {j->jindI, j->gammaI, j->jindF, j->gammaF};
+    const std::array<int, 4> akey = {key[0], key[1], key[2], key[3]};
+    auto it = e->layouts.find(akey);
+    if (it == e->layouts.end()) {
+        // bound the cache: band and band digits of every cached pair below a quarter of the
+        // device memory that is free now (the current pair's are built next)
+        size_t cached = 0;
+        for (auto& kv : e->layouts) cached += layout_bytes(*kv.second);
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && cached > free_b / 4) {
+            GAIN_CUDA(cudaStreamSynchronize(e->st));
+            e->layouts.clear();
+        }
+        it = e->layouts.emplace(akey, std::unique_ptr<PairLayout>(new PairLayout())).first;
+    }
+    e->cur = it->second.get();
+    PairLayout& L = *e->cur;
     const WignerTab* wt = wigner_of(e, j->jindI, j->jindF);
     const long wv = wt ? wt->version : 0;
     if (std::equal(key, key + 4, L.key) && L.dip_version == e->dip_version && L.wig_version == wv) return GAIN_OK;
@@ -663,7 +685,7 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
 // The rotational-dipole band of the current layout from the dipole piece now on the device
 // (rows whose upper vibrational index lies outside the piece are zero).
 gain_status launch_layout_band(gain_engine e, const gain_pair_job* j) {
-    PairLayout& L = e->layout;
+    PairLayout& L = *e->cur;
     const WignerTab* wt = wigner_of(e, j->jindI, j->jindF);
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
@@ -779,7 +801,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     const int npieces = e->pieces.size() > 1 ? (int)e->pieces.size() : 1;
     if (npieces > 1) GAIN_TRY(load_piece(e, 0));
     GAIN_TRY(build_layout(e, j, mI, mF));
-    PairLayout& L = e->layout;
+    PairLayout& L = *e->cur;
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
     // an asynchronous upload of the lower vectors must land before the lower slicing; the upper
@@ -1331,7 +1353,8 @@ gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const i
     GAIN_TRY(b.dvib.upload(b.vib));
     GAIN_TRY(b.dkblock.upload(b.kblock));
     b.present = true;
-    e->layout.key[0] = -1;
+    e->layouts.clear();
+    e->cur = nullptr;
     e->plain.key[0] = -1;
     if (e->infl[jind].present)
         for (auto& m : e->infl[jind].maps) m->built = false;
@@ -1386,7 +1409,8 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
     GAIN_TRY(inf.dicontr.upload(inf.icontr));
     GAIN_TRY(inf.dijterms.upload(inf.ijterms));
     inf.present = true;
-    e->layout.key[0] = -1;
+    e->layouts.clear();
+    e->cur = nullptr;
     e->plain.key[0] = -1;
     return GAIN_OK;
 }
