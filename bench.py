@@ -147,7 +147,7 @@ def setup_engine(inp, device_index: int):
     eng = gainls.Engine(11, 4, 1, device=device_index)
     for jind, (b, inf) in enumerate(zip(inp["bases"], inp["infl"])):
         eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
-        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, 1, inf.N, inf.repres,
+        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, inf.matsize, inf.N, inf.repres,
                              inf.Ntot, inf.sdeg)
     nv = inp["nv"]
     eng.upload_dipole(inp["dipole"].reshape(-1), nv, 0, nv, nv)

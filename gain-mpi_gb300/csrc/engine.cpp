@@ -208,6 +208,16 @@ struct PairLayout {
     DevArray<__nv_bfloat16> bandDig;
     StatsDev bandStats;
     CUtensorMap tmBand, tmBandPair;   // 128-row boxes; 64-row boxes for a CTA pair
+    // an expansion that mixes primitives (not a selection): both GEMM1 layouts run over the
+    // primitives the expansions touch; H = V T_I M is contracted with T_F before GEMM2,
+    // whose inner dimension is then the nsymF symmetric functions padded to ntpad
+    bool general = false;
+    int nsymF = 0, ntpad = 0;
+    double sigmaF = 1.0, gamF = 0.0;      // ||T_F||_2 bound; FP64 contraction rounding factor
+    std::vector<int> cF_ptr, cF_col;      // T_F^T as CSR over symmetric functions, columns in F layout
+    std::vector<double> cF_val;
+    DevArray<int> d_cF_ptr, d_cF_col, d_ident;
+    DevArray<double> d_cF_val;
 };
 
 size_t layout_bytes(const PairLayout& L) {
@@ -269,7 +279,8 @@ struct gain_engine_s {
     gain::DevArray<int> adj_iota;
     gain::DevArray<__nv_bfloat16> Vdig, Hdig, Udig;
     gain::StatsDev Vst, Hst, Ust;
-    gain::DevArray<double> H;
+    gain::DevArray<double> H, Hsym;   // H in the GEMM1 layout; contracted with a mixing expansion
+    gain::DevArray<int> iota;
     gain::DevArray<float> rowerr;
     gain::DevArray<int2> flags1, flags2;
     gain::DevArray<unsigned int> counters;      // [0] nflags1 [1] nflags2
@@ -589,11 +600,19 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     L.rotsym = wt != nullptr;
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
-    L.nI = (int)mI->sym_prim.size();
-    L.nF = (int)mF->sym_prim.size();
-    // lower layout: symmetry functions grouped by K, each group padded to BK
+    // The units of each layout: with selection expansions the symmetric functions (a primitive
+    // times a coefficient each); otherwise the primitives the expansions touch, the lower
+    // vectors expanded before the first GEMM and H contracted after it.
+    L.general = !(mI->selection && mF->selection);
+    const std::vector<int>& uI = L.general ? mI->support : mI->sym_prim;
+    const std::vector<int>& uF = L.general ? mF->support : mF->sym_prim;
+    auto coefI = [&](int s) { return L.general ? 1.0 : mI->sym_coef[s]; };
+    auto coefF = [&](int s) { return L.general ? 1.0 : mF->sym_coef[s]; };
+    L.nI = (int)uI.size();
+    L.nF = (int)uF.size();
+    // lower layout: units grouped by K, each group padded to BK
     std::vector<std::vector<int>> byK(bI.J + 1);
-    for (int s = 0; s < L.nI; ++s) byK[bI.K[mI->sym_prim[s]]].push_back(s);
+    for (int s = 0; s < L.nI; ++s) byK[bI.K[uI[s]]].push_back(s);
     L.kpad_startI.assign(bI.J + 2, 0);
     for (int k = 0; k <= bI.J; ++k) L.kpad_startI[k + 1] = L.kpad_startI[k] + round_up((int)byK[k].size(), split::BK);
     L.kpadI = std::max(L.kpad_startI[bI.J + 1], split::BK);
@@ -605,13 +624,13 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
         for (size_t x = 0; x < byK[k].size(); ++x) {
             const int s = byK[k][x], pos = L.kpad_startI[k] + (int)x;
             L.colposI[s] = pos;
-            L.i_sym[pos] = s;
-            L.i_prim[pos] = mI->sym_prim[s];
-            L.i_coef[pos] = mI->sym_coef[s];
+            L.i_sym[pos] = L.general ? uI[s] : s;   // source column: primitive (expanded) or symmetric
+            L.i_prim[pos] = uI[s];
+            L.i_coef[pos] = coefI(s);
         }
     // upper layout: grouped by K, each group padded to BN
     std::vector<std::vector<int>> byKF(bF.J + 1);
-    for (int s = 0; s < L.nF; ++s) byKF[bF.K[mF->sym_prim[s]]].push_back(s);
+    for (int s = 0; s < L.nF; ++s) byKF[bF.K[uF[s]]].push_back(s);
     L.fblocks.clear();
     int pos = 0;
     L.colposF.assign(L.nF, 0);
@@ -640,8 +659,8 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
                 const int s = byKF[k][x];
                 L.colposF[s] = p2 + x;
                 L.f_sym[p2 + x] = s;
-                L.f_prim[p2 + x] = mF->sym_prim[s];
-                L.f_coef[p2 + x] = mF->sym_coef[s];
+                L.f_prim[p2 + x] = uF[s];
+                L.f_coef[p2 + x] = coefF(s);
             }
             p2 += round_up(n, split::BN);
         }
@@ -660,6 +679,43 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
         L.band_k0[r] = L.kpad_startI[klo];
         L.band_len[r] = L.kpad_startI[khi + 1] - L.kpad_startI[klo];
         L.W = std::max(L.W, L.band_len[r]);
+    }
+    if (L.general) {
+        // T_F^T as CSR over the symmetric functions, its columns moved to the F layout
+        Inflation& iF = e->infl[j->jindF];
+        L.nsymF = iF.Ntot[j->gammaF];
+        L.ntpad = std::max(round_up(L.nsymF, split::BK), split::BK);
+        std::vector<int> unit_of(bF.dimen, -1);
+        for (int u = 0; u < L.nF; ++u) unit_of[uF[u]] = u;
+        L.cF_ptr.assign(mF->csr_ptr.begin(), mF->csr_ptr.end());
+        L.cF_col.resize(mF->csr_col.size());
+        L.cF_val.assign(mF->csr_val.begin(), mF->csr_val.end());
+        std::vector<double> rowsum(L.nF, 0.0);
+        double colmax = 0.0;
+        int kmax = 1;
+        for (int sy = 0; sy < L.nsymF; ++sy) {
+            double cs = 0.0;
+            kmax = std::max(kmax, L.cF_ptr[sy + 1] - L.cF_ptr[sy]);
+            for (int q = L.cF_ptr[sy]; q < L.cF_ptr[sy + 1]; ++q) {
+                const int u = unit_of[mF->csr_col[q]];
+                L.cF_col[q] = L.colposF[u];
+                cs += std::fabs(L.cF_val[q]);
+                rowsum[u] += std::fabs(L.cF_val[q]);
+            }
+            colmax = std::max(colmax, cs);
+        }
+        double rowmax = 0.0;
+        for (double v : rowsum) rowmax = std::max(rowmax, v);
+        // Schur bound of ||T_F||_2, and the FP64 summation bound gamma_k = k u / (1 - k u)
+        L.sigmaF = std::sqrt(rowmax * colmax) * (1.0 + 1e-12);
+        const double u = std::ldexp(1.0, -53);
+        L.gamF = (kmax * u) / (1.0 - kmax * u) * (1.0 + 1e-12);
+        std::vector<int> ident(L.nsymF);
+        for (int q = 0; q < L.nsymF; ++q) ident[q] = q;
+        GAIN_TRY(L.d_cF_ptr.upload(L.cF_ptr));
+        GAIN_TRY(L.d_cF_col.upload(L.cF_col));
+        GAIN_TRY(L.d_cF_val.upload(L.cF_val));
+        GAIN_TRY(L.d_ident.upload(ident));
     }
     GAIN_TRY(L.d_colposI.upload(L.colposI));
     GAIN_TRY(L.d_i_sym.upload(L.i_sym));
@@ -788,9 +844,6 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI);
     GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF);
     if (!mI || !mF) return GAIN_ERR_OOM;
-    if (!mI->selection || !mF->selection)
-        return set_error(GAIN_ERR_UNSUPPORTED,
-                         "split path needs symmetry blocks whose expansion selects one primitive per function");
     if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "split path handles non-degenerate symmetries only");
     const double tol = (opts && opts->tol > 0) ? opts->tol : 4.5e-9;
     cudaStream_t st = e->st;
@@ -827,7 +880,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
             p1x.slices = (56 + p1x.beta - 1) / p1x.beta;
         }
     }
-    const SplitParams p2 = choose_params(L.fpad, opts, 48, 8);
+    const int K2 = L.general ? L.ntpad : L.fpad;   // inner dimension of the second GEMM
+    const SplitParams p2 = choose_params(K2, opts, 48, 8);
     if (p1x.slices * p1x.beta > 62 || p2.slices * p2.beta > 62 || p1x.slices > split::MAX_SLICES ||
         p2.slices > split::MAX_SLICES || p1x.beta < 2 || p1x.beta > 8 || p2.beta < 2 || p2.beta > 8 ||
         2 * (p2.slices - 1) * p2.beta > 126 || 2 * (p1x.slices - 1) * p1x.beta > 126)
@@ -876,8 +930,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     // changes: padding rows and columns are never written, every other entry is.
     const long lkey = (long)L.key[0] * 1000003L + L.key[1] * 1009L + L.key[2] * 31L + L.key[3];
     const size_t vdig = (size_t)p1x.slices * Bpad * L.kpadI;
-    const size_t hdig = (size_t)p2.slices * Bpad * L.fpad;
-    const size_t udig = (size_t)p2.slices * Nupad * L.fpad;
+    const size_t hdig = (size_t)p2.slices * Bpad * K2;
+    const size_t udig = (size_t)p2.slices * Nupad * K2;
     GAIN_TRY(e->Vdig.alloc(vdig));
     GAIN_TRY(e->Vst.alloc(Bpad, p1x.chunks, false));
     GAIN_TRY(e->Hdig.alloc(hdig));
@@ -908,9 +962,35 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     // so it overlaps the lower slicing and precedes the GEMM.
     GAIN_CUDA(cudaEventRecord(e->ev[6], st));
 
-    // ---- lower vectors -> digits in the padded lower layout
-    GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI, Bpad,
-                   e->Vdig.p, p1x, e->Vst, false, nullptr, nullptr, st, L.d_i_sym.p));
+    // ---- lower vectors -> digits in the padded lower layout (expanded to primitives first
+    // when the expansion mixes them)
+    const Basis& bIs = e->bases[j->jindI];
+    if (L.general && B > 65535)
+        return set_error(GAIN_ERR_UNSUPPORTED, "split path with a mixing expansion: at most 65535 lower states per run");
+    if (L.general) {
+        Inflation& iI = e->infl[j->jindI];
+        GAIN_TRY(e->primI.alloc((size_t)B * bIs.dimen));
+        GAIN_TRY(e->iota.alloc(B));
+        {
+            std::vector<int> io(B);
+            for (int b = 0; b < B; ++b) io[b] = b;
+            GAIN_CUDA(cudaMemcpyAsync(e->iota.p, io.data(), sizeof(int) * B, cudaMemcpyHostToDevice, st));
+            GAIN_CUDA(cudaStreamSynchronize(st));
+        }
+        for (int b0 = 0; b0 < B; b0 += 65535) {
+            const int nb = std::min(65535, B - b0);
+            GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
+                                           iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
+                                           EI.d.p, EI.nsize, e->d_lower.p + b0, e->primI.p + (size_t)b0 * bIs.dimen,
+                                           bIs.dimen, nb, st));
+            ++e->launches;
+        }
+        GAIN_TRY(slice(e, e->primI.p, bIs.dimen, nullptr, B, bIs.dimen, nullptr, nullptr, L.kpadI, Bpad, e->Vdig.p,
+                       p1x, e->Vst, false, nullptr, nullptr, st, L.d_i_sym.p));
+    } else {
+        GAIN_TRY(slice(e, EI.d.p, EI.nsize, e->d_lower.p, B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI, Bpad,
+                       e->Vdig.p, p1x, e->Vst, false, nullptr, nullptr, st, L.d_i_sym.p));
+    }
     CUtensorMap tmV, tmH, tmU;
     if (!split::make_digit_map(&tmV, e->Vdig.p, L.kpadI, Bpad, p1x.slices))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (lower digits)");
@@ -995,8 +1075,12 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
             // ---- upper vectors -> digits on the low-priority second stream
             GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
             if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready, 0));
-            GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad, Nupad,
-                           e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p));
+            if (L.general)   // symmetric functions in their own order
+                GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, L.nsymF, nullptr, nullptr, K2, Nupad, e->Udig.p,
+                               p2, e->Ust, false, nullptr, nullptr, e->st2));
+            else
+                GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad,
+                               Nupad, e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p));
             GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
         }
         // inexact first-GEMM entries recomputed in FP64
@@ -1004,9 +1088,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         rh.flags = e->flags1.p;
         rh.nflags = e->counters.p + 0;
         rh.max_flags = kMaxFlags;
-        rh.vecs = EI.d.p;
-        rh.nsize = EI.nsize;
-        rh.row_level = e->d_lower.p;
+        rh.vecs = L.general ? e->primI.p : EI.d.p;
+        rh.nsize = L.general ? bIs.dimen : EI.nsize;
+        rh.row_level = L.general ? e->iota.p : e->d_lower.p;
         rh.i_sym = L.d_i_sym.p;
         rh.band_k0 = L.d_band_k0.p;
         rh.band_len = L.d_band_len.p;
@@ -1025,13 +1109,24 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     }
     if (npieces > 1)
         GAIN_CUDA(cudaMemcpyAsync(e->H.p, e->acc.p, sizeof(double) * (size_t)Bpad * L.fpad, cudaMemcpyDeviceToDevice, st));
+    // ---- mixing expansion: H_sym = H_prim T_F (FP64), row error bounds carried over
+    const double* Hs = e->H.p;
+    if (L.general) {
+        GAIN_TRY(e->Hsym.alloc((size_t)Bpad * K2));
+        GAIN_CUDA(launch_contract_rowerr(B, e->H.p, L.fpad, L.fpad, e->rowerr.p, e->Vst.e.p, L.sigmaF, L.gamF, st));
+        ++e->launches;
+        GAIN_CUDA(launch_contract(L.nsymF, L.d_cF_ptr.p, L.d_cF_col.p, L.d_cF_val.p, e->H.p, L.fpad, e->Hsym.p, K2, B,
+                                  st));
+        ++e->launches;
+        Hs = e->Hsym.p;
+    }
 
     // ---- H -> digits; the upper digits (second stream) must be ready before the second GEMM
-    GAIN_TRY(slice(e, e->H.p, L.fpad, nullptr, B, L.fpad, nullptr, nullptr, L.fpad, Bpad, e->Hdig.p, p2,
+    GAIN_TRY(slice(e, Hs, K2, nullptr, B, L.general ? L.nsymF : L.fpad, nullptr, nullptr, K2, Bpad, e->Hdig.p, p2,
                    e->Hst, true, e->rowerr.p, e->Vst.e.p, st));
     GAIN_CUDA(cudaStreamWaitEvent(st, e->ev[7], 0));
-    if (!split::make_digit_map(&tmH, e->Hdig.p, L.fpad, Bpad, p2.slices) ||
-        !split::make_digit_map(&tmU, e->Udig.p, L.fpad, Nupad, p2.slices, pair ? split::BN / 2 : split::BM))
+    if (!split::make_digit_map(&tmH, e->Hdig.p, K2, Bpad, p2.slices) ||
+        !split::make_digit_map(&tmU, e->Udig.p, K2, Nupad, p2.slices, pair ? split::BN / 2 : split::BM))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (second GEMM digits)");
 
     // ---- GEMM 2: amp = H U^T
@@ -1044,7 +1139,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
             t.n0 = n0;
             t.a_k0 = 0;
             t.b_k0 = 0;
-            t.nkb = L.fpad / split::BK;
+            t.nkb = K2 / split::BK;
             t2.push_back(t);
         }
     const std::vector<split::Prod> pr2 = make_prods(p2);
@@ -1065,7 +1160,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.A = e->Hst.view(false);   // H is FP64-grade: its error is the FP64 method's own
     g2.B = e->Ust.view(false);
     g2.c_fix = fix_const((int)pr2.size());
-    g2.c_f64 = (float)((double)(L.nF + 64) * std::ldexp(1.0, -53) * 1.01);
+    g2.c_f64 = (float)((double)((L.general ? L.nsymF : L.nF) + 64) * std::ldexp(1.0, -53) * 1.01);
     g2.rowerr2 = nullptr;
     g2.absmax = e->ull.p + 2;
     g2.flag_mode = 1;
@@ -1087,9 +1182,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     ra.U = EF.d.p;
     ra.nsize = EF.nsize;
     ra.col_level = e->d_upper.p;
-    ra.colpos = L.d_colposF.p;
-    ra.H = e->H.p;
-    ra.ldh = L.fpad;
+    ra.colpos = L.general ? L.d_ident.p : L.d_colposF.p;
+    ra.H = Hs;
+    ra.ldh = K2;
     ra.h_inerr = e->Hst.inerr.p;
     ra.eH = e->Hst.e.p;
     ra.amp = e->amp.p;

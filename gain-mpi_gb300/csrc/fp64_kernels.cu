@@ -285,6 +285,33 @@ __global__ void k_scatter_select(int dimen, const int* __restrict__ sym_of,
     prim[r] = s >= 0 ? __dmul_rn(vec[s], coef[r]) : 0.0;
 }
 
+// Row error of H_sym = H_prim T (T the upper expansion) from that of H_prim: with sigma a
+// bound of ||T||_2 and gam that of the FP64 contraction's rounding (relative to |T||H|),
+//   ||err_sym||_2 <= sigma ||err_prim||_2 + gam sigma ||H_prim row||_2.
+// rowerr2 is a squared norm in units of 2^{2 e[row]}; one block per row, rounded up.
+__global__ void __launch_bounds__(256)
+k_contract_rowerr(int rows, const double* __restrict__ Hp, long ldp, int ncols, float* __restrict__ rowerr2,
+                  const int* __restrict__ e, double sigma, double gam) {
+    __shared__ double red[8];
+    const int r = blockIdx.x;
+    if (r >= rows) return;
+    double ss = 0.0;
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        const double h = Hp[(long)r * ldp + c];
+        ss = __fma_ru(h, h, ss);
+    }
+    for (int o = 16; o > 0; o >>= 1) ss = __dadd_ru(ss, __shfl_xor_sync(0xffffffffu, ss, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = __dadd_ru(t, red[w]);
+        const double hn = __dmul_ru(__dsqrt_ru(t), ldexp(1.0, -e[r]));
+        const double v = __fma_ru(__dmul_ru(gam, sigma), hn, __dmul_ru(sigma, __dsqrt_ru((double)rowerr2[r])));
+        rowerr2[r] = __double2float_ru(__dmul_ru(__dmul_ru(v, v), 1.0000001));
+    }
+}
+
 __global__ void k_add(double* __restrict__ acc, const double* __restrict__ x, long n) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         acc[i] += x[i];
@@ -451,6 +478,13 @@ cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* co
                                   const double* vec, double* prim, cudaStream_t st) {
     if (dimen <= 0) return cudaSuccess;
     k_scatter_select<<<(dimen + 255) / 256, 256, 0, st>>>(dimen, sym_of, coef, vec, prim);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contract_rowerr(int rows, const double* Hp, long ldp, int ncols, float* rowerr2, const int* e,
+                                  double sigma, double gam, cudaStream_t st) {
+    if (rows <= 0) return cudaSuccess;
+    k_contract_rowerr<<<rows, 256, 0, st>>>(rows, Hp, ldp, ncols, rowerr2, e, sigma, gam);
     return cudaGetLastError();
 }
 

@@ -108,6 +108,9 @@ cudaError_t launch_gemv_batch(int nrows, int n, const double* U, long ldu, const
 cudaError_t launch_scatter_select(int dimen, const int* sym_of, const double* coef,
                                   const double* vec, double* prim, cudaStream_t st);
 
+// row error bound of H_prim T from that of H_prim (split path with a mixing expansion)
+cudaError_t launch_contract_rowerr(int rows, const double* Hp, long ldp, int ncols, float* rowerr2, const int* e,
+                                  double sigma, double gam, cudaStream_t st);
 // acc[i] += x[i], i < n
 cudaError_t launch_add(double* acc, const double* x, long n, cudaStream_t st);
 

@@ -532,7 +532,7 @@ def upload_problem(eng: Engine, p, dipole_block=None, blocks=None):
     for jind, b in enumerate(p.bases):
         eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
         inf = p.infl[jind]
-        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, 1, inf.N, inf.repres,
+        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, inf.matsize, inf.N, inf.repres,
                              inf.Ntot, inf.sdeg)
     nv = p.dipole.shape[-1]
     if dipole_block is None:

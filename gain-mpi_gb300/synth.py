@@ -112,17 +112,19 @@ def classes_of(basis: Basis, rule: str) -> np.ndarray:
         return (2 * (basis.vib % 2) + ((basis.K + basis.tau) % 2)).astype(np.int32)
     if rule == "c4r":   # rotsym basis: level index in place of K + tau
         return (2 * (basis.vib % 2) + (basis.tau % 2)).astype(np.int32)
+    if rule == "c4m":   # classes belong to mixed functions, not primitives (make_mixed_inflation)
+        return np.full(basis.dimen, -1, np.int32)
     raise ValueError(f"unknown symmetry rule {rule!r}")
 
 
 def nsym_of(rule: str) -> int:
-    return {"full": 1, "c4": 4, "c4r": 4}[rule]
+    return {"full": 1, "c4": 4, "c4r": 4, "c4m": 4}[rule]
 
 
 def selection_of(rule: str) -> np.ndarray:
     """isym_pairs: classes with equal entries pair up (SELECTION keyword)."""
     return {"full": np.array([1], np.int32), "c4": np.array([1, 1, 2, 2], np.int32),
-            "c4r": np.array([1, 1, 2, 2], np.int32)}[rule]
+            "c4r": np.array([1, 1, 2, 2], np.int32), "c4m": np.array([1, 1, 2, 2], np.int32)}[rule]
 
 
 def igamma_pair_of(isym_pairs: np.ndarray) -> np.ndarray:
@@ -150,7 +152,8 @@ class Inflation:
     repres: list                # per Gamma float64 [Ntot*sdeg*matsize]
     Ntot: np.ndarray            # int32 [nsym]
     sdeg: np.ndarray            # int32 [nsym]
-    members: list               # per Gamma: primitive indices of the class, ascending
+    members: list               # per Gamma: primitive indices of the class, ascending (selections)
+    matsize: int = 1            # components per case (the repres matrices' last dimension)
 
 
 def make_inflation(basis: Basis, cls: np.ndarray, nsym: int) -> Inflation:
@@ -167,6 +170,62 @@ def make_inflation(basis: Basis, cls: np.ndarray, nsym: int) -> Inflation:
         repres.append(np.ones(int(Ntot[g]), np.float64))
         members.append(np.nonzero(cls == g)[0].astype(np.int32))
     return Inflation(d, icontr, ijterms, Ns, repres, Ntot, np.ones(nsym, np.int32), members)
+
+
+MIX_COEF = 0.7071067811865476   # the double nearest 1/sqrt(2)
+
+
+def make_mixed_inflation(basis: Basis, nsym: int = 4) -> Inflation:
+    """Expansion tables of rule "c4m", a symmetrisation that mixes primitives the way TROVE's
+    symmetry-adapted functions do (a case holds several primitive components and each
+    symmetric function of the case is a linear combination of them):
+
+    * case (K = 0, v): one component, the primitive (0, J mod 2, v); one function of class
+      2 (v mod 2) + (J mod 2);
+    * case (K >= 1, v): components ib = 0, 1 = the primitives (K, 0, v), (K, 1, v); functions
+      (p0 + p1) / sqrt(2) of class 2 (v mod 2) + (K mod 2) and (p0 - p1) / sqrt(2) of class
+      2 (v mod 2) + ((K + 1) mod 2).
+
+    repres has mat_size = 2 (the component index); cases are numbered in primitive order."""
+    d = basis.dimen
+    J = basis.J
+    icontr = np.zeros(2 * d, np.int32)
+    case_of, cases = {}, []          # (K, v) -> case index; per case: list of (ib, primitive)
+    for r in range(d):
+        key = (int(basis.K[r]), int(basis.vib[r]))
+        if key not in case_of:
+            case_of[key] = len(cases)
+            cases.append([])
+        ib = 0 if basis.K[r] == 0 else int(basis.tau[r])
+        cases[case_of[key]].append((ib, r))
+        icontr[r] = case_of[key]
+        icontr[r + d] = ib
+    ncase = len(cases)
+    funcs = [[] for _ in range(nsym)]   # per class: (case, coefficients of components 0, 1)
+    for c, comps in enumerate(cases):
+        K = int(basis.K[comps[0][1]])
+        v = int(basis.vib[comps[0][1]])
+        if K == 0:
+            funcs[2 * (v % 2) + (J % 2)].append((c, (1.0, 0.0)))
+        else:
+            funcs[2 * (v % 2) + (K % 2)].append((c, (MIX_COEF, MIX_COEF)))
+            funcs[2 * (v % 2) + ((K + 1) % 2)].append((c, (MIX_COEF, -MIX_COEF)))
+    ijterms = np.zeros(ncase * nsym, np.int32)
+    Ns, repres = [], []
+    Ntot = np.zeros(nsym, np.int32)
+    for g in range(nsym):
+        n_g = np.zeros(ncase, np.int32)
+        for c, _ in funcs[g]:
+            n_g[c] += 1
+        ijterms[g * ncase:(g + 1) * ncase] = np.concatenate([[0], np.cumsum(n_g)[:-1]]).astype(np.int32)
+        Ns.append(n_g)
+        Ntot[g] = len(funcs[g])
+        rep = np.zeros(2 * int(Ntot[g]), np.float64)   # [s + ib Ntot], sdeg = 1, mat_size = 2
+        for s_idx, (c, co) in enumerate(funcs[g]):     # funcs[g] is in case order
+            rep[s_idx] = co[0]
+            rep[s_idx + int(Ntot[g])] = co[1]
+        repres.append(rep)
+    return Inflation(ncase, icontr, ijterms, Ns, repres, Ntot, np.ones(nsym, np.int32), [None] * nsym, matsize=2)
 
 
 def make_dipole(nv: int, seed: int = DIPOLE_SEED) -> np.ndarray:
@@ -272,7 +331,7 @@ def make_problem(nv: int, jvals, rule: str = "c4", blocks=None, qr_device=None,
         c = classes_of(b, rule)
         bases.append(b)
         classes.append(c)
-        infl.append(make_inflation(b, c, nsym))
+        infl.append(make_mixed_inflation(b, nsym) if rule == "c4m" else make_inflation(b, c, nsym))
     if blocks is None:
         blocks = [(J, g) for J in jvals for g in range(nsym)]
     blk = {}

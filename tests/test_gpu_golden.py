@@ -57,7 +57,7 @@ def _engine_for(d):
     for jind, b in enumerate(bases):
         eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
         inf = infl[jind]
-        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, 1, inf.N, inf.repres,
+        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, inf.matsize, inf.N, inf.repres,
                              inf.Ntot, inf.sdeg)
     s, e = (int(x) for x in d["block"])
     eng.upload_dipole(np.ascontiguousarray(d["dipole"][:, :, s:e]).reshape(-1), nv, s, e, e - s)

@@ -113,3 +113,23 @@ def test_line_strength_formula(oracle_lib):
     assert I == pytest.approx(1.327209365e-12 * A * 1.0 * 3.0 * np.exp(-beta * 100.0) *
                               (1 - np.exp(-beta * 1000.0)) / (1000.0 ** 2 * 2.5), rel=1e-14)
     assert oracle.line(amp, [1], 1, 1, 1, f, 100.0, 100.0, 0, 1, 0) is None   # nu < 1e-40 skipped
+
+
+def test_mixed_expansion_is_orthonormal(oracle_lib):
+    """Rule c4m: every symmetric function is a combination of the components of its case;
+    the expansion T (the reference's expand kernel on unit vectors) has orthonormal columns,
+    partitions the primitives over the four classes, and is not a selection."""
+    import oracle
+    import synth
+    b = synth.make_basis(3, 6)
+    inf = synth.make_mixed_inflation(b, 4)
+    assert inf.matsize == 2 and int(inf.Ntot.sum()) == b.dimen
+    cols = []
+    for g in range(4):
+        for s in range(int(inf.Ntot[g])):
+            e = np.zeros(inf.Ntot[g])
+            e[s] = 1.0
+            cols.append(oracle.expand(inf, g, e))
+    T = np.array(cols).T
+    assert np.allclose(T.T @ T, np.eye(b.dimen), atol=1e-15)
+    assert (np.count_nonzero(T, axis=0) == 2).sum() > 0   # mixed columns exist
