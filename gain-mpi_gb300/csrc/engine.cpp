@@ -212,6 +212,13 @@ struct PairLayout {
     // primitives the expansions touch; H = V T_I M is contracted with T_F before GEMM2,
     // whose inner dimension is then the nsymF symmetric functions padded to ntpad
     bool general = false;
+    // an expansion that mixes primitives of one K only: GEMM1 stays over symmetric functions
+    // and the band combines the primitive entries through both expansions
+    bool symband = false;
+    std::vector<int> fr_ptr, fr_col, ic_ptr, ic_col;   // per padded row / column: (primitive, coefficient)
+    std::vector<double> fr_val, ic_val;
+    DevArray<int> d_fr_ptr, d_fr_col, d_ic_ptr, d_ic_col;
+    DevArray<double> d_fr_val, d_ic_val;
     int nsymF = 0, ntpad = 0;
     double sigmaF = 1.0, gamF = 0.0;      // ||T_F||_2 bound; FP64 contraction rounding factor
     std::vector<int> cF_ptr, cF_col;      // T_F^T as CSR over symmetric functions, columns in F layout
@@ -603,11 +610,32 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     // The units of each layout: with selection expansions the symmetric functions (a primitive
     // times a coefficient each); otherwise the primitives the expansions touch, the lower
     // vectors expanded before the first GEMM and H contracted after it.
-    L.general = !(mI->selection && mF->selection);
-    const std::vector<int>& uI = L.general ? mI->support : mI->sym_prim;
-    const std::vector<int>& uF = L.general ? mF->support : mF->sym_prim;
-    auto coefI = [&](int s) { return L.general ? 1.0 : mI->sym_coef[s]; };
-    auto coefF = [&](int s) { return L.general ? 1.0 : mF->sym_coef[s]; };
+    // With mixing expansions whose symmetric functions each combine primitives of one K, the
+    // band is formed over symmetric functions directly (symband); otherwise GEMM1 runs over
+    // primitives (general).
+    auto one_k = [](const GammaMaps* m, const Basis& b, std::vector<int>& first) {
+        const int n = (int)m->csr_ptr.size() - 1;
+        first.assign(n, 0);
+        for (int sy = 0; sy < n; ++sy) {
+            const int q0 = m->csr_ptr[sy], q1 = m->csr_ptr[sy + 1];
+            if (q0 == q1) continue;
+            first[sy] = m->csr_col[q0];
+            for (int q = q0; q < q1; ++q)
+                if (b.K[m->csr_col[q]] != b.K[first[sy]]) return false;
+        }
+        return true;
+    };
+    std::vector<int> firstI, firstF;
+    const bool sel = mI->selection && mF->selection;
+    // GAINLS_SPLIT_FORM=primitive keeps GEMM1 over primitives for every mixing expansion
+    const char* form_env = getenv("GAINLS_SPLIT_FORM");
+    const bool force_prim = form_env && std::string(form_env) == "primitive";
+    L.symband = !sel && !force_prim && one_k(mI, bI, firstI) && one_k(mF, bF, firstF);
+    L.general = !sel && !L.symband;
+    const std::vector<int>& uI = L.general ? mI->support : (L.symband ? firstI : mI->sym_prim);
+    const std::vector<int>& uF = L.general ? mF->support : (L.symband ? firstF : mF->sym_prim);
+    auto coefI = [&](int s) { return sel ? mI->sym_coef[s] : 1.0; };
+    auto coefF = [&](int s) { return sel ? mF->sym_coef[s] : 1.0; };
     L.nI = (int)uI.size();
     L.nF = (int)uF.size();
     // lower layout: units grouped by K, each group padded to BK
@@ -679,6 +707,33 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
         L.band_k0[r] = L.kpad_startI[klo];
         L.band_len[r] = L.kpad_startI[khi + 1] - L.kpad_startI[klo];
         L.W = std::max(L.W, L.band_len[r]);
+    }
+    if (L.symband) {   // each padded row / column: the primitives of its symmetric function
+        auto build = [](const GammaMaps* m, const std::vector<int>& unit_at, std::vector<int>& ptr,
+                        std::vector<int>& col, std::vector<double>& val) {
+            ptr.assign(unit_at.size() + 1, 0);
+            col.clear();
+            val.clear();
+            for (size_t x = 0; x < unit_at.size(); ++x) {
+                const int sy = unit_at[x];
+                if (sy >= 0)
+                    for (int q = m->csr_ptr[sy]; q < m->csr_ptr[sy + 1]; ++q) {
+                        col.push_back(m->csr_col[q]);
+                        val.push_back(m->csr_val[q]);
+                    }
+                ptr[x + 1] = (int)col.size();
+            }
+        };
+        build(mI, L.i_sym, L.ic_ptr, L.ic_col, L.ic_val);
+        build(mF, L.f_sym, L.fr_ptr, L.fr_col, L.fr_val);
+        if (L.ic_col.empty()) { L.ic_col.push_back(0); L.ic_val.push_back(0.0); }
+        if (L.fr_col.empty()) { L.fr_col.push_back(0); L.fr_val.push_back(0.0); }
+        GAIN_TRY(L.d_ic_ptr.upload(L.ic_ptr));
+        GAIN_TRY(L.d_ic_col.upload(L.ic_col));
+        GAIN_TRY(L.d_ic_val.upload(L.ic_val));
+        GAIN_TRY(L.d_fr_ptr.upload(L.fr_ptr));
+        GAIN_TRY(L.d_fr_col.upload(L.fr_col));
+        GAIN_TRY(L.d_fr_val.upload(L.fr_val));
     }
     if (L.general) {
         // T_F^T as CSR over the symmetric functions, its columns moved to the F layout
@@ -778,6 +833,12 @@ gain_status launch_layout_band(gain_engine e, const gain_pair_job* j) {
     ba.nlevelI = wt ? wt->nI : 0;
     ba.nlevelF = wt ? wt->nF : 0;
     ba.maxdeg = wt ? wt->maxdeg : 0;
+    ba.f_ptr = L.symband ? L.d_fr_ptr.p : nullptr;
+    ba.f_col = L.symband ? L.d_fr_col.p : nullptr;
+    ba.f_val = L.symband ? L.d_fr_val.p : nullptr;
+    ba.i_ptr = L.symband ? L.d_ic_ptr.p : nullptr;
+    ba.i_col = L.symband ? L.d_ic_col.p : nullptr;
+    ba.i_val = L.symband ? L.d_ic_val.p : nullptr;
     GAIN_CUDA(split::launch_band(ba, e->st));
     ++e->launches;
     return GAIN_OK;
@@ -1024,8 +1085,13 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
                 if (npieces > 1) {   // only column tiles holding an upper function of this piece
                     bool any = false;
                     for (int r = n0; r < n0 + split::BN && r < L.fpad && !any; ++r) {
-                        const int fp = L.f_prim[r];
-                        any = fp >= 0 && bFs.vib[fp] >= e->startF && bFs.vib[fp] < e->endF;
+                        if (L.symband) {
+                            for (int q = L.fr_ptr[r]; q < L.fr_ptr[r + 1] && !any; ++q)
+                                any = bFs.vib[L.fr_col[q]] >= e->startF && bFs.vib[L.fr_col[q]] < e->endF;
+                        } else {
+                            const int fp = L.f_prim[r];
+                            any = fp >= 0 && bFs.vib[fp] >= e->startF && bFs.vib[fp] < e->endF;
+                        }
                     }
                     if (!any) continue;
                 }

@@ -995,45 +995,51 @@ k_slice4(const SliceArgs a) {
 // ------------------------------------------------------------------- band builder
 __device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
 
+// The band entry of one (upper primitive rF, lower primitive rI) pair without coefficients
+// (0 outside the dipole piece or the selection rules).
+__device__ __forceinline__ double band_elem(const BandArgs& a, int rF, int rI) {
+    const int vF = a.vibF[rF];
+    if (vF < a.startF || vF >= a.endF) return 0.0;
+    if (a.wigner) {
+        const long d = (long)(vF - a.startF) + (long)a.vibI[rI] * a.ncontrF, ds = (long)a.dipN * a.ncontrF;
+        const long wi = 3 * ((long)a.tauI[rI] + (long)a.nlevelI *
+                             ((long)a.tauF[rF] + (long)a.nlevelF * ((long)a.KI[rI] + (long)a.maxdeg * a.KF[rF])));
+        return __fma_rn(a.wigner[wi + 2], a.dipole[d + 2 * ds],
+                        __fma_rn(a.wigner[wi], a.dipole[d], __dmul_rn(a.wigner[wi + 1], a.dipole[d + ds])));
+    }
+    const int kI = a.KI[rI], kF = a.KF[rF];
+    if (abs(kI - kF) > 1) return 0.0;
+    const int tI = a.tauI[rI], tF = a.tauF[rF] & 1;
+    const int eq = (kF == kI), neq = !eq, tneq = (tF != tI);
+    const int didx = 2 * eq + neq * (!tneq);
+    const int c = (tF - tI) * eq + (tF - tI) * (kF - kI) * neq * tneq - neq * (!tneq);
+    if (c == 0) return 0.0;
+    const int n = a.jmax + 1;
+    double m = a.threej[a.jI + kI * n + (a.jF - a.jI + 1) * n * n + (kF - kI + 1) * n * n * 3];
+    if (kI != kF && kI * kF != 0) m = __dmul_rn(m, kSqrt2Ref);
+    m = __dmul_rn(m, (double)c * parity_sign((kI % 3) * tI + kI) * parity_sign((kF % 3) * tF));
+    const double mu = a.dipole[(long)(vF - a.startF) + (long)a.vibI[rI] * a.ncontrF + (long)didx * a.dipN * a.ncontrF];
+    return __dmul_rn(m, mu);
+}
+
 __global__ void k_band(const BandArgs a) {
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)a.fpad * a.W) return;
     const int row = (int)(idx / a.W), w = (int)(idx - (long)row * a.W);
-    double val = 0.0;
-    const int rF = a.f_prim[row];
     const int kc = a.band_k0[row] + w;
-    if (a.wigner && rF >= 0 && kc < a.kpadI) {
-        const int rI = a.i_prim[kc];
-        const int vF = a.vibF[rF];
-        if (rI >= 0 && vF >= a.startF && vF < a.endF) {
-            const long d = (long)(vF - a.startF) + (long)a.vibI[rI] * a.ncontrF, ds = (long)a.dipN * a.ncontrF;
-            const long wi = 3 * ((long)a.tauI[rI] + (long)a.nlevelI *
-                                 ((long)a.tauF[rF] + (long)a.nlevelF * ((long)a.KI[rI] + (long)a.maxdeg * a.KF[rF])));
-            const double t = __fma_rn(a.wigner[wi + 2], a.dipole[d + 2 * ds],
-                                      __fma_rn(a.wigner[wi], a.dipole[d], __dmul_rn(a.wigner[wi + 1], a.dipole[d + ds])));
-            val = __dmul_rn(t, __dmul_rn(a.i_coef[kc], a.f_coef[row]));
-        }
-    } else if (rF >= 0 && kc < a.kpadI) {
-        const int rI = a.i_prim[kc];
-        if (rI >= 0) {
-            const int kI = a.KI[rI], kF = a.KF[rF];
-            const int vF = a.vibF[rF];
-            if (abs(kI - kF) <= 1 && vF >= a.startF && vF < a.endF) {
-                const int tI = a.tauI[rI], tF = a.tauF[rF] & 1;
-                const int eq = (kF == kI), neq = !eq, tneq = (tF != tI);
-                const int didx = 2 * eq + neq * (!tneq);
-                const int c = (tF - tI) * eq + (tF - tI) * (kF - kI) * neq * tneq - neq * (!tneq);
-                if (c != 0) {
-                    const int n = a.jmax + 1;
-                    double m = a.threej[a.jI + kI * n + (a.jF - a.jI + 1) * n * n + (kF - kI + 1) * n * n * 3];
-                    if (kI != kF && kI * kF != 0) m = __dmul_rn(m, kSqrt2Ref);
-                    m = __dmul_rn(m, (double)c * parity_sign((kI % 3) * tI + kI) * parity_sign((kF % 3) * tF));
-                    const double mu = a.dipole[(long)(vF - a.startF) + (long)a.vibI[rI] * a.ncontrF +
-                                               (long)didx * a.dipN * a.ncontrF];
-                    m = __dmul_rn(m, mu);
-                    m = __dmul_rn(m, __dmul_rn(a.i_coef[kc], a.f_coef[row]));
-                    val = m;
+    double val = 0.0;
+    if (kc < a.kpadI) {
+        if (a.f_ptr) {   // symmetric functions combining primitives: sum over both expansions
+            for (int q = a.f_ptr[row]; q < a.f_ptr[row + 1]; ++q)
+                for (int t = a.i_ptr[kc]; t < a.i_ptr[kc + 1]; ++t) {
+                    const double e = band_elem(a, a.f_col[q], a.i_col[t]);
+                    if (e != 0.0) val = __fma_rn(__dmul_rn(a.f_val[q], a.i_val[t]), e, val);
                 }
+        } else {
+            const int rF = a.f_prim[row], rI = a.i_prim[kc];
+            if (rF >= 0 && rI >= 0) {
+                const double e = band_elem(a, rF, rI);
+                if (e != 0.0) val = __dmul_rn(e, __dmul_rn(a.i_coef[kc], a.f_coef[row]));
             }
         }
     }

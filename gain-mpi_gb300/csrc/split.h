@@ -143,6 +143,12 @@ struct BandArgs {
     // with tau = level index and K = degeneracy index
     const double* wigner;
     int nlevelI, nlevelF, maxdeg;
+    // symmetric functions that combine primitives of one K: when f_ptr is non-null, upper row
+    // r is sum_q f_val[q] prim f_col[q] over q in [f_ptr[r], f_ptr[r+1]) and lower column c
+    // likewise through i_ptr / i_col / i_val; the entry is the double sum of the primitive
+    // entries (f_prim / f_coef / i_prim / i_coef are then unused)
+    const int *f_ptr, *f_col, *i_ptr, *i_col;
+    const double *f_val, *i_val;
 };
 cudaError_t launch_band(const BandArgs& a, cudaStream_t st);
 

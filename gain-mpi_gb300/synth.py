@@ -172,6 +172,13 @@ def make_inflation(basis: Basis, cls: np.ndarray, nsym: int) -> Inflation:
     return Inflation(d, icontr, ijterms, Ns, repres, Ntot, np.ones(nsym, np.int32), members)
 
 
+def inflation_of(basis: Basis, rule: str, nsym: int) -> "Inflation":
+    """The expansion tables of a basis under a symmetry rule."""
+    if rule == "c4m":
+        return make_mixed_inflation(basis, nsym)
+    return make_inflation(basis, classes_of(basis, rule), nsym)
+
+
 MIX_COEF = 0.7071067811865476   # the double nearest 1/sqrt(2)
 
 
@@ -331,7 +338,7 @@ def make_problem(nv: int, jvals, rule: str = "c4", blocks=None, qr_device=None,
         c = classes_of(b, rule)
         bases.append(b)
         classes.append(c)
-        infl.append(make_mixed_inflation(b, nsym) if rule == "c4m" else make_inflation(b, c, nsym))
+        infl.append(inflation_of(b, rule, nsym))
     if blocks is None:
         blocks = [(J, g) for J in jvals for g in range(nsym)]
     blk = {}

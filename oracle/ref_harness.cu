@@ -71,7 +71,7 @@ struct refh_pair {
     const int *tauI, *tauF, *icorrI, *icorrF;
     const int *kstartI, *kblockI, *kstartF, *kblockF;
     int gammaI, gammaF;
-    int maxcoeffI, maxcoeffF, NtotI, NtotF, nsymI, nsymF;
+    int maxcoeffI, maxcoeffF, NtotI, NtotF, nsymI, nsymF, matsizeI, matsizeF;
     const int *ijtermsI, *icontrI, *NI;
     const double* represI;
     const int *ijtermsF, *icontrF, *NF;
@@ -120,10 +120,10 @@ int refh_run_pair(const refh_pair* p, double* amp, double* hls, double* seconds)
         upload(&d_kbI, p->kblockI, p->jI + 1) ||
         upload(&d_ijI, p->ijtermsI, (size_t)p->maxcoeffI * p->nsymI) ||
         upload(&d_ctI, p->icontrI, (size_t)2 * p->dimenI) || upload(&d_NI, p->NI, p->maxcoeffI) ||
-        upload(&d_rpI, p->represI, p->NtotI) ||
+        upload(&d_rpI, p->represI, (size_t)p->NtotI * p->matsizeI) ||
         upload(&d_ijF, p->ijtermsF, (size_t)p->maxcoeffF * p->nsymF) ||
         upload(&d_ctF, p->icontrF, (size_t)2 * p->dimenF) || upload(&d_NF, p->NF, p->maxcoeffF) ||
-        upload(&d_rpF, p->represF, p->NtotF) || upload(&d_dip, p->dipole_me, dipn) ||
+        upload(&d_rpF, p->represF, (size_t)p->NtotF * p->matsizeF) || upload(&d_dip, p->dipole_me, dipn) ||
         upload(&d_3j, p->threej, nj))
         return -1;
     RT(cudaMalloc(&d_vecI, sizeof(double) * p->NtotI));

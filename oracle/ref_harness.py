@@ -29,7 +29,7 @@ class RefhPair(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("jI", "jF", "jmax", "dimenI", "dimenF")] + \
         [(n, _ip) for n in ("tauI", "tauF", "icorrI", "icorrF", "kstartI", "kblockI", "kstartF", "kblockF")] + \
         [(n, ctypes.c_int) for n in ("gammaI", "gammaF", "maxcoeffI", "maxcoeffF", "NtotI", "NtotF",
-                                     "nsymI", "nsymF")] + \
+                                     "nsymI", "nsymF", "matsizeI", "matsizeF")] + \
         [("ijtermsI", _ip), ("icontrI", _ip), ("NI", _ip), ("represI", _dp),
          ("ijtermsF", _ip), ("icontrF", _ip), ("NF", _ip), ("represF", _dp), ("dipole_me", _dp)] + \
         [(n, ctypes.c_int) for n in ("dip_stride", "startFblock", "endFblock", "ncontrF")] + \
@@ -106,6 +106,17 @@ def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, 
     s.maxcoeffI, s.maxcoeffF = iI.maxcoeff, iF.maxcoeff
     s.NtotI, s.NtotF = int(iI.Ntot[gammaI]), int(iF.Ntot[gammaF])
     s.nsymI, s.nsymF = len(iI.N), len(iF.N)
+    s.matsizeI, s.matsizeF = int(getattr(iI, "matsize", 1)), int(getattr(iF, "matsize", 1))
+    # every expansion entry the reference kernel reads lies inside the uploaded tables
+    for inf, g, b, ms in ((iI, gammaI, bI, s.matsizeI), (iF, gammaF, bF, s.matsizeF)):
+        d = b.dimen
+        irow, ib = np.asarray(inf.icontr[:d]), np.asarray(inf.icontr[d:2 * d])
+        n = np.asarray(inf.N[g])[irow]
+        it = np.asarray(inf.ijterms)[irow + g * inf.maxcoeff]
+        used = n > 0
+        if (np.any(irow < 0) or np.any(irow >= inf.maxcoeff) or np.any(ib[used] >= ms) or np.any(ib < 0)
+                or np.any(it[used] + n[used] > int(inf.Ntot[g])) or len(inf.repres[g]) < int(inf.Ntot[g]) * ms):
+            raise ValueError("expansion tables outside their ranges")
     s.ijtermsI, s.icontrI, s.NI, s.represI = I(iI.ijterms), I(iI.icontr), I(iI.N[gammaI]), D(iI.repres[gammaI])
     s.ijtermsF, s.icontrF, s.NF, s.represF = I(iF.ijterms), I(iF.icontr), I(iF.N[gammaF]), D(iF.repres[gammaF])
     s.dipole_me = D(piece.reshape(-1))

@@ -11,7 +11,7 @@ Each fixture stores the exact inputs that are not pure integer tables (eigenvect
 dipole piece, 3j table) next to the reference outputs (half_ls per lower state and the
 amplitudes), so the CPU tests can replay them anywhere.
 
-    python tests/golden/make_golden.py OUTDIR [rotsym]   # needs a GPU and the reference cubin
+    python tests/golden/make_golden.py OUTDIR [rotsym|mixed]   # needs a GPU and the reference cubin
 """
 from __future__ import annotations
 
@@ -36,7 +36,11 @@ CASES = {
     "c4_dJ0": (16, [2, 3], "c4", (3, 2), (3, 3), None, None, None),
     "c4_highJ": (6, [10, 11], "c4", (10, 0), (11, 1), list(range(12)), list(range(20)), None),
     "full_blocked": (16, [2, 3], "full", (2, 0), (3, 0), list(range(6)), list(range(30)), (5, 11)),
+    # expansions that mix primitives (synth rule c4m)
+    "c4m_dJp1": (16, [2, 3], "c4m", (2, 0), (3, 1), None, None, None),
+    "c4m_dJ0_blocked": (16, [2, 3], "c4m", (3, 2), (3, 3), None, None, (3, 12)),
 }
+MIXED = ("c4m_dJp1", "c4m_dJ0_blocked")
 
 
 def make_case(name, jmax=11):
@@ -96,7 +100,13 @@ def main(outdir):
 
 if __name__ == "__main__":
     out = sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__))
-    if len(sys.argv) > 2 and sys.argv[2] == "rotsym":   # only the rotsym fixtures
+    if len(sys.argv) > 2 and sys.argv[2] == "mixed":    # only the mixing-expansion fixtures
+        os.makedirs(out, exist_ok=True)
+        for name in MIXED:
+            d = make_case(name)
+            np.savez_compressed(os.path.join(out, name + ".npz"), **d)
+            print(name, d["ref_hls"].shape, d["ref_amp"].shape, float(np.abs(d["ref_amp"]).max()))
+    elif len(sys.argv) > 2 and sys.argv[2] == "rotsym":   # only the rotsym fixtures
         os.makedirs(out, exist_ok=True)
         for name in ROTSYM_CASES:
             d = make_rotsym_case(name)

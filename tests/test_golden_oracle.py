@@ -22,7 +22,7 @@ def _problem(d):
     import synth
     nv, jvals, rule = int(d["nv"]), [int(x) for x in d["jvals"]], str(d["rule"])
     bases = [synth.make_basis(J, nv) for J in jvals]
-    infl = [synth.make_inflation(b, synth.classes_of(b, rule), synth.nsym_of(rule)) for b in bases]
+    infl = [synth.inflation_of(b, rule, synth.nsym_of(rule)) for b in bases]
     return jvals, bases, infl
 
 

@@ -1,9 +1,10 @@
 """The split path with an expansion that mixes primitives (rule c4m: every symmetric function
 of a K >= 1 case is (p0 +- p1)/sqrt(2), as TROVE's symmetry-adapted functions combine the
-components of a case).  The lower vectors are expanded to primitives before the first GEMM
-and H is contracted with the upper expansion before the second; amplitudes are checked
-against the oracle's double-double restatement of the reference loop (expand -> half_ls ->
-expand -> dot), single CTAs and CTA pairs, with a dipole block and with dipole pieces."""
+components of a case), in both of its forms: the band formed over symmetric functions, and
+GEMM1 over primitives (lower vectors expanded before it, H contracted with the upper
+expansion after it).  Amplitudes are checked against the oracle's double-double restatement
+of the reference loop (expand -> half_ls -> expand -> dot), single CTAs and CTA pairs, with a
+dipole block and with dipole pieces."""
 import numpy as np
 import pytest
 
@@ -25,8 +26,20 @@ def _s_rel(amp, ref):
     return float(np.max(np.abs(S[m] - Sr[m]) / Sr[m]))
 
 
+@pytest.fixture(params=["symband", "primitive"])
+def split_form(request, monkeypatch):
+    """Both forms of the split path for mixing expansions: the band over symmetric functions
+    (every function here combines primitives of one K) and GEMM1 over primitives with the
+    contraction after it (GAINLS_SPLIT_FORM=primitive)."""
+    if request.param == "primitive":
+        monkeypatch.setenv("GAINLS_SPLIT_FORM", "primitive")
+    else:
+        monkeypatch.delenv("GAINLS_SPLIT_FORM", raising=False)
+    return request.param
+
+
 @pytest.mark.parametrize("nv,jv", [(16, (2, 3)), (80, (3, 4))])
-def test_mixed_expansion_split_and_plain_match_oracle(built_lib, nv, jv):
+def test_mixed_expansion_split_and_plain_match_oracle(built_lib, split_form, nv, jv):
     import gainls
     import synth
     p = synth.make_problem(nv, list(jv), "c4m", blocks=[(jv[0], 0), (jv[1], 1)])
@@ -43,11 +56,11 @@ def test_mixed_expansion_split_and_plain_match_oracle(built_lib, nv, jv):
     amp = eng.fetch_amp()
     assert np.max(np.abs(amp - ref)) <= 1e-11 * scale
     assert _s_rel(amp, ref) <= 1e-8
-    if len(lo) > 128:
+    if split_form == "primitive":
         assert st["kernel_launches"] >= 9   # expansion and contraction run too
 
 
-def test_mixed_expansion_with_dipole_block_and_pieces(built_lib):
+def test_mixed_expansion_with_dipole_block_and_pieces(built_lib, split_form):
     import gainls
     import synth
     p = synth.make_problem(24, [2, 3], "c4m", blocks=[(2, 1), (3, 0)])
