@@ -55,6 +55,9 @@ def parse():
                          "against central differences (one JSON line)")
     ap.add_argument("--adj-nv", type=int, default=1000, help="vibrational basis size of --adjoint")
     ap.add_argument("--adj-fd", type=int, default=200, help="entries checked by central differences")
+    ap.add_argument("--rule", choices=["c4", "c4m"], default="c4",
+                    help="symmetrisation of the workload: c4 (selection, the headline) or c4m (functions "
+                         "that combine two primitives, as TROVE's symmetry-adapted functions do)")
     ap.add_argument("--batch", action="store_true",
                     help="every allowed block pair of J=0..--batch-jmax through the split path (one JSON line)")
     ap.add_argument("--batch-nv", type=int, default=200, help="vibrational basis size of --batch")
@@ -88,7 +91,8 @@ def max_over_ranks(value: float, dist=None, device=None) -> float:
 
 
 # ------------------------------------------------------------------------- inputs
-def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = True, n_lower_override: int = 0):
+def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = True, n_lower_override: int = 0,
+                rule: str = "c4"):
     """orthonormal=False replaces the QR eigenvectors by normalised Gaussian rows of the same
     shape (used only where the values do not matter: timing the CPU reference formula)."""
     import synth
@@ -96,8 +100,7 @@ def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = 
     if n_lower_override > 0:
         n_lower = n_lower_override
     bI, bF = synth.make_basis(JI, nv), synth.make_basis(JF, nv)
-    cI, cF = synth.classes_of(bI, "c4"), synth.classes_of(bF, "c4")
-    iI, iF = synth.make_inflation(bI, cI, 4), synth.make_inflation(bF, cF, 4)
+    iI, iF = synth.inflation_of(bI, rule, 4), synth.inflation_of(bF, rule, 4)
     nI, nF = int(iI.Ntot[GI]), int(iF.Ntot[GF])
     # each rank takes its own batch of lower states (weak scaling, no data exchange)
     first = lower_first(rank, n_lower, nI)
@@ -106,7 +109,7 @@ def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = 
         # always load torch's linear-algebra library inside their injected process)
         import tempfile
         cdir = os.environ.get("GAIN_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "gain_bench_inputs"))
-        cfile = os.path.join(cdir, f"eig_nv{nv}_J{JI}g{GI}_{first}_{n_lower}_J{JF}g{GF}.npz")
+        cfile = os.path.join(cdir, f"eig_{rule}_nv{nv}_J{JI}g{GI}_{first}_{n_lower}_J{JF}g{GF}.npz")
         if os.path.exists(cfile):
             z = np.load(cfile)
             vl, vu = z["vl"], z["vu"]
@@ -126,7 +129,7 @@ def make_inputs(small: bool, rank: int, device: str | None, orthonormal: bool = 
     eI = synth.make_energies(nI, JI, GI)[first:first + n_lower]
     eF = synth.make_energies(nF, JF, GF)
     return dict(nv=nv, bases=[bI, bF], infl=[iI, iF], dipole=synth.make_dipole(nv), vl=np.ascontiguousarray(vl),
-                vu=np.ascontiguousarray(vu), eI=eI, eF=eF, first=first)
+                vu=np.ascontiguousarray(vu), eI=eI, eF=eF, first=first, rule=rule)
 
 
 _PINNED = []   # pinned host tensors backing the arrays handed out by pinned()
@@ -258,9 +261,10 @@ def cpu_baseline(inp, n_sample: int):
     import synth
     oracle.build()
     nv = inp["nv"]
-    p = synth.Problem(nv, [JI, JF], "c4", 4, np.ones(4, np.int32), synth.selection_of("c4"),
-                      synth.igamma_pair_of(synth.selection_of("c4")), inp["bases"], inp["infl"],
-                      [synth.classes_of(b, "c4") for b in inp["bases"]], inp["dipole"],
+    rule = inp.get("rule", "c4")
+    p = synth.Problem(nv, [JI, JF], rule, 4, np.ones(4, np.int32), synth.selection_of(rule),
+                      synth.igamma_pair_of(synth.selection_of(rule)), inp["bases"], inp["infl"],
+                      [synth.classes_of(b, rule) for b in inp["bases"]], inp["dipole"],
                       {(0, GI): synth.Block(JI, 0, GI, inp["vl"][:n_sample], inp["eI"][:n_sample]),
                        (1, GF): synth.Block(JF, 1, GF, inp["vu"], inp["eF"])})
     cores = os.cpu_count() or 1
@@ -620,7 +624,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import gainls
-    inp = make_inputs(args.small, rank, "cuda", n_lower_override=args.lower)
+    inp = make_inputs(args.small, rank, "cuda", n_lower_override=args.lower, rule=args.rule)
     eng = setup_engine(inp, local)
     B, NU = inp["vl"].shape[0], inp["vu"].shape[0]
     lo, up = list(range(B)), list(range(NU))
@@ -715,7 +719,8 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-               "config": {"workload": WORKLOAD, "lower_states": B, "upper_states": NU, "N_v": inp["nv"],
+               "config": {"workload": WORKLOAD + ("" if args.rule == "c4" else f", symmetrisation {args.rule}"),
+                          "symmetrisation": args.rule, "lower_states": B, "upper_states": NU, "N_v": inp["nv"],
                           "lower_dim": int(inp["infl"][0].Ntot[GI]), "upper_dim": NF,
                           "l2": "inputs larger than L2 (BF16 digits of the upper vectors ~2 GB per step)",
                           "parallelism": f"replicas by lower-state range x{ws}",
