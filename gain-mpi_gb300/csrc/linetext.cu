@@ -12,6 +12,8 @@
 //                 shared memory, placed at the block's output offset modulo 16, and the block
 //                 copies its text out in aligned 16-byte stores (whole L2 sectors, no partial
 //                 writes).  A block whose text does not fit shared memory writes directly.
+#include <atomic>
+
 #include "gain_internal.h"
 #include "linemath.cuh"
 #include "linefmt.h"
@@ -212,12 +214,14 @@ cudaError_t launch_text_write(const TextArgs& t, unsigned long long max_block_by
     if (b1 > nb) b1 = nb;
     if (b0 < 0 || b1 <= b0) return cudaSuccess;
     if (max_block_bytes + 16 <= (unsigned long long)kStageMax) {
-        static bool attr = false;
-        if (!attr) {
-            const cudaError_t e = cudaFuncSetAttribute(k_text_write_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       kStageMax);
+        static std::atomic<unsigned long long> done{0};   // bit per device ordinal (< 64)
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (!(done.load() & (1ull << (dev & 63)))) {
+            e = cudaFuncSetAttribute(k_text_write_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageMax);
             if (e != cudaSuccess) return e;
-            attr = true;
+            done.fetch_or(1ull << (dev & 63));
         }
         const size_t smem = (size_t)((max_block_bytes + 16 + 15) & ~15ull);
         k_text_write_staged<<<(unsigned)(b1 - b0), kTextThreads, smem, st>>>(t, b0);

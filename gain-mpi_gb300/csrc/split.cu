@@ -1199,15 +1199,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices, int box_rows) {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    // looked up once (thread-safe initialisation of a function-local static)
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult qr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &qr) !=
                 cudaSuccess || qr != cudaDriverEntryPointSuccess || !p)
-            return false;
-        fn = (EncodeTiledFn)p;
-    }
+            return nullptr;
+        return (EncodeTiledFn)p;
+    }();
+    if (!fn) return false;
     if (((uintptr_t)base & 15) || (kpad % BK) || (rows_pad % BM)) return false;
     cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)slices};
     cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)kpad * 2 * (cuuint64_t)rows_pad};
