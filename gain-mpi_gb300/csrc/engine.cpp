@@ -1820,6 +1820,22 @@ gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path pat
     return r;
 }
 
+gain_status gain_selftest_bounded_wait(gain_engine e, double limit_ms) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!(limit_ms > 0.0) || limit_ms > 1000.0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_selftest_bounded_wait: limit outside (0, 1000] ms");
+    GAIN_TRY(e->err.alloc(1));
+    GAIN_TRY(e->err.zero(e->st, 1));
+    GAIN_CUDA(split::launch_wait_selftest((unsigned long long)(limit_ms * 1e6), e->err.p, e->st));
+    int code = 0;
+    GAIN_CUDA(cudaMemcpyAsync(&code, e->err.p, sizeof code, cudaMemcpyDeviceToHost, e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    if (code != 0)
+        return set_error(GAIN_ERR_TIMEOUT, "bounded device wait gave up after %.3f ms (code %d)", limit_ms, code);
+    return GAIN_OK;
+}
+
 gain_status gain_pair_amp_device(gain_engine e, const double** amp, int* ld) {
     clear_error();
     if (!e || !amp || !ld) return set_error(GAIN_ERR_INVALID_ARG, "NULL argument");

@@ -55,14 +55,14 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 // Bounded wait on a barrier phase.  Gives up when another role raised the CTA abort flag
 // (unless ignore_abort) or after kWaitNs, raising the flag and the device error word.
 __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
-                          int code, bool ignore_abort = false) {
+                          int code, bool ignore_abort = false, unsigned long long limit_ns = kWaitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = globaltimer();
     for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 127u) == 0) {
             if (!ignore_abort && *abort_flag) return false;
-            if (globaltimer() - t0 > kWaitNs) {
+            if (globaltimer() - t0 > limit_ns) {
                 *abort_flag = 1;
                 atomicCAS(err, 0, code);
                 return false;
@@ -1046,6 +1046,21 @@ __global__ void k_band(const BandArgs a) {
     a.band[idx] = val;
 }
 
+// Self-test of the bounded wait: an mbarrier nothing arrives on; the wait gives up after
+// limit_ns, raises the abort flag and writes code 9 to err.
+__global__ void k_wait_selftest(unsigned long long limit_ns, int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait(smem_u32(&bar), 0, &abort_flag, err, 9, false, limit_ns);
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------- refinement
 __global__ void k_refine_h(const RefineHArgs a) {
     const int lane = threadIdx.x & 31;
@@ -1243,6 +1258,11 @@ cudaError_t launch_band(const BandArgs& a, cudaStream_t st) {
 
 cudaError_t launch_refine_h(const RefineHArgs& a, int max_blocks, cudaStream_t st) {
     k_refine_h<<<max_blocks, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wait_selftest(unsigned long long limit_ns, int* err, cudaStream_t st) {
+    k_wait_selftest<<<1, 32, 0, st>>>(limit_ns, err);
     return cudaGetLastError();
 }
 

@@ -151,6 +151,8 @@ struct BandArgs {
     const double *f_val, *i_val;
 };
 cudaError_t launch_band(const BandArgs& a, cudaStream_t st);
+// one bounded mbarrier wait on a barrier nothing arrives on (err gets code 9 when it gives up)
+cudaError_t launch_wait_selftest(unsigned long long limit_ns, int* err, cudaStream_t st);
 
 // FP64 recomputation of flagged first-GEMM outputs (H entries).
 struct RefineHArgs {

@@ -186,6 +186,8 @@ def _declare(L):
                                         _ip, _ip]
     L.gain_upload_dipole.argtypes = [_vp, _dp, I, I, I, I]
     L.gain_upload_eigvecs.argtypes = [_vp, I, I, I, I, _dp]
+    L.gain_selftest_bounded_wait.argtypes = [_vp, D]
+    L.gain_selftest_bounded_wait.restype = S
     L.gain_upload_dipole_pieces.argtypes = [_vp, I, ctypes.POINTER(_dp), I, _ip, _ip]
     L.gain_upload_dipole_pieces.restype = S
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]

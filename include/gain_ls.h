@@ -297,6 +297,12 @@ gain_status gain_fetch_lines_text(gain_engine e, char* out, unsigned long long c
 /* Device address and size of that text (valid until the next gain_pair_lines_text). */
 gain_status gain_lines_text_device(gain_engine e, const char** text, unsigned long long* bytes);
 
+/* Self-test of the bounded device waits the tensor-core GEMMs use (every mbarrier wait gives
+ * up after a limit, raises the CTA's abort flag and reports GAIN_ERR_TIMEOUT): one wait on a
+ * barrier nothing arrives on, limited to limit_ms (0 < limit_ms <= 1000).  Returns
+ * GAIN_ERR_TIMEOUT when the wait gave up as it should; the engine stays usable. */
+gain_status gain_selftest_bounded_wait(gain_engine e, double limit_ms);
+
 /* The line-list conversions on their own, on the current device: values[i] printed with
  * "%<width>.<prec>E" (conv 'E', prec <= 17) or "%<width>.<prec>f" (conv 'f', prec <= 9) into
  * out + i*stride (no NUL), lens[i] = its length (the text is written only when it fits in

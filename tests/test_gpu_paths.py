@@ -185,3 +185,25 @@ def test_async_eigvec_upload_orders_reads_after_the_copy(built_lib):
     eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
     assert np.array_equal(eng.fetch_amp(), 2.0 * ref[gainls.PATH_SPLIT])
     del eng
+
+
+def test_bounded_wait_gives_up_and_the_engine_stays_usable(built_lib):
+    """Failure detection without a GPU fault: a bounded mbarrier wait on a barrier nothing
+    arrives on gives up after its limit and reports GAIN_ERR_TIMEOUT; the same engine then
+    computes a block pair as usual."""
+    import time
+    import gainls
+    import synth
+    p = synth.make_problem(16, [2, 3], "c4", blocks=[(2, 0), (3, 1)])
+    eng = gainls.Engine(11, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    t0 = time.perf_counter()
+    with pytest.raises(gainls.GainError) as ex:
+        gainls.check(gainls.lib().gain_selftest_bounded_wait(eng.h, 20.0))
+    assert ex.value.status == gainls.ERR_TIMEOUT
+    assert "gave up" in str(ex.value)
+    assert time.perf_counter() - t0 < 5.0
+    lo = list(range(p.blocks[(0, 0)].vecs.shape[0]))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+    st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    assert st["status"] == gainls.OK
