@@ -929,16 +929,19 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     gain_split_opts o1{};
     if (opts) o1.beta = opts->beta;
     SplitParams p1x;
+    // bits of the first GEMM's digits (GAINLS_GEMM1_BITS, 40..62)
+    int bits1 = 56;
+    if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
     if (L.rotsym) {
         // rotational-symmetry form: every tile spans the whole lower layout, so the inner
         // dimension splits into chunks as in the second GEMM (per-chunk norms of both operands)
-        p1x = choose_params(L.W, &o1, 56, 8);
+        p1x = choose_params(L.W, &o1, bits1, 8);
     } else {
-        p1x = choose_params(L.W, &o1, 56, 7);
+        p1x = choose_params(L.W, &o1, bits1, 7);
         p1x.chunks = 1;
         while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
             --p1x.beta;
-            p1x.slices = (56 + p1x.beta - 1) / p1x.beta;
+            p1x.slices = (bits1 + p1x.beta - 1) / p1x.beta;
         }
     }
     const int K2 = L.general ? L.ntpad : L.fpad;   // inner dimension of the second GEMM
