@@ -922,15 +922,18 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     // vectors are awaited on the second stream only, so their copy overlaps the lower side
     if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EI.ready, 0));
 
-    // First GEMM: 56 bits (its error reaches every amplitude through ||dH||_2 ||u||_2), one
-    // inner chunk per band tile, digits narrowed until that single chunk stays exact.
+    // First GEMM: 49 bits (its error reaches every amplitude through ||dH||_2 ||u||_2; every
+    // entry must certify FP64-grade), one inner chunk per band tile, digits narrowed until that
+    // single chunk stays exact.
     // Second GEMM: 48 bits (8-bit digits in up to MAX_CHUNKS chunks, else 7 x 7 bits);
     // options (beta, slices, kchunks) apply to it.
     gain_split_opts o1{};
     if (opts) o1.beta = opts->beta;
     SplitParams p1x;
-    // bits of the first GEMM's digits (GAINLS_GEMM1_BITS, 40..62)
-    int bits1 = 56;
+    // bits of the first GEMM's digits (GAINLS_GEMM1_BITS, 40..62).  49 bits (7 digits of 7)
+    // leave every H entry of the config-2 workload within the FP64 bound of its dot product;
+    // 42 bits leave none (all recomputed in FP64).
+    int bits1 = 49;
     if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
     if (L.rotsym) {
         // rotational-symmetry form: every tile spans the whole lower layout, so the inner
