@@ -581,6 +581,35 @@ def batch_plan(args):
     eng.close()
 
 
+def reference_gpu_sample(inp, n_lower: int) -> dict:
+    """The reference's own GPU kernels (GPU/dipole_GPU.cu, compiled unmodified into
+    oracle/_ref/dipole_GPU.cubin) in GpuManager's call pattern (oracle/ref_harness.cu): per
+    lower state the expansion and one K-block launch per K'; per upper state the expansion,
+    cublasDdot, an 8-byte copy back and a synchronisation.  One host thread (the reference
+    overlaps such loops over its OpenMP threads, main.cpp:292); a sample of lower states of
+    the workload; wall time of the whole call."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_harness
+    import synth
+    import threej
+    nv = inp["nv"]
+    rule = inp.get("rule", "c4")
+    p = synth.Problem(nv, [JI, JF], rule, 4, np.ones(4, np.int32), synth.selection_of(rule),
+                      synth.igamma_pair_of(synth.selection_of(rule)), inp["bases"], inp["infl"],
+                      [synth.classes_of(b, rule) for b in inp["bases"]], inp["dipole"],
+                      {(0, GI): synth.Block(JI, 0, GI, inp["vl"][:n_lower], inp["eI"][:n_lower]),
+                       (1, GF): synth.Block(JF, 1, GF, inp["vu"], inp["eF"])})
+    NU = inp["vu"].shape[0]
+    tj = threej.threej_table(11)
+    t0 = time.perf_counter()
+    _, _, loop_s = ref_harness.run_pair(p, 0, GI, 1, GF, list(range(n_lower)), list(range(NU)), tj, 11)
+    secs = time.perf_counter() - t0
+    n = n_lower * NU
+    return {"value": n / secs, "unit": UNIT, "per_transition_loop_us": 1e6 * loop_s / n,
+            "sample": f"{n_lower} lower states x {NU} upper states of the workload ({n} transitions, {secs:.2f} s)",
+            "method": "reference GPU kernels, one host thread, GpuManager call pattern"}
+
+
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
@@ -600,6 +629,17 @@ def reference_arm(args, ws, rank):
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port",
                             "sample": r["sample"]},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    # an extra data point beside the CPU arm: the reference's own GPU kernels on this GPU
+    try:
+        import torch
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import ref_harness
+        if torch.cuda.is_available() and ref_harness.available():
+            out["reference_gpu_kernels"] = reference_gpu_sample(inp, 2)
+        else:
+            out["reference_gpu_kernels"] = {"unavailable": "no GPU or no compiled reference kernels"}
+    except Exception as exc:   # the extra data point never fails the arm
+        out["reference_gpu_kernels"] = {"unavailable": str(exc).splitlines()[0][:200]}
     print(json.dumps(out), flush=True)
 
 

@@ -930,10 +930,14 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     gain_split_opts o1{};
     if (opts) o1.beta = opts->beta;
     SplitParams p1x;
-    // bits of the first GEMM's digits (GAINLS_GEMM1_BITS, 40..62).  49 bits (7 digits of 7)
-    // leave every H entry of the config-2 workload within the FP64 bound of its dot product;
-    // 42 bits leave none (all recomputed in FP64).
-    int bits1 = 49;
+    // Bits of the first GEMM's digits.  Every H entry must stay within the FP64 bound of its
+    // dot product, (W + 64) 2^-53 ||x|| ||y||, which loosens as the band width W grows, so
+    // the digits follow it: 53 - log2(W + 64) + 6 bits, between 46 and 56.  At W = 3000
+    // (config 2) that is 49 bits (7 digits of 7; every entry certifies, 42 bits certify
+    // none); narrow bands keep 56.  GAINLS_GEMM1_BITS (40..62) overrides the rule.
+    int bits1 = (int)std::ceil(53.0 - std::log2((double)L.W + 64.0) + 6.0);
+    bits1 = std::max(46, std::min(56, bits1));
+    if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
     if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
     if (L.rotsym) {
         // rotational-symmetry form: every tile spans the whole lower layout, so the inner
