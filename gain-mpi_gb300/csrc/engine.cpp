@@ -938,7 +938,6 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     int bits1 = (int)std::ceil(53.0 - std::log2((double)L.W + 64.0) + 6.0);
     bits1 = std::max(46, std::min(56, bits1));
     if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
-    if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
     if (L.rotsym) {
         // rotational-symmetry form: every tile spans the whole lower layout, so the inner
         // dimension splits into chunks as in the second GEMM (per-chunk norms of both operands)
