@@ -729,6 +729,9 @@ def main():
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_step = float(np.median(e2e_ms))
+    # the end-to-end route (asynchronous uploads, the upper side in two halves while the upper
+    # vectors arrive) gives the device-resident run's line strengths, bit for bit
+    e2e_same = bool(np.array_equal(S_h.reshape(B, NU), split_amp * split_amp))
     h2d = inp["vl"].nbytes + inp["vu"].nbytes
     d2h = 2 * B * NU * 8
     text = line_text_bench(eng, inp, max(2, min(args.steps, 5)))
@@ -773,7 +776,7 @@ def main():
                             "algorithmic_flops": alg2, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
                "cpu_baseline": cpu,
                "e2e": {"value": ws * transitions / (e2e_step * 1e-3), "unit": UNIT, "ms_per_step": e2e_step,
-                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "S_equals_device_run": e2e_same},
                "clocks": clk.summary(),
                "gpu_launches": int(st["kernel_launches"]) * args.steps,
                "gemm1_ms": float(np.median(g1)), "gemm2_ms": g2ms, "wall_ms_per_step": wall * 1e3 / args.steps,

@@ -137,11 +137,15 @@ struct Eig {
     // recorded on the copy stream after an asynchronous upload; every consumer's stream waits
     // on it before reading d (NULL until the first asynchronous upload)
     cudaEvent_t ready = nullptr;
+    // the copy runs in two parts: rows [0, head_rows) are in place when ready_head fires
+    cudaEvent_t ready_head = nullptr;
+    int head_rows = 0;
     Eig() = default;
     Eig(const Eig&) = delete;
     Eig& operator=(const Eig&) = delete;
     ~Eig() {
         if (ready) cudaEventDestroy(ready);
+        if (ready_head) cudaEventDestroy(ready_head);
     }
 };
 
@@ -176,15 +180,15 @@ struct StatsDev {
         if (with_inerr) GAIN_TRY(inerr.zero(st, rows));
         return GAIN_OK;
     }
-    split::RowStats view(bool with_inerr) {
+    split::RowStats view(bool with_inerr, size_t row0 = 0, int nch = 0) {
         split::RowStats r;
-        r.e = e.p;
-        r.nnz = nnz.p;
-        r.l2 = l2.p;
-        r.dn = dn.p;
-        r.dnv = dnv.p;
-        r.rnv = rnv.p;
-        r.inerr = with_inerr ? inerr.p : nullptr;
+        r.e = e.p + row0;
+        r.nnz = nnz.p + row0;
+        r.l2 = l2.p + row0;
+        r.dn = dn.p + row0 * (size_t)nch;
+        r.dnv = dnv.p + row0 * split::MAX_SLICES;
+        r.rnv = rnv.p + row0 * split::MAX_SLICES;
+        r.inerr = with_inerr ? inerr.p + row0 : nullptr;
         return r;
     }
 };
@@ -249,7 +253,7 @@ struct gain_engine_s {
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;   // upper-vector slicing, concurrent with the lower side
     cudaStream_t stc = nullptr;   // asynchronous eigenvector uploads
-    cudaEvent_t ev[9] = {};
+    cudaEvent_t ev[10] = {};
     cudaEvent_t ev_up = nullptr;  // orders an asynchronous upload after queued engine work
     std::vector<long> zkey_V, zkey_H, zkey_U;   // shape/layout the digit buffers were cleared for
     gain::DevArray<double> d3j;
@@ -868,7 +872,8 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
                   const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
                   __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
                   const float* inerr_prev, const int* e_prev, cudaStream_t st, const int* col_inv = nullptr,
-                  int grid_limit = 0) {
+                  int grid_limit = 0, int row0 = 0) {
+    // row0: the output rows start at row row0 of the digit and statistics arrays
     split::SliceArgs a;
     a.grid_limit = grid_limit;
     a.col_inv = col_inv;
@@ -889,13 +894,13 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     a.col_map = col_map;
     a.kpad = kpad;
     a.slice_stride = (long)rows_pad * kpad;
-    a.digits = dig;
+    a.digits = dig + (size_t)row0 * kpad;
     a.slices = p.slices;
     a.beta = p.beta;
     a.nchunks = p.chunks;
-    a.st = stv.view(with_inerr);
-    a.inerr2_prev = inerr_prev;
-    a.e_prev = e_prev;
+    a.st = stv.view(with_inerr, (size_t)row0, p.chunks);
+    a.inerr2_prev = inerr_prev ? inerr_prev + row0 : nullptr;
+    a.e_prev = e_prev ? e_prev + row0 : nullptr;
     GAIN_CUDA(split::launch_slice(a, st));
     ++e->launches;
     return GAIN_OK;
@@ -985,6 +990,22 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     const int mstep = pair ? 2 * split::BM : split::BM;
     const int Bpad = round_up(B, mstep);
     const int Nu = j->nupper, Nupad = round_up(Nu, split::BN);
+    // While the upper vectors are still arriving in two parts, the upper side runs in two
+    // halves: the first half's digits and amplitude GEMM start when the first part lands.
+    int Nu2 = 0;
+    bool arriving = false;
+    if (EF.ready && EF.ready_head && EF.head_rows > 0 && Nu >= 2 * split::BN) {
+        const cudaError_t q = cudaEventQuery(EF.ready);
+        if (q == cudaErrorNotReady) (void)cudaGetLastError();   // not an error: the copy is in flight
+        const char* halves = getenv("GAINLS_UPPER_HALVES");     // "force": also after the copy landed
+        arriving = q == cudaErrorNotReady || (halves && std::string(halves) == "force");
+    }
+    if (arriving) {
+        const int cand = (Nu / 2) / split::BN * split::BN;
+        bool in_head = true;
+        for (int u = 0; u < cand && in_head; ++u) in_head = j->upper_levels[u] < EF.head_rows;
+        if (in_head) Nu2 = cand;
+    }
     GAIN_TRY(e->d_lower.upload(j->lower_levels, B));
     GAIN_TRY(e->d_upper.upload(j->upper_levels, Nu));
     GAIN_TRY(e->counters.alloc(4));
@@ -1147,15 +1168,22 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         }
         if (piece == npieces - 1) GAIN_CUDA(cudaEventRecord(e->ev[3], st));
         if (piece == 0) {
-            // ---- upper vectors -> digits on the low-priority second stream
+            // ---- upper vectors -> digits on the low-priority second stream (rows [r0, r1))
+            auto slice_upper = [&](int r0, int r1) -> gain_status {
+                if (L.general)   // symmetric functions in their own order
+                    return slice(e, EF.d.p, EF.nsize, e->d_upper.p + r0, r1 - r0, L.nsymF, nullptr, nullptr, K2, Nupad,
+                                 e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, nullptr, 0, r0);
+                return slice(e, EF.d.p, EF.nsize, e->d_upper.p + r0, r1 - r0, EF.nsize, L.d_colposF.p, &L.colposF,
+                             L.fpad, Nupad, e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p, 0, r0);
+            };
             GAIN_CUDA(cudaStreamWaitEvent(e->st2, e->ev[6], 0));
+            if (Nu2 > 0) {
+                GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready_head, 0));
+                GAIN_TRY(slice_upper(0, Nu2));
+                GAIN_CUDA(cudaEventRecord(e->ev[9], e->st2));
+            }
             if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st2, EF.ready, 0));
-            if (L.general)   // symmetric functions in their own order
-                GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, L.nsymF, nullptr, nullptr, K2, Nupad, e->Udig.p,
-                               p2, e->Ust, false, nullptr, nullptr, e->st2));
-            else
-                GAIN_TRY(slice(e, EF.d.p, EF.nsize, e->d_upper.p, Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad,
-                               Nupad, e->Udig.p, p2, e->Ust, false, nullptr, nullptr, e->st2, L.d_f_sym.p));
+            GAIN_TRY(slice_upper(Nu2, Nu));
             GAIN_CUDA(cudaEventRecord(e->ev[7], e->st2));
         }
         // inexact first-GEMM entries recomputed in FP64
@@ -1199,7 +1227,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     // ---- H -> digits; the upper digits (second stream) must be ready before the second GEMM
     GAIN_TRY(slice(e, Hs, K2, nullptr, B, L.general ? L.nsymF : L.fpad, nullptr, nullptr, K2, Bpad, e->Hdig.p, p2,
                    e->Hst, true, e->rowerr.p, e->Vst.e.p, st));
-    GAIN_CUDA(cudaStreamWaitEvent(st, e->ev[7], 0));
+    // the upper digits the (first) amplitude GEMM reads
+    GAIN_CUDA(cudaStreamWaitEvent(st, Nu2 > 0 ? e->ev[9] : e->ev[7], 0));
     if (!split::make_digit_map(&tmH, e->Hdig.p, K2, Bpad, p2.slices) ||
         !split::make_digit_map(&tmU, e->Udig.p, K2, Nupad, p2.slices, pair ? split::BN / 2 : split::BM))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (second GEMM digits)");
@@ -1247,8 +1276,22 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     g2.cols_valid = Nu;
     g2.err = e->err.p;
     GAIN_CUDA(cudaEventRecord(e->ev[4], st));
-    GAIN_CUDA(split::launch_gemm(tmH, tmU, g2, e->num_sms, st, pair));
-    ++e->launches;
+    if (Nu2 > 0) {
+        // tiles are upper-block-major: those of the first half (n0 < Nu2) come first
+        int n1 = 0;
+        while (n1 < (int)t2.size() && t2[n1].n0 < Nu2) ++n1;
+        split::GemmArgs ga = g2, gb = g2;
+        ga.ntiles = n1;
+        gb.tiles = e->tiles2.p + n1;
+        gb.ntiles = (int)t2.size() - n1;
+        GAIN_CUDA(split::launch_gemm(tmH, tmU, ga, e->num_sms, st, pair));
+        GAIN_CUDA(cudaStreamWaitEvent(st, e->ev[7], 0));
+        GAIN_CUDA(split::launch_gemm(tmH, tmU, gb, e->num_sms, st, pair));
+        e->launches += 2;
+    } else {
+        GAIN_CUDA(split::launch_gemm(tmH, tmU, g2, e->num_sms, st, pair));
+        ++e->launches;
+    }
     GAIN_CUDA(cudaEventRecord(e->ev[5], st));
     split::RefineAmpArgs ra;
     ra.flags = e->flags2.p;
@@ -1675,6 +1718,7 @@ gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels,
     auto& slot = e->eig[{jind, gamma}];
     if (!slot) slot.reset(new Eig());
     if (slot->ready) GAIN_CUDA(cudaEventSynchronize(slot->ready));   // an asynchronous copy into it
+    slot->head_rows = 0;
     slot->nlevels = nlevels;
     slot->nsize = nsize;
     GAIN_TRY(slot->d.alloc((size_t)nlevels * nsize));
@@ -1701,6 +1745,7 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
     auto& slot = e->eig[{jind, gamma}];
     if (!slot) slot.reset(new Eig());
     if (!slot->ready) GAIN_CUDA(cudaEventCreateWithFlags(&slot->ready, cudaEventDisableTiming));
+    if (!slot->ready_head) GAIN_CUDA(cudaEventCreateWithFlags(&slot->ready_head, cudaEventDisableTiming));
     GAIN_CUDA(cudaEventSynchronize(slot->ready));   // a previous asynchronous copy into it
     slot->nlevels = nlevels;
     slot->nsize = nsize;
@@ -1709,9 +1754,18 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
     // joined to the first before each run ends)
     GAIN_CUDA(cudaEventRecord(e->ev_up, e->st));
     GAIN_CUDA(cudaStreamWaitEvent(e->stc, e->ev_up, 0));
-    GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyHostToDevice,
-                              e->stc));
+    // two parts: a run can start on the upper states of the first part while the second
+    // is still arriving
+    const int head = nlevels >= 512 ? nlevels / 2 : 0;
+    if (head > 0) {
+        GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)head * nsize, cudaMemcpyHostToDevice,
+                                  e->stc));
+        GAIN_CUDA(cudaEventRecord(slot->ready_head, e->stc));
+    }
+    GAIN_CUDA(cudaMemcpyAsync(slot->d.p + (size_t)head * nsize, vecs + (size_t)head * nsize,
+                              sizeof(double) * (size_t)(nlevels - head) * nsize, cudaMemcpyHostToDevice, e->stc));
     GAIN_CUDA(cudaEventRecord(slot->ready, e->stc));
+    slot->head_rows = head;
     return GAIN_OK;
 }
 

@@ -207,3 +207,28 @@ def test_bounded_wait_gives_up_and_the_engine_stays_usable(built_lib):
     up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
     st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
     assert st["status"] == gainls.OK
+
+
+def test_upper_side_in_two_halves_matches_one_phase(built_lib, monkeypatch):
+    """While the upper vectors arrive in two parts (asynchronous upload of at least 512
+    levels), the upper digits and the amplitude GEMM run in two halves; the amplitudes are
+    the same bits as in one phase (GAINLS_UPPER_HALVES=force takes the two-phase route even
+    when the copy has already landed)."""
+    import torch
+    import gainls
+    import synth
+    p = synth.make_problem(160, [7, 8], "c4", blocks=[(7, 0), (8, 1)])
+    eng = gainls.Engine(11, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    vl, vu = p.blocks[(0, 0)].vecs, p.blocks[(1, 1)].vecs
+    assert vu.shape[0] >= 512
+    lo, up = list(range(vl.shape[0])), list(range(vu.shape[0]))
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    one = eng.fetch_amp().copy()
+    pin = torch.empty(vu.shape, dtype=torch.float64, pin_memory=True).numpy()
+    pin[...] = vu
+    monkeypatch.setenv("GAINLS_UPPER_HALVES", "force")
+    eng.upload_eigvecs_async(1, 1, pin)
+    st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    assert st["kernel_launches"] >= 9   # two upper slicings and two amplitude GEMM launches
+    np.testing.assert_array_equal(eng.fetch_amp(), one)
