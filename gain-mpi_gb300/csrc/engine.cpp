@@ -282,6 +282,10 @@ struct gain_engine_s {
     bool have_amp = false;
     std::vector<int> amp_job;   // jindI, gammaI, jindF, gammaF, lower levels, upper levels of amp
     long launches = 0;          // kernels this engine has launched (split path and band builds)
+    // page-locked staging of a run's small uploads (level lists, tiles) and readbacks
+    char* stage = nullptr;
+    size_t stage_cap = 0, stage_off = 0;
+    void* readback = nullptr;
 
     // work buffers
     gain::DevArray<int> d_lower, d_upper;
@@ -375,6 +379,30 @@ GammaMaps* gamma_maps(gain_engine e, int jind, int g) {
         return nullptr;
     m.built = true;
     return &m;
+}
+
+// Copy n elements into d through the engine's page-locked staging area, asynchronously on
+// the engine's stream (the area restarts at each run, after the previous run synchronised).
+template <class T>
+gain_status upload_staged(gain_engine e, DevArray<T>& d, const T* h, size_t n) {
+    GAIN_TRY(d.alloc(n));
+    if (!n) return GAIN_OK;
+    const size_t bytes = sizeof(T) * n;
+    size_t off = (e->stage_off + 255) & ~(size_t)255;
+    if (off + bytes > e->stage_cap) {
+        GAIN_CUDA(cudaStreamSynchronize(e->st));   // copies still reading the old area
+        if (e->stage) cudaFreeHost(e->stage);
+        e->stage = nullptr;
+        e->stage_cap = 0;
+        const size_t cap = std::max(std::max(off + bytes, 2 * e->stage_cap), (size_t)1 << 20);
+        GAIN_CUDA(cudaMallocHost((void**)&e->stage, cap));
+        e->stage_cap = cap;
+        off = 0;
+    }
+    memcpy(e->stage + off, h, bytes);
+    GAIN_CUDA(cudaMemcpyAsync(d.p, e->stage + off, bytes, cudaMemcpyHostToDevice, e->st));
+    e->stage_off = off + bytes;
+    return GAIN_OK;
 }
 
 gain_status validate_job(gain_engine e, const gain_pair_job* j) {
@@ -1006,8 +1034,9 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         for (int u = 0; u < cand && in_head; ++u) in_head = j->upper_levels[u] < EF.head_rows;
         if (in_head) Nu2 = cand;
     }
-    GAIN_TRY(e->d_lower.upload(j->lower_levels, B));
-    GAIN_TRY(e->d_upper.upload(j->upper_levels, Nu));
+    e->stage_off = 0;   // the previous run synchronised: the staging area is free
+    GAIN_TRY(upload_staged(e, e->d_lower, j->lower_levels, (size_t)B));
+    GAIN_TRY(upload_staged(e, e->d_upper, j->upper_levels, (size_t)Nu));
     GAIN_TRY(e->counters.alloc(4));
     GAIN_TRY(e->counters.zero(st, 4));
     GAIN_TRY(e->ull.alloc(4));
@@ -1088,7 +1117,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
 
     // ---- GEMM 1: H = V M (one pass per dipole piece)
     const std::vector<split::Prod> pr1 = make_prods(p1x);
-    GAIN_TRY(e->prods1.upload(pr1));
+    GAIN_TRY(upload_staged(e, e->prods1, pr1.data(), pr1.size()));
     GAIN_TRY(e->H.alloc((size_t)Bpad * L.fpad));
     GAIN_TRY(e->rowerr.alloc(Bpad));
     GAIN_TRY(e->rowerr.zero(st, Bpad));
@@ -1136,7 +1165,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
                     t1.push_back(t);
                 }
             }
-        GAIN_TRY(e->tiles1.upload(t1));
+        GAIN_TRY(upload_staged(e, e->tiles1, t1.data(), t1.size()));
         split::GemmArgs g1;
         memset(&g1, 0, sizeof g1);
         g1.tiles = e->tiles1.p;
@@ -1247,8 +1276,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
             t2.push_back(t);
         }
     const std::vector<split::Prod> pr2 = make_prods(p2);
-    GAIN_TRY(e->tiles2.upload(t2));
-    GAIN_TRY(e->prods2.upload(pr2));
+    GAIN_TRY(upload_staged(e, e->tiles2, t2.data(), t2.size()));
+    GAIN_TRY(upload_staged(e, e->prods2, pr2.data(), pr2.size()));
     GAIN_TRY(e->amp.alloc((size_t)Bpad * Nupad));
     split::GemmArgs g2;
     memset(&g2, 0, sizeof g2);
@@ -1315,14 +1344,21 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     GAIN_CUDA(split::launch_refine_amp(ra, 4 * e->num_sms, st));
     ++e->launches;
     GAIN_CUDA(cudaEventRecord(e->ev[1], st));
-    GAIN_CUDA(cudaStreamSynchronize(st));
 
     unsigned int cnt[4];
     unsigned long long unc[4];
     int errw = 0;
-    GAIN_CUDA(cudaMemcpy(cnt, e->counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
-    GAIN_CUDA(cudaMemcpy(unc, e->ull.p, sizeof unc, cudaMemcpyDeviceToHost));
-    GAIN_CUDA(cudaMemcpy(&errw, e->err.p, sizeof errw, cudaMemcpyDeviceToHost));
+    {   // the run's counters through one page-locked area
+        if (!e->readback) GAIN_CUDA(cudaMallocHost(&e->readback, 128));
+        char* rb = (char*)e->readback;
+        GAIN_CUDA(cudaMemcpyAsync(rb, e->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
+        GAIN_CUDA(cudaMemcpyAsync(rb + 32, e->ull.p, sizeof unc, cudaMemcpyDeviceToHost, st));
+        GAIN_CUDA(cudaMemcpyAsync(rb + 64, e->err.p, sizeof errw, cudaMemcpyDeviceToHost, st));
+        GAIN_CUDA(cudaStreamSynchronize(st));
+        memcpy(cnt, rb, sizeof cnt);
+        memcpy(unc, rb + 32, sizeof unc);
+        memcpy(&errw, rb + 64, sizeof errw);
+    }
     e->amp_rows = B;
     e->amp_cols = Nu;
     e->amp_ld = Nupad;
@@ -1523,6 +1559,8 @@ gain_status gain_engine_destroy(gain_engine e) {
     if (e->stc) cudaStreamDestroy(e->stc);
     if (e->st2) cudaStreamDestroy(e->st2);
     if (e->st) cudaStreamDestroy(e->st);
+    if (e->stage) cudaFreeHost(e->stage);
+    if (e->readback) cudaFreeHost(e->readback);
     delete e;
     return GAIN_OK;
 }
