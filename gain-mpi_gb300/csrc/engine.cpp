@@ -1029,7 +1029,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         arriving = q == cudaErrorNotReady || (halves && std::string(halves) == "force");
     }
     if (arriving) {
-        const int cand = (Nu / 2) / split::BN * split::BN;
+        const int cand = (Nupad / split::BN + 1) / 2 * split::BN;   // the upper blocks halved, rounded up
         bool in_head = true;
         for (int u = 0; u < cand && in_head; ++u) in_head = j->upper_levels[u] < EF.head_rows;
         if (in_head) Nu2 = cand;
@@ -1794,7 +1794,8 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
     GAIN_CUDA(cudaStreamWaitEvent(e->stc, e->ev_up, 0));
     // two parts: a run can start on the upper states of the first part while the second
     // is still arriving
-    const int head = nlevels >= 512 ? nlevels / 2 : 0;
+    // (the head ends on a multiple of 128 rows, where the run's upper halves split)
+    const int head = nlevels >= 512 ? std::min(nlevels - 1, round_up(nlevels / 2, 128)) : 0;
     if (head > 0) {
         GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)head * nsize, cudaMemcpyHostToDevice,
                                   e->stc));
