@@ -282,10 +282,7 @@ struct gain_engine_s {
     bool have_amp = false;
     std::vector<int> amp_job;   // jindI, gammaI, jindF, gammaF, lower levels, upper levels of amp
     long launches = 0;          // kernels this engine has launched (split path and band builds)
-    // page-locked staging of a run's small uploads (level lists, tiles) and readbacks
-    char* stage = nullptr;
-    size_t stage_cap = 0, stage_off = 0;
-    void* readback = nullptr;
+    void* readback = nullptr;   // page-locked area of a run's counter readbacks
 
     // work buffers
     gain::DevArray<int> d_lower, d_upper;
@@ -379,30 +376,6 @@ GammaMaps* gamma_maps(gain_engine e, int jind, int g) {
         return nullptr;
     m.built = true;
     return &m;
-}
-
-// Copy n elements into d through the engine's page-locked staging area, asynchronously on
-// the engine's stream (the area restarts at each run, after the previous run synchronised).
-template <class T>
-gain_status upload_staged(gain_engine e, DevArray<T>& d, const T* h, size_t n) {
-    GAIN_TRY(d.alloc(n));
-    if (!n) return GAIN_OK;
-    const size_t bytes = sizeof(T) * n;
-    size_t off = (e->stage_off + 255) & ~(size_t)255;
-    if (off + bytes > e->stage_cap) {
-        GAIN_CUDA(cudaStreamSynchronize(e->st));   // copies still reading the old area
-        if (e->stage) cudaFreeHost(e->stage);
-        e->stage = nullptr;
-        e->stage_cap = 0;
-        const size_t cap = std::max(std::max(off + bytes, 2 * e->stage_cap), (size_t)1 << 20);
-        GAIN_CUDA(cudaMallocHost((void**)&e->stage, cap));
-        e->stage_cap = cap;
-        off = 0;
-    }
-    memcpy(e->stage + off, h, bytes);
-    GAIN_CUDA(cudaMemcpyAsync(d.p, e->stage + off, bytes, cudaMemcpyHostToDevice, e->st));
-    e->stage_off = off + bytes;
-    return GAIN_OK;
 }
 
 gain_status validate_job(gain_engine e, const gain_pair_job* j) {
@@ -1034,9 +1007,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         for (int u = 0; u < cand && in_head; ++u) in_head = j->upper_levels[u] < EF.head_rows;
         if (in_head) Nu2 = cand;
     }
-    e->stage_off = 0;   // the previous run synchronised: the staging area is free
-    GAIN_TRY(upload_staged(e, e->d_lower, j->lower_levels, (size_t)B));
-    GAIN_TRY(upload_staged(e, e->d_upper, j->upper_levels, (size_t)Nu));
+    // Small uploads stay synchronous: an asynchronous copy on this stream would queue in the
+    // host-to-device engine behind an eigenvector copy still in flight and hold GEMM 1 back.
+    GAIN_TRY(e->d_lower.upload(j->lower_levels, B));
+    GAIN_TRY(e->d_upper.upload(j->upper_levels, Nu));
     GAIN_TRY(e->counters.alloc(4));
     GAIN_TRY(e->counters.zero(st, 4));
     GAIN_TRY(e->ull.alloc(4));
@@ -1117,7 +1091,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
 
     // ---- GEMM 1: H = V M (one pass per dipole piece)
     const std::vector<split::Prod> pr1 = make_prods(p1x);
-    GAIN_TRY(upload_staged(e, e->prods1, pr1.data(), pr1.size()));
+    GAIN_TRY(e->prods1.upload(pr1));
     GAIN_TRY(e->H.alloc((size_t)Bpad * L.fpad));
     GAIN_TRY(e->rowerr.alloc(Bpad));
     GAIN_TRY(e->rowerr.zero(st, Bpad));
@@ -1165,7 +1139,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
                     t1.push_back(t);
                 }
             }
-        GAIN_TRY(upload_staged(e, e->tiles1, t1.data(), t1.size()));
+        GAIN_TRY(e->tiles1.upload(t1));
         split::GemmArgs g1;
         memset(&g1, 0, sizeof g1);
         g1.tiles = e->tiles1.p;
@@ -1276,8 +1250,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
             t2.push_back(t);
         }
     const std::vector<split::Prod> pr2 = make_prods(p2);
-    GAIN_TRY(upload_staged(e, e->tiles2, t2.data(), t2.size()));
-    GAIN_TRY(upload_staged(e, e->prods2, pr2.data(), pr2.size()));
+    GAIN_TRY(e->tiles2.upload(t2));
+    GAIN_TRY(e->prods2.upload(pr2));
     GAIN_TRY(e->amp.alloc((size_t)Bpad * Nupad));
     split::GemmArgs g2;
     memset(&g2, 0, sizeof g2);
@@ -1559,7 +1533,6 @@ gain_status gain_engine_destroy(gain_engine e) {
     if (e->stc) cudaStreamDestroy(e->stc);
     if (e->st2) cudaStreamDestroy(e->st2);
     if (e->st) cudaStreamDestroy(e->st);
-    if (e->stage) cudaFreeHost(e->stage);
     if (e->readback) cudaFreeHost(e->readback);
     delete e;
     return GAIN_OK;
