@@ -447,10 +447,21 @@ def adjoint_check(args):
     grad = np.zeros(mu0.size)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
+    chain_ms = {"f64": 0.0, "f32": 0.0}
     for (jI, gI, jF, gF, lo, up), g in zip(pairs, dLdS):
         eng.adjoint(jI, gI, jF, gF, lo, up, g, grad)
+        chain_ms["f64"] += eng.last_adjoint_stats.device_ms
     times["adjoint_s"] = time.perf_counter() - t1
     grad = grad.reshape(mu0.shape)
+    # the same gradient with the adjoint chain in FP32 arithmetic
+    grad32 = np.zeros(mu0.size)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for (jI, gI, jF, gF, lo, up), g in zip(pairs, dLdS):
+        eng.adjoint(jI, gI, jF, gF, lo, up, g, grad32, precision="f32")
+        chain_ms["f32"] += eng.last_adjoint_stats.device_ms
+    times["adjoint_fp32_s"] = time.perf_counter() - t1
+    fp32_vs_fp64 = float(np.max(np.abs(grad32 - grad.reshape(-1))) / np.abs(grad).max())
     # the same gradient from the split path's amplitudes: per pair the tensor-core forward,
     # dL/dS on the device, then the adjoint (which takes the run's amplitudes)
     grad_split = np.zeros(mu0.size)
@@ -471,7 +482,7 @@ def adjoint_check(args):
     gmax = float(np.abs(gflat).max())
     cand = np.flatnonzero(np.abs(gflat) > 0)
     picks = rng.choice(cand, size=min(args.adj_fd, cand.size), replace=False)
-    rel, absn, jrel = [], [], []
+    rel, absn, jrel, rel32 = [], [], [], []
     t1 = time.perf_counter()
     for k in picks:
         mp, mm = mu0.copy(), mu0.copy()
@@ -480,6 +491,7 @@ def adjoint_check(args):
         fd = (loss(mp) - loss(mm)) / (2 * h)
         rel.append(abs(fd - gflat[k]) / abs(gflat[k]))
         absn.append(abs(fd - gflat[k]) / gmax)
+        rel32.append(abs(fd - grad32[k]) / abs(gflat[k]))
     times["fd_s"] = time.perf_counter() - t1
     t1 = time.perf_counter()
     for k in picks:
@@ -497,13 +509,16 @@ def adjoint_check(args):
     rel, jrel = np.asarray(rel), np.asarray(jrel)
     out = {"mode": "adjoint", "workload": f"N_v={nv}, J=0..5, all allowed block pairs",
            "pairs": len(pairs), "lines": n_lines, "lines_in_loss": int(sum(int(m.sum()) for m in masks)),
-           "loss": L0, "gradient_dtype": "f64", "fd_step": h, "fd_entries": int(len(picks)),
+           "loss": L0, "gradient_dtype": "f64 (and f32: fp32_*)", "fd_step": h, "fd_entries": int(len(picks)),
            "fd_max_rel_err": float(rel.max()), "fd_median_rel_err": float(np.median(rel)),
            "fd_p99_rel_err": float(np.quantile(rel, 0.99)),
            "fd_max_err_over_max_grad": float(max(absn)), "fd_direction_rel_err": [float(x) for x in dirs],
            "exact_partials_max_rel_err": float(jrel.max()), "exact_partials_median_rel_err": float(np.median(jrel)),
            "exact_direction_rel_err": [float(x) for x in jdirs],
            "split_forward_gradient_max_err_over_max_grad": split_vs_fp64,
+           "fp32_gradient_max_err_over_max_grad": fp32_vs_fp64,
+           "fp32_fd_median_rel_err": float(np.median(rel32)), "fp32_fd_p99_rel_err": float(np.quantile(rel32, 0.99)),
+           "adjoint_chain_device_ms": chain_ms,
            "nonzero_gradient_entries": int(cand.size), "gradient_entries": int(mu0.size),
            "setup_s": setup_s}
     out.update(times)

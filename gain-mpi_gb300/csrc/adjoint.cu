@@ -16,45 +16,51 @@ namespace {
 
 __device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
 
+template <class T>
 __global__ void k_adj_scale(int rows, int cols, const double* __restrict__ dLdS, const double* __restrict__ amp,
-                            long ld_amp, double* __restrict__ G) {
+                            long ld_amp, T* __restrict__ G) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long)rows * cols) return;
     const long r = i / cols, c = i - r * cols;
-    G[i] = 2.0 * dLdS[i] * amp[r * ld_amp + c];
+    G[i] = (T)2 * (T)dLdS[i] * (T)amp[r * ld_amp + c];
 }
 
-// C[m][n] = sum_k A[m][k] B[levels[k]][n]: 64 x 64 tiles, 16 x 16 threads, 4 x 4 outputs each.
+// Register-tiled SIMT product: 64 x 64 output tiles, 16 x 16 threads, each thread the 4 x 4
+// outputs (ty + 16 i, tx + 16 j), so a warp's shared-memory reads are broadcasts (rows) or 16
+// consecutive words (columns).  Accumulation in T, one FMA per term in ascending inner order.
 constexpr int kTile = 64, kTk = 16;
+
+// C[m][n] = sum_k A[m][k] B[levels[k]][n]  (B is FP64 eigenvector storage, rounded to T)
+template <class T>
 __global__ void __launch_bounds__(256)
-k_adj_gemm(int M, int N, int K, const double* __restrict__ A, long lda, const double* __restrict__ B, long ldb,
-           const int* __restrict__ levels, double* __restrict__ C, long ldc) {
-    __shared__ double sA[kTk][kTile + 1];
-    __shared__ double sB[kTk][kTile + 1];
+k_adj_gemm(int M, int N, int K, const T* __restrict__ A, long lda, const double* __restrict__ B, long ldb,
+           const int* __restrict__ levels, T* __restrict__ C, long ldc) {
+    __shared__ T sA[kTk][kTile + 1];
+    __shared__ T sB[kTk][kTile];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
-    double acc[4][4] = {};
+    T acc[4][4] = {};
     for (int k0 = 0; k0 < K; k0 += kTk) {
         for (int t = threadIdx.x; t < kTile * kTk; t += 256) {
             const int mm = t / kTk, kk = t % kTk;           // A tile: 64 rows x 16 k
             const int gm = m0 + mm, gk = k0 + kk;
-            sA[kk][mm] = (gm < M && gk < K) ? A[(long)gm * lda + gk] : 0.0;
+            sA[kk][mm] = (gm < M && gk < K) ? A[(long)gm * lda + gk] : (T)0;
             const int kb = t / kTile, nn = t % kTile;       // B tile: 16 k x 64 columns
             const int gk2 = k0 + kb, gn = n0 + nn;
-            sB[kb][nn] = (gk2 < K && gn < N) ? B[(long)levels[gk2] * ldb + gn] : 0.0;
+            sB[kb][nn] = (gk2 < K && gn < N) ? (T)B[(long)levels[gk2] * ldb + gn] : (T)0;
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < kTk; ++kk) {
-            double a[4], b[4];
+            T a[4], b[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty * 4 + i];
+            for (int i = 0; i < 4; ++i) a[i] = sA[kk][ty + 16 * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx * 4 + j];
+            for (int j = 0; j < 4; ++j) b[j] = sB[kk][tx + 16 * j];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = __fma_rn(a[i], b[j], acc[i][j]);
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
         }
         __syncthreads();
     }
@@ -62,75 +68,131 @@ k_adj_gemm(int M, int N, int K, const double* __restrict__ A, long lda, const do
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+            const int gm = m0 + ty + 16 * i, gn = n0 + tx + 16 * j;
             if (gm < M && gn < N) C[(long)gm * ldc + gn] = acc[i][j];
         }
 }
 
-// One thread per (F, I) candidate: I across the block, F over the grid's y dimension; pairs
-// outside the K-block window of F (|K_I - K_F| > 1) or with a vanishing factor return early.
-__device__ void adj_dmu_one(const AdjArgs& a, int F, int I) {
+// The half line strength's factor of (F, I) for the three dipole components: the K-block
+// kernel's 3j, truncated 1/sqrt(2), sign and component rules (one component non-zero), or the
+// rotational-symmetry form's Wigner weights.  Returns false when all three vanish or when F
+// lies outside the dipole piece.
+__device__ __forceinline__ bool adj_factor(const AdjArgs& a, int F, int I, double w[3]) {
+    w[0] = w[1] = w[2] = 0.0;
     const int vF = a.vibF[F];
-    if (vF < a.startF || vF >= a.endF) return;
-    double w[3] = {0.0, 0.0, 0.0};
-    int dsel = -1;   // component of the K-block form (one component per (F, I))
+    if (vF < a.startF || vF >= a.endF) return false;
     if (a.wigner) {
         const long wi = 3 * ((long)a.levI[I] + (long)a.nlevelI *
                              ((long)a.levF[F] + (long)a.nlevelF * ((long)a.KI[I] + (long)a.maxdeg * a.KF[F])));
         w[0] = a.wigner[wi];
         w[1] = a.wigner[wi + 1];
         w[2] = a.wigner[wi + 2];
-    } else {
-        const int kI = a.KI[I], kF = a.KF[F];
-        if (abs(kI - kF) > 1) return;
-        const int tI = a.tauI[I], tF = a.tauF[F] & 1;
-        const int eq = (kF == kI), neq = !eq, tneq = (tF != tI);
-        const int c = (tF - tI) * eq + (tF - tI) * (kF - kI) * neq * tneq - neq * (!tneq);
-        if (c == 0) return;
-        const int n = a.jmax + 1;
-        double m = a.threej[a.jI + kI * n + (a.jF - a.jI + 1) * n * n + (kF - kI + 1) * n * n * 3];
-        if (kI != kF && kI * kF != 0) m *= kSqrt2Ref;
-        m *= (double)c * parity_sign((kI % 3) * tI + kI) * parity_sign((kF % 3) * tF);
-        dsel = 2 * eq + neq * (!tneq);
-        w[dsel] = m;
+        return w[0] != 0.0 || w[1] != 0.0 || w[2] != 0.0;
     }
-    double acc = 0.0;
-    for (int b = 0; b < a.nb; ++b) acc = __fma_rn(a.dh[(long)b * a.ld_dh + F], a.vp[(long)b * a.ld_vp + I], acc);
-    const long base = (long)(vF - a.startF) + (long)a.vibI[I] * a.ncontrF;
-    const long ds = (long)a.dipN * a.ncontrF;
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-        if (w[d] != 0.0) atomicAdd(&a.dmu[base + d * ds], w[d] * acc);
+    const int kI = a.KI[I], kF = a.KF[F];
+    if (abs(kI - kF) > 1) return false;
+    const int tI = a.tauI[I], tF = a.tauF[F] & 1;
+    const int eq = (kF == kI), neq = !eq, tneq = (tF != tI);
+    const int c = (tF - tI) * eq + (tF - tI) * (kF - kI) * neq * tneq - neq * (!tneq);
+    if (c == 0) return false;
+    const int n = a.jmax + 1;
+    double m = a.threej[a.jI + kI * n + (a.jF - a.jI + 1) * n * n + (kF - kI + 1) * n * n * 3];
+    if (kI != kF && kI * kF != 0) m *= kSqrt2Ref;
+    m *= (double)c * parity_sign((kI % 3) * tI + kI) * parity_sign((kF % 3) * tF);
+    w[2 * eq + neq * (!tneq)] = m;
+    return true;
 }
 
+// dM[F][I] = sum_b dh[b][F] vp[b][I] over one listed 64 x 64 (F, I) tile, then
+// dL/dmu_d[vI][vF - startF] += factor_d(F, I) dM[F][I] (atomic: several (F, I) share an entry).
+template <class T>
 __global__ void __launch_bounds__(256)
-k_adj_dmu(AdjArgs a) {
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= a.dimI) return;
-    for (int F = blockIdx.y; F < a.dimF; F += gridDim.y) adj_dmu_one(a, F, I);
+k_adj_dm(AdjArgs a, const int2* __restrict__ tiles) {
+    __shared__ T sH[kTk][kTile];
+    __shared__ T sV[kTk][kTile];
+    const int2 tile = tiles[blockIdx.x];
+    const int f0 = tile.x, i0 = tile.y;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const T* dh = static_cast<const T*>(a.dh);
+    const T* vp = static_cast<const T*>(a.vp);
+    T acc[4][4] = {};
+    for (int b0 = 0; b0 < a.nb; b0 += kTk) {
+        for (int t = threadIdx.x; t < kTile * kTk; t += 256) {
+            const int bb = t / kTile, c = t % kTile;        // both tiles: 16 states x 64 functions
+            const int gb = b0 + bb;
+            sH[bb][c] = (gb < a.nb && f0 + c < a.dimF) ? dh[(long)gb * a.ld_dh + f0 + c] : (T)0;
+            sV[bb][c] = (gb < a.nb && i0 + c < a.dimI) ? vp[(long)gb * a.ld_vp + i0 + c] : (T)0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kTk; ++kk) {
+            T x[4], y[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) x[i] = sH[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) y[j] = sV[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(x[i], y[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    T* dmu = static_cast<T*>(a.dmu);
+    const long ds = (long)a.dipN * a.ncontrF;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int F = f0 + ty + 16 * i;
+        if (F >= a.dimF) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int I = i0 + tx + 16 * j;
+            double w[3];
+            if (I >= a.dimI || !adj_factor(a, F, I, w)) continue;
+            const long base = (long)(a.vibF[F] - a.startF) + (long)a.vibI[I] * a.ncontrF;
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if (w[d] != 0.0) atomicAdd(&dmu[base + d * ds], (T)w[d] * acc[i][j]);
+        }
+    }
 }
 
 }  // namespace
 
-cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, double* G,
-                             cudaStream_t st) {
+cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, void* G,
+                             bool fp32, cudaStream_t st) {
     const long n = (long)rows * cols;
     if (n <= 0) return cudaSuccess;
-    k_adj_scale<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, G);
+    const unsigned nblk = (unsigned)((n + 255) / 256);
+    if (fp32)
+        k_adj_scale<float><<<nblk, 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, static_cast<float*>(G));
+    else
+        k_adj_scale<double><<<nblk, 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, static_cast<double*>(G));
     return cudaGetLastError();
 }
 
-cudaError_t launch_adj_gemm(int M, int N, int K, const double* A, long lda, const double* B, long ldb,
-                            const int* levels, double* C, long ldc, cudaStream_t st) {
+cudaError_t launch_adj_gemm(int M, int N, int K, const void* A, long lda, const double* B, long ldb,
+                            const int* levels, void* C, long ldc, bool fp32, cudaStream_t st) {
     if (M <= 0 || N <= 0) return cudaSuccess;
-    k_adj_gemm<<<dim3((N + kTile - 1) / kTile, (M + kTile - 1) / kTile), 256, 0, st>>>(M, N, K, A, lda, B, ldb,
-                                                                                     levels, C, ldc);
+    const dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
+    if (fp32)
+        k_adj_gemm<float><<<grid, 256, 0, st>>>(M, N, K, static_cast<const float*>(A), lda, B, ldb, levels,
+                                                static_cast<float*>(C), ldc);
+    else
+        k_adj_gemm<double><<<grid, 256, 0, st>>>(M, N, K, static_cast<const double*>(A), lda, B, ldb, levels,
+                                                 static_cast<double*>(C), ldc);
     return cudaGetLastError();
 }
 
-cudaError_t launch_adj_dmu(const AdjArgs& a, cudaStream_t st) {
-    if (a.dimF <= 0 || a.dimI <= 0 || a.nb <= 0) return cudaSuccess;
-    k_adj_dmu<<<dim3((a.dimI + 255) / 256, a.dimF < 65535 ? a.dimF : 65535), 256, 0, st>>>(a);
+int adj_tile() { return kTile; }
+
+cudaError_t launch_adj_dm(const AdjArgs& a, const int* tiles, int ntiles, bool fp32, cudaStream_t st) {
+    if (ntiles <= 0 || a.nb <= 0) return cudaSuccess;
+    const int2* t = reinterpret_cast<const int2*>(tiles);
+    if (fp32)
+        k_adj_dm<float><<<ntiles, 256, 0, st>>>(a, t);
+    else
+        k_adj_dm<double><<<ntiles, 256, 0, st>>>(a, t);
     return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -288,7 +289,7 @@ struct gain_engine_s {
     gain::DevArray<int> d_lower, d_upper;
     gain::DevArray<double> primI, hprim, hsym;
     gain::DevArray<double> adj_dLdS, adj_G, adj_dH, adj_dh, adj_vp, adj_dmu;   // adjoint work space
-    gain::DevArray<int> adj_iota;
+    gain::DevArray<int> adj_iota, adj_tiles;
     gain::DevArray<__nv_bfloat16> Vdig, Hdig, Udig;
     gain::StatsDev Vst, Hst, Ust;
     gain::DevArray<double> H, Hsym;   // H in the GEMM1 layout; contracted with a mixing expansion
@@ -1783,7 +1784,15 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
 
 gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
                               gain_stats* stats) {
+    return gain_adjoint_pair_prec(e, job, dL_dS, dL_dmu, GAIN_ADJOINT_FP64, stats);
+}
+
+gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
+                                   gain_adjoint_precision prec, gain_stats* stats) {
     clear_error();
+    if (prec != GAIN_ADJOINT_FP64 && prec != GAIN_ADJOINT_FP32)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair_prec: unknown precision %d", (int)prec);
+    const bool f32 = prec == GAIN_ADJOINT_FP32;
     GAIN_TRY(check_engine(e));
     GAIN_TRY(validate_job(e, job));
     if (!dL_dS || !dL_dmu) return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair: NULL argument");
@@ -1808,26 +1817,73 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     const size_t nS = (size_t)B * Nu, nmu = (size_t)3 * e->dipN * e->ncontrF;
     cudaStream_t st = e->st;
     GAIN_TRY(e->adj_dLdS.upload(dL_dS, nS));
-    GAIN_TRY(e->adj_G.alloc(nS));
-    GAIN_TRY(e->adj_dH.alloc((size_t)B * NtF));
-    GAIN_TRY(e->adj_dh.alloc((size_t)B * bF.dimen));
-    GAIN_TRY(e->adj_vp.alloc((size_t)B * bI.dimen));
+    // work space in the chain's precision (float arrays live in the double allocations)
+    const size_t esz = f32 ? sizeof(float) : sizeof(double);
+    auto words = [&](size_t n) { return (n * esz + sizeof(double) - 1) / sizeof(double); };
+    GAIN_TRY(e->adj_G.alloc(words(nS)));
+    GAIN_TRY(e->adj_dH.alloc(words((size_t)B * NtF)));
+    GAIN_TRY(e->adj_dh.alloc(words((size_t)B * bF.dimen)));
+    GAIN_TRY(e->adj_vp.alloc(words((size_t)B * bI.dimen)));
     GAIN_TRY(e->adj_dmu.alloc(nmu));
     GAIN_TRY(e->adj_dmu.zero(st, nmu));
     std::vector<int> iota(B);
     for (int b = 0; b < B; ++b) iota[b] = b;
     GAIN_TRY(e->adj_iota.upload(iota));
+    // (F, I) tiles that hold a possibly non-zero factor: F in the dipole piece and, in the
+    // K-block form, |K_I - K_F| <= 1 somewhere in the tile
+    const WignerTab* wt = wigner_of(e, job->jindI, job->jindF);
+    const int tl = adj_tile();
+    auto kranges = [&](const Basis& b, bool upper, std::vector<int>& lo, std::vector<int>& hi) {
+        const int nt = (b.dimen + tl - 1) / tl;
+        lo.assign(nt, INT_MAX);
+        hi.assign(nt, INT_MIN);
+        for (int f = 0; f < b.dimen; ++f) {
+            if (upper && (b.vib[f] < e->startF || b.vib[f] >= e->endF)) continue;
+            lo[f / tl] = std::min(lo[f / tl], b.K[f]);
+            hi[f / tl] = std::max(hi[f / tl], b.K[f]);
+        }
+    };
+    std::vector<int> kFlo, kFhi, kIlo, kIhi, tiles;
+    kranges(bF, true, kFlo, kFhi);
+    kranges(bI, false, kIlo, kIhi);
+    for (size_t tf = 0; tf < kFlo.size(); ++tf) {
+        if (kFlo[tf] > kFhi[tf]) continue;   // no function of the piece
+        for (size_t ti = 0; ti < kIlo.size(); ++ti) {
+            if (!wt && (kIlo[ti] > kFhi[tf] + 1 || kFlo[tf] > kIhi[ti] + 1)) continue;
+            tiles.push_back((int)tf * tl);
+            tiles.push_back((int)ti * tl);
+        }
+    }
+    GAIN_TRY(e->adj_tiles.upload(tiles));
+    void* G = e->adj_G.p;
+    void* dH = e->adj_dH.p;
+    void* dh = e->adj_dh.p;
+    void* vp = e->adj_vp.p;
     GAIN_CUDA(cudaEventRecord(e->ev[0], st));
     // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dL/dH
-    GAIN_CUDA(launch_adj_scale(B, Nu, e->adj_dLdS.p, e->amp.p, e->amp_ld, e->adj_G.p, st));
-    GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, e->adj_G.p, Nu, EF.d.p, EF.nsize, e->d_upper.p, e->adj_dH.p, NtF, st));
-    GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF, iF.dijterms.p,
-                                   iF.dicontr.p, iF.dN[job->gammaF]->p, iF.drepres[job->gammaF]->p, e->adj_dH.p, NtF,
-                                   e->adj_iota.p, e->adj_dh.p, bF.dimen, B, st));
-    // lower vectors in primitive space, then dL/dmu from the band (or dense) products
-    GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, 0, iI.sdeg[job->gammaI], iI.Ntot[job->gammaI],
-                                   iI.dijterms.p, iI.dicontr.p, iI.dN[job->gammaI]->p, iI.drepres[job->gammaI]->p,
-                                   EI.d.p, EI.nsize, e->d_lower.p, e->adj_vp.p, bI.dimen, B, st));
+    GAIN_CUDA(launch_adj_scale(B, Nu, e->adj_dLdS.p, e->amp.p, e->amp_ld, G, f32, st));
+    GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, G, Nu, EF.d.p, EF.nsize, e->d_upper.p, dH, NtF, f32, st));
+    const int* repF_N = iF.dN[job->gammaF]->p;
+    const double* repF = iF.drepres[job->gammaF]->p;
+    const int* repI_N = iI.dN[job->gammaI]->p;
+    const double* repI = iI.drepres[job->gammaI]->p;
+    if (f32) {
+        GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF,
+                                       iF.dijterms.p, iF.dicontr.p, repF_N, repF, (const float*)dH, NtF,
+                                       e->adj_iota.p, (float*)dh, bF.dimen, B, st));
+        GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, 0, iI.sdeg[job->gammaI],
+                                       iI.Ntot[job->gammaI], iI.dijterms.p, iI.dicontr.p, repI_N, repI, EI.d.p,
+                                       EI.nsize, e->d_lower.p, (float*)vp, bI.dimen, B, st));
+    } else {
+        GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF,
+                                       iF.dijterms.p, iF.dicontr.p, repF_N, repF, (const double*)dH, NtF,
+                                       e->adj_iota.p, (double*)dh, bF.dimen, B, st));
+        // lower vectors in primitive space
+        GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, 0, iI.sdeg[job->gammaI],
+                                       iI.Ntot[job->gammaI], iI.dijterms.p, iI.dicontr.p, repI_N, repI, EI.d.p,
+                                       EI.nsize, e->d_lower.p, (double*)vp, bI.dimen, B, st));
+    }
+    // dL/dmu from the band (or dense) products
     AdjArgs a;
     memset(&a, 0, sizeof a);
     a.dimF = bF.dimen;
@@ -1845,7 +1901,7 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     a.jF = bF.J;
     a.jmax = e->jmax;
     a.threej = e->d3j.p;
-    if (const WignerTab* wt = wigner_of(e, job->jindI, job->jindF)) {
+    if (wt) {
         a.wigner = wt->rot.p;
         a.nlevelI = wt->nI;
         a.nlevelF = wt->nF;
@@ -1855,17 +1911,24 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     a.endF = e->endF;
     a.ncontrF = e->ncontrF;
     a.dipN = e->dipN;
-    a.dh = e->adj_dh.p;
+    a.dh = dh;
     a.ld_dh = bF.dimen;
-    a.vp = e->adj_vp.p;
+    a.vp = vp;
     a.ld_vp = bI.dimen;
     a.dmu = e->adj_dmu.p;
-    GAIN_CUDA(launch_adj_dmu(a, st));
+    GAIN_CUDA(launch_adj_dm(a, e->adj_tiles.p, (int)(tiles.size() / 2), f32, st));
     GAIN_CUDA(cudaEventRecord(e->ev[1], st));
-    std::vector<double> h(nmu);
-    GAIN_CUDA(cudaMemcpyAsync(h.data(), e->adj_dmu.p, sizeof(double) * nmu, cudaMemcpyDeviceToHost, st));
-    GAIN_CUDA(cudaStreamSynchronize(st));
-    for (size_t i = 0; i < nmu; ++i) dL_dmu[i] += h[i];
+    if (f32) {
+        std::vector<float> h(nmu);
+        GAIN_CUDA(cudaMemcpyAsync(h.data(), e->adj_dmu.p, sizeof(float) * nmu, cudaMemcpyDeviceToHost, st));
+        GAIN_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < nmu; ++i) dL_dmu[i] += (double)h[i];
+    } else {
+        std::vector<double> h(nmu);
+        GAIN_CUDA(cudaMemcpyAsync(h.data(), e->adj_dmu.p, sizeof(double) * nmu, cudaMemcpyDeviceToHost, st));
+        GAIN_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < nmu; ++i) dL_dmu[i] += h[i];
+    }
     if (stats) {
         memset(stats, 0, sizeof *stats);
         float ms = 0.f;

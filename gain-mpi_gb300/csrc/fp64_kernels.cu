@@ -231,21 +231,24 @@ __global__ void k_contract(int nsym, const int* __restrict__ rowptr, const int* 
 }
 
 // expansion of a batch of stored vectors: blockIdx.y picks the level
+// TV: storage of the vectors; TP: the arithmetic and output (double, or float for the FP32
+// adjoint, where both operands are rounded to float before the product)
+template <class TV, class TP>
 __global__ void k_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
                                 const int* __restrict__ ijterms, const int* __restrict__ icontr,
                                 const int* __restrict__ N, const double* __restrict__ repres,
-                                const double* __restrict__ vecs, long ldv, const int* __restrict__ levels,
-                                double* __restrict__ prim, long ldp) {
+                                const TV* __restrict__ vecs, long ldv, const int* __restrict__ levels,
+                                TP* __restrict__ prim, long ldp) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= dimen) return;
-    const double* vecI = vecs + (long)levels[blockIdx.y] * ldv;
+    const TV* vecI = vecs + (long)levels[blockIdx.y] * ldv;
     const int irow = icontr[r];
     const int ib = icontr[r + dimen];
     const int iterm = ijterms[irow + igamma * maxcoeff];
     const int nelem = N[irow];
     const long base = (long)ideg * Ntot + (long)ib * sdeg * Ntot;
-    double acc = 0.0;
-    for (int i = 0; i < nelem; ++i) acc = __fma_rn(vecI[iterm + i], repres[iterm + i + base], acc);
+    TP acc = 0;
+    for (int i = 0; i < nelem; ++i) acc = fma((TP)vecI[iterm + i], (TP)repres[iterm + i + base], acc);
     prim[(long)blockIdx.y * ldp + r] = acc;
 }
 
@@ -456,14 +459,39 @@ cudaError_t launch_contract(int nsym, const int* rowptr, const int* col, const d
     return cudaGetLastError();
 }
 
+template <class TV, class TP>
+static cudaError_t expand_levels_t(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                   const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                   const TV* vecs, long ldv, const int* levels, TP* prim, long ldp, int nbatch,
+                                   cudaStream_t st) {
+    if (dimen <= 0 || nbatch <= 0) return cudaSuccess;
+    k_expand_levels<TV, TP><<<dim3((dimen + 255) / 256, nbatch), 256, 0, st>>>(
+        dimen, igamma, maxcoeff, ideg, sdeg, Ntot, ijterms, icontr, N, repres, vecs, ldv, levels, prim, ldp);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
                                  const int* ijterms, const int* icontr, const int* N, const double* repres,
                                  const double* vecs, long ldv, const int* levels, double* prim, long ldp,
                                  int nbatch, cudaStream_t st) {
-    if (dimen <= 0 || nbatch <= 0) return cudaSuccess;
-    k_expand_levels<<<dim3((dimen + 255) / 256, nbatch), 256, 0, st>>>(
-        dimen, igamma, maxcoeff, ideg, sdeg, Ntot, ijterms, icontr, N, repres, vecs, ldv, levels, prim, ldp);
-    return cudaGetLastError();
+    return expand_levels_t(dimen, igamma, maxcoeff, ideg, sdeg, Ntot, ijterms, icontr, N, repres, vecs, ldv, levels,
+                           prim, ldp, nbatch, st);
+}
+
+cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                 const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                 const double* vecs, long ldv, const int* levels, float* prim, long ldp,
+                                 int nbatch, cudaStream_t st) {
+    return expand_levels_t(dimen, igamma, maxcoeff, ideg, sdeg, Ntot, ijterms, icontr, N, repres, vecs, ldv, levels,
+                           prim, ldp, nbatch, st);
+}
+
+cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                 const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                 const float* vecs, long ldv, const int* levels, float* prim, long ldp,
+                                 int nbatch, cudaStream_t st) {
+    return expand_levels_t(dimen, igamma, maxcoeff, ideg, sdeg, Ntot, ijterms, icontr, N, repres, vecs, ldv, levels,
+                           prim, ldp, nbatch, st);
 }
 
 cudaError_t launch_gemv_batch(int nrows, int n, const double* U, long ldu, const int* levels, const double* x,

@@ -52,17 +52,23 @@ struct AdjArgs {
     const double* wigner;                      // non-null: rotational-symmetry form
     int nlevelI, nlevelF, maxdeg;
     int startF, endF, ncontrF, dipN;
-    const double* dh;                          // [nb][ld_dh] dL/dh, primitive upper index
+    // arrays of the chain's precision (double, or float with fp32)
+    const void* dh;                            // [nb][ld_dh] dL/dh, primitive upper index
     long ld_dh;
-    const double* vp;                          // [nb][ld_vp] lower vectors, primitive index
+    const void* vp;                            // [nb][ld_vp] lower vectors, primitive index
     long ld_vp;
-    double* dmu;                               // [3][dipN][ncontrF] accumulated
+    void* dmu;                                 // [3][dipN][ncontrF] accumulated
 };
-cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, double* G,
-                             cudaStream_t st);
-cudaError_t launch_adj_gemm(int M, int N, int K, const double* A, long lda, const double* B, long ldb,
-                            const int* levels, double* C, long ldc, cudaStream_t st);
-cudaError_t launch_adj_dmu(const AdjArgs& a, cudaStream_t st);
+// G = 2 dL/dS amp in double or float
+cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, void* G,
+                             bool fp32, cudaStream_t st);
+// C = A U[levels]: A and C double or float, the FP64 eigenvectors rounded to the chain's precision
+cudaError_t launch_adj_gemm(int M, int N, int K, const void* A, long lda, const double* B, long ldb,
+                            const int* levels, void* C, long ldc, bool fp32, cudaStream_t st);
+// functions per side of one (F, I) tile of launch_adj_dm
+int adj_tile();
+// dL/dmu over the listed (F, I) tiles: tiles = ntiles pairs (first F, first I)
+cudaError_t launch_adj_dm(const AdjArgs& a, const int* tiles, int ntiles, bool fp32, cudaStream_t st);
 
 cudaError_t launch_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI,
                               const int* kF, const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF,
@@ -97,6 +103,15 @@ cudaError_t launch_contract(int nsym, const int* rowptr, const int* col, const d
 cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
                                  const int* ijterms, const int* icontr, const int* N, const double* repres,
                                  const double* vecs, long ldv, const int* levels, double* prim, long ldp,
+                                 int nbatch, cudaStream_t st);
+// the same in FP32 arithmetic (the FP32 adjoint): vectors of either precision, float output
+cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                 const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                 const double* vecs, long ldv, const int* levels, float* prim, long ldp,
+                                 int nbatch, cudaStream_t st);
+cudaError_t launch_expand_levels(int dimen, int igamma, int maxcoeff, int ideg, int sdeg, int Ntot,
+                                 const int* ijterms, const int* icontr, const int* N, const double* repres,
+                                 const float* vecs, long ldv, const int* levels, float* prim, long ldp,
                                  int nbatch, cudaStream_t st);
 
 // out[b*ldo + u] = sum_f U[level[u]*ldu + f] * x[b*ldx + f], u < nrows, b < nbatch <= 8

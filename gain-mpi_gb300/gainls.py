@@ -192,6 +192,7 @@ def _declare(L):
     L.gain_upload_dipole_pieces.restype = S
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
     L.gain_adjoint_pair.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.POINTER(Stats)]
+    L.gain_adjoint_pair_prec.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.c_int, ctypes.POINTER(Stats)]
     L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
     L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
@@ -247,7 +248,8 @@ def _declare(L):
         getattr(L, name).restype = S
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
-                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair",
+                 "gain_adjoint_pair_prec", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
                  "gain_lines_text_device",
                  "gain_format_values_device"):
@@ -437,9 +439,12 @@ class Engine:
                 check(s)
         return out
 
-    def adjoint(self, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, dL_dS, dL_dmu=None):
+    def adjoint(self, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, dL_dS, dL_dmu=None,
+                precision="f64"):
         """dL/dmu (the dipole piece's layout [3][N][ncontrF], accumulated into dL_dmu if given)
-        of a loss with gradient dL_dS [nlower, nupper] over the pair's line strengths."""
+        of a loss with gradient dL_dS [nlower, nupper] over the pair's line strengths;
+        precision "f64" or "f32" is the arithmetic of the adjoint chain."""
+        prec = {"f64": 0, "f32": 1}[precision]
         lo, up = _i32(lower_levels), _i32(upper_levels)
         g = _f64(dL_dS)
         assert g.size == len(lo) * len(up)
@@ -448,7 +453,9 @@ class Engine:
         assert dL_dmu.dtype == np.float64 and dL_dmu.flags.c_contiguous
         job = PairJob(jindI, gammaI, jindF, gammaF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
         st = Stats()
-        check(lib().gain_adjoint_pair(self.h, ctypes.byref(job), _p(g, _dp), _p(dL_dmu, _dp), ctypes.byref(st)))
+        check(lib().gain_adjoint_pair_prec(self.h, ctypes.byref(job), _p(g, _dp), _p(dL_dmu, _dp), prec,
+                                           ctypes.byref(st)))
+        self.last_adjoint_stats = st
         self._shape = (len(lo), len(up))
         return dL_dmu
 

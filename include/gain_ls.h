@@ -235,6 +235,18 @@ typedef struct gain_stats {
 gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const double* dL_dS,
                               double* dL_dmu, gain_stats* stats);
 
+/* Arithmetic of the adjoint chain. */
+typedef enum {
+    GAIN_ADJOINT_FP64 = 0,   /* every product and sum in FP64 (gain_adjoint_pair) */
+    GAIN_ADJOINT_FP32 = 1    /* G, dL/dH, dL/dh, the lower vectors and the dL/dmu sums in FP32; the
+                                FP64 amplitudes, eigenvectors and expansion tables are rounded to
+                                FP32 as they are read; dL_dmu is still accumulated in double */
+} gain_adjoint_precision;
+
+/* gain_adjoint_pair in the given precision. */
+gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, const double* dL_dS,
+                                   double* dL_dmu, gain_adjoint_precision prec, gain_stats* stats);
+
 /* Compute amplitudes amp[l][u] = <upper u | mu . rot | lower l> for one block pair into an
  * engine-owned device matrix (row-major; its pointer and leading dimension come from
  * gain_pair_amp_device).  Blocks on completion.  opts may be NULL (defaults).  stats may be

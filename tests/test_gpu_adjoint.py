@@ -75,3 +75,56 @@ def test_adjoint_reuses_the_last_run_of_the_same_job(built_lib):
     eng.upload_dipole((2.0 * p.dipole).reshape(-1), nv, 0, nv, nv)
     g2 = eng.adjoint(0, 0, 1, 1, lo, up, w, np.zeros(p.dipole.size))
     assert np.max(np.abs(g2 - 2.0 * g_plain)) <= 1e-12 * np.abs(g2).max()   # S = amp^2: dS/dmu doubles
+
+
+@pytest.mark.parametrize("rule", ["c4", "c4r"])
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-11), ("f32", 2e-5)])
+def test_adjoint_exact_directions_several_tiles(built_lib, rule, precision, tol):
+    """Blocks of several 64-function tiles per side, so the (F, I) tile list skips the tiles
+    outside |K_I - K_F| <= 1 (K-block form) and keeps all of them (rotational-symmetry form).
+    amp is linear in mu, so dPhi/dmu . d = sum w 2 amp(mu) amp(d) exactly, amp(d) being the
+    FP64 forward of the dipole d.  FP32: the chain's products and sums round to FP32 (unit
+    2^-24) over sums of a few hundred terms; tol is relative to sum |w 2 amp amp(d)|."""
+    import gainls
+    import synth
+    p = synth.make_problem(64, [4, 5], rule, blocks=[(4, 0), (5, 1)])
+    nv = p.dipole.shape[-1]
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    lo = list(range(p.blocks[(0, 0)].vecs.shape[0]))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+    assert min(len(lo), len(up)) > 128
+    rng = np.random.default_rng(91)
+    w = rng.standard_normal((len(lo), len(up)))
+    grad = eng.adjoint(0, 0, 1, 1, lo, up, w, np.zeros(p.dipole.size), precision=precision).reshape(p.dipole.shape)
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+    amp0 = eng.fetch_amp().copy()
+    for _ in range(3):
+        d = rng.standard_normal(p.dipole.shape)
+        eng.upload_dipole(np.ascontiguousarray(d).reshape(-1), nv, 0, nv, nv)
+        eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_PLAIN_FP64)
+        terms = w * 2.0 * amp0 * eng.fetch_amp()
+        assert abs(np.sum(grad * d) - terms.sum()) <= tol * np.abs(terms).sum()
+    # FP32 against FP64 entry by entry
+    if precision == "f32":
+        eng.upload_dipole(np.ascontiguousarray(p.dipole).reshape(-1), nv, 0, nv, nv)
+        g64 = eng.adjoint(0, 0, 1, 1, lo, up, w, np.zeros(p.dipole.size)).reshape(p.dipole.shape)
+        assert np.max(np.abs(grad - g64)) <= tol * np.abs(g64).max()
+        assert np.array_equal(grad == 0, g64 == 0)
+
+
+def test_adjoint_rejects_unknown_precision(built_lib):
+    import ctypes
+    import gainls
+    import synth
+    p = synth.make_problem(16, [2, 3], "c4", blocks=[(2, 0), (3, 1)])
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    lo, up = np.arange(4, dtype=np.int32), np.arange(4, dtype=np.int32)
+    job = gainls.PairJob(0, 0, 1, 1, 4, lo.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), 4,
+                         up.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    g, out = np.zeros(16), np.zeros(p.dipole.size)
+    st = gainls.Stats()
+    rc = gainls.lib().gain_adjoint_pair_prec(eng.h, ctypes.byref(job), g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 7, ctypes.byref(st))
+    assert rc == gainls.ERR_INVALID_ARG
