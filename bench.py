@@ -462,6 +462,15 @@ def adjoint_check(args):
         chain_ms["f32"] += eng.last_adjoint_stats.device_ms
     times["adjoint_fp32_s"] = time.perf_counter() - t1
     fp32_vs_fp64 = float(np.max(np.abs(grad32 - grad.reshape(-1))) / np.abs(grad).max())
+    # algorithmic flops of the chain's two products: dL/dH = G U (2 B N_upper Ntot_F) and
+    # dM = dh^T v over the (F, I) with |K_I - K_F| <= 1 (2 B per pair)
+    chain_flops = 0.0
+    for jI, gI, jF, gF, lo, up in pairs:
+        B, Nu, NtF = len(lo), len(up), int(p.infl[jF].Ntot[gF])
+        kI = np.bincount(p.bases[jI].K, minlength=7)[:7].astype(np.float64)
+        kF = np.bincount(p.bases[jF].K, minlength=7)[:7].astype(np.float64)
+        band = sum(kF[a] * kI[b] for a in range(7) for b in range(7) if abs(a - b) <= 1)
+        chain_flops += 2.0 * B * Nu * NtF + 2.0 * B * band
     # the same gradient from the split path's amplitudes: per pair the tensor-core forward,
     # dL/dS on the device, then the adjoint (which takes the run's amplitudes)
     grad_split = np.zeros(mu0.size)
@@ -518,7 +527,8 @@ def adjoint_check(args):
            "split_forward_gradient_max_err_over_max_grad": split_vs_fp64,
            "fp32_gradient_max_err_over_max_grad": fp32_vs_fp64,
            "fp32_fd_median_rel_err": float(np.median(rel32)), "fp32_fd_p99_rel_err": float(np.quantile(rel32, 0.99)),
-           "adjoint_chain_device_ms": chain_ms,
+           "adjoint_chain_device_ms": chain_ms, "adjoint_chain_flops": chain_flops,
+           "adjoint_chain_tflops": {k: chain_flops / (v * 1e-3) / 1e12 for k, v in chain_ms.items()},
            "nonzero_gradient_entries": int(cand.size), "gradient_entries": int(mu0.size),
            "setup_s": setup_s}
     out.update(times)
