@@ -106,7 +106,7 @@ struct Basis {
     DevArray<int> dK, dtau, dvib, dkblock, dlev;
 };
 
-// Per symmetry of one J: derived structures of the expansion (ideg 0).
+// Per symmetry and degenerate component of one J: derived structures of the expansion.
 struct GammaMaps {
     bool built = false;
     std::vector<int> support;        // primitive functions the expansion touches, ascending
@@ -197,7 +197,7 @@ struct StatsDev {
 // Split-path layout of one block pair (lower layout padded per K block to BK, upper layout
 // padded per K block to BN so that no output tile straddles two upper K blocks).
 struct PairLayout {
-    int key[4] = {-1, -1, -1, -1};
+    int key[6] = {-1, -1, -1, -1, -1, -1};   // pair and components
     long dip_version = -1, wig_version = -1;
     int nI = 0, kpadI = 0, nF = 0, fpad = 0, W = 0;
     bool rotsym = false;
@@ -238,7 +238,7 @@ size_t layout_bytes(const PairLayout& L) {
 
 // Plain-path structures of one block pair.
 struct PlainLayout {
-    int key[4] = {-1, -1, -1, -1};
+    int key[6] = {-1, -1, -1, -1, -1, -1};   // pair and components
     std::vector<HlsCta> ctas;
     DevArray<HlsCta> d_ctas;
     DevArray<int> d_flist;
@@ -281,7 +281,11 @@ struct gain_engine_s {
     int amp_rows = 0, amp_cols = 0;
     long amp_ld = 0;
     bool have_amp = false;
-    std::vector<int> amp_job;   // jindI, gammaI, jindF, gammaF, lower levels, upper levels of amp
+    std::vector<int> amp_job;   // job_key of amp: the pair, its level lists and components
+    // degenerate component slots of one job (gain_run_pair_component): [maxdeg^2][rows * cols]
+    gain::DevArray<double> deg_amp;
+    std::vector<int> deg_job;   // job_key (components 0, 0) of the slots
+    unsigned deg_filled = 0;    // bit idegI + idegF * maxdeg per filled slot
     long launches = 0;          // kernels this engine has launched (split path and band builds)
     void* readback = nullptr;   // page-locked area of a run's counter readbacks
 
@@ -310,7 +314,7 @@ struct gain_engine_s {
     bool have_text = false;
 
     // split-path layouts (band, its digits, padded index maps) per block pair, kept across runs
-    std::map<std::array<int, 4>, std::unique_ptr<gain::PairLayout>> layouts;
+    std::map<std::array<int, 6>, std::unique_ptr<gain::PairLayout>> layouts;
     gain::PairLayout* cur = nullptr;   // the layout of the current run
     gain::PlainLayout plain;
 };
@@ -326,10 +330,11 @@ gain_status check_engine(gain_engine e) {
     return GAIN_OK;
 }
 
-GammaMaps* gamma_maps(gain_engine e, int jind, int g) {
+// The expansion of component ideg of Gamma g (transform_vector_primitive's ideg).
+GammaMaps* gamma_maps(gain_engine e, int jind, int g, int ideg) {
     Basis& b = e->bases[jind];
     Inflation& inf = e->infl[jind];
-    GammaMaps& m = *inf.maps[g];
+    GammaMaps& m = *inf.maps[(size_t)g * e->maxdeg + ideg];
     if (m.built) return &m;
     const int d = inf.dimen;
     const int Ntot = inf.Ntot[g], sdeg = inf.sdeg[g];
@@ -346,7 +351,7 @@ GammaMaps* gamma_maps(gain_engine e, int jind, int g) {
         const int iterm = inf.ijterms[irow + g * inf.maxcoeff];
         for (int i = 0; i < nel; ++i) {
             const int s = iterm + i;
-            const double coef = inf.repres[g][(size_t)s + (size_t)ib * sdeg * Ntot];
+            const double coef = inf.repres[g][(size_t)s + (size_t)ideg * Ntot + (size_t)ib * sdeg * Ntot];
             rows[s].push_back({r, coef});
         }
     }
@@ -419,17 +424,17 @@ const WignerTab* wigner_of(gain_engine e, int jindI, int jindF) {
     return it == e->wigner.end() ? nullptr : it->second.get();
 }
 
-gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) {
+gain_status run_plain(gain_engine e, const gain_pair_job* j, int dI, int dF, gain_stats* stats) {
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
     Inflation& iI = e->infl[j->jindI];
     Inflation& iF = e->infl[j->jindF];
-    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI);
-    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF);
+    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI, dI);
+    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF, dF);
     if (!mI || !mF) return GAIN_ERR_OOM;
     PlainLayout& L = e->plain;
-    const int key[4] = {j->jindI, j->gammaI, j->jindF, j->gammaF};
-    if (!std::equal(key, key + 4, L.key)) {
+    const int key[6] = {j->jindI, j->gammaI, j->jindF, j->gammaF, dI, dF};
+    if (!std::equal(key, key + 6, L.key)) {
         L.ctas.clear();
         std::vector<int> flist;
         for (int k = 0; k <= bF.J; ++k) {
@@ -444,7 +449,7 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) 
             }
         }
         GAIN_TRY(L.d_ctas.upload(L.ctas));
-        std::copy(key, key + 4, L.key);
+        std::copy(key, key + 6, L.key);
     }
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
@@ -466,7 +471,7 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, gain_stats* stats) 
     int launches = 0;
     for (int l0 = 0; l0 < j->nlower; l0 += G) {
         const int nb = std::min(G, j->nlower - l0);
-        GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
+        GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, dI, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
                                        iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
                                        EI.d.p, EI.nsize, e->d_lower.p + l0, e->primI.p, bI.dimen, nb, st));
         if (const WignerTab* wt = wigner_of(e, j->jindI, j->jindF)) {
@@ -513,14 +518,14 @@ gain_status load_piece(gain_engine e, int p);
 
 // The plain path over dipole pieces: one run per piece, amplitudes summed (each piece
 // contributes the upper functions of its vibrational range, MultiGpuManager.cpp:240-288).
-gain_status run_plain_pieces(gain_engine e, const gain_pair_job* j, gain_stats* stats) {
+gain_status run_plain_pieces(gain_engine e, const gain_pair_job* j, int dI, int dF, gain_stats* stats) {
     const size_t n = (size_t)j->nlower * j->nupper;
     double ms = 0;
     long long launches = 0;
     for (int p = 0; p < (int)e->pieces.size(); ++p) {
         GAIN_TRY(load_piece(e, p));
         gain_stats sp;
-        GAIN_TRY(run_plain(e, j, &sp));
+        GAIN_TRY(run_plain(e, j, dI, dF, &sp));
         ms += sp.device_ms;
         launches += sp.kernel_launches + 1;
         if (p == 0) {
@@ -589,9 +594,9 @@ std::vector<split::Prod> make_prods(const SplitParams& p) {
 
 gain_status launch_layout_band(gain_engine e, const gain_pair_job* j);
 
-gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, GammaMaps* mF) {
-    const int key[4] = {j->jindI, j->gammaI, j->jindF, j->gammaF};
-    const std::array<int, 4> akey = {key[0], key[1], key[2], key[3]};
+gain_status build_layout(gain_engine e, const gain_pair_job* j, int dI, int dF, GammaMaps* mI, GammaMaps* mF) {
+    const int key[6] = {j->jindI, j->gammaI, j->jindF, j->gammaF, dI, dF};
+    const std::array<int, 6> akey = {key[0], key[1], key[2], key[3], key[4], key[5]};
     auto it = e->layouts.find(akey);
     if (it == e->layouts.end()) {
         // bound the cache: band and band digits of every cached pair below a quarter of the
@@ -609,7 +614,7 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     PairLayout& L = *e->cur;
     const WignerTab* wt = wigner_of(e, j->jindI, j->jindF);
     const long wv = wt ? wt->version : 0;
-    if (std::equal(key, key + 4, L.key) && L.dip_version == e->dip_version && L.wig_version == wv) return GAIN_OK;
+    if (std::equal(key, key + 6, L.key) && L.dip_version == e->dip_version && L.wig_version == wv) return GAIN_OK;
     L.rotsym = wt != nullptr;
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
@@ -793,7 +798,7 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, GammaMaps* mI, G
     L.beta1 = 0;
     L.s1 = 0;
     L.c1 = 0;
-    std::copy(key, key + 4, L.key);
+    std::copy(key, key + 6, L.key);
     L.dip_version = e->dip_version;
     L.wig_version = wv;
     return GAIN_OK;
@@ -908,11 +913,11 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     return GAIN_OK;
 }
 
-gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_opts* opts, gain_stats* stats) {
-    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI);
-    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF);
+gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, const gain_split_opts* opts,
+                      gain_stats* stats) {
+    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI, dI);
+    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF, dF);
     if (!mI || !mF) return GAIN_ERR_OOM;
-    if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "split path handles non-degenerate symmetries only");
     const double tol = (opts && opts->tol > 0) ? opts->tol : 4.5e-9;
     cudaStream_t st = e->st;
     const long launches0 = e->launches;
@@ -921,7 +926,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
     // GEMM of every piece, the second GEMM runs once
     const int npieces = e->pieces.size() > 1 ? (int)e->pieces.size() : 1;
     if (npieces > 1) GAIN_TRY(load_piece(e, 0));
-    GAIN_TRY(build_layout(e, j, mI, mF));
+    GAIN_TRY(build_layout(e, j, dI, dF, mI, mF));
     PairLayout& L = *e->cur;
     const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
@@ -1074,7 +1079,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
         }
         for (int b0 = 0; b0 < B; b0 += 65535) {
             const int nb = std::min(65535, B - b0);
-            GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
+            GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, dI, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
                                            iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
                                            EI.d.p, EI.nsize, e->d_lower.p + b0, e->primI.p + (size_t)b0 * bIs.dimen,
                                            bIs.dimen, nb, st));
@@ -1376,11 +1381,19 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, const gain_split_op
 }
 
 // The identity of a block-pair job (its blocks and level lists).
-std::vector<int> job_key(const gain_pair_job* j) {
-    std::vector<int> k = {j->jindI, j->gammaI, j->jindF, j->gammaF, j->nlower, j->nupper};
+// A job and the degenerate components its amplitudes belong to.
+std::vector<int> job_key(const gain_pair_job* j, int dI = 0, int dF = 0) {
+    std::vector<int> k = {j->jindI, j->gammaI, j->jindF, j->gammaF, j->nlower, j->nupper, dI, dF};
     k.insert(k.end(), j->lower_levels, j->lower_levels + j->nlower);
     k.insert(k.end(), j->upper_levels, j->upper_levels + j->nupper);
     return k;
+}
+
+// Inputs changed: the stored amplitudes (adjoint reuse, component slots) no longer apply.
+void clear_amp_jobs(gain_engine e) {
+    e->amp_job.clear();
+    e->deg_job.clear();
+    e->deg_filled = 0;
 }
 
 // Output.cpp constants (ACOEF, CMCOEF, the radiation constant of beta) and the INTENSITY
@@ -1398,7 +1411,45 @@ LineParams line_params(const gain_line_params* prm, int jI, int jF, bool with_in
     p.freq_lo = prm->freq_lo;
     p.freq_hi = prm->freq_hi;
     p.with_intensity = with_intensity;
+    p.nslot = 0;
+    p.ndegI = 1;
+    p.reduced_deg = 0;
+    p.slot_stride = 0;
+    for (int i = 0; i < kMaxDegSlots; ++i) p.slot[i] = 0;
     return p;
+}
+
+// The amplitudes the line assembly reads for prm's degeneracies: the last run (ndegI = ndegF
+// = 1), or the component slots gain_run_pair_component filled for the last run's job, in
+// Output.cpp's order (idegF outer, idegI inner).
+gain_status line_source(gain_engine e, const gain_line_params* prm, LineParams& p, const double** amp, long* ld) {
+    if (prm->ndegI < 1 || prm->ndegF < 1 || prm->ndegI > e->maxdeg || prm->ndegF > e->maxdeg)
+        return set_error(GAIN_ERR_INVALID_ARG, "degeneracies (%d, %d) outside 1..%d", prm->ndegI, prm->ndegF,
+                         e->maxdeg);
+    if (prm->ndegI == 1 && prm->ndegF == 1) {
+        *amp = e->amp.p;
+        *ld = e->amp_ld;
+        return GAIN_OK;
+    }
+    const bool same = e->amp_job.size() >= 8 && e->deg_job.size() == e->amp_job.size() &&
+                      std::equal(e->amp_job.begin(), e->amp_job.begin() + 6, e->deg_job.begin()) &&
+                      std::equal(e->amp_job.begin() + 8, e->amp_job.end(), e->deg_job.begin() + 8);
+    if (!same || !e->deg_filled)
+        return set_error(GAIN_ERR_NOT_READY, "degenerate lines: run the component pairs of this job first "
+                                             "(gain_run_pair_component / gain_run_pair_degenerate)");
+    const int md = e->maxdeg;
+    for (int dF = 0; dF < prm->ndegF; ++dF)
+        for (int dI = 0; dI < prm->ndegI; ++dI) {
+            const int slot = dI + dF * md;
+            if (e->deg_filled & (1u << slot)) p.slot[p.nslot++] = slot;
+        }
+    if (!p.nslot) return set_error(GAIN_ERR_NOT_READY, "no component slot inside the degeneracies");
+    p.ndegI = prm->ndegI;
+    p.reduced_deg = prm->reduced && prm->ndegI != 1 && prm->ndegF != 1;
+    p.slot_stride = (long)e->amp_rows * e->amp_cols;
+    *amp = e->deg_amp.p;
+    *ld = e->amp_cols;
+    return GAIN_OK;
 }
 
 }  // namespace
@@ -1543,7 +1594,7 @@ gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const i
                               const int* vib, const int* kblock_size, const int* kstart) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (jind < 0 || jind > 1000 || J < 0 || J > e->jmax || dimen <= 0 || !K || !tau || !vib || !kblock_size || !kstart)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_basis: bad argument");
     // K-sorted, K-blocks consistent with the per-function K (TroveBasisSet.cpp:659-681)
@@ -1591,7 +1642,7 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
                                   const int* Ntot, const int* sdeg) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (jind < 0 || jind >= (int)e->bases.size() || !e->bases[jind].present)
         return set_error(GAIN_ERR_NOT_READY, "upload the basis of jind %d first", jind);
     if (dimen != e->bases[jind].dimen || maxcoeff <= 0 || matsize <= 0 || !icontr || !ijterms || !N || !repres ||
@@ -1616,6 +1667,9 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
     for (int g = 0; g < e->nsym; ++g) {
         if (Ntot[g] < 0 || sdeg[g] <= 0 || !N[g] || (Ntot[g] > 0 && !repres[g]))
             return set_error(GAIN_ERR_INVALID_ARG, "bad expansion table of Gamma %d", g);
+        if (sdeg[g] > e->maxdeg)
+            return set_error(GAIN_ERR_INVALID_ARG, "Gamma %d: degeneracy %d above the engine's maxdeg %d", g, sdeg[g],
+                             e->maxdeg);
         inf.N.emplace_back(N[g], N[g] + maxcoeff);
         const size_t nrep = (size_t)Ntot[g] * sdeg[g] * matsize;
         inf.repres.emplace_back(repres[g], repres[g] + nrep);
@@ -1629,7 +1683,7 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
         inf.drepres.emplace_back(new DevArray<double>());
         GAIN_TRY(inf.dN.back()->upload(inf.N.back()));
         GAIN_TRY(inf.drepres.back()->upload(inf.repres.back()));
-        inf.maps.emplace_back(new GammaMaps());
+        for (int d = 0; d < e->maxdeg; ++d) inf.maps.emplace_back(new GammaMaps());   // [g * maxdeg + ideg]
     }
     GAIN_TRY(inf.dicontr.upload(inf.icontr));
     GAIN_TRY(inf.dijterms.upload(inf.ijterms));
@@ -1643,7 +1697,7 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
 gain_status gain_upload_dipole(gain_engine e, const double* piece, int N, int startF, int endF, int ncontrF) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (!piece || N <= 0 || startF < 0 || endF > N || endF - startF != ncontrF || ncontrF <= 0)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_dipole: bad block (N=%d, [%d,%d), ncontrF=%d)", N, startF,
                          endF, ncontrF);
@@ -1667,7 +1721,7 @@ gain_status gain_upload_dipole_pieces(gain_engine e, int npieces, const double* 
                                       const int* startF, const int* endF) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (npieces <= 0 || !pieces || !startF || !endF || N <= 0)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_dipole_pieces: bad argument");
     for (int p = 0; p < npieces; ++p)
@@ -1694,7 +1748,7 @@ gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI
                                const double* rot) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (jindI < 0 || jindF < 0 || jindI >= (int)e->bases.size() || jindF >= (int)e->bases.size() || nlevelsI <= 0 ||
         nlevelsF <= 0 || maxdeg <= 0 || !rot)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_wigner: bad argument");
@@ -1724,7 +1778,7 @@ gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI
 gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize, const double* vecs) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (jind < 0 || gamma < 0 || gamma >= e->nsym || nlevels <= 0 || nsize <= 0 || !vecs)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs: bad argument");
     auto& slot = e->eig[{jind, gamma}];
@@ -1744,7 +1798,7 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
                                       const double* vecs) {
     clear_error();
     GAIN_TRY(check_engine(e));
-    e->amp_job.clear();   // inputs changed: no adjoint reuse of earlier amplitudes
+    clear_amp_jobs(e);   // inputs changed: no reuse of earlier amplitudes
     if (jind < 0 || gamma < 0 || gamma >= e->nsym || nlevels <= 0 || nsize <= 0 || !vecs)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_upload_eigvecs_async: bad argument");
     cudaPointerAttributes pa{};
@@ -1798,13 +1852,14 @@ gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, cons
     if (!dL_dS || !dL_dmu) return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair: NULL argument");
     if (e && e->pieces.size() > 1)
         return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: upload the dipole as one piece");
-    if (e->maxdeg != 1) return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: non-degenerate symmetries only");
+    if (e->infl[job->jindI].sdeg[job->gammaI] != 1 || e->infl[job->jindF].sdeg[job->gammaF] != 1)
+        return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: non-degenerate symmetries only");
     // forward amplitudes: those of the last run when it computed this job (either path),
     // else the plain FP64 path (the reference's method)
     if (!(e->have_amp && e->amp_job == job_key(job))) {
         e->have_amp = false;
         e->amp_job.clear();
-        GAIN_TRY(run_plain(e, job, nullptr));
+        GAIN_TRY(run_plain(e, job, 0, 0, nullptr));
         e->amp_job = job_key(job);
     }
     const Basis& bI = e->bases[job->jindI];
@@ -1941,21 +1996,91 @@ gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, cons
     return GAIN_OK;
 }
 
-gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path path, const gain_split_opts* opts,
-                          gain_stats* stats) {
-    clear_error();
+namespace {
+gain_status run_component(gain_engine e, const gain_pair_job* job, int dI, int dF, gain_path path,
+                          const gain_split_opts* opts, gain_stats* stats) {
     GAIN_TRY(check_engine(e));
     GAIN_TRY(validate_job(e, job));
+    const int sI = e->infl[job->jindI].sdeg[job->gammaI], sF = e->infl[job->jindF].sdeg[job->gammaF];
+    if (dI < 0 || dI >= sI || dF < 0 || dF >= sF)
+        return set_error(GAIN_ERR_INVALID_ARG, "components (%d, %d) outside the degeneracies (%d, %d)", dI, dF, sI, sF);
     e->have_amp = false;
     gain_status r;
     if (path == GAIN_PATH_PLAIN_FP64)
-        r = e->pieces.size() > 1 ? run_plain_pieces(e, job, stats) : run_plain(e, job, stats);
+        r = e->pieces.size() > 1 ? run_plain_pieces(e, job, dI, dF, stats) : run_plain(e, job, dI, dF, stats);
     else if (path == GAIN_PATH_SPLIT)
-        r = run_split(e, job, opts, stats);
+        r = run_split(e, job, dI, dF, opts, stats);
     else
         return set_error(GAIN_ERR_INVALID_ARG, "unknown path %d", (int)path);
-    e->amp_job = r == GAIN_OK ? job_key(job) : std::vector<int>();
+    e->amp_job = r == GAIN_OK ? job_key(job, dI, dF) : std::vector<int>();
     return r;
+}
+}  // namespace
+
+gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path path, const gain_split_opts* opts,
+                          gain_stats* stats) {
+    clear_error();
+    return run_component(e, job, 0, 0, path, opts, stats);
+}
+
+gain_status gain_run_pair_component(gain_engine e, const gain_pair_job* job, int idegI, int idegF, gain_path path,
+                                    const gain_split_opts* opts, gain_stats* stats) {
+    clear_error();
+    GAIN_TRY(run_component(e, job, idegI, idegF, path, opts, stats));
+    // keep the amplitudes in the job's component slot (compact rows x cols)
+    const std::vector<int> key = job_key(job);
+    const size_t n = (size_t)job->nlower * job->nupper;
+    const int md = e->maxdeg;
+    if (e->deg_job != key) {
+        e->deg_job.clear();
+        e->deg_filled = 0;
+        GAIN_TRY(e->deg_amp.alloc((size_t)md * md * n));
+        e->deg_job = key;
+    }
+    const int slot = idegI + idegF * md;
+    GAIN_CUDA(cudaMemcpy2DAsync(e->deg_amp.p + (size_t)slot * n, sizeof(double) * job->nupper, e->amp.p,
+                                sizeof(double) * e->amp_ld, sizeof(double) * job->nupper, job->nlower,
+                                cudaMemcpyDeviceToDevice, e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    e->deg_filled |= 1u << slot;
+    return GAIN_OK;
+}
+
+gain_status gain_run_pair_degenerate(gain_engine e, const gain_pair_job* job, const gain_filters* f,
+                                     gain_path path, const gain_split_opts* opts, gain_stats* stats) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    GAIN_TRY(validate_job(e, job));
+    if (!f || !f->sym_degen || f->nsym != e->nsym)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_run_pair_degenerate: filters of %d symmetries needed", e->nsym);
+    const int nI = f->sym_degen[job->gammaI], nF = f->sym_degen[job->gammaF];
+    if (nI != e->infl[job->jindI].sdeg[job->gammaI] || nF != e->infl[job->jindF].sdeg[job->gammaF])
+        return set_error(GAIN_ERR_INVALID_ARG, "sym_degen differs from the expansion tables' degeneracies");
+    gain_stats sum;
+    memset(&sum, 0, sizeof sum);
+    int runs = 0;
+    for (int dF = 0; dF < nF; ++dF)      // Output.cpp:78-79 order: idegF outer, idegI inner
+        for (int dI = 0; dI < nI; ++dI) {
+            if (!gain_degeneracy_filter(f, job->gammaI, job->gammaF, dI, dF)) continue;
+            gain_stats one;
+            GAIN_TRY(gain_run_pair_component(e, job, dI, dF, path, opts, &one));
+            sum.device_ms += one.device_ms;
+            sum.refined += one.refined;
+            sum.uncertified += one.uncertified;
+            sum.uncertified_weak += one.uncertified_weak;
+            sum.inexact += one.inexact;
+            sum.amp_max = std::max(sum.amp_max, one.amp_max);
+            sum.kernel_launches += one.kernel_launches;
+            sum.gemm1_ms += one.gemm1_ms;
+            sum.gemm2_ms += one.gemm2_ms;
+            sum.tensor_flops += one.tensor_flops;
+            sum.rows = one.rows;
+            sum.cols = one.cols;
+            ++runs;
+        }
+    if (!runs) return set_error(GAIN_ERR_INVALID_ARG, "no component pair passes the degeneracy filter");
+    if (stats) *stats = sum;
+    return GAIN_OK;
 }
 
 gain_status gain_selftest_bounded_wait(gain_engine e, double limit_ms) {
@@ -2002,10 +2127,12 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     if (!prm || !energiesI || !energiesF || jI < 0 || jF < 0)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines: bad argument");
     if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
-    if (prm->ndegI != 1 || prm->ndegF != 1)
-        return set_error(GAIN_ERR_UNSUPPORTED, "line assembly handles non-degenerate symmetries only");
     if (prm->temperature <= 0 || prm->q_part <= 0)
         return set_error(GAIN_ERR_INVALID_ARG, "temperature and partition function must be positive");
+    LineParams p = line_params(prm, jI, jF, I != nullptr);
+    const double* amp = nullptr;
+    long ld = 0;
+    GAIN_TRY(line_source(e, prm, p, &amp, &ld));
     const int rows = e->amp_rows, cols = e->amp_cols;
     const size_t n = (size_t)rows * cols;
     cudaStream_t st = e->st;
@@ -2017,9 +2144,8 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     if (keep) GAIN_TRY(e->lineKeep.alloc(n));
     GAIN_TRY(e->ull.alloc(4));
     GAIN_TRY(e->ull.zero(st, 4));
-    const LineParams p = line_params(prm, jI, jF, I != nullptr);
     // only the requested outputs are written
-    GAIN_CUDA(launch_lines(rows, cols, e->amp.p, e->amp_ld, e->eIdev.p, e->eFdev.p, p, S ? e->lineS.p : nullptr,
+    GAIN_CUDA(launch_lines(rows, cols, amp, ld, e->eIdev.p, e->eFdev.p, p, S ? e->lineS.p : nullptr,
                            A ? e->lineA.p : nullptr, I ? e->lineI.p : nullptr, keep ? e->lineKeep.p : nullptr,
                            e->ull.p + 1, st));
     unsigned long long nk = 0;
@@ -2045,10 +2171,12 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
         (flags & ~(GAIN_TEXT_INTENSITY | GAIN_TEXT_AMPLITUDES)))
         return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines_text: bad argument");
     if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
-    if (prm->ndegI != 1 || prm->ndegF != 1)
-        return set_error(GAIN_ERR_UNSUPPORTED, "line assembly handles non-degenerate symmetries only");
     if (prm->temperature <= 0 || prm->q_part <= 0)
         return set_error(GAIN_ERR_INVALID_ARG, "temperature and partition function must be positive");
+    LineParams lp = line_params(prm, jI, jF, (flags & GAIN_TEXT_INTENSITY) != 0);
+    const double* amp = nullptr;
+    long ld = 0;
+    GAIN_TRY(line_source(e, prm, lp, &amp, &ld));
     e->have_text = false;
     const int rows = e->amp_rows, cols = e->amp_cols;
     const size_t n = (size_t)rows * cols;
@@ -2062,11 +2190,11 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
     TextArgs t;
     t.rows = rows;
     t.cols = cols;
-    t.amp = e->amp.p;
-    t.ld = e->amp_ld;
+    t.amp = amp;
+    t.ld = ld;
     t.eI = e->eIdev.p;
     t.eF = e->eFdev.p;
-    t.p = line_params(prm, jI, jF, (flags & GAIN_TEXT_INTENSITY) != 0);
+    t.p = lp;
     t.levI = e->d_lower.p;
     t.levF = e->d_upper.p;
     t.jI = jI;

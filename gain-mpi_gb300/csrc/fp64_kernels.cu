@@ -330,7 +330,7 @@ __global__ void k_lines(int rows, int cols, const double* __restrict__ amp, long
     int k = 0;
     if (idx < total) {
         const int r = (int)(idx / cols), c = (int)(idx - (long)r * cols);
-        const LineVals v = line_eval(amp[(long)r * ld + c], eI[r], eF[c], p);
+        const LineVals v = line_eval(amp, (long)r * ld + c, eI[r], eF[c], p);
         k = v.keep;
         if (S) S[idx] = v.ls;
         if (A) A[idx] = v.A;

@@ -129,12 +129,20 @@ cudaError_t launch_contract_rowerr(int rows, const double* Hp, long ldp, int nco
 // acc[i] += x[i], i < n
 cudaError_t launch_add(double* acc, const double* x, long n, cudaStream_t st);
 
-// S, A, I of a [rows x cols] amplitude block (ndeg = 1), Output.cpp:52-112
+// S, A, I of a [rows x cols] amplitude block, Output.cpp:52-112
+constexpr int kMaxDegSlots = 9;   // degenerate component pairs of one line (maxdeg <= 3)
 struct LineParams {
     double acoef_2jI1;   // ACOEF * (2 jI + 1), the first product of Output.cpp:93
     double cmcoef, gnsF, two_jF1;
     double beta, zpe, q_part, thresh, freq_lo, freq_hi;
     int with_intensity;
+    // Degenerate states (Output.cpp:78-91): nslot > 0 sums amp^2 over the listed component
+    // slots (idegF outer, idegI inner, those passing DegeneracyFilter), divides by ndegI and,
+    // with reduced_deg (SYMMETRY REDUCED and both states degenerate), multiplies by ndegI.
+    // nslot = 0: one amplitude per line, S = amp^2.
+    int nslot, ndegI, reduced_deg;
+    long slot_stride;              // doubles from one slot to the next
+    int slot[kMaxDegSlots];
 };
 cudaError_t launch_lines(int rows, int cols, const double* amp, long ld, const double* eI,
                          const double* eF, LineParams p, double* S, double* A, double* I,

@@ -1,4 +1,4 @@
-// S, A and I of one non-degenerate line (BaseClasses/Output.cpp:52-112), shared by the line
+// S, A and I of one line (BaseClasses/Output.cpp:52-112), shared by the line
 // assembly (k_lines) and the line-list text kernels so both see the same doubles.
 #pragma once
 #include "gain_internal.h"
@@ -10,10 +10,27 @@ struct LineVals {
     int keep;   // the reference writes the line: nu in FREQ-WINDOW, nu >= 1e-40, A >= THRESH_LINE
 };
 
-__device__ __forceinline__ LineVals line_eval(double a, double eIr, double eFc, const LineParams& p) {
+// The line strength of the line at amp[off] (and its component slots).
+__device__ __forceinline__ double line_ls(const double* amp, long off, const LineParams& p) {
+    if (p.nslot == 0) {
+        const double a = amp[off];
+        return __dmul_rn(a, a);                               // :83, ndegI = ndegF = 1
+    }
+    double ls = 0.0;
+    for (int s = 0; s < p.nslot; ++s) {                       // :78-85
+        const double a = amp[off + (long)p.slot[s] * p.slot_stride];
+        ls = __dadd_rn(ls, __dmul_rn(a, a));
+    }
+    ls = __ddiv_rn(ls, (double)p.ndegI);                      // :89
+    if (p.reduced_deg) ls = __dmul_rn(ls, (double)p.ndegI);   // :90-91
+    return ls;
+}
+
+__device__ __forceinline__ LineVals line_eval(const double* amp, long off, double eIr, double eFc,
+                                              const LineParams& p) {
     LineVals v;
     v.nu = eFc - eIr;
-    v.ls = __dmul_rn(a, a);                                   // :83, ndegI = ndegF = 1
+    v.ls = line_ls(amp, off, p);
     const double anu = fabs(v.nu);
     v.A = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, v.ls), anu), anu), anu);   // :93
     v.keep = (v.nu >= p.freq_lo && v.nu <= p.freq_hi && v.nu >= 1e-40 && v.A >= p.thresh) ? 1 : 0;

@@ -24,13 +24,20 @@ namespace {
 constexpr int kTextThreads = 256, kTextItems = 4, kTextSpan = kTextThreads * kTextItems;
 constexpr int kStageMax = 200 * 1024;   // shared-memory staging of one block's text
 
-// The fields of line idx; false when the line is not written.
+// The fields of line idx; false when the line is not written.  a_out receives the printed
+// amplitudes (kMaxDegSlots at most).
 __device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double* a_out, fmt::LineFields& f) {
     const int r = (int)(idx / t.cols), c = (int)(idx - (long)r * t.cols);
-    const double a = t.amp[(long)r * t.ld + c];
-    *a_out = a;
-    const LineVals v = line_eval(a, t.eI[r], t.eF[c], t.p);
+    const long off = (long)r * t.ld + c;
+    const LineVals v = line_eval(t.amp, off, t.eI[r], t.eF[c], t.p);
     if (!v.keep) return false;
+    int namp = 1;
+    if (t.p.nslot == 0) {
+        a_out[0] = t.amp[off];
+    } else {
+        namp = t.p.nslot;
+        for (int s = 0; s < namp; ++s) a_out[s] = t.amp[off + (long)t.p.slot[s] * t.p.slot_stride];
+    }
     f.nu = v.nu;
     f.A = v.A;
     f.intensity = v.I;
@@ -42,23 +49,23 @@ __device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double*
     f.gammaI = t.gammaI;
     f.with_intensity = t.p.with_intensity;
     f.amps = t.with_amps ? a_out : nullptr;
-    f.namp = 1;
+    f.namp = namp;
     return true;
 }
 
 __device__ __forceinline__ long line_text(const TextArgs& t, long idx, fmt::Sink& s) {
-    double a;
+    double a[kMaxDegSlots];
     fmt::LineFields f;
-    if (!line_fields(t, idx, &a, f)) return 0;
+    if (!line_fields(t, idx, a, f)) return 0;
     const long n0 = s.n;
     fmt::put_line(s, f);
     return s.n - n0;
 }
 
 __device__ __forceinline__ long line_length(const TextArgs& t, long idx) {
-    double a;
+    double a[kMaxDegSlots];
     fmt::LineFields f;
-    if (!line_fields(t, idx, &a, f)) return 0;
+    if (!line_fields(t, idx, a, f)) return 0;
     return fmt::line_len(f);
 }
 

@@ -193,6 +193,10 @@ def _declare(L):
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
     L.gain_adjoint_pair.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.POINTER(Stats)]
     L.gain_adjoint_pair_prec.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.c_int, ctypes.POINTER(Stats)]
+    L.gain_run_pair_component.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
+    L.gain_run_pair_degenerate.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.POINTER(Filters), ctypes.c_int,
+                                           ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
     L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
@@ -249,7 +253,7 @@ def _declare(L):
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair",
-                 "gain_adjoint_pair_prec", "gain_run_pair", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_adjoint_pair_prec", "gain_run_pair", "gain_run_pair_component", "gain_run_pair_degenerate", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
                  "gain_lines_text_device",
                  "gain_format_values_device"):
@@ -424,12 +428,22 @@ class Engine:
     def run_pair(self, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
                  upper_levels: Sequence[int], path: int = PATH_SPLIT, tol: float = 0.0,
                  slices: int = 0, beta: int = 0, kchunks: int = 0, s_floor: float = 0.0,
-                 raise_on_error: bool = True) -> dict:
+                 raise_on_error: bool = True, components=None, filters=None) -> dict:
+        """Amplitudes of one block pair.  components=(idegI, idegF): that degenerate component
+        pair, kept in its slot (gain_run_pair_component); filters: every component pair
+        passing the degeneracy filter (gain_run_pair_degenerate)."""
         lo, up = _i32(lower_levels), _i32(upper_levels)
         job = PairJob(jindI, gammaI, jindF, gammaF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
         opts = SplitOpts(tol, slices, beta, kchunks, s_floor)
         st = Stats()
-        s = lib().gain_run_pair(self.h, ctypes.byref(job), path, ctypes.byref(opts), ctypes.byref(st))
+        if filters is not None:
+            s = lib().gain_run_pair_degenerate(self.h, ctypes.byref(job), ctypes.byref(filters), path,
+                                               ctypes.byref(opts), ctypes.byref(st))
+        elif components is not None:
+            s = lib().gain_run_pair_component(self.h, ctypes.byref(job), int(components[0]), int(components[1]), path,
+                                              ctypes.byref(opts), ctypes.byref(st))
+        else:
+            s = lib().gain_run_pair(self.h, ctypes.byref(job), path, ctypes.byref(opts), ctypes.byref(st))
         self._shape = (len(lo), len(up))
         out = st.as_dict()
         out["status"] = s
@@ -473,12 +487,13 @@ class Engine:
 
     def lines(self, eI, eF, jI, jF, temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0,
               freq=(-1e9, 1e9), gnsF=1.0, intensity=True, want=("S", "A", "I", "keep"),
-              out_S=None, out_A=None):
+              out_S=None, out_A=None, ndeg=(1, 1), reduced=False):
         """S, A (and I, keep) of the last run; out_S / out_A may be preallocated (e.g. pinned)
-        contiguous float64 arrays of nlower*nupper elements."""
+        contiguous float64 arrays of nlower*nupper elements.  ndeg=(ndegI, ndegF) above 1
+        combines the component slots of the last job."""
         eI, eF = _f64(eI), _f64(eF)
         n = self._shape[0] * self._shape[1]
-        prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
+        prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, ndeg[0], ndeg[1], int(reduced))
         S = (out_S.reshape(-1) if out_S is not None else np.empty(n)) if "S" in want else None
         A = (out_A.reshape(-1) if out_A is not None else np.empty(n)) if "A" in want else None
         I = np.empty(n) if (intensity and "I" in want) else None
@@ -497,12 +512,13 @@ class Engine:
 
 
 def _lines_text(self, eI, eF, jI, jF, gammaI, gammaF, temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0,
-                freq=(-1e9, 1e9), gnsF=1.0, intensity=True, amplitudes=False, out=None):
+                freq=(-1e9, 1e9), gnsF=1.0, intensity=True, amplitudes=False, out=None, ndeg=(1, 1),
+                reduced=False):
     """The line-list text of the last run, built on the device (gain_pair_lines_text) and
     copied into out (a uint8 array of at least the text's size, e.g. pinned) or a new bytes
     object.  Returns (text, n_lines)."""
     eI, eF = _f64(eI), _f64(eF)
-    prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
+    prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, ndeg[0], ndeg[1], int(reduced))
     nb, nl = ctypes.c_ulonglong(), ctypes.c_longlong()
     flags = (TEXT_INTENSITY if intensity else 0) | (TEXT_AMPLITUDES if amplitudes else 0)
     check(lib().gain_pair_lines_text(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF, gammaI, gammaF,
@@ -517,12 +533,13 @@ def _lines_text(self, eI, eF, jI, jF, gammaI, gammaF, temperature=296.0, q_part=
 
 
 def _lines_text_host(self, eI, eF, jI, jF, gammaI, gammaF, out, temperature=296.0, q_part=1.0, zpe=0.0,
-                     thresh=0.0, freq=(-1e9, 1e9), gnsF=1.0, intensity=True, amplitudes=False):
+                     thresh=0.0, freq=(-1e9, 1e9), gnsF=1.0, intensity=True, amplitudes=False, ndeg=(1, 1),
+                     reduced=False):
     """gain_pair_lines_text_host: the text formed on the device and copied into out (a uint8
     array, page-locked for the overlap) part by part.  Returns (text view, n_lines)."""
     eI, eF = _f64(eI), _f64(eF)
     assert out.dtype == np.uint8 and out.flags.c_contiguous
-    prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, 1, 1, 0)
+    prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, ndeg[0], ndeg[1], int(reduced))
     nb, nl = ctypes.c_ulonglong(), ctypes.c_longlong()
     flags = (TEXT_INTENSITY if intensity else 0) | (TEXT_AMPLITUDES if amplitudes else 0)
     check(lib().gain_pair_lines_text_host(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF, gammaI,

@@ -112,19 +112,27 @@ def classes_of(basis: Basis, rule: str) -> np.ndarray:
         return (2 * (basis.vib % 2) + ((basis.K + basis.tau) % 2)).astype(np.int32)
     if rule == "c4r":   # rotsym basis: level index in place of K + tau
         return (2 * (basis.vib % 2) + (basis.tau % 2)).astype(np.int32)
-    if rule == "c4m":   # classes belong to mixed functions, not primitives (make_mixed_inflation)
+    if rule in ("c4m", "c3e"):   # classes belong to mixed functions, not primitives
         return np.full(basis.dimen, -1, np.int32)
     raise ValueError(f"unknown symmetry rule {rule!r}")
 
 
 def nsym_of(rule: str) -> int:
-    return {"full": 1, "c4": 4, "c4r": 4, "c4m": 4}[rule]
+    return {"full": 1, "c4": 4, "c4r": 4, "c4m": 4, "c3e": 3}[rule]
+
+
+def degen_of(rule: str) -> np.ndarray:
+    """Degeneracy of each symmetry: rule "c3e" has a doubly degenerate E (A1, A2, E)."""
+    if rule == "c3e":
+        return np.array([1, 1, 2], np.int32)
+    return np.ones(nsym_of(rule), np.int32)
 
 
 def selection_of(rule: str) -> np.ndarray:
     """isym_pairs: classes with equal entries pair up (SELECTION keyword)."""
     return {"full": np.array([1], np.int32), "c4": np.array([1, 1, 2, 2], np.int32),
-            "c4r": np.array([1, 1, 2, 2], np.int32), "c4m": np.array([1, 1, 2, 2], np.int32)}[rule]
+            "c4r": np.array([1, 1, 2, 2], np.int32), "c4m": np.array([1, 1, 2, 2], np.int32),
+            "c3e": np.array([1, 1, 2], np.int32)}[rule]
 
 
 def igamma_pair_of(isym_pairs: np.ndarray) -> np.ndarray:
@@ -176,6 +184,8 @@ def inflation_of(basis: Basis, rule: str, nsym: int) -> "Inflation":
     """The expansion tables of a basis under a symmetry rule."""
     if rule == "c4m":
         return make_mixed_inflation(basis, nsym)
+    if rule == "c3e":
+        return make_degenerate_inflation(basis)
     return make_inflation(basis, classes_of(basis, rule), nsym)
 
 
@@ -233,6 +243,70 @@ def make_mixed_inflation(basis: Basis, nsym: int = 4) -> Inflation:
             rep[s_idx + int(Ntot[g])] = co[1]
         repres.append(rep)
     return Inflation(ncase, icontr, ijterms, Ns, repres, Ntot, np.ones(nsym, np.int32), [None] * nsym, matsize=2)
+
+
+E_PAIRS = ((0.6, 0.8), (MIX_COEF, MIX_COEF))   # (a, b) of the E components, exact in binary64 terms
+
+
+def make_degenerate_inflation(basis: Basis) -> Inflation:
+    """Expansion tables of rule "c3e": symmetries A1, A2 and a doubly degenerate E, built the
+    way a C3v symmetric top's are (K = 3n mixes into A1/A2, other K form E pairs):
+
+    * case (K = 0, v): one component, the primitive; one function of A1 for even v + J, else A2;
+    * case (K >= 1, v), components ib = 0, 1 = the primitives (K, 0, v), (K, 1, v):
+      - K mod 3 == 0: (p0 + p1) / sqrt(2) and (p0 - p1) / sqrt(2) in A1 and A2 (the other way
+        round for odd v);
+      - otherwise one E function whose component 0 is a p0 + b p1 and component 1 is
+        b p0 - a p1, (a, b) = E_PAIRS[(K + v) mod 2].
+
+    repres[s + ideg Ntot + ib sdeg Ntot] (transform_vector_primitive's index,
+    GPU/dipole_GPU.cu:882), sdeg = (1, 1, 2), mat_size = 2; cases in primitive order."""
+    d = basis.dimen
+    J = basis.J
+    icontr = np.zeros(2 * d, np.int32)
+    case_of, cases = {}, []
+    for r in range(d):
+        key = (int(basis.K[r]), int(basis.vib[r]))
+        if key not in case_of:
+            case_of[key] = len(cases)
+            cases.append([])
+        ib = 0 if basis.K[r] == 0 else int(basis.tau[r])
+        cases[case_of[key]].append((ib, r))
+        icontr[r] = case_of[key]
+        icontr[r + d] = ib
+    ncase = len(cases)
+    nsym = 3
+    sdeg = np.array([1, 1, 2], np.int32)
+    funcs = [[] for _ in range(nsym)]   # per class: (case, [per component: coefficients of ib 0, 1])
+    for c, comps in enumerate(cases):
+        K = int(basis.K[comps[0][1]])
+        v = int(basis.vib[comps[0][1]])
+        if K == 0:
+            funcs[(v + J) % 2].append((c, [(1.0, 0.0)]))
+        elif K % 3 == 0:
+            funcs[v % 2].append((c, [(MIX_COEF, MIX_COEF)]))
+            funcs[1 - v % 2].append((c, [(MIX_COEF, -MIX_COEF)]))
+        else:
+            a, b = E_PAIRS[(K + v) % 2]
+            funcs[2].append((c, [(a, b), (b, -a)]))
+    ijterms = np.zeros(ncase * nsym, np.int32)
+    Ns, repres = [], []
+    Ntot = np.zeros(nsym, np.int32)
+    for g in range(nsym):
+        n_g = np.zeros(ncase, np.int32)
+        for c, _ in funcs[g]:
+            n_g[c] += 1
+        ijterms[g * ncase:(g + 1) * ncase] = np.concatenate([[0], np.cumsum(n_g)[:-1]]).astype(np.int32)
+        Ns.append(n_g)
+        Ntot[g] = len(funcs[g])
+        nt, sd = int(Ntot[g]), int(sdeg[g])
+        rep = np.zeros(nt * sd * 2, np.float64)
+        for s_idx, (c, co) in enumerate(funcs[g]):
+            for ideg in range(sd):
+                for ib in range(2):
+                    rep[s_idx + ideg * nt + ib * sd * nt] = co[ideg][ib]
+        repres.append(rep)
+    return Inflation(ncase, icontr, ijterms, Ns, repres, Ntot, sdeg, [None] * nsym, matsize=2)
 
 
 def make_dipole(nv: int, seed: int = DIPOLE_SEED) -> np.ndarray:
@@ -352,7 +426,7 @@ def make_problem(nv: int, jvals, rule: str = "c4", blocks=None, qr_device=None,
         if max_levels is not None and max_levels < n:
             vecs, en = vecs[:max_levels], en[:max_levels]
         blk[(jind, g)] = Block(J, jind, g, np.ascontiguousarray(vecs), en)
-    p = Problem(nv, list(jvals), rule, nsym, np.ones(nsym, np.int32), isym_pairs,
+    p = Problem(nv, list(jvals), rule, nsym, degen_of(rule), isym_pairs,
                 igamma_pair_of(isym_pairs), bases, infl, classes, make_dipole(nv), blk)
     J_, jind_, g_, lev_, e_ = [], [], [], [], []
     for (jind, g), b in sorted(blk.items()):

@@ -268,12 +268,17 @@ typedef struct gain_line_params {
     double thresh;            /* THRESH_LINE */
     double freq_lo, freq_hi;  /* FREQ-WINDOW */
     double gnsF;              /* GNS of the upper Gamma */
-    int ndegI, ndegF;         /* degeneracies (1 in this build's batched path) */
+    int ndegI, ndegF;         /* degeneracies of the pair's states; above 1 the lines combine the
+                                 component slots of gain_run_pair_component (Output.cpp:78-91) */
     int reduced;              /* SYMMETRY REDUCED */
 } gain_line_params;
 
 /* Line strength S, Einstein A and intensity I of every amplitude of the last run
- * (Output::OutputLinestrength, BaseClasses/Output.cpp:52-112), on the device.
+ * (Output::OutputLinestrength, BaseClasses/Output.cpp:52-112), on the device.  With
+ * ndegI = ndegF = 1, S = amp^2 of the last run.  Otherwise S sums amp^2 over the component
+ * slots (idegI < ndegI, idegF < ndegF, idegF outer) that gain_run_pair_component filled for
+ * the last run's job, divides by ndegI and, when reduced and both states are degenerate,
+ * multiplies by ndegI; the text's amplitude list holds those slots' amplitudes in that order.
  * energiesI/F are host arrays of the rows' / columns' energies.  keep[l*nupper+u] = 1 when
  * the reference would write the line (nu inside FREQ-WINDOW, nu >= 1e-40, A >= THRESH_LINE).
  * Host outputs (any may be NULL): S, A, I [nlower*nupper] doubles, keep [nlower*nupper]
@@ -369,6 +374,22 @@ gain_status gain_transition_details(const gain_filters* f, const gain_state* st,
  * 4 n_pairs, 2 n_pairs + 1 and n_levels ints. */
 gain_status gain_plan_pairs(const gain_filters* f, const gain_state* st, int n, int* n_pairs,
                             int* pairs, int* offs, long long* n_levels, int* levels);
+
+/* Degenerate symmetries (sdeg > 1 in the expansion tables).  Amplitudes of component idegI
+ * of the lower states against component idegF of the upper states: the vectors expanded with
+ * transform_vector_primitive's ideg (GPU/dipole_GPU.cu:137-156, 859-889), the reference's
+ * linestrength[idegI + idegF * MaxDegen] (BaseClasses/GpuManager.cpp:733-746).  They become
+ * the last run (gain_fetch_amp) and are kept in the engine's slot (idegI, idegF) for the line
+ * assembly; a component run of another job empties the slots first.  gain_run_pair is
+ * components (0, 0) without a slot. */
+gain_status gain_run_pair_component(gain_engine e, const gain_pair_job* job, int idegI, int idegF,
+                                    gain_path path, const gain_split_opts* opts, gain_stats* stats);
+/* Every component pair of the job (idegI < sym_degen[gammaI], idegF < sym_degen[gammaF],
+ * idegF outer) that passes gain_degeneracy_filter, through gain_run_pair_component (the
+ * pairs main.cpp:238-342 and Output.cpp:78-85 compute).  stats sums the runs' times, counts
+ * and launches. */
+gain_status gain_run_pair_degenerate(gain_engine e, const gain_pair_job* job, const gain_filters* f,
+                                     gain_path path, const gain_split_opts* opts, gain_stats* stats);
 
 /* Text of one line exactly as Output.cpp:99-111 prints it, " || \n" included (without the
  * amplitude list unless namp > 0), through the C library's snprintf.  Returns the number of

@@ -223,10 +223,11 @@ int orc_run_pair(const orc_pair* p, int nthreads, int mode, double* amp) {
     double* primI = (double*)malloc(sizeof(double) * (size_t)p->dimenI);
     double* hls = (double*)malloc(sizeof(double) * (size_t)p->dimenF);
     if (!primI || !hls) { free(primI); free(hls); return -1; }
+    const int sdegI = p->sdegI > 0 ? p->sdegI : 1, sdegF = p->sdegF > 0 ? p->sdegF : 1;
     int err = 0;
     for (int l = 0; l < p->nlower; l++) {
         const double* vI = p->vec_lower + (size_t)l * p->NtotI;
-        orc_expand(p->dimenI, p->gammaI, p->maxcoeffI, 0, 1, p->NtotI, p->ijtermsI, p->icontrI,
+        orc_expand(p->dimenI, p->gammaI, p->maxcoeffI, p->idegI, sdegI, p->NtotI, p->ijtermsI, p->icontrI,
                    p->NI, p->represI, vI, primI, mode);
         orc_half_ls(p->jI, p->jF, p->dimenI, p->dimenF, p->tauI, p->tauF, p->icorrI, p->icorrF,
                     p->kstartI, p->kblockI, p->kstartF, p->kblockF, p->startFblock, p->endFblock,
@@ -241,7 +242,7 @@ int orc_run_pair(const orc_pair* p, int nthreads, int mode, double* amp) {
 #pragma omp for schedule(static)
                 for (int u = 0; u < p->nupper; u++) {
                     const double* vF = p->vec_upper + (size_t)u * p->NtotF;
-                    orc_expand(p->dimenF, p->gammaF, p->maxcoeffF, 0, 1, p->NtotF, p->ijtermsF,
+                    orc_expand(p->dimenF, p->gammaF, p->maxcoeffF, p->idegF, sdegF, p->NtotF, p->ijtermsF,
                                p->icontrF, p->NF, p->represF, vF, primF, mode);
                     amp[(size_t)l * p->nupper + u] = orc_dot(p->dimenF, primF, hls, mode);
                 }

@@ -101,6 +101,9 @@ typedef struct {
     int nlower, nupper;
     const double* vec_lower;
     const double* vec_upper;
+    /* degenerate components (transform_vector_primitive's ideg) and the degeneracies of the
+       two symmetries (0 reads as 1) */
+    int idegI, idegF, sdegI, sdegF;
 } orc_pair;
 
 int orc_run_pair(const orc_pair* p, int nthreads, int mode, double* amp);

@@ -62,7 +62,8 @@ class OrcPair(ctypes.Structure):
          ("dipole_me", _dp)] + \
         [(n, ctypes.c_int) for n in ("dip_stride", "startFblock", "endFblock", "ncontrF")] + \
         [("threej", _dp), ("nlower", ctypes.c_int), ("nupper", ctypes.c_int),
-         ("vec_lower", _dp), ("vec_upper", _dp)]
+         ("vec_lower", _dp), ("vec_upper", _dp)] + \
+        [(n, ctypes.c_int) for n in ("idegI", "idegF", "sdegI", "sdegF")]
 
 
 def _declare(L):
@@ -176,10 +177,11 @@ def dot(x, y, mode=REF):
 
 def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
              upper_levels: Sequence[int], threej, jmax, mode=REF, nthreads=1,
-             dipole_block=None):
+             dipole_block=None, components=(0, 0)):
     """amp[l, u] through the reference's plain loop order for one block pair.
 
-    lower_levels / upper_levels are level indices inside the (J, Gamma) blocks."""
+    lower_levels / upper_levels are level indices inside the (J, Gamma) blocks; components =
+    (idegI, idegF), the degenerate components of the lower and upper vectors."""
     p = problem
     bI, bF = p.bases[jindI], p.bases[jindF]
     iI, iF = p.infl[jindI], p.infl[jindF]
@@ -212,6 +214,8 @@ def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
     s.threej = D(threej)
     s.nlower, s.nupper = vl.shape[0], vu.shape[0]
     s.vec_lower, s.vec_upper = D(vl), D(vu)
+    s.idegI, s.idegF = int(components[0]), int(components[1])
+    s.sdegI, s.sdegF = int(iI.sdeg[gammaI]), int(iF.sdeg[gammaF])
     amp = np.zeros((vl.shape[0], vu.shape[0]), np.float64)
     rc = lib().orc_run_pair(ctypes.byref(s), nthreads, mode, amp.ctypes.data_as(_dp))
     if rc != 0:

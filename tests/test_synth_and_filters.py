@@ -133,3 +133,60 @@ def test_mixed_expansion_is_orthonormal(oracle_lib):
     T = np.array(cols).T
     assert np.allclose(T.T @ T, np.eye(b.dimen), atol=1e-15)
     assert (np.count_nonzero(T, axis=0) == 2).sum() > 0   # mixed columns exist
+
+
+def test_degenerate_expansion_is_orthonormal(oracle_lib):
+    """Rule c3e: A1, A2 and both components of E together form an orthonormal expansion of
+    the primitives (the reference's expand kernel on unit vectors, with ideg), and the E
+    components are distinct functions."""
+    import oracle
+    import synth
+    b = synth.make_basis(4, 6)
+    inf = synth.make_degenerate_inflation(b)
+    assert list(inf.sdeg) == [1, 1, 2] and inf.matsize == 2
+    assert int(inf.Ntot[0] + inf.Ntot[1] + 2 * inf.Ntot[2]) == b.dimen
+    cols = []
+    for g in range(3):
+        for ideg in range(int(inf.sdeg[g])):
+            for s in range(int(inf.Ntot[g])):
+                e = np.zeros(inf.Ntot[g])
+                e[s] = 1.0
+                cols.append(oracle.expand(inf, g, e, ideg=ideg))
+    T = np.array(cols).T
+    assert np.allclose(T.T @ T, np.eye(b.dimen), atol=1e-15)
+    p = synth.make_problem(6, [1, 2], "c3e", blocks=[(1, 2), (2, 2)])
+    assert list(p.sym_degen) == [1, 1, 2] and list(p.igamma_pair) == [1, 0, 2]
+    assert set(p.st_ndeg.tolist()) == {2}
+
+
+def test_oracle_pair_components_follow_the_expansion(oracle_lib):
+    """oracle.run_pair with components (idegI, idegF) equals the dense restatement: both
+    vectors expanded with their component (numpy over the tables), the half line strength of
+    the lower primitive vector, its dot with the upper primitive vector."""
+    import oracle
+    import synth
+    import threej
+    jmax = 4
+    p = synth.make_problem(8, [2, 3], "c3e", blocks=[(2, 2), (3, 2)])
+    lo = [0, 3, 5]
+    up = list(range(0, p.blocks[(1, 2)].vecs.shape[0], 4))
+    tj = threej.threej_table(jmax)
+
+    def dense_T(jind, ideg):
+        inf, d = p.infl[jind], p.bases[jind].dimen
+        nt, sd = int(inf.Ntot[2]), int(inf.sdeg[2])
+        T = np.zeros((d, nt))
+        for r in range(d):
+            irow, ib = inf.icontr[r], inf.icontr[r + d]
+            it = inf.ijterms[irow + 2 * inf.maxcoeff]
+            for i in range(inf.N[2][irow]):
+                T[r, it + i] = inf.repres[2][it + i + ideg * nt + ib * sd * nt]
+        return T
+
+    for comps in ((0, 0), (1, 0), (0, 1), (1, 1)):
+        amp = oracle.run_pair(p, 0, 2, 1, 2, lo, up, tj, jmax, components=comps)
+        TI, TF = dense_T(0, comps[0]), dense_T(1, comps[1])
+        for a, l in enumerate(lo):
+            h = oracle.half_ls(p.bases[0], p.bases[1], TI @ p.blocks[(0, 2)].vecs[l], p.dipole, tj, jmax)
+            want = (TF @ p.blocks[(1, 2)].vecs[up].T).T @ h
+            assert np.allclose(amp[a], want, rtol=0, atol=1e-12 * np.abs(want).max())
