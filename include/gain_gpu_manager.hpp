@@ -281,21 +281,34 @@ class GpuManager {
         check(gain_upload_eigvecs(engine_, jind, gamma, nlevels, nsize, vecs));
     }
     gain_stats ExecuteBlockPair(const gain_pair_job& job, gain_path path, const gain_split_opts* opts = nullptr) {
-        if (rotsym_) {   // the pair's rotational matrix elements, once per (J'', J') pair
-            const int key = job.jindI * 100000 + job.jindF;
-            if (std::find(wigner_sent_.begin(), wigner_sent_.end(), key) == wigner_sent_.end()) {
-                const Wigner& w = wigner_at(job.jindI, bases_.at(job.jindF).J - bases_.at(job.jindI).J + 1);
-                check(gain_upload_wigner(engine_, job.jindI, job.jindF, w.nI, w.nF, maxdeg_, w.host.data()));
-                wigner_sent_.push_back(key);
-            }
-        }
+        send_wigner(job);
         gain_stats st{};
         check(gain_run_pair(engine_, &job, path, opts, &st));
+        return st;
+    }
+    // A block pair of degenerate symmetries: every component pair (idegI, idegF) that passes
+    // the degeneracy filter, kept in the engine's component slots; gain_pair_lines with the
+    // states' ndegI / ndegF then sums them as OutputLinestrength does.
+    gain_stats ExecuteBlockPairDegenerate(const gain_pair_job& job, const gain_filters& filters, gain_path path,
+                                          const gain_split_opts* opts = nullptr) {
+        send_wigner(job);
+        gain_stats st{};
+        check(gain_run_pair_degenerate(engine_, &job, &filters, path, opts, &st));
         return st;
     }
     gain_engine engine() const { return engine_; }
 
    private:
+    void send_wigner(const gain_pair_job& job) {
+        if (!rotsym_) return;
+        // the pair's rotational matrix elements, once per (J'', J') pair
+        const int key = job.jindI * 100000 + job.jindF;
+        if (std::find(wigner_sent_.begin(), wigner_sent_.end(), key) == wigner_sent_.end()) {
+            const Wigner& w = wigner_at(job.jindI, bases_.at(job.jindF).J - bases_.at(job.jindI).J + 1);
+            check(gain_upload_wigner(engine_, job.jindI, job.jindF, w.nI, w.nF, maxdeg_, w.host.data()));
+            wigner_sent_.push_back(key);
+        }
+    }
     struct Basis {
         int J = 0, dimen = 0;
         int *tau = nullptr, *vib = nullptr, *kblock = nullptr, *K = nullptr, *lev = nullptr;

@@ -2,6 +2,7 @@
 bad arguments on the host with a status (never aborting), and prints lines exactly as the
 reference's Output::OutputLinestrength does."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -73,3 +74,30 @@ def test_line_text_matches_reference_format(built_lib, args):
     a = gainls.format_line(nu, iF, jF, gF, iI, jI, gI, A, intensity=inten, amps=amps)
     b = oracle.line_text(nu, iF, jF, gF, iI, jI, gI, A, intens=inten, amps=amps)
     assert a == b
+
+
+def test_manager_header_compiles_and_links(built_lib, tmp_path):
+    """The C++ GpuManager mirror builds against the library: every method it defines, the
+    block-pair entry points included, compiles and links (no GPU call is made)."""
+    import shutil
+    import subprocess
+    from conftest import ROOT
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "use_manager.cpp"
+    src.write_text(
+        '#include "gain_gpu_manager.hpp"\n'
+        "int main(int argc, char**) {\n"
+        "    auto a = &gain::GpuManager::ExecuteBlockPair;\n"
+        "    auto b = &gain::GpuManager::ExecuteBlockPairDegenerate;\n"
+        "    auto c = &gain::GpuManager::ExecuteDotProduct;\n"
+        "    return argc > 99 ? (int)(sizeof a + sizeof b + sizeof c) : 0;\n"
+        "}\n")
+    lib = os.path.join(ROOT, "gain-mpi_gb300", "lib")
+    cuda = "/usr/local/cuda"
+    out = tmp_path / "use_manager"
+    subprocess.run([gxx, "-std=c++17", "-O0", "-I", os.path.join(ROOT, "include"), "-I", cuda + "/include", str(src),
+                    "-o", str(out), "-L", lib, "-lgainls", "-L", cuda + "/lib64", "-lcudart",
+                    "-Wl,-rpath," + lib], check=True)
+    assert out.exists()
