@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--batch", action="store_true",
                     help="every allowed block pair of J=0..--batch-jmax through the split path (one JSON line)")
     ap.add_argument("--batch-nv", type=int, default=200, help="vibrational basis size of --batch")
+    ap.add_argument("--degenerate", action="store_true",
+                    help="a doubly degenerate E -> E pair of the config-2 sizes (rule c3e), every component pair")
     ap.add_argument("--batch-jmax", type=int, default=30, help="largest J of --batch")
     return ap.parse_args()
 
@@ -536,6 +538,67 @@ def adjoint_check(args):
     eng.close()
 
 
+def degenerate_pair(args):
+    """Degenerate symmetries at the config-2 sizes: rule c3e (A1, A2, doubly degenerate E),
+    N_v = 2000, J'' = 10 E (the 2000 lowest states) -> J' = 11 E (every state).  A step is
+    gain_run_pair_degenerate over the four component pairs (generic symmetry type: all pass)
+    through the split path; the lines combine the four slots (S = sum amp^2 / 2).  S is checked
+    against the plain FP64 path's four components on the same lines.  One JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    import gainls
+    import synth
+    nv = 200 if args.small else NV
+    n_lower = 64 if args.small else N_LOWER
+    E = 2
+    t0 = time.perf_counter()
+    bI, bF = synth.make_basis(JI, nv), synth.make_basis(JF, nv)
+    iI, iF = synth.make_degenerate_inflation(bI), synth.make_degenerate_inflation(bF)
+    nI, nF = int(iI.Ntot[E]), int(iF.Ntot[E])
+    vl = synth.make_eigvecs(nI, JI, E, device="cuda", nstates=n_lower)
+    vu = synth.make_eigvecs(nF, JF, E, device="cuda")
+    eI = synth.make_energies(nI, JI, E)[:n_lower]
+    eF = synth.make_energies(nF, JF, E)
+    p = synth.Problem(nv, [JI, JF], "c3e", 3, synth.degen_of("c3e"), synth.selection_of("c3e"),
+                      synth.igamma_pair_of(synth.selection_of("c3e")), [bI, bF], [iI, iF],
+                      [synth.classes_of(b, "c3e") for b in (bI, bF)], synth.make_dipole(nv),
+                      {(0, E): synth.Block(JI, 0, E, vl, eI), (1, E): synth.Block(JF, 1, E, vu, eF)})
+    eng = gainls.Engine(11, 3, 2)
+    gainls.upload_problem(eng, p)
+    f = gainls.make_filters([1.0] * 3, p.isym_pairs, p.igamma_pair, p.sym_degen, (-1e9, 1e9), (-1e9, 1e9))
+    lo, up = list(range(n_lower)), list(range(nF))
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        eng.run_pair(0, E, 1, E, lo, up, gainls.PATH_SPLIT, filters=f)
+    torch.cuda.synchronize()
+    dev, g1, g2 = [], [], []
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        st = eng.run_pair(0, E, 1, E, lo, up, gainls.PATH_SPLIT, filters=f)
+        dev.append(st["device_ms"])
+        g1.append(st["gemm1_ms"])
+        g2.append(st["gemm2_ms"])
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t1) * 1e3 / args.steps
+    S_split = eng.lines(eI, eF, JI, JF, ndeg=(2, 2), want=("S",))["S"].copy()
+    sp = eng.run_pair(0, E, 1, E, lo, up, gainls.PATH_PLAIN_FP64, filters=f)
+    S_plain = eng.lines(eI, eF, JI, JF, ndeg=(2, 2), want=("S",))["S"]
+    m = S_plain > 1e-10 * S_plain.max()
+    rel = np.abs(S_split[m] - S_plain[m]) / S_plain[m]
+    ms = float(np.median(dev))
+    lines = n_lower * nF
+    out = {"mode": "degenerate", "workload": f"N_v={nv}, J''={JI} E ({nI} functions) -> J'={JF} E ({nF} functions), "
+                                             f"{n_lower} lowest lower states x {nF} upper states, 4 component pairs",
+           "lines": lines, "component_pairs": 4, "setup_s": setup_s,
+           "split_device_ms": ms, "split_wall_ms": wall_ms, "lines_per_s_device": lines / (ms * 1e-3),
+           "gemm1_ms": float(np.median(g1)), "gemm2_ms": float(np.median(g2)),
+           "plain_fp64_device_ms": sp["device_ms"], "speedup_vs_plain_fp64": sp["device_ms"] / ms,
+           "max_rel_err_S_vs_plain": float(rel.max()), "p99_rel_err_S_vs_plain": float(np.quantile(rel, 0.99)),
+           "lines_checked": int(m.sum()), "domain": "S > 1e-10 S_max"}
+    print(json.dumps(out), flush=True)
+    eng.close()
+
+
 def batch_plan(args):
     """Many block pairs: every allowed (J'', Gamma'') -> (J', Gamma') pair of J = 0..jmax, four
     symmetries, lower states below 4000 cm^-1 against every upper state (the reference's
@@ -678,6 +741,8 @@ def main():
         return adjoint_check(args)
     if args.batch:
         return batch_plan(args)
+    if args.degenerate:
+        return degenerate_pair(args)
     if args.impl == "reference":
         if ws > 1 and rank != 0:
             return
