@@ -819,19 +819,37 @@ k_slice(const SliceArgs a) {
 // the destination columns four at a time: col_inv gives each destination column's source
 // column (-1: padding, stored as zero digits), each slice's four digits leave as one 8-byte
 // store, and a chunk is a plain range of destination columns (the GEMM's k-block split).
+//
+// Digits: the balanced digits of the fixed-point integer I (d_i in [1 - 2^(beta-1), 2^(beta-1)]
+// below the top one) are the plain base-2^beta digits of u = I + C, C = (2^(beta-1) - 1) times
+// the sum of the lower digit weights, each shifted down by 2^(beta-1) - 1; the top digit is
+// u >> beta (S - 1).  Every digit has at most 8 significant bits (|d| <= 2^beta <= 256), so its
+// float is exact in BF16 and the BF16 bits are the float's upper half.
 template <int S>
 __global__ void __launch_bounds__(SLICE_THREADS)
 k_slice4(const SliceArgs a) {
     const int tid = threadIdx.x;
     const int nkb = a.kpad / BK;
+    __shared__ unsigned long long red_u[SLICE_THREADS / 32];
+    __shared__ float red_f[SLICE_THREADS / 32];
+    __shared__ int red_i[SLICE_THREADS / 32];
+    __shared__ float red_t[SLICE_THREADS / 32][S];
+    __shared__ unsigned int red_d[SLICE_THREADS / 32][S * MAX_CHUNKS];
+    __shared__ unsigned long long dsum[S * MAX_CHUNKS];   // per (slice, chunk): sum over the row
+    const int beta = a.beta;
+    const int q = S * beta;
+    const long long mask = (1ll << beta) - 1ll;
+    const int off = (1 << (beta - 1)) - 1;
+    long long C = 0;
+#pragma unroll
+    for (int k = 0; k < S - 1; ++k) C += (long long)off << (beta * k);
+    const float inv2q = pow2f(-q);
+    float w2[S];   // 2^{-(i+1) beta}
+#pragma unroll
+    for (int i = 0; i < S; ++i) w2[i] = pow2f(-(i + 1) * beta);
     for (int row = blockIdx.x; row < a.nrows; row += gridDim.x) {
         const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
         const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
-        __shared__ unsigned long long red_u[SLICE_THREADS / 32];
-        __shared__ float red_f[SLICE_THREADS / 32];
-        __shared__ int red_i[SLICE_THREADS / 32];
-        __shared__ float red_t[SLICE_THREADS / 32][S];
-        __shared__ unsigned int red_d[SLICE_THREADS / 32][S * MAX_CHUNKS];
 
         // pass 1: max |x| through the IEEE bit pattern (integer compares only)
         unsigned long long mx = 0;
@@ -852,8 +870,6 @@ k_slice4(const SliceArgs a) {
         const int Emax = (int)(mx >> 52);
         const bool zero_row = (mx == 0);
         const int e = zero_row ? 0 : (Emax > 0 ? Emax - 1022 : -1022);
-        const int beta = a.beta;
-        const int q = S * beta;
         const long sstride = a.slice_stride;
         __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
 
@@ -862,8 +878,6 @@ k_slice4(const SliceArgs a) {
         float tsq[S];
 #pragma unroll
         for (int i = 0; i < S; ++i) tsq[i] = 0.0f;
-        const long long mask = (1ll << beta) - 1ll, halfb = 1ll << (beta - 1);
-        const float inv2q = pow2f(-q);
         for (int ch = 0; ch < a.nchunks; ++ch) {
             unsigned int dsq[S];
 #pragma unroll
@@ -872,6 +886,7 @@ k_slice4(const SliceArgs a) {
             const int d1 = (int)(((long)(ch + 1) * nkb) / a.nchunks) * BK;
             for (int dc = d0 + 4 * tid; dc < d1; dc += 4 * SLICE_THREADS) {
                 uint32_t pk[S][2];
+                uint32_t even[S];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int col = dc + u;
@@ -889,29 +904,25 @@ k_slice4(const SliceArgs a) {
                         const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
                         I = (bits >> 63) ? -(long long)m : (long long)m;
                     }
-                    long long v = I;
+                    const long long uo = I + C;
                     int d[S];
 #pragma unroll
-                    for (int i = S - 1; i >= 1; --i) {
-                        long long r = v & mask;
-                        if (r > halfb) r -= (1ll << beta);
-                        d[i] = (int)r;
-                        v = (v - r) >> beta;
-                    }
-                    d[0] = (int)v;
+                    for (int i = S - 1; i >= 1; --i)
+                        d[i] = (int)(((unsigned long long)uo >> (beta * (S - 1 - i))) & mask) - off;
+                    d[0] = (int)(uo >> (beta * (S - 1)));
                     // tails x^(rounded) - X^(n) = sum_{i>n} d_i 2^{-(i+1) beta}, squared into tsq[n]
                     float tail = 0.0f;
 #pragma unroll
                     for (int i = S - 1; i >= 1; --i) {
-                        tail = __fadd_rn(tail, (float)d[i] * pow2f(-(i + 1) * beta));
+                        tail = __fadd_rn(tail, (float)d[i] * w2[i]);
                         tsq[i - 1] = __fmaf_ru(tail, tail, tsq[i - 1]);
                     }
 #pragma unroll
                     for (int i = 0; i < S; ++i) {
                         dsq[i] += (unsigned int)(d[i] * d[i]);
-                        const uint32_t h16 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)d[i]));
-                        if (u & 1) pk[i][u >> 1] |= h16 << 16;
-                        else pk[i][u >> 1] = h16;
+                        const uint32_t fb = __float_as_uint((float)d[i]);   // exact: BF16 = upper half
+                        if (u & 1) pk[i][u >> 1] = __byte_perm(even[i], fb, 0x7632);
+                        else even[i] = fb;
                     }
                     if (I != 0) {
                         ++nnz;
@@ -946,38 +957,42 @@ k_slice4(const SliceArgs a) {
             for (int i = 0; i < S; ++i) red_t[tid >> 5][i] = tsq[i];
         }
         __syncthreads();
-        if (tid == 0) {
+        // per (slice, chunk) sums over the warps, one thread each (integer: any order)
+        if (tid < S * a.nchunks) {
+            const int i = tid / a.nchunks, c = tid - i * a.nchunks;
+            unsigned long long t = 0;
+            for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
+            dsum[i * MAX_CHUNKS + c] = t;
+        }
+        __syncthreads();
+        // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
+        const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
+        if (tid < MAX_SLICES) {   // one slice per thread; tq in warp order as before
+            const int i = tid;
+            int N = 0;
+            for (int w = 0; w < SLICE_THREADS / 32; ++w) N += red_i[w];
+            const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
+            float tq = 0.0f;
+            unsigned long long dd = 0;
+            if (i < S) {
+                for (int w = 0; w < SLICE_THREADS / 32; ++w) tq = __fadd_ru(tq, red_t[w][i]);
+                for (int c = 0; c < a.nchunks; ++c) dd += dsum[i * MAX_CHUNKS + c];
+            }
+            a.st.dnv[(long)row * MAX_SLICES + i] = i < S ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
+            a.st.rnv[(long)row * MAX_SLICES + i] = i < S ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
+        } else if (tid >= 32 && tid < 32 + a.nchunks) {   // one chunk per thread: the largest digit norm
+            const int c = tid - 32;
+            unsigned long long m = 0;
+            for (int i = 0; i < S; ++i) m = dsum[i * MAX_CHUNKS + c] > m ? dsum[i * MAX_CHUNKS + c] : m;
+            a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
+        } else if (tid == 64) {
             float L2 = 0.0f;
             int N = 0;
             for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
-            // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
             const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
-            const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
             a.st.e[row] = e;
             a.st.nnz[row] = N;
             a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(L2), slack), dq);
-            for (int i = 0; i < MAX_SLICES; ++i) {
-                float tq = 0.0f;
-                unsigned long long dd = 0;
-                if (i < S) {
-                    for (int w = 0; w < SLICE_THREADS / 32; ++w) {
-                        tq = __fadd_ru(tq, red_t[w][i]);
-                        for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
-                    }
-                }
-                a.st.dnv[(long)row * MAX_SLICES + i] = i < S ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
-                a.st.rnv[(long)row * MAX_SLICES + i] =
-                    i < S ? __fadd_ru(__fmul_ru(__fsqrt_ru(tq), slack), dq) : 0.0f;
-            }
-            for (int c = 0; c < a.nchunks; ++c) {
-                unsigned long long m = 0;
-                for (int i = 0; i < S; ++i) {
-                    unsigned long long t = 0;
-                    for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
-                    m = t > m ? t : m;
-                }
-                a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
-            }
             if (a.st.inerr) {
                 float v = 0.0f;
                 if (a.inerr2_prev && !zero_row) {
