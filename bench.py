@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--batch", action="store_true",
                     help="every allowed block pair of J=0..--batch-jmax through the split path (one JSON line)")
     ap.add_argument("--batch-nv", type=int, default=200, help="vibrational basis size of --batch")
+    ap.add_argument("--batch-engines", type=int, default=4,
+                    help="engines (streams, host threads) of the --batch plan run through gain_run_plan")
     ap.add_argument("--degenerate", action="store_true",
                     help="a doubly degenerate E -> E pair of the config-2 sizes (rule c3e), every component pair")
     ap.add_argument("--batch-jmax", type=int, default=30, help="largest J of --batch")
@@ -639,6 +641,29 @@ def batch_plan(args):
     dev_ms = [float(np.sum(d)) for d, _ in runs]
     wall_ms = [w for _, w in runs]
     per_pair = np.median(np.array([d for d, _ in runs]), axis=0)
+    # the same plan over several engines of this GPU (gain_run_plan: one stream and host
+    # thread each, largest pairs first), wall time of the whole plan
+    plan = None
+    if args.batch_engines > 1:
+        engines = [eng]
+        for _ in range(args.batch_engines - 1):
+            e2 = gainls.Engine(jmax, p.nsym, 1)
+            gainls.upload_problem(e2, p)
+            engines.append(e2)
+        for _ in range(max(1, args.warmup)):
+            gainls.run_plan(engines, pairs, gainls.PATH_SPLIT)
+        pw = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            gainls.run_plan(engines, pairs, gainls.PATH_SPLIT)
+            torch.cuda.synchronize()
+            pw.append((time.perf_counter() - w0) * 1e3)
+        plan = {"engines": len(engines), "wall_ms": float(np.median(pw)),
+                "transitions_per_s_wall": total / (np.median(pw) * 1e-3),
+                "speedup_vs_one_engine_wall": float(np.median(wall_ms)) / float(np.median(pw))}
+        for e2 in engines[1:]:
+            e2.close()
     # accuracy and time of the plain FP64 path, pair by pair
     worst, plain_ms, nchk = 0.0, 0.0, 0
     for (jI, gI, jF, gF, lo, up) in pairs:
@@ -664,7 +689,8 @@ def batch_plan(args):
            "largest_pairs": [{"pair": list(pairs[i][:4]), "lower": len(pairs[i][4]), "upper": len(pairs[i][5]),
                               "ms": float(per_pair[i])} for i in order],
            "pairs_under_1M_transitions_ms": float(np.sum([per_pair[i] for i in range(len(pairs))
-                                                          if trans[i] < 1_000_000]))}
+                                                          if trans[i] < 1_000_000])),
+           "plan": plan}
     print(json.dumps(out), flush=True)
     eng.close()
 

@@ -4,14 +4,17 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -2080,6 +2083,59 @@ gain_status gain_run_pair_degenerate(gain_engine e, const gain_pair_job* job, co
         }
     if (!runs) return set_error(GAIN_ERR_INVALID_ARG, "no component pair passes the degeneracy filter");
     if (stats) *stats = sum;
+    return GAIN_OK;
+}
+
+gain_status gain_run_plan(gain_engine* engines, int n_engines, const gain_pair_job* jobs, int n_jobs,
+                          gain_path path, const gain_split_opts* opts, gain_job_done_fn on_done, void* user,
+                          gain_stats* stats) {
+    clear_error();
+    if (!engines || n_engines <= 0 || n_engines > 64 || (!jobs && n_jobs > 0) || n_jobs < 0)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_run_plan: bad engine or job list");
+    for (int i = 0; i < n_engines; ++i) {
+        if (!engines[i]) return set_error(GAIN_ERR_INVALID_ARG, "gain_run_plan: engine %d is NULL", i);
+        for (int k = 0; k < i; ++k)
+            if (engines[k] == engines[i]) return set_error(GAIN_ERR_INVALID_ARG, "gain_run_plan: engine %d repeated", i);
+    }
+    // largest jobs first (longest-processing-time order): the small ones fill in at the end
+    std::vector<int> order(n_jobs);
+    for (int j = 0; j < n_jobs; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long long)jobs[a].nlower * jobs[a].nupper > (long long)jobs[b].nlower * jobs[b].nupper;
+    });
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    std::mutex mu;
+    gain_status first_status = GAIN_OK;
+    std::string first_error;
+    auto worker = [&](gain_engine e) {
+        for (;;) {
+            if (failed.load()) return;
+            const int k = next.fetch_add(1);
+            if (k >= n_jobs) return;
+            const int j = order[k];
+            gain_stats st;
+            memset(&st, 0, sizeof st);
+            const gain_status r = gain_run_pair(e, &jobs[j], path, opts, &st);
+            if (stats) stats[j] = st;
+            if (r != GAIN_OK) {
+                std::lock_guard<std::mutex> g(mu);
+                if (first_status == GAIN_OK) {
+                    first_status = r;
+                    first_error = "job " + std::to_string(j) + ": " + g_last_error;
+                }
+                failed.store(true);
+            }
+            if (on_done) on_done(user, j, e, r);
+            if (r != GAIN_OK) return;
+        }
+    };
+    std::vector<std::thread> threads;
+    const int nt = std::min(n_engines, std::max(n_jobs, 1));
+    for (int i = 1; i < nt; ++i) threads.emplace_back(worker, engines[i]);
+    worker(engines[0]);   // the calling thread drives the first engine
+    for (auto& t : threads) t.join();
+    if (first_status != GAIN_OK) return set_error(first_status, "%s", first_error.c_str());
     return GAIN_OK;
 }
 

@@ -193,6 +193,8 @@ def _declare(L):
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
     L.gain_adjoint_pair.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.POINTER(Stats)]
     L.gain_adjoint_pair_prec.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.c_int, ctypes.POINTER(Stats)]
+    L.gain_run_plan.argtypes = [ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int,
+                                ctypes.POINTER(SplitOpts), JOB_DONE_FN, _vp, ctypes.POINTER(Stats)]
     L.gain_run_pair_component.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_run_pair_degenerate.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.POINTER(Filters), ctypes.c_int,
@@ -253,7 +255,8 @@ def _declare(L):
     for name in ("gain_hls_kblock", "gain_hls_rotsym", "gain_expand", "gain_dot", "gain_threej_table", "gain_engine_create",
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair",
-                 "gain_adjoint_pair_prec", "gain_run_pair", "gain_run_pair_component", "gain_run_pair_degenerate", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_adjoint_pair_prec", "gain_run_pair", "gain_run_pair_component", "gain_run_pair_degenerate",
+                 "gain_run_plan", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
                  "gain_lines_text_device",
                  "gain_format_values_device"):
@@ -546,6 +549,42 @@ def _lines_text_host(self, eI, eF, jI, jF, gammaI, gammaF, out, temperature=296.
                                           gammaF, flags, out.ctypes.data, out.size, ctypes.byref(nb),
                                           ctypes.byref(nl)))
     return memoryview(out)[:nb.value], nl.value
+
+
+JOB_DONE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int)
+
+
+def run_plan(engines, jobs, path=PATH_SPLIT, tol=0.0, on_done=None):
+    """gain_run_plan: jobs = [(jindI, gammaI, jindF, gammaF, lower_levels, upper_levels)] over
+    the engines (each holding the uploads the jobs need).  on_done(job, engine, status) runs in
+    the worker's thread after each job (the engine's amplitudes are that job's meanwhile; the
+    engine argument is the matching Engine).  Returns the per-job stats dicts."""
+    keep = []
+    arr = (PairJob * max(1, len(jobs)))()
+    for i, (jI, gI, jF, gF, lo, up) in enumerate(jobs):
+        lo, up = _i32(lo), _i32(up)
+        keep += [lo, up]
+        arr[i] = PairJob(jI, gI, jF, gF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
+    hs = (_vp * len(engines))(*[e.h for e in engines])
+    by_handle = {(e.h.value if isinstance(e.h, ctypes.c_void_p) else e.h): e for e in engines}
+    st = (Stats * max(1, len(jobs)))()
+    cb = JOB_DONE_FN(0)
+    errors = []
+    if on_done is not None:
+        def _done(user, job, eh, status):
+            eng = by_handle[eh]
+            lo_n, up_n = arr[job].nlower, arr[job].nupper
+            eng._shape = (lo_n, up_n)
+            try:
+                on_done(job, eng, status)
+            except Exception as exc:   # never raise through the C frames
+                errors.append(exc)
+        cb = JOB_DONE_FN(_done)
+    opts = SplitOpts(tol, 0, 0, 0, 0.0)
+    check(lib().gain_run_plan(hs, len(engines), arr, len(jobs), path, ctypes.byref(opts), cb, None, st))
+    if errors:
+        raise errors[0]
+    return [st[i].as_dict() for i in range(len(jobs))]
 
 
 Engine.lines_text = _lines_text

@@ -254,6 +254,20 @@ gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, cons
 gain_status gain_run_pair(gain_engine e, const gain_pair_job* job, gain_path path,
                           const gain_split_opts* opts, gain_stats* stats);
 
+/* A plan of block pairs over several engines of one device.  Each engine keeps its own
+ * stream and buffers, so the jobs of different engines overlap on the GPU (small pairs leave
+ * most SMs idle one at a time).  Every engine must hold the uploads the jobs need (bases,
+ * expansion tables, dipole, eigenvectors).  One host thread per engine takes the largest
+ * remaining job (the calling thread drives engines[0]) and runs gain_run_pair on it; then
+ * on_done(user, job, engine, status), when given, is called from that thread, and the
+ * engine's amplitudes (gain_fetch_amp, gain_pair_lines, ...) are that job's until it returns.
+ * stats, when given, receives each job's stats at its index.  After a failure no further job
+ * starts; the first failing status is returned, its message names the job. */
+typedef void (*gain_job_done_fn)(void* user, int job, gain_engine engine, gain_status status);
+gain_status gain_run_plan(gain_engine* engines, int n_engines, const gain_pair_job* jobs, int n_jobs,
+                          gain_path path, const gain_split_opts* opts, gain_job_done_fn on_done, void* user,
+                          gain_stats* stats);
+
 /* Device pointer / leading dimension of the last run's amplitude matrix. */
 gain_status gain_pair_amp_device(gain_engine e, const double** amp, int* ld);
 
