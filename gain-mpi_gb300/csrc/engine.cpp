@@ -257,6 +257,10 @@ struct gain_engine_s {
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;   // upper-vector slicing, concurrent with the lower side
     cudaStream_t stc = nullptr;   // asynchronous eigenvector uploads
+    cudaStream_t std2h = nullptr; // device-to-host copies of an asynchronous line assembly
+    cudaEvent_t ev_lines = nullptr, ev_lines_d2h = nullptr;
+    bool lines_pending = false;     // gain_pair_lines_async copies still in flight
+    long long* lines_nout = nullptr;   // their caller's n_lines
     cudaEvent_t ev[10] = {};
     cudaEvent_t ev_up = nullptr;  // orders an asynchronous upload after queued engine work
     std::vector<long> zkey_V, zkey_H, zkey_U;   // shape/layout the digit buffers were cleared for
@@ -1566,6 +1570,9 @@ gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_
         GAIN_CUDA(cudaStreamCreateWithPriority(&e->st2, cudaStreamNonBlocking, lo));
     }
     GAIN_CUDA(cudaStreamCreateWithFlags(&e->stc, cudaStreamNonBlocking));
+    GAIN_CUDA(cudaStreamCreateWithFlags(&e->std2h, cudaStreamNonBlocking));
+    GAIN_CUDA(cudaEventCreateWithFlags(&e->ev_lines, cudaEventDisableTiming));
+    GAIN_CUDA(cudaEventCreateWithFlags(&e->ev_lines_d2h, cudaEventDisableTiming));
     for (auto& ev : e->ev) GAIN_CUDA(cudaEventCreate(&ev));
     GAIN_CUDA(cudaEventCreateWithFlags(&e->ev_up, cudaEventDisableTiming));
     std::vector<double> t((size_t)(jmax + 1) * (jmax + 1) * 9);
@@ -1579,12 +1586,17 @@ gain_status gain_engine_destroy(gain_engine e) {
     clear_error();
     if (!e) return GAIN_OK;
     cudaSetDevice(e->device);
+    if (e->lines_pending) cudaEventSynchronize(e->ev_lines_d2h);
     cudaStreamSynchronize(e->st);
     if (e->st2) cudaStreamSynchronize(e->st2);
     if (e->stc) cudaStreamSynchronize(e->stc);
+    if (e->std2h) cudaStreamSynchronize(e->std2h);
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
     if (e->ev_up) cudaEventDestroy(e->ev_up);
+    if (e->ev_lines) cudaEventDestroy(e->ev_lines);
+    if (e->ev_lines_d2h) cudaEventDestroy(e->ev_lines_d2h);
+    if (e->std2h) cudaStreamDestroy(e->std2h);
     if (e->stc) cudaStreamDestroy(e->stc);
     if (e->st2) cudaStreamDestroy(e->st2);
     if (e->st) cudaStreamDestroy(e->st);
@@ -2175,11 +2187,23 @@ gain_status gain_fetch_amp(gain_engine e, double* amp_host) {
     return GAIN_OK;
 }
 
-gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI,
-                            const double* energiesF, int jI, int jF, double* S, double* A, double* I,
-                            unsigned char* keep, long long* n_lines) {
-    clear_error();
+namespace {
+// A pending asynchronous line assembly completes: its copies have landed, n_lines is set and
+// the line buffers are free again.
+gain_status lines_settle(gain_engine e) {
+    if (!e->lines_pending) return GAIN_OK;
+    e->lines_pending = false;
+    GAIN_CUDA(cudaEventSynchronize(e->ev_lines_d2h));
+    if (e->lines_nout) *e->lines_nout = (long long)*(const unsigned long long*)((const char*)e->readback + 96);
+    e->lines_nout = nullptr;
+    return GAIN_OK;
+}
+
+gain_status pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI, const double* energiesF,
+                       int jI, int jF, double* S, double* A, double* I, unsigned char* keep, long long* n_lines,
+                       bool async) {
     GAIN_TRY(check_engine(e));
+    GAIN_TRY(lines_settle(e));
     if (!prm || !energiesI || !energiesF || jI < 0 || jF < 0)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines: bad argument");
     if (!e->have_amp) return set_error(GAIN_ERR_NOT_READY, "no completed run");
@@ -2204,6 +2228,24 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     GAIN_CUDA(launch_lines(rows, cols, amp, ld, e->eIdev.p, e->eFdev.p, p, S ? e->lineS.p : nullptr,
                            A ? e->lineA.p : nullptr, I ? e->lineI.p : nullptr, keep ? e->lineKeep.p : nullptr,
                            e->ull.p + 1, st));
+    if (async) {
+        // the copies run on their own stream: the engine's next run (on st, after the line
+        // kernel) and its uploads overlap them
+        if (!e->readback) GAIN_CUDA(cudaMallocHost(&e->readback, 128));
+        GAIN_CUDA(cudaEventRecord(e->ev_lines, st));
+        GAIN_CUDA(cudaStreamWaitEvent(e->std2h, e->ev_lines, 0));
+        cudaStream_t sd = e->std2h;
+        GAIN_CUDA(cudaMemcpyAsync((char*)e->readback + 96, e->ull.p + 1, sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, sd));
+        if (S) GAIN_CUDA(cudaMemcpyAsync(S, e->lineS.p, sizeof(double) * n, cudaMemcpyDeviceToHost, sd));
+        if (A) GAIN_CUDA(cudaMemcpyAsync(A, e->lineA.p, sizeof(double) * n, cudaMemcpyDeviceToHost, sd));
+        if (I) GAIN_CUDA(cudaMemcpyAsync(I, e->lineI.p, sizeof(double) * n, cudaMemcpyDeviceToHost, sd));
+        if (keep) GAIN_CUDA(cudaMemcpyAsync(keep, e->lineKeep.p, n, cudaMemcpyDeviceToHost, sd));
+        GAIN_CUDA(cudaEventRecord(e->ev_lines_d2h, sd));
+        e->lines_pending = true;
+        e->lines_nout = n_lines;
+        return GAIN_OK;
+    }
     unsigned long long nk = 0;
     GAIN_CUDA(cudaMemcpyAsync(&nk, e->ull.p + 1, sizeof nk, cudaMemcpyDeviceToHost, st));
     if (S) GAIN_CUDA(cudaMemcpyAsync(S, e->lineS.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
@@ -2214,6 +2256,27 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
     if (n_lines) *n_lines = (long long)nk;
     return GAIN_OK;
 }
+}  // namespace
+
+gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                            const double* energiesF, int jI, int jF, double* S, double* A, double* I,
+                            unsigned char* keep, long long* n_lines) {
+    clear_error();
+    return pair_lines(e, prm, energiesI, energiesF, jI, jF, S, A, I, keep, n_lines, false);
+}
+
+gain_status gain_pair_lines_async(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                  const double* energiesF, int jI, int jF, double* S, double* A, double* I,
+                                  unsigned char* keep, long long* n_lines) {
+    clear_error();
+    return pair_lines(e, prm, energiesI, energiesF, jI, jF, S, A, I, keep, n_lines, true);
+}
+
+gain_status gain_lines_wait(gain_engine e) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    return lines_settle(e);
+}
 
 namespace {
 // The text of the last run's lines: lengths, offsets and (into out, when given and large
@@ -2223,6 +2286,7 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
                        int jI, int jF, int gammaI, int gammaF, int flags, char* out, unsigned long long cap,
                        unsigned long long* text_bytes, long long* n_lines) {
     GAIN_TRY(check_engine(e));
+    GAIN_TRY(lines_settle(e));
     if (!prm || !energiesI || !energiesF || jI < 0 || jF < 0 || gammaI < 0 || gammaF < 0 ||
         (flags & ~(GAIN_TEXT_INTENSITY | GAIN_TEXT_AMPLITUDES)))
         return set_error(GAIN_ERR_INVALID_ARG, "gain_pair_lines_text: bad argument");

@@ -205,6 +205,9 @@ def _declare(L):
     L.gain_fetch_amp.argtypes = [_vp, _dp]
     L.gain_pair_lines.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, _dp, _dp, _dp,
                                   ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_longlong)]
+    L.gain_pair_lines_async.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, _dp, _dp, _dp,
+                                  ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_longlong)]
+    L.gain_lines_wait.argtypes = [_vp]
     L.gain_format_line.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
     L.gain_format_line.restype = I
     L.gain_format_line_native.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
@@ -257,7 +260,7 @@ def _declare(L):
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair",
                  "gain_adjoint_pair_prec", "gain_run_pair", "gain_run_pair_component", "gain_run_pair_degenerate",
                  "gain_run_plan", "gain_pair_amp_device", "gain_fetch_amp",
-                 "gain_pair_lines", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
+                 "gain_pair_lines", "gain_pair_lines_async", "gain_lines_wait", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
                  "gain_lines_text_device",
                  "gain_format_values_device"):
         getattr(L, name).restype = S
@@ -476,6 +479,13 @@ class Engine:
         self._shape = (len(lo), len(up))
         return dL_dmu
 
+    def lines_wait(self) -> int:
+        """Wait for the copies of the last asynchronous lines call; returns its n_lines."""
+        check(lib().gain_lines_wait(self.h))
+        pend = getattr(self, "_pending_lines", None)
+        self._pending_lines = None
+        return pend[0].value if pend else 0
+
     def amp_device(self):
         p, ld = ctypes.c_void_p(), ctypes.c_int()
         check(lib().gain_pair_amp_device(self.h, ctypes.byref(p), ctypes.byref(ld)))
@@ -490,10 +500,11 @@ class Engine:
 
     def lines(self, eI, eF, jI, jF, temperature=296.0, q_part=1.0, zpe=0.0, thresh=0.0,
               freq=(-1e9, 1e9), gnsF=1.0, intensity=True, want=("S", "A", "I", "keep"),
-              out_S=None, out_A=None, ndeg=(1, 1), reduced=False):
+              out_S=None, out_A=None, ndeg=(1, 1), reduced=False, asynchronous=False):
         """S, A (and I, keep) of the last run; out_S / out_A may be preallocated (e.g. pinned)
         contiguous float64 arrays of nlower*nupper elements.  ndeg=(ndegI, ndegF) above 1
-        combines the component slots of the last job."""
+        combines the component slots of the last job.  asynchronous=True queues the copies
+        (gain_pair_lines_async): the arrays and n_lines are complete after lines_wait()."""
         eI, eF = _f64(eI), _f64(eF)
         n = self._shape[0] * self._shape[1]
         prm = LineParams(temperature, q_part, zpe, thresh, freq[0], freq[1], gnsF, ndeg[0], ndeg[1], int(reduced))
@@ -502,7 +513,10 @@ class Engine:
         I = np.empty(n) if (intensity and "I" in want) else None
         K = np.empty(n, np.uint8) if "keep" in want else None
         nl = ctypes.c_longlong()
-        check(lib().gain_pair_lines(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF,
+        fn = lib().gain_pair_lines_async if asynchronous else lib().gain_pair_lines
+        if asynchronous:
+            self._pending_lines = (nl, eI, eF)   # kept alive until the copies land
+        check(fn(self.h, ctypes.byref(prm), _p(eI, _dp), _p(eF, _dp), jI, jF,
                                     _p(S, _dp) if S is not None else None,
                                     _p(A, _dp) if A is not None else None,
                                     _p(I, _dp) if I is not None else None,

@@ -301,6 +301,17 @@ gain_status gain_pair_lines(gain_engine e, const gain_line_params* prm, const do
                             const double* energiesF, int jI, int jF, double* S, double* A,
                             double* I, unsigned char* keep, long long* n_lines);
 
+/* gain_pair_lines without waiting: the line kernel is queued after the last run and its
+ * copies into the host arrays (page-locked ones for a true overlap) run on a stream of their
+ * own, so the engine's next uploads and run overlap them.  The arrays and *n_lines are
+ * complete when gain_lines_wait returns; the next line assembly or text call on the engine,
+ * and gain_engine_destroy, wait for them first. */
+gain_status gain_pair_lines_async(gain_engine e, const gain_line_params* prm, const double* energiesI,
+                                  const double* energiesF, int jI, int jF, double* S, double* A,
+                                  double* I, unsigned char* keep, long long* n_lines);
+/* Wait for the copies of the last gain_pair_lines_async (immediate when none is pending). */
+gain_status gain_lines_wait(gain_engine e);
+
 /* Line-list text of the last run, built on the device: every line gain_pair_lines keeps,
  * written exactly as Output::OutputLinestrength prints it (BaseClasses/Output.cpp:99-111:
  * "%12.6f %8d %4d %4d <- %8d %4d %4d %16.9E " [intensity "%16.9E "] [ "[ " " %16.9E" " ] " ]

@@ -127,3 +127,29 @@ def test_text_into_host_buffer_in_several_parts(built_lib):
     out = np.zeros(len(ref), np.uint8)
     got, n2 = eng.lines_text_host(bI.energies, bF.energies, 7, 8, 0, 1, out)
     assert n2 == n and bytes(got) == bytes(ref)
+
+
+def test_async_lines_equal_sync_and_overlap_the_next_run(pair_run):
+    """gain_pair_lines_async gives gain_pair_lines' S, A and count once gain_lines_wait
+    returns, also when the engine's next run was started before the wait."""
+    import gainls
+    import torch
+    p, eng, lo, up, eI, eF = pair_run
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    want = eng.lines(eI, eF, 2, 3, intensity=False, want=("S", "A"))
+    n = len(lo) * len(up)
+    S = torch.zeros(n, dtype=torch.float64).pin_memory().numpy()
+    A = torch.zeros(n, dtype=torch.float64).pin_memory().numpy()
+    eng.lines(eI, eF, 2, 3, intensity=False, want=("S", "A"), out_S=S, out_A=A, asynchronous=True)
+    eng.run_pair(0, 0, 1, 1, lo[:2], up, gainls.PATH_PLAIN_FP64)   # the next run, before the wait
+    nl = eng.lines_wait()
+    assert nl == want["n_lines"]
+    assert np.array_equal(S.reshape(want["S"].shape), want["S"])
+    assert np.array_equal(A.reshape(want["A"].shape), want["A"])
+    assert eng.lines_wait() == 0   # nothing pending
+    # a synchronous call after an asynchronous one waits for it first
+    eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    eng.lines(eI, eF, 2, 3, intensity=False, want=("S", "A"), out_S=S, out_A=A, asynchronous=True)
+    again = eng.lines(eI, eF, 2, 3, intensity=False, want=("S", "A"))
+    assert np.array_equal(again["S"], want["S"])
+    assert np.array_equal(S.reshape(want["S"].shape), want["S"])
