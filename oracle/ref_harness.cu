@@ -82,6 +82,7 @@ struct refh_pair {
     int nlower, nupper;
     const double* vec_lower;
     const double* vec_upper;
+    int idegI, idegF, sdegI, sdegF;   // degenerate components and degeneracies (0 reads as 1)
 };
 
 const char* refh_error(void) { return g_err; }
@@ -120,10 +121,11 @@ int refh_run_pair(const refh_pair* p, double* amp, double* hls, double* seconds)
         upload(&d_kbI, p->kblockI, p->jI + 1) ||
         upload(&d_ijI, p->ijtermsI, (size_t)p->maxcoeffI * p->nsymI) ||
         upload(&d_ctI, p->icontrI, (size_t)2 * p->dimenI) || upload(&d_NI, p->NI, p->maxcoeffI) ||
-        upload(&d_rpI, p->represI, (size_t)p->NtotI * p->matsizeI) ||
+        upload(&d_rpI, p->represI, (size_t)p->NtotI * (p->sdegI > 0 ? p->sdegI : 1) * p->matsizeI) ||
         upload(&d_ijF, p->ijtermsF, (size_t)p->maxcoeffF * p->nsymF) ||
         upload(&d_ctF, p->icontrF, (size_t)2 * p->dimenF) || upload(&d_NF, p->NF, p->maxcoeffF) ||
-        upload(&d_rpF, p->represF, (size_t)p->NtotF * p->matsizeF) || upload(&d_dip, p->dipole_me, dipn) ||
+        upload(&d_rpF, p->represF, (size_t)p->NtotF * (p->sdegF > 0 ? p->sdegF : 1) * p->matsizeF) ||
+        upload(&d_dip, p->dipole_me, dipn) ||
         upload(&d_3j, p->threej, nj))
         return -1;
     RT(cudaMalloc(&d_vecI, sizeof(double) * p->NtotI));
@@ -153,7 +155,8 @@ int refh_run_pair(const refh_pair* p, double* amp, double* hls, double* seconds)
                       cudaMemcpyHostToDevice));
         RT(cudaMemset(d_hls, 0, sizeof(double) * p->dimenF));
         {
-            int dimen = p->dimenI, g = p->gammaI, mc = p->maxcoeffI, ideg = 0, sdeg = 1, nt = p->NtotI;
+            int dimen = p->dimenI, g = p->gammaI, mc = p->maxcoeffI, ideg = p->idegI,
+                sdeg = p->sdegI > 0 ? p->sdegI : 1, nt = p->NtotI;
             void* args[] = {&dimen, &g, &mc, &ideg, &sdeg, &nt, &d_ijI, &d_ctI, &d_NI, &d_rpI, &d_vecI, &d_primI};
             DRV(cuLaunchKernel(g_expand, (dimen + 511) / 512, 1, 1, 512, 1, 1, 0, st, args, nullptr));
         }
@@ -174,7 +177,8 @@ int refh_run_pair(const refh_pair* p, double* amp, double* hls, double* seconds)
         for (int u = 0; u < p->nupper; u++) {
             memcpy(h_vecF, p->vec_upper + (size_t)u * p->NtotF, sizeof(double) * p->NtotF);
             RT(cudaMemcpyAsync(d_vecF, h_vecF, sizeof(double) * p->NtotF, cudaMemcpyHostToDevice, st));
-            int dimen = p->dimenF, g = p->gammaF, mc = p->maxcoeffF, ideg = 0, sdeg = 1, nt = p->NtotF;
+            int dimen = p->dimenF, g = p->gammaF, mc = p->maxcoeffF, ideg = p->idegF,
+                sdeg = p->sdegF > 0 ? p->sdegF : 1, nt = p->NtotF;
             void* args[] = {&dimen, &g, &mc, &ideg, &sdeg, &nt, &d_ijF, &d_ctF, &d_NF, &d_rpF, &d_vecF, &d_primF};
             DRV(cuLaunchKernel(g_expand, (dimen + 511) / 512, 1, 1, 512, 1, 1, 0, st, args, nullptr));
             if (cublasDdot(h, p->dimenF, d_primF, 1, d_hls, 1, d_res) != CUBLAS_STATUS_SUCCESS) {

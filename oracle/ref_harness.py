@@ -34,7 +34,8 @@ class RefhPair(ctypes.Structure):
          ("ijtermsF", _ip), ("icontrF", _ip), ("NF", _ip), ("represF", _dp), ("dipole_me", _dp)] + \
         [(n, ctypes.c_int) for n in ("dip_stride", "startFblock", "endFblock", "ncontrF")] + \
         [("threej", _dp), ("nlower", ctypes.c_int), ("nupper", ctypes.c_int), ("vec_lower", _dp),
-         ("vec_upper", _dp)]
+         ("vec_upper", _dp)] + \
+        [(n, ctypes.c_int) for n in ("idegI", "idegF", "sdegI", "sdegF")]
 
 
 def available() -> bool:
@@ -74,8 +75,9 @@ def lib():
 
 
 def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, threej, jmax,
-             dipole_block=None, vec_lower=None, vec_upper=None):
-    """(amp [nl, nu], half_ls [nl, dimenF], seconds of the per-transition loop)."""
+             dipole_block=None, vec_lower=None, vec_upper=None, components=(0, 0)):
+    """(amp [nl, nu], half_ls [nl, dimenF], seconds of the per-transition loop); components =
+    (idegI, idegF), the degenerate components the expansions take."""
     p = problem
     bI, bF = p.bases[jindI], p.bases[jindF]
     iI, iF = p.infl[jindI], p.infl[jindF]
@@ -107,15 +109,19 @@ def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, 
     s.NtotI, s.NtotF = int(iI.Ntot[gammaI]), int(iF.Ntot[gammaF])
     s.nsymI, s.nsymF = len(iI.N), len(iF.N)
     s.matsizeI, s.matsizeF = int(getattr(iI, "matsize", 1)), int(getattr(iF, "matsize", 1))
+    s.idegI, s.idegF = int(components[0]), int(components[1])
+    s.sdegI, s.sdegF = int(iI.sdeg[gammaI]), int(iF.sdeg[gammaF])
+    if not (0 <= s.idegI < s.sdegI and 0 <= s.idegF < s.sdegF):
+        raise ValueError("components outside the degeneracies")
     # every expansion entry the reference kernel reads lies inside the uploaded tables
-    for inf, g, b, ms in ((iI, gammaI, bI, s.matsizeI), (iF, gammaF, bF, s.matsizeF)):
+    for inf, g, b, ms, sd in ((iI, gammaI, bI, s.matsizeI, s.sdegI), (iF, gammaF, bF, s.matsizeF, s.sdegF)):
         d = b.dimen
         irow, ib = np.asarray(inf.icontr[:d]), np.asarray(inf.icontr[d:2 * d])
         n = np.asarray(inf.N[g])[irow]
         it = np.asarray(inf.ijterms)[irow + g * inf.maxcoeff]
         used = n > 0
         if (np.any(irow < 0) or np.any(irow >= inf.maxcoeff) or np.any(ib[used] >= ms) or np.any(ib < 0)
-                or np.any(it[used] + n[used] > int(inf.Ntot[g])) or len(inf.repres[g]) < int(inf.Ntot[g]) * ms):
+                or np.any(it[used] + n[used] > int(inf.Ntot[g])) or len(inf.repres[g]) < int(inf.Ntot[g]) * sd * ms):
             raise ValueError("expansion tables outside their ranges")
     s.ijtermsI, s.icontrI, s.NI, s.represI = I(iI.ijterms), I(iI.icontr), I(iI.N[gammaI]), D(iI.repres[gammaI])
     s.ijtermsF, s.icontrF, s.NF, s.represF = I(iF.ijterms), I(iF.icontr), I(iF.N[gammaF]), D(iF.repres[gammaF])

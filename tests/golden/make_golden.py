@@ -11,7 +11,7 @@ Each fixture stores the exact inputs that are not pure integer tables (eigenvect
 dipole piece, 3j table) next to the reference outputs (half_ls per lower state and the
 amplitudes), so the CPU tests can replay them anywhere.
 
-    python tests/golden/make_golden.py OUTDIR [rotsym|mixed]   # needs a GPU and the reference cubin
+    python tests/golden/make_golden.py OUTDIR [rotsym|mixed|degenerate]   # needs a GPU and the reference cubin
 """
 from __future__ import annotations
 
@@ -41,10 +41,24 @@ CASES = {
     "c4m_dJ0_blocked": (16, [2, 3], "c4m", (3, 2), (3, 3), None, None, (3, 12)),
 }
 MIXED = ("c4m_dJp1", "c4m_dJ0_blocked")
+# degenerate symmetries (synth rule c3e: A1, A2, E): every component pair (idegI, idegF) of an
+# E -> E pair, and an A1 -> A2 pair of the same tables; name -> case, components
+DEGENERATE = {
+    "c3e_EE_c00": ((12, [2, 3], "c3e", (2, 2), (3, 2), None, None, None), (0, 0)),
+    "c3e_EE_c10": ((12, [2, 3], "c3e", (2, 2), (3, 2), None, None, None), (1, 0)),
+    "c3e_EE_c01": ((12, [2, 3], "c3e", (2, 2), (3, 2), None, None, None), (0, 1)),
+    "c3e_EE_c11_blocked": ((12, [2, 3], "c3e", (2, 2), (3, 2), None, None, (2, 9)), (1, 1)),
+    "c3e_A1A2": ((12, [2, 3], "c3e", (3, 0), (2, 1), None, None, None), (0, 0)),
+}
 
 
 def make_case(name, jmax=11):
-    nv, jvals, rule, (JI, gI), (JF, gF), lo, up, blk = CASES[name]
+    comps = (0, 0)
+    if name in DEGENERATE:
+        case, comps = DEGENERATE[name]
+    else:
+        case = CASES[name]
+    nv, jvals, rule, (JI, gI), (JF, gF), lo, up, blk = case
     p = synth.make_problem(nv, jvals, rule, blocks=[(JI, gI), (JF, gF)])
     jI, jF = jvals.index(JI), jvals.index(JF)
     nI = p.blocks[(jI, gI)].vecs.shape[0]
@@ -55,8 +69,9 @@ def make_case(name, jmax=11):
     vl = p.blocks[(jI, gI)].vecs[lo]
     vu = p.blocks[(jF, gF)].vecs[up]
     amp, hls, _ = ref_harness.run_pair(p, jI, gI, jF, gF, lo, up, tj, jmax, dipole_block=blk,
-                                       vec_lower=vl, vec_upper=vu)
+                                       vec_lower=vl, vec_upper=vu, components=comps)
     return dict(nv=nv, jvals=np.array(jvals), rule=rule, JI=JI, gI=gI, JF=JF, gF=gF,
+                idegI=comps[0], idegF=comps[1],
                 lower=np.array(lo), upper=np.array(up), block=np.array(blk if blk else (0, nv)),
                 jmax=jmax, threej=tj, dipole=p.dipole, vec_lower=vl, vec_upper=vu,
                 ref_hls=hls, ref_amp=amp)
@@ -103,6 +118,12 @@ if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "mixed":    # only the mixing-expansion fixtures
         os.makedirs(out, exist_ok=True)
         for name in MIXED:
+            d = make_case(name)
+            np.savez_compressed(os.path.join(out, name + ".npz"), **d)
+            print(name, d["ref_hls"].shape, d["ref_amp"].shape, float(np.abs(d["ref_amp"]).max()))
+    elif len(sys.argv) > 2 and sys.argv[2] == "degenerate":   # only the degenerate fixtures
+        os.makedirs(out, exist_ok=True)
+        for name in DEGENERATE:
             d = make_case(name)
             np.savez_compressed(os.path.join(out, name + ".npz"), **d)
             print(name, d["ref_hls"].shape, d["ref_amp"].shape, float(np.abs(d["ref_amp"]).max()))

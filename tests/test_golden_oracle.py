@@ -26,9 +26,15 @@ def _problem(d):
     return jvals, bases, infl
 
 
+def _components(d):
+    """(idegI, idegF) of a fixture (0, 0 for the non-degenerate ones)."""
+    return (int(d["idegI"]), int(d["idegF"])) if "idegI" in d.files else (0, 0)
+
+
 def test_fixtures_present():
     names = {os.path.basename(f)[:-4] for f in FIXTURES}
     assert {"cfg1_small", "c4_dJp1", "c4_dJm1", "c4_dJ0", "c4_highJ", "full_blocked"} <= names
+    assert {"c3e_EE_c00", "c3e_EE_c10", "c3e_EE_c01", "c3e_EE_c11_blocked", "c3e_A1A2"} <= names
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=lambda p: os.path.basename(p)[:-4])
@@ -50,11 +56,12 @@ def test_oracle_half_ls_bit_exact(oracle_lib, path):
     jvals, bases, infl = _problem(d)
     jI, jF = jvals.index(int(d["JI"])), jvals.index(int(d["JF"]))
     gI = int(d["gI"])
+    dI, _ = _components(d)
     s, e = (int(x) for x in d["block"])
     piece = np.ascontiguousarray(d["dipole"][:, :, s:e])
     nbad = 0
     for l in range(d["vec_lower"].shape[0]):
-        prim = oracle.expand(infl[jI], gI, d["vec_lower"][l])
+        prim = oracle.expand(infl[jI], gI, d["vec_lower"][l], ideg=dI)
         hls = np.zeros(bases[jF].dimen)
         for kF in range(bases[jF].J + 1):
             oracle.hls_kblock(int(bases[jF].kblock[kF]), bases[jI].dimen, bases[jI].J, bases[jF].J, kF,
@@ -72,10 +79,11 @@ def test_oracle_amplitudes_within_dot_bound(oracle_lib, path):
     jvals, bases, infl = _problem(d)
     jI, jF = jvals.index(int(d["JI"])), jvals.index(int(d["JF"]))
     gI, gF = int(d["gI"]), int(d["gF"])
+    _, dF = _components(d)
     for l in range(d["vec_lower"].shape[0]):
         h = d["ref_hls"][l]
         for u in range(d["vec_upper"].shape[0]):
-            prim = oracle.expand(infl[jF], gF, d["vec_upper"][u])
+            prim = oracle.expand(infl[jF], gF, d["vec_upper"][u], ideg=dF)
             a = oracle.dot(prim, h, oracle.DD)
             bound = 2 * len(h) * 1.12e-16 * float(np.sum(np.abs(prim * h))) + 1e-300
             assert abs(a - d["ref_amp"][l, u]) <= bound

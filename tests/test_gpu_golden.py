@@ -31,12 +31,13 @@ def test_dropin_hls_bit_exact_vs_reference_kernel(built_lib, path):
     jI, jF = jvals.index(int(d["JI"])), jvals.index(int(d["JF"]))
     bI, bF = bases[jI], bases[jF]
     gI = int(d["gI"])
+    dI = int(d["idegI"]) if "idegI" in d.files else 0
     s, e = (int(x) for x in d["block"])
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
     keep = [dev(x) for x in (bI.tau, bF.tau, bI.vib, bF.vib, bI.kblock,
                              np.ascontiguousarray(d["dipole"][:, :, s:e]).reshape(-1), d["threej"])]
     for l in range(d["vec_lower"].shape[0]):
-        prim = dev(oracle.expand(infl[jI], gI, d["vec_lower"][l]))
+        prim = dev(oracle.expand(infl[jI], gI, d["vec_lower"][l], ideg=dI))
         out = torch.zeros(bF.dimen, dtype=torch.float64, device="cuda")
         for kF in range(bF.J + 1):
             gainls.hls_kblock(int(bF.kblock[kF]), bI.dimen, bI.J, bF.J, kF, *[k.data_ptr() for k in keep[:4]],
@@ -53,7 +54,7 @@ def _engine_for(d):
     nv, jvals, rule, bases, infl = _problem(d)
     jI, jF = jvals.index(int(d["JI"])), jvals.index(int(d["JF"]))
     gI, gF = int(d["gI"]), int(d["gF"])
-    eng = gainls.Engine(int(d["jmax"]), len(infl[0].N), 1)
+    eng = gainls.Engine(int(d["jmax"]), len(infl[0].N), int(max(int(x) for x in infl[0].sdeg)))
     for jind, b in enumerate(bases):
         eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
         inf = infl[jind]
@@ -72,11 +73,12 @@ def test_engine_paths_vs_reference_amplitudes(built_lib, path):
     d = np.load(path)
     eng, (jI, gI, jF, gF) = _engine_for(d)
     ref = d["ref_amp"]
+    comps = (int(d["idegI"]), int(d["idegF"])) if "idegI" in d.files else None
     lo, up = list(range(ref.shape[0])), list(range(ref.shape[1]))
-    eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_PLAIN_FP64)
+    eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_PLAIN_FP64, components=comps)
     plain = eng.fetch_amp().copy()
     assert np.max(np.abs(plain - ref)) <= 1e-13 * np.abs(ref).max()
-    st = eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_SPLIT)
+    st = eng.run_pair(jI, gI, jF, gF, lo, up, gainls.PATH_SPLIT, components=comps)
     split = eng.fetch_amp()
     assert st["uncertified"] == 0
     S, Sr = split ** 2, ref ** 2
