@@ -18,11 +18,11 @@ __device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1
 
 template <class T>
 __global__ void k_adj_scale(int rows, int cols, const double* __restrict__ dLdS, const double* __restrict__ amp,
-                            long ld_amp, T* __restrict__ G) {
+                            long ld_amp, double two_scale, T* __restrict__ G) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long)rows * cols) return;
     const long r = i / cols, c = i - r * cols;
-    G[i] = (T)2 * (T)dLdS[i] * (T)amp[r * ld_amp + c];
+    G[i] = (T)two_scale * (T)dLdS[i] * (T)amp[r * ld_amp + c];
 }
 
 // Register-tiled SIMT product: 64 x 64 output tiles, 16 x 16 threads, each thread the 4 x 4
@@ -159,15 +159,15 @@ k_adj_dm(AdjArgs a, const int2* __restrict__ tiles) {
 
 }  // namespace
 
-cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, void* G,
-                             bool fp32, cudaStream_t st) {
+cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp,
+                             double two_scale, void* G, bool fp32, cudaStream_t st) {
     const long n = (long)rows * cols;
     if (n <= 0) return cudaSuccess;
     const unsigned nblk = (unsigned)((n + 255) / 256);
     if (fp32)
-        k_adj_scale<float><<<nblk, 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, static_cast<float*>(G));
+        k_adj_scale<float><<<nblk, 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, two_scale, static_cast<float*>(G));
     else
-        k_adj_scale<double><<<nblk, 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, static_cast<double*>(G));
+        k_adj_scale<double><<<nblk, 256, 0, st>>>(rows, cols, dLdS, amp, ld_amp, two_scale, static_cast<double*>(G));
     return cudaGetLastError();
 }
 

@@ -1856,27 +1856,13 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
     return gain_adjoint_pair_prec(e, job, dL_dS, dL_dmu, GAIN_ADJOINT_FP64, stats);
 }
 
-gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
-                                   gain_adjoint_precision prec, gain_stats* stats) {
-    clear_error();
-    if (prec != GAIN_ADJOINT_FP64 && prec != GAIN_ADJOINT_FP32)
-        return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair_prec: unknown precision %d", (int)prec);
-    const bool f32 = prec == GAIN_ADJOINT_FP32;
-    GAIN_TRY(check_engine(e));
-    GAIN_TRY(validate_job(e, job));
-    if (!dL_dS || !dL_dmu) return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair: NULL argument");
-    if (e && e->pieces.size() > 1)
-        return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: upload the dipole as one piece");
-    if (e->infl[job->jindI].sdeg[job->gammaI] != 1 || e->infl[job->jindF].sdeg[job->gammaF] != 1)
-        return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: non-degenerate symmetries only");
-    // forward amplitudes: those of the last run when it computed this job (either path),
-    // else the plain FP64 path (the reference's method)
-    if (!(e->have_amp && e->amp_job == job_key(job))) {
-        e->have_amp = false;
-        e->amp_job.clear();
-        GAIN_TRY(run_plain(e, job, 0, 0, nullptr));
-        e->amp_job = job_key(job);
-    }
+namespace {
+// dL/dmu of one block pair through the adjoint chain, summed over the component pairs comps
+// (one pair, (0, 0), for non-degenerate symmetries) with dS/damp = 2 scale amp.  Each pair's
+// forward amplitudes: the last run's when it computed this job and pair, a component slot of
+// the job, else the plain FP64 path (the reference's method).
+gain_status adjoint_run(gain_engine e, const gain_pair_job* job, const std::vector<std::pair<int, int>>& comps,
+                        double scale, const double* dL_dS, double* dL_dmu, bool f32, gain_stats* stats) {
     const Basis& bI = e->bases[job->jindI];
     const Basis& bF = e->bases[job->jindF];
     Inflation& iI = e->infl[job->jindI];
@@ -1929,65 +1915,91 @@ gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, cons
     void* dH = e->adj_dH.p;
     void* dh = e->adj_dh.p;
     void* vp = e->adj_vp.p;
-    GAIN_CUDA(cudaEventRecord(e->ev[0], st));
-    // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dL/dH
-    GAIN_CUDA(launch_adj_scale(B, Nu, e->adj_dLdS.p, e->amp.p, e->amp_ld, G, f32, st));
-    GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, G, Nu, EF.d.p, EF.nsize, e->d_upper.p, dH, NtF, f32, st));
-    const int* repF_N = iF.dN[job->gammaF]->p;
-    const double* repF = iF.drepres[job->gammaF]->p;
-    const int* repI_N = iI.dN[job->gammaI]->p;
-    const double* repI = iI.drepres[job->gammaI]->p;
-    if (f32) {
-        GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF,
-                                       iF.dijterms.p, iF.dicontr.p, repF_N, repF, (const float*)dH, NtF,
-                                       e->adj_iota.p, (float*)dh, bF.dimen, B, st));
-        GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, 0, iI.sdeg[job->gammaI],
-                                       iI.Ntot[job->gammaI], iI.dijterms.p, iI.dicontr.p, repI_N, repI, EI.d.p,
-                                       EI.nsize, e->d_lower.p, (float*)vp, bI.dimen, B, st));
-    } else {
-        GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, 0, iF.sdeg[job->gammaF], NtF,
-                                       iF.dijterms.p, iF.dicontr.p, repF_N, repF, (const double*)dH, NtF,
-                                       e->adj_iota.p, (double*)dh, bF.dimen, B, st));
-        // lower vectors in primitive space
-        GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, 0, iI.sdeg[job->gammaI],
-                                       iI.Ntot[job->gammaI], iI.dijterms.p, iI.dicontr.p, repI_N, repI, EI.d.p,
-                                       EI.nsize, e->d_lower.p, (double*)vp, bI.dimen, B, st));
+    const std::vector<int> key = job_key(job);
+    double chain_ms = 0.0;
+    for (const auto& c : comps) {
+        const int dI = c.first, dF = c.second;
+        const double* amp = nullptr;
+        long ld_amp = 0;
+        const int slot = dI + dF * e->maxdeg;
+        if (e->have_amp && e->amp_job == job_key(job, dI, dF)) {
+            amp = e->amp.p;
+            ld_amp = e->amp_ld;
+        } else if (e->deg_job == key && (e->deg_filled & (1u << slot))) {
+            amp = e->deg_amp.p + (size_t)slot * nS;
+            ld_amp = Nu;
+        } else {
+            e->have_amp = false;
+            e->amp_job.clear();
+            GAIN_TRY(run_plain(e, job, dI, dF, nullptr));
+            e->amp_job = job_key(job, dI, dF);
+            amp = e->amp.p;
+            ld_amp = e->amp_ld;
+        }
+        GAIN_CUDA(cudaEventRecord(e->ev[2], st));
+        // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dL/dH
+        GAIN_CUDA(launch_adj_scale(B, Nu, e->adj_dLdS.p, amp, ld_amp, 2.0 * scale, G, f32, st));
+        GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, G, Nu, EF.d.p, EF.nsize, e->d_upper.p, dH, NtF, f32, st));
+        const int* repF_N = iF.dN[job->gammaF]->p;
+        const double* repF = iF.drepres[job->gammaF]->p;
+        const int* repI_N = iI.dN[job->gammaI]->p;
+        const double* repI = iI.drepres[job->gammaI]->p;
+        if (f32) {
+            GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, dF, iF.sdeg[job->gammaF], NtF,
+                                           iF.dijterms.p, iF.dicontr.p, repF_N, repF, (const float*)dH, NtF,
+                                           e->adj_iota.p, (float*)dh, bF.dimen, B, st));
+            GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, dI, iI.sdeg[job->gammaI],
+                                           iI.Ntot[job->gammaI], iI.dijterms.p, iI.dicontr.p, repI_N, repI, EI.d.p,
+                                           EI.nsize, e->d_lower.p, (float*)vp, bI.dimen, B, st));
+        } else {
+            GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, dF, iF.sdeg[job->gammaF], NtF,
+                                           iF.dijterms.p, iF.dicontr.p, repF_N, repF, (const double*)dH, NtF,
+                                           e->adj_iota.p, (double*)dh, bF.dimen, B, st));
+            // lower vectors in primitive space
+            GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, dI, iI.sdeg[job->gammaI],
+                                           iI.Ntot[job->gammaI], iI.dijterms.p, iI.dicontr.p, repI_N, repI, EI.d.p,
+                                           EI.nsize, e->d_lower.p, (double*)vp, bI.dimen, B, st));
+        }
+        // dL/dmu from the band (or dense) products
+        AdjArgs a;
+        memset(&a, 0, sizeof a);
+        a.dimF = bF.dimen;
+        a.dimI = bI.dimen;
+        a.nb = B;
+        a.vibF = bF.dvib.p;
+        a.vibI = bI.dvib.p;
+        a.KF = bF.dK.p;
+        a.KI = bI.dK.p;
+        a.tauF = bF.dtau.p;
+        a.tauI = bI.dtau.p;
+        a.levF = bF.dlev.p;
+        a.levI = bI.dlev.p;
+        a.jI = bI.J;
+        a.jF = bF.J;
+        a.jmax = e->jmax;
+        a.threej = e->d3j.p;
+        if (wt) {
+            a.wigner = wt->rot.p;
+            a.nlevelI = wt->nI;
+            a.nlevelF = wt->nF;
+            a.maxdeg = wt->maxdeg;
+        }
+        a.startF = e->startF;
+        a.endF = e->endF;
+        a.ncontrF = e->ncontrF;
+        a.dipN = e->dipN;
+        a.dh = dh;
+        a.ld_dh = bF.dimen;
+        a.vp = vp;
+        a.ld_vp = bI.dimen;
+        a.dmu = e->adj_dmu.p;
+        GAIN_CUDA(launch_adj_dm(a, e->adj_tiles.p, (int)(tiles.size() / 2), f32, st));
+        GAIN_CUDA(cudaEventRecord(e->ev[3], st));
+        GAIN_CUDA(cudaEventSynchronize(e->ev[3]));
+        float ms = 0.f;
+        GAIN_CUDA(cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]));
+        chain_ms += ms;
     }
-    // dL/dmu from the band (or dense) products
-    AdjArgs a;
-    memset(&a, 0, sizeof a);
-    a.dimF = bF.dimen;
-    a.dimI = bI.dimen;
-    a.nb = B;
-    a.vibF = bF.dvib.p;
-    a.vibI = bI.dvib.p;
-    a.KF = bF.dK.p;
-    a.KI = bI.dK.p;
-    a.tauF = bF.dtau.p;
-    a.tauI = bI.dtau.p;
-    a.levF = bF.dlev.p;
-    a.levI = bI.dlev.p;
-    a.jI = bI.J;
-    a.jF = bF.J;
-    a.jmax = e->jmax;
-    a.threej = e->d3j.p;
-    if (wt) {
-        a.wigner = wt->rot.p;
-        a.nlevelI = wt->nI;
-        a.nlevelF = wt->nF;
-        a.maxdeg = wt->maxdeg;
-    }
-    a.startF = e->startF;
-    a.endF = e->endF;
-    a.ncontrF = e->ncontrF;
-    a.dipN = e->dipN;
-    a.dh = dh;
-    a.ld_dh = bF.dimen;
-    a.vp = vp;
-    a.ld_vp = bI.dimen;
-    a.dmu = e->adj_dmu.p;
-    GAIN_CUDA(launch_adj_dm(a, e->adj_tiles.p, (int)(tiles.size() / 2), f32, st));
-    GAIN_CUDA(cudaEventRecord(e->ev[1], st));
     if (f32) {
         std::vector<float> h(nmu);
         GAIN_CUDA(cudaMemcpyAsync(h.data(), e->adj_dmu.p, sizeof(float) * nmu, cudaMemcpyDeviceToHost, st));
@@ -2001,14 +2013,56 @@ gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, cons
     }
     if (stats) {
         memset(stats, 0, sizeof *stats);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]);
-        stats->device_ms = ms;
+        stats->device_ms = chain_ms;
         stats->rows = B;
         stats->cols = Nu;
-        stats->kernel_launches = 5;
+        stats->kernel_launches = 5 * (int)comps.size();
     }
     return GAIN_OK;
+}
+
+gain_status adjoint_checks(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
+                           gain_adjoint_precision prec) {
+    if (prec != GAIN_ADJOINT_FP64 && prec != GAIN_ADJOINT_FP32)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair_prec: unknown precision %d", (int)prec);
+    GAIN_TRY(check_engine(e));
+    GAIN_TRY(validate_job(e, job));
+    if (!dL_dS || !dL_dmu) return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair: NULL argument");
+    if (e->pieces.size() > 1)
+        return set_error(GAIN_ERR_UNSUPPORTED, "gain_adjoint_pair: upload the dipole as one piece");
+    return GAIN_OK;
+}
+}  // namespace
+
+gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
+                                   gain_adjoint_precision prec, gain_stats* stats) {
+    clear_error();
+    GAIN_TRY(adjoint_checks(e, job, dL_dS, dL_dmu, prec));
+    if (e->infl[job->jindI].sdeg[job->gammaI] != 1 || e->infl[job->jindF].sdeg[job->gammaF] != 1)
+        return set_error(GAIN_ERR_UNSUPPORTED,
+                         "gain_adjoint_pair: degenerate symmetries go through gain_adjoint_pair_degenerate");
+    return adjoint_run(e, job, {{0, 0}}, 1.0, dL_dS, dL_dmu, prec == GAIN_ADJOINT_FP32, stats);
+}
+
+gain_status gain_adjoint_pair_degenerate(gain_engine e, const gain_pair_job* job, const gain_filters* f,
+                                         const double* dL_dS, double* dL_dmu, gain_adjoint_precision prec,
+                                         gain_stats* stats) {
+    clear_error();
+    GAIN_TRY(adjoint_checks(e, job, dL_dS, dL_dmu, prec));
+    if (!f || !f->sym_degen || f->nsym != e->nsym)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair_degenerate: filters of %d symmetries needed",
+                         e->nsym);
+    const int nI = f->sym_degen[job->gammaI], nF = f->sym_degen[job->gammaF];
+    if (nI != e->infl[job->jindI].sdeg[job->gammaI] || nF != e->infl[job->jindF].sdeg[job->gammaF])
+        return set_error(GAIN_ERR_INVALID_ARG, "sym_degen differs from the expansion tables' degeneracies");
+    std::vector<std::pair<int, int>> comps;
+    for (int dF = 0; dF < nF; ++dF)
+        for (int dI = 0; dI < nI; ++dI)
+            if (gain_degeneracy_filter(f, job->gammaI, job->gammaF, dI, dF)) comps.push_back({dI, dF});
+    if (comps.empty()) return set_error(GAIN_ERR_INVALID_ARG, "no component pair passes the degeneracy filter");
+    // S = sum amp^2 / ndegI, times ndegI when reduced and both states are degenerate
+    const double scale = (f->reduced && nI != 1 && nF != 1) ? 1.0 : 1.0 / nI;
+    return adjoint_run(e, job, comps, scale, dL_dS, dL_dmu, prec == GAIN_ADJOINT_FP32, stats);
 }
 
 namespace {

@@ -59,9 +59,9 @@ struct AdjArgs {
     long ld_vp;
     void* dmu;                                 // [3][dipN][ncontrF] accumulated
 };
-// G = 2 dL/dS amp in double or float
-cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp, void* G,
-                             bool fp32, cudaStream_t st);
+// G = two_scale dL/dS amp in double or float
+cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp,
+                             double two_scale, void* G, bool fp32, cudaStream_t st);
 // C = A U[levels]: A and C double or float, the FP64 eigenvectors rounded to the chain's precision
 cudaError_t launch_adj_gemm(int M, int N, int K, const void* A, long lda, const double* B, long ldb,
                             const int* levels, void* C, long ldc, bool fp32, cudaStream_t st);

@@ -193,6 +193,8 @@ def _declare(L):
     L.gain_upload_wigner.argtypes = [_vp, I, I, I, I, I, _dp]
     L.gain_adjoint_pair.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.POINTER(Stats)]
     L.gain_adjoint_pair_prec.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.c_int, ctypes.POINTER(Stats)]
+    L.gain_adjoint_pair_degenerate.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.POINTER(Filters), _dp, _dp,
+                                               ctypes.c_int, ctypes.POINTER(Stats)]
     L.gain_run_plan.argtypes = [ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int,
                                 ctypes.POINTER(SplitOpts), JOB_DONE_FN, _vp, ctypes.POINTER(Stats)]
     L.gain_run_pair_component.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -259,7 +261,7 @@ def _declare(L):
                  "gain_engine_destroy", "gain_upload_basis", "gain_upload_inflation", "gain_upload_dipole",
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair",
                  "gain_adjoint_pair_prec", "gain_run_pair", "gain_run_pair_component", "gain_run_pair_degenerate",
-                 "gain_run_plan", "gain_pair_amp_device", "gain_fetch_amp",
+                 "gain_run_plan", "gain_adjoint_pair_degenerate", "gain_pair_amp_device", "gain_fetch_amp",
                  "gain_pair_lines", "gain_pair_lines_async", "gain_lines_wait", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
                  "gain_lines_text_device",
                  "gain_format_values_device"):
@@ -460,7 +462,7 @@ class Engine:
         return out
 
     def adjoint(self, jindI, gammaI, jindF, gammaF, lower_levels, upper_levels, dL_dS, dL_dmu=None,
-                precision="f64"):
+                precision="f64", filters=None):
         """dL/dmu (the dipole piece's layout [3][N][ncontrF], accumulated into dL_dmu if given)
         of a loss with gradient dL_dS [nlower, nupper] over the pair's line strengths;
         precision "f64" or "f32" is the arithmetic of the adjoint chain."""
@@ -473,8 +475,12 @@ class Engine:
         assert dL_dmu.dtype == np.float64 and dL_dmu.flags.c_contiguous
         job = PairJob(jindI, gammaI, jindF, gammaF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
         st = Stats()
-        check(lib().gain_adjoint_pair_prec(self.h, ctypes.byref(job), _p(g, _dp), _p(dL_dmu, _dp), prec,
-                                           ctypes.byref(st)))
+        if filters is not None:   # degenerate symmetries: every passing component pair
+            check(lib().gain_adjoint_pair_degenerate(self.h, ctypes.byref(job), ctypes.byref(filters), _p(g, _dp),
+                                                     _p(dL_dmu, _dp), prec, ctypes.byref(st)))
+        else:
+            check(lib().gain_adjoint_pair_prec(self.h, ctypes.byref(job), _p(g, _dp), _p(dL_dmu, _dp), prec,
+                                               ctypes.byref(st)))
         self.last_adjoint_stats = st
         self._shape = (len(lo), len(up))
         return dL_dmu

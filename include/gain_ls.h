@@ -231,7 +231,7 @@ typedef struct gain_stats {
  * amplitudes) and the adjoint chain in FP64: dL/damp = 2 amp dL/dS, dL/dH = dL/damp U,
  * dL/dh = T_F dL/dH, dL/dM = dL/dh^T v and the scatter of dL/dM into mu through the half line
  * strength's per-element factors (K-block or rotational-symmetry form).  Non-degenerate
- * symmetries (maxdeg 1). */
+ * symmetries (sdeg 1 on both sides; gain_adjoint_pair_degenerate takes the others). */
 gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const double* dL_dS,
                               double* dL_dmu, gain_stats* stats);
 
@@ -415,6 +415,15 @@ gain_status gain_run_pair_component(gain_engine e, const gain_pair_job* job, int
  * and launches. */
 gain_status gain_run_pair_degenerate(gain_engine e, const gain_pair_job* job, const gain_filters* f,
                                      gain_path path, const gain_split_opts* opts, gain_stats* stats);
+/* gain_adjoint_pair_prec for a pair of degenerate symmetries: dL_dS is the gradient over the
+ * lines' S = sum over the component pairs passing gain_degeneracy_filter of amp^2, divided
+ * by ndegI (times ndegI when filters->reduced and both states are degenerate), as
+ * gain_pair_lines forms it; dL/dmu sums the adjoint chain of every such component pair, each
+ * with its components' expansions.  A pair's forward amplitudes come from the last run or
+ * the job's component slots when they hold it, else from the plain FP64 path. */
+gain_status gain_adjoint_pair_degenerate(gain_engine e, const gain_pair_job* job, const gain_filters* f,
+                                         const double* dL_dS, double* dL_dmu, gain_adjoint_precision prec,
+                                         gain_stats* stats);
 
 /* Text of one line exactly as Output.cpp:99-111 prints it, " || \n" included (without the
  * amplitude list unless namp > 0), through the C library's snprintf.  Returns the number of

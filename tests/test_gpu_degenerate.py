@@ -158,3 +158,54 @@ def test_degenerate_argument_errors(ee_problem):
     with pytest.raises(gainls.GainError, match="maxdeg"):
         eng1.upload_inflation(0, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, inf.matsize, inf.N, inf.repres,
                               inf.Ntot, inf.sdeg)
+
+
+@pytest.mark.parametrize("reduced,symmetry_type,precision,tol", [(False, 1, "f64", 1e-11), (True, 2, "f64", 1e-11),
+                                                                (False, 1, "f32", 2e-5)])
+def test_degenerate_adjoint_exact_directions(ee_problem, reduced, symmetry_type, precision, tol):
+    """gain_adjoint_pair_degenerate: for Phi = sum w S with S combined over the passing component
+    pairs as the line assembly forms it, dPhi/dmu . d = sum w r sum_c 2 amp_c(mu) amp_c(d)
+    exactly (amp_c is linear in mu; r = 1/ndegI, or 1 when reduced with both states
+    degenerate), amp_c(d) the plain FP64 forward of component pair c for the dipole d."""
+    import gainls
+    p = ee_problem
+    nv = p.dipole.shape[-1]
+    eng = gainls.Engine(JMAX, p.nsym, 2)
+    gainls.upload_problem(eng, p)
+    lo = list(range(0, p.blocks[(0, E)].vecs.shape[0], 2))
+    up = list(range(p.blocks[(1, E)].vecs.shape[0]))
+    f = _filters(p, reduced, symmetry_type)
+    passing = [(dI, dF) for dF in range(2) for dI in range(2) if gainls.degeneracy_filter(f, E, E, dI, dF)]
+    r = 1.0 if (reduced and True) else 0.5
+    rng = np.random.default_rng(17)
+    w = rng.standard_normal((len(lo), len(up)))
+    # the lines' S equals r sum_c amp_c^2 (so w is a gradient over exactly those S)
+    eng.run_pair(0, E, 1, E, lo, up, gainls.PATH_PLAIN_FP64, filters=f)
+    S = eng.lines(p.blocks[(0, E)].energies[lo], p.blocks[(1, E)].energies[up], 3, 4, ndeg=(2, 2),
+                  reduced=reduced, want=("S",))["S"]
+    amp0 = {}
+    for c in passing:
+        eng.run_pair(0, E, 1, E, lo, up, gainls.PATH_PLAIN_FP64, components=c)
+        amp0[c] = eng.fetch_amp().copy()
+    assert np.allclose(S, r * sum(a * a for a in amp0.values()), rtol=1e-14, atol=0)
+    grad = eng.adjoint(0, E, 1, E, lo, up, w, np.zeros(p.dipole.size), precision=precision, filters=f)
+    grad = grad.reshape(p.dipole.shape)
+    assert np.abs(grad).max() > 0
+    for _ in range(2):
+        d = rng.standard_normal(p.dipole.shape)
+        eng.upload_dipole(np.ascontiguousarray(d).reshape(-1), nv, 0, nv, nv)
+        terms = np.zeros_like(w)
+        for c in passing:
+            eng.run_pair(0, E, 1, E, lo, up, gainls.PATH_PLAIN_FP64, components=c)
+            terms += w * r * 2.0 * amp0[c] * eng.fetch_amp()
+        eng.upload_dipole(np.ascontiguousarray(p.dipole).reshape(-1), nv, 0, nv, nv)
+        assert abs(np.sum(grad * d) - terms.sum()) <= tol * np.abs(terms).sum()
+
+
+def test_plain_adjoint_refuses_degenerate_pairs(ee_problem):
+    import gainls
+    p = ee_problem
+    eng = gainls.Engine(JMAX, p.nsym, 2)
+    gainls.upload_problem(eng, p)
+    with pytest.raises(gainls.GainError, match="degenerate"):
+        eng.adjoint(0, E, 1, E, [0, 1], [0, 1, 2], np.ones((2, 3)), np.zeros(p.dipole.size))
