@@ -1462,6 +1462,28 @@ gain_status line_source(gain_engine e, const gain_line_params* prm, LineParams& 
 }  // namespace
 }  // namespace gain
 
+// Every resource of an engine, whatever of it exists (also a partly created one).
+void destroy_engine(gain_engine e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->lines_pending) cudaEventSynchronize(e->ev_lines_d2h);
+    cudaStreamSynchronize(e->st);
+    if (e->st2) cudaStreamSynchronize(e->st2);
+    if (e->stc) cudaStreamSynchronize(e->stc);
+    if (e->std2h) cudaStreamSynchronize(e->std2h);
+    for (auto& ev : e->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->ev_up) cudaEventDestroy(e->ev_up);
+    if (e->ev_lines) cudaEventDestroy(e->ev_lines);
+    if (e->ev_lines_d2h) cudaEventDestroy(e->ev_lines_d2h);
+    if (e->std2h) cudaStreamDestroy(e->std2h);
+    if (e->stc) cudaStreamDestroy(e->stc);
+    if (e->st2) cudaStreamDestroy(e->st2);
+    if (e->st) cudaStreamDestroy(e->st);
+    if (e->readback) cudaFreeHost(e->readback);
+    delete e;
+}
+
 // ====================================================================== C ABI
 using namespace gain;
 
@@ -1550,14 +1572,15 @@ gain_status gain_threej_table(int jmax, double* table) {
 
 gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_engine* out) {
     clear_error();
-    if (!out || jmax < 0 || jmax > 200 || nsym <= 0 || maxdeg <= 0)
-        return set_error(GAIN_ERR_INVALID_ARG, "gain_engine_create: bad argument");
+    if (!out || jmax < 0 || jmax > 200 || nsym <= 0 || maxdeg <= 0 || maxdeg * maxdeg > kMaxDegSlots)
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_engine_create: bad argument (maxdeg 1..3)");
     *out = nullptr;
     int ndev = 0;
     GAIN_CUDA(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) return set_error(GAIN_ERR_INVALID_ARG, "no CUDA device %d", device);
     GAIN_CUDA(cudaSetDevice(device));
-    std::unique_ptr<gain_engine_s> e(new gain_engine_s());
+    // a failure below releases what was created so far (streams, events, memory)
+    std::unique_ptr<gain_engine_s, void (*)(gain_engine)> e(new gain_engine_s(), destroy_engine);
     e->device = device;
     e->jmax = jmax;
     e->nsym = nsym;
@@ -1584,24 +1607,7 @@ gain_status gain_engine_create(int device, int jmax, int nsym, int maxdeg, gain_
 
 gain_status gain_engine_destroy(gain_engine e) {
     clear_error();
-    if (!e) return GAIN_OK;
-    cudaSetDevice(e->device);
-    if (e->lines_pending) cudaEventSynchronize(e->ev_lines_d2h);
-    cudaStreamSynchronize(e->st);
-    if (e->st2) cudaStreamSynchronize(e->st2);
-    if (e->stc) cudaStreamSynchronize(e->stc);
-    if (e->std2h) cudaStreamSynchronize(e->std2h);
-    for (auto& ev : e->ev)
-        if (ev) cudaEventDestroy(ev);
-    if (e->ev_up) cudaEventDestroy(e->ev_up);
-    if (e->ev_lines) cudaEventDestroy(e->ev_lines);
-    if (e->ev_lines_d2h) cudaEventDestroy(e->ev_lines_d2h);
-    if (e->std2h) cudaStreamDestroy(e->std2h);
-    if (e->stc) cudaStreamDestroy(e->stc);
-    if (e->st2) cudaStreamDestroy(e->st2);
-    if (e->st) cudaStreamDestroy(e->st);
-    if (e->readback) cudaFreeHost(e->readback);
-    delete e;
+    destroy_engine(e);
     return GAIN_OK;
 }
 
