@@ -321,24 +321,33 @@ __global__ void k_add(double* __restrict__ acc, const double* __restrict__ x, lo
 }
 
 // S / A / I of every amplitude (non-degenerate symmetries), Output.cpp:52-112.
-__global__ void k_lines(int rows, int cols, const double* __restrict__ amp, long ld,
-                        const double* __restrict__ eI, const double* __restrict__ eF, LineParams p,
-                        double* __restrict__ S, double* __restrict__ A, double* __restrict__ I,
-                        unsigned char* __restrict__ keep, unsigned long long* nkeep) {
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+// Grid-stride over the rows x cols lines (each pass coalesced); the kept-line count is
+// reduced in the block and added once per block.
+__global__ void __launch_bounds__(256)
+k_lines(int rows, int cols, const double* __restrict__ amp, long ld,
+        const double* __restrict__ eI, const double* __restrict__ eF, LineParams p,
+        double* __restrict__ S, double* __restrict__ A, double* __restrict__ I,
+        unsigned char* __restrict__ keep, unsigned long long* nkeep) {
+    __shared__ unsigned int warp_kept[8];
     const long total = (long)rows * cols;
-    int k = 0;
-    if (idx < total) {
+    unsigned int kept = 0;
+    for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
         const int r = (int)(idx / cols), c = (int)(idx - (long)r * cols);
         const LineVals v = line_eval(amp, (long)r * ld + c, eI[r], eF[c], p);
-        k = v.keep;
+        kept += v.keep;
         if (S) S[idx] = v.ls;
         if (A) A[idx] = v.A;
         if (I) I[idx] = v.I;
-        if (keep) keep[idx] = (unsigned char)k;
+        if (keep) keep[idx] = (unsigned char)v.keep;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, k);
-    if ((threadIdx.x & 31) == 0 && m) atomicAdd(nkeep, (unsigned long long)__popc(m));
+    for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+    if ((threadIdx.x & 31) == 0) warp_kept[threadIdx.x >> 5] = kept;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < 8; ++w) t += warp_kept[w];
+        if (t) atomicAdd(nkeep, t);
+    }
 }
 
 }  // namespace
@@ -528,7 +537,12 @@ cudaError_t launch_lines(int rows, int cols, const double* amp, long ld, const d
                          unsigned char* keep, unsigned long long* nkeep, cudaStream_t st) {
     const long total = (long)rows * cols;
     if (total <= 0) return cudaSuccess;
-    const long blocks = (total + 255) / 256;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long blocks = (total + 255) / 256;
+    const long cap = (long)(sms > 0 ? sms : 152) * 4;   // one wave at four resident blocks per SM
+    if (blocks > cap) blocks = cap;
     k_lines<<<(unsigned)blocks, 256, 0, st>>>(rows, cols, amp, ld, eI, eF, p, S, A, I, keep, nkeep);
     return cudaGetLastError();
 }
