@@ -259,6 +259,9 @@ struct gain_engine_s {
     cudaStream_t stc = nullptr;   // asynchronous eigenvector uploads
     cudaStream_t std2h = nullptr; // device-to-host copies of an asynchronous line assembly
     cudaEvent_t ev_lines = nullptr, ev_lines_d2h = nullptr;
+    // kept-line count of the line assembly (apart from the run's counters, which the next run
+    // zeroes while an asynchronous copy of this one may still be pending)
+    gain::DevArray<unsigned long long> lcnt;
     bool lines_pending = false;     // gain_pair_lines_async copies still in flight
     long long* lines_nout = nullptr;   // their caller's n_lines
     cudaEvent_t ev[10] = {};
@@ -2282,12 +2285,12 @@ gain_status pair_lines(gain_engine e, const gain_line_params* prm, const double*
     if (A) GAIN_TRY(e->lineA.alloc(n));
     if (I) GAIN_TRY(e->lineI.alloc(n));
     if (keep) GAIN_TRY(e->lineKeep.alloc(n));
-    GAIN_TRY(e->ull.alloc(4));
-    GAIN_TRY(e->ull.zero(st, 4));
+    GAIN_TRY(e->lcnt.alloc(1));
+    GAIN_TRY(e->lcnt.zero(st, 1));
     // only the requested outputs are written
     GAIN_CUDA(launch_lines(rows, cols, amp, ld, e->eIdev.p, e->eFdev.p, p, S ? e->lineS.p : nullptr,
                            A ? e->lineA.p : nullptr, I ? e->lineI.p : nullptr, keep ? e->lineKeep.p : nullptr,
-                           e->ull.p + 1, st));
+                           e->lcnt.p, st));
     if (async) {
         // the copies run on their own stream: the engine's next run (on st, after the line
         // kernel) and its uploads overlap them
@@ -2295,7 +2298,7 @@ gain_status pair_lines(gain_engine e, const gain_line_params* prm, const double*
         GAIN_CUDA(cudaEventRecord(e->ev_lines, st));
         GAIN_CUDA(cudaStreamWaitEvent(e->std2h, e->ev_lines, 0));
         cudaStream_t sd = e->std2h;
-        GAIN_CUDA(cudaMemcpyAsync((char*)e->readback + 96, e->ull.p + 1, sizeof(unsigned long long),
+        GAIN_CUDA(cudaMemcpyAsync((char*)e->readback + 96, e->lcnt.p, sizeof(unsigned long long),
                                   cudaMemcpyDeviceToHost, sd));
         if (S) GAIN_CUDA(cudaMemcpyAsync(S, e->lineS.p, sizeof(double) * n, cudaMemcpyDeviceToHost, sd));
         if (A) GAIN_CUDA(cudaMemcpyAsync(A, e->lineA.p, sizeof(double) * n, cudaMemcpyDeviceToHost, sd));
@@ -2307,7 +2310,7 @@ gain_status pair_lines(gain_engine e, const gain_line_params* prm, const double*
         return GAIN_OK;
     }
     unsigned long long nk = 0;
-    GAIN_CUDA(cudaMemcpyAsync(&nk, e->ull.p + 1, sizeof nk, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaMemcpyAsync(&nk, e->lcnt.p, sizeof nk, cudaMemcpyDeviceToHost, st));
     if (S) GAIN_CUDA(cudaMemcpyAsync(S, e->lineS.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     if (A) GAIN_CUDA(cudaMemcpyAsync(A, e->lineA.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     if (I) GAIN_CUDA(cudaMemcpyAsync(I, e->lineI.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
