@@ -42,6 +42,25 @@ def test_engine_rejects_bad_arguments(built_lib):
     assert gainls.lib().gain_engine_create(0, 11, 0, 1, ctypes.byref(h)) == gainls.ERR_INVALID_ARG
     assert "bad argument" in gainls.lib().gain_last_error_string().decode()
     assert gainls.lib().gain_run_pair(None, None, 0, None, None) == gainls.ERR_INVALID_ARG
+    assert gainls.lib().gain_engine_create(0, 11, 4, 4, ctypes.byref(h)) == gainls.ERR_INVALID_ARG   # maxdeg 1..3
+
+
+def test_new_entry_points_reject_bad_arguments_on_the_host(built_lib):
+    """The plan executor, the component runs, the asynchronous lines and the adjoints check
+    their arguments before touching a device."""
+    import gainls
+    L = gainls.lib()
+    assert L.gain_run_plan(None, 1, None, 0, 0, None, gainls.JOB_DONE_FN(0), None, None) == gainls.ERR_INVALID_ARG
+    engines = (ctypes.c_void_p * 2)(None, None)
+    assert L.gain_run_plan(engines, 2, None, 0, 0, None, gainls.JOB_DONE_FN(0), None, None) == gainls.ERR_INVALID_ARG
+    assert "NULL" in L.gain_last_error_string().decode()
+    assert L.gain_run_pair_component(None, None, 0, 0, 0, None, None) == gainls.ERR_INVALID_ARG
+    assert L.gain_run_pair_degenerate(None, None, None, 0, None, None) == gainls.ERR_INVALID_ARG
+    assert L.gain_pair_lines_async(None, None, None, None, 0, 0, None, None, None, None, None) == gainls.ERR_INVALID_ARG
+    assert L.gain_lines_wait(None) == gainls.ERR_INVALID_ARG
+    assert L.gain_adjoint_pair_prec(None, None, None, None, 7, None) == gainls.ERR_INVALID_ARG
+    assert "precision" in L.gain_last_error_string().decode()
+    assert L.gain_adjoint_pair_degenerate(None, None, None, None, None, 0, None) == gainls.ERR_INVALID_ARG
 
 
 def test_dropin_validation_is_host_side(built_lib):
