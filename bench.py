@@ -275,12 +275,41 @@ def cpu_baseline(inp, n_sample: int):
     tj = threej.threej_table(11)
     t0 = time.perf_counter()
     oracle.run_pair(p, 0, GI, 1, GF, list(range(n_sample)), list(range(inp["vu"].shape[0])), tj, 11,
-                    oracle.REF, cores)
+                    oracle.REF, cores, fast=True)
     secs = time.perf_counter() - t0
     n = n_sample * inp["vu"].shape[0]
     return {"value": n / secs, "unit": UNIT, "cores": cores, "kind": "port",
+            "build": "gcc " + " ".join(oracle.FAST_FLAGS),
             "sample": f"{n_sample} lower states x {inp['vu'].shape[0]} upper states of the workload "
                       f"({n} transitions, {secs:.1f} s)"}
+
+
+def oracle_sample(inp, sample, nthreads: int = 0) -> np.ndarray:
+    """Amplitudes of the sampled lower states (indices into the workload's lower states)
+    against every upper state, from the double-double oracle (the accurate FP64 answer of
+    the reference's formula); all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import synth
+    import threej
+    oracle.build()
+    rule = inp.get("rule", "c4")
+    sample = list(sample)
+    p = synth.Problem(inp["nv"], [JI, JF], rule, 4, np.ones(4, np.int32), synth.selection_of(rule),
+                      synth.igamma_pair_of(synth.selection_of(rule)), inp["bases"], inp["infl"],
+                      [synth.classes_of(b, rule) for b in inp["bases"]], inp["dipole"],
+                      {(0, GI): synth.Block(JI, 0, GI, inp["vl"][sample], inp["eI"][sample]),
+                       (1, GF): synth.Block(JF, 1, GF, inp["vu"], inp["eF"])})
+    return oracle.run_pair(p, 0, GI, 1, GF, list(range(len(sample))), list(range(inp["vu"].shape[0])),
+                           threej.threej_table(11), 11, oracle.DD, nthreads or (os.cpu_count() or 1))
+
+
+def s_rel_err(S: np.ndarray, Sref: np.ndarray, floor: float = 1e-10):
+    """max and p99 relative error of S against Sref over the lines with Sref > floor Sref_max,
+    and the number of such lines."""
+    m = Sref > floor * Sref.max()
+    r = np.abs(S[m] - Sref[m]) / Sref[m]
+    return float(r.max()), float(np.quantile(r, 0.99)), int(m.sum())
 
 
 def precision_sweep(args):
@@ -811,22 +840,37 @@ def main():
     ms_step = total_ms / args.steps
     value = ws * transitions / (ms_step * 1e-3)
 
-    # accuracy of this run against the plain FP64 path (the reference's own method)
+    # accuracy of this run against (a) the double-double oracle on sampled lower states and
+    # (b) the plain FP64 path (the reference's own method) on every transition
     split_amp = eng.fetch_amp().copy()
     extra = {}
+    if rank == 0 and not args.no_cpu:
+        sample = list(range(0, B, max(1, B // 8)))[:8]
+        t0 = time.perf_counter()
+        dd = oracle_sample(inp, sample)
+        dd_secs = time.perf_counter() - t0
+        e_split = s_rel_err(split_amp[sample] ** 2, dd ** 2)
+        extra["accuracy"] = {"reference": "double-double oracle (oracle/gain_oracle.c, DD mode)",
+                             "oracle_sample": f"{len(sample)} lower states (rows {sample[0]}..{sample[-1]} step "
+                                              f"{sample[1] - sample[0] if len(sample) > 1 else 0}) x {NU} upper "
+                                              f"states ({dd_secs:.1f} s on {os.cpu_count()} cores)",
+                             "lines_checked": e_split[2], "max_rel_err_S": e_split[0], "p99_rel_err_S": e_split[1],
+                             "domain": "S > 1e-10 S_max", "refined_lines": st["refined"],
+                             "uncertified": st["uncertified"], "uncertified_weak": st["uncertified_weak"]}
     if not args.no_plain:
         sp = eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_PLAIN_FP64)
         plain_amp = eng.fetch_amp()
-        S, Sr = split_amp ** 2, plain_amp ** 2
-        m = Sr > 1e-10 * Sr.max()
-        rel = np.abs(S[m] - Sr[m]) / Sr[m]
+        e_fp = s_rel_err(split_amp ** 2, plain_amp ** 2)
         extra["plain_fp64"] = {"value": transitions / (sp["device_ms"] * 1e-3), "unit": UNIT,
                                "ms_per_step": sp["device_ms"], "kernel_launches": sp["kernel_launches"]}
         extra["speedup_vs_plain_fp64"] = extra["plain_fp64"]["ms_per_step"] / ms_step
-        extra["accuracy"] = {"reference": "plain FP64 GPU path", "lines_checked": int(m.sum()),
-                             "max_rel_err_S": float(rel.max()), "p99_rel_err_S": float(np.quantile(rel, 0.99)),
-                             "domain": "S > 1e-10 S_max", "refined_lines": st["refined"],
-                             "uncertified": st["uncertified"], "uncertified_weak": st["uncertified_weak"]}
+        acc = extra.setdefault("accuracy", {"domain": "S > 1e-10 S_max", "refined_lines": st["refined"],
+                                            "uncertified": st["uncertified"]})
+        acc["vs_plain_fp64_all_lines"] = {"lines_checked": e_fp[2], "max_rel_err_S": e_fp[0],
+                                          "p99_rel_err_S": e_fp[1]}
+        if "oracle_sample" in acc:
+            e_pl = s_rel_err(plain_amp[sample] ** 2, dd ** 2)
+            acc["plain_fp64_vs_oracle"] = {"max_rel_err_S": e_pl[0], "p99_rel_err_S": e_pl[1]}
         eng.run_pair(0, GI, 1, GF, lo, up, gainls.PATH_SPLIT)   # leave the split result resident
 
     # e2e: host buffers through the C ABI (inputs up, S and A down), every step

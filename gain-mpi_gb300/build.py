@@ -41,9 +41,13 @@ def _compile(src: str) -> str:
     obj = os.path.join(OBJ, src + ".o")
     deps = [path, os.path.join(ROOT, "include", "gain_ls.h"), os.path.join(ROOT, "include", "gain_trove.h")]
     deps += [os.path.join(CSRC, h) for h in HEADERS]
+    deps.append(os.path.abspath(__file__))   # the flags below
     if not _stale(obj, deps):
         return obj
+    # host code: no floating-point contraction (the host's line arithmetic rounds every
+    # product as the reference's does; aarch64 compilers fuse multiply-adds by default)
     cmd = [nvcc(), "-c", "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+           "-Xcompiler", "-ffp-contract=off",
            "-I", os.path.join(ROOT, "include")] + ARCH
     cmd += [path, "-o", obj + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)

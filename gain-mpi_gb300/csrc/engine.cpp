@@ -292,10 +292,29 @@ struct gain_engine_s {
     long amp_ld = 0;
     bool have_amp = false;
     std::vector<int> amp_job;   // job_key of amp: the pair, its level lists and components
+    // split path: the certified absolute error bound of every amplitude (ld amp_ld); the line
+    // assembly recomputes in FP64 the lines whose Einstein A lies within its bound of
+    // THRESH_LINE (line-list membership)
+    gain::DevArray<float> ampbnd;
+    bool have_bnd = false;
+    long long thresh_refined = 0;   // lines the last line assembly recomputed for THRESH_LINE
     // degenerate component slots of one job (gain_run_pair_component): [maxdeg^2][rows * cols]
     gain::DevArray<double> deg_amp;
     std::vector<int> deg_job;   // job_key (components 0, 0) of the slots
     unsigned deg_filled = 0;    // bit idegI + idegF * maxdeg per filled slot
+    gain::DevArray<float> deg_bnd;   // the slots' amplitude bounds (0 for plain-path slots)
+    // FP64 recomputation of lines near THRESH_LINE: flagged lines, level subsets, amplitudes
+    gain::DevArray<int2> thr_list;
+    gain::DevArray<unsigned int> thr_cnt;
+    gain::DevArray<int> sub_lower, sub_upper;
+    gain::DevArray<double> sub_amp, sub_acc;
+    gain::DevArray<long long> sub_patch;
+    // intensity column: lines whose intensity the host evaluates (see gain_pair_lines_text)
+    gain::DevArray<gain::TextArgs::HardLine> hardLines;
+    gain::DevArray<unsigned int> hardCount;
+    gain::DevArray<long long> ovrIdx;
+    gain::DevArray<double> ovrVal;
+    long long intensity_host = 0;
     long launches = 0;          // kernels this engine has launched (split path and band builds)
     void* readback = nullptr;   // page-locked area of a run's counter readbacks
 
@@ -434,7 +453,13 @@ const WignerTab* wigner_of(gain_engine e, int jindI, int jindF) {
     return it == e->wigner.end() ? nullptr : it->second.get();
 }
 
-gain_status run_plain(gain_engine e, const gain_pair_job* j, int dI, int dF, gain_stats* stats) {
+// The reference's method for nlo lower levels (device list d_lo) x nup upper levels (d_up) of
+// job j's blocks, with the dipole piece now on the device: one half line strength per lower
+// state followed by its dot products with every upper vector, into out[nlo][nup].
+// kPlainBatch lower states share each launch (and each read of an upper vector); every
+// amplitude keeps its own FP64 summation, so it does not depend on the other levels listed.
+gain_status plain_amps(gain_engine e, const gain_pair_job* j, int dI, int dF, const int* d_lo, int nlo,
+                       const int* d_up, int nup, double* out, int* launches_out) {
     Basis& bI = e->bases[j->jindI];
     Basis& bF = e->bases[j->jindF];
     Inflation& iI = e->infl[j->jindI];
@@ -465,25 +490,18 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, int dI, int dF, gai
     const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
     if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st, EI.ready, 0));
     if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(e->st, EF.ready, 0));
-    GAIN_TRY(e->d_lower.upload(j->lower_levels, j->nlower));
-    GAIN_TRY(e->d_upper.upload(j->upper_levels, j->nupper));
-    // The reference's method, one half line strength per lower state followed by its dot
-    // products with every upper vector; kPlainBatch lower states share each launch (and each
-    // read of an upper vector), every amplitude keeps its own FP64 summation.
     const int G = kPlainBatch;
     const int NtF = iF.Ntot[j->gammaF];
     GAIN_TRY(e->primI.alloc((size_t)G * bI.dimen));
     GAIN_TRY(e->hprim.alloc((size_t)G * bF.dimen));
     GAIN_TRY(e->hsym.alloc((size_t)G * NtF));
-    GAIN_TRY(e->amp.alloc((size_t)j->nlower * j->nupper));
     cudaStream_t st = e->st;
-    GAIN_CUDA(cudaEventRecord(e->ev[0], st));
     int launches = 0;
-    for (int l0 = 0; l0 < j->nlower; l0 += G) {
-        const int nb = std::min(G, j->nlower - l0);
+    for (int l0 = 0; l0 < nlo; l0 += G) {
+        const int nb = std::min(G, nlo - l0);
         GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, dI, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
                                        iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
-                                       EI.d.p, EI.nsize, e->d_lower.p + l0, e->primI.p, bI.dimen, nb, st));
+                                       EI.d.p, EI.nsize, d_lo + l0, e->primI.p, bI.dimen, nb, st));
         if (const WignerTab* wt = wigner_of(e, j->jindI, j->jindF)) {
             // rotational-symmetry form (GpuManager::ExecuteRotSymHalfLs): reset, then the dense
             // half line strength of each lower state
@@ -502,10 +520,22 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, int dI, int dF, gai
         }
         GAIN_CUDA(launch_contract(NtF, mF->d_csr_ptr.p, mF->d_csr_col.p, mF->d_csr_val.p, e->hprim.p, bF.dimen,
                                   e->hsym.p, NtF, nb, st));
-        GAIN_CUDA(launch_gemv_batch(j->nupper, EF.nsize, EF.d.p, EF.nsize, e->d_upper.p, e->hsym.p, NtF, nb,
-                                    e->amp.p + (size_t)l0 * j->nupper, j->nupper, st));
+        GAIN_CUDA(launch_gemv_batch(nup, EF.nsize, EF.d.p, EF.nsize, d_up, e->hsym.p, NtF, nb,
+                                    out + (size_t)l0 * nup, nup, st));
         launches += 4;
     }
+    if (launches_out) *launches_out = launches;
+    return GAIN_OK;
+}
+
+gain_status run_plain(gain_engine e, const gain_pair_job* j, int dI, int dF, gain_stats* stats) {
+    GAIN_TRY(e->d_lower.upload(j->lower_levels, j->nlower));
+    GAIN_TRY(e->d_upper.upload(j->upper_levels, j->nupper));
+    GAIN_TRY(e->amp.alloc((size_t)j->nlower * j->nupper));
+    cudaStream_t st = e->st;
+    GAIN_CUDA(cudaEventRecord(e->ev[0], st));
+    int launches = 0;
+    GAIN_TRY(plain_amps(e, j, dI, dF, e->d_lower.p, j->nlower, e->d_upper.p, j->nupper, e->amp.p, &launches));
     GAIN_CUDA(cudaEventRecord(e->ev[1], st));
     GAIN_CUDA(cudaStreamSynchronize(st));
     float ms = 0.f;
@@ -514,6 +544,7 @@ gain_status run_plain(gain_engine e, const gain_pair_job* j, int dI, int dF, gai
     e->amp_cols = j->nupper;
     e->amp_ld = j->nupper;
     e->have_amp = true;
+    e->have_bnd = false;
     if (stats) {
         memset(stats, 0, sizeof *stats);
         stats->device_ms = ms;
@@ -1035,6 +1066,10 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     GAIN_TRY(e->err.zero(st, 1));
     GAIN_TRY(e->flags1.alloc(kMaxFlags));
     GAIN_TRY(e->flags2.alloc(kMaxFlags));
+    // capacity of the refinement lists (GAINLS_MAX_FLAGS lowers it, to exercise the overflow
+    // handling on small cases)
+    int max_flags = kMaxFlags;
+    if (const char* mf = getenv("GAINLS_MAX_FLAGS")) max_flags = std::max(0, std::min(kMaxFlags, atoi(mf)));
 
     // Digit buffers and their row statistics are cleared only when their shape or layout
     // changes: padding rows and columns are never written, every other entry is.
@@ -1117,9 +1152,16 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     }
     const Basis& bFs = e->bases[j->jindF];
     std::vector<split::Tile> t1;
+    // first-GEMM refinement counts of the pieces before the last (the counter restarts per piece)
+    unsigned long long inexact_prev = 0;
+    bool overflow_prev = false;
     for (int piece = 0; piece < npieces; ++piece) {
         if (piece > 0) {   // the next piece's band (the previous GEMM and refinement read theirs)
             GAIN_CUDA(cudaStreamSynchronize(st));
+            unsigned int c0 = 0;
+            GAIN_CUDA(cudaMemcpy(&c0, e->counters.p, sizeof c0, cudaMemcpyDeviceToHost));
+            inexact_prev += c0;
+            overflow_prev = overflow_prev || c0 > (unsigned)max_flags;
             GAIN_TRY(load_piece(e, piece));
             GAIN_TRY(launch_layout_band(e, j));
             L.dip_version = e->dip_version;
@@ -1176,7 +1218,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
         g1.tol = (float)tol;
         g1.flags = e->flags1.p;
         g1.nflags = e->counters.p + 0;
-        g1.max_flags = kMaxFlags;
+        g1.max_flags = max_flags;
         g1.rows_valid = B;
         g1.cols_valid = L.fpad;
         g1.err = e->err.p;
@@ -1209,7 +1251,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
         split::RefineHArgs rh;
         rh.flags = e->flags1.p;
         rh.nflags = e->counters.p + 0;
-        rh.max_flags = kMaxFlags;
+        rh.max_flags = max_flags;
         rh.vecs = L.general ? e->primI.p : EI.d.p;
         rh.nsize = L.general ? bIs.dimen : EI.nsize;
         rh.row_level = L.general ? e->iota.p : e->d_lower.p;
@@ -1269,6 +1311,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     GAIN_TRY(e->tiles2.upload(t2));
     GAIN_TRY(e->prods2.upload(pr2));
     GAIN_TRY(e->amp.alloc((size_t)Bpad * Nupad));
+    GAIN_TRY(e->ampbnd.alloc((size_t)Bpad * Nupad));
     split::GemmArgs g2;
     memset(&g2, 0, sizeof g2);
     g2.tiles = e->tiles2.p;
@@ -1290,10 +1333,12 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     g2.tol = (float)tol;
     g2.flags = e->flags2.p;
     g2.nflags = e->counters.p + 1;
-    g2.max_flags = kMaxFlags;
+    g2.max_flags = max_flags;
     g2.rows_valid = B;
     g2.cols_valid = Nu;
     g2.err = e->err.p;
+    g2.bnd = e->ampbnd.p;
+    g2.ldb = Nupad;
     GAIN_CUDA(cudaEventRecord(e->ev[4], st));
     if (Nu2 > 0) {
         // tiles are upper-block-major: those of the first half (n0 < Nu2) come first
@@ -1315,7 +1360,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     split::RefineAmpArgs ra;
     ra.flags = e->flags2.p;
     ra.nflags = e->counters.p + 1;
-    ra.max_flags = kMaxFlags;
+    ra.max_flags = max_flags;
     ra.U = EF.d.p;
     ra.nsize = EF.nsize;
     ra.col_level = e->d_upper.p;
@@ -1326,6 +1371,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     ra.eH = e->Hst.e.p;
     ra.amp = e->amp.p;
     ra.lda = Nupad;
+    ra.bnd = e->ampbnd.p;
+    ra.ldb = Nupad;
     ra.tol = tol;
     ra.absmax = e->ull.p + 2;
     ra.amp_floor = std::sqrt((opts && opts->s_floor > 0) ? opts->s_floor : 1e-10);
@@ -1352,7 +1399,11 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     e->amp_rows = B;
     e->amp_cols = Nu;
     e->amp_ld = Nupad;
-    e->have_amp = errw == 0;
+    // a refinement list that overflowed in any piece leaves entries unrefined: such a run's
+    // amplitudes are not served
+    const bool overflow = overflow_prev || cnt[0] > (unsigned)max_flags || cnt[1] > (unsigned)max_flags;
+    e->have_amp = errw == 0 && !overflow;
+    e->have_bnd = e->have_amp;
     if (stats) {
         memset(stats, 0, sizeof *stats);
         float ms = 0.f, g1ms = 0.f, g2ms = 0.f;
@@ -1364,11 +1415,13 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
         stats->gemm2_ms = g2ms;
         stats->rows = B;
         stats->cols = Nu;
-        stats->refined = (long long)std::min<unsigned>(cnt[1], kMaxFlags) + std::min<unsigned>(cnt[0], kMaxFlags);
+        stats->refined = (long long)std::min<unsigned>(cnt[1], (unsigned)max_flags) +
+                         (long long)std::min<unsigned>(cnt[0], (unsigned)max_flags) +
+                         (long long)std::min<unsigned long long>(inexact_prev, (unsigned long long)max_flags * (npieces - 1));
         stats->uncertified = (long long)unc[0];
         stats->uncertified_weak = (long long)unc[3];
         stats->amp_max = __builtin_bit_cast(double, unc[2]);
-        stats->inexact = (long long)cnt[0];
+        stats->inexact = (long long)cnt[0] + (long long)inexact_prev;
         stats->beta1 = p1x.beta;
         stats->slices1 = p1x.slices;
         stats->chunks1 = p1x.chunks;
@@ -1379,13 +1432,14 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
         stats->products2 = (int)pr2.size();
         stats->kernel_launches = e->launches - launches0;
         double f = 0;
-        for (auto& t : t1) f += 2.0 * split::BM * split::BN * split::BK * (double)t.nkb * p1x.slices * (p1x.slices + 1) / 2;
-        for (auto& t : t2) f += 2.0 * split::BM * split::BN * split::BK * (double)t.nkb * p2.slices * (p2.slices + 1) / 2;
+        // a tile covers mstep rows (256 for CTA pairs); t1 holds the last piece's tiles
+        for (auto& t : t1) f += 2.0 * mstep * split::BN * split::BK * (double)t.nkb * pr1.size() / p1x.chunks;
+        for (auto& t : t2) f += 2.0 * mstep * split::BN * split::BK * (double)t.nkb * pr2.size() / p2.chunks;
         stats->tensor_flops = f;
     }
     if (errw != 0)
         return set_error(GAIN_ERR_TIMEOUT, "a bounded device wait of the tensor-core GEMM gave up (code %d)", errw);
-    if (cnt[0] > (unsigned)kMaxFlags || cnt[1] > (unsigned)kMaxFlags)
+    if (overflow)
         return set_error(GAIN_ERR_TOL_NOT_MET, "more lines need FP64 refinement than the refinement list holds");
     return GAIN_OK;
 }
@@ -2083,6 +2137,7 @@ gain_status run_component(gain_engine e, const gain_pair_job* job, int dI, int d
     if (dI < 0 || dI >= sI || dF < 0 || dF >= sF)
         return set_error(GAIN_ERR_INVALID_ARG, "components (%d, %d) outside the degeneracies (%d, %d)", dI, dF, sI, sF);
     e->have_amp = false;
+    e->have_bnd = false;
     gain_status r;
     if (path == GAIN_PATH_PLAIN_FP64)
         r = e->pieces.size() > 1 ? run_plain_pieces(e, job, dI, dF, stats) : run_plain(e, job, dI, dF, stats);
@@ -2113,12 +2168,20 @@ gain_status gain_run_pair_component(gain_engine e, const gain_pair_job* job, int
         e->deg_job.clear();
         e->deg_filled = 0;
         GAIN_TRY(e->deg_amp.alloc((size_t)md * md * n));
+        GAIN_TRY(e->deg_bnd.alloc((size_t)md * md * n));
         e->deg_job = key;
     }
     const int slot = idegI + idegF * md;
     GAIN_CUDA(cudaMemcpy2DAsync(e->deg_amp.p + (size_t)slot * n, sizeof(double) * job->nupper, e->amp.p,
                                 sizeof(double) * e->amp_ld, sizeof(double) * job->nupper, job->nlower,
                                 cudaMemcpyDeviceToDevice, e->st));
+    // the slot's amplitude bounds: the split run's, or zero (the plain path is the FP64 method)
+    if (e->have_bnd)
+        GAIN_CUDA(cudaMemcpy2DAsync(e->deg_bnd.p + (size_t)slot * n, sizeof(float) * job->nupper, e->ampbnd.p,
+                                    sizeof(float) * e->amp_ld, sizeof(float) * job->nupper, job->nlower,
+                                    cudaMemcpyDeviceToDevice, e->st));
+    else
+        GAIN_CUDA(cudaMemsetAsync(e->deg_bnd.p + (size_t)slot * n, 0, sizeof(float) * n, e->st));
     GAIN_CUDA(cudaStreamSynchronize(e->st));
     e->deg_filled |= 1u << slot;
     return GAIN_OK;
@@ -2262,6 +2325,107 @@ gain_status lines_settle(gain_engine e) {
     return GAIN_OK;
 }
 
+// Line-list membership under THRESH_LINE (Output.cpp:95-96) for split-path amplitudes: the
+// lines whose A lies within its certified bound of the threshold are recomputed by the plain
+// FP64 path (the reference's method) for every component the line combines, and those
+// amplitudes replace the split ones (their bounds become 0) before the line assembly reads
+// them.  Energies are on the device (eIdev, eFdev).
+constexpr int kThreshCap = 1 << 16;
+gain_status thresh_certify(gain_engine e, const gain_line_params* prm, const LineParams& p, const double* amp, long ld) {
+    e->thresh_refined = 0;
+    if (!(prm->thresh > 0.0)) return GAIN_OK;
+    if (p.nslot == 0 && !e->have_bnd) return GAIN_OK;   // the plain path is the FP64 method itself
+    const int rows = e->amp_rows, cols = e->amp_cols;
+    const size_t n = (size_t)rows * cols;
+    const float* bnd = p.nslot == 0 ? e->ampbnd.p : e->deg_bnd.p;
+    const long ldb = p.nslot == 0 ? e->amp_ld : cols;
+    cudaStream_t st = e->st;
+    GAIN_TRY(e->thr_list.alloc(kThreshCap));
+    GAIN_TRY(e->thr_cnt.alloc(1));
+    GAIN_TRY(e->thr_cnt.zero(st, 1));
+    GAIN_CUDA(launch_thresh_flag(rows, cols, amp, ld, bnd, ldb, e->eIdev.p, e->eFdev.p, p, e->thr_list.p,
+                                 e->thr_cnt.p, kThreshCap, st));
+    unsigned int cnt = 0;
+    GAIN_CUDA(cudaMemcpyAsync(&cnt, e->thr_cnt.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    if (cnt == 0) return GAIN_OK;
+    if (cnt > (unsigned)kThreshCap)
+        return set_error(GAIN_ERR_TOL_NOT_MET, "%u lines lie within their bound of THRESH_LINE (at most %d are "
+                         "recomputed)", cnt, kThreshCap);
+    std::vector<int2> list(cnt);
+    GAIN_CUDA(cudaMemcpy(list.data(), e->thr_list.p, sizeof(int2) * cnt, cudaMemcpyDeviceToHost));
+    // the job's level lists: job_key = {pair (4), nlower, nupper, dI, dF, lower..., upper...}
+    const std::vector<int>& key = e->amp_job;
+    if (key.size() < 8 || key[4] != rows || key[5] != cols)
+        return set_error(GAIN_ERR_NOT_READY, "THRESH_LINE certification: the amplitudes' job is unknown");
+    std::vector<int> R, C;
+    for (const int2& rc : list) {
+        R.push_back(rc.x);
+        C.push_back(rc.y);
+    }
+    std::sort(R.begin(), R.end());
+    R.erase(std::unique(R.begin(), R.end()), R.end());
+    std::sort(C.begin(), C.end());
+    C.erase(std::unique(C.begin(), C.end()), C.end());
+    std::vector<int> lev_lo(R.size()), lev_up(C.size());
+    for (size_t i = 0; i < R.size(); ++i) lev_lo[i] = key[8 + R[i]];
+    for (size_t i = 0; i < C.size(); ++i) lev_up[i] = key[8 + rows + C[i]];
+    GAIN_TRY(e->sub_lower.upload(lev_lo));
+    GAIN_TRY(e->sub_upper.upload(lev_up));
+    gain_pair_job sj;
+    sj.jindI = key[0];
+    sj.gammaI = key[1];
+    sj.jindF = key[2];
+    sj.gammaF = key[3];
+    sj.nlower = (int)R.size();
+    sj.lower_levels = lev_lo.data();
+    sj.nupper = (int)C.size();
+    sj.upper_levels = lev_up.data();
+    const size_t ns = R.size() * C.size();
+    GAIN_TRY(e->sub_amp.alloc(ns));
+    // components: the last run's, or every slot the lines combine
+    std::vector<std::pair<int, int>> comps;
+    std::vector<size_t> base;
+    if (p.nslot == 0) {
+        comps.push_back({key[6], key[7]});
+        base.push_back(0);
+    } else {
+        for (int q = 0; q < p.nslot; ++q) {
+            comps.push_back({p.slot[q] % e->maxdeg, p.slot[q] / e->maxdeg});
+            base.push_back((size_t)p.slot[q] * n);
+        }
+    }
+    double* dst = p.nslot == 0 ? e->amp.p : e->deg_amp.p;
+    float* dstb = p.nslot == 0 ? e->ampbnd.p : e->deg_bnd.p;
+    std::vector<long long> pairs(2 * (size_t)cnt);
+    for (size_t q = 0; q < comps.size(); ++q) {
+        const int npieces = e->pieces.size() > 1 ? (int)e->pieces.size() : 1;
+        for (int pc = 0; pc < npieces; ++pc) {
+            if (npieces > 1) GAIN_TRY(load_piece(e, pc));
+            double* out = e->sub_amp.p;
+            if (pc > 0) {
+                GAIN_TRY(e->sub_acc.alloc(ns));
+                out = e->sub_acc.p;
+            }
+            GAIN_TRY(plain_amps(e, &sj, comps[q].first, comps[q].second, e->sub_lower.p, sj.nlower, e->sub_upper.p,
+                                sj.nupper, out, nullptr));
+            if (pc > 0) GAIN_CUDA(launch_add(e->sub_amp.p, e->sub_acc.p, (long)ns, st));
+        }
+        for (unsigned int k = 0; k < cnt; ++k) {
+            const int r = list[k].x, c = list[k].y;
+            const size_t ri = std::lower_bound(R.begin(), R.end(), r) - R.begin();
+            const size_t ci = std::lower_bound(C.begin(), C.end(), c) - C.begin();
+            pairs[2 * k] = (long long)(base[q] + (size_t)r * (p.nslot == 0 ? (size_t)ld : (size_t)cols) + c);
+            pairs[2 * k + 1] = (long long)(ri * C.size() + ci);
+        }
+        GAIN_TRY(e->sub_patch.upload(pairs));
+        GAIN_CUDA(launch_patch((int)cnt, e->sub_patch.p, e->sub_amp.p, dst, dstb, st));
+        GAIN_CUDA(cudaStreamSynchronize(st));   // sub_amp and the pair list are reused by the next component
+    }
+    e->thresh_refined = cnt;
+    return GAIN_OK;
+}
+
 gain_status pair_lines(gain_engine e, const gain_line_params* prm, const double* energiesI, const double* energiesF,
                        int jI, int jF, double* S, double* A, double* I, unsigned char* keep, long long* n_lines,
                        bool async) {
@@ -2281,6 +2445,7 @@ gain_status pair_lines(gain_engine e, const gain_line_params* prm, const double*
     cudaStream_t st = e->st;
     GAIN_TRY(e->eIdev.upload(energiesI, rows));
     GAIN_TRY(e->eFdev.upload(energiesF, cols));
+    GAIN_TRY(thresh_certify(e, prm, p, amp, ld));
     if (S) GAIN_TRY(e->lineS.alloc(n));
     if (A) GAIN_TRY(e->lineA.alloc(n));
     if (I) GAIN_TRY(e->lineI.alloc(n));
@@ -2341,7 +2506,37 @@ gain_status gain_lines_wait(gain_engine e) {
     return lines_settle(e);
 }
 
+gain_status gain_lines_intensity_host(gain_engine e, long long* n_lines) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!n_lines) return set_error(GAIN_ERR_INVALID_ARG, "gain_lines_intensity_host: NULL output");
+    *n_lines = e->intensity_host;
+    return GAIN_OK;
+}
+
+gain_status gain_lines_threshold_refined(gain_engine e, long long* n_lines) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    if (!n_lines) return set_error(GAIN_ERR_INVALID_ARG, "gain_lines_threshold_refined: NULL output");
+    *n_lines = e->thresh_refined;
+    return GAIN_OK;
+}
+
 namespace {
+constexpr int kHardCap = 1 << 20;
+
+// The intensity of Output.cpp:101-102 in line_eval's operation order (every product and
+// quotient rounded once; this file is built without floating-point contraction), with this
+// host's exp -- the value the reference's own sprintf prints.
+double host_intensity(const LineParams& p, double A, double nu, double eI) {
+    double t = p.cmcoef * A;
+    t = t * p.gnsF;
+    t = t * p.two_jF1;
+    t = t * std::exp(-p.beta * (eI - p.zpe));
+    t = t * (1.0 - std::exp(-p.beta * nu));
+    return t / ((nu * nu) * p.q_part);
+}
+
 // The text of the last run's lines: lengths, offsets and (into out, when given and large
 // enough) the text itself, its device-to-host copy in parts that overlap the formatting of
 // the following parts.
@@ -2367,6 +2562,7 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
     cudaStream_t st = e->st;
     GAIN_TRY(e->eIdev.upload(energiesI, rows));
     GAIN_TRY(e->eFdev.upload(energiesF, cols));
+    GAIN_TRY(thresh_certify(e, prm, lp, amp, ld));
     GAIN_TRY(e->textLens.alloc(n));
     GAIN_TRY(e->textBlocks.alloc(nb + 3));
     GAIN_TRY(e->textBlocks.zero(st, nb + 3));
@@ -2390,11 +2586,62 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
     t.nkeep = e->textBlocks.p + nb + 1;
     t.text = nullptr;
     t.text_size = 0;
+    t.hard = nullptr;
+    t.nhard = nullptr;
+    t.hard_cap = 0;
+    t.ovr_idx = nullptr;
+    t.ovr_val = nullptr;
+    t.n_ovr = 0;
+    if (lp.with_intensity) {
+        GAIN_TRY(e->hardLines.alloc(kHardCap));
+        GAIN_TRY(e->hardCount.alloc(1));
+        GAIN_TRY(e->hardCount.zero(st, 1));
+        t.hard = e->hardLines.p;
+        t.nhard = e->hardCount.p;
+        t.hard_cap = kHardCap;
+    }
     GAIN_CUDA(launch_text_len(t, st));
     std::vector<unsigned long long> offs(nb + 3);   // block offsets, text size, lines, largest block
+    unsigned int nhard = 0;
     GAIN_CUDA(cudaMemcpyAsync(offs.data(), e->textBlocks.p, sizeof(unsigned long long) * (nb + 3),
                               cudaMemcpyDeviceToHost, st));
+    if (t.nhard) GAIN_CUDA(cudaMemcpyAsync(&nhard, t.nhard, sizeof nhard, cudaMemcpyDeviceToHost, st));
     GAIN_CUDA(cudaStreamSynchronize(st));
+    e->intensity_host = 0;
+    if (nhard > 0) {
+        // Output.cpp:101-102 on the host, with this host's exp, for the lines whose printed
+        // intensity the device's exp could change; both passes then print these values
+        if (nhard > (unsigned)kHardCap)
+            return set_error(GAIN_ERR_UNSUPPORTED, "%u lines need the host's intensity (at most %d)", nhard, kHardCap);
+        std::vector<TextArgs::HardLine> hl(nhard);
+        GAIN_CUDA(cudaMemcpy(hl.data(), e->hardLines.p, sizeof(TextArgs::HardLine) * nhard, cudaMemcpyDeviceToHost));
+        std::sort(hl.begin(), hl.end(), [](const TextArgs::HardLine& a, const TextArgs::HardLine& b) {
+            return a.idx < b.idx;
+        });
+        std::vector<long long> oi(nhard);
+        std::vector<double> ov(nhard);
+        bool relen = false;
+        for (unsigned int k = 0; k < nhard; ++k) {
+            oi[k] = hl[k].idx;
+            ov[k] = host_intensity(lp, hl[k].A, hl[k].nu, hl[k].eI);
+            char b1[64], b2[64];
+            relen = relen || snprintf(b1, sizeof b1, "%16.9E", hl[k].I) != snprintf(b2, sizeof b2, "%16.9E", ov[k]);
+        }
+        GAIN_TRY(e->ovrIdx.upload(oi));
+        GAIN_TRY(e->ovrVal.upload(ov));
+        t.ovr_idx = e->ovrIdx.p;
+        t.ovr_val = e->ovrVal.p;
+        t.n_ovr = (int)nhard;
+        e->intensity_host = nhard;
+        if (relen) {   // a field length changed (an exponent of three digits, say): lengths again
+            t.hard = nullptr;
+            GAIN_TRY(e->textBlocks.zero(st, nb + 3));
+            GAIN_CUDA(launch_text_len(t, st));
+            GAIN_CUDA(cudaMemcpyAsync(offs.data(), e->textBlocks.p, sizeof(unsigned long long) * (nb + 3),
+                                      cudaMemcpyDeviceToHost, st));
+            GAIN_CUDA(cudaStreamSynchronize(st));
+        }
+    }
     const unsigned long long total = offs[nb], lines = offs[nb + 1], largest = offs[nb + 2];
     if (text_bytes) *text_bytes = total;
     if (n_lines) *n_lines = (long long)lines;

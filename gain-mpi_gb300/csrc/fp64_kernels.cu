@@ -350,7 +350,86 @@ k_lines(int rows, int cols, const double* __restrict__ amp, long ld,
     }
 }
 
+// Lines whose Einstein A may lie on either side of THRESH_LINE given the amplitudes'
+// certified bounds (Output.cpp:95 keeps a line when A >= THRESH_LINE): the line strength is
+// evaluated, in the reference's operation order, at |amp| - bound and at |amp| + bound for
+// every amplitude it combines; S and then A are monotone in each |amp| under round to
+// nearest, so the true A lies between the two results.  A line with A_lo < THRESH_LINE <=
+// A_hi is listed for recomputation in FP64.
+__global__ void __launch_bounds__(256)
+k_thresh_flag(int rows, int cols, const double* __restrict__ amp, long ld, const float* __restrict__ bnd, long ldb,
+              const double* __restrict__ eI, const double* __restrict__ eF, LineParams p, int2* list,
+              unsigned int* count, int cap) {
+    const long total = (long)rows * cols;
+    for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(idx / cols), c = (int)(idx - (long)r * cols);
+        const double nu = eF[c] - eI[r];
+        if (!(nu >= p.freq_lo && nu <= p.freq_hi && nu >= 1e-40)) continue;   // not written in any case
+        double lo, hi;
+        if (p.nslot == 0) {
+            const double a = fabs(amp[(long)r * ld + c]), b = (double)bnd[(long)r * ldb + c];
+            if (b == 0.0) continue;
+            const double al = a > b ? a - b : 0.0, ah = a + b;
+            lo = __dmul_rn(al, al);
+            hi = __dmul_rn(ah, ah);
+        } else {
+            lo = 0.0;
+            hi = 0.0;
+            bool any = false;
+            for (int s = 0; s < p.nslot; ++s) {
+                const long o = (long)p.slot[s] * p.slot_stride + (long)r * ld + c;
+                const double a = fabs(amp[o]), b = (double)bnd[(long)p.slot[s] * p.slot_stride + (long)r * ldb + c];
+                any = any || b != 0.0;
+                const double al = a > b ? a - b : 0.0, ah = a + b;
+                lo = __dadd_rn(lo, __dmul_rn(al, al));
+                hi = __dadd_rn(hi, __dmul_rn(ah, ah));
+            }
+            if (!any) continue;
+            lo = __ddiv_rn(lo, (double)p.ndegI);
+            hi = __ddiv_rn(hi, (double)p.ndegI);
+            if (p.reduced_deg) {
+                lo = __dmul_rn(lo, (double)p.ndegI);
+                hi = __dmul_rn(hi, (double)p.ndegI);
+            }
+        }
+        const double anu = fabs(nu);
+        const double Alo = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, lo), anu), anu), anu);
+        const double Ahi = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, hi), anu), anu), anu);
+        if (Alo < p.thresh && Ahi >= p.thresh) {
+            const unsigned int k = atomicAdd(count, 1u);
+            if ((int)k < cap) list[k] = make_int2(r, c);
+        }
+    }
+}
+
+// dst[pairs[2i]] = src[pairs[2i+1]], and the bound of that entry (when given) becomes 0
+__global__ void k_patch(int n, const long long* __restrict__ pairs, const double* __restrict__ src, double* dst,
+                        float* dstbnd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long d = pairs[2 * i], s = pairs[2 * i + 1];
+    dst[d] = src[s];
+    if (dstbnd) dstbnd[d] = 0.0f;
+}
+
 }  // namespace
+
+cudaError_t launch_thresh_flag(int rows, int cols, const double* amp, long ld, const float* bnd, long ldb,
+                               const double* eI, const double* eF, const LineParams& p, int2* list,
+                               unsigned int* count, int cap, cudaStream_t st) {
+    const long total = (long)rows * cols;
+    if (total <= 0) return cudaSuccess;
+    const long blocks = std::min<long>((total + 255) / 256, 152L * 8);
+    k_thresh_flag<<<(unsigned)blocks, 256, 0, st>>>(rows, cols, amp, ld, bnd, ldb, eI, eF, p, list, count, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_patch(int n, const long long* pairs, const double* src, double* dst, float* dstbnd,
+                         cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_patch<<<(n + 255) / 256, 256, 0, st>>>(n, pairs, src, dst, dstbnd);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_hls_kblock(int dimenF, int dimenI, int jI, int jF, int kF, const int* tauI,
                               const int* tauF, const int* icorrI, const int* icorrF, int startF_idx,

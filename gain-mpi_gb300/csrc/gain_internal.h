@@ -147,6 +147,13 @@ struct LineParams {
 cudaError_t launch_lines(int rows, int cols, const double* amp, long ld, const double* eI,
                          const double* eF, LineParams p, double* S, double* A, double* I,
                          unsigned char* keep, unsigned long long* nkeep, cudaStream_t st);
+// lines whose A lies within its certified bound of THRESH_LINE -> list (at most cap, count all)
+cudaError_t launch_thresh_flag(int rows, int cols, const double* amp, long ld, const float* bnd, long ldb,
+                               const double* eI, const double* eF, const LineParams& p, int2* list,
+                               unsigned int* count, int cap, cudaStream_t st);
+// dst[pairs[2i]] = src[pairs[2i+1]] for i < n; dstbnd (optional) zeroed at the same offsets
+cudaError_t launch_patch(int n, const long long* pairs, const double* src, double* dst, float* dstbnd,
+                         cudaStream_t st);
 
 // ---------------------------------------------------------------- line-list text (linetext.cu)
 struct TextArgs {
@@ -162,6 +169,17 @@ struct TextArgs {
     unsigned long long* nkeep;             // lines written
     char* text;
     unsigned long long text_size;          // bytes of text (the write pass stays inside)
+    // Intensity column: lines whose printed intensity could differ from the host C library's
+    // (the device exp and the host exp may differ in the last bits) are listed by the length
+    // pass; the host evaluates their intensity with its own exp and both passes then print
+    // those values (ovr_idx sorted, n_ovr entries)
+    struct HardLine { long long idx; double A, nu, eI, I; };
+    HardLine* hard;                        // may be null (no collection)
+    unsigned int* nhard;
+    int hard_cap;
+    const long long* ovr_idx;
+    const double* ovr_val;
+    int n_ovr;
 };
 long text_blocks(long lines);
 cudaError_t launch_text_len(const TextArgs& t, cudaStream_t st);     // lens, offsets, total, nkeep

@@ -24,13 +24,50 @@ namespace {
 constexpr int kTextThreads = 256, kTextItems = 4, kTextSpan = kTextThreads * kTextItems;
 constexpr int kStageMax = 200 * 1024;   // shared-memory staging of one block's text
 
+// Could the printed intensity (%16.9E: ten significant digits) of a line whose device value
+// is I differ from what the host C library's exp gives?  Both exp results lie within 1 ulp of
+// the exact value, so the two intensities differ by a relative
+//   delta <= 2^-52 (7 + 2 e2 / (1 - e2)),  e2 = exp(-beta nu)
+// (the rounding of 1 - e2 amplifies the exp difference); five times that is allowed.  The
+// line is hard when a ten-digit rounding boundary lies within delta of I (or the decimal
+// exponent could change, or I is zero, tiny, huge or not finite).  x = |I| 10^(9 - e) is
+// formed with log10/exp10 and carries a relative error below 2^-51, covered by the margin.
+__device__ __forceinline__ bool intensity_hard(double I, double nu, double beta) {
+    const double a = fabs(I);
+    if (!(a >= 1e-290 && a <= 1e290)) return true;
+    const double e2 = exp(-beta * nu);
+    if (!(e2 < 1.0)) return true;
+    const double delta = 0x1p-52 * (40.0 + 8.0 * e2 / (1.0 - e2));
+    if (!(delta < 1e-6)) return true;
+    int e10 = (int)floor(log10(a));
+    double x = a * exp10((double)(9 - e10));
+    if (x < 1e9) x *= 10.0;
+    else if (x >= 1e10) x *= 0.1;
+    if (!(x >= 1e9 + 1.0 && x <= 1e10 - 2.0)) return true;
+    const double fr = x - floor(x);
+    return fabs(fr - 0.5) <= (delta + 0x1p-50) * x + 1e-6;
+}
+
+// Intensity the host gave for line idx (binary search of the override list), or v_dev.
+__device__ __forceinline__ double intensity_of(const TextArgs& t, long idx, double v_dev) {
+    int lo = 0, hi = t.n_ovr;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (t.ovr_idx[mid] < idx) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < t.n_ovr && t.ovr_idx[lo] == idx ? t.ovr_val[lo] : v_dev;
+}
+
 // The fields of line idx; false when the line is not written.  a_out receives the printed
-// amplitudes (kMaxDegSlots at most).
-__device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double* a_out, fmt::LineFields& f) {
+// amplitudes (kMaxDegSlots at most).  eI_out (optional) receives the lower energy.
+__device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double* a_out, fmt::LineFields& f,
+                                            double* eI_out = nullptr) {
     const int r = (int)(idx / t.cols), c = (int)(idx - (long)r * t.cols);
     const long off = (long)r * t.ld + c;
     const LineVals v = line_eval(t.amp, off, t.eI[r], t.eF[c], t.p);
     if (!v.keep) return false;
+    if (eI_out) *eI_out = t.eI[r];
     int namp = 1;
     if (t.p.nslot == 0) {
         a_out[0] = t.amp[off];
@@ -40,7 +77,7 @@ __device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double*
     }
     f.nu = v.nu;
     f.A = v.A;
-    f.intensity = v.I;
+    f.intensity = (t.p.with_intensity && t.n_ovr > 0) ? intensity_of(t, idx, v.I) : v.I;
     f.indexF = t.levF[c];
     f.jF = t.jF;
     f.gammaF = t.gammaF;
@@ -65,7 +102,12 @@ __device__ __forceinline__ long line_text(const TextArgs& t, long idx, fmt::Sink
 __device__ __forceinline__ long line_length(const TextArgs& t, long idx) {
     double a[kMaxDegSlots];
     fmt::LineFields f;
-    if (!line_fields(t, idx, a, f)) return 0;
+    double eI = 0.0;
+    if (!line_fields(t, idx, a, f, &eI)) return 0;
+    if (t.hard && t.p.with_intensity && intensity_hard(f.intensity, f.nu, t.p.beta)) {
+        const unsigned int k = atomicAdd(t.nhard, 1u);
+        if ((int)k < t.hard_cap) t.hard[k] = TextArgs::HardLine{(long long)idx, f.A, f.nu, eI, f.intensity};
+    }
     return fmt::line_len(f);
 }
 

@@ -3,7 +3,9 @@
 // reduces a fixed chunk of GAIN_DOT_NOALLOC_CHUNK elements into one partial sum, and the
 // last block to finish adds the partials in block order.  The partials and the completion
 // ticket live in a file-scope device array of fixed size (no cudaMalloc, no library that
-// allocates); its address is looked up once per device.
+// allocates); its address is looked up on the first call on each device, with that device
+// current, and again whenever the device's context has changed since (after a
+// cudaDeviceReset the module is loaded anew and the array may move).
 //
 // Zero state: the completion ticket must be zero when a launch starts.  It is cleared by a
 // stream-ordered memset before every launch (and the last block leaves it at zero), so a
@@ -13,6 +15,9 @@
 // The scratch is shared by every call on a device: calls whose kernels overlap on the GPU
 // (e.g. on two streams without ordering between them) race on it.
 #include <mutex>
+#include <utility>
+
+#include <cuda.h>
 
 #include "gain_internal.h"
 
@@ -32,6 +37,31 @@ static __device__ __align__(256) double g_dot_scratch[kScratchWords];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};   // context id the address belongs to
+
+// Unique id of the calling thread's current context (driver entry points, resolved once; 0
+// when they are unavailable, which only disables the change check).
+unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrentFn)(CUcontext*);
+    typedef CUresult (*GetIdFn)(CUcontext, unsigned long long*);
+    static const std::pair<GetCurrentFn, GetIdFn> fns = []() {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess)
+            a = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qb != cudaDriverEntryPointSuccess)
+            b = nullptr;
+        return std::make_pair((GetCurrentFn)a, (GetIdFn)b);
+    }();
+    if (!fns.first || !fns.second) return 0ull;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0ull;
+    if (fns.first(&ctx) != CUDA_SUCCESS || !ctx || fns.second(ctx, &id) != CUDA_SUCCESS) return 0ull;
+    return id;
+}
 
 __global__ void __launch_bounds__(kThreads) k_dot_blocks(int n, const double* __restrict__ x,
                                                           const double* __restrict__ y, double* result,
@@ -70,16 +100,20 @@ __global__ void __launch_bounds__(kThreads) k_dot_blocks(int n, const double* __
     }
 }
 
-// Address of this device's scratch; looked up on the first call on each device.
+// Address of this device's scratch: looked up on the first call on each device (the device
+// is current), and again when the device's context is no longer the one it was found in.
 gain_status scratch_for_current_device(double** out) {
     int dev = 0;
     GAIN_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return set_error(GAIN_ERR_UNSUPPORTED, "gain_dot_noalloc: device ordinal %d", dev);
+    GAIN_CUDA(cudaSetDevice(dev));   // initialises the device's primary context if a reset dropped it
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
         void* p = nullptr;
         GAIN_CUDA(cudaGetSymbolAddress(&p, g_dot_scratch));
         g_scratch_ptr[dev] = (double*)p;
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_ptr[dev];
     return GAIN_OK;

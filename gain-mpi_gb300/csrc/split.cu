@@ -570,7 +570,10 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         float av;
                         const unsigned long long vbits = scaled_bits(run, eA + eB - kFixTotal, &av);
                         orow[col] = __longlong_as_double((long long)vbits);
-                        if (nnzA == 0 || l2B == 0.0f) continue;   // an exact zero
+                        if (nnzA == 0 || l2B == 0.0f) {   // an exact zero
+                            if (a.bnd) a.bnd[(long)r * a.ldb + col] = 0.0f;
+                            continue;
+                        }
                         bool exact = __fmul_ru(sA, sB) < 4096.0f;
                         if (exact && __fmul_ru(dnAmax, dnBmax) >= two24) {
                             for (int cc = 0; cc < a.nchunks; ++cc)
@@ -599,6 +602,13 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         if (exact && rvalid && col < a.cols_valid) {
                             const unsigned long long vb = vbits & 0x7FFFFFFFFFFFFFFFull;
                             vmax = vb > vmax ? vb : vmax;
+                        }
+                        if (a.bnd) {
+                            // absolute bound: units 2^{eA+eB}; below float's normal range the
+                            // smallest normal scale over-states it (still a bound)
+                            const int es = eA + eB;
+                            a.bnd[(long)r * a.ldb + col] =
+                                !exact || es > 127 ? __int_as_float(0x7f800000) : __fmul_ru(bound, pow2f(max(es, -126)));
                         }
                         if (a.rowerr2) {
                             const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
@@ -1139,7 +1149,10 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
             // of this dot product plus the H error, which the first GEMM certified FP64-grade.
             // Lines where even that bound exceeds tol |amp| are counted (information only).
             const double f64b = aacc * (double)(a.nsize + 64) * 1.1102230246251565e-16 * 1.01;
-            (void)l2;
+            if (a.bnd) {
+                const double herr = a.h_inerr ? (double)a.h_inerr[r] * pow2d(a.eH[r]) * sqrt(l2) * 1.01 : 0.0;
+                a.bnd[(long)r * a.ldb + c] = __double2float_ru(f64b + herr);
+            }
             if (!(f64b <= a.tol * fabs(acc))) {
                 const double amax = __longlong_as_double((long long)*a.absmax);
                 atomicAdd(fabs(acc) >= a.amp_floor * amax ? a.uncertified : a.uncertified_weak, 1ull);

@@ -86,6 +86,10 @@ struct GemmArgs {
     int max_flags;
     int rows_valid, cols_valid;
     int* err;               // device error word (0 ok, else timeout code)
+    // optional: the absolute error bound of every output (float, rounded up; +inf where the
+    // exact-accumulation certificate failed), bnd[row * ldb + col]
+    float* bnd;
+    long ldb;
 };
 
 size_t gemm_smem_bytes();
@@ -189,6 +193,8 @@ struct RefineAmpArgs {
     const int* eH;
     double* amp;
     long lda;
+    float* bnd;             // optional: the recomputed amplitude's error bound, bnd[r * ldb + c]
+    long ldb;
     double tol;
     const unsigned long long* absmax;    // largest |amp| of the run (IEEE bits)
     double amp_floor;                    // sqrt(s_floor): certification domain |amp| >= floor*max

@@ -210,6 +210,8 @@ def _declare(L):
     L.gain_pair_lines_async.argtypes = [_vp, ctypes.POINTER(LineParams), _dp, _dp, I, I, _dp, _dp, _dp,
                                   ctypes.POINTER(ctypes.c_ubyte), ctypes.POINTER(ctypes.c_longlong)]
     L.gain_lines_wait.argtypes = [_vp]
+    L.gain_lines_threshold_refined.argtypes = [_vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.gain_lines_intensity_host.argtypes = [_vp, ctypes.POINTER(ctypes.c_longlong)]
     L.gain_format_line.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
     L.gain_format_line.restype = I
     L.gain_format_line_native.argtypes = [ctypes.c_char_p, ctypes.c_size_t, D, I, I, I, I, I, I, D, I, D, _dp, I]
@@ -262,7 +264,8 @@ def _declare(L):
                  "gain_upload_eigvecs", "gain_upload_eigvecs_async", "gain_upload_wigner", "gain_adjoint_pair",
                  "gain_adjoint_pair_prec", "gain_run_pair", "gain_run_pair_component", "gain_run_pair_degenerate",
                  "gain_run_plan", "gain_adjoint_pair_degenerate", "gain_pair_amp_device", "gain_fetch_amp",
-                 "gain_pair_lines", "gain_pair_lines_async", "gain_lines_wait", "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
+                 "gain_pair_lines", "gain_pair_lines_async", "gain_lines_wait", "gain_lines_threshold_refined", "gain_lines_intensity_host",
+                 "gain_pair_lines_text", "gain_pair_lines_text_host", "gain_fetch_lines_text",
                  "gain_lines_text_device",
                  "gain_format_values_device"):
         getattr(L, name).restype = S
@@ -491,6 +494,19 @@ class Engine:
         pend = getattr(self, "_pending_lines", None)
         self._pending_lines = None
         return pend[0].value if pend else 0
+
+    def threshold_refined(self) -> int:
+        """Lines the last line assembly / text call recomputed in FP64 because their A lay
+        within its certified bound of THRESH_LINE."""
+        n = ctypes.c_longlong()
+        check(lib().gain_lines_threshold_refined(self.h, ctypes.byref(n)))
+        return n.value
+
+    def intensity_host(self) -> int:
+        """Lines of the last text call whose intensity was evaluated on the host."""
+        n = ctypes.c_longlong()
+        check(lib().gain_lines_intensity_host(self.h, ctypes.byref(n)))
+        return n.value
 
     def amp_device(self):
         p, ld = ctypes.c_void_p(), ctypes.c_int()

@@ -90,12 +90,17 @@ gain_status gain_dot(int n, const double* x, const double* y, double* result, vo
 
 /* Same result as gain_dot (summed in another order: blocks of GAIN_DOT_NOALLOC_CHUNK
  * elements, then the block sums in block order) for callers that cannot allocate device
- * memory: it calls no cudaMalloc/cudaFree and no allocating library.  Its scratch is a
- * fixed device array (GAIN_DOT_NOALLOC_MAX_N / GAIN_DOT_NOALLOC_CHUNK partial sums plus a
- * completion ticket, about 128 KB per device); n above GAIN_DOT_NOALLOC_MAX_N is rejected
- * with GAIN_ERR_INVALID_ARG.  The first call on each device looks up that array's address
- * (set-up); make that first call before any stream capture.  The scratch is shared by all
- * calls on a device: calls whose kernels overlap on the GPU race on it.
+ * memory: host programs whose device memory is all handed out by their own pool allocator
+ * (a framework's caching allocator that has already reserved the free memory, or a budget
+ * that a direct cudaMalloc would break), and code on a path where an allocation's implicit
+ * device synchronisation is not acceptable.  It calls no cudaMalloc/cudaFree and no
+ * allocating library.  Its scratch is a fixed device array (GAIN_DOT_NOALLOC_MAX_N /
+ * GAIN_DOT_NOALLOC_CHUNK partial sums plus a completion ticket, about 128 KB, held on every
+ * device that loads the library until the process exits); n above GAIN_DOT_NOALLOC_MAX_N is
+ * rejected with GAIN_ERR_INVALID_ARG.  The first call on each device looks up that array's
+ * address (set-up, and again after the device's context was reset); make that first call
+ * before any stream capture.  The scratch is shared by all calls on a device and keeps the
+ * last call's contents: calls whose kernels overlap on the GPU race on it.
  * No counterpart in the reference (its dot product is the cuBLAS call gain_dot replaces). */
 #define GAIN_DOT_NOALLOC_CHUNK 4096
 #define GAIN_DOT_NOALLOC_MAX_N (16384LL * GAIN_DOT_NOALLOC_CHUNK)
@@ -221,7 +226,8 @@ typedef struct gain_stats {
     int products1, products2;   /* BF16 digit products per GEMM */
     int kernel_launches;        /* kernels launched by the last run */
     double gemm1_ms, gemm2_ms;  /* device time of the two tensor-core GEMMs */
-    double tensor_flops;        /* BF16 MMA flops issued by the two GEMMs (no padding) */
+    double tensor_flops;        /* BF16 MMA flops issued by the two GEMMs (whole tiles, padding
+                                   included; the first GEMM counts its last dipole piece) */
 } gain_stats;
 
 /* Adjoint of one block pair (no counterpart in the reference): for a loss L over the line
@@ -311,6 +317,23 @@ gain_status gain_pair_lines_async(gain_engine e, const gain_line_params* prm, co
                                   double* I, unsigned char* keep, long long* n_lines);
 /* Wait for the copies of the last gain_pair_lines_async (immediate when none is pending). */
 gain_status gain_lines_wait(gain_engine e);
+
+/* Line-list membership with THRESH_LINE > 0 (Output.cpp:95-96 drops a line when
+ * A < THRESH_LINE): before the line assembly reads split-path amplitudes, every line whose A
+ * lies within its certified error bound of THRESH_LINE is recomputed by the plain FP64 path
+ * (the reference's method), for every component slot it combines, and those amplitudes
+ * replace the split ones; the line assembly and text calls do this themselves.  This
+ * returns how many lines the last line assembly or text call recomputed.  More than 65536
+ * such lines fail that call with GAIN_ERR_TOL_NOT_MET.  No counterpart in the reference. */
+gain_status gain_lines_threshold_refined(gain_engine e, long long* n_lines);
+
+/* The intensity column of the line text (GAIN_TEXT_INTENSITY) is printed from the value the
+ * reference's host code computes (Output.cpp:101-102 with the host C library's exp): a line
+ * whose ten printed digits could change with the last bits of exp is evaluated on the host
+ * and printed from that value; every other line's digits are the same either way.  This
+ * returns how many lines the last text call evaluated on the host.  No counterpart in the
+ * reference. */
+gain_status gain_lines_intensity_host(gain_engine e, long long* n_lines);
 
 /* Line-list text of the last run, built on the device: every line gain_pair_lines keeps,
  * written exactly as Output::OutputLinestrength prints it (BaseClasses/Output.cpp:99-111:

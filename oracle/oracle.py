@@ -21,26 +21,48 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build", platform.machine())
 LIB = os.path.join(BUILD, "libgainoracle.so")
+# The same source built for speed, used only as the timed CPU baseline: -O3 and the
+# compiler's default floating-point contraction (fused multiply-adds where it finds them).
+# No -march=native: the same host code must build and behave alike on x86_64 and aarch64.
+LIB_FAST = os.path.join(BUILD, "libgainoracle_fast.so")
 SRC = os.path.join(HERE, "gain_oracle.c")
+FAST_FLAGS = ["-O3", "-fopenmp"]
 
 REF, DD = 0, 1
 
 _lib = None
+_lib_fast = None
+
+
+def _stale(target: str) -> bool:
+    return not os.path.exists(target) or os.path.getmtime(target) < max(
+        os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "gain_oracle.h")))
 
 
 def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "gain_oracle.h"))):
+    if force or _stale(LIB):
+        # parity build: no contraction, so every product and sum rounds as written
         cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp",
                SRC, "-o", LIB + ".tmp", "-lm"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
+    if force or _stale(LIB_FAST):
+        cmd = ["gcc"] + FAST_FLAGS + ["-fPIC", "-shared", "-std=c11", SRC, "-o", LIB_FAST + ".tmp", "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB_FAST + ".tmp", LIB_FAST)
     return LIB
 
 
-def lib():
-    global _lib
+def lib(fast: bool = False):
+    """The parity build, or (fast=True) the speed build the CPU baseline times."""
+    global _lib, _lib_fast
+    if fast:
+        if _lib_fast is None:
+            build()
+            _lib_fast = ctypes.CDLL(LIB_FAST)
+            _declare(_lib_fast)
+        return _lib_fast
     if _lib is None:
         build()
         _lib = ctypes.CDLL(LIB)
@@ -177,11 +199,12 @@ def dot(x, y, mode=REF):
 
 def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
              upper_levels: Sequence[int], threej, jmax, mode=REF, nthreads=1,
-             dipole_block=None, components=(0, 0)):
+             dipole_block=None, components=(0, 0), fast=False):
     """amp[l, u] through the reference's plain loop order for one block pair.
 
     lower_levels / upper_levels are level indices inside the (J, Gamma) blocks; components =
-    (idegI, idegF), the degenerate components of the lower and upper vectors."""
+    (idegI, idegF), the degenerate components of the lower and upper vectors.  fast=True runs
+    the speed build (the CPU baseline's timing only; its roundings may differ)."""
     p = problem
     bI, bF = p.bases[jindI], p.bases[jindF]
     iI, iF = p.infl[jindI], p.infl[jindF]
@@ -217,7 +240,7 @@ def run_pair(problem, jindI, gammaI, jindF, gammaF, lower_levels: Sequence[int],
     s.idegI, s.idegF = int(components[0]), int(components[1])
     s.sdegI, s.sdegF = int(iI.sdeg[gammaI]), int(iF.sdeg[gammaF])
     amp = np.zeros((vl.shape[0], vu.shape[0]), np.float64)
-    rc = lib().orc_run_pair(ctypes.byref(s), nthreads, mode, amp.ctypes.data_as(_dp))
+    rc = lib(fast).orc_run_pair(ctypes.byref(s), nthreads, mode, amp.ctypes.data_as(_dp))
     if rc != 0:
         raise MemoryError("oracle run_pair failed")
     return amp

@@ -94,3 +94,41 @@ def test_engine_loops_over_dipole_pieces(tmp_path, built_lib, rule):
     assert np.max(np.abs(S[m] - Sr[m]) / Sr[m]) <= 1e-8
     with pytest.raises(gainls.GainError):
         eng.adjoint(0, 0, 1, 1, lo, up, np.ones((len(lo), len(up))), np.zeros(p.dipole.size))
+
+
+def test_refinement_overflow_in_an_earlier_piece_fails_the_run(built_lib, monkeypatch):
+    """With dipole pieces the first GEMM's refinement list restarts per piece: a list that
+    overflows in an earlier piece (entries left unrefined) must fail the run with
+    TOL_NOT_MET and leave no amplitudes to fetch, even when the last piece's list fits."""
+    import gainls
+    import synth
+    p = synth.make_problem(24, [3, 4], "c4", blocks=[(3, 0), (4, 1)])
+    nv = p.dipole.shape[-1]
+    eng = gainls.Engine(JMAX, p.nsym, 1)
+    gainls.upload_problem(eng, p)
+    lo = list(range(p.blocks[(0, 0)].vecs.shape[0]))
+    up = list(range(p.blocks[(1, 1)].vecs.shape[0]))
+
+    def piece(s, e):
+        return (s, e, np.ascontiguousarray(p.dipole[:, :, s:e]).reshape(-1))
+
+    # 40-bit first-GEMM digits: no H entry certifies FP64-grade, every non-zero one is flagged
+    monkeypatch.setenv("GAINLS_GEMM1_BITS", "40")
+    counts = []
+    for rng in ((0, nv - 1), (nv - 1, nv)):
+        eng.upload_dipole_pieces([piece(*rng)], nv)
+        st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+        assert st["status"] == gainls.OK
+        counts.append(st["inexact"])
+    first, last = counts
+    assert first > last + 1 > 1, counts
+    eng.upload_dipole_pieces([piece(0, nv - 1), piece(nv - 1, nv)], nv)
+    st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    assert st["status"] == gainls.OK and st["inexact"] == first + last
+    monkeypatch.setenv("GAINLS_MAX_FLAGS", str((first + last) // 2))   # holds the last piece's only
+    st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT, raise_on_error=False)
+    assert st["status"] == gainls.ERR_TOL_NOT_MET, st
+    with pytest.raises(gainls.GainError) as ei:
+        eng.fetch_amp()
+    assert ei.value.status == gainls.ERR_NOT_READY
+    eng.close()
