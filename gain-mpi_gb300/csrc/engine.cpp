@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <climits>
 #include <cstdarg>
@@ -12,6 +13,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <queue>
 #include <memory>
 #include <string>
 #include <thread>
@@ -274,6 +276,7 @@ struct gain_engine_s {
     int dipN = 0, startF = 0, endF = 0, ncontrF = 0;
     bool dip_present = false;
     long dip_version = 0;
+    long struct_version = 0;   // bases and expansion tables (plans re-capture when it moves)
     // dipole pieces kept in host memory (gain_upload_dipole_pieces); runs loop over them
     struct HostPiece {
         const double* host;
@@ -314,6 +317,7 @@ struct gain_engine_s {
     gain::DevArray<unsigned int> hardCount;
     gain::DevArray<long long> ovrIdx;
     gain::DevArray<double> ovrVal;
+    gain::DevArray<double> pow10;   // 10^k, k = -300..300, correctly rounded (C library strtod)
     long long intensity_host = 0;
     long launches = 0;          // kernels this engine has launched (split path and band builds)
     void* readback = nullptr;   // page-locked area of a run's counter readbacks
@@ -343,7 +347,7 @@ struct gain_engine_s {
     bool have_text = false;
 
     // split-path layouts (band, its digits, padded index maps) per block pair, kept across runs
-    std::map<std::array<int, 6>, std::unique_ptr<gain::PairLayout>> layouts;
+    std::map<std::array<int, 6>, std::shared_ptr<gain::PairLayout>> layouts;   // plans share them
     gain::PairLayout* cur = nullptr;   // the layout of the current run
     gain::PlainLayout plain;
 };
@@ -649,7 +653,7 @@ gain_status build_layout(gain_engine e, const gain_pair_job* j, int dI, int dF, 
             GAIN_CUDA(cudaStreamSynchronize(e->st));
             e->layouts.clear();
         }
-        it = e->layouts.emplace(akey, std::unique_ptr<PairLayout>(new PairLayout())).first;
+        it = e->layouts.emplace(akey, std::make_shared<PairLayout>()).first;
     }
     e->cur = it->second.get();
     PairLayout& L = *e->cur;
@@ -954,6 +958,57 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     return GAIN_OK;
 }
 
+// The band digits of layout L for the first GEMM's digit configuration p1 (kept until the
+// configuration or the band changes) and their tensor maps.
+gain_status layout_band_digits(gain_engine e, PairLayout& L, const SplitParams& p1, cudaStream_t st) {
+    if (L.beta1 != p1.beta || L.s1 != p1.slices || L.c1 != p1.chunks) {
+        GAIN_TRY(L.bandDig.alloc((size_t)p1.slices * L.fpad * L.W));
+        GAIN_TRY(L.bandDig.zero(st, (size_t)p1.slices * L.fpad * L.W));
+        GAIN_TRY(L.bandStats.alloc(L.fpad, p1.chunks, false));
+        GAIN_TRY(L.bandStats.zero(st, L.fpad, p1.chunks, false));
+        GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, nullptr, L.W, L.fpad, L.bandDig.p, p1,
+                       L.bandStats, false, nullptr, nullptr, st));
+        if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1.slices) ||
+            !split::make_digit_map(&L.tmBandPair, L.bandDig.p, L.W, L.fpad, p1.slices, split::BN / 2))
+            return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed for the band digits");
+        L.beta1 = p1.beta;
+        L.s1 = p1.slices;
+        L.c1 = p1.chunks;
+    }
+    return GAIN_OK;
+}
+
+// Digit configuration of the first GEMM for layout L: 53 - log2(W + 64) + 6 bits between 46
+// and 56 (every H entry must stay within the FP64 bound of its dot product, which loosens
+// with the band width W); one inner chunk per band tile with the digits narrowed until it
+// stays exact, or (rotational-symmetry form, every tile spanning the whole lower layout)
+// chunks as in the second GEMM.  GAINLS_GEMM1_BITS (40..62) overrides the bits.
+SplitParams gemm1_params(const PairLayout& L, const gain_split_opts* opts) {
+    gain_split_opts o1{};
+    if (opts) o1.beta = opts->beta;
+    int bits1 = (int)std::ceil(53.0 - std::log2((double)L.W + 64.0) + 6.0);
+    bits1 = std::max(46, std::min(56, bits1));
+    if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
+    SplitParams p1x;
+    if (L.rotsym) {
+        p1x = choose_params(L.W, &o1, bits1, 8);
+    } else {
+        p1x = choose_params(L.W, &o1, bits1, 7);
+        p1x.chunks = 1;
+        while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
+            --p1x.beta;
+            p1x.slices = (bits1 + p1x.beta - 1) / p1x.beta;
+        }
+    }
+    return p1x;
+}
+
+bool digits_supported(const SplitParams& p1, const SplitParams& p2) {
+    return !(p1.slices * p1.beta > 62 || p2.slices * p2.beta > 62 || p1.slices > split::MAX_SLICES ||
+             p2.slices > split::MAX_SLICES || p1.beta < 2 || p1.beta > 8 || p2.beta < 2 || p2.beta > 8 ||
+             2 * (p2.slices - 1) * p2.beta > 126 || 2 * (p1.slices - 1) * p1.beta > 126);
+}
+
 gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, const gain_split_opts* opts,
                       gain_stats* stats) {
     GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI, dI);
@@ -975,59 +1030,17 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     // vectors are awaited on the second stream only, so their copy overlaps the lower side
     if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EI.ready, 0));
 
-    // First GEMM: 49 bits (its error reaches every amplitude through ||dH||_2 ||u||_2; every
-    // entry must certify FP64-grade), one inner chunk per band tile, digits narrowed until that
-    // single chunk stays exact.
+    // First GEMM: about 49 bits at config-2 band widths (its error reaches every amplitude
+    // through ||dH||_2 ||u||_2; every entry must certify FP64-grade), see gemm1_params.
     // Second GEMM: 48 bits (8-bit digits in up to MAX_CHUNKS chunks, else 7 x 7 bits);
     // options (beta, slices, kchunks) apply to it.
-    gain_split_opts o1{};
-    if (opts) o1.beta = opts->beta;
-    SplitParams p1x;
-    // Bits of the first GEMM's digits.  Every H entry must stay within the FP64 bound of its
-    // dot product, (W + 64) 2^-53 ||x|| ||y||, which loosens as the band width W grows, so
-    // the digits follow it: 53 - log2(W + 64) + 6 bits, between 46 and 56.  At W = 3000
-    // (config 2) that is 49 bits (7 digits of 7; every entry certifies, 42 bits certify
-    // none); narrow bands keep 56.  GAINLS_GEMM1_BITS (40..62) overrides the rule.
-    int bits1 = (int)std::ceil(53.0 - std::log2((double)L.W + 64.0) + 6.0);
-    bits1 = std::max(46, std::min(56, bits1));
-    if (const char* b1 = getenv("GAINLS_GEMM1_BITS")) bits1 = std::max(40, std::min(62, atoi(b1)));
-    if (L.rotsym) {
-        // rotational-symmetry form: every tile spans the whole lower layout, so the inner
-        // dimension splits into chunks as in the second GEMM (per-chunk norms of both operands)
-        p1x = choose_params(L.W, &o1, bits1, 8);
-    } else {
-        p1x = choose_params(L.W, &o1, bits1, 7);
-        p1x.chunks = 1;
-        while (p1x.beta > 4 && (double)L.W * std::ldexp(1.0, 2 * p1x.beta) / 12.0 > 8388608.0) {
-            --p1x.beta;
-            p1x.slices = (bits1 + p1x.beta - 1) / p1x.beta;
-        }
-    }
+    const SplitParams p1x = gemm1_params(L, opts);
     const int K2 = L.general ? L.ntpad : L.fpad;   // inner dimension of the second GEMM
     const SplitParams p2 = choose_params(K2, opts, 48, 8);
-    if (p1x.slices * p1x.beta > 62 || p2.slices * p2.beta > 62 || p1x.slices > split::MAX_SLICES ||
-        p2.slices > split::MAX_SLICES || p1x.beta < 2 || p1x.beta > 8 || p2.beta < 2 || p2.beta > 8 ||
-        2 * (p2.slices - 1) * p2.beta > 126 || 2 * (p1x.slices - 1) * p1x.beta > 126)
-        return set_error(GAIN_ERR_INVALID_ARG, "unsupported digit configuration");
+    if (!digits_supported(p1x, p2)) return set_error(GAIN_ERR_INVALID_ARG, "unsupported digit configuration");
 
     // band digits (cached per digit configuration)
-    auto band_digits = [&]() -> gain_status {
-    if (L.beta1 != p1x.beta || L.s1 != p1x.slices || L.c1 != p1x.chunks) {
-        GAIN_TRY(L.bandDig.alloc((size_t)p1x.slices * L.fpad * L.W));
-        GAIN_TRY(L.bandDig.zero(st, (size_t)p1x.slices * L.fpad * L.W));
-        GAIN_TRY(L.bandStats.alloc(L.fpad, p1x.chunks, false));
-        GAIN_TRY(L.bandStats.zero(st, L.fpad, p1x.chunks, false));
-        GAIN_TRY(slice(e, L.band.p, L.W, nullptr, L.fpad, L.W, nullptr, nullptr, L.W, L.fpad, L.bandDig.p, p1x,
-                       L.bandStats, false, nullptr, nullptr, st));
-        if (!split::make_digit_map(&L.tmBand, L.bandDig.p, L.W, L.fpad, p1x.slices) ||
-            !split::make_digit_map(&L.tmBandPair, L.bandDig.p, L.W, L.fpad, p1x.slices, split::BN / 2))
-            return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed for the band digits");
-        L.beta1 = p1x.beta;
-        L.s1 = p1x.slices;
-        L.c1 = p1x.chunks;
-    }
-    return GAIN_OK;
-    };
+    auto band_digits = [&]() -> gain_status { return layout_band_digits(e, L, p1x, st); };
     GAIN_TRY(band_digits());
 
     // CTA pairs (256 x 128 tiles) whenever the lower states fill more than one 128-row block;
@@ -1708,6 +1721,7 @@ gain_status gain_upload_basis(gain_engine e, int jind, int J, int dimen, const i
     GAIN_TRY(b.dkblock.upload(b.kblock));
     b.present = true;
     e->layouts.clear();
+    ++e->struct_version;
     e->cur = nullptr;
     e->plain.key[0] = -1;
     if (e->infl[jind].present)
@@ -1767,6 +1781,7 @@ gain_status gain_upload_inflation(gain_engine e, int jind, const int* icontr, co
     GAIN_TRY(inf.dijterms.upload(inf.ijterms));
     inf.present = true;
     e->layouts.clear();
+    ++e->struct_version;
     e->cur = nullptr;
     e->plain.key[0] = -1;
     return GAIN_OK;
@@ -2589,10 +2604,21 @@ gain_status lines_text(gain_engine e, const gain_line_params* prm, const double*
     t.hard = nullptr;
     t.nhard = nullptr;
     t.hard_cap = 0;
+    t.pow10 = nullptr;
     t.ovr_idx = nullptr;
     t.ovr_val = nullptr;
     t.n_ovr = 0;
     if (lp.with_intensity) {
+        if (!e->pow10.p) {
+            std::vector<double> pw(601);
+            for (int k = -300; k <= 300; ++k) {
+                char b[16];
+                snprintf(b, sizeof b, "1e%d", k);
+                pw[k + 300] = strtod(b, nullptr);
+            }
+            GAIN_TRY(e->pow10.upload(pw));
+        }
+        t.pow10 = e->pow10.p;
         GAIN_TRY(e->hardLines.alloc(kHardCap));
         GAIN_TRY(e->hardCount.alloc(1));
         GAIN_TRY(e->hardCount.zero(st, 1));
@@ -2757,3 +2783,806 @@ int gain_format_line(char* buf, size_t cap, double nu, int indexF, int jF, int g
 }
 
 }  // extern "C"
+
+// ====================================================================================
+// Grouped plans: every job's split path in two grouped tensor-core launches, captured into a
+// CUDA graph (gain_plan_*).
+namespace {
+constexpr int kPlanStreams = 4;   // concurrent branches of the per-job stages
+
+struct PlanJob {
+    std::vector<int> lower, upper;
+    gain_pair_job job{};
+    std::shared_ptr<PairLayout> L;
+    SplitParams p1{}, p2{};
+    int beta2 = 0, slices2 = 0;   // the second GEMM's digits when chosen (0: the default rule)
+    int B = 0, Bpad = 0, Nu = 0, Nupad = 0, K2 = 0, cap1 = 0, cap2 = 0, klass = 0;
+    DevArray<int> d_lower, d_upper, iota;
+    DevArray<double> primI, H, Hsym, amp;
+    DevArray<float> rowerr, ampbnd;
+    DevArray<__nv_bfloat16> Vdig, Hdig, Udig;
+    StatsDev Vst, Hst, Ust;
+    DevArray<int2> flags1, flags2;
+    DevArray<split::Prod> prods1, prods2;
+    int nprods1 = 0, nprods2 = 0;
+    CUtensorMap tmV{}, tmH{}, tmU{};
+    const void* vI = nullptr;     // eigenvector and band-digit buffers the graph captured
+    const void* vF = nullptr;
+    int nlevI = 0, nlevF = 0;     // and the eigenvector blocks' shapes
+    const void* band = nullptr;
+    gain_status status = GAIN_OK;
+};
+
+// Size class of the second GEMM's inner dimension (the autotuner's unit).
+int k2_class(int K2) { return K2 <= 2048 ? 0 : K2 <= 8192 ? 1 : K2 <= 16384 ? 2 : 3; }
+
+struct TuneChoice {
+    bool pair = false;
+    int beta2[4] = {0, 0, 0, 0}, slices2[4] = {0, 0, 0, 0};
+};
+std::mutex g_tune_mutex;
+std::map<std::string, TuneChoice> g_tune_cache;   // plan shape -> choice (this process)
+}  // namespace
+
+struct gain_plan_s {
+    gain_engine e = nullptr;
+    std::vector<std::unique_ptr<PlanJob>> jobs;
+    gain_split_opts opts{};
+    bool has_opts = false;
+    int flags = 0;
+    bool pair = false;
+    int units = 0;
+    DevArray<split::GemmGroup> groups1, groups2;
+    DevArray<split::Tile> tiles1, tiles2;
+    int ntiles1 = 0, ntiles2 = 0, real1 = 0, real2 = 0;
+    int s1max = 1, c1max = 1, s2max = 1, c2max = 1;
+    double flops = 0.0;
+    DevArray<unsigned int> counters;        // [2 * njobs]: GEMM1 / GEMM2 refinement counts
+    DevArray<unsigned long long> ull;       // [4 * njobs]: uncertified, -, amp max, uncertified weak
+    DevArray<int> err;
+    char* rb = nullptr;                     // page-locked readback of counters, ull, err
+    cudaStream_t side[kPlanStreams - 1] = {};
+    cudaEvent_t fork = nullptr, join[kPlanStreams - 1] = {}, ev[6] = {};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long dip_version = -1, wig_version = -1, struct_version = -1;
+    bool ready = false;
+    int captures = 0, graph_nodes = 0, kernel_nodes = 0;
+    bool tuned = false;
+    double tune_ms = 0.0;
+    std::vector<gain_stats> job_stats;
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        ready = false;
+    }
+    ~gain_plan_s() {
+        if (e) cudaSetDevice(e->device);
+        drop_graph();
+        for (auto& s : side)
+            if (s) cudaStreamDestroy(s);
+        if (fork) cudaEventDestroy(fork);
+        for (auto& v : join)
+            if (v) cudaEventDestroy(v);
+        for (auto& v : ev)
+            if (v) cudaEventDestroy(v);
+        if (rb) cudaFreeHost(rb);
+    }
+};
+
+namespace {
+// Buffers, layout, digit configuration and tensor maps of one job (before any capture).
+gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
+    gain_engine e = P->e;
+    const gain_pair_job* j = &J.job;
+    cudaStream_t st = e->st;
+    GAIN_TRY(validate_job(e, j));   // the uploads may have changed since the plan was made
+    GammaMaps* mI = gamma_maps(e, j->jindI, j->gammaI, 0);
+    GammaMaps* mF = gamma_maps(e, j->jindF, j->gammaF, 0);
+    if (!mI || !mF) return GAIN_ERR_OOM;
+    GAIN_TRY(build_layout(e, j, 0, 0, mI, mF));
+    const std::array<int, 6> akey = {j->jindI, j->gammaI, j->jindF, j->gammaF, 0, 0};
+    J.L = e->layouts.at(akey);
+    PairLayout& L = *J.L;
+    const gain_split_opts* opts = P->has_opts ? &P->opts : nullptr;
+    J.p1 = gemm1_params(L, opts);
+    J.K2 = L.general ? L.ntpad : L.fpad;
+    gain_split_opts o2 = P->has_opts ? P->opts : gain_split_opts{};
+    if (J.beta2) {
+        o2.beta = J.beta2;
+        o2.slices = J.slices2;
+        o2.kchunks = 0;
+    }
+    J.p2 = choose_params(J.K2, &o2, 48, 8);
+    J.klass = k2_class(J.K2);
+    if (!digits_supported(J.p1, J.p2)) return set_error(GAIN_ERR_INVALID_ARG, "unsupported digit configuration");
+    GAIN_TRY(layout_band_digits(e, L, J.p1, st));
+    const Basis& bI = e->bases[j->jindI];
+    const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+    const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+    J.B = j->nlower;
+    J.Nu = j->nupper;
+    if (L.general && J.B > 65535)
+        return set_error(GAIN_ERR_UNSUPPORTED, "plan job with a mixing expansion: at most 65535 lower states");
+    const int mstep = P->pair ? 2 * split::BM : split::BM;
+    J.Bpad = round_up(J.B, mstep);
+    J.Nupad = round_up(J.Nu, split::BN);
+    J.cap1 = (int)std::min<long>(kMaxFlags, std::max<long>(4096, (long)J.Bpad * L.fpad / 8));
+    J.cap2 = (int)std::min<long>(kMaxFlags, std::max<long>(4096, (long)J.Bpad * J.Nupad / 8));
+    const size_t vdig = (size_t)J.p1.slices * J.Bpad * L.kpadI;
+    const size_t hdig = (size_t)J.p2.slices * J.Bpad * J.K2;
+    const size_t udig = (size_t)J.p2.slices * J.Nupad * J.K2;
+    GAIN_TRY(J.Vdig.alloc(vdig));
+    GAIN_TRY(J.Vdig.zero(st, vdig));
+    GAIN_TRY(J.Vst.alloc(J.Bpad, J.p1.chunks, false));
+    GAIN_TRY(J.Vst.zero(st, J.Bpad, J.p1.chunks, false));
+    GAIN_TRY(J.Hdig.alloc(hdig));
+    GAIN_TRY(J.Hdig.zero(st, hdig));
+    GAIN_TRY(J.Hst.alloc(J.Bpad, J.p2.chunks, true));
+    GAIN_TRY(J.Hst.zero(st, J.Bpad, J.p2.chunks, true));
+    GAIN_TRY(J.Udig.alloc(udig));
+    GAIN_TRY(J.Udig.zero(st, udig));
+    GAIN_TRY(J.Ust.alloc(J.Nupad, J.p2.chunks, false));
+    GAIN_TRY(J.Ust.zero(st, J.Nupad, J.p2.chunks, false));
+    GAIN_TRY(J.H.alloc((size_t)J.Bpad * L.fpad));
+    GAIN_TRY(J.rowerr.alloc(J.Bpad));
+    GAIN_TRY(J.amp.alloc((size_t)J.Bpad * J.Nupad));
+    GAIN_TRY(J.ampbnd.alloc((size_t)J.Bpad * J.Nupad));
+    GAIN_TRY(J.flags1.alloc(J.cap1));
+    GAIN_TRY(J.flags2.alloc(J.cap2));
+    GAIN_TRY(J.d_lower.upload(J.lower));
+    GAIN_TRY(J.d_upper.upload(J.upper));
+    if (L.general) {
+        GAIN_TRY(J.primI.alloc((size_t)J.B * bI.dimen));
+        std::vector<int> io(J.B);
+        for (int b = 0; b < J.B; ++b) io[b] = b;
+        GAIN_TRY(J.iota.upload(io));
+        GAIN_TRY(J.Hsym.alloc((size_t)J.Bpad * J.K2));
+    }
+    const std::vector<split::Prod> pr1 = make_prods(J.p1), pr2 = make_prods(J.p2);
+    GAIN_TRY(J.prods1.upload(pr1));
+    GAIN_TRY(J.prods2.upload(pr2));
+    J.nprods1 = (int)pr1.size();
+    J.nprods2 = (int)pr2.size();
+    if (!split::make_digit_map(&J.tmV, J.Vdig.p, L.kpadI, J.Bpad, J.p1.slices) ||
+        !split::make_digit_map(&J.tmH, J.Hdig.p, J.K2, J.Bpad, J.p2.slices) ||
+        !split::make_digit_map(&J.tmU, J.Udig.p, J.K2, J.Nupad, J.p2.slices, P->pair ? split::BN / 2 : split::BM))
+        return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (plan job digits)");
+    J.vI = EI.d.p;
+    J.vF = EF.d.p;
+    J.nlevI = EI.nlevels;
+    J.nlevF = EF.nlevels;
+    J.band = L.bandDig.p;
+    return GAIN_OK;
+}
+
+// Longest-first spread of tiles over `units` persistent CTAs (CTA pairs): each tile goes to
+// the least loaded unit; the list is then laid out so that unit u runs entries u, u + units,
+// ... (empty slots: group -1).  Within a unit the tiles keep their list order.
+std::vector<split::Tile> lpt_schedule(const std::vector<split::Tile>& tiles, const std::vector<double>& cost,
+                                      int units) {
+    std::vector<int> order(tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<std::vector<int>> per(units);
+    std::vector<double> load(units, 0.0);
+    typedef std::pair<double, int> LU;
+    std::priority_queue<LU, std::vector<LU>, std::greater<LU>> heap;
+    for (int u = 0; u < units; ++u) heap.push({0.0, u});
+    for (int t : order) {
+        LU top = heap.top();
+        heap.pop();
+        per[top.second].push_back(t);
+        top.first += cost[t];
+        heap.push(top);
+    }
+    size_t depth = 0;
+    for (auto& v : per) {
+        std::sort(v.begin(), v.end());   // list order inside a unit (L2 reuse of shared operands)
+        depth = std::max(depth, v.size());
+    }
+    split::Tile empty;
+    memset(&empty, 0, sizeof empty);
+    empty.group = -1;
+    std::vector<split::Tile> out(depth * units, empty);
+    for (int u = 0; u < units; ++u)
+        for (size_t k = 0; k < per[u].size(); ++k) out[k * units + u] = tiles[per[u][k]];
+    return out;
+}
+
+// Groups and schedules of both grouped launches.
+gain_status plan_build_groups(gain_plan P) {
+    gain_engine e = P->e;
+    const int mstep = P->pair ? 2 * split::BM : split::BM;
+    P->units = P->pair ? e->num_sms / 2 : e->num_sms;
+    const int nj = (int)P->jobs.size();
+    std::vector<split::GemmGroup> g1(nj), g2(nj);
+    std::vector<split::Tile> t1, t2;
+    std::vector<double> c1, c2;
+    P->s1max = P->c1max = P->s2max = P->c2max = 1;
+    P->flops = 0.0;
+    const double tol = (P->has_opts && P->opts.tol > 0) ? P->opts.tol : 4.5e-9;
+    for (int q = 0; q < nj; ++q) {
+        PlanJob& J = *P->jobs[q];
+        PairLayout& L = *J.L;
+        memset(&g1[q], 0, sizeof g1[q]);
+        memset(&g2[q], 0, sizeof g2[q]);
+        g1[q].tmA = J.tmV;
+        g1[q].tmB = P->pair ? L.tmBandPair : L.tmBand;
+        split::GemmArgs& a1 = g1[q].args;
+        a1.prods = J.prods1.p;
+        a1.nprods = J.nprods1;
+        a1.nchunks = J.p1.chunks;
+        a1.beta = J.p1.beta;
+        a1.slices = J.p1.slices;
+        a1.out = J.H.p;
+        a1.ldo = L.fpad;
+        a1.A = J.Vst.view(false);
+        a1.B = L.bandStats.view(false);
+        a1.c_fix = fix_const(J.nprods1);
+        a1.c_f64 = (float)((double)(L.W + 64) * std::ldexp(1.0, -53) * 1.01);
+        a1.rowerr2 = J.rowerr.p;
+        a1.flag_mode = 2;
+        a1.tol = (float)tol;
+        a1.flags = J.flags1.p;
+        a1.nflags = P->counters.p + 2 * q;
+        a1.max_flags = J.cap1;
+        a1.rows_valid = J.B;
+        a1.cols_valid = L.fpad;
+        g2[q].tmA = J.tmH;
+        g2[q].tmB = J.tmU;
+        split::GemmArgs& a2 = g2[q].args;
+        a2.prods = J.prods2.p;
+        a2.nprods = J.nprods2;
+        a2.nchunks = J.p2.chunks;
+        a2.beta = J.p2.beta;
+        a2.slices = J.p2.slices;
+        a2.out = J.amp.p;
+        a2.ldo = J.Nupad;
+        a2.A = J.Hst.view(false);
+        a2.B = J.Ust.view(false);
+        a2.c_fix = fix_const(J.nprods2);
+        a2.c_f64 = (float)((double)((L.general ? L.nsymF : L.nF) + 64) * std::ldexp(1.0, -53) * 1.01);
+        a2.absmax = P->ull.p + 4 * q + 2;
+        a2.flag_mode = 1;
+        a2.tol = (float)tol;
+        a2.flags = J.flags2.p;
+        a2.nflags = P->counters.p + 2 * q + 1;
+        a2.max_flags = J.cap2;
+        a2.rows_valid = J.B;
+        a2.cols_valid = J.Nu;
+        a2.bnd = J.ampbnd.p;
+        a2.ldb = J.Nupad;
+        P->s1max = std::max(P->s1max, J.p1.slices);
+        P->c1max = std::max(P->c1max, J.p1.chunks);
+        P->s2max = std::max(P->s2max, J.p2.slices);
+        P->c2max = std::max(P->c2max, J.p2.chunks);
+        const double tri1 = (double)J.nprods1 / J.p1.chunks, tri2 = (double)J.nprods2 / J.p2.chunks;
+        for (auto& fb : L.fblocks)
+            for (int n0 = fb.first; n0 < fb.second; n0 += split::BN)
+                for (int m0 = 0; m0 < J.Bpad; m0 += mstep) {
+                    split::Tile t;
+                    memset(&t, 0, sizeof t);
+                    t.m0 = m0;
+                    t.n0 = n0;
+                    t.a_k0 = L.band_k0[n0];
+                    t.nkb = L.band_len[n0] / split::BK;
+                    t.group = q;
+                    t1.push_back(t);
+                    c1.push_back(t.nkb * tri1 + 2.0 * J.nprods1);
+                    P->flops += 2.0 * mstep * split::BN * split::BK * t.nkb * tri1;
+                }
+        for (int n0 = 0; n0 < J.Nupad; n0 += split::BN)
+            for (int m0 = 0; m0 < J.Bpad; m0 += mstep) {
+                split::Tile t;
+                memset(&t, 0, sizeof t);
+                t.m0 = m0;
+                t.n0 = n0;
+                t.nkb = J.K2 / split::BK;
+                t.group = q;
+                t2.push_back(t);
+                c2.push_back(t.nkb * tri2 + 2.0 * J.nprods2);
+                P->flops += 2.0 * mstep * split::BN * split::BK * t.nkb * tri2;
+            }
+    }
+    P->real1 = (int)t1.size();
+    P->real2 = (int)t2.size();
+    const std::vector<split::Tile> s1 = lpt_schedule(t1, c1, P->units), s2 = lpt_schedule(t2, c2, P->units);
+    P->ntiles1 = (int)s1.size();
+    P->ntiles2 = (int)s2.size();
+    GAIN_TRY(P->groups1.upload(g1));
+    GAIN_TRY(P->groups2.upload(g2));
+    GAIN_TRY(P->tiles1.upload(s1));
+    GAIN_TRY(P->tiles2.upload(s2));
+    return GAIN_OK;
+}
+
+// The plan's work on the engine's stream (and its side streams), to be captured.
+gain_status plan_enqueue(gain_plan P) {
+    gain_engine e = P->e;
+    cudaStream_t st = e->st;
+    const int nj = (int)P->jobs.size();
+    auto stream_of = [&](int q) { return q % kPlanStreams == 0 ? st : P->side[q % kPlanStreams - 1]; };
+    auto fork = [&]() -> gain_status {
+        GAIN_CUDA(cudaEventRecord(P->fork, st));
+        for (auto s : P->side) GAIN_CUDA(cudaStreamWaitEvent(s, P->fork, 0));
+        return GAIN_OK;
+    };
+    auto join = [&]() -> gain_status {
+        for (int k = 0; k < kPlanStreams - 1; ++k) {
+            GAIN_CUDA(cudaEventRecord(P->join[k], P->side[k]));
+            GAIN_CUDA(cudaStreamWaitEvent(st, P->join[k], 0));
+        }
+        return GAIN_OK;
+    };
+    GAIN_CUDA(cudaMemsetAsync(P->counters.p, 0, sizeof(unsigned int) * 2 * nj, st));
+    GAIN_CUDA(cudaMemsetAsync(P->ull.p, 0, sizeof(unsigned long long) * 4 * nj, st));
+    GAIN_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
+    GAIN_CUDA(cudaEventRecord(P->ev[0], st));
+    // ---- stage 1: digits of the lower and the upper eigenvectors, every job
+    GAIN_TRY(fork());
+    for (int q = 0; q < nj; ++q) {
+        PlanJob& J = *P->jobs[q];
+        PairLayout& L = *J.L;
+        const gain_pair_job* j = &J.job;
+        cudaStream_t sq = stream_of(q);
+        const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+        const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+        const Basis& bI = e->bases[j->jindI];
+        if (L.general) {
+            Inflation& iI = e->infl[j->jindI];
+            GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
+                                           iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
+                                           EI.d.p, EI.nsize, J.d_lower.p, J.primI.p, bI.dimen, J.B, sq));
+            GAIN_TRY(slice(e, J.primI.p, bI.dimen, nullptr, J.B, bI.dimen, nullptr, nullptr, L.kpadI, J.Bpad, J.Vdig.p,
+                           J.p1, J.Vst, false, nullptr, nullptr, sq, L.d_i_sym.p));
+            GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, L.nsymF, nullptr, nullptr, J.K2, J.Nupad, J.Udig.p,
+                           J.p2, J.Ust, false, nullptr, nullptr, sq, nullptr));
+        } else {
+            GAIN_TRY(slice(e, EI.d.p, EI.nsize, J.d_lower.p, J.B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI,
+                           J.Bpad, J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr, sq, L.d_i_sym.p));
+            GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad,
+                           J.Nupad, J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr, sq, L.d_f_sym.p));
+        }
+        GAIN_CUDA(cudaMemsetAsync(J.rowerr.p, 0, sizeof(float) * J.Bpad, sq));
+    }
+    GAIN_TRY(join());
+    // ---- stage 2: the first GEMM of every job, one grouped launch
+    split::GemmArgs ga;
+    memset(&ga, 0, sizeof ga);
+    ga.err = P->err.p;
+    ga.groups = P->groups1.p;
+    ga.tiles = P->tiles1.p;
+    ga.ntiles = P->ntiles1;
+    GAIN_CUDA(cudaEventRecord(P->ev[1], st));
+    GAIN_CUDA(split::launch_gemm_grouped(ga, P->units, P->s1max, P->c1max, st, P->pair));
+    GAIN_CUDA(cudaEventRecord(P->ev[2], st));
+    // ---- stage 3: FP64 refinement of H, contraction (mixing expansions), digits of H
+    GAIN_TRY(fork());
+    for (int q = 0; q < nj; ++q) {
+        PlanJob& J = *P->jobs[q];
+        PairLayout& L = *J.L;
+        const gain_pair_job* j = &J.job;
+        cudaStream_t sq = stream_of(q);
+        const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+        const Basis& bI = e->bases[j->jindI];
+        split::RefineHArgs rh;
+        rh.flags = J.flags1.p;
+        rh.nflags = P->counters.p + 2 * q;
+        rh.max_flags = J.cap1;
+        rh.vecs = L.general ? J.primI.p : EI.d.p;
+        rh.nsize = L.general ? bI.dimen : EI.nsize;
+        rh.row_level = L.general ? J.iota.p : J.d_lower.p;
+        rh.i_sym = L.d_i_sym.p;
+        rh.band_k0 = L.d_band_k0.p;
+        rh.band_len = L.d_band_len.p;
+        rh.band = L.band.p;
+        rh.W = L.W;
+        rh.H = J.H.p;
+        rh.ldh = L.fpad;
+        rh.eA = J.Vst.e.p;
+        rh.rowerr2 = J.rowerr.p;
+        GAIN_CUDA(split::launch_refine_h(rh, std::min(2 * e->num_sms, std::max(1, J.cap1 / 8)), sq));
+        const double* Hs = J.H.p;
+        if (L.general) {
+            GAIN_CUDA(launch_contract_rowerr(J.B, J.H.p, L.fpad, L.fpad, J.rowerr.p, J.Vst.e.p, L.sigmaF, L.gamF, sq));
+            GAIN_CUDA(launch_contract(L.nsymF, L.d_cF_ptr.p, L.d_cF_col.p, L.d_cF_val.p, J.H.p, L.fpad, J.Hsym.p, J.K2,
+                                      J.B, sq));
+            Hs = J.Hsym.p;
+        }
+        GAIN_TRY(slice(e, Hs, J.K2, nullptr, J.B, L.general ? L.nsymF : L.fpad, nullptr, nullptr, J.K2, J.Bpad,
+                       J.Hdig.p, J.p2, J.Hst, true, J.rowerr.p, J.Vst.e.p, sq));
+    }
+    GAIN_TRY(join());
+    // ---- stage 4: the second GEMM of every job, one grouped launch
+    ga.groups = P->groups2.p;
+    ga.tiles = P->tiles2.p;
+    ga.ntiles = P->ntiles2;
+    GAIN_CUDA(cudaEventRecord(P->ev[3], st));
+    GAIN_CUDA(split::launch_gemm_grouped(ga, P->units, P->s2max, P->c2max, st, P->pair));
+    GAIN_CUDA(cudaEventRecord(P->ev[4], st));
+    // ---- stage 5: FP64 refinement of the amplitudes
+    GAIN_TRY(fork());
+    for (int q = 0; q < nj; ++q) {
+        PlanJob& J = *P->jobs[q];
+        PairLayout& L = *J.L;
+        const gain_pair_job* j = &J.job;
+        cudaStream_t sq = stream_of(q);
+        const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+        split::RefineAmpArgs ra;
+        ra.flags = J.flags2.p;
+        ra.nflags = P->counters.p + 2 * q + 1;
+        ra.max_flags = J.cap2;
+        ra.U = EF.d.p;
+        ra.nsize = EF.nsize;
+        ra.col_level = J.d_upper.p;
+        ra.colpos = L.general ? L.d_ident.p : L.d_colposF.p;
+        ra.H = L.general ? J.Hsym.p : J.H.p;
+        ra.ldh = J.K2;
+        ra.h_inerr = J.Hst.inerr.p;
+        ra.eH = J.Hst.e.p;
+        ra.amp = J.amp.p;
+        ra.lda = J.Nupad;
+        ra.bnd = J.ampbnd.p;
+        ra.ldb = J.Nupad;
+        ra.tol = (P->has_opts && P->opts.tol > 0) ? P->opts.tol : 4.5e-9;
+        ra.absmax = P->ull.p + 4 * q + 2;
+        ra.amp_floor = std::sqrt((P->has_opts && P->opts.s_floor > 0) ? P->opts.s_floor : 1e-10);
+        ra.uncertified = P->ull.p + 4 * q;
+        ra.uncertified_weak = P->ull.p + 4 * q + 3;
+        GAIN_CUDA(split::launch_refine_amp(ra, std::min(4 * e->num_sms, std::max(1, J.cap2 / 8)), sq));
+    }
+    GAIN_TRY(join());
+    GAIN_CUDA(cudaEventRecord(P->ev[5], st));
+    GAIN_CUDA(cudaMemcpyAsync(P->rb, P->counters.p, sizeof(unsigned int) * 2 * nj, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaMemcpyAsync(P->rb + 8 * (size_t)nj, P->ull.p, sizeof(unsigned long long) * 4 * nj,
+                              cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaMemcpyAsync(P->rb + 40 * (size_t)nj, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    return GAIN_OK;
+}
+
+// Prepare every job, build the grouped launches and capture the graph.
+gain_status plan_build(gain_plan P) {
+    gain_engine e = P->e;
+    P->drop_graph();
+    const int nj = (int)P->jobs.size();
+    for (auto& J : P->jobs) GAIN_TRY(plan_prepare_job(P, *J));
+    GAIN_TRY(P->counters.alloc(2 * nj));
+    GAIN_TRY(P->ull.alloc(4 * nj));
+    GAIN_TRY(P->err.alloc(1));
+    GAIN_TRY(plan_build_groups(P));
+    if (!P->rb) GAIN_CUDA(cudaMallocHost(&P->rb, 40 * (size_t)nj + 64));
+    GAIN_CUDA(split::prepare_device());   // kernel attributes are set outside the capture
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    GAIN_CUDA(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+    const gain_status s = plan_enqueue(P);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+    if (s != GAIN_OK) {
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        return s;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "capturing the plan");
+    P->graph = g;
+    GAIN_CUDA(cudaGraphInstantiate(&P->exec, P->graph, 0));
+    size_t nodes = 0;
+    GAIN_CUDA(cudaGraphGetNodes(P->graph, nullptr, &nodes));
+    std::vector<cudaGraphNode_t> nv(nodes);
+    GAIN_CUDA(cudaGraphGetNodes(P->graph, nv.data(), &nodes));
+    int kern = 0;
+    for (auto n : nv) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(n, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kern;
+    }
+    P->graph_nodes = (int)nodes;
+    P->kernel_nodes = kern;
+    ++P->captures;
+    P->dip_version = e->dip_version;
+    P->wig_version = e->wig_version;
+    P->struct_version = e->struct_version;
+    P->ready = true;
+    return GAIN_OK;
+}
+
+// The plan's inputs still where the graph read them?
+bool plan_current(gain_plan P) {
+    gain_engine e = P->e;
+    if (!P->ready || P->dip_version != e->dip_version || P->wig_version != e->wig_version ||
+        P->struct_version != e->struct_version)
+        return false;
+    for (auto& J : P->jobs) {
+        const gain_pair_job* j = &J->job;
+        auto iI = e->eig.find({j->jindI, j->gammaI});
+        auto iF = e->eig.find({j->jindF, j->gammaF});
+        if (iI == e->eig.end() || iF == e->eig.end()) return false;
+        if (iI->second->d.p != J->vI || iF->second->d.p != J->vF || J->L->bandDig.p != J->band) return false;
+        if (iI->second->nlevels != J->nlevI || iF->second->nlevels != J->nlevF) return false;
+        if (J->L->beta1 != J->p1.beta || J->L->s1 != J->p1.slices || J->L->c1 != J->p1.chunks) return false;
+    }
+    return true;
+}
+
+// One replay: device time, per-job counters and statuses.
+gain_status plan_replay(gain_plan P, double* ms_out) {
+    gain_engine e = P->e;
+    cudaStream_t st = e->st;
+    if (!plan_current(P)) GAIN_TRY(plan_build(P));
+    for (auto& J : P->jobs) {   // asynchronous eigenvector uploads land before the replay
+        const gain_pair_job* j = &J->job;
+        const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+        const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+        if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EI.ready, 0));
+        if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EF.ready, 0));
+    }
+    GAIN_CUDA(cudaGraphLaunch(P->exec, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    GAIN_CUDA(cudaEventElapsedTime(&ms, P->ev[0], P->ev[5]));
+    if (ms_out) *ms_out = ms;
+    const int nj = (int)P->jobs.size();
+    const unsigned int* cnt = (const unsigned int*)P->rb;
+    const unsigned long long* unc = (const unsigned long long*)(P->rb + 8 * (size_t)nj);
+    int errw = 0;
+    memcpy(&errw, P->rb + 40 * (size_t)nj, sizeof errw);
+    P->job_stats.assign(nj, gain_stats{});
+    gain_status first = GAIN_OK;
+    for (int q = 0; q < nj; ++q) {
+        PlanJob& J = *P->jobs[q];
+        gain_stats& s = P->job_stats[q];
+        memset(&s, 0, sizeof s);
+        s.rows = J.B;
+        s.cols = J.Nu;
+        s.refined = (long long)std::min<unsigned>(cnt[2 * q], J.cap1) + std::min<unsigned>(cnt[2 * q + 1], J.cap2);
+        s.inexact = cnt[2 * q];
+        s.uncertified = (long long)unc[4 * q];
+        s.uncertified_weak = (long long)unc[4 * q + 3];
+        s.amp_max = __builtin_bit_cast(double, unc[4 * q + 2]);
+        s.beta1 = J.p1.beta;
+        s.slices1 = J.p1.slices;
+        s.chunks1 = J.p1.chunks;
+        s.beta2 = J.p2.beta;
+        s.slices2 = J.p2.slices;
+        s.chunks2 = J.p2.chunks;
+        s.products1 = J.nprods1;
+        s.products2 = J.nprods2;
+        J.status = GAIN_OK;
+        if (errw != 0) J.status = GAIN_ERR_TIMEOUT;
+        else if (cnt[2 * q] > (unsigned)J.cap1 || cnt[2 * q + 1] > (unsigned)J.cap2) J.status = GAIN_ERR_TOL_NOT_MET;
+        if (J.status != GAIN_OK && first == GAIN_OK) {
+            first = J.status;
+            if (errw != 0)
+                set_error(GAIN_ERR_TIMEOUT, "a bounded device wait of the grouped GEMM gave up (code %d)", errw);
+            else
+                set_error(GAIN_ERR_TOL_NOT_MET, "plan job %d: more entries need FP64 refinement than its list holds", q);
+        }
+    }
+    return first;
+}
+
+std::string plan_shape_key(gain_plan P) {
+    std::string k;
+    char buf[96];
+    for (auto& J : P->jobs) {
+        snprintf(buf, sizeof buf, "%d,%d,%d,%d,%d,%d;", J->job.jindI, J->job.gammaI, J->job.jindF, J->job.gammaF,
+                 J->job.nlower, J->job.nupper);
+        k += buf;
+    }
+    snprintf(buf, sizeof buf, "|%d|%.3g", P->has_opts ? P->opts.beta * 100 + P->opts.slices : 0,
+             P->has_opts ? P->opts.tol : 0.0);
+    return k + buf;
+}
+
+void plan_apply(gain_plan P, const TuneChoice& c) {
+    P->pair = c.pair;
+    for (auto& J : P->jobs) {
+        const int k = k2_class(J->L ? (J->L->general ? J->L->ntpad : J->L->fpad) : J->K2);
+        J->beta2 = c.beta2[k];
+        J->slices2 = c.slices2[k];
+    }
+}
+
+// The autotuner: the plan's own replays time each candidate (the best of two replays after
+// one warm-up); a candidate whose replay fails (a refinement list overflowed) is dropped.
+// First the tile shape with the default digits, then, one size class at a time, the 7-bit x 7
+// digits of the second GEMM against the default 8-bit x 6.
+gain_status plan_autotune(gain_plan P, TuneChoice* out) {
+    const auto t0 = std::chrono::steady_clock::now();
+    auto time_of = [&](const TuneChoice& c, double* best) -> gain_status {
+        plan_apply(P, c);
+        GAIN_TRY(plan_build(P));
+        *best = 1e300;
+        for (int r = 0; r < 3; ++r) {
+            double ms = 0;
+            const gain_status s = plan_replay(P, &ms);
+            if (s != GAIN_OK) return s;
+            if (r > 0) *best = std::min(*best, ms);
+        }
+        return GAIN_OK;
+    };
+    TuneChoice best_c;
+    double best = 1e300;
+    bool any_pairable = false;
+    for (auto& J : P->jobs) any_pairable = any_pairable || J->job.nlower > split::BM;
+    for (int pr = 0; pr < (any_pairable ? 2 : 1); ++pr) {
+        TuneChoice c;
+        c.pair = pr == 1;
+        double ms;
+        if (time_of(c, &ms) == GAIN_OK && ms < best) {
+            best = ms;
+            best_c = c;
+        }
+    }
+    if (best >= 1e300) return set_error(GAIN_ERR_TOL_NOT_MET, "autotuner: no candidate configuration ran");
+    bool present[4] = {false, false, false, false};
+    for (auto& J : P->jobs) present[k2_class(J->K2)] = true;
+    for (int k = 0; k < 4; ++k) {
+        if (!present[k]) continue;
+        TuneChoice c = best_c;
+        c.beta2[k] = 7;
+        c.slices2[k] = 7;
+        double ms;
+        if (time_of(c, &ms) == GAIN_OK && ms < 0.99 * best) {
+            best = ms;
+            best_c = c;
+        }
+    }
+    clear_error();
+    *out = best_c;
+    P->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return GAIN_OK;
+}
+}  // namespace
+
+gain_status gain_plan_create(gain_engine e, const gain_pair_job* jobs, int n_jobs, const gain_split_opts* opts,
+                             int flags, gain_plan* out) {
+    clear_error();
+    if (!out) return set_error(GAIN_ERR_INVALID_ARG, "gain_plan_create: NULL output");
+    *out = nullptr;
+    GAIN_TRY(check_engine(e));
+    if (!jobs || n_jobs <= 0 || (flags & ~GAIN_PLAN_AUTOTUNE))
+        return set_error(GAIN_ERR_INVALID_ARG, "gain_plan_create: bad job list or flags");
+    if (e->pieces.size() > 1)
+        return set_error(GAIN_ERR_UNSUPPORTED, "plans take a single dipole piece (gain_upload_dipole)");
+    std::unique_ptr<gain_plan_s> P(new gain_plan_s());
+    P->e = e;
+    P->flags = flags;
+    if (opts) {
+        P->opts = *opts;
+        P->has_opts = true;
+    }
+    for (int q = 0; q < n_jobs; ++q) {
+        GAIN_TRY(validate_job(e, &jobs[q]));
+        const int sI = e->infl[jobs[q].jindI].sdeg[jobs[q].gammaI], sF = e->infl[jobs[q].jindF].sdeg[jobs[q].gammaF];
+        if (sI != 1 || sF != 1)
+            return set_error(GAIN_ERR_UNSUPPORTED, "plan job %d: degenerate symmetries run per component pair", q);
+        std::unique_ptr<PlanJob> J(new PlanJob());
+        J->lower.assign(jobs[q].lower_levels, jobs[q].lower_levels + jobs[q].nlower);
+        J->upper.assign(jobs[q].upper_levels, jobs[q].upper_levels + jobs[q].nupper);
+        J->job = jobs[q];
+        J->job.lower_levels = J->lower.data();
+        J->job.upper_levels = J->upper.data();
+        P->jobs.push_back(std::move(J));
+    }
+    for (auto& s : P->side) GAIN_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    GAIN_CUDA(cudaEventCreateWithFlags(&P->fork, cudaEventDisableTiming));
+    for (auto& v : P->join) GAIN_CUDA(cudaEventCreateWithFlags(&v, cudaEventDisableTiming));
+    for (auto& v : P->ev) GAIN_CUDA(cudaEventCreate(&v));
+    // default configuration: CTA pairs when any job fills more than one 128-row block
+    TuneChoice c;
+    for (auto& J : P->jobs) c.pair = c.pair || J->job.nlower > split::BM;
+    if (const char* pe = getenv("GAINLS_GEMM_PAIR")) c.pair = c.pair && pe[0] != '0';
+    if (flags & GAIN_PLAN_AUTOTUNE) {
+        const std::string key = plan_shape_key(P.get());
+        bool hit = false;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                c = it->second;
+                hit = true;
+            }
+        }
+        if (!hit) {
+            plan_apply(P.get(), c);
+            GAIN_TRY(plan_build(P.get()));   // layouts and sizes for the size classes
+            GAIN_TRY(plan_autotune(P.get(), &c));
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            g_tune_cache[key] = c;
+        }
+        P->tuned = true;
+    }
+    plan_apply(P.get(), c);
+    GAIN_TRY(plan_build(P.get()));
+    *out = P.release();
+    return GAIN_OK;
+}
+
+gain_status gain_plan_run(gain_plan P, gain_stats* job_stats, gain_plan_stats* stats) {
+    clear_error();
+    if (!P) return set_error(GAIN_ERR_INVALID_ARG, "plan is NULL");
+    GAIN_TRY(check_engine(P->e));
+    double ms = 0.0;
+    const gain_status s = plan_replay(P, &ms);
+    const int nj = (int)P->jobs.size();
+    if (job_stats && (int)P->job_stats.size() == nj)
+        for (int q = 0; q < nj; ++q) job_stats[q] = P->job_stats[q];
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        stats->device_ms = ms;
+        float g1 = 0.f, g2 = 0.f;
+        cudaEventElapsedTime(&g1, P->ev[1], P->ev[2]);
+        cudaEventElapsedTime(&g2, P->ev[3], P->ev[4]);
+        stats->gemm1_ms = g1;
+        stats->gemm2_ms = g2;
+        stats->jobs = nj;
+        for (int q = 0; q < nj && q < (int)P->job_stats.size(); ++q) {
+            stats->transitions += P->job_stats[q].rows * P->job_stats[q].cols;
+            stats->refined += P->job_stats[q].refined;
+            stats->uncertified += P->job_stats[q].uncertified;
+            stats->failed_jobs += P->jobs[q]->status != GAIN_OK;
+            const int k = P->jobs[q]->klass;
+            stats->beta2[k] = P->jobs[q]->p2.beta;
+            stats->slices2[k] = P->jobs[q]->p2.slices;
+        }
+        stats->graph_nodes = P->graph_nodes;
+        stats->kernel_launches = P->kernel_nodes;
+        stats->gemm1_tiles = P->real1;
+        stats->gemm2_tiles = P->real2;
+        stats->units = P->units;
+        stats->pair = P->pair ? 1 : 0;
+        stats->captures = P->captures;
+        stats->tuned = P->tuned ? 1 : 0;
+        stats->tune_ms = P->tune_ms;
+        stats->tensor_flops = P->flops;
+    }
+    return s;
+}
+
+gain_status gain_plan_amp_device(gain_plan P, int job, const double** amp, int* ld) {
+    clear_error();
+    if (!P || !amp || !ld) return set_error(GAIN_ERR_INVALID_ARG, "gain_plan_amp_device: NULL argument");
+    if (job < 0 || job >= (int)P->jobs.size()) return set_error(GAIN_ERR_INVALID_ARG, "job %d out of range", job);
+    if (P->job_stats.empty() || P->jobs[job]->status != GAIN_OK)
+        return set_error(GAIN_ERR_NOT_READY, "job %d has no completed run", job);
+    *amp = P->jobs[job]->amp.p;
+    *ld = P->jobs[job]->Nupad;
+    return GAIN_OK;
+}
+
+gain_status gain_plan_select(gain_plan P, int job) {
+    clear_error();
+    if (!P) return set_error(GAIN_ERR_INVALID_ARG, "plan is NULL");
+    GAIN_TRY(check_engine(P->e));
+    if (job < 0 || job >= (int)P->jobs.size()) return set_error(GAIN_ERR_INVALID_ARG, "job %d out of range", job);
+    PlanJob& J = *P->jobs[job];
+    if (P->job_stats.empty() || J.status != GAIN_OK) return set_error(GAIN_ERR_NOT_READY, "job %d has no completed run", job);
+    gain_engine e = P->e;
+    GAIN_TRY(lines_settle(e));
+    const size_t n = (size_t)J.Bpad * J.Nupad;
+    GAIN_TRY(e->amp.alloc(n));
+    GAIN_TRY(e->ampbnd.alloc(n));
+    GAIN_CUDA(cudaMemcpyAsync(e->amp.p, J.amp.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, e->st));
+    GAIN_CUDA(cudaMemcpyAsync(e->ampbnd.p, J.ampbnd.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, e->st));
+    GAIN_TRY(e->d_lower.alloc(J.B));
+    GAIN_TRY(e->d_upper.alloc(J.Nu));
+    GAIN_CUDA(cudaMemcpyAsync(e->d_lower.p, J.d_lower.p, sizeof(int) * J.B, cudaMemcpyDeviceToDevice, e->st));
+    GAIN_CUDA(cudaMemcpyAsync(e->d_upper.p, J.d_upper.p, sizeof(int) * J.Nu, cudaMemcpyDeviceToDevice, e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    e->amp_rows = J.B;
+    e->amp_cols = J.Nu;
+    e->amp_ld = J.Nupad;
+    e->amp_job = job_key(&J.job, 0, 0);
+    e->have_amp = true;
+    e->have_bnd = true;
+    return GAIN_OK;
+}
+
+gain_status gain_plan_destroy(gain_plan P) {
+    clear_error();
+    delete P;
+    return GAIN_OK;
+}

@@ -175,6 +175,7 @@ struct TextArgs {
     // those values (ovr_idx sorted, n_ovr entries)
     struct HardLine { long long idx; double A, nu, eI, I; };
     HardLine* hard;                        // may be null (no collection)
+    const double* pow10;                   // [601]: pow10[k + 300] = 10^k correctly rounded
     unsigned int* nhard;
     int hard_cap;
     const long long* ovr_idx;

@@ -7,6 +7,7 @@ namespace gain {
 
 struct LineVals {
     double nu, ls, A, I;
+    double e2;  // exp(-beta nu) as the intensity used it (0 without the intensity)
     int keep;   // the reference writes the line: nu in FREQ-WINDOW, nu >= 1e-40, A >= THRESH_LINE
 };
 
@@ -35,13 +36,15 @@ __device__ __forceinline__ LineVals line_eval(const double* amp, long off, doubl
     v.A = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(p.acoef_2jI1, v.ls), anu), anu), anu);   // :93
     v.keep = (v.nu >= p.freq_lo && v.nu <= p.freq_hi && v.nu >= 1e-40 && v.A >= p.thresh) ? 1 : 0;
     v.I = 0.0;
+    v.e2 = 0.0;
     if (p.with_intensity && v.nu >= 1e-40) {
         // CMCOEF*A*gns*(2jF+1)*exp(-beta E'')*(1-exp(-beta nu))/(nu^2 Q), :101-102
         double t = __dmul_rn(p.cmcoef, v.A);
         t = __dmul_rn(t, p.gnsF);
         t = __dmul_rn(t, p.two_jF1);
         t = __dmul_rn(t, exp(-p.beta * (eIr - p.zpe)));
-        t = __dmul_rn(t, 1.0 - exp(-p.beta * v.nu));
+        v.e2 = exp(-p.beta * v.nu);
+        t = __dmul_rn(t, 1.0 - v.e2);
         v.I = __ddiv_rn(t, __dmul_rn(__dmul_rn(v.nu, v.nu), p.q_part));
     }
     return v;

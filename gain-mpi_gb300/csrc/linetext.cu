@@ -30,19 +30,22 @@ constexpr int kStageMax = 200 * 1024;   // shared-memory staging of one block's 
 //   delta <= 2^-52 (7 + 2 e2 / (1 - e2)),  e2 = exp(-beta nu)
 // (the rounding of 1 - e2 amplifies the exp difference); five times that is allowed.  The
 // line is hard when a ten-digit rounding boundary lies within delta of I (or the decimal
-// exponent could change, or I is zero, tiny, huge or not finite).  x = |I| 10^(9 - e) is
-// formed with log10/exp10 and carries a relative error below 2^-51, covered by the margin.
-__device__ __forceinline__ bool intensity_hard(double I, double nu, double beta) {
+// exponent could change, or I is zero, tiny, huge or not finite).  x = |I| 10^(9 - e) comes
+// from the correctly rounded power of ten (pow10[k + 300] = 10^k) and one rounded product: a
+// relative error of at most 2^-52, covered by the margin.  The decimal exponent e starts from
+// the binary one and is corrected by comparing x with 10^9 and 10^10 (exact doubles).
+__device__ __forceinline__ bool intensity_hard(double I, double e2, const double* __restrict__ pow10) {
     const double a = fabs(I);
     if (!(a >= 1e-290 && a <= 1e290)) return true;
-    const double e2 = exp(-beta * nu);
     if (!(e2 < 1.0)) return true;
     const double delta = 0x1p-52 * (40.0 + 8.0 * e2 / (1.0 - e2));
     if (!(delta < 1e-6)) return true;
-    int e10 = (int)floor(log10(a));
-    double x = a * exp10((double)(9 - e10));
-    if (x < 1e9) x *= 10.0;
-    else if (x >= 1e10) x *= 0.1;
+    const int e2b = (int)((__double_as_longlong(a) >> 52) & 0x7ff) - 1023;   // a is normal here
+    int k = 9 - (int)floorf((float)e2b * 0.30103f);
+    k = max(-300, min(300, k));
+    double x = a * __ldg(&pow10[k + 300]);
+    if (x < 1e9 && k < 300) x = a * __ldg(&pow10[k + 301]);
+    else if (x >= 1e10 && k > -300) x = a * __ldg(&pow10[k + 299]);
     if (!(x >= 1e9 + 1.0 && x <= 1e10 - 2.0)) return true;
     const double fr = x - floor(x);
     return fabs(fr - 0.5) <= (delta + 0x1p-50) * x + 1e-6;
@@ -60,14 +63,16 @@ __device__ __forceinline__ double intensity_of(const TextArgs& t, long idx, doub
 }
 
 // The fields of line idx; false when the line is not written.  a_out receives the printed
-// amplitudes (kMaxDegSlots at most).  eI_out (optional) receives the lower energy.
+// amplitudes (kMaxDegSlots at most); eI_out / e2_out (optional) the lower energy and the
+// exp(-beta nu) of the intensity.
 __device__ __forceinline__ bool line_fields(const TextArgs& t, long idx, double* a_out, fmt::LineFields& f,
-                                            double* eI_out = nullptr) {
+                                            double* eI_out = nullptr, double* e2_out = nullptr) {
     const int r = (int)(idx / t.cols), c = (int)(idx - (long)r * t.cols);
     const long off = (long)r * t.ld + c;
     const LineVals v = line_eval(t.amp, off, t.eI[r], t.eF[c], t.p);
     if (!v.keep) return false;
     if (eI_out) *eI_out = t.eI[r];
+    if (e2_out) *e2_out = v.e2;
     int namp = 1;
     if (t.p.nslot == 0) {
         a_out[0] = t.amp[off];
@@ -102,9 +107,9 @@ __device__ __forceinline__ long line_text(const TextArgs& t, long idx, fmt::Sink
 __device__ __forceinline__ long line_length(const TextArgs& t, long idx) {
     double a[kMaxDegSlots];
     fmt::LineFields f;
-    double eI = 0.0;
-    if (!line_fields(t, idx, a, f, &eI)) return 0;
-    if (t.hard && t.p.with_intensity && intensity_hard(f.intensity, f.nu, t.p.beta)) {
+    double eI = 0.0, e2 = 0.0;
+    if (!line_fields(t, idx, a, f, &eI, &e2)) return 0;
+    if (t.hard && t.p.with_intensity && intensity_hard(f.intensity, e2, t.pow10)) {
         const unsigned int k = atomicAdd(t.nhard, 1u);
         if ((int)k < t.hard_cap) t.hard[k] = TextArgs::HardLine{(long long)idx, f.A, f.nu, eI, f.intensity};
     }

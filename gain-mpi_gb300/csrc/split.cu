@@ -251,13 +251,20 @@ __device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, in
     *hi = (int)(((long)(c + 1) * nkb) / nch);
 }
 
+// The arguments of a tile: the launch's own, or (grouped launch) those of the tile's group.
+template <bool G>
+__device__ __forceinline__ const GemmArgs& group_args(const GemmArgs& a, const Tile& tl) {
+    if constexpr (G) return a.groups[tl.group].args;
+    else return a;
+}
+
 // ------------------------------------------------------------------- the GEMM kernel
 // SMAX / CMAX: compile-time bounds of the slices and chunks a launch may use (register arrays
 // of the epilogue are sized by them).  PAIR: the two CTAs of a cluster compute one 256 x 128
 // tile together -- each loads its 128 rows of A and 64 of the 128 rows of B, the first CTA
 // (rank 0) issues the M = 256 MMAs for both, and each CTA's epilogue reads its own TMEM rows.
 // Every shared-memory operand byte then serves twice the MMA work of the single-CTA form.
-template <int SMAX, int CMAX, bool PAIR>
+template <int SMAX, int CMAX, bool PAIR, bool GROUPED>
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
              const GemmArgs a) {
@@ -300,7 +307,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0 && lane == 0) {
+    if (!GROUPED && warp == 0 && lane == 0) {
         asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmA) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&tmB) : "memory");
     }
@@ -326,10 +333,14 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             bool ok = true;
             for (int t = unit; t < a.ntiles && ok; t += nunits) {
                 const Tile tl = a.tiles[t];
-                for (int p = 0; p < a.nprods && ok; ++p) {
-                    const Prod pr = a.prods[p];
+                if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
+                const GemmArgs& g = group_args<GROUPED>(a, tl);
+                const CUtensorMap* mapA = GROUPED ? &a.groups[tl.group].tmA : &tmA;
+                const CUtensorMap* mapB = GROUPED ? &a.groups[tl.group].tmB : &tmB;
+                for (int p = 0; p < g.nprods && ok; ++p) {
+                    const Prod pr = g.prods[p];
                     int lo, hi;
-                    chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
+                    chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
                     // one stage holds up to KS consecutive k-blocks of the pass
                     for (int kb = lo; kb < hi; kb += KS) {
                         const int nk = hi - kb < KS ? hi - kb : KS;
@@ -343,18 +354,18 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const uint32_t fb = cluster_map(smem_u32(&full[stage]), 0);
                             if (rank == 0) mbar_expect_tx(smem_u32(&full[stage]), 2u * (uint32_t)nk * (BOX_A + BOXB));
                             for (int h = 0; h < nk; ++h) {
-                                tma_load_3d_pair(smem_u32(sA + stage * STA + h * BOX_A), &tmA, fb,
+                                tma_load_3d_pair(smem_u32(sA + stage * STA + h * BOX_A), mapA, fb,
                                                  tl.a_k0 + (kb + h) * BK, tl.m0 + (int)rank * BM, pr.ia);
-                                tma_load_3d_pair(smem_u32(sB + stage * STB + h * BOXB), &tmB, fb,
+                                tma_load_3d_pair(smem_u32(sB + stage * STB + h * BOXB), mapB, fb,
                                                  tl.b_k0 + (kb + h) * BK, tl.n0 + (int)rank * (BN / 2), pr.ib);
                             }
                         } else {
                             const uint32_t fb = smem_u32(&full[stage]);
                             mbar_expect_tx(fb, (uint32_t)nk * (BOX_A + BOX_B));
                             for (int h = 0; h < nk; ++h) {
-                                tma_load_3d(smem_u32(sA + stage * STA + h * BOX_A), &tmA, fb,
+                                tma_load_3d(smem_u32(sA + stage * STA + h * BOX_A), mapA, fb,
                                             tl.a_k0 + (kb + h) * BK, tl.m0, pr.ia);
-                                tma_load_3d(smem_u32(sB + stage * STB + h * BOXB), &tmB, fb,
+                                tma_load_3d(smem_u32(sB + stage * STB + h * BOXB), mapB, fb,
                                             tl.b_k0 + (kb + h) * BK, tl.n0, pr.ib);
                             }
                         }
@@ -385,10 +396,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             bool ok = true, any = false;
             for (int t = unit; t < a.ntiles && ok; t += nunits) {
                 const Tile tl = a.tiles[t];
-                for (int p = 0; p < a.nprods && ok; ++p) {
-                    const Prod pr = a.prods[p];
+                if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
+                const GemmArgs& g = group_args<GROUPED>(a, tl);
+                for (int p = 0; p < g.nprods && ok; ++p) {
+                    const Prod pr = g.prods[p];
                     int lo, hi;
-                    chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
+                    chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
                     if (hi <= lo) continue;
                     const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
                     if (!mbar_wait(smem_u32(&accempty[b]), aphase ^ 1, abort_flag, a.err, 2)) {
@@ -449,16 +462,18 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         const int row_in_tile = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         const float two24 = 16777216.0f;
-        const int s = a.slices;
         uint32_t acc_cnt = 0;
         bool ok = true;
         for (int t = unit; t < a.ntiles && ok; t += nunits) {
             const Tile tl = a.tiles[t];
+            if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
+            const GemmArgs& g = group_args<GROUPED>(a, tl);
+            const int s = g.slices;
             bool first = true;
-            for (int p = 0; p < a.nprods && ok; ++p) {
-                const Prod pr = a.prods[p];
+            for (int p = 0; p < g.nprods && ok; ++p) {
+                const Prod pr = g.prods[p];
                 int lo, hi;
-                chunk_range(tl.nkb, a.nchunks, pr.chunk, &lo, &hi);
+                chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
                 if (hi <= lo) continue;
                 const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
                 if (!mbar_wait(smem_u32(&accfull[b]), aphase, abort_flag, a.err, 5)) {
@@ -466,7 +481,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     break;
                 }
                 tc_fence_after();
-                const int sh = fix_bits(a.beta) - pr.t * a.beta;
+                const int sh = fix_bits(g.beta) - pr.t * g.beta;
 #pragma unroll 1
                 for (int c = 0; c < BN / 32; ++c) {
                     uint32_t acc[32], lo_r[32], hi_r[32];
@@ -501,13 +516,13 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             // Row terms live in registers; the statistics of 32 columns at a time are read one
             // column per lane and broadcast with shuffles (no shared memory, no cross-warp sync).
             const int r = tl.m0 + (int)rank * BM + row_in_tile;
-            const bool rvalid = r < a.rows_valid;
-            const int eA = a.A.e[r];
-            const int nnzA = a.A.nnz[r];
-            const float l2A = a.A.l2[r];
-            const float inA = a.A.inerr ? a.A.inerr[r] : 0.0f;
-            const float* dvA = a.A.dnv + (long)r * MAX_SLICES;
-            const float* rvA = a.A.rnv + (long)r * MAX_SLICES;
+            const bool rvalid = r < g.rows_valid;
+            const int eA = g.A.e[r];
+            const int nnzA = g.A.nnz[r];
+            const float l2A = g.A.l2[r];
+            const float inA = g.A.inerr ? g.A.inerr[r] : 0.0f;
+            const float* dvA = g.A.dnv + (long)r * MAX_SLICES;
+            const float* rvA = g.A.rnv + (long)r * MAX_SLICES;
             const float rlastA = rvA[s - 1];
             // Row terms of the certificates.  The cheap forms need one value per column (all
             // rounded up):
@@ -518,34 +533,34 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             // that fail a cheap test are checked again with the exact per-chunk and two-order
             // forms, which read the column's statistics directly.
             float dnAmax = 0.0f, sA = 0.0f, sumdA = 0.0f;
-            for (int c = 0; c < a.nchunks; ++c) dnAmax = fmaxf(dnAmax, a.A.dn[(long)r * a.nchunks + c]);
+            for (int c = 0; c < g.nchunks; ++c) dnAmax = fmaxf(dnAmax, g.A.dn[(long)r * g.nchunks + c]);
             for (int i = 0; i < s; ++i) {
                 const float dv = dvA[i];
                 // |running sum| <= 2^kFixTotal SA SB, S = sum_i 2^{-(i+1) beta} ||d_i||: below 2^62
                 // (SA SB < 2^12) the int64 recombination cannot overflow
-                sA = __fmaf_ru(pow2f(-(i + 1) * a.beta), dv, sA);
+                sA = __fmaf_ru(pow2f(-(i + 1) * g.beta), dv, sA);
                 sumdA = __fadd_ru(sumdA, dv);
             }
-            const float sigA = __fmul_ru(sumdA, pow2f(-(s + 1) * a.beta));
-            const float cf64A = __fmul_ru(a.c_f64, l2A);
+            const float sigA = __fmul_ru(sumdA, pow2f(-(s + 1) * g.beta));
+            const float cf64A = __fmul_ru(g.c_f64, l2A);
             float rowerr2 = 0.0f;
             unsigned long long vmax = 0ull;
-            double* orow = a.out + (long)r * a.ldo;
+            double* orow = g.out + (long)r * g.ldo;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
                 // this lane's column of the group of 32: its five summary values
                 const int mycol = tl.n0 + c * 32 + lane;
-                const int ceB = __ldg(&a.B.e[mycol]);
-                const float cl2 = __ldg(&a.B.l2[mycol]);   // 0 exactly for an all-zero column
-                const float* dvB = a.B.dnv + (long)mycol * MAX_SLICES;
-                const float* rvB = a.B.rnv + (long)mycol * MAX_SLICES;
+                const int ceB = __ldg(&g.B.e[mycol]);
+                const float cl2 = __ldg(&g.B.l2[mycol]);   // 0 exactly for an all-zero column
+                const float* dvB = g.B.dnv + (long)mycol * MAX_SLICES;
+                const float* rvB = g.B.rnv + (long)mycol * MAX_SLICES;
                 float crho = 0.0f, csB = 0.0f, cdnmax = 0.0f;
                 for (int k = 0; k < s; ++k) {
-                    crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * a.beta)));
-                    csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * a.beta), __ldg(&dvB[k])));
+                    crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * g.beta)));
+                    csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * g.beta), __ldg(&dvB[k])));
                 }
-                for (int cc = 0; cc < a.nchunks; ++cc)
-                    cdnmax = fmaxf(cdnmax, __ldg(&a.B.dn[(long)mycol * a.nchunks + cc]));
+                for (int cc = 0; cc < g.nchunks; ++cc)
+                    cdnmax = fmaxf(cdnmax, __ldg(&g.B.dn[(long)mycol * g.nchunks + cc]));
 #pragma unroll 1
                 for (int h = 0; h < 2; ++h) {
                     uint32_t lo_r[16], hi_r[16];
@@ -571,61 +586,61 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         const unsigned long long vbits = scaled_bits(run, eA + eB - kFixTotal, &av);
                         orow[col] = __longlong_as_double((long long)vbits);
                         if (nnzA == 0 || l2B == 0.0f) {   // an exact zero
-                            if (a.bnd) a.bnd[(long)r * a.ldb + col] = 0.0f;
+                            if (g.bnd) g.bnd[(long)r * g.ldb + col] = 0.0f;
                             continue;
                         }
                         bool exact = __fmul_ru(sA, sB) < 4096.0f;
                         if (exact && __fmul_ru(dnAmax, dnBmax) >= two24) {
-                            for (int cc = 0; cc < a.nchunks; ++cc)
-                                if (__fmul_ru(a.A.dn[(long)r * a.nchunks + cc],
-                                              __ldg(&a.B.dn[(long)col * a.nchunks + cc])) >= two24)
+                            for (int cc = 0; cc < g.nchunks; ++cc)
+                                if (__fmul_ru(g.A.dn[(long)r * g.nchunks + cc],
+                                              __ldg(&g.B.dn[(long)col * g.nchunks + cc])) >= two24)
                                     exact = false;
                         }
                         const float f64b = __fmul_ru(cf64A, l2B);
-                        const float limit = a.flag_mode == 1 ? fmaxf(a.tol * av, f64b) : f64b;
-                        float bound = __fadd_ru(__fmaf_ru(rlastA, l2B, __fmul_ru(sigA, rhoB)), a.c_fix);
+                        const float limit = g.flag_mode == 1 ? fmaxf(g.tol * av, f64b) : f64b;
+                        float bound = __fadd_ru(__fmaf_ru(rlastA, l2B, __fmul_ru(sigA, rhoB)), g.c_fix);
                         bound = __fmaf_ru(inA, l2B, bound);
-                        if (a.flag_mode != 0 && bound > limit) {
+                        if (g.flag_mode != 0 && bound > limit) {
                             // |x^ y^ - C| <= ||x^ - X|| ||y^|| + sum_i 2^{-(i+1)b} ||d_i(x)|| ||y^ - Y^(s-1-i)||
                             // and the same with x and y exchanged; the smaller of the two holds
-                            const float* cdv = a.B.dnv + (long)col * MAX_SLICES;
-                            const float* crv = a.B.rnv + (long)col * MAX_SLICES;
+                            const float* cdv = g.B.dnv + (long)col * MAX_SLICES;
+                            const float* crv = g.B.rnv + (long)col * MAX_SLICES;
                             float bA = __fmul_ru(rlastA, l2B);
                             float bB = __fmul_ru(__ldg(&crv[s - 1]), l2A);
                             for (int i = 0; i < s; ++i) {
-                                const float w = pow2f(-(i + 1) * a.beta);
+                                const float w = pow2f(-(i + 1) * g.beta);
                                 bA = __fmaf_ru(__fmul_ru(w, dvA[i]), __ldg(&crv[s - 1 - i]), bA);
                                 bB = __fmaf_ru(__fmul_ru(w, __ldg(&cdv[i])), rvA[s - 1 - i], bB);
                             }
-                            bound = __fmaf_ru(inA, l2B, __fadd_ru(fminf(bA, bB), a.c_fix));
+                            bound = __fmaf_ru(inA, l2B, __fadd_ru(fminf(bA, bB), g.c_fix));
                         }
-                        if (exact && rvalid && col < a.cols_valid) {
+                        if (exact && rvalid && col < g.cols_valid) {
                             const unsigned long long vb = vbits & 0x7FFFFFFFFFFFFFFFull;
                             vmax = vb > vmax ? vb : vmax;
                         }
-                        if (a.bnd) {
+                        if (g.bnd) {
                             // absolute bound: units 2^{eA+eB}; below float's normal range the
                             // smallest normal scale over-states it (still a bound)
                             const int es = eA + eB;
-                            a.bnd[(long)r * a.ldb + col] =
+                            g.bnd[(long)r * g.ldb + col] =
                                 !exact || es > 127 ? __int_as_float(0x7f800000) : __fmul_ru(bound, pow2f(max(es, -126)));
                         }
-                        if (a.rowerr2) {
+                        if (g.rowerr2) {
                             const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
                             rowerr2 = __fmaf_ru(bb, bb, rowerr2);
                         }
                         // certification: flag_mode 1 -> within max(tol |value|, FP64 bound of the
                         // same dot product); flag_mode 2 -> within the FP64 bound (FP64-grade)
-                        const bool flag = !exact || (a.flag_mode != 0 && bound > limit);
-                        if (flag && rvalid && col < a.cols_valid) {
-                            const unsigned int idx = atomicAdd(a.nflags, 1u);
-                            if ((int)idx < a.max_flags) a.flags[idx] = make_int2(r, col);
+                        const bool flag = !exact || (g.flag_mode != 0 && bound > limit);
+                        if (flag && rvalid && col < g.cols_valid) {
+                            const unsigned int idx = atomicAdd(g.nflags, 1u);
+                            if ((int)idx < g.max_flags) g.flags[idx] = make_int2(r, col);
                         }
                     }
                 }
             }
-            if (a.absmax && vmax) atomicMax(a.absmax, vmax);
-            if (a.rowerr2 && rvalid && rowerr2 > 0.0f) atomicAdd(&a.rowerr2[r], rowerr2);
+            if (g.absmax && vmax) atomicMax(g.absmax, vmax);
+            if (g.rowerr2 && rvalid && rowerr2 > 0.0f) atomicAdd(&g.rowerr2[r], rowerr2);
             // make sure TMEM reads finished before the next tile overwrites the running sums
             tc_fence_before();
         }
@@ -1171,11 +1186,15 @@ size_t gemm_smem_bytes() {   // the larger of the two stage rings (the pair's th
 // GEMM: up to 8 slices in one chunk; second GEMM: up to 6 slices in up to 8 chunks) and a
 // general one, each as a single CTA and as a CTA pair.
 typedef void (*GemmKernel)(const CUtensorMap, const CUtensorMap, const GemmArgs);
-static GemmKernel gemm_kernel_for(int slices, int chunks, bool pair) {
-    if (slices <= 8 && chunks <= 1) return pair ? k_digit_gemm<8, 1, true> : k_digit_gemm<8, 1, false>;
+template <bool G>
+static GemmKernel gemm_kernel_of(int slices, int chunks, bool pair) {
+    if (slices <= 8 && chunks <= 1) return pair ? k_digit_gemm<8, 1, true, G> : k_digit_gemm<8, 1, false, G>;
     if (slices <= 6 && chunks <= MAX_CHUNKS)
-        return pair ? k_digit_gemm<6, MAX_CHUNKS, true> : k_digit_gemm<6, MAX_CHUNKS, false>;
-    return pair ? k_digit_gemm<MAX_SLICES, MAX_CHUNKS, true> : k_digit_gemm<MAX_SLICES, MAX_CHUNKS, false>;
+        return pair ? k_digit_gemm<6, MAX_CHUNKS, true, G> : k_digit_gemm<6, MAX_CHUNKS, false, G>;
+    return pair ? k_digit_gemm<MAX_SLICES, MAX_CHUNKS, true, G> : k_digit_gemm<MAX_SLICES, MAX_CHUNKS, false, G>;
+}
+static GemmKernel gemm_kernel_for(int slices, int chunks, bool pair, bool grouped = false) {
+    return grouped ? gemm_kernel_of<true>(slices, chunks, pair) : gemm_kernel_of<false>(slices, chunks, pair);
 }
 
 // Function attributes are per device: set them once on each device that launches.
@@ -1187,9 +1206,10 @@ static cudaError_t set_attributes_once() {
     if (e != cudaSuccess) return e;
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load() & bit) return cudaSuccess;
-    const GemmKernel ks[6] = {k_digit_gemm<8, 1, false>,          k_digit_gemm<6, MAX_CHUNKS, false>,
-                              k_digit_gemm<MAX_SLICES, MAX_CHUNKS, false>, k_digit_gemm<8, 1, true>,
-                              k_digit_gemm<6, MAX_CHUNKS, true>,   k_digit_gemm<MAX_SLICES, MAX_CHUNKS, true>};
+    GemmKernel ks[12];
+    const int cfg[3][2] = {{8, 1}, {6, MAX_CHUNKS}, {MAX_SLICES, MAX_CHUNKS}};
+    for (int i = 0; i < 12; ++i)
+        ks[i] = gemm_kernel_for(cfg[i % 3][0], cfg[i % 3][1], (i / 3) & 1, i >= 6);
     for (GemmKernel k : ks) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
@@ -1204,6 +1224,8 @@ static cudaError_t set_attributes_once() {
     done.fetch_or(bit);
     return cudaSuccess;
 }
+
+cudaError_t prepare_device() { return set_attributes_once(); }
 
 cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a, int num_sms,
                         cudaStream_t st, bool pair) {
@@ -1234,6 +1256,32 @@ cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const Ge
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k, tmA, tmB, a);
+}
+
+cudaError_t launch_gemm_grouped(const GemmArgs& a, int units, int max_slices, int max_chunks, cudaStream_t st,
+                                bool pair) {
+    const size_t smem = gemm_smem_bytes();
+    cudaError_t e = set_attributes_once();
+    if (e != cudaSuccess) return e;
+    if (a.ntiles <= 0 || units <= 0) return cudaSuccess;
+    if (!a.groups || a.ntiles % units) return cudaErrorInvalidValue;
+    if (max_slices < 1 || max_slices > MAX_SLICES || max_chunks < 1 || max_chunks > MAX_CHUNKS)
+        return cudaErrorInvalidValue;
+    GemmKernel k = gemm_kernel_for(max_slices, max_chunks, pair, true);
+    const CUtensorMap unused = {};   // every tile's maps come from its group
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(pair ? 2 * units : units));
+    cfg.blockDim = dim3(NTHREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = pair ? 2 : 1;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pair ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, unused, unused, a);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,

@@ -31,7 +31,8 @@ struct Tile {
     int a_k0;       // A inner coordinate of k-block 0
     int b_k0;       // B inner coordinate of k-block 0
     int nkb;        // k-blocks of BK
-    int pad[3];
+    int group;      // grouped launch: the tile's group (-1: an empty slot of the schedule)
+    int pad[2];
 };
 
 struct Prod {
@@ -57,9 +58,14 @@ struct RowStats {
     float* inerr;    // optional: ||input error of the row||_2 in units of 2^e
 };
 
+struct GemmGroup;
+
 struct GemmArgs {
     const Tile* tiles;
     int ntiles;
+    // grouped launch: per-group arguments and tensor maps (device memory); tiles, ntiles and
+    // err are the launch's, every other field comes from the tile's group
+    const GemmGroup* groups;
     const Prod* prods;
     int nprods;
     int nchunks;
@@ -92,7 +98,16 @@ struct GemmArgs {
     long ldb;
 };
 
+// One group of a grouped launch: a block pair's operands (tensor maps) and arguments.
+struct alignas(64) GemmGroup {
+    CUtensorMap tmA, tmB;
+    GemmArgs args;
+};
+
 size_t gemm_smem_bytes();
+// The kernels' attributes on the current device (done by the first launch otherwise; call it
+// before capturing launches into a graph).
+cudaError_t prepare_device();
 // pair: CTA pairs computing 256 x 128 tiles (tile m0 multiples of 256, rows padded to 256;
 // the B operand's map with 64-row boxes)
 cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const GemmArgs& a,
@@ -101,6 +116,12 @@ cudaError_t launch_gemm(const CUtensorMap& tmA, const CUtensorMap& tmB, const Ge
 // Tensor map of a digit array [slices][rows_pad][kpad] BF16 (box 64 x box_rows x 1, 128B
 // swizzle; box_rows 128, or 64 for the B operand of a CTA pair).
 bool make_digit_map(CUtensorMap* map, void* base, int kpad, int rows_pad, int slices, int box_rows = BM);
+
+// One persistent launch over the tiles of several groups (block pairs): a.tiles holds
+// ntiles = units x k entries, unit u taking entries u, u + units, ... (empty slots have
+// group -1); a.groups the groups; max_slices / max_chunks bound every group's.
+cudaError_t launch_gemm_grouped(const GemmArgs& a, int units, int max_slices, int max_chunks, cudaStream_t st,
+                                bool pair);
 
 struct SliceArgs {
     const double* src;      // source rows

@@ -64,6 +64,21 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PlanStats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("gemm1_ms", ctypes.c_double), ("gemm2_ms", ctypes.c_double),
+                ("transitions", ctypes.c_longlong), ("refined", ctypes.c_longlong),
+                ("uncertified", ctypes.c_longlong), ("jobs", ctypes.c_int), ("failed_jobs", ctypes.c_int),
+                ("graph_nodes", ctypes.c_int), ("kernel_launches", ctypes.c_int), ("gemm1_tiles", ctypes.c_int),
+                ("gemm2_tiles", ctypes.c_int), ("units", ctypes.c_int), ("pair", ctypes.c_int),
+                ("captures", ctypes.c_int), ("tuned", ctypes.c_int), ("tune_ms", ctypes.c_double),
+                ("tensor_flops", ctypes.c_double), ("beta2", ctypes.c_int * 4), ("slices2", ctypes.c_int * 4)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["beta2"], d["slices2"] = list(self.beta2), list(self.slices2)
+        return d
+
+
 class LineParams(ctypes.Structure):
     _fields_ = [("temperature", ctypes.c_double), ("q_part", ctypes.c_double), ("zpe", ctypes.c_double),
                 ("thresh", ctypes.c_double), ("freq_lo", ctypes.c_double), ("freq_hi", ctypes.c_double),
@@ -195,6 +210,13 @@ def _declare(L):
     L.gain_adjoint_pair_prec.argtypes = [_vp, ctypes.POINTER(PairJob), _dp, _dp, ctypes.c_int, ctypes.POINTER(Stats)]
     L.gain_adjoint_pair_degenerate.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.POINTER(Filters), _dp, _dp,
                                                ctypes.c_int, ctypes.POINTER(Stats)]
+    L.gain_plan_create.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), I, ctypes.POINTER(_vp)]
+    L.gain_plan_run.argtypes = [_vp, ctypes.POINTER(Stats), ctypes.POINTER(PlanStats)]
+    L.gain_plan_select.argtypes = [_vp, I]
+    L.gain_plan_amp_device.argtypes = [_vp, I, ctypes.POINTER(ctypes.c_void_p), _ip]
+    L.gain_plan_destroy.argtypes = [_vp]
+    for name in ("gain_plan_create", "gain_plan_run", "gain_plan_select", "gain_plan_amp_device", "gain_plan_destroy"):
+        getattr(L, name).restype = S
     L.gain_run_plan.argtypes = [ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int,
                                 ctypes.POINTER(SplitOpts), JOB_DONE_FN, _vp, ctypes.POINTER(Stats)]
     L.gain_run_pair_component.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -621,6 +643,60 @@ def run_plan(engines, jobs, path=PATH_SPLIT, tol=0.0, on_done=None):
     if errors:
         raise errors[0]
     return [st[i].as_dict() for i in range(len(jobs))]
+
+
+PLAN_AUTOTUNE = 1
+
+
+class Plan:
+    """gain_plan_*: block pairs run as one unit (two grouped tensor-core launches in a CUDA
+    graph) on one engine.  jobs = [(jindI, gammaI, jindF, gammaF, lower_levels, upper_levels)]."""
+
+    def __init__(self, eng: "Engine", jobs, tol: float = 0.0, autotune: bool = False, beta: int = 0,
+                 slices: int = 0):
+        self.eng = eng
+        self.shapes = []
+        keep = []
+        arr = (PairJob * len(jobs))()
+        for i, (jI, gI, jF, gF, lo, up) in enumerate(jobs):
+            lo, up = _i32(lo), _i32(up)
+            keep += [lo, up]
+            arr[i] = PairJob(jI, gI, jF, gF, len(lo), _p(lo, _ip), len(up), _p(up, _ip))
+            self.shapes.append((len(lo), len(up)))
+        opts = SplitOpts(tol, slices, beta, 0, 0.0)
+        self.h = _vp()
+        check(lib().gain_plan_create(eng.h, arr, len(jobs), ctypes.byref(opts), PLAN_AUTOTUNE if autotune else 0,
+                                     ctypes.byref(self.h)))
+        self.n = len(jobs)
+
+    def run(self, raise_on_error: bool = True):
+        """Replay the plan; returns (plan stats dict, [job stats dicts], status)."""
+        js = (Stats * self.n)()
+        ps = PlanStats()
+        s = lib().gain_plan_run(self.h, js, ctypes.byref(ps))
+        if s != OK and raise_on_error:
+            check(s)
+        return ps.as_dict(), [js[i].as_dict() for i in range(self.n)], s
+
+    def select(self, job: int):
+        """Make job's amplitudes the engine's last run (fetch_amp, lines, lines_text...)."""
+        check(lib().gain_plan_select(self.h, job))
+        self.eng._shape = self.shapes[job]
+
+    def amp(self, job: int) -> np.ndarray:
+        self.select(job)
+        return self.eng.fetch_amp().copy()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gain_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 Engine.lines_text = _lines_text

@@ -274,6 +274,69 @@ gain_status gain_run_plan(gain_engine* engines, int n_engines, const gain_pair_j
                           gain_path path, const gain_split_opts* opts, gain_job_done_fn on_done, void* user,
                           gain_stats* stats);
 
+/* ----------------------------------------------------------------------------------------
+ * Grouped plans: many block pairs as ONE unit on one engine (the batched form of
+ * main.cpp:238-342's loop over (J'', Gamma'') -> (J', Gamma') pairs and their lower states;
+ * no counterpart in the reference, which launches per lower state and per transition,
+ * BaseClasses/GpuManager.cpp:645-746).  The split path of every job runs as
+ *   per-job digit slicing of the lower and upper eigenvectors   (concurrent streams)
+ *   ONE persistent grouped tensor-core launch of the first GEMM over the tiles of all jobs
+ *   per-job FP64 refinement and slicing of H                    (concurrent streams)
+ *   ONE persistent grouped tensor-core launch of the second GEMM over all jobs' tiles
+ *   per-job FP64 refinement of the amplitudes
+ * captured once into a CUDA graph and replayed by gain_plan_run.  The tiles of each grouped
+ * launch are spread over the persistent CTAs longest-first (cost = k-blocks x digit
+ * products), so block pairs of very uneven sizes share one launch.  Each job keeps its own
+ * device buffers; the engine's uploads (bases, expansion tables, dipole, eigenvectors) must
+ * hold every job's inputs.  Jobs are non-degenerate (components 0, 0) with a single dipole
+ * piece.  After gain_plan_run, gain_plan_select makes one job's amplitudes the engine's last
+ * run (for gain_fetch_amp, gain_pair_lines*, gain_pair_lines_text*, ...).
+ *
+ * Re-running after new eigenvectors of the same sizes were uploaded replays the same graph;
+ * when inputs moved (a re-allocated eigenvector buffer, new dipole, bases or tables) the
+ * plan is prepared and captured anew on its next run.  Destroy plans before their engine. */
+typedef struct gain_plan_s* gain_plan;
+
+/* gain_plan_create flags */
+#define GAIN_PLAN_AUTOTUNE 1   /* choose the tile shape (CTA pairs or single CTAs) and, per size
+                                  class of the second GEMM's inner dimension, its digit
+                                  configuration (8-bit x 6 or 7-bit x 7) by timing the plan's
+                                  candidates on first use; the choice is cached per plan shape
+                                  for the process */
+
+typedef struct gain_plan_stats {
+    double device_ms;            /* the graph replay (CUDA events around it) */
+    double gemm1_ms, gemm2_ms;   /* the two grouped GEMM launches inside it */
+    long long transitions;       /* sum over jobs of lower x upper levels */
+    long long refined;           /* H entries and amplitudes recomputed in FP64, all jobs */
+    long long uncertified;       /* as gain_stats.uncertified, all jobs */
+    int jobs, failed_jobs;
+    int graph_nodes;             /* nodes of the captured graph */
+    int kernel_launches;         /* kernel nodes among them */
+    int gemm1_tiles, gemm2_tiles;/* tiles of the two grouped launches (empty slots excluded) */
+    int units;                   /* persistent CTAs (CTA pairs) of each grouped launch */
+    int pair;                    /* 1: 256 x 128 tiles on CTA pairs; 0: 128 x 128 tiles */
+    int captures;                /* graph captures so far */
+    int tuned;                   /* 1: the configuration came from the autotuner */
+    double tune_ms;              /* wall time the autotuner spent (first use) */
+    double tensor_flops;         /* BF16 MMA flops of the two grouped launches (whole tiles) */
+    int beta2[4], slices2[4];    /* second-GEMM digits per size class of its inner dimension K:
+                                    K <= 2048, <= 8192, <= 16384, above (0: class absent) */
+} gain_plan_stats;
+
+gain_status gain_plan_create(gain_engine e, const gain_pair_job* jobs, int n_jobs, const gain_split_opts* opts,
+                             int flags, gain_plan* out);
+/* Run (replay) the plan; job_stats[n_jobs] (may be NULL) receives each job's rows, cols and
+ * refinement counts, stats (may be NULL) the plan's.  Returns the first failing job's status
+ * (a refinement list that overflowed: GAIN_ERR_TOL_NOT_MET; a bounded device wait that gave
+ * up: GAIN_ERR_TIMEOUT); the other jobs' amplitudes stay valid. */
+gain_status gain_plan_run(gain_plan p, gain_stats* job_stats, gain_plan_stats* stats);
+/* Make job's amplitudes (of the last gain_plan_run) the engine's last run. */
+gain_status gain_plan_select(gain_plan p, int job);
+/* Device pointer and leading dimension of job's amplitudes (valid until the next run). */
+gain_status gain_plan_amp_device(gain_plan p, int job, const double** amp, int* ld);
+gain_status gain_plan_destroy(gain_plan p);
+
 /* Device pointer / leading dimension of the last run's amplitude matrix. */
 gain_status gain_pair_amp_device(gain_engine e, const double** amp, int* ld);
 

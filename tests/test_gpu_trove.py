@@ -115,14 +115,16 @@ def test_refinement_overflow_in_an_earlier_piece_fails_the_run(built_lib, monkey
     # 40-bit first-GEMM digits: no H entry certifies FP64-grade, every non-zero one is flagged
     monkeypatch.setenv("GAINLS_GEMM1_BITS", "40")
     counts = []
-    for rng in ((0, nv - 1), (nv - 1, nv)):
+    # the last piece holds the last two vibrational indices (class 1 of rule c4 has only the
+    # even ones, so it must reach vib nv - 2)
+    for rng in ((0, nv - 2), (nv - 2, nv)):
         eng.upload_dipole_pieces([piece(*rng)], nv)
         st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
         assert st["status"] == gainls.OK
         counts.append(st["inexact"])
     first, last = counts
     assert first > last + 1 > 1, counts
-    eng.upload_dipole_pieces([piece(0, nv - 1), piece(nv - 1, nv)], nv)
+    eng.upload_dipole_pieces([piece(0, nv - 2), piece(nv - 2, nv)], nv)
     st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
     assert st["status"] == gainls.OK and st["inexact"] == first + last
     monkeypatch.setenv("GAINLS_MAX_FLAGS", str((first + last) // 2))   # holds the last piece's only
