@@ -157,7 +157,100 @@ k_adj_dm(AdjArgs a, const int2* __restrict__ tiles) {
     }
 }
 
+// ---- the tensor-core form: operands of the two digit GEMMs, their refinement, the scatter
+// out[p][b] = src[row(b) * ld + map[p]] for p < np, b < nb (0 where map[p] < 0 or b >= nb,
+// up to the padded sizes np_pad x nb_pad; row(b) = rows[b], or b without rows).  32 x 32
+// tiles through shared memory: the reads run along map (the source rows), the writes along b.
+__global__ void __launch_bounds__(256)
+k_gather_t(int np_pad, int nb, int nb_pad, const double* __restrict__ src, long ld, const int* __restrict__ rows,
+           const int* __restrict__ map, double* __restrict__ out) {
+    __shared__ double tile[32][33];
+    const int p0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    for (int i = ty; i < 32; i += 8) {
+        const int b = b0 + i, p = p0 + tx;
+        double v = 0.0;
+        if (b < nb && p < np_pad) {
+            const int c = map[p];
+            if (c >= 0) v = src[(long)(rows ? rows[b] : b) * ld + c];
+        }
+        tile[i][tx] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+        const int p = p0 + i, b = b0 + tx;
+        if (p < np_pad && b < nb_pad) out[(long)p * nb_pad + b] = tile[tx][i];
+    }
+}
+
+// FP64 recomputation of the flagged entries of a digit product C[r][c] = sum_k A[r][k] B[c][k]
+// (rows of length K, leading dimensions lda / ldb; one warp per entry).
+__global__ void k_refine_rows(const int2* __restrict__ flags, const unsigned int* nflags, int max_flags,
+                              const double* __restrict__ A, long lda, const double* __restrict__ B, long ldb, int K,
+                              double* C, long ldc) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = min((int)*nflags, max_flags);
+    for (int f = gw; f < n; f += nw) {
+        const int2 rc = flags[f];
+        const double* a = A + (long)rc.x * lda;
+        const double* b = B + (long)rc.y * ldb;
+        double acc = 0.0;
+        for (int k = lane; k < K; k += 32) acc = __fma_rn(a[k], b[k], acc);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) C[(long)rc.x * ldc + rc.y] = acc;
+    }
+}
+
+// dL/dmu_d[vI][vF - startF] += factor_d(F, I) dM[r][c] over the band of every F position r
+// (columns [band_lo[r], band_hi[r]) of the lower positions; F = fmap[r], I = imap[c]).  One
+// block per F position, its threads along the band.
+__global__ void __launch_bounds__(256)
+k_adj_scatter_band(AdjArgs a, const int* __restrict__ fmap, const int* __restrict__ imap,
+                   const int* __restrict__ band_lo, const int* __restrict__ band_hi, const double* __restrict__ dM,
+                   long ld) {
+    const int r = blockIdx.x;
+    const int F = fmap[r];
+    if (F < 0) return;
+    double* dmu = static_cast<double*>(a.dmu);
+    const long ds = (long)a.dipN * a.ncontrF;
+    for (int c = band_lo[r] + threadIdx.x; c < band_hi[r]; c += blockDim.x) {
+        const int I = imap[c];
+        double w[3];
+        if (I < 0 || !adj_factor(a, F, I, w)) continue;
+        const double v = dM[(long)r * ld + c];
+        if (v == 0.0) continue;
+        const long base = (long)(a.vibF[F] - a.startF) + (long)a.vibI[I] * a.ncontrF;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (w[d] != 0.0) atomicAdd(&dmu[base + d * ds], w[d] * v);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_gather_t(int np_pad, int nb, int nb_pad, const double* src, long ld, const int* rows,
+                            const int* map, double* out, cudaStream_t st) {
+    if (np_pad <= 0 || nb_pad <= 0) return cudaSuccess;
+    const dim3 grid((np_pad + 31) / 32, (nb_pad + 31) / 32);
+    k_gather_t<<<grid, 256, 0, st>>>(np_pad, nb, nb_pad, src, ld, rows, map, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_rows(const int2* flags, const unsigned int* nflags, int max_flags, const double* A,
+                               long lda, const double* B, long ldb, int K, double* C, long ldc, int max_blocks,
+                               cudaStream_t st) {
+    k_refine_rows<<<max_blocks, 256, 0, st>>>(flags, nflags, max_flags, A, lda, B, ldb, K, C, ldc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_scatter_band(const AdjArgs& a, int nrows, const int* fmap, const int* imap, const int* band_lo,
+                                    const int* band_hi, const double* dM, long ld, cudaStream_t st) {
+    if (nrows <= 0) return cudaSuccess;
+    k_adj_scatter_band<<<nrows, 256, 0, st>>>(a, fmap, imap, band_lo, band_hi, dM, ld);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_adj_scale(int rows, int cols, const double* dLdS, const double* amp, long ld_amp,
                              double two_scale, void* G, bool fp32, cudaStream_t st) {

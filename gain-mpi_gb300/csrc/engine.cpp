@@ -327,6 +327,15 @@ struct gain_engine_s {
     gain::DevArray<double> primI, hprim, hsym;
     gain::DevArray<double> adj_dLdS, adj_G, adj_dH, adj_dh, adj_vp, adj_dmu;   // adjoint work space
     gain::DevArray<int> adj_iota, adj_tiles;
+    // the tensor-core adjoint: transposed operands, digits, statistics, layout and GEMM lists
+    gain::DevArray<double> adjs_UT, adjs_dhT, adjs_vpT, adjs_dM, adjs_dH;
+    gain::DevArray<__nv_bfloat16> adjs_dig[4];
+    gain::StatsDev adjs_st[4];
+    gain::DevArray<int> adjs_fmap, adjs_imap, adjs_blo, adjs_bhi, adjs_err, adjs_umap;
+    gain::DevArray<int2> adjs_flags;
+    gain::DevArray<unsigned int> adjs_cnt;
+    gain::DevArray<gain::split::Tile> adjs_tiles1, adjs_tiles2;
+    gain::DevArray<gain::split::Prod> adjs_prods1, adjs_prods2;
     gain::DevArray<__nv_bfloat16> Vdig, Hdig, Udig;
     gain::StatsDev Vst, Hst, Ust;
     gain::DevArray<double> H, Hsym;   // H in the GEMM1 layout; contracted with a mixing expansion
@@ -1939,8 +1948,242 @@ namespace {
 // (one pair, (0, 0), for non-degenerate symmetries) with dS/damp = 2 scale amp.  Each pair's
 // forward amplitudes: the last run's when it computed this job and pair, a component slot of
 // the job, else the plain FP64 path (the reference's method).
+// The tensor-core adjoint chain of one component pair after G = dL/damp (FP64 [B][Nu]):
+//   dH = G U                 digit GEMM, rows B, columns the upper symmetric functions, inner Nu
+//   dh = T_F dH, vp = T_I v  the expansions (FP64)
+//   dM = dh^T vp             digit GEMM, rows the upper primitives of the expansion's support
+//                            (grouped by K, padded to 128), columns the lower ones (grouped by
+//                            K, padded to 64), inner the B lower states; only the band tiles
+//   dL/dmu += factor dM      FP64 scatter over the band
+// Entries whose exact-accumulation certificate fails are recomputed in FP64.
+constexpr int kAdjSplitBits = 48;
+gain_status adjoint_split_chain(gain_engine e, const gain_pair_job* job, int dI, int dF, const double* G,
+                                double* tflops) {
+    using split::BK;
+    using split::BM;
+    using split::BN;
+    const Basis& bI = e->bases[job->jindI];
+    const Basis& bF = e->bases[job->jindF];
+    Inflation& iI = e->infl[job->jindI];
+    Inflation& iF = e->infl[job->jindF];
+    const Eig& EI = *e->eig[{job->jindI, job->gammaI}];
+    const Eig& EF = *e->eig[{job->jindF, job->gammaF}];
+    GammaMaps* mI = gamma_maps(e, job->jindI, job->gammaI, dI);
+    GammaMaps* mF = gamma_maps(e, job->jindF, job->gammaF, dF);
+    if (!mI || !mF) return GAIN_ERR_OOM;
+    const WignerTab* wt = wigner_of(e, job->jindI, job->jindF);
+    cudaStream_t st = e->st;
+    const int B = job->nlower, Nu = job->nupper, NtF = iF.Ntot[job->gammaF];
+    const int Bpad = round_up(B, BM), Bk = round_up(B, BK);
+    const int Nuk = round_up(Nu, BK), NtFpad = round_up(NtF, BN);
+    const SplitParams pA = choose_params(Nuk, nullptr, kAdjSplitBits, 8);
+    const SplitParams pB = choose_params(Bk, nullptr, kAdjSplitBits, 8);
+    const int cap = kMaxFlags;
+    GAIN_TRY(e->adjs_flags.alloc(cap));
+    GAIN_TRY(e->adjs_cnt.alloc(2));
+    GAIN_TRY(e->adjs_cnt.zero(st, 2));
+    GAIN_TRY(e->adjs_err.alloc(1));
+    GAIN_TRY(e->adjs_err.zero(st, 1));
+    double fl = 0.0;
+    auto zero_dig = [&](int k, size_t n, size_t rows, int nch) -> gain_status {
+        GAIN_TRY(e->adjs_dig[k].alloc(n));
+        GAIN_TRY(e->adjs_dig[k].zero(st, n));
+        GAIN_TRY(e->adjs_st[k].alloc(rows, nch, false));
+        GAIN_TRY(e->adjs_st[k].zero(st, rows, nch, false));
+        return GAIN_OK;
+    };
+    // C = A B^T over the listed tiles from digit buffers ka (rowsA rows) and kb (rowsB rows),
+    // inner length ldk; the flags of uncertified entries go to the list behind cnt
+    auto gemm = [&](int ka, int kb, const SplitParams& p, int ldk, int rowsA, int rowsB, double* out, long ldo,
+                    int rows_valid, int cols_valid, const std::vector<split::Tile>& tiles,
+                    DevArray<split::Tile>& dtiles, DevArray<split::Prod>& dprods, unsigned int* cnt) -> gain_status {
+        CUtensorMap ta, tb;
+        if (!split::make_digit_map(&ta, e->adjs_dig[ka].p, ldk, rowsA, p.slices) ||
+            !split::make_digit_map(&tb, e->adjs_dig[kb].p, ldk, rowsB, p.slices))
+            return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (adjoint digits)");
+        const std::vector<split::Prod> pr = make_prods(p);
+        GAIN_TRY(dprods.upload(pr));
+        GAIN_TRY(dtiles.upload(tiles));
+        split::GemmArgs g;
+        memset(&g, 0, sizeof g);
+        g.tiles = dtiles.p;
+        g.ntiles = (int)tiles.size();
+        g.prods = dprods.p;
+        g.nprods = (int)pr.size();
+        g.nchunks = p.chunks;
+        g.beta = p.beta;
+        g.slices = p.slices;
+        g.out = out;
+        g.ldo = ldo;
+        g.A = e->adjs_st[ka].view(false);
+        g.B = e->adjs_st[kb].view(false);
+        g.c_fix = fix_const((int)pr.size());
+        g.c_f64 = (float)((double)(ldk + 64) * std::ldexp(1.0, -53) * 1.01);
+        g.flag_mode = 0;   // only entries whose exact accumulation is not certified
+        g.flags = e->adjs_flags.p;
+        g.nflags = cnt;
+        g.max_flags = cap;
+        g.rows_valid = rows_valid;
+        g.cols_valid = cols_valid;
+        g.err = e->adjs_err.p;
+        GAIN_CUDA(split::launch_gemm(ta, tb, g, e->num_sms, st, false));
+        for (auto& t : tiles) fl += 2.0 * BM * BN * BK * t.nkb * (double)pr.size() / p.chunks;
+        return GAIN_OK;
+    };
+    // ---- dH = G U: A = G rows (inner: upper states), B = U^T rows (upper symmetric functions)
+    {
+        std::vector<int> umap(NtFpad, -1);
+        for (int f = 0; f < NtF; ++f) umap[f] = f;
+        GAIN_TRY(e->adjs_umap.upload(umap));
+        GAIN_TRY(e->adjs_UT.alloc((size_t)NtFpad * Nuk));
+        GAIN_CUDA(launch_gather_t(NtFpad, Nu, Nuk, EF.d.p, EF.nsize, e->d_upper.p, e->adjs_umap.p, e->adjs_UT.p, st));
+        GAIN_TRY(zero_dig(0, (size_t)pA.slices * Bpad * Nuk, Bpad, pA.chunks));
+        GAIN_TRY(zero_dig(1, (size_t)pA.slices * NtFpad * Nuk, NtFpad, pA.chunks));
+        GAIN_TRY(slice(e, G, Nu, nullptr, B, Nu, nullptr, nullptr, Nuk, Bpad, e->adjs_dig[0].p, pA, e->adjs_st[0],
+                       false, nullptr, nullptr, st));
+        GAIN_TRY(slice(e, e->adjs_UT.p, Nuk, nullptr, NtFpad, Nuk, nullptr, nullptr, Nuk, NtFpad, e->adjs_dig[1].p, pA,
+                       e->adjs_st[1], false, nullptr, nullptr, st));
+        std::vector<split::Tile> t;
+        for (int n0 = 0; n0 < NtFpad; n0 += BN)
+            for (int m0 = 0; m0 < Bpad; m0 += BM) {
+                split::Tile x;
+                memset(&x, 0, sizeof x);
+                x.m0 = m0;
+                x.n0 = n0;
+                x.nkb = Nuk / BK;
+                t.push_back(x);
+            }
+        GAIN_TRY(e->adjs_dH.alloc((size_t)Bpad * NtFpad));
+        GAIN_TRY(gemm(0, 1, pA, Nuk, Bpad, NtFpad, e->adjs_dH.p, NtFpad, B, NtF, t, e->adjs_tiles1, e->adjs_prods1,
+                      e->adjs_cnt.p));
+        GAIN_CUDA(launch_refine_rows(e->adjs_flags.p, e->adjs_cnt.p, cap, G, Nu, e->adjs_UT.p, Nuk, Nu, e->adjs_dH.p,
+                                     NtFpad, 2 * e->num_sms, st));
+    }
+    // ---- dh = T_F dH, vp = T_I v (primitive spaces)
+    GAIN_TRY(e->adj_dh.alloc((size_t)B * bF.dimen));
+    GAIN_TRY(e->adj_vp.alloc((size_t)B * bI.dimen));
+    double* dh = e->adj_dh.p;
+    double* vp = e->adj_vp.p;
+    GAIN_CUDA(launch_expand_levels(iF.dimen, job->gammaF, iF.maxcoeff, dF, iF.sdeg[job->gammaF], NtF, iF.dijterms.p,
+                                   iF.dicontr.p, iF.dN[job->gammaF]->p, iF.drepres[job->gammaF]->p,
+                                   (const double*)e->adjs_dH.p, NtFpad, e->adj_iota.p, dh, bF.dimen, B, st));
+    GAIN_CUDA(launch_expand_levels(iI.dimen, job->gammaI, iI.maxcoeff, dI, iI.sdeg[job->gammaI], iI.Ntot[job->gammaI],
+                                   iI.dijterms.p, iI.dicontr.p, iI.dN[job->gammaI]->p, iI.drepres[job->gammaI]->p,
+                                   EI.d.p, EI.nsize, e->d_lower.p, vp, bI.dimen, B, st));
+    // ---- the band layout over the expansions' supports, grouped by K
+    std::vector<int> fmap, imap, fstart(bF.J + 2, 0), istart(bI.J + 2, 0);
+    for (int k = 0; k <= bF.J; ++k) {
+        for (int q = mF->sup_start[k]; q < mF->sup_start[k + 1]; ++q) fmap.push_back(mF->support[q]);
+        while (fmap.size() % BM) fmap.push_back(-1);
+        fstart[k + 1] = (int)fmap.size();
+    }
+    for (int k = 0; k <= bI.J; ++k) {
+        for (int q = mI->sup_start[k]; q < mI->sup_start[k + 1]; ++q) imap.push_back(mI->support[q]);
+        while (imap.size() % BK) imap.push_back(-1);
+        istart[k + 1] = (int)imap.size();
+    }
+    const int Fpad = std::max((int)fmap.size(), BM), Ipad = (int)imap.size();
+    fmap.resize(Fpad, -1);
+    const int ldM = round_up(Ipad + BN, BN);
+    imap.resize(ldM, -1);
+    std::vector<int> blo(Fpad, 0), bhi(Fpad, 0);
+    std::vector<split::Tile> t2;
+    for (int k = 0; k <= bF.J; ++k) {
+        if (fstart[k + 1] == fstart[k]) continue;
+        int lo = 0, hi = Ipad;
+        if (!wt) {
+            const int klo = std::max(k - 1, 0), khi = std::min(k + 1, bI.J);
+            if (klo > khi) continue;
+            lo = istart[klo];
+            hi = istart[khi + 1];
+        }
+        if (hi <= lo) continue;
+        for (int r = fstart[k]; r < fstart[k + 1]; ++r) {
+            blo[r] = lo;
+            bhi[r] = hi;
+        }
+        for (int m0 = fstart[k]; m0 < fstart[k + 1]; m0 += BM)
+            for (int n0 = lo; n0 < hi; n0 += BN) {
+                split::Tile x;
+                memset(&x, 0, sizeof x);
+                x.m0 = m0;
+                x.n0 = n0;
+                x.nkb = Bk / BK;
+                t2.push_back(x);
+            }
+    }
+    GAIN_TRY(e->adjs_fmap.upload(fmap));
+    GAIN_TRY(e->adjs_imap.upload(imap));
+    GAIN_TRY(e->adjs_blo.upload(blo));
+    GAIN_TRY(e->adjs_bhi.upload(bhi));
+    // ---- dM = dh^T vp on the band: A = dh^T rows (upper positions), B = vp^T rows (lower)
+    GAIN_TRY(e->adjs_dhT.alloc((size_t)Fpad * Bk));
+    GAIN_TRY(e->adjs_vpT.alloc((size_t)ldM * Bk));
+    GAIN_CUDA(launch_gather_t(Fpad, B, Bk, dh, bF.dimen, nullptr, e->adjs_fmap.p, e->adjs_dhT.p, st));
+    GAIN_CUDA(launch_gather_t(ldM, B, Bk, vp, bI.dimen, nullptr, e->adjs_imap.p, e->adjs_vpT.p, st));
+    GAIN_TRY(zero_dig(2, (size_t)pB.slices * Fpad * Bk, Fpad, pB.chunks));
+    GAIN_TRY(zero_dig(3, (size_t)pB.slices * ldM * Bk, ldM, pB.chunks));
+    GAIN_TRY(slice(e, e->adjs_dhT.p, Bk, nullptr, Fpad, Bk, nullptr, nullptr, Bk, Fpad, e->adjs_dig[2].p, pB,
+                   e->adjs_st[2], false, nullptr, nullptr, st));
+    GAIN_TRY(slice(e, e->adjs_vpT.p, Bk, nullptr, ldM, Bk, nullptr, nullptr, Bk, ldM, e->adjs_dig[3].p, pB,
+                   e->adjs_st[3], false, nullptr, nullptr, st));
+    GAIN_TRY(e->adjs_dM.alloc((size_t)Fpad * ldM));
+    if (!t2.empty()) {
+        GAIN_TRY(gemm(2, 3, pB, Bk, Fpad, ldM, e->adjs_dM.p, ldM, Fpad, ldM, t2, e->adjs_tiles2, e->adjs_prods2,
+                      e->adjs_cnt.p + 1));
+        GAIN_CUDA(launch_refine_rows(e->adjs_flags.p, e->adjs_cnt.p + 1, cap, e->adjs_dhT.p, Bk, e->adjs_vpT.p, Bk,
+                                     Bk, e->adjs_dM.p, ldM, 2 * e->num_sms, st));
+    }
+    // ---- dL/dmu from the band
+    AdjArgs a;
+    memset(&a, 0, sizeof a);
+    a.dimF = bF.dimen;
+    a.dimI = bI.dimen;
+    a.nb = B;
+    a.vibF = bF.dvib.p;
+    a.vibI = bI.dvib.p;
+    a.KF = bF.dK.p;
+    a.KI = bI.dK.p;
+    a.tauF = bF.dtau.p;
+    a.tauI = bI.dtau.p;
+    a.levF = bF.dlev.p;
+    a.levI = bI.dlev.p;
+    a.jI = bI.J;
+    a.jF = bF.J;
+    a.jmax = e->jmax;
+    a.threej = e->d3j.p;
+    if (wt) {
+        a.wigner = wt->rot.p;
+        a.nlevelI = wt->nI;
+        a.nlevelF = wt->nF;
+        a.maxdeg = wt->maxdeg;
+    }
+    a.startF = e->startF;
+    a.endF = e->endF;
+    a.ncontrF = e->ncontrF;
+    a.dipN = e->dipN;
+    a.dmu = e->adj_dmu.p;
+    GAIN_CUDA(launch_adj_scatter_band(a, Fpad, e->adjs_fmap.p, e->adjs_imap.p, e->adjs_blo.p, e->adjs_bhi.p,
+                                      e->adjs_dM.p, ldM, st));
+    // the refinement lists must have held every flagged entry, and no bounded wait gave up
+    unsigned int cnt[2] = {0, 0};
+    int errw = 0;
+    GAIN_CUDA(cudaMemcpyAsync(cnt, e->adjs_cnt.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaMemcpyAsync(&errw, e->adjs_err.p, sizeof errw, cudaMemcpyDeviceToHost, st));
+    GAIN_CUDA(cudaStreamSynchronize(st));
+    if (errw) return set_error(GAIN_ERR_TIMEOUT, "a bounded device wait of the adjoint GEMM gave up (code %d)", errw);
+    if (cnt[0] > (unsigned)cap || cnt[1] > (unsigned)cap)
+        return set_error(GAIN_ERR_TOL_NOT_MET, "adjoint: more uncertified products than the refinement list holds");
+    if (tflops) *tflops += fl;
+    return GAIN_OK;
+}
+
 gain_status adjoint_run(gain_engine e, const gain_pair_job* job, const std::vector<std::pair<int, int>>& comps,
-                        double scale, const double* dL_dS, double* dL_dmu, bool f32, gain_stats* stats) {
+                        double scale, const double* dL_dS, double* dL_dmu, gain_adjoint_precision prec,
+                        gain_stats* stats) {
+    const bool f32 = prec == GAIN_ADJOINT_FP32;
+    const bool tc = prec == GAIN_ADJOINT_SPLIT;
+    double tflops = 0.0;
     const Basis& bI = e->bases[job->jindI];
     const Basis& bF = e->bases[job->jindF];
     Inflation& iI = e->infl[job->jindI];
@@ -2007,16 +2250,29 @@ gain_status adjoint_run(gain_engine e, const gain_pair_job* job, const std::vect
             amp = e->deg_amp.p + (size_t)slot * nS;
             ld_amp = Nu;
         } else {
+            // the pair's forward: the split path for the tensor-core adjoint (half line
+            // strengths recomputed on the tensor cores), else the FP64 plain path
             e->have_amp = false;
             e->amp_job.clear();
-            GAIN_TRY(run_plain(e, job, dI, dF, nullptr));
+            if (tc) GAIN_TRY(run_split(e, job, dI, dF, nullptr, nullptr));
+            else GAIN_TRY(run_plain(e, job, dI, dF, nullptr));
             e->amp_job = job_key(job, dI, dF);
+            e->have_amp = true;
             amp = e->amp.p;
             ld_amp = e->amp_ld;
         }
         GAIN_CUDA(cudaEventRecord(e->ev[2], st));
-        // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dL/dH
+        // dL/damp = dL/dS 2 amp;  dL/dH = G U (upper symmetry space);  dL/dh = T_F dH
         GAIN_CUDA(launch_adj_scale(B, Nu, e->adj_dLdS.p, amp, ld_amp, 2.0 * scale, G, f32, st));
+        if (tc) {
+            GAIN_TRY(adjoint_split_chain(e, job, dI, dF, (const double*)G, &tflops));
+            GAIN_CUDA(cudaEventRecord(e->ev[3], st));
+            GAIN_CUDA(cudaEventSynchronize(e->ev[3]));
+            float ms = 0.f;
+            GAIN_CUDA(cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]));
+            chain_ms += ms;
+            continue;
+        }
         GAIN_CUDA(launch_adj_gemm(B, NtF, Nu, G, Nu, EF.d.p, EF.nsize, e->d_upper.p, dH, NtF, f32, st));
         const int* repF_N = iF.dN[job->gammaF]->p;
         const double* repF = iF.drepres[job->gammaF]->p;
@@ -2094,14 +2350,15 @@ gain_status adjoint_run(gain_engine e, const gain_pair_job* job, const std::vect
         stats->device_ms = chain_ms;
         stats->rows = B;
         stats->cols = Nu;
-        stats->kernel_launches = 5 * (int)comps.size();
+        stats->kernel_launches = (tc ? 17 : 5) * (int)comps.size();
+        stats->tensor_flops = tflops;
     }
     return GAIN_OK;
 }
 
 gain_status adjoint_checks(gain_engine e, const gain_pair_job* job, const double* dL_dS, double* dL_dmu,
                            gain_adjoint_precision prec) {
-    if (prec != GAIN_ADJOINT_FP64 && prec != GAIN_ADJOINT_FP32)
+    if (prec != GAIN_ADJOINT_FP64 && prec != GAIN_ADJOINT_FP32 && prec != GAIN_ADJOINT_SPLIT)
         return set_error(GAIN_ERR_INVALID_ARG, "gain_adjoint_pair_prec: unknown precision %d", (int)prec);
     GAIN_TRY(check_engine(e));
     GAIN_TRY(validate_job(e, job));
@@ -2119,7 +2376,7 @@ gain_status gain_adjoint_pair_prec(gain_engine e, const gain_pair_job* job, cons
     if (e->infl[job->jindI].sdeg[job->gammaI] != 1 || e->infl[job->jindF].sdeg[job->gammaF] != 1)
         return set_error(GAIN_ERR_UNSUPPORTED,
                          "gain_adjoint_pair: degenerate symmetries go through gain_adjoint_pair_degenerate");
-    return adjoint_run(e, job, {{0, 0}}, 1.0, dL_dS, dL_dmu, prec == GAIN_ADJOINT_FP32, stats);
+    return adjoint_run(e, job, {{0, 0}}, 1.0, dL_dS, dL_dmu, prec, stats);
 }
 
 gain_status gain_adjoint_pair_degenerate(gain_engine e, const gain_pair_job* job, const gain_filters* f,
@@ -2140,7 +2397,7 @@ gain_status gain_adjoint_pair_degenerate(gain_engine e, const gain_pair_job* job
     if (comps.empty()) return set_error(GAIN_ERR_INVALID_ARG, "no component pair passes the degeneracy filter");
     // S = sum amp^2 / ndegI, times ndegI when reduced and both states are degenerate
     const double scale = (f->reduced && nI != 1 && nF != 1) ? 1.0 : 1.0 / nI;
-    return adjoint_run(e, job, comps, scale, dL_dS, dL_dmu, prec == GAIN_ADJOINT_FP32, stats);
+    return adjoint_run(e, job, comps, scale, dL_dS, dL_dmu, prec, stats);
 }
 
 namespace {
@@ -2842,6 +3099,8 @@ struct gain_plan_s {
     DevArray<int> err;
     char* rb = nullptr;                     // page-locked readback of counters, ull, err
     cudaStream_t side[kPlanStreams - 1] = {};
+    // fork / join order the capture's branches; ev[] are timing events recorded as graph nodes
+    // (cudaEventRecordExternal) around the stages
     cudaEvent_t fork = nullptr, join[kPlanStreams - 1] = {}, ev[6] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -3121,7 +3380,7 @@ gain_status plan_enqueue(gain_plan P) {
     GAIN_CUDA(cudaMemsetAsync(P->counters.p, 0, sizeof(unsigned int) * 2 * nj, st));
     GAIN_CUDA(cudaMemsetAsync(P->ull.p, 0, sizeof(unsigned long long) * 4 * nj, st));
     GAIN_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
-    GAIN_CUDA(cudaEventRecord(P->ev[0], st));
+    GAIN_CUDA(cudaEventRecordWithFlags(P->ev[0], st, cudaEventRecordExternal));
     // ---- stage 1: digits of the lower and the upper eigenvectors, every job
     GAIN_TRY(fork());
     for (int q = 0; q < nj; ++q) {
@@ -3157,9 +3416,9 @@ gain_status plan_enqueue(gain_plan P) {
     ga.groups = P->groups1.p;
     ga.tiles = P->tiles1.p;
     ga.ntiles = P->ntiles1;
-    GAIN_CUDA(cudaEventRecord(P->ev[1], st));
+    GAIN_CUDA(cudaEventRecordWithFlags(P->ev[1], st, cudaEventRecordExternal));
     GAIN_CUDA(split::launch_gemm_grouped(ga, P->units, P->s1max, P->c1max, st, P->pair));
-    GAIN_CUDA(cudaEventRecord(P->ev[2], st));
+    GAIN_CUDA(cudaEventRecordWithFlags(P->ev[2], st, cudaEventRecordExternal));
     // ---- stage 3: FP64 refinement of H, contraction (mixing expansions), digits of H
     GAIN_TRY(fork());
     for (int q = 0; q < nj; ++q) {
@@ -3201,9 +3460,9 @@ gain_status plan_enqueue(gain_plan P) {
     ga.groups = P->groups2.p;
     ga.tiles = P->tiles2.p;
     ga.ntiles = P->ntiles2;
-    GAIN_CUDA(cudaEventRecord(P->ev[3], st));
+    GAIN_CUDA(cudaEventRecordWithFlags(P->ev[3], st, cudaEventRecordExternal));
     GAIN_CUDA(split::launch_gemm_grouped(ga, P->units, P->s2max, P->c2max, st, P->pair));
-    GAIN_CUDA(cudaEventRecord(P->ev[4], st));
+    GAIN_CUDA(cudaEventRecordWithFlags(P->ev[4], st, cudaEventRecordExternal));
     // ---- stage 5: FP64 refinement of the amplitudes
     GAIN_TRY(fork());
     for (int q = 0; q < nj; ++q) {
@@ -3236,7 +3495,7 @@ gain_status plan_enqueue(gain_plan P) {
         GAIN_CUDA(split::launch_refine_amp(ra, std::min(4 * e->num_sms, std::max(1, J.cap2 / 8)), sq));
     }
     GAIN_TRY(join());
-    GAIN_CUDA(cudaEventRecord(P->ev[5], st));
+    GAIN_CUDA(cudaEventRecordWithFlags(P->ev[5], st, cudaEventRecordExternal));
     GAIN_CUDA(cudaMemcpyAsync(P->rb, P->counters.p, sizeof(unsigned int) * 2 * nj, cudaMemcpyDeviceToHost, st));
     GAIN_CUDA(cudaMemcpyAsync(P->rb + 8 * (size_t)nj, P->ull.p, sizeof(unsigned long long) * 4 * nj,
                               cudaMemcpyDeviceToHost, st));

@@ -69,6 +69,17 @@ cudaError_t launch_adj_gemm(int M, int N, int K, const void* A, long lda, const 
 int adj_tile();
 // dL/dmu over the listed (F, I) tiles: tiles = ntiles pairs (first F, first I)
 cudaError_t launch_adj_dm(const AdjArgs& a, const int* tiles, int ntiles, bool fp32, cudaStream_t st);
+// out[p][b] = src[(rows ? rows[b] : b) * ld + map[p]] (0 where map[p] < 0 or b >= nb), the
+// [np_pad][nb_pad] transpose-gather that lays out a digit GEMM operand
+cudaError_t launch_gather_t(int np_pad, int nb, int nb_pad, const double* src, long ld, const int* rows,
+                            const int* map, double* out, cudaStream_t st);
+// FP64 recomputation of flagged C[r][c] = sum_k A[r][k] B[c][k]
+cudaError_t launch_refine_rows(const int2* flags, const unsigned int* nflags, int max_flags, const double* A,
+                               long lda, const double* B, long ldb, int K, double* C, long ldc, int max_blocks,
+                               cudaStream_t st);
+// dL/dmu (double) from the band entries dM[r][c], c in [band_lo[r], band_hi[r]) of nrows F positions
+cudaError_t launch_adj_scatter_band(const AdjArgs& a, int nrows, const int* fmap, const int* imap, const int* band_lo,
+                                    const int* band_hi, const double* dM, long ld, cudaStream_t st);
 
 cudaError_t launch_hls_rotsym(int dimenF, int dimenI, int nlevelI, int nlevelF, int maxdeg, const int* kI,
                               const int* kF, const int* ktauI, const int* ktauF, const int* icorrI, const int* icorrF,

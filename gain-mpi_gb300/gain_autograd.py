@@ -55,7 +55,8 @@ def line_strengths(mu: torch.Tensor, eng, pair: Sequence[int], lower: Sequence[i
                    block=None, path: int = gainls.PATH_PLAIN_FP64, precision: str = "f64") -> torch.Tensor:
     """S[l, u] = amp^2 of one block pair as a differentiable function of the dipole piece mu
     (float64, [3][N][endF - startF], the gain_upload_dipole layout; block = (startF, endF),
-    default the whole range).  precision ("f64" or "f32") is the arithmetic of the adjoint."""
+    default the whole range).  precision ("f64", "f32" or "split": tensor-core digit GEMMs) is
+    the arithmetic of the adjoint."""
     if block is None:
         block = (0, int(mu.shape[1]))
     return PairLineStrengths.apply(mu, eng, tuple(pair), tuple(lower), tuple(upper), tuple(block), path, precision)

@@ -490,8 +490,9 @@ class Engine:
                 precision="f64", filters=None):
         """dL/dmu (the dipole piece's layout [3][N][ncontrF], accumulated into dL_dmu if given)
         of a loss with gradient dL_dS [nlower, nupper] over the pair's line strengths;
-        precision "f64" or "f32" is the arithmetic of the adjoint chain."""
-        prec = {"f64": 0, "f32": 1}[precision]
+        precision "f64", "f32" (SIMT chains) or "split" (both products as tensor-core digit
+        GEMMs) is the arithmetic of the adjoint chain."""
+        prec = {"f64": 0, "f32": 1, "split": 2}[precision]
         lo, up = _i32(lower_levels), _i32(upper_levels)
         g = _f64(dL_dS)
         assert g.size == len(lo) * len(up)

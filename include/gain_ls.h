@@ -244,9 +244,19 @@ gain_status gain_adjoint_pair(gain_engine e, const gain_pair_job* job, const dou
 /* Arithmetic of the adjoint chain. */
 typedef enum {
     GAIN_ADJOINT_FP64 = 0,   /* every product and sum in FP64 (gain_adjoint_pair) */
-    GAIN_ADJOINT_FP32 = 1    /* G, dL/dH, dL/dh, the lower vectors and the dL/dmu sums in FP32; the
+    GAIN_ADJOINT_FP32 = 1,   /* G, dL/dH, dL/dh, the lower vectors and the dL/dmu sums in FP32; the
                                 FP64 amplitudes, eigenvectors and expansion tables are rounded to
                                 FP32 as they are read; dL_dmu is still accumulated in double */
+    GAIN_ADJOINT_SPLIT = 2   /* both products on the tensor cores as digit GEMMs (the split
+                                path's Ozaki digits, 48 bits, exact accumulation, FP64
+                                recombination; entries whose exactness certificate fails are
+                                recomputed in FP64): dL/dH = G U over the upper states, and the
+                                batched outer product dL/dM = sum_b dh_b v_b^T over the band of
+                                the rotational-dipole matrix (|K_I - K_F| <= 1, or all K in the
+                                rotational-symmetry form), then the FP64 scatter into dL/dmu.
+                                Without the job's amplitudes from the last run it runs the split
+                                forward (half line strengths recomputed, nothing per transition
+                                kept from an earlier forward). */
 } gain_adjoint_precision;
 
 /* gain_adjoint_pair in the given precision. */
