@@ -55,6 +55,8 @@ def parse():
                          "against central differences (one JSON line)")
     ap.add_argument("--adj-nv", type=int, default=1000, help="vibrational basis size of --adjoint")
     ap.add_argument("--adj-fd", type=int, default=200, help="entries checked by central differences")
+    ap.add_argument("--adj-fd-direct", type=int, default=4,
+                    help="of those, entries also checked with two plain FP64 forwards each")
     ap.add_argument("--rule", choices=["c4", "c4m"], default="c4",
                     help="symmetrisation of the workload: c4 (selection, the headline) or c4m (functions "
                          "that combine two primitives, as TROVE's symmetry-adapted functions do)")
@@ -66,6 +68,8 @@ def parse():
     ap.add_argument("--degenerate", action="store_true",
                     help="a doubly degenerate E -> E pair of the config-2 sizes (rule c3e), every component pair")
     ap.add_argument("--batch-jmax", type=int, default=30, help="largest J of --batch")
+    ap.add_argument("--batch-stream", action="store_true",
+                    help="many block pairs at the full size (N_v from --batch-nv, default 2000 here), in waves")
     return ap.parse_args()
 
 
@@ -312,6 +316,13 @@ def s_rel_err(S: np.ndarray, Sref: np.ndarray, floor: float = 1e-10):
     return float(r.max()), float(np.quantile(r, 0.99)), int(m.sum())
 
 
+def _peak(key: str, default: float = 1900.0) -> float:
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))[key])
+    except Exception:
+        return default
+
+
 def precision_sweep(args):
     """Digit configurations of the amplitude GEMM (8-bit digits x 3..7 slices, 7-bit x 5..7) on
     the workload: time, refinement counts, and the relative error of S = amp^2 for lines with
@@ -516,25 +527,67 @@ def adjoint_check(args):
         eng.adjoint(jI, gI, jF, gF, lo, up, g, grad_split)
     times["gradient_split_forward_s"] = time.perf_counter() - t1
     split_vs_fp64 = float(np.max(np.abs(grad_split - grad.reshape(-1))) / np.abs(grad).max())
+    # the tensor-core adjoint (GAIN_ADJOINT_SPLIT): both products as digit GEMMs, each pair's
+    # own split forward (nothing kept from an earlier forward)
+    eng.upload_dipole(mu0.reshape(-1), nv, 0, nv, nv)
+    grad_tc = np.zeros(mu0.size)
+    tc_flops = 0.0
+    chain_ms["split_tensor_core"] = 0.0
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for (jI, gI, jF, gF, lo, up), g in zip(pairs, dLdS):
+        eng.adjoint(jI, gI, jF, gF, lo, up, g, grad_tc, precision="split")
+        chain_ms["split_tensor_core"] += eng.last_adjoint_stats.device_ms
+        tc_flops += eng.last_adjoint_stats.tensor_flops
+    times["adjoint_tensor_core_s"] = time.perf_counter() - t1
+    tc_vs_fp64 = float(np.max(np.abs(grad_tc - grad.reshape(-1))) / np.abs(grad).max())
 
-    # central differences
+    # central differences (h = 1e-6) of L on args.adj_fd random entries with a non-zero gradient.
+    # amp is linear in mu, so the perturbed forwards are amp(mu0 +- h e_k) = amp0 +- h amp(e_k),
+    # amp(e_k) the forward of the one-hot dipole e_k (split path, certified); the difference
+    # L(mu0 + h e_k) - L(mu0 - h e_k) is summed line by line as (d+ - d-)(d+ + d-), with
+    # d+ - d- = 2 [log1p(h r) - log1p(-h r)], r = amp(e_k) / amp0, so that no cancellation
+    # between the two losses limits it.  A few entries are also checked with two plain FP64
+    # forwards at mu0 +- h e_k and the difference of the two losses.
     h = 1e-6
     rng = np.random.default_rng(78)
     gflat = grad.reshape(-1)
+    gflat_tc = grad_tc.reshape(-1)
     gmax = float(np.abs(gflat).max())
     cand = np.flatnonzero(np.abs(gflat) > 0)
     picks = rng.choice(cand, size=min(args.adj_fd, cand.size), replace=False)
-    rel, absn, jrel, rel32 = [], [], [], []
+    rel, absn, jrel, rel32, reltc = [], [], [], [], []
+    lt_all = logS_t
+
+    def fd_linear(k):
+        e = np.zeros(mu0.size)
+        e[k] = 1.0
+        ak = forward(e.reshape(mu0.shape), gainls.PATH_SPLIT, keep=True)
+        num = torch.zeros((), dtype=torch.float64, device="cuda")
+        for a0, a1, m, lt in zip(amp0, ak, masks, lt_all):
+            r = torch.where(m, a1 / a0, torch.zeros_like(a0))
+            dm = torch.where(m, 2.0 * torch.log(torch.abs(a0)) - lt, torch.zeros_like(a0))
+            diff = 2.0 * (torch.log1p(h * r) - torch.log1p(-h * r))   # d+ - d-
+            num += torch.sum(diff * (2.0 * dm + 2.0 * (torch.log1p(h * r) + torch.log1p(-h * r))))   # d+ + d-
+        return float(num) / (2 * h)
+
     t1 = time.perf_counter()
     for k in picks:
+        fd = fd_linear(k)
+        rel.append(abs(fd - gflat[k]) / abs(gflat[k]))
+        absn.append(abs(fd - gflat[k]) / gmax)
+        rel32.append(abs(fd - grad32[k]) / abs(gflat[k]))
+        reltc.append(abs(fd - gflat_tc[k]) / abs(gflat[k]))
+    times["fd_s"] = time.perf_counter() - t1
+    direct = []
+    t1 = time.perf_counter()
+    for k in picks[:args.adj_fd_direct]:
         mp, mm = mu0.copy(), mu0.copy()
         mp.reshape(-1)[k] += h
         mm.reshape(-1)[k] -= h
         fd = (loss(mp) - loss(mm)) / (2 * h)
-        rel.append(abs(fd - gflat[k]) / abs(gflat[k]))
-        absn.append(abs(fd - gflat[k]) / gmax)
-        rel32.append(abs(fd - grad32[k]) / abs(gflat[k]))
-    times["fd_s"] = time.perf_counter() - t1
+        direct.append(abs(fd - gflat[k]) / abs(gflat[k]))
+    times["fd_direct_s"] = time.perf_counter() - t1
     t1 = time.perf_counter()
     for k in picks:
         e = np.zeros(mu0.size)
@@ -557,6 +610,18 @@ def adjoint_check(args):
            "fd_max_err_over_max_grad": float(max(absn)), "fd_direction_rel_err": [float(x) for x in dirs],
            "exact_partials_max_rel_err": float(jrel.max()), "exact_partials_median_rel_err": float(np.median(jrel)),
            "exact_direction_rel_err": [float(x) for x in jdirs],
+           "fd_method": "central differences of L at h, perturbed forwards formed as amp0 +- h amp(e_k) "
+                        "(amp linear in mu), loss difference summed line by line",
+           "fd_direct_entries": len(direct), "fd_direct_max_rel_err": float(max(direct)) if direct else None,
+           "fd_direct_median_rel_err": float(np.median(direct)) if direct else None,
+           "tensor_core_adjoint": {"max_err_over_max_grad_vs_fp64": tc_vs_fp64,
+                                   "fd_max_rel_err": float(max(reltc)), "fd_median_rel_err": float(np.median(reltc)),
+                                   "fd_p99_rel_err": float(np.quantile(reltc, 0.99)),
+                                   "chain_device_ms": chain_ms["split_tensor_core"],
+                                   "tensor_flops": tc_flops,
+                                   "tensor_tflops": tc_flops / (chain_ms["split_tensor_core"] * 1e-3) / 1e12,
+                                   "peak_bf16_tflops": _peak("bf16_tflops"),
+                                   "digits": "48 bits (8-bit digits x 6, exact FP32 accumulation)"},
            "split_forward_gradient_max_err_over_max_grad": split_vs_fp64,
            "fp32_gradient_max_err_over_max_grad": fp32_vs_fp64,
            "fp32_fd_median_rel_err": float(np.median(rel32)), "fp32_fd_p99_rel_err": float(np.quantile(rel32, 0.99)),
@@ -753,6 +818,107 @@ def batch_plan(args):
     eng.close()
 
 
+def batch_stream(args):
+    """Many block pairs at the full batching size: N_v = 2000, J = 0..30, four symmetries,
+    every allowed (J'', Gamma'') -> (J', Gamma') pair (|dJ| <= 1, Gamma' = Gamma'' ^ 1,
+    J'' + J' >= 1, not both J_max), lower states below 4000 cm^-1 against every upper state.
+    The upper eigenvectors alone (318 GB in FP64) exceed one GPU, so the pairs run in waves,
+    one wave per upper block: its eigenvectors and the lower states of its (up to three) lower
+    blocks are made on the device (a fast orthonormal generator: Kronecker products of QR
+    factors, rows and columns permuted), uploaded into the engine (device to device), the
+    wave's jobs run as one grouped plan (two grouped tensor-core launches in a CUDA graph), and
+    the blocks are released.  Each wave's plan is replayed once after its first (capturing)
+    run; the device time of that replay is summed.  A sample of lower states of the largest
+    job of every tenth wave is checked against the plain FP64 path.  One JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    import gainls
+    import synth
+    nv, jmax = args.batch_nv, args.batch_jmax
+    t0 = time.perf_counter()
+    bases = [synth.make_basis(J, nv) for J in range(jmax + 1)]
+    infl = [synth.inflation_of(b, "c4", 4) for b in bases]
+    eng = gainls.Engine(jmax, 4, 1)
+    for jind, (b, inf) in enumerate(zip(bases, infl)):
+        eng.upload_basis(jind, b.J, b.K, b.tau, b.vib, b.kblock, b.kstart)
+        eng.upload_inflation(jind, inf.icontr, inf.ijterms, b.dimen, inf.maxcoeff, inf.matsize, inf.N, inf.repres,
+                             inf.Ntot, inf.sdeg)
+    eng.upload_dipole(synth.make_dipole(nv).reshape(-1), nv, 0, nv, nv)
+    dims = {(J, c): int(infl[J].Ntot[c]) for J in range(jmax + 1) for c in range(4)}
+    nlow = {k: int(np.searchsorted(synth.make_energies(n, k[0], k[1]), 4000.0)) for k, n in dims.items()}
+    waves = []
+    for JF in range(jmax + 1):
+        for cF in range(4):
+            jobs = []
+            for JI in (JF - 1, JF, JF + 1):
+                cI = cF ^ 1
+                if JI < 0 or JI > jmax or JI + JF < 1 or (JI == jmax and JF == jmax):
+                    continue
+                if nlow[(JI, cI)] == 0 or dims[(JF, cF)] == 0:
+                    continue
+                jobs.append((JI, cI, JF, cF, list(range(nlow[(JI, cI)])), list(range(dims[(JF, cF)]))))
+            if jobs:
+                waves.append(((JF, cF), jobs))
+    setup_s = time.perf_counter() - t0
+    total = sum(len(j[4]) * len(j[5]) for _, jobs in waves for j in jobs)
+    dev_ms, wall_ms, gen_s, worst, nchk = 0.0, 0.0, 0.0, 0.0, 0
+    biggest = None
+    t_all = time.perf_counter()
+    for w, ((JF, cF), jobs) in enumerate(waves):
+        g0 = time.perf_counter()
+        need = {(JF, cF): dims[(JF, cF)]}
+        for JI, cI, *_ in jobs:
+            need.setdefault((JI, cI), nlow[(JI, cI)])
+        for (J, c), rows in need.items():
+            U = synth.make_eigvecs_kron(dims[(J, c)], J, c, "cuda")
+            rows_t = U[:rows].contiguous() if (J, c) != (JF, cF) else U
+            eng.upload_eigvecs_device(J, c, rows_t.data_ptr(), int(rows_t.shape[0]), dims[(J, c)])
+            del U, rows_t
+        torch.cuda.synchronize()
+        gen_s += time.perf_counter() - g0
+        w0 = time.perf_counter()
+        plan = gainls.Plan(eng, [(a, b, c, d, lo, up) for a, b, c, d, lo, up in jobs])
+        plan.run()
+        ps, js, st = plan.run()
+        wall_ms += (time.perf_counter() - w0) * 1e3
+        dev_ms += ps["device_ms"]
+        trans = sum(len(j[4]) * len(j[5]) for j in jobs)
+        if biggest is None or trans > biggest["transitions"]:
+            biggest = {"upper_block": [JF, cF], "jobs": len(jobs), "transitions": trans, "device_ms": ps["device_ms"],
+                       "gemm1_ms": ps["gemm1_ms"], "gemm2_ms": ps["gemm2_ms"], "graph_nodes": ps["graph_nodes"],
+                       "tiles": [ps["gemm1_tiles"], ps["gemm2_tiles"]],
+                       "tensor_tflops_in_gemms": ps["tensor_flops"] / ((ps["gemm1_ms"] + ps["gemm2_ms"]) * 1e-3) / 1e12}
+        if w % 10 == 0:   # accuracy sample: two lower states of the wave's largest job
+            q = int(np.argmax([len(j[4]) * len(j[5]) for j in jobs]))
+            JI, cI, _, _, lo, up = jobs[q]
+            a = plan.amp(q)
+            rows = [0, len(lo) // 2]
+            eng.run_pair(JI, cI, JF, cF, [lo[r] for r in rows], up, gainls.PATH_PLAIN_FP64)
+            ref = eng.fetch_amp()
+            S, Sr = a[rows] ** 2, ref ** 2
+            m = Sr > 1e-10 * Sr.max()
+            worst = max(worst, float(np.max(np.abs(S[m] - Sr[m]) / Sr[m])))
+            nchk += int(m.sum())
+        plan.close()
+        for (J, c) in need:
+            eng.release_eigvecs(J, c)
+    total_wall = time.perf_counter() - t_all
+    out = {"mode": "batch_stream",
+           "workload": f"N_v={nv}, J=0..{jmax}, 4 symmetries, all allowed block pairs, lower states E < 4000 cm^-1 "
+                       "x all upper states; one grouped plan per upper block (wave)",
+           "pairs": sum(len(j) for _, j in waves), "waves": len(waves), "transitions": total,
+           "largest_block": max(dims.values()), "setup_s": setup_s,
+           "device_ms": dev_ms, "transitions_per_s_device": total / (dev_ms * 1e-3),
+           "plan_wall_ms": wall_ms, "generation_and_upload_s": gen_s, "total_wall_s": total_wall,
+           "largest_wave": biggest,
+           "accuracy_sample": {"max_rel_err_S_vs_plain": worst, "lines_checked": nchk,
+                               "sample": "2 lower states of the largest job of every 10th wave, all upper states",
+                               "domain": "S > 1e-10 S_max"},
+           "eigenvectors": "Kronecker products of seeded QR factors, rows/columns permuted (device)"}
+    print(json.dumps(out), flush=True)
+    eng.close()
+
+
 def reference_gpu_sample(inp, n_lower: int) -> dict:
     """The reference's own GPU kernels (GPU/dipole_GPU.cu, compiled unmodified into
     oracle/_ref/dipole_GPU.cubin) in GpuManager's call pattern (oracle/ref_harness.cu): per
@@ -823,6 +989,10 @@ def main():
         return precision_sweep(args)
     if args.adjoint:
         return adjoint_check(args)
+    if args.batch_stream:
+        if args.batch_nv == 200:
+            args.batch_nv = 2000
+        return batch_stream(args)
     if args.batch:
         return batch_plan(args)
     if args.degenerate:

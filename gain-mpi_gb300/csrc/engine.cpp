@@ -1890,9 +1890,23 @@ gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels,
     slot->nlevels = nlevels;
     slot->nsize = nsize;
     GAIN_TRY(slot->d.alloc((size_t)nlevels * nsize));
-    GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyHostToDevice,
-                              e->st));
+    // host or device memory (unified addressing tells them apart)
+    GAIN_CUDA(cudaMemcpyAsync(slot->d.p, vecs, sizeof(double) * (size_t)nlevels * nsize, cudaMemcpyDefault, e->st));
     GAIN_CUDA(cudaStreamSynchronize(e->st));
+    return GAIN_OK;
+}
+
+gain_status gain_release_eigvecs(gain_engine e, int jind, int gamma) {
+    clear_error();
+    GAIN_TRY(check_engine(e));
+    auto it = e->eig.find({jind, gamma});
+    if (it == e->eig.end()) return GAIN_OK;
+    GAIN_TRY(gain_lines_wait(e));
+    GAIN_CUDA(cudaStreamSynchronize(e->st));
+    GAIN_CUDA(cudaStreamSynchronize(e->st2));
+    if (it->second->ready) GAIN_CUDA(cudaEventSynchronize(it->second->ready));
+    clear_amp_jobs(e);
+    e->eig.erase(it);
     return GAIN_OK;
 }
 

@@ -224,6 +224,8 @@ def _declare(L):
     L.gain_run_pair_degenerate.argtypes = [_vp, ctypes.POINTER(PairJob), ctypes.POINTER(Filters), ctypes.c_int,
                                            ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_upload_eigvecs_async.argtypes = [_vp, I, I, I, I, _dp]
+    L.gain_release_eigvecs.argtypes = [_vp, I, I]
+    L.gain_release_eigvecs.restype = S
     L.gain_run_pair.argtypes = [_vp, ctypes.POINTER(PairJob), I, ctypes.POINTER(SplitOpts), ctypes.POINTER(Stats)]
     L.gain_pair_amp_device.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _ip]
     L.gain_fetch_amp.argtypes = [_vp, _dp]
@@ -451,6 +453,14 @@ class Engine:
         rot = _f64(rot)
         assert rot.size == 3 * nlevelsI * nlevelsF * maxdeg * maxdeg
         check(lib().gain_upload_wigner(self.h, jindI, jindF, nlevelsI, nlevelsF, maxdeg, _p(rot, _dp)))
+
+    def upload_eigvecs_device(self, jind, gamma, ptr: int, nlevels: int, nsize: int):
+        """gain_upload_eigvecs from device memory (ptr: a device address of nlevels x nsize
+        doubles, e.g. a torch tensor's data_ptr())."""
+        check(lib().gain_upload_eigvecs(self.h, jind, gamma, nlevels, nsize, ctypes.cast(ptr, _dp)))
+
+    def release_eigvecs(self, jind, gamma):
+        check(lib().gain_release_eigvecs(self.h, jind, gamma))
 
     def upload_eigvecs_async(self, jind, gamma, vecs):
         """Queue the copy of page-locked vecs (C-contiguous float64, kept unchanged until the

@@ -360,6 +360,36 @@ def make_eigvecs(n: int, J: int, gamma: int, device: str | None = None,
     return np.ascontiguousarray(q.T.cpu().numpy())
 
 
+def make_eigvecs_kron(n: int, J: int, gamma: int, device: str = "cuda"):
+    """A dense orthonormal n x n matrix made quickly on the device (for block sizes whose QR
+    factorisation would take minutes): with n1 = floor(sqrt(n)), n2 = n // n1 and r = n - n1 n2,
+    U = P_r blockdiag(Q1 (x) Q2, Q3) P_c, where Q1, Q2, Q3 are the Q factors of seeded N(0,1)
+    matrices of sizes n1, n2, r (the same seeds as make_eigvecs) and P_r, P_c seeded
+    permutations of the rows and columns.  A Kronecker product of orthogonal matrices is
+    orthogonal, so U is orthonormal to rounding.  Returns a torch tensor [n, n] (rows = states)."""
+    import torch
+    rng = np.random.default_rng(vec_seed(J, gamma))
+    n1 = max(1, int(np.floor(np.sqrt(n))))
+    n2 = n // n1
+    r = n - n1 * n2
+
+    def q(m):
+        g = torch.from_numpy(rng.standard_normal((m, m))).to(device)
+        qq, rr = torch.linalg.qr(g)
+        sgn = torch.sign(torch.diagonal(rr))
+        sgn[sgn == 0] = 1.0
+        return qq * sgn[None, :]
+
+    Q1, Q2 = q(n1), q(n2)
+    U = torch.zeros((n, n), dtype=torch.float64, device=device)
+    U[: n1 * n2, : n1 * n2] = torch.kron(Q1, Q2)
+    if r > 0:
+        U[n1 * n2:, n1 * n2:] = q(r)
+    pr = torch.from_numpy(rng.permutation(n)).to(device)
+    pc = torch.from_numpy(rng.permutation(n)).to(device)
+    return U[pr][:, pc].contiguous()
+
+
 @dataclasses.dataclass
 class Block:
     J: int

@@ -166,9 +166,15 @@ gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI
 
 /* Eigenvectors of one (J, Gamma) block kept resident (the reference re-uploads one vector
  * per transition, GpuManager::UpdateEigenVector, :537-545): vecs[level*nsize + c].  Host
- * array (pinned memory transfers fastest), copied synchronously. */
+ * array (pinned memory transfers fastest) or device array, copied synchronously. */
 gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize,
                                 const double* vecs);
+
+/* Free the device copy of one (J, Gamma) block's eigenvectors (waits for the engine's queued
+ * work).  For block sets larger than the device: upload the blocks a set of pairs needs, run
+ * them, release, go on.  Plans that read the block re-capture on their next run (and fail
+ * there with GAIN_ERR_NOT_READY until it is uploaded again).  No counterpart in the reference. */
+gain_status gain_release_eigvecs(gain_engine e, int jind, int gamma);
 
 /* As gain_upload_eigvecs, but from page-locked host memory the copy is only queued (on the
  * engine's copy stream) and the call returns at once; the next gain_run_pair orders every

@@ -60,7 +60,7 @@ def test_plan_equals_single_pair_runs(built_lib, rule):
 def test_plan_single_cta_tiles_equal_pairs(built_lib, monkeypatch):
     """128 x 128 tiles (GAINLS_GEMM_PAIR=0) and 256 x 128 CTA-pair tiles give the same bits."""
     import gainls
-    p, eng = _problem("c4", nv=60, jvals=(3, 4, 5))
+    p, eng = _problem("c4", nv=120, jvals=(4, 5, 6))
     jobs = _jobs(p)
     assert max(len(j[4]) for j in jobs) > 128   # some job has CTA-pair tiles
     a = gainls.Plan(eng, jobs)
