@@ -240,7 +240,9 @@ def line_text_bench(eng, inp, steps: int) -> dict:
     m = float(np.median(ms))
     return {"lines": int(nl), "bytes": len(text), "ms": m, "lines_per_s": nl / (m * 1e-3),
             "GB_per_s": len(text) / (m * 1e-3) / 1e9,
-            "includes": "S/A/I, text on the device, copy to pinned host overlapped part by part"}
+            "intensity_evaluated_on_host": eng.intensity_host(),
+            "includes": "S/A/I, text on the device, copy to pinned host overlapped part by part; the "
+                        "intensity of lines whose printed digits depend on exp's last bit from the host"}
 
 
 def cpu_text_baseline(eng, inp, rows: int) -> dict:
