@@ -638,12 +638,49 @@ float fix_const(int nprods) {
 // (tens of MB) stay in L2 and are read from HBM once, and consecutive passes reuse the same
 // A plane (product-major order re-streamed every plane of every chunk from HBM).  The int64
 // recombination does not depend on the order.
-std::vector<split::Prod> make_prods(const SplitParams& p) {
+std::vector<split::Prod> make_prods(const SplitParams& p, int fuse = 1) {
     std::vector<split::Prod> v;
+    auto add = [&](int i, int j, int c, bool open, bool close) {
+        split::Prod q;
+        memset(&q, 0, sizeof q);
+        q.ia = i;
+        q.ib = j;
+        q.t = i + j;
+        q.chunk = c;
+        q.open = open ? 1 : 0;
+        q.close = close ? 1 : 0;
+        v.push_back(q);
+    };
+    if (fuse <= 1) {
+        for (int c = 0; c < p.chunks; ++c)
+            for (int i = 0; i < p.slices; ++i)
+                for (int j = 0; i + j < p.slices; ++j) add(i, j, c, true, true);
+        return v;
+    }
+    // fused: per chunk and weight t, the t + 1 products (i, t - i) in groups of at most `fuse`
+    // that share one accumulator
     for (int c = 0; c < p.chunks; ++c)
-        for (int i = 0; i < p.slices; ++i)
-            for (int j = 0; i + j < p.slices; ++j) v.push_back({i, j, i + j, c});
+        for (int t = 0; t < p.slices; ++t)
+            for (int i = 0; i <= t; ++i) {
+                const int k = i % fuse;
+                add(i, t - i, c, k == 0, k == fuse - 1 || i == t);
+            }
     return v;
+}
+
+// Products fused per accumulator in the first GEMM: only where each product is short (fewer
+// than 16 k-blocks per tile, so that draining the accumulator after every product would pace
+// the tensor pipe); as many as keep the expected sum of their digit norms' products, K_chunk
+// 4^beta / 12 each for balanced digits, within 2^23 (the factor-two margin of choose_params).
+// The exactness certificate checks it per output.  GAINLS_FUSE1=0 disables.
+int gemm1_fuse(const PairLayout& L, const SplitParams& p1) {
+    if (const char* f = getenv("GAINLS_FUSE1"))
+        if (f[0] == '0') return 1;
+    const int kchunk = L.W / std::max(1, p1.chunks);
+    if (kchunk / split::BK >= 16) return 1;
+    const double per = (double)kchunk * std::ldexp(1.0, 2 * p1.beta) / 12.0;
+    const int f = (int)std::floor(8388608.0 / std::max(per, 1.0));
+    return std::max(1, std::min(p1.slices, f));
 }
 
 gain_status launch_layout_band(gain_engine e, const gain_pair_job* j);
@@ -1163,7 +1200,8 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (lower digits)");
 
     // ---- GEMM 1: H = V M (one pass per dipole piece)
-    const std::vector<split::Prod> pr1 = make_prods(p1x);
+    const int fuse1 = gemm1_fuse(L, p1x);
+    const std::vector<split::Prod> pr1 = make_prods(p1x, fuse1);
     GAIN_TRY(e->prods1.upload(pr1));
     GAIN_TRY(e->H.alloc((size_t)Bpad * L.fpad));
     GAIN_TRY(e->rowerr.alloc(Bpad));
@@ -1244,6 +1282,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
         g1.rows_valid = B;
         g1.cols_valid = L.fpad;
         g1.err = e->err.p;
+        g1.fuse = fuse1;
         if (piece == 0) GAIN_CUDA(cudaEventRecord(e->ev[2], st));
         if (!t1.empty()) {
             GAIN_CUDA(split::launch_gemm(tmV, pair ? L.tmBandPair : L.tmBand, g1, e->num_sms, st, pair));
@@ -3075,7 +3114,7 @@ struct PlanJob {
     StatsDev Vst, Hst, Ust;
     DevArray<int2> flags1, flags2;
     DevArray<split::Prod> prods1, prods2;
-    int nprods1 = 0, nprods2 = 0;
+    int nprods1 = 0, nprods2 = 0, fuse1 = 1;
     CUtensorMap tmV{}, tmH{}, tmU{};
     const void* vI = nullptr;     // eigenvector and band-digit buffers the graph captured
     const void* vF = nullptr;
@@ -3215,7 +3254,8 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
         GAIN_TRY(J.iota.upload(io));
         GAIN_TRY(J.Hsym.alloc((size_t)J.Bpad * J.K2));
     }
-    const std::vector<split::Prod> pr1 = make_prods(J.p1), pr2 = make_prods(J.p2);
+    J.fuse1 = gemm1_fuse(L, J.p1);
+    const std::vector<split::Prod> pr1 = make_prods(J.p1, J.fuse1), pr2 = make_prods(J.p2);
     GAIN_TRY(J.prods1.upload(pr1));
     GAIN_TRY(J.prods2.upload(pr2));
     J.nprods1 = (int)pr1.size();
@@ -3305,6 +3345,7 @@ gain_status plan_build_groups(gain_plan P) {
         a1.max_flags = J.cap1;
         a1.rows_valid = J.B;
         a1.cols_valid = L.fpad;
+        a1.fuse = J.fuse1;
         g2[q].tmA = J.tmH;
         g2[q].tmB = J.tmU;
         split::GemmArgs& a2 = g2[q].args;

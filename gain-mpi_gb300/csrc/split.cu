@@ -404,11 +404,13 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
                     if (hi <= lo) continue;
                     const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
-                    if (!mbar_wait(smem_u32(&accempty[b]), aphase ^ 1, abort_flag, a.err, 2)) {
-                        ok = false;
-                        break;
+                    if (pr.open) {   // a new accumulator: wait until the epilogue drained it
+                        if (!mbar_wait(smem_u32(&accempty[b]), aphase ^ 1, abort_flag, a.err, 2)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
                     }
-                    tc_fence_after();
                     const uint32_t d = tmem + b * BN;
                     for (int kb = lo; kb < hi; kb += KS) {
                         const int nk = hi - kb < KS ? hi - kb : KS;
@@ -426,7 +428,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             if (h < nk) {
 #pragma unroll
                                 for (int kk = 0; kk < BK / 16; ++kk) {
-                                    const uint32_t acc = (kb > lo || h > 0 || kk > 0) ? 1u : 0u;
+                                    const uint32_t acc = (!pr.open || kb > lo || h > 0 || kk > 0) ? 1u : 0u;
                                     const uint64_t a2 = ad + h * (BOX_A >> 4) + 2 * kk;
                                     const uint64_t b2 = bd + h * (BOXB >> 4) + 2 * kk;
                                     if (PAIR) mma_bf16_pair(d, a2, b2, kIdescPair, acc);
@@ -440,9 +442,11 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         if (++stage == NST) { stage = 0; phase ^= 1; }
                     }
                     if (!ok) break;
-                    if (PAIR) mma_commit_pair(smem_u32(&accfull[b]), (uint16_t)3);
-                    else mma_commit(smem_u32(&accfull[b]));
-                    ++acc_cnt;
+                    if (pr.close) {   // the group is complete: hand the accumulator over
+                        if (PAIR) mma_commit_pair(smem_u32(&accfull[b]), (uint16_t)3);
+                        else mma_commit(smem_u32(&accfull[b]));
+                        ++acc_cnt;
+                    }
                 }
             }
             if (any) {
@@ -474,7 +478,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 const Prod pr = g.prods[p];
                 int lo, hi;
                 chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
-                if (hi <= lo) continue;
+                if (hi <= lo || !pr.close) continue;   // drained once per (fused) group
                 const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
                 if (!mbar_wait(smem_u32(&accfull[b]), aphase, abort_flag, a.err, 5)) {
                     ok = false;
@@ -517,6 +521,9 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             // column per lane and broadcast with shuffles (no shared memory, no cross-warp sync).
             const int r = tl.m0 + (int)rank * BM + row_in_tile;
             const bool rvalid = r < g.rows_valid;
+            // products summed in one accumulator: every partial sum of up to `fuse` exact
+            // integer dot products stays below 2^24 when fuse max_c ||d_c(x)|| ||d_c(y)|| does
+            const float fuse = g.fuse > 1 ? (float)g.fuse : 1.0f;
             const int eA = g.A.e[r];
             const int nnzA = g.A.nnz[r];
             const float l2A = g.A.l2[r];
@@ -590,10 +597,11 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             continue;
                         }
                         bool exact = __fmul_ru(sA, sB) < 4096.0f;
-                        if (exact && __fmul_ru(dnAmax, dnBmax) >= two24) {
+                        if (exact && __fmul_ru(__fmul_ru(dnAmax, dnBmax), fuse) >= two24) {
                             for (int cc = 0; cc < g.nchunks; ++cc)
-                                if (__fmul_ru(g.A.dn[(long)r * g.nchunks + cc],
-                                              __ldg(&g.B.dn[(long)col * g.nchunks + cc])) >= two24)
+                                if (__fmul_ru(__fmul_ru(g.A.dn[(long)r * g.nchunks + cc],
+                                                        __ldg(&g.B.dn[(long)col * g.nchunks + cc])),
+                                              fuse) >= two24)
                                     exact = false;
                         }
                         const float f64b = __fmul_ru(cf64A, l2B);

@@ -39,6 +39,11 @@ struct Prod {
     int ia, ib;     // digit index of A and of B
     int t;          // ia + ib (weight 2^{-t beta})
     int chunk;      // inner-dimension chunk
+    // Products of one weight and chunk may share an accumulator (a fused group): open = the
+    // first of its group (the accumulator starts from zero), close = the last (the epilogue
+    // drains it).  Unfused products have both.
+    int open, close;
+    int pad[2];
 };
 
 // Fixed-point position of the exact recombination: the running sum of the digit products
@@ -96,6 +101,9 @@ struct GemmArgs {
     // exact-accumulation certificate failed), bnd[row * ldb + col]
     float* bnd;
     long ldb;
+    // largest number of products a fused group adds into one accumulator (0 or 1: none); the
+    // exactness certificate then bounds that many products' sum
+    int fuse;
 };
 
 // One group of a grouped launch: a block pair's operands (tensor maps) and arguments.

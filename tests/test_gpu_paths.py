@@ -232,3 +232,19 @@ def test_upper_side_in_two_halves_matches_one_phase(built_lib, monkeypatch):
     st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
     assert st["kernel_launches"] >= 9   # two upper slicings and two amplitude GEMM launches
     np.testing.assert_array_equal(eng.fetch_amp(), one)
+
+
+def test_fused_first_gemm_products_are_exact(c4_medium, monkeypatch):
+    """Short band tiles add the digit products of one weight into one accumulator before the
+    drain; the sums are exact integers, so the amplitudes equal the unfused run's bit for bit."""
+    import gainls
+    p, eng = c4_medium
+    nI = p.blocks[(0, 0)].vecs.shape[0]
+    nF = p.blocks[(1, 1)].vecs.shape[0]
+    lo, up = list(range(nI)), list(range(nF))
+    st = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    fused = eng.fetch_amp().copy()
+    monkeypatch.setenv("GAINLS_FUSE1", "0")
+    st0 = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
+    assert st["inexact"] == 0 and st0["inexact"] == 0
+    np.testing.assert_array_equal(eng.fetch_amp(), fused)
