@@ -3115,6 +3115,7 @@ struct PlanJob {
     DevArray<int2> flags1, flags2;
     DevArray<split::Prod> prods1, prods2;
     int nprods1 = 0, nprods2 = 0, fuse1 = 1;
+    int uowner = -1;              // a job whose upper digits this one reads (same block, levels, layout)
     CUtensorMap tmV{}, tmH{}, tmU{};
     const void* vI = nullptr;     // eigenvector and band-digit buffers the graph captured
     const void* vF = nullptr;
@@ -3224,9 +3225,23 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     J.Nupad = round_up(J.Nu, split::BN);
     J.cap1 = (int)std::min<long>(kMaxFlags, std::max<long>(4096, (long)J.Bpad * L.fpad / 8));
     J.cap2 = (int)std::min<long>(kMaxFlags, std::max<long>(4096, (long)J.Bpad * J.Nupad / 8));
+    // jobs with the same upper block, upper levels, upper layout and digits share one set of
+    // upper digits (the first of them slices it)
+    J.uowner = -1;
+    for (auto& Q : P->jobs) {
+        if (Q.get() == &J) break;
+        const PairLayout& QL = *Q->L;
+        if (Q->job.jindF == j->jindF && Q->job.gammaF == j->gammaF && Q->upper == J.upper && Q->K2 == J.K2 &&
+            Q->p2.beta == J.p2.beta && Q->p2.slices == J.p2.slices && Q->p2.chunks == J.p2.chunks &&
+            QL.general == L.general && QL.colposF == L.colposF && QL.f_sym == L.f_sym && QL.nsymF == L.nsymF &&
+            Q->uowner < 0) {
+            J.uowner = (int)(&Q - &P->jobs[0]);
+            break;
+        }
+    }
     const size_t vdig = (size_t)J.p1.slices * J.Bpad * L.kpadI;
     const size_t hdig = (size_t)J.p2.slices * J.Bpad * J.K2;
-    const size_t udig = (size_t)J.p2.slices * J.Nupad * J.K2;
+    const size_t udig = J.uowner < 0 ? (size_t)J.p2.slices * J.Nupad * J.K2 : 0;
     GAIN_TRY(J.Vdig.alloc(vdig));
     GAIN_TRY(J.Vdig.zero(st, vdig));
     GAIN_TRY(J.Vst.alloc(J.Bpad, J.p1.chunks, false));
@@ -3235,10 +3250,15 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     GAIN_TRY(J.Hdig.zero(st, hdig));
     GAIN_TRY(J.Hst.alloc(J.Bpad, J.p2.chunks, true));
     GAIN_TRY(J.Hst.zero(st, J.Bpad, J.p2.chunks, true));
-    GAIN_TRY(J.Udig.alloc(udig));
-    GAIN_TRY(J.Udig.zero(st, udig));
-    GAIN_TRY(J.Ust.alloc(J.Nupad, J.p2.chunks, false));
-    GAIN_TRY(J.Ust.zero(st, J.Nupad, J.p2.chunks, false));
+    if (J.uowner < 0) {
+        GAIN_TRY(J.Udig.alloc(udig));
+        GAIN_TRY(J.Udig.zero(st, udig));
+        GAIN_TRY(J.Ust.alloc(J.Nupad, J.p2.chunks, false));
+        GAIN_TRY(J.Ust.zero(st, J.Nupad, J.p2.chunks, false));
+    } else {   // not this job's: release what an earlier preparation left
+        J.Udig.release();
+        J.Ust = StatsDev();
+    }
     GAIN_TRY(J.H.alloc((size_t)J.Bpad * L.fpad));
     GAIN_TRY(J.rowerr.alloc(J.Bpad));
     GAIN_TRY(J.amp.alloc((size_t)J.Bpad * J.Nupad));
@@ -3262,7 +3282,8 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     J.nprods2 = (int)pr2.size();
     if (!split::make_digit_map(&J.tmV, J.Vdig.p, L.kpadI, J.Bpad, J.p1.slices) ||
         !split::make_digit_map(&J.tmH, J.Hdig.p, J.K2, J.Bpad, J.p2.slices) ||
-        !split::make_digit_map(&J.tmU, J.Udig.p, J.K2, J.Nupad, J.p2.slices, P->pair ? split::BN / 2 : split::BM))
+        (J.uowner < 0 &&
+         !split::make_digit_map(&J.tmU, J.Udig.p, J.K2, J.Nupad, J.p2.slices, P->pair ? split::BN / 2 : split::BM)))
         return set_error(GAIN_ERR_CUDA, "cuTensorMapEncodeTiled failed (plan job digits)");
     J.vI = EI.d.p;
     J.vF = EF.d.p;
@@ -3347,7 +3368,8 @@ gain_status plan_build_groups(gain_plan P) {
         a1.cols_valid = L.fpad;
         a1.fuse = J.fuse1;
         g2[q].tmA = J.tmH;
-        g2[q].tmB = J.tmU;
+        PlanJob& JU = J.uowner < 0 ? J : *P->jobs[J.uowner];   // the upper digits' owner
+        g2[q].tmB = JU.tmU;
         split::GemmArgs& a2 = g2[q].args;
         a2.prods = J.prods2.p;
         a2.nprods = J.nprods2;
@@ -3357,7 +3379,7 @@ gain_status plan_build_groups(gain_plan P) {
         a2.out = J.amp.p;
         a2.ldo = J.Nupad;
         a2.A = J.Hst.view(false);
-        a2.B = J.Ust.view(false);
+        a2.B = JU.Ust.view(false);
         a2.c_fix = fix_const(J.nprods2);
         a2.c_f64 = (float)((double)((L.general ? L.nsymF : L.nF) + 64) * std::ldexp(1.0, -53) * 1.01);
         a2.absmax = P->ull.p + 4 * q + 2;
@@ -3453,13 +3475,15 @@ gain_status plan_enqueue(gain_plan P) {
                                            EI.d.p, EI.nsize, J.d_lower.p, J.primI.p, bI.dimen, J.B, sq));
             GAIN_TRY(slice(e, J.primI.p, bI.dimen, nullptr, J.B, bI.dimen, nullptr, nullptr, L.kpadI, J.Bpad, J.Vdig.p,
                            J.p1, J.Vst, false, nullptr, nullptr, sq, L.d_i_sym.p));
-            GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, L.nsymF, nullptr, nullptr, J.K2, J.Nupad, J.Udig.p,
-                           J.p2, J.Ust, false, nullptr, nullptr, sq, nullptr));
+            if (J.uowner < 0)
+                GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, L.nsymF, nullptr, nullptr, J.K2, J.Nupad,
+                               J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr, sq, nullptr));
         } else {
             GAIN_TRY(slice(e, EI.d.p, EI.nsize, J.d_lower.p, J.B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI,
                            J.Bpad, J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr, sq, L.d_i_sym.p));
-            GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad,
-                           J.Nupad, J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr, sq, L.d_f_sym.p));
+            if (J.uowner < 0)
+                GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad,
+                               J.Nupad, J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr, sq, L.d_f_sym.p));
         }
         GAIN_CUDA(cudaMemsetAsync(J.rowerr.p, 0, sizeof(float) * J.Bpad, sq));
     }
