@@ -597,7 +597,10 @@ def adjoint_check(args):
     times["fd_direct_s"] = time.perf_counter() - t1
     dirs, jdirs = [], []
     for _ in range(3):
+        # a unit direction: h d then moves each entry by about h / sqrt(entries), the regime in
+        # which the central difference of this (weak-line dominated) loss is accurate
         d = rng.standard_normal(mu0.shape)
+        d /= np.linalg.norm(d)
         gd = float(np.sum(grad * d))
         fd = (loss(mu0 + h * d) - loss(mu0 - h * d)) / (2 * h)
         dirs.append(abs(fd - gd) / abs(gd))

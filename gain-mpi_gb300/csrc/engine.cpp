@@ -3223,8 +3223,14 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     const int mstep = P->pair ? 2 * split::BM : split::BM;
     J.Bpad = round_up(J.B, mstep);
     J.Nupad = round_up(J.Nu, split::BN);
-    J.cap1 = (int)std::min<long>(kMaxFlags, std::max<long>(4096, (long)J.Bpad * L.fpad / 8));
-    J.cap2 = (int)std::min<long>(kMaxFlags, std::max<long>(4096, (long)J.Bpad * J.Nupad / 8));
+    // refinement-list capacity: every entry of a small job (up to 2^20), an eighth of a large
+    // one's (at least 2^20, at most the single-pair runs' list)
+    auto cap_of = [](long entries) {
+        return (int)(entries <= (1L << 20) ? std::max<long>(entries, 1)
+                                          : std::min<long>(kMaxFlags, std::max<long>(1L << 20, entries / 8)));
+    };
+    J.cap1 = cap_of((long)J.Bpad * L.fpad);
+    J.cap2 = cap_of((long)J.Bpad * J.Nupad);
     // jobs with the same upper block, upper levels, upper layout and digits share one set of
     // upper digits (the first of them slices it)
     J.uowner = -1;

@@ -362,29 +362,39 @@ def make_eigvecs(n: int, J: int, gamma: int, device: str | None = None,
 
 def make_eigvecs_kron(n: int, J: int, gamma: int, device: str = "cuda"):
     """A dense orthonormal n x n matrix made quickly on the device (for block sizes whose QR
-    factorisation would take minutes): with n1 = floor(sqrt(n)), n2 = n // n1 and r = n - n1 n2,
-    U = P_r blockdiag(Q1 (x) Q2, Q3) P_c, where Q1, Q2, Q3 are the Q factors of seeded N(0,1)
-    matrices of sizes n1, n2, r (the same seeds as make_eigvecs) and P_r, P_c seeded
-    permutations of the rows and columns.  A Kronecker product of orthogonal matrices is
-    orthogonal, so U is orthonormal to rounding.  Returns a torch tensor [n, n] (rows = states)."""
+    factorisation would take minutes).  With n1 = floor(sqrt(n)), n2 = n // n1, m = n1 n2 and
+    r = n - m: Y = (Q3 (x) Q4) P (Q1 (x) Q2) on the first m coordinates (a row permutation P
+    between two Kronecker products of Q factors of seeded N(0,1) matrices, the second product
+    applied as two small contractions, so every entry sums n1 n2 products and the rows are
+    dense rather than spiky), Q5 (r x r) on the rest, then seeded permutations of rows and
+    columns.  Kronecker products and permutations of orthogonal matrices are orthogonal, so the
+    result is orthonormal to rounding.  Returns a torch tensor [n, n] (rows = states)."""
     import torch
     rng = np.random.default_rng(vec_seed(J, gamma))
     n1 = max(1, int(np.floor(np.sqrt(n))))
     n2 = n // n1
-    r = n - n1 * n2
+    m = n1 * n2
+    r = n - m
 
-    def q(m):
-        g = torch.from_numpy(rng.standard_normal((m, m))).to(device)
+    def q(k):
+        g = torch.from_numpy(rng.standard_normal((k, k))).to(device)
         qq, rr = torch.linalg.qr(g)
         sgn = torch.sign(torch.diagonal(rr))
         sgn[sgn == 0] = 1.0
         return qq * sgn[None, :]
 
-    Q1, Q2 = q(n1), q(n2)
+    Q1, Q2, Q3, Q4 = q(n1), q(n2), q(n1), q(n2)
+    Y = torch.kron(Q1, Q2)
+    Y = Y[torch.from_numpy(rng.permutation(m)).to(device)]
+    # (Q3 (x) Q4) Y: rows indexed (a, b), a < n1, b < n2
+    Y = Y.view(n1, n2, m)
+    Y = torch.einsum("bc,acj->abj", Q4, Y)
+    Y = torch.einsum("ac,cbj->abj", Q3, Y).reshape(m, m)
     U = torch.zeros((n, n), dtype=torch.float64, device=device)
-    U[: n1 * n2, : n1 * n2] = torch.kron(Q1, Q2)
+    U[:m, :m] = Y
+    del Y
     if r > 0:
-        U[n1 * n2:, n1 * n2:] = q(r)
+        U[m:, m:] = q(r)
     pr = torch.from_numpy(rng.permutation(n)).to(device)
     pc = torch.from_numpy(rng.permutation(n)).to(device)
     return U[pr][:, pc].contiguous()
