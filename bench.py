@@ -901,8 +901,9 @@ def batch_stream(args):
             ref = eng.fetch_amp()
             S, Sr = a[rows] ** 2, ref ** 2
             m = Sr > 1e-10 * Sr.max()
-            worst = max(worst, float(np.max(np.abs(S[m] - Sr[m]) / Sr[m])))
-            nchk += int(m.sum())
+            if m.any():
+                worst = max(worst, float(np.max(np.abs(S[m] - Sr[m]) / Sr[m])))
+                nchk += int(m.sum())
         plan.close()
         for (J, c) in need:
             eng.release_eigvecs(J, c)

@@ -236,7 +236,9 @@ def test_upper_side_in_two_halves_matches_one_phase(built_lib, monkeypatch):
 
 def test_fused_first_gemm_products_are_exact(c4_medium, monkeypatch):
     """Short band tiles add the digit products of one weight into one accumulator before the
-    drain; the sums are exact integers, so the amplitudes equal the unfused run's bit for bit."""
+    drain.  The sums are exact integers; only the truncation of weights below 2^-50 of the
+    fixed-point recombination moves (once per group instead of once per product), so the
+    amplitudes agree with the unfused run's to that level and both certify."""
     import gainls
     p, eng = c4_medium
     nI = p.blocks[(0, 0)].vecs.shape[0]
@@ -247,4 +249,5 @@ def test_fused_first_gemm_products_are_exact(c4_medium, monkeypatch):
     monkeypatch.setenv("GAINLS_FUSE1", "0")
     st0 = eng.run_pair(0, 0, 1, 1, lo, up, gainls.PATH_SPLIT)
     assert st["inexact"] == 0 and st0["inexact"] == 0
-    np.testing.assert_array_equal(eng.fetch_amp(), fused)
+    unfused = eng.fetch_amp()
+    assert np.max(np.abs(unfused - fused)) <= 1e-13 * np.abs(unfused).max()
