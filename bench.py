@@ -879,9 +879,15 @@ def batch_stream(args):
             eng.upload_eigvecs_device(J, c, rows_t.data_ptr(), int(rows_t.shape[0]), dims[(J, c)])
             del U, rows_t
         torch.cuda.synchronize()
+        torch.cuda.empty_cache()   # the generator's blocks go back to the device for the plan
         gen_s += time.perf_counter() - g0
         w0 = time.perf_counter()
-        plan = gainls.Plan(eng, [(a, b, c, d, lo, up) for a, b, c, d, lo, up in jobs])
+        try:
+            plan = gainls.Plan(eng, [(a, b, c, d, lo, up) for a, b, c, d, lo, up in jobs])
+        except gainls.GainError as exc:
+            free, total = torch.cuda.mem_get_info()
+            raise RuntimeError(f"wave {w} (upper block J={JF} Gamma={cF}, {len(jobs)} jobs): {exc}; device memory "
+                               f"free {free / 1e9:.1f} of {total / 1e9:.1f} GB") from exc
         plan.run()
         ps, js, st = plan.run()
         wall_ms += (time.perf_counter() - w0) * 1e3
