@@ -267,7 +267,11 @@ struct gain_engine_s {
     bool lines_pending = false;     // gain_pair_lines_async copies still in flight
     long long* lines_nout = nullptr;   // their caller's n_lines
     cudaEvent_t ev[10] = {};
-    cudaEvent_t ev_up = nullptr;  // orders an asynchronous upload after queued engine work
+    // orders an asynchronous upload after the engine work that reads eigenvectors: recorded
+    // at the end of every run (runs, plans, adjoints and line recomputations return only when
+    // their work is done), so an upload need not wait for line kernels queued after a run
+    cudaEvent_t ev_up = nullptr;
+    bool ev_up_fresh = false;   // recorded after the last eigenvector reader (else record anew)
     std::vector<long> zkey_V, zkey_H, zkey_U;   // shape/layout the digit buffers were cleared for
     gain::DevArray<double> d3j;
     std::vector<gain::Basis> bases;
@@ -1973,7 +1977,7 @@ gain_status gain_upload_eigvecs_async(gain_engine e, int jind, int gamma, int nl
     GAIN_TRY(slot->d.alloc((size_t)nlevels * nsize));
     // after everything already queued on the engine's streams (the second stream's work is
     // joined to the first before each run ends)
-    GAIN_CUDA(cudaEventRecord(e->ev_up, e->st));
+    if (!e->ev_up_fresh) GAIN_CUDA(cudaEventRecord(e->ev_up, e->st));   // after all queued work
     GAIN_CUDA(cudaStreamWaitEvent(e->stc, e->ev_up, 0));
     // two parts: a run can start on the upper states of the first part while the second
     // is still arriving
@@ -2237,6 +2241,7 @@ gain_status adjoint_run(gain_engine e, const gain_pair_job* job, const std::vect
     const bool f32 = prec == GAIN_ADJOINT_FP32;
     const bool tc = prec == GAIN_ADJOINT_SPLIT;
     double tflops = 0.0;
+    e->ev_up_fresh = false;
     const Basis& bI = e->bases[job->jindI];
     const Basis& bF = e->bases[job->jindF];
     Inflation& iI = e->infl[job->jindI];
@@ -2406,6 +2411,8 @@ gain_status adjoint_run(gain_engine e, const gain_pair_job* job, const std::vect
         stats->kernel_launches = (tc ? 17 : 5) * (int)comps.size();
         stats->tensor_flops = tflops;
     }
+    GAIN_CUDA(cudaEventRecord(e->ev_up, st));
+    e->ev_up_fresh = true;
     return GAIN_OK;
 }
 
@@ -2463,6 +2470,7 @@ gain_status run_component(gain_engine e, const gain_pair_job* job, int dI, int d
         return set_error(GAIN_ERR_INVALID_ARG, "components (%d, %d) outside the degeneracies (%d, %d)", dI, dF, sI, sF);
     e->have_amp = false;
     e->have_bnd = false;
+    e->ev_up_fresh = false;
     gain_status r;
     if (path == GAIN_PATH_PLAIN_FP64)
         r = e->pieces.size() > 1 ? run_plain_pieces(e, job, dI, dF, stats) : run_plain(e, job, dI, dF, stats);
@@ -2471,6 +2479,10 @@ gain_status run_component(gain_engine e, const gain_pair_job* job, int dI, int d
     else
         return set_error(GAIN_ERR_INVALID_ARG, "unknown path %d", (int)path);
     e->amp_job = r == GAIN_OK ? job_key(job, dI, dF) : std::vector<int>();
+    if (r == GAIN_OK) {   // the run's readers of the eigenvectors are done
+        GAIN_CUDA(cudaEventRecord(e->ev_up, e->st));
+        e->ev_up_fresh = true;
+    }
     return r;
 }
 }  // namespace
@@ -2679,6 +2691,7 @@ gain_status thresh_certify(gain_engine e, const gain_line_params* prm, const Lin
                          "recomputed)", cnt, kThreshCap);
     std::vector<int2> list(cnt);
     GAIN_CUDA(cudaMemcpy(list.data(), e->thr_list.p, sizeof(int2) * cnt, cudaMemcpyDeviceToHost));
+    e->ev_up_fresh = false;   // the FP64 recomputation reads the eigenvectors
     // the job's level lists: job_key = {pair (4), nlower, nupper, dI, dF, lower..., upper...}
     const std::vector<int>& key = e->amp_job;
     if (key.size() < 8 || key[4] != rows || key[5] != cols)
@@ -2748,6 +2761,8 @@ gain_status thresh_certify(gain_engine e, const gain_line_params* prm, const Lin
         GAIN_CUDA(cudaStreamSynchronize(st));   // sub_amp and the pair list are reused by the next component
     }
     e->thresh_refined = cnt;
+    GAIN_CUDA(cudaEventRecord(e->ev_up, st));
+    e->ev_up_fresh = true;
     return GAIN_OK;
 }
 
@@ -3662,8 +3677,11 @@ gain_status plan_replay(gain_plan P, double* ms_out) {
         if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EI.ready, 0));
         if (EF.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EF.ready, 0));
     }
+    e->ev_up_fresh = false;
     GAIN_CUDA(cudaGraphLaunch(P->exec, st));
+    GAIN_CUDA(cudaEventRecord(e->ev_up, st));
     GAIN_CUDA(cudaStreamSynchronize(st));
+    e->ev_up_fresh = true;
     float ms = 0.f;
     GAIN_CUDA(cudaEventElapsedTime(&ms, P->ev[0], P->ev[5]));
     if (ms_out) *ms_out = ms;
