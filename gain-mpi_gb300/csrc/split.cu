@@ -1040,160 +1040,6 @@ k_slice4(const SliceArgs a) {
     }
 }
 
-// The same digits and statistics as k_slice4, one WARP per row: no block barriers, no
-// shared memory; the row's sums reduce with warp shuffles (integer sums exactly, float sums
-// rounded up as before, in another order, so the norms stay upper bounds).  Eight rows per
-// 256-thread block.
-template <int S>
-__global__ void __launch_bounds__(SLICE_THREADS, 3)
-k_slice4w(const SliceArgs a) {
-    constexpr int WPB = SLICE_THREADS / 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nkb = a.kpad / BK;
-    const int beta = a.beta;
-    const int q = S * beta;
-    const long long mask = (1ll << beta) - 1ll;
-    const int off = (1 << (beta - 1)) - 1;
-    long long C = 0;
-#pragma unroll
-    for (int k = 0; k < S - 1; ++k) C += (long long)off << (beta * k);
-    const float inv2q = pow2f(-q);
-    float w2[S];   // 2^{-(i+1) beta}
-#pragma unroll
-    for (int i = 0; i < S; ++i) w2[i] = pow2f(-(i + 1) * beta);
-    for (int row = blockIdx.x * WPB + warp; row < a.nrows; row += gridDim.x * WPB) {
-        const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
-        const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
-        // pass 1: max |x| through the IEEE bit pattern
-        unsigned long long mx = 0;
-#pragma unroll 4
-        for (int c = lane; c < a.ncols; c += 32) {
-            const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
-            mx = b > mx ? b : mx;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
-            mx = y > mx ? y : mx;
-        }
-        if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
-        const int Emax = (int)(mx >> 52);
-        const bool zero_row = (mx == 0);
-        const int e = zero_row ? 0 : (Emax > 0 ? Emax - 1022 : -1022);
-        const long sstride = a.slice_stride;
-        __nv_bfloat16* drow = a.digits + (long)row * a.kpad;
-        int nnz = 0;
-        float l2sq = 0.0f;
-        float tsq[S];
-        unsigned long long dtot[S];   // the row's digit sums of squares (all lanes)
-#pragma unroll
-        for (int i = 0; i < S; ++i) {
-            tsq[i] = 0.0f;
-            dtot[i] = 0ull;
-        }
-        for (int ch = 0; ch < a.nchunks; ++ch) {
-            unsigned int dsq[S];   // this lane's: at most kpad / 32 squares below 2^16 each
-#pragma unroll
-            for (int i = 0; i < S; ++i) dsq[i] = 0u;
-            const int d0 = (int)(((long)ch * nkb) / a.nchunks) * BK;
-            const int d1 = (int)(((long)(ch + 1) * nkb) / a.nchunks) * BK;
-            for (int dc = d0 + 4 * lane; dc < d1; dc += 128) {
-                uint32_t pk[S][2];
-                uint32_t even[S];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int col = dc + u;
-                    const int sc = a.col_inv ? a.col_inv[col] : (col < a.ncols ? col : -1);
-                    const unsigned long long bits = sc >= 0 ? src[sc] : 0ull;
-                    const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
-                    long long I = 0;
-                    if (!zero_row && ab != 0 && ab < 0x7FF0000000000000ull) {
-                        const int E = (int)(ab >> 52);
-                        unsigned long long mant = ab & 0xFFFFFFFFFFFFFull;
-                        int ex;
-                        if (E > 0) { mant |= 1ull << 52; ex = E - 1075; }
-                        else ex = -1074;
-                        const int sh = ex + q - e;
-                        const unsigned long long m = sh >= 0 ? (mant << sh) : rne_shr(mant, -sh);
-                        I = (bits >> 63) ? -(long long)m : (long long)m;
-                    }
-                    const long long uo = I + C;
-                    int d[S];
-#pragma unroll
-                    for (int i = S - 1; i >= 1; --i)
-                        d[i] = (int)(((unsigned long long)uo >> (beta * (S - 1 - i))) & mask) - off;
-                    d[0] = (int)(uo >> (beta * (S - 1)));
-                    float tail = 0.0f;
-#pragma unroll
-                    for (int i = S - 1; i >= 1; --i) {
-                        tail = __fadd_rn(tail, (float)d[i] * w2[i]);
-                        tsq[i - 1] = __fmaf_ru(tail, tail, tsq[i - 1]);
-                    }
-#pragma unroll
-                    for (int i = 0; i < S; ++i) {
-                        dsq[i] += (unsigned int)(d[i] * d[i]);
-                        const uint32_t fb = __float_as_uint((float)d[i]);   // exact: BF16 = upper half
-                        if (u & 1) pk[i][u >> 1] = __byte_perm(even[i], fb, 0x7632);
-                        else even[i] = fb;
-                    }
-                    if (I != 0) {
-                        ++nnz;
-                        const unsigned long long aI = (unsigned long long)(I < 0 ? -I : I);
-                        const float xv = __fmul_ru(__ull2float_ru(aI), inv2q);
-                        l2sq = __fmaf_ru(xv, xv, l2sq);
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < S; ++i)
-                    *reinterpret_cast<uint2*>(drow + i * sstride + dc) = make_uint2(pk[i][0], pk[i][1]);
-            }
-            // this chunk's digit sums of squares over the warp (exact integers)
-            unsigned long long mch = 0ull;
-#pragma unroll
-            for (int i = 0; i < S; ++i) {
-                unsigned long long t = dsq[i];
-                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-                dtot[i] += t;
-                mch = t > mch ? t : mch;
-            }
-            if (lane == 0) a.st.dn[(long)row * a.nchunks + ch] = __fsqrt_ru(__ull2float_ru(mch));
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            l2sq = __fadd_ru(l2sq, __shfl_xor_sync(0xffffffffu, l2sq, o));
-            nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
-        }
-#pragma unroll
-        for (int i = 0; i < S; ++i)
-            for (int o = 16; o > 0; o >>= 1) tsq[i] = __fadd_ru(tsq[i], __shfl_xor_sync(0xffffffffu, tsq[i], o));
-        // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
-        const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
-        const float dq = __fmul_ru(__fsqrt_ru((float)nnz), pow2f(-q - 1));
-        if (lane < MAX_SLICES) {   // one slice per lane
-            float dv = 0.0f, rv = 0.0f;
-#pragma unroll
-            for (int i = 0; i < S; ++i)
-                if (lane == i) {
-                    dv = __fsqrt_ru(__ull2float_ru(dtot[i]));
-                    rv = __fadd_ru(__fmul_ru(__fsqrt_ru(tsq[i]), slack), dq);
-                }
-            a.st.dnv[(long)row * MAX_SLICES + lane] = dv;
-            a.st.rnv[(long)row * MAX_SLICES + lane] = rv;
-        } else if (lane == 31) {
-            a.st.e[row] = e;
-            a.st.nnz[row] = nnz;
-            a.st.l2[row] = __fadd_ru(__fmul_ru(__fsqrt_ru(l2sq), slack), dq);
-            if (a.st.inerr) {
-                float v = 0.0f;
-                if (a.inerr2_prev && !zero_row) {
-                    const int de = a.e_prev[row] - e;
-                    v = __fmul_ru(__fmul_ru(__fsqrt_ru(a.inerr2_prev[row]), 1.0001f), pow2f(max(-126, min(127, de))));
-                    if (de > 127) v = __int_as_float(0x7f800000);   // cannot certify: infinite bound
-                }
-                a.st.inerr[row] = v;
-            }
-        }
-    }
-}
-
 // ------------------------------------------------------------------- band builder
 __device__ __forceinline__ double parity_sign(int x) { return (x & 1) ? -1.0 : 1.0; }
 
@@ -1478,19 +1324,9 @@ cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st) {
     cudaError_t e = set_attributes_once();
     if (e != cudaSuccess) return e;
     const int grid = (a.grid_limit > 0 && a.grid_limit < a.nrows) ? a.grid_limit : a.nrows;
-    // the four-column kernels need the destination map (or the identity) and whole k-blocks;
-    // the warp-per-row form (GAINLS_SLICE_WARP=0 keeps the block-per-row one)
+    // the four-column kernel needs the destination map (or the identity) and whole k-blocks
     const bool four = (a.col_inv || !a.col_map) && (a.kpad % BK) == 0;
-    const char* wv = getenv("GAINLS_SLICE_WARP");
-    const bool warp_rows = !(wv && wv[0] == '0');
-    if (four && warp_rows) {
-        constexpr int WPB = SLICE_THREADS / 32;
-        const int wgrid = std::max(1, std::min(grid, (a.nrows + WPB - 1) / WPB));
-        if (a.slices == 6) k_slice4w<6><<<wgrid, SLICE_THREADS, 0, st>>>(a);
-        else if (a.slices == 7) k_slice4w<7><<<wgrid, SLICE_THREADS, 0, st>>>(a);
-        else if (a.slices == 8) k_slice4w<8><<<wgrid, SLICE_THREADS, 0, st>>>(a);
-        else k_slice<<<grid, SLICE_THREADS, 0, st>>>(a);
-    } else if (four && a.slices == 6) k_slice4<6><<<grid, SLICE_THREADS, 0, st>>>(a);
+    if (four && a.slices == 6) k_slice4<6><<<grid, SLICE_THREADS, 0, st>>>(a);
     else if (four && a.slices == 7) k_slice4<7><<<grid, SLICE_THREADS, 0, st>>>(a);
     else if (four && a.slices == 8) k_slice4<8><<<grid, SLICE_THREADS, 0, st>>>(a);
     else k_slice<<<grid, SLICE_THREADS, 0, st>>>(a);
