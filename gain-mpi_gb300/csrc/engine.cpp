@@ -672,6 +672,27 @@ std::vector<split::Prod> make_prods(const SplitParams& p, int fuse = 1) {
     return v;
 }
 
+// Tile order for L2 reuse: a list built column-block-major (all row tiles of a column block,
+// then the next column block) is regrouped into row groups of kRowGroup row tiles: for each
+// group, every column block's tiles of those rows.  The persistent CTAs take consecutive
+// tiles, so the concurrent tiles then share kRowGroup A row tiles and about units/kRowGroup
+// B column tiles, whose digits stay in L2 across the digit products (with all row tiles of a
+// tall operand per column block, the A tiles of one product exceed L2 and are read from DRAM
+// again for every product).  key_split (optional) keeps tiles with key_split(t) = 0 before the
+// others (the upper halves of a run whose upper vectors are still arriving).
+constexpr int kRowGroup = 8;
+template <class Split>
+void row_grouped(std::vector<split::Tile>& t, int mstep, Split key_split) {
+    std::stable_sort(t.begin(), t.end(), [&](const split::Tile& a, const split::Tile& b) {
+        const int sa = key_split(a), sb = key_split(b);
+        if (sa != sb) return sa < sb;
+        return a.m0 / (kRowGroup * mstep) < b.m0 / (kRowGroup * mstep);
+    });
+}
+void row_grouped(std::vector<split::Tile>& t, int mstep) {
+    row_grouped(t, mstep, [](const split::Tile&) { return 0; });
+}
+
 // Products fused per accumulator in the first GEMM: only where each product is short (fewer
 // than 16 k-blocks per tile, so that draining the accumulator after every product would pace
 // the tensor pipe); as many as keep the expected sum of their digit norms' products, K_chunk
@@ -1261,6 +1282,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
                     t1.push_back(t);
                 }
             }
+        row_grouped(t1, mstep);
         GAIN_TRY(e->tiles1.upload(t1));
         split::GemmArgs g1;
         memset(&g1, 0, sizeof g1);
@@ -1372,6 +1394,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
             t.nkb = K2 / split::BK;
             t2.push_back(t);
         }
+    row_grouped(t2, mstep, [&](const split::Tile& t) { return Nu2 > 0 && t.n0 >= Nu2 ? 1 : 0; });
     const std::vector<split::Prod> pr2 = make_prods(p2);
     GAIN_TRY(e->tiles2.upload(t2));
     GAIN_TRY(e->prods2.upload(pr2));
@@ -2110,6 +2133,7 @@ gain_status adjoint_split_chain(gain_engine e, const gain_pair_job* job, int dI,
                 x.nkb = Nuk / BK;
                 t.push_back(x);
             }
+        row_grouped(t, BM);
         GAIN_TRY(e->adjs_dH.alloc((size_t)Bpad * NtFpad));
         GAIN_TRY(gemm(0, 1, pA, Nuk, Bpad, NtFpad, e->adjs_dH.p, NtFpad, B, NtF, t, e->adjs_tiles1, e->adjs_prods1,
                       e->adjs_cnt.p));
@@ -3445,6 +3469,25 @@ gain_status plan_build_groups(gain_plan P) {
                 P->flops += 2.0 * mstep * split::BN * split::BK * t.nkb * tri2;
             }
     }
+    // each job's tiles in row groups (concurrent tiles share their operands' digits in L2)
+    auto regroup = [&](std::vector<split::Tile>& t, std::vector<double>& c) {
+        std::vector<int> idx(t.size());
+        for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+            if (t[a].group != t[b].group) return t[a].group < t[b].group;
+            return t[a].m0 / (kRowGroup * mstep) < t[b].m0 / (kRowGroup * mstep);
+        });
+        std::vector<split::Tile> t2s(t.size());
+        std::vector<double> c2s(c.size());
+        for (size_t i = 0; i < idx.size(); ++i) {
+            t2s[i] = t[idx[i]];
+            c2s[i] = c[idx[i]];
+        }
+        t.swap(t2s);
+        c.swap(c2s);
+    };
+    regroup(t1, c1);
+    regroup(t2, c2);
     P->real1 = (int)t1.size();
     P->real2 = (int)t2.size();
     const std::vector<split::Tile> s1 = lpt_schedule(t1, c1, P->units), s2 = lpt_schedule(t2, c2, P->units);
