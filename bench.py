@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--batch-jmax", type=int, default=30, help="largest J of --batch")
     ap.add_argument("--batch-stream", action="store_true",
                     help="many block pairs at the full size (N_v from --batch-nv, default 2000 here), in waves")
+    ap.add_argument("--stream-upper-j", type=int, default=-1,
+                    help="--batch-stream: only the waves whose upper J is this one, each also run pair by pair")
     return ap.parse_args()
 
 
@@ -864,7 +866,7 @@ def batch_stream(args):
                 if nlow[(JI, cI)] == 0 or dims[(JF, cF)] == 0:
                     continue
                 jobs.append((JI, cI, JF, cF, list(range(nlow[(JI, cI)])), list(range(dims[(JF, cF)]))))
-            if jobs:
+            if jobs and (args.stream_upper_j < 0 or JF == args.stream_upper_j):
                 waves.append(((JF, cF), jobs))
     setup_s = time.perf_counter() - t0
     total = sum(len(j[4]) * len(j[5]) for _, jobs in waves for j in jobs)
@@ -896,6 +898,18 @@ def batch_stream(args):
         wall_ms += (time.perf_counter() - w0) * 1e3
         dev_ms += ps["device_ms"]
         trans = sum(len(j[4]) * len(j[5]) for j in jobs)
+        if args.stream_upper_j >= 0:   # the same jobs one by one through single-pair runs
+            single = []
+            for JI, cI, _, _, lo, up in jobs:
+                eng.run_pair(JI, cI, JF, cF, lo, up, gainls.PATH_SPLIT)
+                s1 = eng.run_pair(JI, cI, JF, cF, lo, up, gainls.PATH_SPLIT)
+                single.append({"device_ms": s1["device_ms"], "gemm1_ms": s1["gemm1_ms"], "gemm2_ms": s1["gemm2_ms"],
+                               "beta2": s1["beta2"], "slices2": s1["slices2"], "chunks2": s1["chunks2"],
+                               "refined": s1["refined"], "tensor_flops": s1["tensor_flops"]})
+            print(json.dumps({"wave": [JF, cF], "plan": {k: ps[k] for k in ("device_ms", "gemm1_ms", "gemm2_ms",
+                                                                           "tensor_flops", "refined", "pair")},
+                              "jobs": [[len(j[4]), len(j[5])] for j in jobs], "single_pair_runs": single}),
+                  flush=True)
         if biggest is None or trans > biggest["transitions"]:
             biggest = {"upper_block": [JF, cF], "jobs": len(jobs), "transitions": trans, "device_ms": ps["device_ms"],
                        "gemm1_ms": ps["gemm1_ms"], "gemm2_ms": ps["gemm2_ms"], "graph_nodes": ps["graph_nodes"],
