@@ -337,6 +337,10 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 const GemmArgs& g = group_args<GROUPED>(a, tl);
                 const CUtensorMap* mapA = GROUPED ? &a.groups[tl.group].tmA : &tmA;
                 const CUtensorMap* mapB = GROUPED ? &a.groups[tl.group].tmB : &tmB;
+                if (GROUPED) {   // the tile's tensor maps live in global memory: fetch them early
+                    asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)mapA) : "memory");
+                    asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)mapB) : "memory");
+                }
                 for (int p = 0; p < g.nprods && ok; ++p) {
                     const Prod pr = g.prods[p];
                     int lo, hi;
