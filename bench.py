@@ -872,6 +872,7 @@ def batch_stream(args):
     total = sum(len(j[4]) * len(j[5]) for _, jobs in waves for j in jobs)
     dev_ms, wall_ms, gen_s, worst, nchk = 0.0, 0.0, 0.0, 0.0, 0
     biggest = None
+    sampled = []
     t_all = time.perf_counter()
     for w, ((JF, cF), jobs) in enumerate(waves):
         g0 = time.perf_counter()
@@ -915,7 +916,7 @@ def batch_stream(args):
                        "gemm1_ms": ps["gemm1_ms"], "gemm2_ms": ps["gemm2_ms"], "graph_nodes": ps["graph_nodes"],
                        "tiles": [ps["gemm1_tiles"], ps["gemm2_tiles"]],
                        "tensor_tflops_in_gemms": ps["tensor_flops"] / ((ps["gemm1_ms"] + ps["gemm2_ms"]) * 1e-3) / 1e12}
-        if w % 10 == 0:   # accuracy sample: two lower states of the wave's largest job
+        if w % 10 == 0 or args.stream_upper_j >= 0:   # accuracy sample: two lower states of the largest job
             q = int(np.argmax([len(j[4]) * len(j[5]) for j in jobs]))
             JI, cI, _, _, lo, up = jobs[q]
             a = plan.amp(q)
@@ -923,10 +924,14 @@ def batch_stream(args):
             eng.run_pair(JI, cI, JF, cF, [lo[r] for r in rows], up, gainls.PATH_PLAIN_FP64)
             ref = eng.fetch_amp()
             S, Sr = a[rows] ** 2, ref ** 2
+            if not (np.isfinite(S).all() and np.isfinite(Sr).all()):
+                raise RuntimeError(f"wave {w} (upper block J={JF} Gamma={cF}): non-finite line strengths")
             m = Sr > 1e-10 * Sr.max()
-            if m.any():
-                worst = max(worst, float(np.max(np.abs(S[m] - Sr[m]) / Sr[m])))
-                nchk += int(m.sum())
+            err = float(np.max(np.abs(S[m] - Sr[m]) / Sr[m])) if m.any() else 0.0
+            worst = max(worst, err)
+            nchk += int(m.sum())
+            sampled.append({"upper_block": [JF, cF], "lower_block": [JI, cI], "lines_checked": int(m.sum()),
+                            "max_rel_err_S": err, "S_max": float(Sr.max())})
         plan.close()
         for (J, c) in need:
             eng.release_eigvecs(J, c)
@@ -941,7 +946,7 @@ def batch_stream(args):
            "largest_wave": biggest,
            "accuracy_sample": {"max_rel_err_S_vs_plain": worst, "lines_checked": nchk,
                                "sample": "2 lower states of the largest job of every 10th wave, all upper states",
-                               "domain": "S > 1e-10 S_max"},
+                               "domain": "S > 1e-10 S_max", "waves": sampled},
            "eigenvectors": "Kronecker products of seeded QR factors, rows/columns permuted (device)"}
     print(json.dumps(out), flush=True)
     eng.close()

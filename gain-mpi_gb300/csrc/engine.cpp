@@ -3338,16 +3338,22 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     return GAIN_OK;
 }
 
-// Longest-first spread of tiles over `units` persistent CTAs (CTA pairs): each tile goes to
-// the least loaded unit; the list is then laid out so that unit u runs entries u, u + units,
-// ... (empty slots: group -1).  Within a unit the tiles keep their list order.
-std::vector<split::Tile> lpt_schedule(const std::vector<split::Tile>& tiles, const std::vector<double>& cost,
-                                      int units) {
+// Spread of tiles over `units` persistent CTAs (CTA pairs) in list order: each tile goes to
+// the unit that frees up first, the order a dynamic scheduler would give, so that the tiles
+// running at any moment are neighbours in the list and share their operands' digits in L2 as
+// in a single run (a longest-first spread scatters every unit's k-th tile over the whole
+// list, and the digits of each then come from DRAM).  The jobs with the costliest tiles go
+// first, so that cheap tiles even out the end.  The list is laid out so that unit u runs
+// entries u, u + units, ... (empty slots: group -1).
+std::vector<split::Tile> list_schedule(const std::vector<split::Tile>& tiles, const std::vector<double>& cost,
+                                       int units) {
+    std::map<int, double> job_cost;
+    for (size_t i = 0; i < tiles.size(); ++i) job_cost[tiles[i].group] = std::max(job_cost[tiles[i].group], cost[i]);
     std::vector<int> order(tiles.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return job_cost[tiles[a].group] > job_cost[tiles[b].group]; });
     std::vector<std::vector<int>> per(units);
-    std::vector<double> load(units, 0.0);
     typedef std::pair<double, int> LU;
     std::priority_queue<LU, std::vector<LU>, std::greater<LU>> heap;
     for (int u = 0; u < units; ++u) heap.push({0.0, u});
@@ -3359,10 +3365,7 @@ std::vector<split::Tile> lpt_schedule(const std::vector<split::Tile>& tiles, con
         heap.push(top);
     }
     size_t depth = 0;
-    for (auto& v : per) {
-        std::sort(v.begin(), v.end());   // list order inside a unit (L2 reuse of shared operands)
-        depth = std::max(depth, v.size());
-    }
+    for (auto& v : per) depth = std::max(depth, v.size());
     split::Tile empty;
     memset(&empty, 0, sizeof empty);
     empty.group = -1;
@@ -3490,7 +3493,7 @@ gain_status plan_build_groups(gain_plan P) {
     regroup(t2, c2);
     P->real1 = (int)t1.size();
     P->real2 = (int)t2.size();
-    const std::vector<split::Tile> s1 = lpt_schedule(t1, c1, P->units), s2 = lpt_schedule(t2, c2, P->units);
+    const std::vector<split::Tile> s1 = list_schedule(t1, c1, P->units), s2 = list_schedule(t2, c2, P->units);
     P->ntiles1 = (int)s1.size();
     P->ntiles2 = (int)s2.size();
     GAIN_TRY(P->groups1.upload(g1));

@@ -341,10 +341,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)mapA) : "memory");
                     asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)mapB) : "memory");
                 }
-                for (int p = 0; p < g.nprods && ok; ++p) {
-                    const Prod pr = g.prods[p];
+                const Prod* prods = g.prods;
+                const int nprods = g.nprods, nchunks = g.nchunks;
+                for (int p = 0; p < nprods && ok; ++p) {
+                    const Prod pr = prods[p];
                     int lo, hi;
-                    chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
+                    chunk_range(tl.nkb, nchunks, pr.chunk, &lo, &hi);
                     // one stage holds up to KS consecutive k-blocks of the pass
                     for (int kb = lo; kb < hi; kb += KS) {
                         const int nk = hi - kb < KS ? hi - kb : KS;
@@ -402,10 +404,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 const Tile tl = a.tiles[t];
                 if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
                 const GemmArgs& g = group_args<GROUPED>(a, tl);
-                for (int p = 0; p < g.nprods && ok; ++p) {
-                    const Prod pr = g.prods[p];
+                const Prod* prods = g.prods;
+                const int nprods = g.nprods, nchunks = g.nchunks;
+                for (int p = 0; p < nprods && ok; ++p) {
+                    const Prod pr = prods[p];
                     int lo, hi;
-                    chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
+                    chunk_range(tl.nkb, nchunks, pr.chunk, &lo, &hi);
                     if (hi <= lo) continue;
                     const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
                     if (pr.open) {   // a new accumulator: wait until the epilogue drained it
@@ -475,13 +479,20 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         for (int t = unit; t < a.ntiles && ok; t += nunits) {
             const Tile tl = a.tiles[t];
             if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
-            const GemmArgs& g = group_args<GROUPED>(a, tl);
-            const int s = g.slices;
+            const Prod* prods;
+            int nprods, nchunks, beta;
+            {
+                const GemmArgs& g = group_args<GROUPED>(a, tl);
+                prods = g.prods;
+                nprods = g.nprods;
+                nchunks = g.nchunks;
+                beta = g.beta;
+            }
             bool first = true;
-            for (int p = 0; p < g.nprods && ok; ++p) {
-                const Prod pr = g.prods[p];
+            for (int p = 0; p < nprods && ok; ++p) {
+                const Prod pr = prods[p];
                 int lo, hi;
-                chunk_range(tl.nkb, g.nchunks, pr.chunk, &lo, &hi);
+                chunk_range(tl.nkb, nchunks, pr.chunk, &lo, &hi);
                 if (hi <= lo || !pr.close) continue;   // drained once per (fused) group
                 const uint32_t b = acc_cnt & 1, aphase = (acc_cnt >> 1) & 1;
                 if (!mbar_wait(smem_u32(&accfull[b]), aphase, abort_flag, a.err, 5)) {
@@ -489,7 +500,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     break;
                 }
                 tc_fence_after();
-                const int sh = fix_bits(g.beta) - pr.t * g.beta;
+                const int sh = fix_bits(beta) - pr.t * beta;
 #pragma unroll 1
                 for (int c = 0; c < BN / 32; ++c) {
                     uint32_t acc[32], lo_r[32], hi_r[32];
@@ -520,6 +531,13 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 first = false;
             }
             if (!ok) break;
+            // The finalisation reads many of the tile's arguments for every output.  A grouped
+            // launch keeps them in global memory, where any store of an output might alias them
+            // and force them to be read again: there they are copied to registers first.
+            GemmArgs gcopy;
+            if constexpr (GROUPED) gcopy = a.groups[tl.group].args;
+            const GemmArgs& g = GROUPED ? gcopy : a;
+            const int s = g.slices;
             // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags.
             // Row terms live in registers; the statistics of 32 columns at a time are read one
             // column per lane and broadcast with shuffles (no shared memory, no cross-warp sync).

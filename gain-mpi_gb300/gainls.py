@@ -456,7 +456,14 @@ class Engine:
 
     def upload_eigvecs_device(self, jind, gamma, ptr: int, nlevels: int, nsize: int):
         """gain_upload_eigvecs from device memory (ptr: a device address of nlevels x nsize
-        doubles, e.g. a torch tensor's data_ptr())."""
+        doubles, e.g. a torch tensor's data_ptr()).  The engine copies on its own stream, so
+        torch's current stream (which may still be writing the tensor) is synchronised first."""
+        try:
+            import torch
+            if torch.cuda.is_available():
+                torch.cuda.current_stream().synchronize()
+        except ImportError:
+            pass
         check(lib().gain_upload_eigvecs(self.h, jind, gamma, nlevels, nsize, ctypes.cast(ptr, _dp)))
 
     def release_eigvecs(self, jind, gamma):

@@ -166,7 +166,9 @@ gain_status gain_upload_wigner(gain_engine e, int jindI, int jindF, int nlevelsI
 
 /* Eigenvectors of one (J, Gamma) block kept resident (the reference re-uploads one vector
  * per transition, GpuManager::UpdateEigenVector, :537-545): vecs[level*nsize + c].  Host
- * array (pinned memory transfers fastest) or device array, copied synchronously. */
+ * array (pinned memory transfers fastest) or device array, copied synchronously.  The copy
+ * runs on the engine's own stream: a device array must be complete when the call is made
+ * (work still queued on another stream that writes it is not waited for). */
 gain_status gain_upload_eigvecs(gain_engine e, int jind, int gamma, int nlevels, int nsize,
                                 const double* vecs);
 
