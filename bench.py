@@ -787,6 +787,9 @@ def batch_plan(args):
                "transitions_per_s_wall": total / (np.median(gwall) * 1e-3),
                "speedup_vs_one_engine_wall": float(np.median(wall_ms)) / float(np.median(gwall)),
                "gemm1_ms": ps["gemm1_ms"], "gemm2_ms": ps["gemm2_ms"],
+               "stages_ms": {"eigenvector_digits": ps["digits_ms"], "gemm1": ps["gemm1_ms"],
+                             "h_refinement_and_digits": ps["middle_ms"], "gemm2": ps["gemm2_ms"],
+                             "amplitude_refinement": ps["refine_ms"]},
                "grouped_launches": 2, "graph_nodes": ps["graph_nodes"], "kernel_nodes": ps["kernel_launches"],
                "gemm1_tiles": ps["gemm1_tiles"], "gemm2_tiles": ps["gemm2_tiles"], "units": ps["units"],
                "tile": "256x128 (CTA pairs)" if ps["pair"] else "128x128",

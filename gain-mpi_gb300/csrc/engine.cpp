@@ -991,13 +991,14 @@ gain_status load_piece(gain_engine e, int p) {
 
 // Digits of nrows source rows into dig [slices][rows_pad][kpad].  host_map (the host copy of
 // col_map, increasing; NULL for the identity) locates each GEMM chunk's source columns.
-gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows, int nrows, int ncols,
-                  const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
-                  __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
-                  const float* inerr_prev, const int* e_prev, cudaStream_t st, const int* col_inv = nullptr,
-                  int grid_limit = 0, int row0 = 0) {
+split::SliceArgs slice_args(const double* src, long ld, const int* src_rows, int nrows, int ncols,
+                            const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
+                            __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
+                            const float* inerr_prev, const int* e_prev, const int* col_inv = nullptr,
+                            int grid_limit = 0, int row0 = 0) {
     // row0: the output rows start at row row0 of the digit and statistics arrays
     split::SliceArgs a;
+    memset(&a, 0, sizeof a);
     a.grid_limit = grid_limit;
     a.col_inv = col_inv;
     const int nkb = kpad / split::BK;
@@ -1024,6 +1025,16 @@ gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows
     a.st = stv.view(with_inerr, (size_t)row0, p.chunks);
     a.inerr2_prev = inerr_prev ? inerr_prev + row0 : nullptr;
     a.e_prev = e_prev ? e_prev + row0 : nullptr;
+    return a;
+}
+
+gain_status slice(gain_engine e, const double* src, long ld, const int* src_rows, int nrows, int ncols,
+                  const int* col_map, const std::vector<int>* host_map, int kpad, int rows_pad,
+                  __nv_bfloat16* dig, const SplitParams& p, StatsDev& stv, bool with_inerr,
+                  const float* inerr_prev, const int* e_prev, cudaStream_t st, const int* col_inv = nullptr,
+                  int grid_limit = 0, int row0 = 0) {
+    const split::SliceArgs a = slice_args(src, ld, src_rows, nrows, ncols, col_map, host_map, kpad, rows_pad, dig, p,
+                                          stv, with_inerr, inerr_prev, e_prev, col_inv, grid_limit, row0);
     GAIN_CUDA(split::launch_slice(a, st));
     ++e->launches;
     return GAIN_OK;
@@ -3187,6 +3198,14 @@ struct gain_plan_s {
     int ntiles1 = 0, ntiles2 = 0, real1 = 0, real2 = 0;
     int s1max = 1, c1max = 1, s2max = 1, c2max = 1;
     double flops = 0.0;
+    // the plan's digit slicings, one launch per slicing kernel: the eigenvectors (before the
+    // first GEMM) and H (before the second)
+    struct SliceBatch {
+        int kernel = 0, n = 0, rows = 0;
+        DevArray<split::SliceArgs> args;
+        DevArray<int> offs;
+    };
+    std::vector<SliceBatch> slices1, slices3;
     DevArray<unsigned int> counters;        // [2 * njobs]: GEMM1 / GEMM2 refinement counts
     DevArray<unsigned long long> ull;       // [4 * njobs]: uncertified, -, amp max, uncertified weak
     DevArray<int> err;
@@ -3375,6 +3394,77 @@ std::vector<split::Tile> list_schedule(const std::vector<split::Tile>& tiles, co
     return out;
 }
 
+// The slicings `all` grouped by kernel into batches of one launch each (device memory).
+gain_status plan_slice_batches(const std::vector<split::SliceArgs>& all, std::vector<gain_plan_s::SliceBatch>& out) {
+    out.clear();
+    std::map<int, std::vector<split::SliceArgs>> by;
+    for (const auto& a : all)
+        if (a.nrows > 0) by[split::slice_kernel_of(a)].push_back(a);
+    for (auto& kv : by) {
+        gain_plan_s::SliceBatch b;
+        b.kernel = kv.first;
+        b.n = (int)kv.second.size();
+        std::vector<int> offs(b.n + 1, 0);
+        for (int g = 0; g < b.n; ++g) offs[g + 1] = offs[g] + kv.second[g].nrows;
+        b.rows = offs[b.n];
+        GAIN_TRY(b.args.upload(kv.second));
+        GAIN_TRY(b.offs.upload(offs));
+        out.push_back(std::move(b));
+    }
+    return GAIN_OK;
+}
+
+// Every job's slicings: its lower vectors and (for the owner of an upper block's digits) its
+// upper vectors before the first GEMM, its H before the second.  Each produces exactly what
+// the single-pair run's slicing of the same rows does.
+gain_status plan_build_slices(gain_plan P) {
+    gain_engine e = P->e;
+    std::vector<split::SliceArgs> s1, s3;
+    for (auto& Jp : P->jobs) {
+        PlanJob& J = *Jp;
+        PairLayout& L = *J.L;
+        const gain_pair_job* j = &J.job;
+        const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+        const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
+        const Basis& bI = e->bases[j->jindI];
+        if (L.general) {
+            s1.push_back(slice_args(J.primI.p, bI.dimen, nullptr, J.B, bI.dimen, nullptr, nullptr, L.kpadI, J.Bpad,
+                                    J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr, L.d_i_sym.p));
+            if (J.uowner < 0)
+                s1.push_back(slice_args(EF.d.p, EF.nsize, J.d_upper.p, J.Nu, L.nsymF, nullptr, nullptr, J.K2, J.Nupad,
+                                        J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr));
+        } else {
+            s1.push_back(slice_args(EI.d.p, EI.nsize, J.d_lower.p, J.B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI,
+                                    J.Bpad, J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr, L.d_i_sym.p));
+            if (J.uowner < 0)
+                s1.push_back(slice_args(EF.d.p, EF.nsize, J.d_upper.p, J.Nu, EF.nsize, L.d_colposF.p, &L.colposF,
+                                        L.fpad, J.Nupad, J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr,
+                                        L.d_f_sym.p));
+        }
+        s3.push_back(slice_args(L.general ? J.Hsym.p : J.H.p, J.K2, nullptr, J.B, L.general ? L.nsymF : L.fpad,
+                                nullptr, nullptr, J.K2, J.Bpad, J.Hdig.p, J.p2, J.Hst, true, J.rowerr.p,
+                                J.Vst.e.p));
+    }
+    GAIN_TRY(plan_slice_batches(s1, P->slices1));
+    GAIN_TRY(plan_slice_batches(s3, P->slices3));
+    return GAIN_OK;
+}
+
+// Batch k on stream streams[k % nstreams] (independent outputs: the batches may overlap).
+gain_status plan_launch_slices(const std::vector<gain_plan_s::SliceBatch>& batches, const cudaStream_t* streams,
+                               int nstreams) {
+    for (size_t k = 0; k < batches.size(); ++k) {
+        const auto& b = batches[k];
+        split::SliceGroups g;
+        g.args = b.args.p;
+        g.offs = b.offs.p;
+        g.n = b.n;
+        g.rows = b.rows;
+        GAIN_CUDA(split::launch_slice_grouped(g, b.kernel, streams[k % nstreams]));
+    }
+    return GAIN_OK;
+}
+
 // Groups and schedules of both grouped launches.
 gain_status plan_build_groups(gain_plan P) {
     gain_engine e = P->e;
@@ -3525,35 +3615,29 @@ gain_status plan_enqueue(gain_plan P) {
     GAIN_CUDA(cudaMemsetAsync(P->ull.p, 0, sizeof(unsigned long long) * 4 * nj, st));
     GAIN_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
     GAIN_CUDA(cudaEventRecordWithFlags(P->ev[0], st, cudaEventRecordExternal));
-    // ---- stage 1: digits of the lower and the upper eigenvectors, every job
+    // ---- stage 1: expansions of mixing lower vectors (per job, on the branches), then the
+    // digits of every job's lower and upper eigenvectors (one launch per slicing kernel)
     GAIN_TRY(fork());
     for (int q = 0; q < nj; ++q) {
         PlanJob& J = *P->jobs[q];
         PairLayout& L = *J.L;
         const gain_pair_job* j = &J.job;
         cudaStream_t sq = stream_of(q);
-        const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
-        const Eig& EF = *e->eig[{j->jindF, j->gammaF}];
-        const Basis& bI = e->bases[j->jindI];
         if (L.general) {
+            const Eig& EI = *e->eig[{j->jindI, j->gammaI}];
+            const Basis& bI = e->bases[j->jindI];
             Inflation& iI = e->infl[j->jindI];
             GAIN_CUDA(launch_expand_levels(iI.dimen, j->gammaI, iI.maxcoeff, 0, iI.sdeg[j->gammaI], iI.Ntot[j->gammaI],
                                            iI.dijterms.p, iI.dicontr.p, iI.dN[j->gammaI]->p, iI.drepres[j->gammaI]->p,
                                            EI.d.p, EI.nsize, J.d_lower.p, J.primI.p, bI.dimen, J.B, sq));
-            GAIN_TRY(slice(e, J.primI.p, bI.dimen, nullptr, J.B, bI.dimen, nullptr, nullptr, L.kpadI, J.Bpad, J.Vdig.p,
-                           J.p1, J.Vst, false, nullptr, nullptr, sq, L.d_i_sym.p));
-            if (J.uowner < 0)
-                GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, L.nsymF, nullptr, nullptr, J.K2, J.Nupad,
-                               J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr, sq, nullptr));
-        } else {
-            GAIN_TRY(slice(e, EI.d.p, EI.nsize, J.d_lower.p, J.B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI,
-                           J.Bpad, J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr, sq, L.d_i_sym.p));
-            if (J.uowner < 0)
-                GAIN_TRY(slice(e, EF.d.p, EF.nsize, J.d_upper.p, J.Nu, EF.nsize, L.d_colposF.p, &L.colposF, L.fpad,
-                               J.Nupad, J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr, sq, L.d_f_sym.p));
         }
         GAIN_CUDA(cudaMemsetAsync(J.rowerr.p, 0, sizeof(float) * J.Bpad, sq));
     }
+    GAIN_TRY(join());
+    cudaStream_t streams[kPlanStreams];
+    for (int k = 0; k < kPlanStreams; ++k) streams[k] = stream_of(k);
+    GAIN_TRY(fork());
+    GAIN_TRY(plan_launch_slices(P->slices1, streams, kPlanStreams));
     GAIN_TRY(join());
     // ---- stage 2: the first GEMM of every job, one grouped launch
     split::GemmArgs ga;
@@ -3591,16 +3675,15 @@ gain_status plan_enqueue(gain_plan P) {
         rh.eA = J.Vst.e.p;
         rh.rowerr2 = J.rowerr.p;
         GAIN_CUDA(split::launch_refine_h(rh, std::min(2 * e->num_sms, std::max(1, J.cap1 / 8)), sq));
-        const double* Hs = J.H.p;
         if (L.general) {
             GAIN_CUDA(launch_contract_rowerr(J.B, J.H.p, L.fpad, L.fpad, J.rowerr.p, J.Vst.e.p, L.sigmaF, L.gamF, sq));
             GAIN_CUDA(launch_contract(L.nsymF, L.d_cF_ptr.p, L.d_cF_col.p, L.d_cF_val.p, J.H.p, L.fpad, J.Hsym.p, J.K2,
                                       J.B, sq));
-            Hs = J.Hsym.p;
         }
-        GAIN_TRY(slice(e, Hs, J.K2, nullptr, J.B, L.general ? L.nsymF : L.fpad, nullptr, nullptr, J.K2, J.Bpad,
-                       J.Hdig.p, J.p2, J.Hst, true, J.rowerr.p, J.Vst.e.p, sq));
     }
+    GAIN_TRY(join());
+    GAIN_TRY(fork());
+    GAIN_TRY(plan_launch_slices(P->slices3, streams, kPlanStreams));   // every job's H digits
     GAIN_TRY(join());
     // ---- stage 4: the second GEMM of every job, one grouped launch
     ga.groups = P->groups2.p;
@@ -3659,6 +3742,7 @@ gain_status plan_build(gain_plan P) {
     GAIN_TRY(P->ull.alloc(4 * nj));
     GAIN_TRY(P->err.alloc(1));
     GAIN_TRY(plan_build_groups(P));
+    GAIN_TRY(plan_build_slices(P));
     if (!P->rb) GAIN_CUDA(cudaMallocHost(&P->rb, 40 * (size_t)nj + 64));
     GAIN_CUDA(split::prepare_device());   // kernel attributes are set outside the capture
     GAIN_CUDA(cudaStreamSynchronize(e->st));
@@ -3926,6 +4010,13 @@ gain_status gain_plan_run(gain_plan P, gain_stats* job_stats, gain_plan_stats* s
         cudaEventElapsedTime(&g2, P->ev[3], P->ev[4]);
         stats->gemm1_ms = g1;
         stats->gemm2_ms = g2;
+        float d1 = 0.f, d3 = 0.f, d5 = 0.f;
+        cudaEventElapsedTime(&d1, P->ev[0], P->ev[1]);
+        cudaEventElapsedTime(&d3, P->ev[2], P->ev[3]);
+        cudaEventElapsedTime(&d5, P->ev[4], P->ev[5]);
+        stats->digits_ms = d1;
+        stats->middle_ms = d3;
+        stats->refine_ms = d5;
         stats->jobs = nj;
         for (int q = 0; q < nj && q < (int)P->job_stats.size(); ++q) {
             stats->transitions += P->job_stats[q].rows * P->job_stats[q].cols;

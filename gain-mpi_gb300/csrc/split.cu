@@ -697,25 +697,51 @@ __device__ __forceinline__ unsigned long long rne_shr(unsigned long long m, int 
     return (rem > half || (rem == half && (q & 1ull))) ? q + 1ull : q;
 }
 
-constexpr int SLICE_THREADS = 256;
+// Rows of at most kShortRow destination columns are sliced by 128 threads (flag
+// kShortRowKernel in the kernel code), longer ones by 256.
+constexpr int kShortRow = 4096;
+constexpr int kShortRowKernel = 16;
 
-__global__ void __launch_bounds__(SLICE_THREADS)
-k_slice(const SliceArgs a) {
+// The slicing of output row `flat` of a grouped launch: the block copies that slicing's
+// arguments to shared memory (in global memory any digit store might alias them, and copies
+// in registers would cost the kernel half its resident blocks) and returns the row within it.
+// The caller's previous row has passed its closing barrier.
+__device__ __forceinline__ int slice_group_row(const SliceGroups& gs, int flat, SliceArgs* sa) {
+    int lo = 0, hi = gs.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (gs.offs[mid] <= flat) lo = mid;
+        else hi = mid - 1;
+    }
+    static_assert(sizeof(SliceArgs) % 4 == 0, "word copy");
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(gs.args + lo);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(sa);
+    for (int w = threadIdx.x; w < (int)(sizeof(SliceArgs) / 4); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    return flat - gs.offs[lo];
+}
+
+template <bool G, int NT>
+__device__ __forceinline__ void slice_rows(const SliceArgs& a0, const SliceGroups& gs) {
     const int tid = threadIdx.x;
     // one row per iteration; the grid may be smaller than the row count (a capped grid
     // leaves room on every SM for a concurrent kernel)
-    for (int row = blockIdx.x; row < a.nrows; row += gridDim.x) {
+    __shared__ SliceArgs sa;   // grouped launch: the current row's slicing
+    const int nflat = G ? gs.rows : a0.nrows;
+    for (int flat = blockIdx.x; flat < nflat; flat += gridDim.x) {
+        const int row = G ? slice_group_row(gs, flat, &sa) : flat;
+        const SliceArgs& a = G ? sa : a0;
         const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
         const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
-        __shared__ unsigned long long red_u[SLICE_THREADS / 32];
-        __shared__ float red_f[SLICE_THREADS / 32];
-        __shared__ int red_i[SLICE_THREADS / 32];
-        __shared__ float red_t[SLICE_THREADS / 32][MAX_SLICES];
-        __shared__ unsigned int red_d[SLICE_THREADS / 32][MAX_SLICES * MAX_CHUNKS];
+        __shared__ unsigned long long red_u[NT / 32];
+        __shared__ float red_f[NT / 32];
+        __shared__ int red_i[NT / 32];
+        __shared__ float red_t[NT / 32][MAX_SLICES];
+        __shared__ unsigned int red_d[NT / 32][MAX_SLICES * MAX_CHUNKS];
 
         // pass 1: max |x| through the IEEE bit pattern (integer compares only)
         unsigned long long mx = 0;
-        for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+        for (int c = tid; c < a.ncols; c += NT) {
             const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
             mx = b > mx ? b : mx;
         }
@@ -726,7 +752,7 @@ k_slice(const SliceArgs a) {
         if ((tid & 31) == 0) red_u[tid >> 5] = mx;
         __syncthreads();
         mx = 0;
-        for (int w = 0; w < SLICE_THREADS / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
+        for (int w = 0; w < NT / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
         if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
         const int Emax = (int)(mx >> 52);
         const bool zero_row = (mx == 0);
@@ -750,7 +776,7 @@ k_slice(const SliceArgs a) {
     #pragma unroll
         for (int i = 0; i < MAX_SLICES; ++i) dsq[i] = 0u;
         const int cend = a.src_chunk[ch + 1];
-        for (int c = a.src_chunk[ch] + tid; c < cend; c += SLICE_THREADS) {
+        for (int c = a.src_chunk[ch] + tid; c < cend; c += NT) {
             const unsigned long long bits = src[c];
             const int dc = a.col_map ? a.col_map[c] : c;
             const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
@@ -827,7 +853,7 @@ k_slice(const SliceArgs a) {
         if (tid == 0) {
             float L2 = 0.0f;
             int N = 0;
-            for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
+            for (int w = 0; w < NT / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
             // rounding of x^ to q fractional bits: |delta| <= 2^{-q-1} per non-zero entry
             const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
             const float slack = 1.0f + 1.0e-6f;   // FP32 evaluation of the tails and sums
@@ -838,7 +864,7 @@ k_slice(const SliceArgs a) {
                 float tq = 0.0f;
                 unsigned long long dd = 0;
                 if (i < s) {
-                    for (int w = 0; w < SLICE_THREADS / 32; ++w) {
+                    for (int w = 0; w < NT / 32; ++w) {
                         tq = __fadd_ru(tq, red_t[w][i]);
                         for (int c = 0; c < a.nchunks; ++c) dd += red_d[w][i * MAX_CHUNKS + c];
                     }
@@ -851,7 +877,7 @@ k_slice(const SliceArgs a) {
                 unsigned long long m = 0;
                 for (int i = 0; i < s; ++i) {
                     unsigned long long t = 0;
-                    for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
+                    for (int w = 0; w < NT / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
                     m = t > m ? t : m;
                 }
                 a.st.dn[(long)row * a.nchunks + c] = __fsqrt_ru(__ull2float_ru(m));
@@ -880,36 +906,39 @@ k_slice(const SliceArgs a) {
 // the sum of the lower digit weights, each shifted down by 2^(beta-1) - 1; the top digit is
 // u >> beta (S - 1).  Every digit has at most 8 significant bits (|d| <= 2^beta <= 256), so its
 // float is exact in BF16 and the BF16 bits are the float's upper half.
-template <int S>
-__global__ void __launch_bounds__(SLICE_THREADS)
-k_slice4(const SliceArgs a) {
+template <int S, bool G, int NT>
+__device__ __forceinline__ void slice4_rows(const SliceArgs& a0, const SliceGroups& gs) {
     const int tid = threadIdx.x;
-    const int nkb = a.kpad / BK;
-    __shared__ unsigned long long red_u[SLICE_THREADS / 32];
-    __shared__ float red_f[SLICE_THREADS / 32];
-    __shared__ int red_i[SLICE_THREADS / 32];
-    __shared__ float red_t[SLICE_THREADS / 32][S];
-    __shared__ unsigned int red_d[SLICE_THREADS / 32][S * MAX_CHUNKS];
+    __shared__ unsigned long long red_u[NT / 32];
+    __shared__ float red_f[NT / 32];
+    __shared__ int red_i[NT / 32];
+    __shared__ float red_t[NT / 32][S];
+    __shared__ unsigned int red_d[NT / 32][S * MAX_CHUNKS];
     __shared__ unsigned long long dsum[S * MAX_CHUNKS];   // per (slice, chunk): sum over the row
-    const int beta = a.beta;
-    const int q = S * beta;
-    const long long mask = (1ll << beta) - 1ll;
-    const int off = (1 << (beta - 1)) - 1;
-    long long C = 0;
+    __shared__ SliceArgs sa;   // grouped launch: the current row's slicing
+    const int nflat = G ? gs.rows : a0.nrows;
+    for (int flat = blockIdx.x; flat < nflat; flat += gridDim.x) {
+        const int row = G ? slice_group_row(gs, flat, &sa) : flat;
+        const SliceArgs& a = G ? sa : a0;
+        const int nkb = a.kpad / BK;
+        const int beta = a.beta;
+        const int q = S * beta;
+        const long long mask = (1ll << beta) - 1ll;
+        const int off = (1 << (beta - 1)) - 1;
+        long long C = 0;
 #pragma unroll
-    for (int k = 0; k < S - 1; ++k) C += (long long)off << (beta * k);
-    const float inv2q = pow2f(-q);
-    float w2[S];   // 2^{-(i+1) beta}
+        for (int k = 0; k < S - 1; ++k) C += (long long)off << (beta * k);
+        const float inv2q = pow2f(-q);
+        float w2[S];   // 2^{-(i+1) beta}
 #pragma unroll
-    for (int i = 0; i < S; ++i) w2[i] = pow2f(-(i + 1) * beta);
-    for (int row = blockIdx.x; row < a.nrows; row += gridDim.x) {
+        for (int i = 0; i < S; ++i) w2[i] = pow2f(-(i + 1) * beta);
         const long srow = a.src_rows ? (long)a.src_rows[row] : (long)row;
         const unsigned long long* src = (const unsigned long long*)(a.src + srow * a.ld_src);
 
         // pass 1: max |x| through the IEEE bit pattern (integer compares only)
         unsigned long long mx = 0;
 #pragma unroll 4
-        for (int c = tid; c < a.ncols; c += SLICE_THREADS) {
+        for (int c = tid; c < a.ncols; c += NT) {
             const unsigned long long b = src[c] & 0x7FFFFFFFFFFFFFFFull;
             mx = b > mx ? b : mx;
         }
@@ -920,7 +949,7 @@ k_slice4(const SliceArgs a) {
         if ((tid & 31) == 0) red_u[tid >> 5] = mx;
         __syncthreads();
         mx = 0;
-        for (int w = 0; w < SLICE_THREADS / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
+        for (int w = 0; w < NT / 32; ++w) mx = red_u[w] > mx ? red_u[w] : mx;
         if (mx >= 0x7FF0000000000000ull) mx = 0x7FEFFFFFFFFFFFFFull;   // non-finite input: clamp scale
         const int Emax = (int)(mx >> 52);
         const bool zero_row = (mx == 0);
@@ -939,7 +968,7 @@ k_slice4(const SliceArgs a) {
             for (int i = 0; i < S; ++i) dsq[i] = 0u;
             const int d0 = (int)(((long)ch * nkb) / a.nchunks) * BK;
             const int d1 = (int)(((long)(ch + 1) * nkb) / a.nchunks) * BK;
-            for (int dc = d0 + 4 * tid; dc < d1; dc += 4 * SLICE_THREADS) {
+            for (int dc = d0 + 4 * tid; dc < d1; dc += 4 * NT) {
                 uint32_t pk[S][2];
                 uint32_t even[S];
 #pragma unroll
@@ -1016,7 +1045,7 @@ k_slice4(const SliceArgs a) {
         if (tid < S * a.nchunks) {
             const int i = tid / a.nchunks, c = tid - i * a.nchunks;
             unsigned long long t = 0;
-            for (int w = 0; w < SLICE_THREADS / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
+            for (int w = 0; w < NT / 32; ++w) t += red_d[w][i * MAX_CHUNKS + c];
             dsum[i * MAX_CHUNKS + c] = t;
         }
         __syncthreads();
@@ -1025,12 +1054,12 @@ k_slice4(const SliceArgs a) {
         if (tid < MAX_SLICES) {   // one slice per thread; tq in warp order as before
             const int i = tid;
             int N = 0;
-            for (int w = 0; w < SLICE_THREADS / 32; ++w) N += red_i[w];
+            for (int w = 0; w < NT / 32; ++w) N += red_i[w];
             const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
             float tq = 0.0f;
             unsigned long long dd = 0;
             if (i < S) {
-                for (int w = 0; w < SLICE_THREADS / 32; ++w) tq = __fadd_ru(tq, red_t[w][i]);
+                for (int w = 0; w < NT / 32; ++w) tq = __fadd_ru(tq, red_t[w][i]);
                 for (int c = 0; c < a.nchunks; ++c) dd += dsum[i * MAX_CHUNKS + c];
             }
             a.st.dnv[(long)row * MAX_SLICES + i] = i < S ? __fsqrt_ru(__ull2float_ru(dd)) : 0.0f;
@@ -1043,7 +1072,7 @@ k_slice4(const SliceArgs a) {
         } else if (tid == 64) {
             float L2 = 0.0f;
             int N = 0;
-            for (int w = 0; w < SLICE_THREADS / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
+            for (int w = 0; w < NT / 32; ++w) { L2 = __fadd_ru(L2, red_f[w]); N += red_i[w]; }
             const float dq = __fmul_ru(__fsqrt_ru((float)N), pow2f(-q - 1));
             a.st.e[row] = e;
             a.st.nnz[row] = N;
@@ -1060,6 +1089,24 @@ k_slice4(const SliceArgs a) {
         }
         __syncthreads();   // the shared reduction buffers are reused by the next row
     }
+}
+
+// The slicing kernels: one slicing (its arguments in the parameter space), or a grouped
+// launch of several, capped at 64 registers so that it keeps four resident blocks per SM (a
+// row's work is short and latency-bound).  NT threads per row: 256, or 128 for rows of at
+// most kShortRow destination columns (twice the rows in flight for the same threads).  The
+// single and the grouped form pick NT the same way, so both produce the same statistics.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_slice(const SliceArgs a) { slice_rows<false, NT>(a, SliceGroups{}); }
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_slice_grouped(const SliceGroups gs) {
+    slice_rows<true, NT>(SliceArgs{}, gs);
+}
+template <int S, int NT>
+__global__ void __launch_bounds__(NT) k_slice4(const SliceArgs a) { slice4_rows<S, false, NT>(a, SliceGroups{}); }
+template <int S, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_slice4_grouped(const SliceGroups gs) {
+    slice4_rows<S, true, NT>(SliceArgs{}, gs);
 }
 
 // ------------------------------------------------------------------- band builder
@@ -1245,11 +1292,17 @@ static cudaError_t set_attributes_once() {
             e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     }
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_slice, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_slice4<6>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_slice4<7>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_slice4<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    const void* slicers[] = {
+        (const void*)k_slice<256>,             (const void*)k_slice<128>,
+        (const void*)k_slice_grouped<256>,     (const void*)k_slice_grouped<128>,
+        (const void*)k_slice4<6, 256>,         (const void*)k_slice4<6, 128>,
+        (const void*)k_slice4<7, 256>,         (const void*)k_slice4<7, 128>,
+        (const void*)k_slice4<8, 256>,         (const void*)k_slice4<8, 128>,
+        (const void*)k_slice4_grouped<6, 256>, (const void*)k_slice4_grouped<6, 128>,
+        (const void*)k_slice4_grouped<7, 256>, (const void*)k_slice4_grouped<7, 128>,
+        (const void*)k_slice4_grouped<8, 256>, (const void*)k_slice4_grouped<8, 128>};
+    for (const void* f : slicers)
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     done.fetch_or(bit);
     return cudaSuccess;
@@ -1346,12 +1399,51 @@ cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st) {
     cudaError_t e = set_attributes_once();
     if (e != cudaSuccess) return e;
     const int grid = (a.grid_limit > 0 && a.grid_limit < a.nrows) ? a.grid_limit : a.nrows;
+    const int k = slice_kernel_of(a);
+    if (k & kShortRowKernel) {
+        switch (k & 15) {
+            case 6: k_slice4<6, 128><<<grid, 128, 0, st>>>(a); break;
+            case 7: k_slice4<7, 128><<<grid, 128, 0, st>>>(a); break;
+            case 8: k_slice4<8, 128><<<grid, 128, 0, st>>>(a); break;
+            default: k_slice<128><<<grid, 128, 0, st>>>(a); break;
+        }
+    } else {
+        switch (k) {
+            case 6: k_slice4<6, 256><<<grid, 256, 0, st>>>(a); break;
+            case 7: k_slice4<7, 256><<<grid, 256, 0, st>>>(a); break;
+            case 8: k_slice4<8, 256><<<grid, 256, 0, st>>>(a); break;
+            default: k_slice<256><<<grid, 256, 0, st>>>(a); break;
+        }
+    }
+    return cudaGetLastError();
+}
+
+int slice_kernel_of(const SliceArgs& a) {
     // the four-column kernel needs the destination map (or the identity) and whole k-blocks
     const bool four = (a.col_inv || !a.col_map) && (a.kpad % BK) == 0;
-    if (four && a.slices == 6) k_slice4<6><<<grid, SLICE_THREADS, 0, st>>>(a);
-    else if (four && a.slices == 7) k_slice4<7><<<grid, SLICE_THREADS, 0, st>>>(a);
-    else if (four && a.slices == 8) k_slice4<8><<<grid, SLICE_THREADS, 0, st>>>(a);
-    else k_slice<<<grid, SLICE_THREADS, 0, st>>>(a);
+    const int k = four && a.slices >= 6 && a.slices <= 8 ? a.slices : 0;
+    return a.kpad <= kShortRow ? (k | kShortRowKernel) : k;
+}
+
+cudaError_t launch_slice_grouped(const SliceGroups& g, int kernel, cudaStream_t st) {
+    if (g.rows <= 0 || g.n <= 0) return cudaSuccess;
+    cudaError_t e = set_attributes_once();
+    if (e != cudaSuccess) return e;
+    if (kernel & kShortRowKernel) {
+        switch (kernel & 15) {
+            case 6: k_slice4_grouped<6, 128><<<g.rows, 128, 0, st>>>(g); break;
+            case 7: k_slice4_grouped<7, 128><<<g.rows, 128, 0, st>>>(g); break;
+            case 8: k_slice4_grouped<8, 128><<<g.rows, 128, 0, st>>>(g); break;
+            default: k_slice_grouped<128><<<g.rows, 128, 0, st>>>(g); break;
+        }
+    } else {
+        switch (kernel) {
+            case 6: k_slice4_grouped<6, 256><<<g.rows, 256, 0, st>>>(g); break;
+            case 7: k_slice4_grouped<7, 256><<<g.rows, 256, 0, st>>>(g); break;
+            case 8: k_slice4_grouped<8, 256><<<g.rows, 256, 0, st>>>(g); break;
+            default: k_slice_grouped<256><<<g.rows, 256, 0, st>>>(g); break;
+        }
+    }
     return cudaGetLastError();
 }
 

@@ -154,6 +154,16 @@ struct SliceArgs {
     int grid_limit;            // CTAs at most (0: one per row)
 };
 cudaError_t launch_slice(const SliceArgs& a, cudaStream_t st);
+// Several slicings in one launch: args[g] (device memory) produces the rows
+// offs[g] <= r < offs[g + 1] of the flat row range [0, rows); all use the same kernel.
+struct SliceGroups {
+    const SliceArgs* args;
+    const int* offs;
+    int n, rows;
+};
+// The kernel a slicing runs on: S for the four-column kernel of S slices, 0 for the general one.
+int slice_kernel_of(const SliceArgs& a);
+cudaError_t launch_slice_grouped(const SliceGroups& g, int kernel, cudaStream_t st);
 
 // Rotational-dipole band matrix of one block pair (rows: padded upper functions,
 // columns: W band positions starting at band_k0[row] of the padded lower layout).

@@ -340,6 +340,9 @@ typedef struct gain_plan_stats {
     double tensor_flops;         /* BF16 MMA flops of the two grouped launches (whole tiles) */
     int beta2[4], slices2[4];    /* second-GEMM digits per size class of its inner dimension K:
                                     K <= 2048, <= 8192, <= 16384, above (0: class absent) */
+    double digits_ms;            /* before the first GEMM: expansions and eigenvector digits */
+    double middle_ms;            /* between the GEMMs: refinement of H, contraction, H digits */
+    double refine_ms;            /* after the second GEMM: refinement of the amplitudes */
 } gain_plan_stats;
 
 gain_status gain_plan_create(gain_engine e, const gain_pair_job* jobs, int n_jobs, const gain_split_opts* opts,
