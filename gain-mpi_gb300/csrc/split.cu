@@ -17,6 +17,10 @@ constexpr uint32_t BOX_B = BN * BK * 2;     // bytes of one B k-block box (16 KB
 constexpr uint32_t STAGE_A = KSTEP * BOX_A; // bytes per A stage
 constexpr uint32_t STAGE_B = KSTEP * BOX_B; // bytes per B stage
 constexpr int NTHREADS = 192;               // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+// shared memory of the GEMM after its stage ring (the larger, the pair's) and the barriers:
+// the current tile's column statistics, five floats per column
+constexpr uint32_t COLSTAT_OFF = STAGES * 3 * (BOX_A + BOX_B / 2) + 256;
+constexpr uint32_t COLSTAT_BYTES = 5 * BN * 4;
 constexpr uint32_t TMEM_COLS = 512;         // acc0 [0,128) acc1 [128,256) hi [256,384) lo [384,512)
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s per wait before giving up
 
@@ -251,6 +255,9 @@ __device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, in
     *hi = (int)(((long)(c + 1) * nkb) / nch);
 }
 
+// Barrier of the four epilogue warps (named barrier 1, 128 threads).
+__device__ __forceinline__ void epilogue_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
 // The arguments of a tile: the launch's own, or (grouped launch) those of the tile's group.
 template <bool G>
 __device__ __forceinline__ const GemmArgs& group_args(const GemmArgs& a, const Tile& tl) {
@@ -275,7 +282,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     constexpr uint32_t BOXB = PAIR ? BOX_B / 2 : BOX_B;
     constexpr uint32_t STA = KS * BOX_A;
     constexpr uint32_t STB = KS * BOXB;
-    static_assert(NST * (STA + STB) + 1024 + 256 <= 227 * 1024, "stage ring");
+    static_assert(NST * (STA + STB) + 256 <= COLSTAT_OFF, "stage ring");
+    static_assert(COLSTAT_OFF + COLSTAT_BYTES + 1024 <= 227 * 1024, "shared memory");
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
@@ -288,6 +296,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     uint64_t* drain = bars + 2 * NST + 4;
     uint32_t* tmem_holder = (uint32_t*)(bars + 2 * NST + 5);
     volatile int* abort_flag = (volatile int*)(tmem_holder + 1);
+    // column statistics of the epilogue's current tile: e (as int bits), ||y^||, rho, sB, max_c ||d_c(y)||
+    float* s_col = (float*)(smem + COLSTAT_OFF);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t rank = PAIR ? cluster_rank() : 0u;
@@ -487,6 +497,27 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 nprods = g.nprods;
                 nchunks = g.nchunks;
                 beta = g.beta;
+                // The tile's column statistics, one column per epilogue thread, into shared
+                // memory (computed while the tile's first products run; the finalisation reads
+                // them as broadcasts).  The barrier keeps the previous tile's finalisation
+                // from reading values of this one.
+                epilogue_sync();
+                const int ncol = tl.n0 + row_in_tile;
+                const int sl = g.slices;
+                const float* dvB = g.B.dnv + (long)ncol * MAX_SLICES;
+                const float* rvB = g.B.rnv + (long)ncol * MAX_SLICES;
+                float crho = 0.0f, csB = 0.0f, cdnmax = 0.0f;
+                for (int k = 0; k < sl; ++k) {
+                    crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * beta)));
+                    csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * beta), __ldg(&dvB[k])));
+                }
+                for (int cc = 0; cc < nchunks; ++cc)
+                    cdnmax = fmaxf(cdnmax, __ldg(&g.B.dn[(long)ncol * nchunks + cc]));
+                s_col[0 * BN + row_in_tile] = __int_as_float(__ldg(&g.B.e[ncol]));
+                s_col[1 * BN + row_in_tile] = __ldg(&g.B.l2[ncol]);   // 0 exactly for an all-zero column
+                s_col[2 * BN + row_in_tile] = crho;
+                s_col[3 * BN + row_in_tile] = csB;
+                s_col[4 * BN + row_in_tile] = cdnmax;
             }
             bool first = true;
             for (int p = 0; p < nprods && ok; ++p) {
@@ -539,8 +570,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             const GemmArgs& g = GROUPED ? gcopy : a;
             const int s = g.slices;
             // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags.
-            // Row terms live in registers; the statistics of 32 columns at a time are read one
-            // column per lane and broadcast with shuffles (no shared memory, no cross-warp sync).
+            // Row terms live in registers; the column statistics come from shared memory.
+            epilogue_sync();   // every column's statistics are in place
             const int r = tl.m0 + (int)rank * BM + row_in_tile;
             const bool rvalid = r < g.rows_valid;
             // products summed in one accumulator: every partial sum of up to `fuse` exact
@@ -575,23 +606,15 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             float rowerr2 = 0.0f;
             unsigned long long vmax = 0ull;
             double* orow = g.out + (long)r * g.ldo;
+            float* brow = g.bnd ? g.bnd + (long)r * g.ldb : nullptr;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
-                // this lane's column of the group of 32: its five summary values
-                const int mycol = tl.n0 + c * 32 + lane;
-                const int ceB = __ldg(&g.B.e[mycol]);
-                const float cl2 = __ldg(&g.B.l2[mycol]);   // 0 exactly for an all-zero column
-                const float* dvB = g.B.dnv + (long)mycol * MAX_SLICES;
-                const float* rvB = g.B.rnv + (long)mycol * MAX_SLICES;
-                float crho = 0.0f, csB = 0.0f, cdnmax = 0.0f;
-                for (int k = 0; k < s; ++k) {
-                    crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * g.beta)));
-                    csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * g.beta), __ldg(&dvB[k])));
-                }
-                for (int cc = 0; cc < g.nchunks; ++cc)
-                    cdnmax = fmaxf(cdnmax, __ldg(&g.B.dn[(long)mycol * g.nchunks + cc]));
 #pragma unroll 1
                 for (int h = 0; h < 2; ++h) {
+                    // this thread's 16 outputs leave as eight 16-byte stores (and four for the
+                    // bounds) instead of sixteen 8-byte ones
+                    unsigned long long vout[16];
+                    float bout[16];
                     uint32_t lo_r[16], hi_r[16];
                     if (!first) {
                         tmem_ld16(tmem + lane_off + 256 + c * 32 + h * 16, lo_r);
@@ -603,21 +626,19 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                     }
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int src = h * 16 + j;   // lane holding this column's values
-                        const int col = tl.n0 + c * 32 + src;
+                        const int cl = c * 32 + h * 16 + j;   // the column within the tile
+                        const int col = tl.n0 + cl;
                         const long long run = (long long)(((unsigned long long)hi_r[j] << 32) | lo_r[j]);
-                        const int eB = __shfl_sync(0xffffffffu, ceB, src);
-                        const float l2B = __shfl_sync(0xffffffffu, cl2, src);
-                        const float rhoB = __shfl_sync(0xffffffffu, crho, src);
-                        const float sB = __shfl_sync(0xffffffffu, csB, src);
-                        const float dnBmax = __shfl_sync(0xffffffffu, cdnmax, src);
+                        const int eB = __float_as_int(s_col[0 * BN + cl]);
+                        const float l2B = s_col[1 * BN + cl];
+                        const float rhoB = s_col[2 * BN + cl];
+                        const float sB = s_col[3 * BN + cl];
+                        const float dnBmax = s_col[4 * BN + cl];
                         float av;
                         const unsigned long long vbits = scaled_bits(run, eA + eB - kFixTotal, &av);
-                        orow[col] = __longlong_as_double((long long)vbits);
-                        if (nnzA == 0 || l2B == 0.0f) {   // an exact zero
-                            if (g.bnd) g.bnd[(long)r * g.ldb + col] = 0.0f;
-                            continue;
-                        }
+                        vout[j] = vbits;
+                        bout[j] = 0.0f;
+                        if (nnzA == 0 || l2B == 0.0f) continue;   // an exact zero
                         bool exact = __fmul_ru(sA, sB) < 4096.0f;
                         if (exact && __fmul_ru(__fmul_ru(dnAmax, dnBmax), fuse) >= two24) {
                             for (int cc = 0; cc < g.nchunks; ++cc)
@@ -648,12 +669,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const unsigned long long vb = vbits & 0x7FFFFFFFFFFFFFFFull;
                             vmax = vb > vmax ? vb : vmax;
                         }
-                        if (g.bnd) {
+                        {
                             // absolute bound: units 2^{eA+eB}; below float's normal range the
                             // smallest normal scale over-states it (still a bound)
                             const int es = eA + eB;
-                            g.bnd[(long)r * g.ldb + col] =
-                                !exact || es > 127 ? __int_as_float(0x7f800000) : __fmul_ru(bound, pow2f(max(es, -126)));
+                            bout[j] = !exact || es > 127 ? __int_as_float(0x7f800000)
+                                                         : __fmul_ru(bound, pow2f(max(es, -126)));
                         }
                         if (g.rowerr2) {
                             const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
@@ -666,6 +687,19 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const unsigned int idx = atomicAdd(g.nflags, 1u);
                             if ((int)idx < g.max_flags) g.flags[idx] = make_int2(r, col);
                         }
+                    }
+                    // the row's 16 columns are contiguous and 16-byte aligned (the leading
+                    // dimensions are multiples of 128 columns)
+                    double2* o2 = reinterpret_cast<double2*>(orow + tl.n0 + c * 32 + h * 16);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        o2[q] = make_double2(__longlong_as_double((long long)vout[2 * q]),
+                                             __longlong_as_double((long long)vout[2 * q + 1]));
+                    if (brow) {
+                        float4* b4 = reinterpret_cast<float4*>(brow + tl.n0 + c * 32 + h * 16);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            b4[q] = make_float4(bout[4 * q], bout[4 * q + 1], bout[4 * q + 2], bout[4 * q + 3]);
                     }
                 }
             }
@@ -1256,7 +1290,7 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
 }  // namespace
 
 size_t gemm_smem_bytes() {   // the larger of the two stage rings (the pair's three 72 KB stages)
-    return (size_t)STAGES * 3 * (BOX_A + BOX_B / 2) + 1024 /* align slack */ + 256 /* barriers */;
+    return (size_t)COLSTAT_OFF + COLSTAT_BYTES + 1024 /* align slack */;
 }
 
 // Kernel instances by (max slices, max chunks, pair): the two common configurations (first
