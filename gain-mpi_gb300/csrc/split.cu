@@ -16,11 +16,20 @@ constexpr uint32_t BOX_A = BM * BK * 2;     // bytes of one A k-block box (16 KB
 constexpr uint32_t BOX_B = BN * BK * 2;     // bytes of one B k-block box (16 KB)
 constexpr uint32_t STAGE_A = KSTEP * BOX_A; // bytes per A stage
 constexpr uint32_t STAGE_B = KSTEP * BOX_B; // bytes per B stage
-constexpr int NTHREADS = 192;               // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+// Warp 0 issues the TMA copies, warp 1 the MMAs, warps 2.. are the epilogue: EPI_WARPS
+// warps, two per TMEM lane quadrant, each draining and finalising half of the tile's
+// columns (so the finalisation, which holds the next tile's first drain back, is short).
+constexpr int EPI_WARPS = 8;
+constexpr int NTHREADS = 64 + 32 * EPI_WARPS;
+constexpr int EPI_HALVES = EPI_WARPS / 4;     // column parts of a tile
+constexpr int EPI_GROUPS = BN / 32 / EPI_HALVES;   // 32-column groups per epilogue warp
 // shared memory of the GEMM after its stage ring (the larger, the pair's) and the barriers:
 // the current tile's column statistics, five floats per column
 constexpr uint32_t COLSTAT_OFF = STAGES * 3 * (BOX_A + BOX_B / 2) + 256;
 constexpr uint32_t COLSTAT_BYTES = 5 * BN * 4;
+// then (grouped launch) the arguments of the epilogue's current tile
+constexpr uint32_t GARGS_OFF = COLSTAT_OFF + COLSTAT_BYTES;
+constexpr uint32_t GARGS_BYTES = (sizeof(GemmArgs) + 15) / 16 * 16;
 constexpr uint32_t TMEM_COLS = 512;         // acc0 [0,128) acc1 [128,256) hi [256,384) lo [384,512)
 constexpr unsigned long long kWaitNs = 2000000000ull;   // 2 s per wait before giving up
 
@@ -194,6 +203,13 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32
         GAIN_W8(0), GAIN_W8(8), GAIN_W8(16), GAIN_W8(24)
         : "memory");
 }
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr),
+        GAIN_W8(0), GAIN_W8(8)
+        : "memory");
+}
 
 // Shared-memory matrix descriptor of a K-major tile written by TMA with 128-byte swizzle:
 // rows of 128 bytes, 8-row groups 1024 bytes apart (SBO), base 1024-byte aligned.
@@ -255,8 +271,8 @@ __device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, in
     *hi = (int)(((long)(c + 1) * nkb) / nch);
 }
 
-// Barrier of the four epilogue warps (named barrier 1, 128 threads).
-__device__ __forceinline__ void epilogue_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// Barrier of the epilogue warps (named barrier 1).
+__device__ __forceinline__ void epilogue_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory"); }
 
 // The arguments of a tile: the launch's own, or (grouped launch) those of the tile's group.
 template <bool G>
@@ -283,7 +299,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
     constexpr uint32_t STA = KS * BOX_A;
     constexpr uint32_t STB = KS * BOXB;
     static_assert(NST * (STA + STB) + 256 <= COLSTAT_OFF, "stage ring");
-    static_assert(COLSTAT_OFF + COLSTAT_BYTES + 1024 <= 227 * 1024, "shared memory");
+    static_assert(GARGS_OFF + GARGS_BYTES + 1024 <= 227 * 1024, "shared memory");
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
@@ -311,7 +327,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_u32(&accfull[b]), 1);
-            mbar_init(smem_u32(&accempty[b]), PAIR ? 256 : 128);   // both CTAs' epilogues drain
+            mbar_init(smem_u32(&accempty[b]), (PAIR ? 64 : 32) * EPI_WARPS);   // both CTAs' epilogues drain
         }
         mbar_init(smem_u32(drain), 1);
         *abort_flag = 0;
@@ -482,6 +498,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         // weights below 2^{-kFixTotal} are truncated (floor), at most one unit per product.
         const int q = warp & 3;
         const int row_in_tile = q * 32 + lane;
+        const int c0 = ((warp - 2) / 4) * EPI_GROUPS;   // this warp's first 32-column group
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         const float two24 = 16777216.0f;
         uint32_t acc_cnt = 0;
@@ -502,22 +519,31 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 // them as broadcasts).  The barrier keeps the previous tile's finalisation
                 // from reading values of this one.
                 epilogue_sync();
-                const int ncol = tl.n0 + row_in_tile;
-                const int sl = g.slices;
-                const float* dvB = g.B.dnv + (long)ncol * MAX_SLICES;
-                const float* rvB = g.B.rnv + (long)ncol * MAX_SLICES;
-                float crho = 0.0f, csB = 0.0f, cdnmax = 0.0f;
-                for (int k = 0; k < sl; ++k) {
-                    crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * beta)));
-                    csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * beta), __ldg(&dvB[k])));
+                if constexpr (GROUPED) {   // the tile's arguments for the finalisation
+                    static_assert(sizeof(GemmArgs) % 4 == 0, "word copy");
+                    const uint32_t* src = reinterpret_cast<const uint32_t*>(&a.groups[tl.group].args);
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(smem + GARGS_OFF);
+                    for (int w = (warp - 2) * 32 + lane; w < (int)(sizeof(GemmArgs) / 4); w += 32 * EPI_WARPS)
+                        dst[w] = src[w];
                 }
-                for (int cc = 0; cc < nchunks; ++cc)
-                    cdnmax = fmaxf(cdnmax, __ldg(&g.B.dn[(long)ncol * nchunks + cc]));
-                s_col[0 * BN + row_in_tile] = __int_as_float(__ldg(&g.B.e[ncol]));
-                s_col[1 * BN + row_in_tile] = __ldg(&g.B.l2[ncol]);   // 0 exactly for an all-zero column
-                s_col[2 * BN + row_in_tile] = crho;
-                s_col[3 * BN + row_in_tile] = csB;
-                s_col[4 * BN + row_in_tile] = cdnmax;
+                if (c0 == 0) {
+                    const int ncol = tl.n0 + row_in_tile;
+                    const int sl = g.slices;
+                    const float* dvB = g.B.dnv + (long)ncol * MAX_SLICES;
+                    const float* rvB = g.B.rnv + (long)ncol * MAX_SLICES;
+                    float crho = 0.0f, csB = 0.0f, cdnmax = 0.0f;
+                    for (int k = 0; k < sl; ++k) {
+                        crho = fmaxf(crho, __fmul_ru(__ldg(&rvB[k]), pow2f((k + 1) * beta)));
+                        csB = __fadd_ru(csB, __fmul_ru(pow2f(-(k + 1) * beta), __ldg(&dvB[k])));
+                    }
+                    for (int cc = 0; cc < nchunks; ++cc)
+                        cdnmax = fmaxf(cdnmax, __ldg(&g.B.dn[(long)ncol * nchunks + cc]));
+                    s_col[0 * BN + row_in_tile] = __int_as_float(__ldg(&g.B.e[ncol]));
+                    s_col[1 * BN + row_in_tile] = __ldg(&g.B.l2[ncol]);   // 0 exactly for an all-zero column
+                    s_col[2 * BN + row_in_tile] = crho;
+                    s_col[3 * BN + row_in_tile] = csB;
+                    s_col[4 * BN + row_in_tile] = cdnmax;
+                }
             }
             bool first = true;
             for (int p = 0; p < nprods && ok; ++p) {
@@ -533,16 +559,16 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 tc_fence_after();
                 const int sh = fix_bits(beta) - pr.t * beta;
 #pragma unroll 1
-                for (int c = 0; c < BN / 32; ++c) {
-                    uint32_t acc[32], lo_r[32], hi_r[32];
-                    tmem_ld32(tmem + lane_off + b * BN + c * 32, acc);
+                for (int c = 2 * c0; c < 2 * (c0 + EPI_GROUPS); ++c) {   // 16-column pieces
+                    uint32_t acc[16], lo_r[16], hi_r[16];
+                    tmem_ld16(tmem + lane_off + b * BN + c * 16, acc);
                     if (!first) {
-                        tmem_ld32(tmem + lane_off + 256 + c * 32, lo_r);
-                        tmem_ld32(tmem + lane_off + 384 + c * 32, hi_r);
+                        tmem_ld16(tmem + lane_off + 256 + c * 16, lo_r);
+                        tmem_ld16(tmem + lane_off + 384 + c * 16, hi_r);
                     }
                     tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
+                    for (int j = 0; j < 16; ++j) {
                         const long long ai = (long long)__float2int_rz(__uint_as_float(acc[j]));
                         const long long v = sh >= 0 ? (ai << sh) : (ai >> (-sh));
                         long long run = first ? 0ll
@@ -551,8 +577,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         lo_r[j] = (uint32_t)(unsigned long long)run;
                         hi_r[j] = (uint32_t)((unsigned long long)run >> 32);
                     }
-                    tmem_st32(tmem + lane_off + 256 + c * 32, lo_r);
-                    tmem_st32(tmem + lane_off + 384 + c * 32, hi_r);
+                    tmem_st16(tmem + lane_off + 256 + c * 16, lo_r);
+                    tmem_st16(tmem + lane_off + 384 + c * 16, hi_r);
                 }
                 tmem_wait_st();
                 tc_fence_before();
@@ -564,10 +590,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             if (!ok) break;
             // The finalisation reads many of the tile's arguments for every output.  A grouped
             // launch keeps them in global memory, where any store of an output might alias them
-            // and force them to be read again: there they are copied to registers first.
-            GemmArgs gcopy;
-            if constexpr (GROUPED) gcopy = a.groups[tl.group].args;
-            const GemmArgs& g = GROUPED ? gcopy : a;
+            // and force them to be read again: it reads the copy in shared memory.
+            const GemmArgs& g = GROUPED ? *reinterpret_cast<const GemmArgs*>(smem + GARGS_OFF) : a;
             const int s = g.slices;
             // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags.
             // Row terms live in registers; the column statistics come from shared memory.
@@ -608,11 +632,13 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             double* orow = g.out + (long)r * g.ldo;
             float* brow = g.bnd ? g.bnd + (long)r * g.ldb : nullptr;
 #pragma unroll 1
-            for (int c = 0; c < BN / 32; ++c) {
+            for (int c = c0; c < c0 + EPI_GROUPS; ++c) {
 #pragma unroll 1
                 for (int h = 0; h < 2; ++h) {
                     // this thread's 16 outputs leave as eight 16-byte stores (and four for the
                     // bounds) instead of sixteen 8-byte ones
+                    double2* o2 = reinterpret_cast<double2*>(orow + tl.n0 + c * 32 + h * 16);
+                    float4* b4 = brow ? reinterpret_cast<float4*>(brow + tl.n0 + c * 32 + h * 16) : nullptr;
                     unsigned long long vout[16];
                     float bout[16];
                     uint32_t lo_r[16], hi_r[16];
@@ -638,7 +664,16 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                         const unsigned long long vbits = scaled_bits(run, eA + eB - kFixTotal, &av);
                         vout[j] = vbits;
                         bout[j] = 0.0f;
-                        if (nnzA == 0 || l2B == 0.0f) continue;   // an exact zero
+                        // the row's 16 columns are contiguous and 16-byte aligned (the leading
+                        // dimensions are multiples of 128 columns): pairs of values and quads of
+                        // bounds leave as 16-byte stores once complete
+                        if (j & 1)
+                            o2[j >> 1] = make_double2(__longlong_as_double((long long)vout[j - 1]),
+                                                      __longlong_as_double((long long)vbits));
+                        if (nnzA == 0 || l2B == 0.0f) {   // an exact zero
+                            if (b4 && (j & 3) == 3) b4[j >> 2] = make_float4(bout[j - 3], bout[j - 2], bout[j - 1], 0.0f);
+                            continue;
+                        }
                         bool exact = __fmul_ru(sA, sB) < 4096.0f;
                         if (exact && __fmul_ru(__fmul_ru(dnAmax, dnBmax), fuse) >= two24) {
                             for (int cc = 0; cc < g.nchunks; ++cc)
@@ -675,6 +710,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const int es = eA + eB;
                             bout[j] = !exact || es > 127 ? __int_as_float(0x7f800000)
                                                          : __fmul_ru(bound, pow2f(max(es, -126)));
+                            if (b4 && (j & 3) == 3) b4[j >> 2] = make_float4(bout[j - 3], bout[j - 2], bout[j - 1], bout[j]);
                         }
                         if (g.rowerr2) {
                             const float bb = __fmul_ru(bound, pow2f(max(-126, min(127, eB))));
@@ -687,19 +723,6 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                             const unsigned int idx = atomicAdd(g.nflags, 1u);
                             if ((int)idx < g.max_flags) g.flags[idx] = make_int2(r, col);
                         }
-                    }
-                    // the row's 16 columns are contiguous and 16-byte aligned (the leading
-                    // dimensions are multiples of 128 columns)
-                    double2* o2 = reinterpret_cast<double2*>(orow + tl.n0 + c * 32 + h * 16);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        o2[q] = make_double2(__longlong_as_double((long long)vout[2 * q]),
-                                             __longlong_as_double((long long)vout[2 * q + 1]));
-                    if (brow) {
-                        float4* b4 = reinterpret_cast<float4*>(brow + tl.n0 + c * 32 + h * 16);
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            b4[q] = make_float4(bout[4 * q], bout[4 * q + 1], bout[4 * q + 2], bout[4 * q + 3]);
                     }
                 }
             }
@@ -1290,7 +1313,7 @@ __global__ void k_refine_amp(const RefineAmpArgs a) {
 }  // namespace
 
 size_t gemm_smem_bytes() {   // the larger of the two stage rings (the pair's three 72 KB stages)
-    return (size_t)COLSTAT_OFF + COLSTAT_BYTES + 1024 /* align slack */;
+    return (size_t)GARGS_OFF + GARGS_BYTES + 1024 /* align slack */;
 }
 
 // Kernel instances by (max slices, max chunks, pair): the two common configurations (first
