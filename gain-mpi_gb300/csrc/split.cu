@@ -491,7 +491,8 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             }
         }
     } else {
-        // ---------------- epilogue: warps 2..5, one TMEM lane (output row) per thread
+        // ---------------- epilogue: warps 2.., one TMEM lane (output row) per thread, each
+        // warp half of the tile's columns (c0: its first 32-column group)
         // Each digit product arrives as an FP32 accumulator holding an exact integer (|acc| <
         // 2^24 where certified).  It is added, shifted to its weight, into an int64 fixed-point
         // running sum (TMEM columns 256..383 low words, 384..511 high words); only the
