@@ -3166,6 +3166,7 @@ struct PlanJob {
     DevArray<split::Prod> prods1, prods2;
     int nprods1 = 0, nprods2 = 0, fuse1 = 1;
     int uowner = -1;              // a job whose upper digits this one reads (same block, levels, layout)
+    int lowner = -1;              // a job whose lower digits this one reads (same block, levels, layout)
     CUtensorMap tmV{}, tmH{}, tmU{};
     const void* vI = nullptr;     // eigenvector and band-digit buffers the graph captured
     const void* vF = nullptr;
@@ -3303,13 +3304,34 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
             break;
         }
     }
-    const size_t vdig = (size_t)J.p1.slices * J.Bpad * L.kpadI;
+    // and likewise jobs with the same lower block, lower levels, lower layout and first-GEMM
+    // digits share one set of lower digits (mixing expansions excluded: theirs come from
+    // each job's own expansion)
+    J.lowner = -1;
+    if (!L.general)
+        for (auto& Q : P->jobs) {
+            if (Q.get() == &J) break;
+            const PairLayout& QL = *Q->L;
+            if (Q->job.jindI == j->jindI && Q->job.gammaI == j->gammaI && Q->lower == J.lower && Q->Bpad == J.Bpad &&
+                Q->p1.beta == J.p1.beta && Q->p1.slices == J.p1.slices && Q->p1.chunks == J.p1.chunks &&
+                !QL.general && QL.kpadI == L.kpadI && QL.colposI == L.colposI && QL.i_sym == L.i_sym &&
+                Q->lowner < 0) {
+                J.lowner = (int)(&Q - &P->jobs[0]);
+                break;
+            }
+        }
+    const size_t vdig = J.lowner < 0 ? (size_t)J.p1.slices * J.Bpad * L.kpadI : 0;
     const size_t hdig = (size_t)J.p2.slices * J.Bpad * J.K2;
     const size_t udig = J.uowner < 0 ? (size_t)J.p2.slices * J.Nupad * J.K2 : 0;
-    GAIN_TRY(J.Vdig.alloc(vdig));
-    GAIN_TRY(J.Vdig.zero(st, vdig));
-    GAIN_TRY(J.Vst.alloc(J.Bpad, J.p1.chunks, false));
-    GAIN_TRY(J.Vst.zero(st, J.Bpad, J.p1.chunks, false));
+    if (J.lowner < 0) {
+        GAIN_TRY(J.Vdig.alloc(vdig));
+        GAIN_TRY(J.Vdig.zero(st, vdig));
+        GAIN_TRY(J.Vst.alloc(J.Bpad, J.p1.chunks, false));
+        GAIN_TRY(J.Vst.zero(st, J.Bpad, J.p1.chunks, false));
+    } else {   // not this job's: release what an earlier preparation left
+        J.Vdig.release();
+        J.Vst = StatsDev();
+    }
     GAIN_TRY(J.Hdig.alloc(hdig));
     GAIN_TRY(J.Hdig.zero(st, hdig));
     GAIN_TRY(J.Hst.alloc(J.Bpad, J.p2.chunks, true));
@@ -3344,7 +3366,7 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     GAIN_TRY(J.prods2.upload(pr2));
     J.nprods1 = (int)pr1.size();
     J.nprods2 = (int)pr2.size();
-    if (!split::make_digit_map(&J.tmV, J.Vdig.p, L.kpadI, J.Bpad, J.p1.slices) ||
+    if ((J.lowner < 0 && !split::make_digit_map(&J.tmV, J.Vdig.p, L.kpadI, J.Bpad, J.p1.slices)) ||
         !split::make_digit_map(&J.tmH, J.Hdig.p, J.K2, J.Bpad, J.p2.slices) ||
         (J.uowner < 0 &&
          !split::make_digit_map(&J.tmU, J.Udig.p, J.K2, J.Nupad, J.p2.slices, P->pair ? split::BN / 2 : split::BM)))
@@ -3414,8 +3436,8 @@ gain_status plan_slice_batches(const std::vector<split::SliceArgs>& all, std::ve
     return GAIN_OK;
 }
 
-// Every job's slicings: its lower vectors and (for the owner of an upper block's digits) its
-// upper vectors before the first GEMM, its H before the second.  Each produces exactly what
+// Every job's slicings: its lower and upper vectors before the first GEMM (only the owner of
+// a shared set of lower or upper digits slices it), its H before the second.  Each produces exactly what
 // the single-pair run's slicing of the same rows does.
 gain_status plan_build_slices(gain_plan P) {
     gain_engine e = P->e;
@@ -3434,16 +3456,19 @@ gain_status plan_build_slices(gain_plan P) {
                 s1.push_back(slice_args(EF.d.p, EF.nsize, J.d_upper.p, J.Nu, L.nsymF, nullptr, nullptr, J.K2, J.Nupad,
                                         J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr));
         } else {
-            s1.push_back(slice_args(EI.d.p, EI.nsize, J.d_lower.p, J.B, EI.nsize, L.d_colposI.p, &L.colposI, L.kpadI,
-                                    J.Bpad, J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr, L.d_i_sym.p));
+            if (J.lowner < 0)
+                s1.push_back(slice_args(EI.d.p, EI.nsize, J.d_lower.p, J.B, EI.nsize, L.d_colposI.p, &L.colposI,
+                                        L.kpadI, J.Bpad, J.Vdig.p, J.p1, J.Vst, false, nullptr, nullptr,
+                                        L.d_i_sym.p));
             if (J.uowner < 0)
                 s1.push_back(slice_args(EF.d.p, EF.nsize, J.d_upper.p, J.Nu, EF.nsize, L.d_colposF.p, &L.colposF,
                                         L.fpad, J.Nupad, J.Udig.p, J.p2, J.Ust, false, nullptr, nullptr,
                                         L.d_f_sym.p));
         }
+        const PlanJob& JL = J.lowner < 0 ? J : *P->jobs[J.lowner];   // the lower digits' owner
         s3.push_back(slice_args(L.general ? J.Hsym.p : J.H.p, J.K2, nullptr, J.B, L.general ? L.nsymF : L.fpad,
                                 nullptr, nullptr, J.K2, J.Bpad, J.Hdig.p, J.p2, J.Hst, true, J.rowerr.p,
-                                J.Vst.e.p));
+                                JL.Vst.e.p));
     }
     GAIN_TRY(plan_slice_batches(s1, P->slices1));
     GAIN_TRY(plan_slice_batches(s3, P->slices3));
@@ -3482,7 +3507,8 @@ gain_status plan_build_groups(gain_plan P) {
         PairLayout& L = *J.L;
         memset(&g1[q], 0, sizeof g1[q]);
         memset(&g2[q], 0, sizeof g2[q]);
-        g1[q].tmA = J.tmV;
+        PlanJob& JL = J.lowner < 0 ? J : *P->jobs[J.lowner];   // the lower digits' owner
+        g1[q].tmA = JL.tmV;
         g1[q].tmB = P->pair ? L.tmBandPair : L.tmBand;
         split::GemmArgs& a1 = g1[q].args;
         a1.prods = J.prods1.p;
@@ -3492,7 +3518,7 @@ gain_status plan_build_groups(gain_plan P) {
         a1.slices = J.p1.slices;
         a1.out = J.H.p;
         a1.ldo = L.fpad;
-        a1.A = J.Vst.view(false);
+        a1.A = JL.Vst.view(false);
         a1.B = L.bandStats.view(false);
         a1.c_fix = fix_const(J.nprods1);
         a1.c_f64 = (float)((double)(L.W + 64) * std::ldexp(1.0, -53) * 1.01);
@@ -3672,7 +3698,7 @@ gain_status plan_enqueue(gain_plan P) {
         rh.W = L.W;
         rh.H = J.H.p;
         rh.ldh = L.fpad;
-        rh.eA = J.Vst.e.p;
+        rh.eA = (J.lowner < 0 ? J : *P->jobs[J.lowner]).Vst.e.p;
         rh.rowerr2 = J.rowerr.p;
         GAIN_CUDA(split::launch_refine_h(rh, std::min(2 * e->num_sms, std::max(1, J.cap1 / 8)), sq));
         if (L.general) {
