@@ -693,6 +693,43 @@ void row_grouped(std::vector<split::Tile>& t, int mstep) {
     row_grouped(t, mstep, [](const split::Tile&) { return 0; });
 }
 
+// Spread of tiles over `units` persistent CTAs (CTA pairs) in list order: each tile goes to
+// the unit that frees up first, the order a dynamic scheduler would give, so that the tiles
+// running at any moment are neighbours in the list and share their operands' digits in L2 as
+// in a single run (a longest-first spread scatters every unit's k-th tile over the whole
+// list, and the digits of each then come from DRAM).  The jobs (tile groups) with the
+// costliest tiles go first, so that cheap tiles even out the end.  The list is laid out so
+// that unit u runs entries u, u + units, ... (empty slots: group -1).
+std::vector<split::Tile> list_schedule(const std::vector<split::Tile>& tiles, const std::vector<double>& cost,
+                                       int units) {
+    std::map<int, double> job_cost;
+    for (size_t i = 0; i < tiles.size(); ++i) job_cost[tiles[i].group] = std::max(job_cost[tiles[i].group], cost[i]);
+    std::vector<int> order(tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return job_cost[tiles[a].group] > job_cost[tiles[b].group]; });
+    std::vector<std::vector<int>> per(units);
+    typedef std::pair<double, int> LU;
+    std::priority_queue<LU, std::vector<LU>, std::greater<LU>> heap;
+    for (int u = 0; u < units; ++u) heap.push({0.0, u});
+    for (int t : order) {
+        LU top = heap.top();
+        heap.pop();
+        per[top.second].push_back(t);
+        top.first += cost[t];
+        heap.push(top);
+    }
+    size_t depth = 0;
+    for (auto& v : per) depth = std::max(depth, v.size());
+    split::Tile empty;
+    memset(&empty, 0, sizeof empty);
+    empty.group = -1;
+    std::vector<split::Tile> out(depth * units, empty);
+    for (int u = 0; u < units; ++u)
+        for (size_t k = 0; k < per[u].size(); ++k) out[k * units + u] = tiles[per[u][k]];
+    return out;
+}
+
 // Products fused per accumulator in the first GEMM: only where each product is short (fewer
 // than 16 k-blocks per tile, so that draining the accumulator after every product would pace
 // the tensor pipe); as many as keep the expected sum of their digit norms' products, K_chunk
@@ -1294,6 +1331,14 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
                 }
             }
         row_grouped(t1, mstep);
+        {   // band tiles of the edge K blocks are shorter: dealt in list order to the unit that
+            // frees up first, no unit runs a tile more than the rest (a static round robin of
+            // the list left the last units up to two thirds of a tile behind)
+            const double per_kb = (double)pr1.size() / p1x.chunks;
+            std::vector<double> c1(t1.size());
+            for (size_t i = 0; i < t1.size(); ++i) c1[i] = t1[i].nkb * per_kb + 2.0 * (double)pr1.size();
+            t1 = list_schedule(t1, c1, pair ? e->num_sms / 2 : e->num_sms);
+        }
         GAIN_TRY(e->tiles1.upload(t1));
         split::GemmArgs g1;
         memset(&g1, 0, sizeof g1);
@@ -3377,43 +3422,6 @@ gain_status plan_prepare_job(gain_plan P, PlanJob& J) {
     J.nlevF = EF.nlevels;
     J.band = L.bandDig.p;
     return GAIN_OK;
-}
-
-// Spread of tiles over `units` persistent CTAs (CTA pairs) in list order: each tile goes to
-// the unit that frees up first, the order a dynamic scheduler would give, so that the tiles
-// running at any moment are neighbours in the list and share their operands' digits in L2 as
-// in a single run (a longest-first spread scatters every unit's k-th tile over the whole
-// list, and the digits of each then come from DRAM).  The jobs with the costliest tiles go
-// first, so that cheap tiles even out the end.  The list is laid out so that unit u runs
-// entries u, u + units, ... (empty slots: group -1).
-std::vector<split::Tile> list_schedule(const std::vector<split::Tile>& tiles, const std::vector<double>& cost,
-                                       int units) {
-    std::map<int, double> job_cost;
-    for (size_t i = 0; i < tiles.size(); ++i) job_cost[tiles[i].group] = std::max(job_cost[tiles[i].group], cost[i]);
-    std::vector<int> order(tiles.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return job_cost[tiles[a].group] > job_cost[tiles[b].group]; });
-    std::vector<std::vector<int>> per(units);
-    typedef std::pair<double, int> LU;
-    std::priority_queue<LU, std::vector<LU>, std::greater<LU>> heap;
-    for (int u = 0; u < units; ++u) heap.push({0.0, u});
-    for (int t : order) {
-        LU top = heap.top();
-        heap.pop();
-        per[top.second].push_back(t);
-        top.first += cost[t];
-        heap.push(top);
-    }
-    size_t depth = 0;
-    for (auto& v : per) depth = std::max(depth, v.size());
-    split::Tile empty;
-    memset(&empty, 0, sizeof empty);
-    empty.group = -1;
-    std::vector<split::Tile> out(depth * units, empty);
-    for (int u = 0; u < units; ++u)
-        for (size_t k = 0; k < per[u].size(); ++k) out[k * units + u] = tiles[per[u][k]];
-    return out;
 }
 
 // The slicings `all` grouped by kernel into batches of one launch each (device memory).

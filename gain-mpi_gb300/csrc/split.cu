@@ -359,7 +359,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             bool ok = true;
             for (int t = unit; t < a.ntiles && ok; t += nunits) {
                 const Tile tl = a.tiles[t];
-                if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
+                if (tl.group < 0) continue;   // an empty slot of the schedule
                 const GemmArgs& g = group_args<GROUPED>(a, tl);
                 const CUtensorMap* mapA = GROUPED ? &a.groups[tl.group].tmA : &tmA;
                 const CUtensorMap* mapB = GROUPED ? &a.groups[tl.group].tmB : &tmB;
@@ -428,7 +428,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             bool ok = true, any = false;
             for (int t = unit; t < a.ntiles && ok; t += nunits) {
                 const Tile tl = a.tiles[t];
-                if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
+                if (tl.group < 0) continue;   // an empty slot of the schedule
                 const GemmArgs& g = group_args<GROUPED>(a, tl);
                 const Prod* prods = g.prods;
                 const int nprods = g.nprods, nchunks = g.nchunks;
@@ -506,7 +506,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         bool ok = true;
         for (int t = unit; t < a.ntiles && ok; t += nunits) {
             const Tile tl = a.tiles[t];
-            if (GROUPED && tl.group < 0) continue;   // an empty slot of the schedule
+            if (tl.group < 0) continue;   // an empty slot of the schedule
             const Prod* prods;
             int nprods, nchunks, beta;
             {

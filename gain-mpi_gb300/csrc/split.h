@@ -31,7 +31,7 @@ struct Tile {
     int a_k0;       // A inner coordinate of k-block 0
     int b_k0;       // B inner coordinate of k-block 0
     int nkb;        // k-blocks of BK
-    int group;      // grouped launch: the tile's group (-1: an empty slot of the schedule)
+    int group;      // grouped launch: the tile's group; -1 in any launch: an empty slot of the schedule
     int pad[2];
 };
 
