@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--batch-engines", type=int, default=4,
                     help="engines (streams, host threads) of the --batch plan run through gain_run_plan")
     ap.add_argument("--degenerate", action="store_true",
-                    help="a doubly degenerate E -> E pair of the config-2 sizes (rule c3e), every component pair")
+                    help="a doubly degenerate E -> E pair at N_v = 2000, J''=10 -> J'=11 (rule c3e), every component pair")
     ap.add_argument("--batch-jmax", type=int, default=30, help="largest J of --batch")
     ap.add_argument("--batch-stream", action="store_true",
                     help="many block pairs at the full size (N_v from --batch-nv, default 2000 here), in waves")
@@ -644,8 +644,8 @@ def adjoint_check(args):
 
 
 def degenerate_pair(args):
-    """Degenerate symmetries at the config-2 sizes: rule c3e (A1, A2, doubly degenerate E),
-    N_v = 2000, J'' = 10 E (the 2000 lowest states) -> J' = 11 E (every state).  A step is
+    """Degenerate symmetries at the sizes of the N_v = 2000 pair: rule c3e (A1, A2, doubly
+    degenerate E), N_v = 2000, J'' = 10 E (the 2000 lowest states) -> J' = 11 E (every state).  A step is
     gain_run_pair_degenerate over the four component pairs (generic symmetry type: all pass)
     through the split path; the lines combine the four slots (S = sum amp^2 / 2).  S is checked
     against the plain FP64 path's four components on the same lines.  One JSON line."""

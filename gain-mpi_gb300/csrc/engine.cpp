@@ -1149,7 +1149,7 @@ gain_status run_split(gain_engine e, const gain_pair_job* j, int dI, int dF, con
     // vectors are awaited on the second stream only, so their copy overlaps the lower side
     if (EI.ready) GAIN_CUDA(cudaStreamWaitEvent(st, EI.ready, 0));
 
-    // First GEMM: about 49 bits at config-2 band widths (its error reaches every amplitude
+    // First GEMM: about 49 bits at band widths near 3000 (its error reaches every amplitude
     // through ||dH||_2 ||u||_2; every entry must certify FP64-grade), see gemm1_params.
     // Second GEMM: 48 bits (8-bit digits in up to MAX_CHUNKS chunks, else 7 x 7 bits);
     // options (beta, slices, kchunks) apply to it.
