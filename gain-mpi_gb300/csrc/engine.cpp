@@ -4051,6 +4051,10 @@ gain_status gain_plan_run(gain_plan P, gain_stats* job_stats, gain_plan_stats* s
         stats->digits_ms = d1;
         stats->middle_ms = d3;
         stats->refine_ms = d5;
+        for (auto& J : P->jobs) {
+            stats->shared_lower += J->lowner >= 0;
+            stats->shared_upper += J->uowner >= 0;
+        }
         stats->jobs = nj;
         for (int q = 0; q < nj && q < (int)P->job_stats.size(); ++q) {
             stats->transitions += P->job_stats[q].rows * P->job_stats[q].cols;

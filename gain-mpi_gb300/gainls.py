@@ -72,7 +72,8 @@ class PlanStats(ctypes.Structure):
                 ("gemm2_tiles", ctypes.c_int), ("units", ctypes.c_int), ("pair", ctypes.c_int),
                 ("captures", ctypes.c_int), ("tuned", ctypes.c_int), ("tune_ms", ctypes.c_double),
                 ("tensor_flops", ctypes.c_double), ("beta2", ctypes.c_int * 4), ("slices2", ctypes.c_int * 4),
-                ("digits_ms", ctypes.c_double), ("middle_ms", ctypes.c_double), ("refine_ms", ctypes.c_double)]
+                ("digits_ms", ctypes.c_double), ("middle_ms", ctypes.c_double), ("refine_ms", ctypes.c_double),
+                ("shared_lower", ctypes.c_int), ("shared_upper", ctypes.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -343,6 +343,9 @@ typedef struct gain_plan_stats {
     double digits_ms;            /* before the first GEMM: expansions and eigenvector digits */
     double middle_ms;            /* between the GEMMs: refinement of H, contraction, H digits */
     double refine_ms;            /* after the second GEMM: refinement of the amplitudes */
+    int shared_lower;            /* jobs reading another job's lower digits (same lower block,
+                                    levels, layout and first-GEMM digits) */
+    int shared_upper;            /* jobs reading another job's upper digits */
 } gain_plan_stats;
 
 gain_status gain_plan_create(gain_engine e, const gain_pair_job* jobs, int n_jobs, const gain_split_opts* opts,

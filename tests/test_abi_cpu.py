@@ -120,3 +120,36 @@ def test_manager_header_compiles_and_links(built_lib, tmp_path):
                     "-o", str(out), "-L", lib, "-lgainls", "-L", cuda + "/lib64", "-lcudart",
                     "-Wl,-rpath," + lib], check=True)
     assert out.exists()
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror of a C ABI struct has the header struct's size and, member by member
+    (same names), its offsets: a C program built from include/*.h prints them."""
+    import shutil
+    import subprocess
+    import gainls
+    from conftest import ROOT
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [(gainls.PairJob, "gain_pair_job"), (gainls.SplitOpts, "gain_split_opts"), (gainls.Stats, "gain_stats"),
+             (gainls.PlanStats, "gain_plan_stats"), (gainls.LineParams, "gain_line_params"),
+             (gainls.State, "gain_state"), (gainls.Filters, "gain_filters"), (gainls.TroveState, "gain_trove_state")]
+    lines = ['#include <stdio.h>', '#include "gain_trove.h"', "int main(void) {"]
+    for cls, cname in pairs:
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'    printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layouts.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layouts"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, what, val = line.split()
+        got[(cname, what)] = int(val)
+    for cls, cname in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)

@@ -4,7 +4,7 @@ grouped launch of the second GEMM, per-job refinement -- captured in a CUDA grap
 
 The digit arithmetic is exact and the recombination order-independent, so with the same digit
 configuration every job's amplitudes equal the single-pair run's bit for bit, whatever the
-tile shape or the schedule.  Replays reuse the graph; new eigenvectors of the same sizes are
+tile shape, the schedule or which job's digits of a shared lower or upper block it reads.  Replays reuse the graph; new eigenvectors of the same sizes are
 picked up without a new capture; the autotuner's choice keeps S within 1e-8 of the plain FP64
 path; lines and text read through gain_plan_select equal the single-pair run's."""
 import numpy as np
@@ -46,6 +46,11 @@ def test_plan_equals_single_pair_runs(built_lib, rule):
     ps, js, st = plan.run()
     assert st == gainls.OK and ps["failed_jobs"] == 0
     assert ps["jobs"] == len(jobs) and ps["captures"] == 1
+    # jobs of one upper block read its first job's upper digits, and (without mixing
+    # expansions) jobs of one lower block its first job's lower digits
+    assert ps["shared_upper"] > 0
+    if rule != "c4m":
+        assert ps["shared_lower"] > 0
     assert ps["transitions"] == sum(len(j[4]) * len(j[5]) for j in jobs)
     for q in range(len(jobs)):
         np.testing.assert_array_equal(plan.amp(q), want[q])
