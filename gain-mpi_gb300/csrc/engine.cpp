@@ -611,13 +611,18 @@ struct SplitParams {
 };
 
 // Digits and chunking from the inner length K of the exact accumulations: the Cauchy-Schwarz
-// certificate needs ||d_i|| ||d_j|| < 2^24 over every chunk; balanced residual digits have
-// ||d||^2 ~ K 4^beta / 12, so K_chunk 4^beta / 12 <= 2^23 leaves a factor-two margin.
+// certificate needs ||d_i|| ||d_j|| < 2^24 over every chunk.  Balanced residual digits have
+// ||d||^2 ~ K_chunk 4^beta / 12, and over a chunk of a few thousand digits the norms of
+// eigenvector-like rows stay within a few percent of it, so K_chunk 4^beta / 12 <=
+// 2^24 / kChunkMargin.  An output whose digit norms exceed the budget anyway fails its
+// certificate and is recomputed in FP64.  (A factor-two margin took 8 chunks at K = 12 288
+// and 8-bit digits, this one 5: 168 -> 105 accumulator drains per output tile.)
 // Without an explicit digit width the widest one (from beta_default down) whose chunks fit
 // MAX_CHUNKS is taken: wider digits mean fewer digit products for the same bits.
+constexpr double kChunkMargin = 1.25;
 SplitParams choose_params(int K, const gain_split_opts* o, int bits, int beta_default) {
     auto chunks_for = [K](int beta) {
-        const double limit = 8388608.0 * 12.0 / std::ldexp(1.0, 2 * beta);
+        const double limit = 16777216.0 / kChunkMargin * 12.0 / std::ldexp(1.0, 2 * beta);
         return std::max(1, (int)std::ceil((double)K / limit));
     };
     SplitParams p;
@@ -733,7 +738,8 @@ std::vector<split::Tile> list_schedule(const std::vector<split::Tile>& tiles, co
 // Products fused per accumulator in the first GEMM: only where each product is short (fewer
 // than 16 k-blocks per tile, so that draining the accumulator after every product would pace
 // the tensor pipe); as many as keep the expected sum of their digit norms' products, K_chunk
-// 4^beta / 12 each for balanced digits, within 2^23 (the factor-two margin of choose_params).
+// 4^beta / 12 each for balanced digits, within 2^23 (a factor-two margin: the first GEMM's
+// band rows are short and sparse, so their norms vary more than an eigenvector row's).
 // The exactness certificate checks it per output.  GAINLS_FUSE1=0 disables.
 int gemm1_fuse(const PairLayout& L, const SplitParams& p1) {
     if (const char* f = getenv("GAINLS_FUSE1"))
