@@ -271,8 +271,24 @@ __device__ __forceinline__ void chunk_range(int nkb, int nch, int c, int* lo, in
     *hi = (int)(((long)(c + 1) * nkb) / nch);
 }
 
-// Barrier of the epilogue warps (named barrier 1).
+// Barriers of the epilogue warps (named barrier 1); the second form also takes their vote:
+// true when any of them passes `fail`.  Every epilogue warp reaches each of these barriers
+// (its waits are bounded), and all of them leave the tile loop together at a vote when one
+// gave up on a drain, so no warp is left waiting at a barrier the others will not reach.
+// Both order the shared-memory writes before them with the reads after them.
 __device__ __forceinline__ void epilogue_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory"); }
+__device__ __forceinline__ bool epilogue_sync_any(bool fail) {
+    uint32_t any;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(any)
+        : "r"((uint32_t)fail), "n"(32 * EPI_WARPS)
+        : "memory");
+    return any != 0;
+}
 
 // The arguments of a tile: the launch's own, or (grouped launch) those of the tile's group.
 template <bool G>
@@ -507,6 +523,10 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
         for (int t = unit; t < a.ntiles && ok; t += nunits) {
             const Tile tl = a.tiles[t];
             if (tl.group < 0) continue;   // an empty slot of the schedule
+            // the previous tile's finalisation has read its shared-memory statistics (every
+            // epilogue warp gets here: none has left since the vote before that finalisation,
+            // which has no waits)
+            epilogue_sync();
             const Prod* prods;
             int nprods, nchunks, beta;
             {
@@ -517,9 +537,7 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 beta = g.beta;
                 // The tile's column statistics, one column per epilogue thread, into shared
                 // memory (computed while the tile's first products run; the finalisation reads
-                // them as broadcasts).  The barrier keeps the previous tile's finalisation
-                // from reading values of this one.
-                epilogue_sync();
+                // them as broadcasts).
                 if constexpr (GROUPED) {   // the tile's arguments for the finalisation
                     static_assert(sizeof(GemmArgs) % 4 == 0, "word copy");
                     const uint32_t* src = reinterpret_cast<const uint32_t*>(&a.groups[tl.group].args);
@@ -588,7 +606,12 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
                 ++acc_cnt;
                 first = false;
             }
-            if (!ok) break;
+            // every column's statistics are in place; all epilogue warps leave together if any
+            // of them gave up on a drain
+            if (epilogue_sync_any(!ok)) {
+                ok = false;
+                break;
+            }
             // The finalisation reads many of the tile's arguments for every output.  A grouped
             // launch keeps them in global memory, where any store of an output might alias them
             // and force them to be read again: it reads the copy in shared memory.
@@ -596,7 +619,6 @@ k_digit_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CU
             const int s = g.slices;
             // ---- finalize the tile: value, certified bound (Cauchy-Schwarz), flags.
             // Row terms live in registers; the column statistics come from shared memory.
-            epilogue_sync();   // every column's statistics are in place
             const int r = tl.m0 + (int)rank * BM + row_in_tile;
             const bool rvalid = r < g.rows_valid;
             // products summed in one accumulator: every partial sum of up to `fuse` exact
