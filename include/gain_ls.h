@@ -297,16 +297,18 @@ gain_status gain_run_plan(gain_engine* engines, int n_engines, const gain_pair_j
  * main.cpp:238-342's loop over (J'', Gamma'') -> (J', Gamma') pairs and their lower states;
  * no counterpart in the reference, which launches per lower state and per transition,
  * BaseClasses/GpuManager.cpp:645-746).  The split path of every job runs as
- *   per-job digit slicing of the lower and upper eigenvectors   (concurrent streams)
+ *   the digits of all jobs' lower and upper eigenvectors        (one launch per slicing
+ *                                                                kernel; jobs of one block
+ *                                                                share its digits)
  *   ONE persistent grouped tensor-core launch of the first GEMM over the tiles of all jobs
- *   per-job FP64 refinement and slicing of H                    (concurrent streams)
+ *   per-job FP64 refinement of H (concurrent streams), then the digits of all jobs' H
  *   ONE persistent grouped tensor-core launch of the second GEMM over all jobs' tiles
- *   per-job FP64 refinement of the amplitudes
+ *   per-job FP64 refinement of the amplitudes                   (concurrent streams)
  * captured once into a CUDA graph and replayed by gain_plan_run.  The tiles of each grouped
- * launch are spread over the persistent CTAs longest-first (cost = k-blocks x digit
- * products), so block pairs of very uneven sizes share one launch.  Each job keeps its own
- * device buffers; the engine's uploads (bases, expansion tables, dipole, eigenvectors) must
- * hold every job's inputs.  Jobs are non-degenerate (components 0, 0) with a single dipole
+ * launch are dealt to the persistent CTAs in list order, each to the first free one, with
+ * the jobs with the costliest tiles (k-blocks x digit products) first, so block pairs of
+ * very uneven sizes share one launch.  Each job keeps its own device buffers; the engine's
+ * uploads (bases, expansion tables, dipole, eigenvectors) must hold every job's inputs.  Jobs are non-degenerate (components 0, 0) with a single dipole
  * piece.  After gain_plan_run, gain_plan_select makes one job's amplitudes the engine's last
  * run (for gain_fetch_amp, gain_pair_lines*, gain_pair_lines_text*, ...).
  *
